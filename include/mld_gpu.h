@@ -1,0 +1,147 @@
+/*
+ * mld_gpu.h -- C ABI of the GB300 bispectrum-SO(4) descriptor-to-fit path.
+ *
+ * Plain C types and pointers only; one opaque handle per fitting job.  Every entry point
+ * returns an int status (MLD_OK = 0) and never aborts the host process; the text of the last
+ * failure is available from mld_gpu_last_error().  All arrays are caller-owned host memory
+ * unless the name ends in _device (device pointers, e.g. from cudaMalloc).
+ *
+ * Layouts follow the reference's Fortran column-major arrays, so a Fortran caller passes its
+ * arrays through ISO_C_BINDING (c_loc) without copies:
+ *   pos_cart(3, nat)   -> pos[3*i + c]
+ *   cell(3, 3)         -> cell[3*i + c] = component c of lattice vector a_i  (columns = vectors)
+ *   force(3, nat)      -> force[3*i + c]
+ *   stress(6)          -> xx, yy, zz, yz, xz, xy
+ *   energy(dim, nat)   -> B[dim*i + k]   (descriptor k of atom i; channel-major within dim)
+ *   Amat(D, M)         -> A[D*r + c]     (design row r, column c)
+ * Types are 0-based indices into the element list of the configuration.
+ *
+ * Reference interfaces replaced (paths inside the MILADY project):
+ *   &input_ml namelist subset      src/mld/read_ml_file.F90:174-252 (defaults :307-611)
+ *   compute_descriptors, case 9    src/mld/descriptors.F90:87-382, :658-671;
+ *                                  src/mld/compute/compute_bispectrum_so4.F90:43
+ *   calc_neighbours                src/mld/neighbours.F90:852 (small :1147, large :1091)
+ *   train_fill_Amat_with_energy    src/mld/mld_energy.F90:364
+ *   train_fill_Amat_with_force     src/mld/mld_forces.F90:649
+ *   train_fill_Amat_with_stress    src/mld/mld_stress.F90:181
+ *   train_snap_get_parameters      src/mld/parameters.F90:354 (linear :1018)
+ *   gram%accumulate / reduce_and_solve  src/mld/module_online_fit.F90:138-265, :432-598
+ *   md_mld_compute_energy/force/stress  src/mld/mld.F90:1579, :1673, :1777
+ */
+#ifndef MLD_GPU_H
+#define MLD_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MLD_OK 0
+#define MLD_ERR_INVALID 1        /* bad argument or configuration */
+#define MLD_ERR_CUDA 2           /* CUDA runtime error (message in mld_gpu_last_error) */
+#define MLD_ERR_NEIGHBOUR_CAP 3  /* an atom has more than imm_neigh neighbours within r_cut */
+#define MLD_ERR_OOM 4            /* device allocation failed */
+#define MLD_ERR_SOLVE 5          /* the normal matrix could not be solved */
+#define MLD_ERR_STATE 6          /* call order: e.g. fit before structures were staged */
+#define MLD_ERR_UNSUPPORTED 7    /* option outside this build (e.g. descriptor_type != 9) */
+
+#define MLD_PRECISION_PLAIN_FP64 0  /* all-FP64 on the GPU */
+#define MLD_PRECISION_MIXED 1       /* FP32 descriptors/rows, FP64 Gram accumulation and solve */
+
+#define MLD_MAX_ELEMENTS 8
+
+/* The &input_ml subset read by the descriptor-to-fit path (read_ml_file.F90:174-252). */
+typedef struct mld_gpu_config {
+  int descriptor_type;      /* must be 9 (bispectrum SO(4)) */
+  double j_max;             /* j_max (half-integers allowed); default 1.5 */
+  double r_cut;             /* r_cut [Angstrom]; default 5.0 */
+  double inv_r0_input;      /* default 1 - 0.02/pi; must lie in (0,1) */
+  int weighted;             /* weighted: second channel with per-element weights */
+  int weighted_3ch;         /* weighted_3ch: third channel */
+  int n_elements;           /* fix_no_of_elements (types are 0..n_elements-1) */
+  double weight_per_element[MLD_MAX_ELEMENTS];      /* channel-2 weights (after any weighted_auto renorm) */
+  double weight_per_element_3ch[MLD_MAX_ELEMENTS];  /* channel-3 weights */
+  double r_cut_pair_in[MLD_MAX_ELEMENTS * MLD_MAX_ELEMENTS];  /* inner cutoff per element pair, 0 = off */
+  double r_cut_width_in;    /* default 0.4 */
+  int desc_forces;          /* 1: force and stress design rows */
+  int ml_type;              /* 0 (linear / quadratic models) */
+  int mld_order;            /* 1 linear (this build) */
+  double lambda_krr;        /* ridge added to the diagonal of the normal matrix; < 0 -> 0; default -1 */
+  double svd_rcond;         /* singular-value cut of the min-norm solve; < 0 -> machine precision; default -1 */
+  double sign_stress;       /* default 1 */
+  double sign_stress_big_box; /* default 1 */
+  int imm_neigh;            /* neighbour cap per atom; default 300 */
+  int precision;            /* MLD_PRECISION_PLAIN_FP64 or MLD_PRECISION_MIXED */
+} mld_gpu_config;
+
+typedef struct mld_gpu_handle mld_gpu_handle;
+
+/* Fill *cfg with the reference's namelist defaults (read_ml_file.F90:307-611). */
+void mld_gpu_config_defaults(mld_gpu_config* cfg);
+
+/* Create a handle on the current CUDA device (init_descriptors, descriptors.F90:658-671). */
+int mld_gpu_create(const mld_gpu_config* cfg, mld_gpu_handle** out);
+void mld_gpu_destroy(mld_gpu_handle* h);
+const char* mld_gpu_last_error(const mld_gpu_handle* h);
+
+/* Dimensions: K = bispectrum components per channel (bisso4_dim), dim_desc = channels*K
+ * (dim_xdesc), dim_design_line = width of one design row (1 + dim_desc for the linear model). */
+int mld_gpu_dims(const mld_gpu_handle* h, int* K, int* dim_desc, int* dim_design_line);
+
+/* Stage a batch of structures (the per-configuration loop of mld.F90:376-404).
+ * nat[S]; pos[3*sum(nat)]; cell[9*S]; types[sum(nat)].  Copies to the device. */
+int mld_gpu_set_structures(mld_gpu_handle* h, int nstruct, const int* nat, const double* pos, const double* cell,
+                           const int* types);
+
+/* Labels and per-structure weights of the design rows
+ * (train_fill_Amat_with_energy/force/stress):
+ *   energy[S]   = energy(iread_energy) (already minus the per-element reference energies),
+ *   force[3*sum(nat)], stress[6*S],
+ *   has_efs[3*S] = has_energy, has_force, has_stress flags (0/1),
+ *   w_efs[3*S]   = w_e_model, w_f_model, w_s_model.
+ * Any pointer may be NULL when no structure uses that block. */
+int mld_gpu_set_labels(mld_gpu_handle* h, const double* energy, const double* force, const double* stress,
+                       const int* has_efs, const double* w_efs);
+
+/* Neighbour lists + descriptors of the staged batch (compute_descriptors).
+ * B_out[dim_desc*sum(nat)] (may be NULL); n_neigh_out[sum(nat)] (may be NULL). */
+int mld_gpu_descriptors(mld_gpu_handle* h, double* B_out, int* n_neigh_out);
+
+/* Per-pair derivatives dB/du of the last mld_gpu_descriptors call, in neighbour-list order:
+ * nbr_out[P] (global atom index of each neighbour, per centre atom in order), u_out[3*P]
+ * (x_neighbour - x_centre), dB_out[3*dim_desc*P] (derivative with the sign of
+ * descriptors.F90:298-302).  *P_inout: capacity in pairs on input, pairs on output. */
+int mld_gpu_descriptor_derivatives(mld_gpu_handle* h, long long* P_inout, int* nbr_out, double* u_out,
+                                   double* dB_out);
+
+/* Number of design rows of the staged batch (energy + 3N force + 6 stress rows per structure,
+ * as the has_efs flags and desc_forces select). */
+int mld_gpu_num_rows(mld_gpu_handle* h, long long* M);
+
+/* Build and return the design matrix A[M*dim_design_line], labels y[M] and row weights w[M]
+ * (any may be NULL). */
+int mld_gpu_design_matrix(mld_gpu_handle* h, double* A, double* y, double* w);
+
+/* Weighted normal matrix G[D*D] = A^T W A and rhs[D] = A^T W y of the staged batch
+ * (no ridge term; module_online_fit.F90 gram%accumulate). */
+int mld_gpu_gram(mld_gpu_handle* h, double* G, double* rhs);
+
+/* Min-norm ridge solve of (G + lambda*I) w = rhs with the handle's lambda_krr / svd_rcond
+ * (serial_lsystem_by_svd).  rank_out may be NULL. */
+int mld_gpu_solve(mld_gpu_handle* h, const double* G, const double* rhs, int D, double* w, int* rank_out);
+
+/* Full fit of the staged batch: neighbours, descriptors, rows, Gram, ridge solve
+ * (main_train_mld / train_snap_get_parameters).  w_params[dim_design_line];
+ * rmse_efs[3] (may be NULL) = train RMSE of energy, force components, stress. */
+int mld_gpu_fit(mld_gpu_handle* h, double* w_params, double* rmse_efs);
+
+/* Predictions of the staged batch with coefficients w_params (md_mld_compute_energy/force/stress):
+ * E[S] (w . energy row, excluding reference energies), F[3*sum(nat)], S[6*S]; any may be NULL. */
+int mld_gpu_predict(mld_gpu_handle* h, const double* w_params, double* E, double* F, double* S);
+
+/* Block until the handle's stream has finished. */
+int mld_gpu_synchronize(mld_gpu_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MLD_GPU_H */

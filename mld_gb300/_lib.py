@@ -1,0 +1,222 @@
+"""ctypes binding of libmld_gpu.so (include/mld_gpu.h).  No PyTorch on this path.
+
+The library is built in-tree by ``mld_gb300.build`` (nvcc, sm_103a).  Loading fails loudly when
+it is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence, Tuple
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmld_gpu.so")
+
+MLD_OK = 0
+ERRORS = {1: "MLD_ERR_INVALID", 2: "MLD_ERR_CUDA", 3: "MLD_ERR_NEIGHBOUR_CAP", 4: "MLD_ERR_OOM",
+          5: "MLD_ERR_SOLVE", 6: "MLD_ERR_STATE", 7: "MLD_ERR_UNSUPPORTED"}
+PLAIN_FP64 = 0
+MIXED = 1
+MAX_ELEMENTS = 8
+
+EXPORTED = ["mld_gpu_config_defaults", "mld_gpu_create", "mld_gpu_destroy", "mld_gpu_last_error", "mld_gpu_dims",
+            "mld_gpu_set_structures", "mld_gpu_set_labels", "mld_gpu_descriptors",
+            "mld_gpu_descriptor_derivatives", "mld_gpu_num_rows", "mld_gpu_design_matrix", "mld_gpu_gram",
+            "mld_gpu_solve", "mld_gpu_fit", "mld_gpu_predict", "mld_gpu_synchronize"]
+
+
+class MldGpuConfig(ctypes.Structure):
+    _fields_ = [
+        ("descriptor_type", ctypes.c_int),
+        ("j_max", ctypes.c_double),
+        ("r_cut", ctypes.c_double),
+        ("inv_r0_input", ctypes.c_double),
+        ("weighted", ctypes.c_int),
+        ("weighted_3ch", ctypes.c_int),
+        ("n_elements", ctypes.c_int),
+        ("weight_per_element", ctypes.c_double * MAX_ELEMENTS),
+        ("weight_per_element_3ch", ctypes.c_double * MAX_ELEMENTS),
+        ("r_cut_pair_in", ctypes.c_double * (MAX_ELEMENTS * MAX_ELEMENTS)),
+        ("r_cut_width_in", ctypes.c_double),
+        ("desc_forces", ctypes.c_int),
+        ("ml_type", ctypes.c_int),
+        ("mld_order", ctypes.c_int),
+        ("lambda_krr", ctypes.c_double),
+        ("svd_rcond", ctypes.c_double),
+        ("sign_stress", ctypes.c_double),
+        ("sign_stress_big_box", ctypes.c_double),
+        ("imm_neigh", ctypes.c_int),
+        ("precision", ctypes.c_int),
+    ]
+
+
+class MldError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def load(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load the native library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -m mld_gb300.build` (needs nvcc)")
+    L = ctypes.CDLL(path)
+    P, I, D, LL = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
+    L.mld_gpu_config_defaults.argtypes = [ctypes.POINTER(MldGpuConfig)]
+    L.mld_gpu_config_defaults.restype = None
+    L.mld_gpu_create.argtypes = [ctypes.POINTER(MldGpuConfig), ctypes.POINTER(P)]
+    L.mld_gpu_destroy.argtypes = [P]
+    L.mld_gpu_destroy.restype = None
+    L.mld_gpu_last_error.argtypes = [P]
+    L.mld_gpu_last_error.restype = ctypes.c_char_p
+    L.mld_gpu_dims.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]
+    L.mld_gpu_set_structures.argtypes = [P, I, P, P, P, P]
+    L.mld_gpu_set_labels.argtypes = [P, P, P, P, P, P]
+    L.mld_gpu_descriptors.argtypes = [P, P, P]
+    L.mld_gpu_descriptor_derivatives.argtypes = [P, ctypes.POINTER(LL), P, P, P]
+    L.mld_gpu_num_rows.argtypes = [P, ctypes.POINTER(LL)]
+    L.mld_gpu_design_matrix.argtypes = [P, P, P, P]
+    L.mld_gpu_gram.argtypes = [P, P, P]
+    L.mld_gpu_solve.argtypes = [P, P, P, I, P, ctypes.POINTER(I)]
+    L.mld_gpu_fit.argtypes = [P, P, P]
+    L.mld_gpu_predict.argtypes = [P, P, P, P, P]
+    L.mld_gpu_synchronize.argtypes = [P]
+    for n in EXPORTED:
+        if n not in ("mld_gpu_config_defaults", "mld_gpu_destroy", "mld_gpu_last_error"):
+            getattr(L, n).restype = I
+    _lib = L
+    return L
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def default_config() -> MldGpuConfig:
+    c = MldGpuConfig()
+    load().mld_gpu_config_defaults(ctypes.byref(c))
+    return c
+
+
+class Handle:
+    """Thin owner of an ``mld_gpu_handle``; methods map 1:1 onto the C entry points."""
+
+    def __init__(self, cfg: MldGpuConfig):
+        self._L = load()
+        self._h = ctypes.c_void_p()
+        rc = self._L.mld_gpu_create(ctypes.byref(cfg), ctypes.byref(self._h))
+        if rc != MLD_OK:
+            raise MldError(rc, "mld_gpu_create failed")
+        self.cfg = cfg
+        K, dd, D = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._L.mld_gpu_dims(self._h, ctypes.byref(K), ctypes.byref(dd), ctypes.byref(D))
+        self.K, self.dim_desc, self.dim_design_line = K.value, dd.value, D.value
+        self.nat = np.zeros(0, np.int32)
+
+    def close(self):
+        if self._h:
+            self._L.mld_gpu_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != MLD_OK:
+            raise MldError(rc, self._L.mld_gpu_last_error(self._h).decode())
+
+    def set_structures(self, nat: Sequence[int], pos: np.ndarray, cell: np.ndarray, types: np.ndarray):
+        self.nat = np.ascontiguousarray(nat, dtype=np.int32)
+        self._pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        self._cell = np.ascontiguousarray(cell, dtype=np.float64).reshape(-1)
+        self._types = np.ascontiguousarray(types, dtype=np.int32).reshape(-1)
+        self._check(self._L.mld_gpu_set_structures(self._h, len(self.nat), _p(self.nat), _p(self._pos),
+                                                   _p(self._cell), _p(self._types)))
+
+    def set_labels(self, energy, force, stress, has_efs, w_efs):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+                for a in (energy, force, stress)]
+        has = np.ascontiguousarray(has_efs, dtype=np.int32).reshape(-1)
+        w = np.ascontiguousarray(w_efs, dtype=np.float64).reshape(-1)
+        self._check(self._L.mld_gpu_set_labels(self._h, _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), _p(has), _p(w)))
+
+    def descriptors(self) -> Tuple[np.ndarray, np.ndarray]:
+        A = int(self.nat.sum())
+        B = np.zeros((A, self.dim_desc))
+        nn = np.zeros(A, np.int32)
+        self._check(self._L.mld_gpu_descriptors(self._h, _p(B), _p(nn)))
+        return B, nn
+
+    def descriptor_derivatives(self, cap: int):
+        P = ctypes.c_longlong(cap)
+        nbr = np.zeros(cap, np.int32)
+        u = np.zeros((cap, 3))
+        dB = np.zeros((cap, 3, self.dim_desc))
+        self._check(self._L.mld_gpu_descriptor_derivatives(self._h, ctypes.byref(P), _p(nbr), _p(u), _p(dB)))
+        n = P.value
+        return nbr[:n], u[:n], dB[:n]
+
+    def num_rows(self) -> int:
+        M = ctypes.c_longlong()
+        self._check(self._L.mld_gpu_num_rows(self._h, ctypes.byref(M)))
+        return M.value
+
+    def design_matrix(self):
+        M = self.num_rows()
+        A = np.zeros((M, self.dim_design_line))
+        y = np.zeros(M)
+        w = np.zeros(M)
+        self._check(self._L.mld_gpu_design_matrix(self._h, _p(A), _p(y), _p(w)))
+        return A, y, w
+
+    def gram(self):
+        D = self.dim_design_line
+        G = np.zeros((D, D))
+        h = np.zeros(D)
+        self._check(self._L.mld_gpu_gram(self._h, _p(G), _p(h)))
+        return G, h
+
+    def solve(self, G: np.ndarray, rhs: np.ndarray):
+        D = G.shape[0]
+        G = np.ascontiguousarray(G, dtype=np.float64)
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+        w = np.zeros(D)
+        rank = ctypes.c_int()
+        self._check(self._L.mld_gpu_solve(self._h, _p(G), _p(rhs), D, _p(w), ctypes.byref(rank)))
+        return w, rank.value
+
+    def fit(self):
+        w = np.zeros(self.dim_design_line)
+        rmse = np.zeros(3)
+        self._check(self._L.mld_gpu_fit(self._h, _p(w), _p(rmse)))
+        return w, rmse
+
+    def predict(self, w: np.ndarray):
+        A = int(self.nat.sum())
+        S = len(self.nat)
+        E = np.zeros(S)
+        F = np.zeros((A, 3))
+        St = np.zeros((S, 6))
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        self._check(self._L.mld_gpu_predict(self._h, _p(w), _p(E), _p(F), _p(St)))
+        return E, F, St
+
+    def synchronize(self):
+        self._check(self._L.mld_gpu_synchronize(self._h))

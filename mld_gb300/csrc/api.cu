@@ -1,0 +1,770 @@
+// C ABI of libmld_gpu (declared in include/mld_gpu.h): handle, staging, orchestration.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mld_gpu.h"
+#include "mld_internal.h"
+
+namespace mld {
+template <typename T>
+cudaError_t launch_predict_sq(const T* X, const double* w, long long M, int D, double* pred, const double* y,
+                              const int* kind, double* sq, cudaStream_t st);
+template <typename T>
+cudaError_t launch_rows_prep(int S, const int* atom_start, const DevRows& rows, const double* E, const double* F,
+                             const double* Sv, const double* wefs, T* X, double* y, double* wrow, int* kind,
+                             cudaStream_t st);
+}  // namespace mld
+
+using namespace mld;
+
+namespace {
+
+struct Buf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+struct RowLayout {
+  std::vector<long long> rowE, rowF, rowS;
+  long long M = 0;
+};
+
+}  // namespace
+
+struct mld_gpu_handle {
+  mld_gpu_config cfg;
+  std::string err;
+  cudaStream_t st = nullptr;
+  int device = 0;
+  Bso4Tables tab;
+  DevTables dt;
+  BsoParams bp;
+  int nch = 1, K = 0, KK = 0, D = 0;
+  bool mixed = false;
+
+  // staged batch
+  int S = 0, A = 0;
+  std::vector<int> h_atom_start;
+  DevBatch b;
+  bool has_batch = false;
+  bool nbr_valid = false;
+  int max_nn = 0;
+
+  // labels
+  bool has_labels = false;
+  std::vector<int> h_has;  // 3*S
+  RowLayout fit_rows;
+
+  std::vector<void*> owned;  // table allocations
+  Buf bufs[40];
+  enum {
+    B_ATOM_START, B_ATOM_STRUCT, B_TYPES, B_POS, B_CELL, B_RECIP, B_SMALL, B_NSIZE, B_VOL,
+    B_NN, B_NBR_OFF, B_NBR_IDX, B_NBR_U, B_SCAN_TMP, B_MAXNN,
+    B_E, B_F, B_S, B_WEFS,
+    B_ROWE, B_ROWF, B_ROWS, B_X, B_Y, B_WROW, B_KIND,
+    B_G, B_H, B_W, B_EVALS, B_INFO, B_SQ, B_PRED, B_BOUT, B_DBOUT,
+    B_COUNT
+  };
+};
+
+namespace {
+
+int fail(mld_gpu_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int cuda_fail(mld_gpu_handle* h, cudaError_t e, const char* where) {
+  return fail(h, e == cudaErrorMemoryAllocation ? MLD_ERR_OOM : MLD_ERR_CUDA,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                   \
+  do {                                             \
+    cudaError_t _e = (call);                       \
+    if (_e != cudaSuccess) return cuda_fail(h, _e, #call); \
+  } while (0)
+
+cudaError_t ensure(mld_gpu_handle* h, int id, size_t bytes) {
+  Buf& bf = h->bufs[id];
+  if (bytes <= bf.cap && bf.p) return cudaSuccess;
+  if (bf.p) cudaFree(bf.p);
+  bf.p = nullptr;
+  bf.cap = 0;
+  size_t want = std::max<size_t>(bytes, 256);
+  want = want + want / 8;  // headroom for slowly growing batches
+  cudaError_t e = cudaMalloc(&bf.p, want);
+  if (e != cudaSuccess) return e;
+  bf.cap = want;
+  return cudaSuccess;
+}
+
+template <typename P>
+P* bp_(mld_gpu_handle* h, int id) {
+  return reinterpret_cast<P*>(h->bufs[id].p);
+}
+
+template <typename V>
+cudaError_t upload(mld_gpu_handle* h, int id, const V* src, size_t n) {
+  cudaError_t e = ensure(h, id, sizeof(V) * n);
+  if (e != cudaSuccess) return e;
+  if (n == 0) return cudaSuccess;
+  return cudaMemcpyAsync(h->bufs[id].p, src, sizeof(V) * n, cudaMemcpyHostToDevice, h->st);
+}
+
+template <typename V>
+cudaError_t dev_alloc_copy(mld_gpu_handle* h, V** dst, const V* src, size_t n) {
+  cudaError_t e = cudaMalloc((void**)dst, sizeof(V) * std::max<size_t>(n, 1));
+  if (e != cudaSuccess) return e;
+  h->owned.push_back(*dst);
+  if (n) e = cudaMemcpy(*dst, src, sizeof(V) * n, cudaMemcpyHostToDevice);
+  return e;
+}
+
+void recips(const double* cell, double* bg) {
+  const double *a1 = cell, *a2 = cell + 3, *a3 = cell + 6;
+  double c23[3] = {a2[1] * a3[2] - a2[2] * a3[1], a2[2] * a3[0] - a2[0] * a3[2], a2[0] * a3[1] - a2[1] * a3[0]};
+  double c31[3] = {a3[1] * a1[2] - a3[2] * a1[1], a3[2] * a1[0] - a3[0] * a1[2], a3[0] * a1[1] - a3[1] * a1[0]};
+  double c12[3] = {a1[1] * a2[2] - a1[2] * a2[1], a1[2] * a2[0] - a1[0] * a2[2], a1[0] * a2[1] - a1[1] * a2[0]};
+  double vol = a1[0] * c23[0] + a1[1] * c23[1] + a1[2] * c23[2];
+  for (int c = 0; c < 3; ++c) {
+    bg[c] = c23[c] / vol;
+    bg[3 + c] = c31[c] / vol;
+    bg[6 + c] = c12[c] / vol;
+  }
+}
+
+// Row layout: energy row, 3*nat force rows, 6 stress rows per structure, in structure order.
+RowLayout make_layout(const mld_gpu_handle* h, const std::vector<int>& has, bool force_all) {
+  RowLayout L;
+  L.rowE.assign(h->S, -1);
+  L.rowF.assign(h->S, -1);
+  L.rowS.assign(h->S, -1);
+  long long r = 0;
+  for (int s = 0; s < h->S; ++s) {
+    int nat = h->h_atom_start[s + 1] - h->h_atom_start[s];
+    bool e = force_all || has[3 * s];
+    bool f = force_all || (has[3 * s + 1] && h->cfg.desc_forces);
+    bool st = force_all || (has[3 * s + 2] && h->cfg.desc_forces);
+    if (e) L.rowE[s] = r++;
+    if (f) {
+      L.rowF[s] = r;
+      r += 3LL * nat;
+    }
+    if (st) {
+      L.rowS[s] = r;
+      r += 6;
+    }
+  }
+  L.M = r;
+  return L;
+}
+
+int build_neighbours(mld_gpu_handle* h) {
+  if (!h->has_batch) return fail(h, MLD_ERR_STATE, "no structures staged");
+  DevBatch& b = h->b;
+  CK(ensure(h, mld_gpu_handle::B_NN, sizeof(int) * std::max(1, h->A)));
+  CK(ensure(h, mld_gpu_handle::B_NBR_OFF, sizeof(int) * (h->A + 1)));
+  CK(ensure(h, mld_gpu_handle::B_SCAN_TMP, sizeof(int) * ((h->A + 1023) / 1024 + 2)));
+  CK(ensure(h, mld_gpu_handle::B_MAXNN, sizeof(int) * 2));
+  b.nn = bp_<int>(h, mld_gpu_handle::B_NN);
+  b.nbr_off = bp_<int>(h, mld_gpu_handle::B_NBR_OFF);
+  int* dmax = bp_<int>(h, mld_gpu_handle::B_MAXNN);
+  CK(cudaMemsetAsync(dmax, 0, sizeof(int), h->st));
+  CK(launch_neighbours(b, h->cfg.r_cut, b.nn, dmax, h->st, 0));
+  CK(launch_scan(b.nn, b.nbr_off, h->A, bp_<int>(h, mld_gpu_handle::B_SCAN_TMP), h->st));
+  int hv[2] = {0, 0};
+  CK(cudaMemcpyAsync(&hv[0], b.nbr_off + h->A, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(&hv[1], dmax, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (hv[1] > h->cfg.imm_neigh)
+    return fail(h, MLD_ERR_NEIGHBOUR_CAP,
+                "an atom has " + std::to_string(hv[1]) + " neighbours within r_cut, more than imm_neigh=" +
+                    std::to_string(h->cfg.imm_neigh));
+  h->max_nn = hv[1];
+  b.P = hv[0];
+  CK(ensure(h, mld_gpu_handle::B_NBR_IDX, sizeof(int) * std::max<long long>(b.P, 1)));
+  CK(ensure(h, mld_gpu_handle::B_NBR_U, sizeof(double) * 3 * std::max<long long>(b.P, 1)));
+  b.nbr_idx = bp_<int>(h, mld_gpu_handle::B_NBR_IDX);
+  b.nbr_u = bp_<double>(h, mld_gpu_handle::B_NBR_U);
+  CK(launch_neighbours(b, h->cfg.r_cut, b.nn, dmax, h->st, 1));
+  h->nbr_valid = true;
+  return MLD_OK;
+}
+
+template <typename T>
+int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) {
+  DevRows rows;
+  rows.M = L.M;
+  rows.D = h->D;
+  CK(upload(h, mld_gpu_handle::B_ROWE, L.rowE.data(), h->S));
+  CK(upload(h, mld_gpu_handle::B_ROWF, L.rowF.data(), h->S));
+  CK(upload(h, mld_gpu_handle::B_ROWS, L.rowS.data(), h->S));
+  rows.rowE = bp_<long long>(h, mld_gpu_handle::B_ROWE);
+  rows.rowF = bp_<long long>(h, mld_gpu_handle::B_ROWF);
+  rows.rowS = bp_<long long>(h, mld_gpu_handle::B_ROWS);
+  size_t xbytes = sizeof(T) * (size_t)std::max<long long>(L.M, 1) * h->D;
+  CK(ensure(h, mld_gpu_handle::B_X, xbytes));
+  CK(ensure(h, mld_gpu_handle::B_Y, sizeof(double) * std::max<long long>(L.M, 1)));
+  CK(ensure(h, mld_gpu_handle::B_WROW, sizeof(double) * std::max<long long>(L.M, 1)));
+  CK(ensure(h, mld_gpu_handle::B_KIND, sizeof(int) * std::max<long long>(L.M, 1)));
+  T* X = bp_<T>(h, mld_gpu_handle::B_X);
+  CK(cudaMemsetAsync(X, 0, xbytes, h->st));
+  const double* dE = with_labels ? bp_<double>(h, mld_gpu_handle::B_E) : nullptr;
+  if (with_labels) {
+    CK(launch_rows_prep<T>(h->S, h->b.atom_start, rows, bp_<double>(h, mld_gpu_handle::B_E),
+                           bp_<double>(h, mld_gpu_handle::B_F), bp_<double>(h, mld_gpu_handle::B_S),
+                           bp_<double>(h, mld_gpu_handle::B_WEFS), X, bp_<double>(h, mld_gpu_handle::B_Y),
+                           bp_<double>(h, mld_gpu_handle::B_WROW), bp_<int>(h, mld_gpu_handle::B_KIND), h->st));
+  } else {
+    // energy-row constant column only; labels unused
+    std::vector<double> zeros(1, 0.0);
+    (void)zeros;
+    (void)dE;
+    CK(ensure(h, mld_gpu_handle::B_E, sizeof(double) * std::max(1, h->S)));
+    CK(ensure(h, mld_gpu_handle::B_F, sizeof(double) * 3 * std::max(1, h->A)));
+    CK(ensure(h, mld_gpu_handle::B_S, sizeof(double) * 6 * std::max(1, h->S)));
+    CK(ensure(h, mld_gpu_handle::B_WEFS, sizeof(double) * 3 * std::max(1, h->S)));
+    CK(launch_rows_prep<T>(h->S, h->b.atom_start, rows, bp_<double>(h, mld_gpu_handle::B_E),
+                           bp_<double>(h, mld_gpu_handle::B_F), bp_<double>(h, mld_gpu_handle::B_S),
+                           bp_<double>(h, mld_gpu_handle::B_WEFS), X, bp_<double>(h, mld_gpu_handle::B_Y),
+                           bp_<double>(h, mld_gpu_handle::B_WROW), bp_<int>(h, mld_gpu_handle::B_KIND), h->st));
+  }
+  CK(launch_bso4_rows<T>(h->dt, h->b, rows, h->bp, X, (T*)nullptr, (T*)nullptr, 1, h->st));
+  *Xout = X;
+  return MLD_OK;
+}
+
+template <typename T>
+int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
+  int rc = build_neighbours(h);
+  if (rc) return rc;
+  T* X = nullptr;
+  rc = run_rows<T>(h, h->fit_rows, true, &X);
+  if (rc) return rc;
+  const long long M = h->fit_rows.M;
+  const int D = h->D;
+  CK(ensure(h, mld_gpu_handle::B_G, sizeof(double) * D * D));
+  CK(ensure(h, mld_gpu_handle::B_H, sizeof(double) * D));
+  CK(ensure(h, mld_gpu_handle::B_W, sizeof(double) * D));
+  CK(ensure(h, mld_gpu_handle::B_EVALS, sizeof(double) * D));
+  CK(ensure(h, mld_gpu_handle::B_INFO, sizeof(int) * 4));
+  CK(ensure(h, mld_gpu_handle::B_SQ, sizeof(double) * 6));
+  double* G = bp_<double>(h, mld_gpu_handle::B_G);
+  double* hv = bp_<double>(h, mld_gpu_handle::B_H);
+  double* w = bp_<double>(h, mld_gpu_handle::B_W);
+  CK(launch_gram<T>(X, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D, G, hv,
+                    h->st));
+  CK(launch_solve_sym(G, hv, D, h->cfg.lambda_krr, h->cfg.svd_rcond, w, bp_<double>(h, mld_gpu_handle::B_EVALS),
+                      bp_<int>(h, mld_gpu_handle::B_INFO), h->st));
+  double* sq = bp_<double>(h, mld_gpu_handle::B_SQ);
+  CK(cudaMemsetAsync(sq, 0, sizeof(double) * 6, h->st));
+  CK(launch_predict_sq<T>(X, w, M, D, nullptr, bp_<double>(h, mld_gpu_handle::B_Y), bp_<int>(h, mld_gpu_handle::B_KIND),
+                          sq, h->st));
+  double hsq[6];
+  if (w_params) CK(cudaMemcpyAsync(w_params, w, sizeof(double) * D, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(hsq, sq, sizeof(double) * 6, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (rmse)
+    for (int k = 0; k < 3; ++k) rmse[k] = hsq[3 + k] > 0 ? std::sqrt(hsq[k] / hsq[3 + k]) : 0.0;
+  return MLD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void mld_gpu_config_defaults(mld_gpu_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->descriptor_type = 9;
+  c->j_max = 1.5;
+  c->r_cut = 5.0;
+  c->inv_r0_input = 1.0 - 0.02 / 3.14159265358979323846;
+  c->weighted = 0;
+  c->weighted_3ch = 0;
+  c->n_elements = 1;
+  for (int i = 0; i < MLD_MAX_ELEMENTS; ++i) {
+    c->weight_per_element[i] = 1.0;
+    c->weight_per_element_3ch[i] = 1.0;
+  }
+  c->r_cut_width_in = 0.4;
+  c->desc_forces = 1;
+  c->ml_type = 0;
+  c->mld_order = 1;
+  c->lambda_krr = -1.0;
+  c->svd_rcond = -1.0;
+  c->sign_stress = 1.0;
+  c->sign_stress_big_box = 1.0;
+  c->imm_neigh = 300;
+  c->precision = MLD_PRECISION_PLAIN_FP64;
+}
+
+const char* mld_gpu_last_error(const mld_gpu_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int mld_gpu_create(const mld_gpu_config* cfg, mld_gpu_handle** out) {
+  if (!cfg || !out) return MLD_ERR_INVALID;
+  *out = nullptr;
+  if (cfg->descriptor_type != 9) return MLD_ERR_UNSUPPORTED;
+  if (cfg->ml_type != 0 || cfg->mld_order != 1) return MLD_ERR_UNSUPPORTED;
+  if (!(cfg->inv_r0_input > 0.0 && cfg->inv_r0_input < 1.0)) return MLD_ERR_INVALID;  // test_parameters_bso4
+  if (cfg->j_max < 0 || !(cfg->r_cut > 0)) return MLD_ERR_INVALID;
+  if (cfg->n_elements < 1 || cfg->n_elements > MLD_MAX_ELEMENTS) return MLD_ERR_INVALID;
+  if (cfg->weighted_3ch && !cfg->weighted) return MLD_ERR_INVALID;
+  if (cfg->precision != MLD_PRECISION_PLAIN_FP64 && cfg->precision != MLD_PRECISION_MIXED) return MLD_ERR_INVALID;
+  if (cfg->imm_neigh < 1) return MLD_ERR_INVALID;
+  mld_gpu_handle* h = new mld_gpu_handle();
+  h->cfg = *cfg;
+  h->mixed = cfg->precision == MLD_PRECISION_MIXED;
+  if (!build_bso4_tables(cfg->j_max, &h->tab, &h->err)) {
+    delete h;
+    return MLD_ERR_INVALID;
+  }
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete h;
+    return MLD_ERR_CUDA;
+  }
+  const Bso4Tables& t = h->tab;
+  h->nch = cfg->weighted ? (cfg->weighted_3ch ? 3 : 2) : 1;
+  h->K = t.K;
+  h->KK = h->nch * t.K;
+  h->D = 1 + h->KK;
+  // device tables
+  DevTables& d = h->dt;
+  d.J = t.J;
+  d.NU = t.NU;
+  d.K = t.K;
+  d.NY = (int)t.yslots.size();
+  std::vector<float> cg32(t.cg.begin(), t.cg.end());
+  std::vector<double> tz(t.NU, 0.0), tx(t.NU, 0.0);
+  std::vector<int16_t> sz(t.NU, -1), sx(t.NU, -1), uj(t.NU), up(t.NU), uq(t.NU);
+  std::vector<int8_t> qn(t.NU, 0);
+  for (int j = 0; j <= t.J; ++j) {
+    int e2 = 0;
+    for (int p = -j; p <= j; p += 2)
+      for (int q = -j; q <= j; q += 2, ++e2) {
+        int idx = t.off[j] + e2;
+        uj[idx] = (int16_t)j;
+        up[idx] = (int16_t)p;
+        uq[idx] = (int16_t)q;
+        if (j == 0) continue;
+        auto loc = [&](int pp, int qq) { return ((pp + j - 1) / 2) * j + (qq + j - 1) / 2; };
+        if (q != -j) {
+          double den = (double)(j + q);
+          if (p != -j) {
+            tz[idx] = std::sqrt((double)(j + p) / den);
+            sz[idx] = (int16_t)loc(p - 1, q - 1);
+          }
+          if (p != j) {
+            tx[idx] = std::sqrt((double)(j - p) / den);
+            sx[idx] = (int16_t)loc(p + 1, q - 1);
+          }
+        } else {
+          qn[idx] = 1;
+          double den = (double)(j - q);
+          if (p != j) {
+            tz[idx] = std::sqrt((double)(j - p) / den);
+            sz[idx] = (int16_t)loc(p + 1, q + 1);
+          }
+          if (p != -j) {
+            tx[idx] = std::sqrt((double)(j + p) / den);
+            sx[idx] = (int16_t)loc(p - 1, q + 1);
+          }
+        }
+      }
+  }
+  std::vector<float> tz32(tz.begin(), tz.end()), tx32(tx.begin(), tx.end());
+  e = cudaSuccess;
+#define UP(dst, vec) \
+  if (e == cudaSuccess) e = dev_alloc_copy(h, &dst, vec.data(), vec.size())
+  UP(d.zterms, t.zterms);
+  UP(d.yslots, t.yslots);
+  UP(d.kslot_begin, t.kslot_begin);
+  UP(d.yorder, t.yorder);
+  UP(d.cg64, t.cg);
+  UP(d.cg32, cg32);
+  UP(d.rec_tz64, tz);
+  UP(d.rec_tx64, tx);
+  UP(d.rec_tz32, tz32);
+  UP(d.rec_tx32, tx32);
+  UP(d.rec_sz, sz);
+  UP(d.rec_sx, sx);
+  UP(d.rec_qneg, qn);
+  UP(d.uj, uj);
+  UP(d.up, up);
+  UP(d.uq, uq);
+#undef UP
+  if (e != cudaSuccess) {
+    int code = cuda_fail(h, e, "table upload");
+    mld_gpu_destroy(h);
+    return code;
+  }
+  // parameters
+  BsoParams& p = h->bp;
+  std::memset(&p, 0, sizeof(p));
+  p.rcut = cfg->r_cut;
+  p.inv_r0 = 3.14159265358979323846 * cfg->inv_r0_input;
+  p.nch = h->nch;
+  p.ntypes = cfg->n_elements;
+  for (int tt = 0; tt < cfg->n_elements; ++tt) {
+    p.chw[0 * p.ntypes + tt] = 1.0;
+    if (h->nch > 1) p.chw[1 * p.ntypes + tt] = cfg->weight_per_element[tt];
+    if (h->nch > 2) p.chw[2 * p.ntypes + tt] = cfg->weight_per_element_3ch[tt];
+  }
+  p.has_rin = 0;
+  for (int a = 0; a < cfg->n_elements; ++a)
+    for (int c2 = 0; c2 < cfg->n_elements; ++c2) {
+      double v = cfg->r_cut_pair_in[a * MLD_MAX_ELEMENTS + c2];
+      p.rin[a * p.ntypes + c2] = v;
+      if (v > 0) p.has_rin = 1;
+    }
+  p.rin_width = cfg->r_cut_width_in;
+  p.sign_stress = cfg->sign_stress;
+  p.sign_big = cfg->sign_stress_big_box;
+  *out = h;
+  return MLD_OK;
+}
+
+void mld_gpu_destroy(mld_gpu_handle* h) {
+  if (!h) return;
+  if (h->st) cudaStreamSynchronize(h->st);
+  for (auto& bf : h->bufs)
+    if (bf.p) cudaFree(bf.p);
+  for (void* p : h->owned) cudaFree(p);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+}
+
+int mld_gpu_dims(const mld_gpu_handle* h, int* K, int* dim_desc, int* dim_design_line) {
+  if (!h) return MLD_ERR_INVALID;
+  if (K) *K = h->K;
+  if (dim_desc) *dim_desc = h->KK;
+  if (dim_design_line) *dim_design_line = h->D;
+  return MLD_OK;
+}
+
+int mld_gpu_set_structures(mld_gpu_handle* h, int nstruct, const int* nat, const double* pos, const double* cell,
+                           const int* types) {
+  if (!h) return MLD_ERR_INVALID;
+  if (nstruct < 0 || (nstruct > 0 && (!nat || !cell))) return fail(h, MLD_ERR_INVALID, "bad structure arrays");
+  std::vector<int> start(nstruct + 1, 0);
+  for (int s = 0; s < nstruct; ++s) {
+    if (nat[s] < 0) return fail(h, MLD_ERR_INVALID, "negative atom count");
+    start[s + 1] = start[s] + nat[s];
+  }
+  const int A = start[nstruct];
+  if (A > 0 && (!pos || !types)) return fail(h, MLD_ERR_INVALID, "missing positions or types");
+  std::vector<int> astruct(A);
+  for (int s = 0; s < nstruct; ++s)
+    for (int i = start[s]; i < start[s + 1]; ++i) astruct[i] = s;
+  for (int i = 0; i < A; ++i)
+    if (types[i] < 0 || types[i] >= h->cfg.n_elements) return fail(h, MLD_ERR_INVALID, "type index out of range");
+  for (long long i = 0; i < 3LL * A; ++i)
+    if (!std::isfinite(pos[i])) return fail(h, MLD_ERR_INVALID, "non-finite position");
+  std::vector<double> rec(9 * (size_t)nstruct), vol(nstruct);
+  std::vector<int> small(nstruct), nsize(3 * (size_t)nstruct);
+  for (int s = 0; s < nstruct; ++s) {
+    const double* cl = cell + 9 * (size_t)s;
+    recips(cl, &rec[9 * (size_t)s]);
+    double v = cl[0] * (cl[4] * cl[8] - cl[5] * cl[7]) - cl[1] * (cl[3] * cl[8] - cl[5] * cl[6]) +
+               cl[2] * (cl[3] * cl[7] - cl[4] * cl[6]);
+    if (!(std::fabs(v) > 0)) return fail(h, MLD_ERR_INVALID, "singular cell");
+    vol[s] = std::fabs(v);
+    // neighbours.F90:787-847
+    int sm = 0;
+    for (int i = 0; i < 3; ++i) {
+      const double* bgi = &rec[9 * (size_t)s + 3 * i];
+      double bval = 1.0 / std::sqrt(bgi[0] * bgi[0] + bgi[1] * bgi[1] + bgi[2] * bgi[2]);
+      int nc = (int)(2.0 * h->cfg.r_cut / bval) + 1;
+      if (nc > 1) sm = 1;
+      nsize[3 * s + i] = nc / 2 + 1;
+    }
+    small[s] = sm;
+  }
+  h->S = nstruct;
+  h->A = A;
+  h->h_atom_start = start;
+  DevBatch& b = h->b;
+  b.S = nstruct;
+  b.A = A;
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_ATOM_START, start.data(), start.size());
+  if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_ATOM_STRUCT, astruct.data(), astruct.size());
+  if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_TYPES, types, (size_t)A);
+  if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_POS, pos, 3 * (size_t)A);
+  if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_CELL, cell, 9 * (size_t)nstruct);
+  if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_RECIP, rec.data(), rec.size());
+  if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_SMALL, small.data(), small.size());
+  if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_NSIZE, nsize.data(), nsize.size());
+  if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_VOL, vol.data(), vol.size());
+  if (e != cudaSuccess) return cuda_fail(h, e, "mld_gpu_set_structures");
+  b.atom_start = bp_<int>(h, mld_gpu_handle::B_ATOM_START);
+  b.atom_struct = bp_<int>(h, mld_gpu_handle::B_ATOM_STRUCT);
+  b.types = bp_<int>(h, mld_gpu_handle::B_TYPES);
+  b.pos = bp_<double>(h, mld_gpu_handle::B_POS);
+  b.cell = bp_<double>(h, mld_gpu_handle::B_CELL);
+  b.recip = bp_<double>(h, mld_gpu_handle::B_RECIP);
+  b.small = bp_<int>(h, mld_gpu_handle::B_SMALL);
+  b.nsize = bp_<int>(h, mld_gpu_handle::B_NSIZE);
+  b.volume = bp_<double>(h, mld_gpu_handle::B_VOL);
+  // the host arrays of this call are read by the stream above: wait before returning
+  e = cudaStreamSynchronize(h->st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "mld_gpu_set_structures");
+  h->has_batch = true;
+  h->nbr_valid = false;
+  h->has_labels = false;
+  return MLD_OK;
+}
+
+int mld_gpu_set_labels(mld_gpu_handle* h, const double* energy, const double* force, const double* stress,
+                       const int* has_efs, const double* w_efs) {
+  if (!h) return MLD_ERR_INVALID;
+  if (!h->has_batch) return fail(h, MLD_ERR_STATE, "no structures staged");
+  if (!has_efs || !w_efs) return fail(h, MLD_ERR_INVALID, "has_efs and w_efs are required");
+  const int S = h->S, A = h->A;
+  h->h_has.assign(has_efs, has_efs + 3 * (size_t)S);
+  bool anyE = false, anyF = false, anyS = false;
+  for (int s = 0; s < S; ++s) {
+    anyE |= has_efs[3 * s] != 0;
+    anyF |= has_efs[3 * s + 1] != 0;
+    anyS |= has_efs[3 * s + 2] != 0;
+  }
+  if ((anyE && !energy) || (anyF && h->cfg.desc_forces && !force) || (anyS && h->cfg.desc_forces && !stress))
+    return fail(h, MLD_ERR_INVALID, "missing label array for a flagged block");
+  std::vector<double> zE, zF, zS;
+  if (!energy) zE.assign(std::max(S, 1), 0.0), energy = zE.data();
+  if (!force) zF.assign(3 * (size_t)std::max(A, 1), 0.0), force = zF.data();
+  if (!stress) zS.assign(6 * (size_t)std::max(S, 1), 0.0), stress = zS.data();
+  cudaError_t e = upload(h, mld_gpu_handle::B_E, energy, (size_t)S);
+  if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_F, force, 3 * (size_t)A);
+  if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_S, stress, 6 * (size_t)S);
+  if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_WEFS, w_efs, 3 * (size_t)S);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  if (e != cudaSuccess) return cuda_fail(h, e, "mld_gpu_set_labels");
+  h->fit_rows = make_layout(h, h->h_has, false);
+  h->has_labels = true;
+  return MLD_OK;
+}
+
+int mld_gpu_descriptors(mld_gpu_handle* h, double* B_out, int* n_neigh_out) {
+  if (!h) return MLD_ERR_INVALID;
+  int rc = build_neighbours(h);
+  if (rc) return rc;
+  RowLayout none;
+  none.rowE.assign(h->S, -1);
+  none.rowF.assign(h->S, -1);
+  none.rowS.assign(h->S, -1);
+  DevRows rows;
+  rows.D = h->D;
+  CK(upload(h, mld_gpu_handle::B_ROWE, none.rowE.data(), h->S));
+  CK(upload(h, mld_gpu_handle::B_ROWF, none.rowF.data(), h->S));
+  CK(upload(h, mld_gpu_handle::B_ROWS, none.rowS.data(), h->S));
+  rows.rowE = bp_<long long>(h, mld_gpu_handle::B_ROWE);
+  rows.rowF = bp_<long long>(h, mld_gpu_handle::B_ROWF);
+  rows.rowS = bp_<long long>(h, mld_gpu_handle::B_ROWS);
+  const size_t nB = (size_t)h->A * h->KK;
+  const size_t nd = (size_t)h->b.P * 3 * h->KK;
+  if (h->mixed) {
+    CK(ensure(h, mld_gpu_handle::B_BOUT, sizeof(float) * std::max<size_t>(nB, 1)));
+    CK(ensure(h, mld_gpu_handle::B_DBOUT, sizeof(float) * std::max<size_t>(nd, 1)));
+    CK(launch_bso4_rows<float>(h->dt, h->b, rows, h->bp, (float*)nullptr, bp_<float>(h, mld_gpu_handle::B_BOUT),
+                               bp_<float>(h, mld_gpu_handle::B_DBOUT), 0, h->st));
+    if (B_out) {
+      std::vector<float> tmp(nB);
+      CK(cudaMemcpyAsync(tmp.data(), bp_<float>(h, mld_gpu_handle::B_BOUT), sizeof(float) * nB,
+                         cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+      for (size_t i = 0; i < nB; ++i) B_out[i] = tmp[i];
+    }
+  } else {
+    CK(ensure(h, mld_gpu_handle::B_BOUT, sizeof(double) * std::max<size_t>(nB, 1)));
+    CK(ensure(h, mld_gpu_handle::B_DBOUT, sizeof(double) * std::max<size_t>(nd, 1)));
+    CK(launch_bso4_rows<double>(h->dt, h->b, rows, h->bp, (double*)nullptr, bp_<double>(h, mld_gpu_handle::B_BOUT),
+                                bp_<double>(h, mld_gpu_handle::B_DBOUT), 0, h->st));
+    if (B_out)
+      CK(cudaMemcpyAsync(B_out, bp_<double>(h, mld_gpu_handle::B_BOUT), sizeof(double) * nB, cudaMemcpyDeviceToHost,
+                         h->st));
+  }
+  if (n_neigh_out)
+    CK(cudaMemcpyAsync(n_neigh_out, h->b.nn, sizeof(int) * h->A, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return MLD_OK;
+}
+
+int mld_gpu_descriptor_derivatives(mld_gpu_handle* h, long long* P_inout, int* nbr_out, double* u_out,
+                                   double* dB_out) {
+  if (!h || !P_inout) return MLD_ERR_INVALID;
+  if (!h->nbr_valid) return fail(h, MLD_ERR_STATE, "call mld_gpu_descriptors first");
+  const long long P = h->b.P;
+  if (*P_inout < P) {
+    *P_inout = P;
+    return fail(h, MLD_ERR_INVALID, "pair capacity too small");
+  }
+  *P_inout = P;
+  if (nbr_out) CK(cudaMemcpyAsync(nbr_out, h->b.nbr_idx, sizeof(int) * P, cudaMemcpyDeviceToHost, h->st));
+  if (u_out) CK(cudaMemcpyAsync(u_out, h->b.nbr_u, sizeof(double) * 3 * P, cudaMemcpyDeviceToHost, h->st));
+  const size_t nd = (size_t)P * 3 * h->KK;
+  if (dB_out) {
+    if (h->mixed) {
+      std::vector<float> tmp(nd);
+      CK(cudaMemcpyAsync(tmp.data(), bp_<float>(h, mld_gpu_handle::B_DBOUT), sizeof(float) * nd,
+                         cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+      for (size_t i = 0; i < nd; ++i) dB_out[i] = tmp[i];
+    } else {
+      CK(cudaMemcpyAsync(dB_out, bp_<double>(h, mld_gpu_handle::B_DBOUT), sizeof(double) * nd,
+                         cudaMemcpyDeviceToHost, h->st));
+    }
+  }
+  CK(cudaStreamSynchronize(h->st));
+  return MLD_OK;
+}
+
+int mld_gpu_num_rows(mld_gpu_handle* h, long long* M) {
+  if (!h || !M) return MLD_ERR_INVALID;
+  if (!h->has_labels) return fail(h, MLD_ERR_STATE, "labels not set");
+  *M = h->fit_rows.M;
+  return MLD_OK;
+}
+
+int mld_gpu_design_matrix(mld_gpu_handle* h, double* A, double* y, double* w) {
+  if (!h) return MLD_ERR_INVALID;
+  if (!h->has_labels) return fail(h, MLD_ERR_STATE, "labels not set");
+  int rc = build_neighbours(h);
+  if (rc) return rc;
+  const long long M = h->fit_rows.M;
+  const size_t n = (size_t)M * h->D;
+  if (h->mixed) {
+    float* X = nullptr;
+    rc = run_rows<float>(h, h->fit_rows, true, &X);
+    if (rc) return rc;
+    if (A) {
+      std::vector<float> tmp(n);
+      CK(cudaMemcpyAsync(tmp.data(), X, sizeof(float) * n, cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+      for (size_t i = 0; i < n; ++i) A[i] = tmp[i];
+    }
+  } else {
+    double* X = nullptr;
+    rc = run_rows<double>(h, h->fit_rows, true, &X);
+    if (rc) return rc;
+    if (A) CK(cudaMemcpyAsync(A, X, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+  }
+  if (y) CK(cudaMemcpyAsync(y, bp_<double>(h, mld_gpu_handle::B_Y), sizeof(double) * M, cudaMemcpyDeviceToHost, h->st));
+  if (w)
+    CK(cudaMemcpyAsync(w, bp_<double>(h, mld_gpu_handle::B_WROW), sizeof(double) * M, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return MLD_OK;
+}
+
+int mld_gpu_gram(mld_gpu_handle* h, double* G, double* rhs) {
+  if (!h) return MLD_ERR_INVALID;
+  if (!h->has_labels) return fail(h, MLD_ERR_STATE, "labels not set");
+  int rc = build_neighbours(h);
+  if (rc) return rc;
+  const int D = h->D;
+  const long long M = h->fit_rows.M;
+  CK(ensure(h, mld_gpu_handle::B_G, sizeof(double) * D * D));
+  CK(ensure(h, mld_gpu_handle::B_H, sizeof(double) * D));
+  if (h->mixed) {
+    float* X = nullptr;
+    rc = run_rows<float>(h, h->fit_rows, true, &X);
+    if (rc) return rc;
+    CK(launch_gram<float>(X, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D,
+                          bp_<double>(h, mld_gpu_handle::B_G), bp_<double>(h, mld_gpu_handle::B_H), h->st));
+  } else {
+    double* X = nullptr;
+    rc = run_rows<double>(h, h->fit_rows, true, &X);
+    if (rc) return rc;
+    CK(launch_gram<double>(X, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D,
+                           bp_<double>(h, mld_gpu_handle::B_G), bp_<double>(h, mld_gpu_handle::B_H), h->st));
+  }
+  if (G) CK(cudaMemcpyAsync(G, bp_<double>(h, mld_gpu_handle::B_G), sizeof(double) * D * D, cudaMemcpyDeviceToHost, h->st));
+  if (rhs) CK(cudaMemcpyAsync(rhs, bp_<double>(h, mld_gpu_handle::B_H), sizeof(double) * D, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return MLD_OK;
+}
+
+int mld_gpu_solve(mld_gpu_handle* h, const double* G, const double* rhs, int D, double* w, int* rank_out) {
+  if (!h || !G || !rhs || !w || D < 1) return MLD_ERR_INVALID;
+  if (D > 112) return fail(h, MLD_ERR_UNSUPPORTED, "symmetric solve limited to D <= 112 in this build");
+  double *dG = nullptr, *dh = nullptr, *dw = nullptr;
+  int* dinfo = nullptr;
+  CK(ensure(h, mld_gpu_handle::B_G, sizeof(double) * D * D));
+  CK(ensure(h, mld_gpu_handle::B_H, sizeof(double) * D));
+  CK(ensure(h, mld_gpu_handle::B_W, sizeof(double) * D));
+  CK(ensure(h, mld_gpu_handle::B_INFO, sizeof(int) * 4));
+  dG = bp_<double>(h, mld_gpu_handle::B_G);
+  dh = bp_<double>(h, mld_gpu_handle::B_H);
+  dw = bp_<double>(h, mld_gpu_handle::B_W);
+  dinfo = bp_<int>(h, mld_gpu_handle::B_INFO);
+  CK(cudaMemcpyAsync(dG, G, sizeof(double) * D * D, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(dh, rhs, sizeof(double) * D, cudaMemcpyHostToDevice, h->st));
+  CK(launch_solve_sym(dG, dh, D, h->cfg.lambda_krr, h->cfg.svd_rcond, dw, nullptr, dinfo, h->st));
+  int info[2];
+  CK(cudaMemcpyAsync(w, dw, sizeof(double) * D, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(info, dinfo, sizeof(int) * 2, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (rank_out) *rank_out = info[1];
+  return MLD_OK;
+}
+
+int mld_gpu_fit(mld_gpu_handle* h, double* w_params, double* rmse_efs) {
+  if (!h) return MLD_ERR_INVALID;
+  if (!h->has_labels) return fail(h, MLD_ERR_STATE, "labels not set");
+  if (h->D > 112) return fail(h, MLD_ERR_UNSUPPORTED, "symmetric solve limited to D <= 112 in this build");
+  return h->mixed ? fit_impl<float>(h, w_params, rmse_efs) : fit_impl<double>(h, w_params, rmse_efs);
+}
+
+int mld_gpu_predict(mld_gpu_handle* h, const double* w_params, double* E, double* F, double* Sout) {
+  if (!h || !w_params) return MLD_ERR_INVALID;
+  int rc = build_neighbours(h);
+  if (rc) return rc;
+  std::vector<int> all(3 * (size_t)h->S, 1);
+  RowLayout L = make_layout(h, all, true);
+  const int D = h->D;
+  CK(ensure(h, mld_gpu_handle::B_W, sizeof(double) * D));
+  CK(ensure(h, mld_gpu_handle::B_PRED, sizeof(double) * std::max<long long>(L.M, 1)));
+  double* dw = bp_<double>(h, mld_gpu_handle::B_W);
+  double* pred = bp_<double>(h, mld_gpu_handle::B_PRED);
+  CK(cudaMemcpyAsync(dw, w_params, sizeof(double) * D, cudaMemcpyHostToDevice, h->st));
+  if (h->mixed) {
+    float* X = nullptr;
+    rc = run_rows<float>(h, L, false, &X);
+    if (rc) return rc;
+    CK(launch_predict_sq<float>(X, dw, L.M, D, pred, nullptr, nullptr, nullptr, h->st));
+  } else {
+    double* X = nullptr;
+    rc = run_rows<double>(h, L, false, &X);
+    if (rc) return rc;
+    CK(launch_predict_sq<double>(X, dw, L.M, D, pred, nullptr, nullptr, nullptr, h->st));
+  }
+  std::vector<double> hp(L.M);
+  CK(cudaMemcpyAsync(hp.data(), pred, sizeof(double) * L.M, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int s = 0; s < h->S; ++s) {
+    int a0 = h->h_atom_start[s], nat = h->h_atom_start[s + 1] - a0;
+    if (E) E[s] = hp[L.rowE[s]];
+    if (F && L.rowF[s] >= 0)
+      for (int i = 0; i < 3 * nat; ++i) F[3 * (size_t)a0 + i] = hp[L.rowF[s] + i];
+    if (Sout && L.rowS[s] >= 0)
+      for (int k = 0; k < 6; ++k) Sout[6 * s + k] = hp[L.rowS[s] + k];
+  }
+  return MLD_OK;
+}
+
+int mld_gpu_synchronize(mld_gpu_handle* h) {
+  if (!h) return MLD_ERR_INVALID;
+  cudaError_t e = cudaStreamSynchronize(h->st);
+  return e == cudaSuccess ? MLD_OK : cuda_fail(h, e, "cudaStreamSynchronize");
+}
+
+}  // extern "C"

@@ -1,0 +1,369 @@
+// Design-row labels, weighted Gram / right-hand side, ridge solve and predictions.
+//
+//   phi = X^T W X + lambda*I (lambda < 0 -> 0; the intercept column is penalised too),
+//   rhs = X^T W y                        -- MILADY src/mld/parameters.F90:1018-1099
+//   w   = minimum-norm solution of phi w = rhs with singular values <= rcond*s_max dropped
+//         (rcond < 0 -> machine precision), the semantics of LAPACK dgelsd as called by
+//         serial_lsystem_by_svd (src/mld/stats_tools.F90:1153-1213)
+//   predictions  X w                     -- src/mld/mld.F90:40-86,944-1020
+// The symmetric solve uses a parallel cyclic Jacobi eigen-decomposition in one CTA (FP64):
+// for a symmetric positive semi-definite phi its eigenvalues are its singular values.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "mld_internal.h"
+
+namespace mld {
+
+// ------------------------------------------------------------------------------------
+// row labels / weights and the constant column of the energy rows
+// ------------------------------------------------------------------------------------
+template <typename T>
+__global__ void k_rows_prep(int S, const int* __restrict__ atom_start, const long long* __restrict__ rowE,
+                            const long long* __restrict__ rowF, const long long* __restrict__ rowS,
+                            const double* __restrict__ E, const double* __restrict__ F, const double* __restrict__ Sv,
+                            const double* __restrict__ wefs, int D, T* __restrict__ X, double* __restrict__ y,
+                            double* __restrict__ wrow, int* __restrict__ kind) {
+  const int s = blockIdx.x;
+  if (s >= S) return;
+  const int a0 = atom_start[s], nat = atom_start[s + 1] - a0;
+  if (rowE[s] >= 0 && threadIdx.x == 0) {
+    long long r = rowE[s];
+    X[r * D] = (T)nat;
+    y[r] = E[s];
+    wrow[r] = wefs[3 * s];
+    kind[r] = 0;
+  }
+  if (rowF[s] >= 0) {
+    for (int i = threadIdx.x; i < 3 * nat; i += blockDim.x) {
+      long long r = rowF[s] + i;
+      y[r] = F[3 * (size_t)a0 + i];
+      wrow[r] = wefs[3 * s + 1];
+      kind[r] = 1;
+    }
+  }
+  if (rowS[s] >= 0 && threadIdx.x < 6) {
+    long long r = rowS[s] + threadIdx.x;
+    y[r] = Sv[6 * s + threadIdx.x];
+    wrow[r] = wefs[3 * s + 2];
+    kind[r] = 2;
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Gram:  G += X^T diag(w) X over a chunk of rows, 32x32 output tiles, FP64 accumulation.
+// ------------------------------------------------------------------------------------
+constexpr int GT = 32;   // tile edge
+constexpr int GR = 32;   // rows per smem stage
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_gram(const T* __restrict__ X, const double* __restrict__ w, long long M,
+                                              int D, long long rows_per_block, double* __restrict__ G) {
+  const int nt = (D + GT - 1) / GT;
+  // decode upper-triangular tile pair from blockIdx.x
+  int t = blockIdx.x, ti = 0;
+  while (t >= nt - ti) {
+    t -= nt - ti;
+    ++ti;
+  }
+  const int tj = ti + t;
+  const int i0 = ti * GT, j0 = tj * GT;
+  const long long r0 = (long long)blockIdx.y * rows_per_block;
+  const long long r1 = min(M, r0 + rows_per_block);
+  __shared__ double sa[GR][GT + 1];
+  __shared__ double sb[GR][GT + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // 16x16 threads, 2x2 outputs each
+  double acc[2][2] = {{0, 0}, {0, 0}};
+  for (long long rb = r0; rb < r1; rb += GR) {
+    for (int e = threadIdx.x; e < GR * GT; e += 256) {
+      const int rr = e / GT, cc = e % GT;
+      const long long r = rb + rr;
+      double va = 0, vb = 0;
+      if (r < r1) {
+        const double wr = w[r];
+        if (i0 + cc < D) va = (double)X[r * D + i0 + cc] * wr;
+        if (j0 + cc < D) vb = (double)X[r * D + j0 + cc];
+      }
+      sa[rr][cc] = va;
+      sb[rr][cc] = vb;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int rr = 0; rr < GR; ++rr) {
+      const double a0 = sa[rr][ty], a1 = sa[rr][ty + 16];
+      const double b0 = sb[rr][tx], b1 = sb[rr][tx + 16];
+      acc[0][0] = fma(a0, b0, acc[0][0]);
+      acc[0][1] = fma(a0, b1, acc[0][1]);
+      acc[1][0] = fma(a1, b0, acc[1][0]);
+      acc[1][1] = fma(a1, b1, acc[1][1]);
+    }
+    __syncthreads();
+  }
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) {
+      const int i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
+      if (i < D && j < D && (ti != tj || i <= j)) atomicAdd(&G[(size_t)i * D + j], acc[a][b]);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_rhs(const T* __restrict__ X, const double* __restrict__ w,
+                                             const double* __restrict__ y, long long M, int D,
+                                             long long rows_per_block, double* __restrict__ h) {
+  const long long r0 = (long long)blockIdx.x * rows_per_block;
+  const long long r1 = min(M, r0 + rows_per_block);
+  for (int c = threadIdx.x; c < D; c += blockDim.x) {
+    double acc = 0;
+    for (long long r = r0; r < r1; ++r) acc = fma((double)X[r * D + c], w[r] * y[r], acc);
+    atomicAdd(&h[c], acc);
+  }
+}
+
+__global__ void k_symmetrize(double* G, int D) {
+  const int i = blockIdx.x, j = threadIdx.x;
+  for (int jj = j; jj < D; jj += blockDim.x)
+    if (jj < i) G[(size_t)i * D + jj] = G[(size_t)jj * D + i];
+}
+
+template <typename T>
+cudaError_t launch_gram(const T* X, const double* w, const double* y, long long M, int D, double* G, double* h,
+                        cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(G, 0, sizeof(double) * (size_t)D * D, st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(h, 0, sizeof(double) * (size_t)D, st);
+  if (e != cudaSuccess) return e;
+  if (M == 0) return cudaSuccess;
+  const int nt = (D + GT - 1) / GT;
+  const int npairs = nt * (nt + 1) / 2;
+  // enough row chunks to fill the machine (~8 CTAs per SM overall)
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  long long chunks = (long long)nsm * 8 / npairs;
+  if (chunks < 1) chunks = 1;
+  long long rpb = (M + chunks - 1) / chunks;
+  rpb = ((rpb + GR - 1) / GR) * GR;
+  chunks = (M + rpb - 1) / rpb;
+  if (chunks > 65535) {
+    chunks = 65535;
+    rpb = (M + chunks - 1) / chunks;
+  }
+  k_gram<T><<<dim3(npairs, (unsigned)chunks), 256, 0, st>>>(X, w, M, D, rpb, G);
+  long long hch = (long long)nsm * 4;
+  long long hrpb = (M + hch - 1) / hch;
+  hch = (M + hrpb - 1) / hrpb;
+  k_rhs<T><<<(unsigned)hch, 128, 0, st>>>(X, w, y, M, D, hrpb, h);
+  k_symmetrize<<<D, 128, 0, st>>>(G, D);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------
+// Symmetric min-norm solve by parallel cyclic Jacobi (one CTA, D <= kJacobiMax).
+// ------------------------------------------------------------------------------------
+constexpr int kJacobiMax = 112;
+
+__global__ void __launch_bounds__(1024) k_jacobi_solve(const double* __restrict__ Gin, const double* __restrict__ h,
+                                                       int D, double lambda, double rcond, double* __restrict__ wout,
+                                                       double* __restrict__ evals, int* __restrict__ info) {
+  extern __shared__ double sm[];
+  const int n = (D + 1) & ~1;  // even
+  double* A = sm;               // n*n
+  double* V = A + n * n;        // n*n
+  double* cs = V + n * n;       // n/2 * 2
+  int* pp = reinterpret_cast<int*>(cs + n);  // n/2
+  int* qq = pp + n / 2;
+  int* perm = qq + n / 2;       // n
+  double* red = reinterpret_cast<double*>(perm + n);  // 2 doubles + flag
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int e = tid; e < n * n; e += nth) {
+    int i = e / n, j = e % n;
+    double v = 0;
+    if (i < D && j < D) v = Gin[(size_t)i * D + j] + ((i == j && lambda > 0) ? lambda : 0.0);
+    A[e] = v;
+    V[e] = (i == j) ? 1.0 : 0.0;
+  }
+  for (int e = tid; e < n; e += nth) perm[e] = e;
+  __syncthreads();
+  const int npair = n / 2;
+  int sweep = 0;
+  for (; sweep < 40; ++sweep) {
+    // convergence test: off-diagonal Frobenius vs diagonal
+    if (tid == 0) {
+      red[0] = 0;
+      red[1] = 0;
+    }
+    __syncthreads();
+    double off = 0, dia = 0;
+    for (int e = tid; e < n * n; e += nth) {
+      int i = e / n, j = e % n;
+      double v = A[e] * A[e];
+      if (i == j) dia += v;
+      else off += v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      dia += __shfl_xor_sync(0xffffffffu, dia, o);
+    }
+    if ((tid & 31) == 0) {
+      atomicAdd(&red[0], off);
+      atomicAdd(&red[1], dia);
+    }
+    __syncthreads();
+    if (red[0] <= 1e-28 * red[1] || red[1] == 0.0) break;
+    __syncthreads();
+    for (int round = 0; round < n - 1; ++round) {
+      // tournament pairing: perm[0] fixed, the rest rotate
+      if (tid < npair) {
+        int p = perm[tid], q = perm[n - 1 - tid];
+        if (p > q) {
+          int t = p;
+          p = q;
+          q = t;
+        }
+        pp[tid] = p;
+        qq[tid] = q;
+        double apq = A[p * n + q];
+        double c = 1.0, s = 0.0;
+        if (p < D && q < D && apq != 0.0) {
+          double app = A[p * n + p], aqq = A[q * n + q];
+          double tau = (aqq - app) / (2.0 * apq);
+          double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+          c = 1.0 / sqrt(1.0 + t * t);
+          s = t * c;
+        }
+        cs[2 * tid] = c;
+        cs[2 * tid + 1] = s;
+      }
+      __syncthreads();
+      // columns: A <- A J, V <- V J
+      for (int e = tid; e < n * npair; e += nth) {
+        int i = e / npair, k = e % npair;
+        int p = pp[k], q = qq[k];
+        double c = cs[2 * k], s = cs[2 * k + 1];
+        double aip = A[i * n + p], aiq = A[i * n + q];
+        A[i * n + p] = c * aip - s * aiq;
+        A[i * n + q] = s * aip + c * aiq;
+        double vip = V[i * n + p], viq = V[i * n + q];
+        V[i * n + p] = c * vip - s * viq;
+        V[i * n + q] = s * vip + c * viq;
+      }
+      __syncthreads();
+      // rows: A <- J^T A
+      for (int e = tid; e < n * npair; e += nth) {
+        int j = e / npair, k = e % npair;
+        int p = pp[k], q = qq[k];
+        double c = cs[2 * k], s = cs[2 * k + 1];
+        double apj = A[p * n + j], aqj = A[q * n + j];
+        A[p * n + j] = c * apj - s * aqj;
+        A[q * n + j] = s * apj + c * aqj;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        int last = perm[n - 1];
+        for (int k = n - 1; k > 1; --k) perm[k] = perm[k - 1];
+        perm[1] = last;
+      }
+      __syncthreads();
+    }
+  }
+  // min-norm solution: w = sum_{|lambda_i| > thr} (v_i . h / lambda_i) v_i
+  __syncthreads();
+  if (tid == 0) {
+    double mx = 0;
+    for (int i = 0; i < D; ++i) mx = fmax(mx, fabs(A[i * n + i]));
+    red[0] = mx;
+    int rank = 0;
+    double thr = (rcond < 0 ? 1.1102230246251565e-16 : rcond) * mx;
+    for (int i = 0; i < D; ++i) rank += fabs(A[i * n + i]) > thr;
+    info[0] = sweep;
+    info[1] = rank;
+  }
+  __syncthreads();
+  const double thr = (rcond < 0 ? 1.1102230246251565e-16 : rcond) * red[0];
+  double* coef = cs;  // reuse (n entries)
+  for (int i = tid; i < D; i += nth) {
+    double lam = A[i * n + i];
+    double d = 0;
+    for (int r = 0; r < D; ++r) d = fma(V[r * n + i], h[r], d);
+    if (evals) evals[i] = lam;
+    coef[i] = (fabs(lam) > thr) ? d / lam : 0.0;
+  }
+  __syncthreads();
+  for (int r = tid; r < D; r += nth) {
+    double acc = 0;
+    for (int i = 0; i < D; ++i) acc = fma(V[r * n + i], coef[i], acc);
+    wout[r] = acc;
+  }
+}
+
+cudaError_t launch_solve_sym(double* G, const double* h, int D, double lambda, double rcond, double* wout,
+                             double* evals, int* info, cudaStream_t st) {
+  if (D > kJacobiMax) return cudaErrorInvalidValue;
+  const int n = (D + 1) & ~1;
+  size_t smem = sizeof(double) * (2 * (size_t)n * n + n) + sizeof(int) * (2 * n) + 4 * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(k_jacobi_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_jacobi_solve<<<1, 1024, smem, st>>>(G, h, D, lambda, rcond, wout, evals, info);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------
+// predictions and squared-error sums per row kind (0 energy, 1 force, 2 stress)
+// ------------------------------------------------------------------------------------
+template <typename T>
+__global__ void k_predict(const T* __restrict__ X, const double* __restrict__ w, long long M, int D,
+                          double* __restrict__ pred, const double* __restrict__ y, const int* __restrict__ kind,
+                          double* __restrict__ sq /*3 sums + 3 counts*/) {
+  const int lane = threadIdx.x & 31;
+  const long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= M) return;
+  double acc = 0;
+  for (int c = lane; c < D; c += 32) acc = fma((double)X[r * D + c], w[c], acc);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) {
+    if (pred) pred[r] = acc;
+    if (sq) {
+      double d = acc - y[r];
+      int k = kind[r];
+      atomicAdd(&sq[k], d * d);
+      atomicAdd(&sq[3 + k], 1.0);
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_predict_sq(const T* X, const double* w, long long M, int D, double* pred, const double* y,
+                              const int* kind, double* sq, cudaStream_t st) {
+  if (M == 0) return cudaSuccess;
+  long long threads = M * 32;
+  unsigned blocks = (unsigned)((threads + 255) / 256);
+  k_predict<T><<<blocks, 256, 0, st>>>(X, w, M, D, pred, y, kind, sq);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_rows_prep(int S, const int* atom_start, const DevRows& rows, const double* E, const double* F,
+                             const double* Sv, const double* wefs, T* X, double* y, double* wrow, int* kind,
+                             cudaStream_t st) {
+  if (S == 0) return cudaSuccess;
+  k_rows_prep<T><<<S, 128, 0, st>>>(S, atom_start, rows.rowE, rows.rowF, rows.rowS, E, F, Sv, wefs, rows.D, X, y,
+                                    wrow, kind);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_gram<double>(const double*, const double*, const double*, long long, int, double*,
+                                         double*, cudaStream_t);
+template cudaError_t launch_gram<float>(const float*, const double*, const double*, long long, int, double*, double*,
+                                        cudaStream_t);
+template cudaError_t launch_predict_sq<double>(const double*, const double*, long long, int, double*, const double*,
+                                               const int*, double*, cudaStream_t);
+template cudaError_t launch_predict_sq<float>(const float*, const double*, long long, int, double*, const double*,
+                                              const int*, double*, cudaStream_t);
+template cudaError_t launch_rows_prep<double>(int, const int*, const DevRows&, const double*, const double*,
+                                              const double*, const double*, double*, double*, double*, int*,
+                                              cudaStream_t);
+template cudaError_t launch_rows_prep<float>(int, const int*, const DevRows&, const double*, const double*,
+                                             const double*, const double*, float*, double*, double*, int*,
+                                             cudaStream_t);
+
+}  // namespace mld

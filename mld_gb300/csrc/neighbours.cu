@@ -1,0 +1,167 @@
+// Neighbour lists within r < r_cut for a batch of periodic structures (one warp per atom).
+//
+// Small box (some perpendicular cell width below 2*r_cut): every atom j and periodic image
+// n in [-nsize, nsize]^3 is a candidate, u = x_j + n.cell - x_i, kept when 1e-15 <= |u|^2 and
+// |u| < r_cut -- MILADY src/mld/neighbours.F90:1147-1328 followed by the strict filter of
+// build_local_neighbours_ja (:330).  Large box: minimum image through the fractional
+// coordinates, wrapping components with |ds| > 0.5 by nint (neighbours.F90:315-324).
+// Candidates are scanned in (j, n1, n2, n3) order and compacted with a warp ballot, so the
+// neighbour order (and hence every floating-point sum over neighbours) is deterministic.
+#include <cuda_runtime.h>
+
+#include "mld_internal.h"
+
+namespace mld {
+
+__global__ void k_neighbours(int A, const int* __restrict__ atom_struct, const int* __restrict__ atom_start,
+                             const double* __restrict__ pos, const double* __restrict__ cell,
+                             const double* __restrict__ recip, const int* __restrict__ small,
+                             const int* __restrict__ nsize, double rcut, int pass, int* __restrict__ counts, int* __restrict__ maxcount,
+                             const int* __restrict__ offsets, int* __restrict__ nbr_idx, double* __restrict__ nbr_u) {
+  const int lane = threadIdx.x & 31;
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (g >= A) return;
+  const int s = atom_struct[g];
+  const int a0 = atom_start[s], nat = atom_start[s + 1] - a0;
+  const double* cl = cell + 9 * (size_t)s;
+  const double* bg = recip + 9 * (size_t)s;
+  const double xi0 = pos[3 * (size_t)g], xi1 = pos[3 * (size_t)g + 1], xi2 = pos[3 * (size_t)g + 2];
+  const double rc2 = rcut * rcut;
+  const int sm = small[s];
+  int n1s = 0, n2s = 0, n3s = 0, nimg = 1;
+  if (sm) {
+    n1s = nsize[3 * s];
+    n2s = nsize[3 * s + 1];
+    n3s = nsize[3 * s + 2];
+    nimg = (2 * n1s + 1) * (2 * n2s + 1) * (2 * n3s + 1);
+  }
+  const long long ncand = (long long)nat * nimg;
+  int count = 0;
+  const int wbase = (pass == 1) ? offsets[g] : 0;
+  for (long long base = 0; base < ncand; base += 32) {
+    const long long cidx = base + lane;
+    bool ok = false;
+    double u0 = 0, u1 = 0, u2 = 0;
+    int jj = 0;
+    if (cidx < ncand) {
+      if (sm) {
+        jj = (int)(cidx / nimg);
+        int im = (int)(cidx - (long long)jj * nimg);
+        int n3 = im % (2 * n3s + 1) - n3s;
+        im /= (2 * n3s + 1);
+        int n2 = im % (2 * n2s + 1) - n2s;
+        int n1 = im / (2 * n2s + 1) - n1s;
+        const double* xj = pos + 3 * (size_t)(a0 + jj);
+        double t0 = xi0 - (xj[0] + cl[0] * n1 + cl[3] * n2 + cl[6] * n3);
+        double t1 = xi1 - (xj[1] + cl[1] * n1 + cl[4] * n2 + cl[7] * n3);
+        double t2 = xi2 - (xj[2] + cl[2] * n1 + cl[5] * n2 + cl[8] * n3);
+        double r2 = t0 * t0 + t1 * t1 + t2 * t2;
+        ok = (r2 >= 1e-15) && (r2 <= rc2) && (sqrt(r2) < rcut);
+        u0 = -t0;
+        u1 = -t1;
+        u2 = -t2;
+      } else {
+        jj = (int)cidx;
+        if (a0 + jj != g) {
+          const double* xj = pos + 3 * (size_t)(a0 + jj);
+          double d0 = xj[0] - xi0, d1 = xj[1] - xi1, d2 = xj[2] - xi2;
+          double ds[3];
+          for (int k = 0; k < 3; ++k) {
+            double v = d0 * bg[3 * k] + d1 * bg[3 * k + 1] + d2 * bg[3 * k + 2];
+            if (v > 0.5 || v < -0.5) v -= round(v);
+            ds[k] = v;
+          }
+          u0 = cl[0] * ds[0] + cl[3] * ds[1] + cl[6] * ds[2];
+          u1 = cl[1] * ds[0] + cl[4] * ds[1] + cl[7] * ds[2];
+          u2 = cl[2] * ds[0] + cl[5] * ds[1] + cl[8] * ds[2];
+          ok = sqrt(u0 * u0 + u1 * u1 + u2 * u2) < rcut;
+        }
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    if (pass == 1 && ok) {
+      const int slot = wbase + count + __popc(m & ((1u << lane) - 1u));
+      nbr_idx[slot] = a0 + jj;
+      nbr_u[3 * (size_t)slot] = u0;
+      nbr_u[3 * (size_t)slot + 1] = u1;
+      nbr_u[3 * (size_t)slot + 2] = u2;
+    }
+    count += __popc(m);
+  }
+  if (pass == 0 && lane == 0) {
+    counts[g] = count;
+    atomicMax(maxcount, count);
+  }
+}
+
+// Three-phase exclusive scan of n ints: out[0..n], out[n] = total.
+constexpr int kScanBlock = 1024;
+
+__global__ void k_scan_blocks(const int* __restrict__ in, int* __restrict__ out, int n, int* __restrict__ bsum) {
+  __shared__ int sh[kScanBlock];
+  const int i = blockIdx.x * kScanBlock + threadIdx.x;
+  int v = (i < n) ? in[i] : 0;
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = 1; o < kScanBlock; o <<= 1) {
+    int t = (threadIdx.x >= o) ? sh[threadIdx.x - o] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += t;
+    __syncthreads();
+  }
+  if (i < n) out[i] = sh[threadIdx.x] - v;  // exclusive
+  if (threadIdx.x == kScanBlock - 1) bsum[blockIdx.x] = sh[threadIdx.x];
+}
+
+__global__ void k_scan_sums(int* __restrict__ bsum, int nb, int* __restrict__ total_out) {
+  // single block: sequential chunks of kScanBlock
+  __shared__ int sh[kScanBlock];
+  int carry = 0;
+  for (int base = 0; base < nb; base += kScanBlock) {
+    const int i = base + threadIdx.x;
+    int v = (i < nb) ? bsum[i] : 0;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < kScanBlock; o <<= 1) {
+      int t = (threadIdx.x >= o) ? sh[threadIdx.x - o] : 0;
+      __syncthreads();
+      sh[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < nb) bsum[i] = carry + sh[threadIdx.x] - v;
+    const int tot = sh[kScanBlock - 1];
+    __syncthreads();
+    carry += tot;
+  }
+  if (threadIdx.x == 0) *total_out = carry;
+}
+
+__global__ void k_scan_add(int* __restrict__ out, int n, const int* __restrict__ bsum, const int* total) {
+  const int i = blockIdx.x * kScanBlock + threadIdx.x;
+  if (i < n) out[i] += bsum[blockIdx.x];
+  if (i == 0) out[n] = *total;
+}
+
+cudaError_t launch_scan(const int* in, int* out, int n, int* d_tmp, cudaStream_t st) {
+  // d_tmp must hold ceil(n/1024) + 1 ints
+  if (n <= 0) {
+    return cudaMemsetAsync(out, 0, sizeof(int), st);
+  }
+  const int nb = (n + kScanBlock - 1) / kScanBlock;
+  k_scan_blocks<<<nb, kScanBlock, 0, st>>>(in, out, n, d_tmp);
+  k_scan_sums<<<1, kScanBlock, 0, st>>>(d_tmp, nb, d_tmp + nb);
+  k_scan_add<<<nb, kScanBlock, 0, st>>>(out, n, d_tmp, d_tmp + nb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_neighbours(const DevBatch& b, double rcut, int* counts, int* maxcount, cudaStream_t st, int pass) {
+  if (b.A == 0) return cudaSuccess;
+  const int threads = 256;
+  const long long warps = b.A;
+  const int blocks = (int)((warps * 32 + threads - 1) / threads);
+  k_neighbours<<<blocks, threads, 0, st>>>(b.A, b.atom_struct, b.atom_start, b.pos, b.cell, b.recip, b.small,
+                                           b.nsize, rcut, pass, counts, maxcount, b.nbr_off, b.nbr_idx, b.nbr_u);
+  return cudaGetLastError();
+}
+
+}  // namespace mld

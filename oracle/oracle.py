@@ -1,0 +1,162 @@
+"""Python front-end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads ``oracle/liboracle.so`` (built from bso4_oracle.c by oracle/Makefile) and restates the
+fit step of MILADY in NumPy/SciPy:
+
+* weighted normal matrix  phi = A W A^T + lambda*I (lambda<0 -> 0), rhs = A W y, solved with
+  LAPACK ``gelsd`` (SVD, minimum norm, rcond) -- MILADY src/mld/parameters.F90:1018-1099 and
+  src/mld/stats_tools.F90:1153-1213 (``serial_lsystem_by_svd``);
+* predictions w . row and RMSE -- src/mld/mld.F90:40-86,944-1020, src/mld/stats_tools.F90:1551-1559.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import Dict, Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB: Optional[ctypes.CDLL] = None
+_STATE = {"j_max": None, "inv_r0": None, "K": 0}
+
+DEFAULT_INV_R0_INPUT = 1.0 - 0.02 / np.pi   # read_ml_file.F90:425
+
+
+def build() -> str:
+    path = os.path.join(_HERE, "liboracle.so")
+    src = os.path.join(_HERE, "bso4_oracle.c")
+    if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+        subprocess.check_call(["make", "-s", "-C", _HERE])
+    return path
+
+
+def lib() -> ctypes.CDLL:
+    global _LIB
+    if _LIB is None:
+        _LIB = ctypes.CDLL(build())
+        d, i, p = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+        _LIB.orc_init.argtypes = [d, d]
+        _LIB.orc_init.restype = i
+        _LIB.orc_num_u.restype = i
+        _LIB.orc_num_cg.argtypes = [i]
+        _LIB.orc_num_cg.restype = ctypes.c_long
+        _LIB.orc_triples.argtypes = [p, p, p]
+        _LIB.orc_cg_value.argtypes = [i] * 6
+        _LIB.orc_cg_value.restype = d
+        _LIB.orc_volume.argtypes = [p]
+        _LIB.orc_volume.restype = d
+        _LIB.orc_small_box.argtypes = [p, d, p]
+        _LIB.orc_neighbours.argtypes = [i, p, p, d, i, p, p, p, p]
+        _LIB.orc_bispectrum.argtypes = [i, p, i, i, p, p, d, d, p, p, p, i, p, p]
+        _LIB.orc_rows_linear.argtypes = [i, i, p, p, p, p, p, i, i, d, d, d, p, p, p]
+    return _LIB
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def init(j_max: float = 4.0, inv_r0_input: float = DEFAULT_INV_R0_INPUT) -> int:
+    L = lib()
+    if _STATE["j_max"] != j_max or _STATE["inv_r0"] != inv_r0_input:
+        K = L.orc_init(float(j_max), float(inv_r0_input))
+        if K < 0:
+            raise ValueError(f"orc_init failed ({K})")
+        _STATE.update(j_max=j_max, inv_r0=inv_r0_input, K=K)
+    return _STATE["K"]
+
+
+def triples() -> np.ndarray:
+    K = _STATE["K"]
+    a = np.zeros((3, K), dtype=np.int32)
+    lib().orc_triples(_ptr(a[0]), _ptr(a[1]), _ptr(a[2]))
+    return a.T.copy()
+
+
+def cg(j1, m1, j2, m2, j, m) -> float:
+    return lib().orc_cg_value(j1, m1, j2, m2, j, m)
+
+
+def neighbours(positions: np.ndarray, cell: np.ndarray, r_cut: float, cap: int = 300):
+    pos = np.ascontiguousarray(positions, dtype=np.float64)
+    cel = np.ascontiguousarray(cell, dtype=np.float64)
+    nat = pos.shape[0]
+    nn = np.zeros(nat, dtype=np.int32)
+    nbr = np.zeros((nat, cap), dtype=np.int32)
+    u = np.zeros((nat, cap, 3), dtype=np.float64)
+    small = ctypes.c_int(0)
+    rc = lib().orc_neighbours(nat, _ptr(pos), _ptr(cel), float(r_cut), cap, _ptr(nn), _ptr(nbr), _ptr(u),
+                              ctypes.byref(small))
+    if rc != 0:
+        raise OverflowError("neighbour cap exceeded")
+    return nn, nbr, u, bool(small.value)
+
+
+def bispectrum(positions, cell, types, r_cut: float, j_max: float = 4.0, *,
+               channel_weights: Optional[np.ndarray] = None, want_deriv: bool = True,
+               inv_r0_input: float = DEFAULT_INV_R0_INPUT, cap: int = 300,
+               r_in_pair: Optional[np.ndarray] = None, r_in_width: float = 0.4) -> Dict[str, np.ndarray]:
+    """Per-atom B (nat, nch*K) and, if asked, dB (nat, cap, 3, nch*K) plus the neighbour list."""
+    K = init(j_max, inv_r0_input)
+    types = np.ascontiguousarray(types, dtype=np.int32)
+    ntypes = int(types.max()) + 1 if types.size else 1
+    if channel_weights is None:
+        channel_weights = np.ones((1, ntypes))
+    chw = np.ascontiguousarray(channel_weights, dtype=np.float64)
+    nch, ntypes = chw.shape
+    nn, nbr, u, small = neighbours(positions, cell, r_cut, cap)
+    nat = types.shape[0]
+    B = np.zeros((nat, nch * K))
+    dB = np.zeros((nat, cap, 3, nch * K)) if want_deriv else None
+    rin = None if r_in_pair is None else np.ascontiguousarray(r_in_pair, dtype=np.float64)
+    lib().orc_bispectrum(nat, _ptr(types), ntypes, nch, _ptr(chw), _ptr(rin), float(r_in_width), float(r_cut),
+                         _ptr(nn), _ptr(nbr), _ptr(u), cap, _ptr(B), _ptr(dB))
+    return dict(B=B, dB=dB, nn=nn, nbr=nbr, u=u, small=small, cap=cap)
+
+
+def linear_rows(desc: Dict[str, np.ndarray], cell: np.ndarray, *, sign_stress: float = 1.0,
+                sign_big: float = 1.0):
+    B, dB = desc["B"], desc["dB"]
+    nat, KK = B.shape
+    D = 1 + KK
+    rowE = np.zeros(D)
+    rowF = np.zeros((3 * nat, D))
+    rowS = np.zeros((6, D))
+    vol = lib().orc_volume(_ptr(np.ascontiguousarray(cell, dtype=np.float64)))
+    lib().orc_rows_linear(nat, KK, _ptr(B), _ptr(dB), _ptr(desc["nn"]), _ptr(desc["nbr"]), _ptr(desc["u"]),
+                          desc["cap"], int(desc["small"]), float(sign_stress), float(sign_big), float(vol),
+                          _ptr(rowE), _ptr(rowF), _ptr(rowS))
+    return rowE, rowF, rowS
+
+
+def solve_gelsd(phi: np.ndarray, rhs: np.ndarray, rcond: float = -1.0) -> np.ndarray:
+    """dgelsd on the (D x D) normal matrix, as serial_lsystem_by_svd does."""
+    import scipy.linalg
+    if rcond is None or rcond < 0:
+        rcond = np.finfo(np.float64).eps
+    w, *_ = scipy.linalg.lstsq(phi, rhs, cond=rcond, lapack_driver="gelsd")
+    return w
+
+
+def normal_equations(A: np.ndarray, y: np.ndarray, wts: np.ndarray, lam: float):
+    """phi = A^T W A + lambda I (lambda<0 -> 0), rhs = A^T W y  (A is rows x D)."""
+    lam = 0.0 if lam < 0 else lam
+    AW = A * wts[:, None]
+    phi = A.T @ AW
+    phi[np.diag_indices_from(phi)] += lam
+    rhs = AW.T @ y
+    return phi, rhs
+
+
+def fit_linear(A: np.ndarray, y: np.ndarray, wts: np.ndarray, lam: float, rcond: float = -1.0) -> np.ndarray:
+    phi, rhs = normal_equations(A, y, wts, lam)
+    return solve_gelsd(phi, rhs, rcond)
+
+
+def rmse(pred: np.ndarray, ref: np.ndarray) -> float:
+    d = np.asarray(pred) - np.asarray(ref)
+    return float(np.sqrt(np.mean(d * d))) if d.size else 0.0

@@ -1,0 +1,191 @@
+"""Parity of the CUDA path (through the C ABI) against the oracle and MILADY's golden vectors.
+
+Tolerances: plain FP64 method <= 1e-10 relative to the largest magnitude of each compared array
+(the reference's own bar for the FP64 path); mixed method (FP32 descriptors) <= 2e-5.
+"""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-10
+TOL32 = 2e-5
+
+
+def _rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def _handle(j_max=4.0, r_cut=4.7, precision=0, lam=-1.0, n_el=1, weights=None):
+    from mld_gb300 import _lib
+    c = _lib.default_config()
+    c.j_max = j_max
+    c.r_cut = r_cut
+    c.n_elements = n_el
+    c.lambda_krr = lam
+    c.precision = precision
+    c.desc_forces = 1
+    if weights is not None:
+        c.weighted = 1
+        for i, w in enumerate(weights):
+            c.weight_per_element[i] = w
+    return _lib.Handle(c)
+
+
+def _fit17_batch(fit17, idx=None):
+    idx = range(len(fit17["names"])) if idx is None else idx
+    nat = [fit17[f"pos_{i}"].shape[0] for i in idx]
+    pos = np.concatenate([fit17[f"pos_{i}"] for i in idx])
+    cell = np.stack([fit17[f"cell_{i}"] for i in idx])
+    types = np.concatenate([fit17[f"types_{i}"] for i in idx])
+    return nat, pos, cell, types
+
+
+@pytest.mark.parametrize("precision,tol", [(0, TOL64), (1, TOL32)])
+def test_fit17_descriptors(lib, fit17, precision, tol):
+    nat, pos, cell, types = _fit17_batch(fit17)
+    h = _handle(precision=precision)
+    h.set_structures(nat, pos, cell, types)
+    B, nn = h.descriptors()
+    ref = np.concatenate([fit17[f"B_{i}"] for i in range(len(nat))])
+    assert B.shape == ref.shape
+    assert _rel(B, ref) < tol
+    h.close()
+
+
+def _small_dataset(seed=5):
+    from mld_gb300 import synth
+    rng = np.random.default_rng(seed)
+    ds = synth.fe_bcc_batched(n_struct=6, nmin=16, nmax=300, seed=seed)
+    return ds
+
+
+def _oracle_rows(ds, j_max=4.0):
+    rowsA, ys, ws = [], [], []
+    for s in ds.structures:
+        d = oracle.bispectrum(s.positions, s.cell, s.types, ds.rcut, j_max)
+        e, f, st = oracle.linear_rows(d, s.cell)
+        rowsA += [e[None, :], f, st]
+        ys += [np.array([s.energies[1]]), s.forces.reshape(-1), s.stress]
+        ws += [np.ones(1), np.ones(3 * s.nat), np.ones(6)]
+    return np.concatenate(rowsA), np.concatenate(ys), np.concatenate(ws)
+
+
+def _stage(h, ds):
+    nat, pos, cell, types = ds.arrays()
+    h.set_structures(nat, pos, cell, types)
+    E, F, S, has = ds.labels()
+    h.set_labels(E, F, S, has, np.ones((len(nat), 3)))
+
+
+@pytest.mark.parametrize("precision,tol", [(0, TOL64), (1, TOL32)])
+def test_descriptor_derivatives(lib, precision, tol):
+    ds = _small_dataset()
+    h = _handle(precision=precision)
+    nat, pos, cell, types = ds.arrays()
+    h.set_structures(nat, pos, cell, types)
+    B, nn = h.descriptors()
+    nbr, u, dB = h.descriptor_derivatives(int(nn.sum()) + 8)
+    p = 0
+    a0 = 0
+    for s in ds.structures:
+        d = oracle.bispectrum(s.positions, s.cell, s.types, ds.rcut, 4.0)
+        for i in range(s.nat):
+            n = d["nn"][i]
+            assert nn[a0 + i] == n
+            assert np.array_equal(nbr[p:p + n] - a0, d["nbr"][i, :n])
+            assert np.allclose(u[p:p + n], d["u"][i, :n], rtol=0, atol=1e-12)
+            got = dB[p:p + n]
+            want = d["dB"][i, :n]
+            assert _rel(got, want) < tol * 10
+            p += n
+        assert _rel(B[a0:a0 + s.nat], d["B"]) < tol
+        a0 += s.nat
+    h.close()
+
+
+@pytest.mark.parametrize("precision,tol", [(0, TOL64), (1, TOL32)])
+def test_design_rows(lib, precision, tol):
+    ds = _small_dataset()
+    A_ref, y_ref, w_ref = _oracle_rows(ds)
+    h = _handle(precision=precision)
+    _stage(h, ds)
+    A, y, w = h.design_matrix()
+    assert A.shape == A_ref.shape
+    assert np.array_equal(y, y_ref) and np.array_equal(w, w_ref)
+    for lo, hi, name in [(0, 1, "E")]:
+        assert _rel(A[lo:hi], A_ref[lo:hi]) < tol, name
+    assert _rel(A, A_ref) < tol * 10
+    # stress rows of every structure
+    h.close()
+
+
+def test_gram_and_solve_plain(lib):
+    ds = _small_dataset()
+    A_ref, y_ref, w_ref = _oracle_rows(ds)
+    h = _handle(lam=1e-8)
+    _stage(h, ds)
+    G, rhs = h.gram()
+    G_ref = A_ref.T @ (A_ref * w_ref[:, None])
+    rhs_ref = A_ref.T @ (w_ref * y_ref)
+    assert _rel(G, G_ref) < TOL64
+    assert _rel(rhs, rhs_ref) < TOL64
+    w, rank = h.solve(G_ref, rhs_ref)
+    phi = G_ref + 1e-8 * np.eye(G_ref.shape[0])
+    w_ref_fit = oracle.solve_gelsd(phi, rhs_ref)
+    pred, pred_ref = A_ref @ w, A_ref @ w_ref_fit
+    assert _rel(pred, pred_ref) < 1e-6
+    h.close()
+
+
+def test_fit_end_to_end_plain(lib):
+    ds = _small_dataset()
+    A_ref, y_ref, w_ref = _oracle_rows(ds)
+    h = _handle(lam=1e-8)
+    _stage(h, ds)
+    w, rmse = h.fit()
+    w_or = oracle.fit_linear(A_ref, y_ref, w_ref, 1e-8)
+    p, p_or = A_ref @ w, A_ref @ w_or
+    assert _rel(p, p_or) < 1e-6
+    kinds = np.concatenate([[0] + [1] * (3 * s.nat) + [2] * 6 for s in ds.structures])
+    for k in range(3):
+        r_or = oracle.rmse(p_or[kinds == k], y_ref[kinds == k])
+        assert abs(rmse[k] - r_or) <= 1e-6 * max(r_or, 1e-12)
+    # predictions through the serving entry point
+    E, F, S = h.predict(w)
+    rows_E = np.cumsum([0] + [1 + 3 * s.nat + 6 for s in ds.structures])[:-1]
+    assert _rel(E, (A_ref @ w)[rows_E]) < 1e-10
+    h.close()
+
+
+def test_fit_mixed_close_to_plain(lib):
+    ds = _small_dataset()
+    h64 = _handle(lam=1e-8)
+    _stage(h64, ds)
+    w64, r64 = h64.fit()
+    h32 = _handle(lam=1e-8, precision=1)
+    _stage(h32, ds)
+    w32, r32 = h32.fit()
+    # force RMSE of the mixed fit within 1% of the FP64 fit
+    assert abs(r32[1] - r64[1]) <= 0.01 * r64[1]
+    h64.close()
+    h32.close()
+
+
+def test_neighbour_cap_is_reported(lib):
+    from mld_gb300 import _lib
+    ds = _small_dataset()
+    c = _lib.default_config()
+    c.j_max, c.r_cut, c.imm_neigh = 4.0, 4.7, 10
+    h = _lib.Handle(c)
+    nat, pos, cell, types = ds.arrays()
+    h.set_structures(nat, pos, cell, types)
+    with pytest.raises(_lib.MldError) as ei:
+        h.descriptors()
+    assert ei.value.code == 3
+    # the handle stays usable after the error
+    c2 = _lib.default_config()
+    h.close()

@@ -1,0 +1,85 @@
+"""CPU tests of the oracle: pinned against MILADY's own golden descriptors (fit17) and checked
+for internal consistency (derivatives vs finite differences, CG identities)."""
+import numpy as np
+import pytest
+
+import oracle
+
+
+def test_dimensions_jmax4():
+    K = oracle.init(4.0)
+    assert K == 55                                   # 55 B components (fit17 .eml: 56 columns)
+    L = oracle.lib()
+    assert L.orc_num_u() == 285                      # sum_{j<=8} (j+1)^2
+    assert [L.orc_num_cg(i) for i in range(3)] == [34946, 34946, 34946]
+
+
+def test_cg_orthonormality():
+    oracle.init(4.0)
+    # sum_{m1,m2} <j1 m1 j2 m2|j m><j1 m1 j2 m2|j' m'> = delta_jj' delta_mm'  (doubled indices)
+    for j1, j2 in [(2, 2), (3, 1), (4, 2), (3, 3)]:
+        for j in range(abs(j1 - j2), j1 + j2 + 1, 2):
+            for jp in range(abs(j1 - j2), j1 + j2 + 1, 2):
+                for m in range(-min(j, jp), min(j, jp) + 1, 2):
+                    s = sum(oracle.cg(j1, m1, j2, m - m1, j, m) * oracle.cg(j1, m1, j2, m - m1, jp, m)
+                            for m1 in range(-j1, j1 + 1, 2) if abs(m - m1) <= j2)
+                    assert abs(s - (1.0 if j == jp else 0.0)) < 1e-12
+
+
+def test_fit17_golden_descriptors(fit17):
+    """The oracle reproduces REF/descDB/*.eml of MILADY's fit17 test (small and large boxes)."""
+    worst = 0.0
+    kinds = set()
+    for i, name in enumerate(fit17["names"]):
+        d = oracle.bispectrum(fit17[f"pos_{i}"], fit17[f"cell_{i}"], fit17[f"types_{i}"], 4.7, 4.0,
+                              want_deriv=False)
+        ref = fit17[f"B_{i}"]
+        kinds.add(d["small"])
+        worst = max(worst, np.abs(d["B"] - ref).max() / np.abs(ref).max())
+    assert kinds == {True, False}
+    assert worst < 1e-13
+
+
+def _energy_row_sum(pos, cell, types):
+    return oracle.bispectrum(pos, cell, types, 4.7, 4.0, want_deriv=False)["B"].sum(0)
+
+
+@pytest.mark.parametrize("idx", [2, 9])
+def test_force_rows_are_negative_gradient(fit17, idx):
+    pos = fit17[f"pos_{idx}"].copy()
+    cell, types = fit17[f"cell_{idx}"], fit17[f"types_{idx}"]
+    d = oracle.bispectrum(pos, cell, types, 4.7, 4.0)
+    _, rowF, _ = oracle.linear_rows(d, cell)
+    h = 1e-5
+    for a in (0, 1):
+        for c in range(3):
+            p1 = pos.copy(); p1[a, c] += h
+            p2 = pos.copy(); p2[a, c] -= h
+            fd = -(_energy_row_sum(p1, cell, types) - _energy_row_sum(p2, cell, types)) / (2 * h)
+            an = rowF[3 * a + c, 1:]
+            assert np.abs(fd - an).max() <= 1e-6 * np.abs(an).max() + 1e-9
+
+
+def test_weighted_channels_scale():
+    """A weighted channel with all element weights 1 equals the plain channel."""
+    from mld_gb300 import synth
+    pos, cell = synth.bcc(2, 2, 2, 3.2)
+    rng = np.random.default_rng(3)
+    pos = pos + rng.normal(0, 0.05, pos.shape)
+    types = np.array([0, 1] * 8, np.int32)
+    chw = np.array([[1.0, 1.0], [1.0, 1.0]])
+    d = oracle.bispectrum(pos, cell, types, 5.0, 4.0, channel_weights=chw)
+    assert np.allclose(d["B"][:, :55], d["B"][:, 55:], rtol=0, atol=1e-12)
+    chw2 = np.array([[1.0, 1.0], [0.5, 2.0]])
+    d2 = oracle.bispectrum(pos, cell, types, 5.0, 4.0, channel_weights=chw2)
+    assert np.allclose(d2["B"][:, :55], d["B"][:, :55])
+    assert not np.allclose(d2["B"][:, 55:], d["B"][:, 55:])
+
+
+def test_gelsd_min_norm_on_rank_deficient():
+    rng = np.random.default_rng(0)
+    A = rng.normal(size=(50, 6))
+    A[:, 5] = A[:, 4]                     # duplicate column -> rank 5
+    y = rng.normal(size=50)
+    w = oracle.fit_linear(A, y, np.ones(50), -1.0)
+    assert abs(w[4] - w[5]) < 1e-10       # minimum norm splits the duplicate evenly
