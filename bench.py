@@ -1,0 +1,351 @@
+"""Benchmark of the batched bispectrum-SO(4) linear fit (MILADY descriptor-to-fit path).
+
+Workload: 2,000 bcc Fe structures, atom counts log-uniform in 16..1024, supercells trimmed to size
+with 0-3 extra vacancies, sigma = 0.08 A noise, +-2 % strain, Morse labels; bispectrum j_max = 4
+(55 components), r_cut = 4.7 A, linear model (1 + 55 columns), energy + 3N force + 6 stress
+rows per structure, ridge lambda = 1e-8, min-norm solve.  Seeded synthetic data (no dataset).
+
+One step = one full fit of the whole set on the GPU: neighbour lists, fused descriptor +
+design-row kernel, weighted Gram, ridge solve, train predictions/RMSE.
+
+  value   design rows / s of the mixed method (FP32 descriptors and rows, FP64 Gram and solve),
+          inputs resident in HBM, device time from CUDA events on the library's stream;
+  e2e     the same through the C ABI with host buffers: each step stages positions, cells, types
+          and labels from pinned host memory and reads back the coefficients and RMSE;
+  plain   the all-FP64 method on the same data (the baseline named by the metric);
+  roofline  for the dominant kernel (fused descriptor kernel) against the measured FMA peak of
+          the pipe it runs on.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_STRUCT = 2000
+RCUT = 4.7
+J_MAX = 4.0
+LAMBDA = 1e-8
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--structures", type=int, default=N_STRUCT)
+    p.add_argument("--plain-steps", type=int, default=2)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return rank, world
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                      "-i", os.environ.get("LOCAL_RANK", "0")],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_dataset(n_struct):
+    from mld_gb300 import synth
+    return synth.fe_bcc_batched(n_struct=n_struct, rcut=RCUT, workers=min(16, os.cpu_count() or 1))
+
+
+def flops_model(wc, n_pairs, n_atoms):
+    """Algorithmic FLOPs of one launch of the fused descriptor kernel (per atom and per pair).
+
+    Per neighbour pair: U recursion (8 flops for a one-term entry, 18 for a two-term entry),
+    f_c*w*U accumulation (4 per entry per channel), U+dU recursion (U as above plus 54 per source
+    term), vecall (12 per entry), dB contraction (3 components x 4 flops per merged Y slot per
+    channel) and the row scatter (3*K adds per channel).  Per atom: the Z contraction (8 flops per
+    CG term + 2 per row extent + 4 per output for the scale) and B (4 flops per ZA slot), per
+    channel."""
+    nch, NU, one, two = wc["nch"], wc["NU"], wc["u_one_term"], wc["u_two_term"]
+    u_flops = 8 * one + 18 * two
+    per_pair = (u_flops + 4 * NU * nch) + (u_flops + 54 * (one + 2 * two) + 12 * NU) + \
+        nch * (12 * wc["y_slots"] + 3 * wc["K"])
+    per_atom = nch * (8 * wc["cg_terms"] + 2 * wc["z_row_extents"] + 4 * wc["z_outputs"] + 4 * wc["y_slots_za"])
+    return per_pair * n_pairs + per_atom * n_atoms, per_pair, per_atom
+
+
+def run_ours(a, rank, world):
+    from mld_gb300 import _lib
+    ds = make_dataset(a.structures)
+    nat, pos, cell, types = ds.arrays()
+    E, F, S, has = ds.labels()
+    wefs = np.ones((len(nat), 3))
+
+    def handle(precision):
+        c = _lib.default_config()
+        c.j_max, c.r_cut, c.lambda_krr, c.precision = J_MAX, RCUT, LAMBDA, precision
+        c.n_elements = 1
+        h = _lib.Handle(c)
+        h.set_structures(nat, pos, cell, types)
+        h.set_labels(E, F, S, has, wefs)
+        return h
+
+    res = {}
+    # ---------------- mixed method, inputs resident ---------------------------------------
+    h = handle(_lib.MIXED)
+    M = h.num_rows()
+    A = int(nat.sum())
+    for _ in range(a.warmup):
+        w_mixed, rmse_mixed = h.fit()
+    h.set_profiling(True)
+    h.profile(reset=True)
+    with Clocks() as clk:
+        h.timer_start()
+        for _ in range(a.steps):
+            w_mixed, rmse_mixed = h.fit()
+        ms_total = h.timer_stop()
+    prof = h.profile(reset=True)
+    h.set_profiling(False)
+    ms_step = ms_total / a.steps
+    wc = h.work_counts()
+    flops, per_pair, per_atom = flops_model(wc, wc["pairs"], wc["atoms"])
+    t_desc = prof["descriptors"][0] / max(prof["descriptors"][2], 1)
+    peak32 = h.peak_flops(_lib.MIXED)
+    launches = sum(v[1] for v in prof.values())
+    res.update(M=M, A=A, ms_step=ms_step, rmse_mixed=rmse_mixed.tolist(), prof=prof, wc=wc, flops=flops,
+               t_desc=t_desc, peak32=peak32, launches=launches, clocks=clk.summary(),
+               per_pair=per_pair, per_atom=per_atom)
+
+    # ---------------- e2e through the C ABI with host buffers -----------------------------
+    if not a.no_e2e:
+        try:
+            import torch
+            def pinned(x):
+                t = torch.from_numpy(np.ascontiguousarray(x)).pin_memory()
+                return t, t.numpy()
+        except Exception:  # pragma: no cover - torch absent: pageable host memory
+            def pinned(x):
+                y = np.ascontiguousarray(x)
+                return None, y
+        keep = [pinned(x) for x in (nat, pos, cell, types, E, F, S, has, wefs)]
+        hn = [k[1] for k in keep]
+        for _ in range(1):
+            h.set_structures(hn[0], hn[1], hn[2], hn[3])
+            h.set_labels(hn[4], hn[5], hn[6], hn[7], hn[8])
+            h.fit()
+        h.timer_start()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            h.set_structures(hn[0], hn[1], hn[2], hn[3])
+            h.set_labels(hn[4], hn[5], hn[6], hn[7], hn[8])
+            w_e2e, _ = h.fit()
+        ms_e2e = h.timer_stop() / a.steps
+        wall_e2e = (time.perf_counter() - t0) * 1e3 / a.steps
+        S_ = len(nat)
+        h2d = (nat.nbytes + pos.nbytes + cell.nbytes + types.nbytes + E.nbytes + F.nbytes + S.nbytes +
+               has.nbytes + wefs.nbytes + 4 * A + 4 * (S_ + 1) + 8 * 9 * S_ + 4 * S_ + 12 * S_ + 8 * S_ +
+               3 * 8 * S_)
+        d2h = 8 * h.dim_design_line + 8 * 6 + 8
+        res.update(ms_e2e=ms_e2e, wall_e2e=wall_e2e, h2d=int(h2d), d2h=int(d2h))
+    h.close()
+
+    # ---------------- plain FP64 method on the same data ----------------------------------
+    h64 = handle(_lib.PLAIN_FP64)
+    w64, rmse64 = h64.fit()
+    h64.set_profiling(True)
+    h64.profile(reset=True)
+    h64.timer_start()
+    for _ in range(a.plain_steps):
+        w64, rmse64 = h64.fit()
+    ms64 = h64.timer_stop() / a.plain_steps
+    prof64 = h64.profile(reset=True)
+    peak64 = h64.peak_flops(_lib.PLAIN_FP64)
+    h64.close()
+    res.update(ms64=ms64, rmse64=rmse64.tolist(), prof64=prof64, peak64=peak64)
+    res["ds"] = ds
+    return res
+
+
+def cpu_sample(ds, target_s=15.0, threads=None):
+    """Time the oracle (CPU restatement of the reference) on a bounded sample of the same set:
+    neighbours + descriptors + rows in C (OpenMP over structures), Gram + gelsd in NumPy/LAPACK."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ctypes
+    import oracle
+    oracle.init(J_MAX)
+    L = oracle.lib()
+    L.orc_rows_batch.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                                                         ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                                                         ctypes.c_double, ctypes.c_void_p]
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+    def run(idx):
+        ss = [ds.structures[i] for i in idx]
+        nat = np.array([s.nat for s in ss], np.int32)
+        pos = np.ascontiguousarray(np.concatenate([s.positions for s in ss]))
+        cell = np.ascontiguousarray(np.stack([s.cell for s in ss]))
+        types = np.ascontiguousarray(np.concatenate([s.types for s in ss]).astype(np.int32))
+        rows = int(sum(1 + 3 * s.nat + 6 for s in ss))
+        A = np.zeros((rows, 56))
+        chw = np.ones(1)
+        t0 = time.perf_counter()
+        rc = L.orc_rows_batch(len(ss), nat.ctypes.data, pos.ctypes.data, cell.ctypes.data, types.ctypes.data, 1, 1,
+                              chw.ctypes.data, RCUT, 300, 1.0, 1.0, A.ctypes.data)
+        assert rc == 0
+        y = np.concatenate([np.concatenate([[s.energies[1]], s.forces.reshape(-1), s.stress]) for s in ss])
+        w = oracle.fit_linear(A, y, np.ones(rows), LAMBDA)
+        dt = time.perf_counter() - t0
+        return rows, int(nat.sum()), dt
+
+    # calibrate on a few structures, then pick a sample of about target_s seconds
+    order = np.random.default_rng(0).permutation(len(ds.structures))
+    r0, a0, t0 = run(order[:8])
+    per_atom = t0 / max(a0, 1)
+    total_atoms = sum(s.nat for s in ds.structures)
+    want_atoms = min(total_atoms, int(target_s / max(per_atom, 1e-9)))
+    idx, acc = [], 0
+    for i in order:
+        if acc >= want_atoms:
+            break
+        idx.append(int(i))
+        acc += ds.structures[i].nat
+    rows, atoms, dt = run(idx)
+    return {"value": rows / dt, "unit": "design rows/s", "cores": cores, "kind": "port",
+            "sample": f"{len(idx)} of {len(ds.structures)} structures ({atoms} atoms, {rows} rows), "
+                      f"full fit pipeline, {dt:.1f} s", "atoms_per_s": atoms / dt}
+
+
+def main():
+    a = _args()
+    rank, world = _dist()
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        ds = make_dataset(a.structures)
+        vals = []
+        for i in range(a.warmup + a.steps):
+            r = cpu_sample(ds, target_s=8.0)
+            if i >= a.warmup:
+                vals.append(r["value"])
+        v = float(np.mean(vals))
+        line = {"metric": "design rows/s (batched linear fit, bispectrum j_max=4)", "value": v,
+                "unit": "design rows/s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+                "higher_is_better": True, "impl": "reference", "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "fe_bcc_2000_struct_16to1024_atoms_linear_jmax4", "structures": a.structures},
+                "cpu_baseline": dict(r, value=v),
+                "e2e": {"value": v, "unit": "design rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "vs_baseline": None}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    res = run_ours(a, rank, world)
+    ms_step = res["ms_step"]
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms_step], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    if rank != 0:
+        return
+    M, A = res["M"], res["A"]
+    value = world * M / (ms_step * 1e-3)
+    achieved = res["flops"] / (res["t_desc"] * 1e-3) / 1e12
+    cpu = None if a.no_cpu else cpu_sample(res["ds"])
+    line = {
+        "metric": "design rows/s (batched linear fit, bispectrum j_max=4)",
+        "value": value,
+        "unit": "design rows/s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": ms_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 descriptors/rows + fp64 gram/solve",
+        "data": "synthetic",
+        "config": {"workload": "fe_bcc_2000_struct_16to1024_atoms_linear_jmax4", "structures": len(res["ds"].structures),
+                   "atoms": A, "design_rows": M, "dim_design_line": 56, "r_cut": RCUT, "lambda_krr": LAMBDA,
+                   "l2": "working set above L2 every step (design matrix %.2f GB)" % (M * 56 * 4 / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "atom_evals_per_s": world * A / (ms_step * 1e-3),
+        "rmse_efs": res["rmse_mixed"],
+        "plain_fp64": {"value": M / (res["ms64"] * 1e-3), "ms_per_step": res["ms64"], "rmse_efs": res["rmse64"],
+                       "steps": a.plain_steps,
+                       "phase_ms": {k: v[0] / max(v[2], 1) for k, v in res["prof64"].items()},
+                       "fp64_peak_tflops_measured": res["peak64"]},
+        "speedup_vs_plain_fp64": res["ms64"] / ms_step,
+        "phase_ms": {k: v[0] / max(v[2], 1) for k, v in res["prof"].items()},
+        "roofline": {"kernel": "k_bso4<float> (fused descriptor + design rows)", "bound": "fp32",
+                     "achieved": achieved, "peak": res["peak32"], "unit": "TFLOP/s", "frac": achieved / res["peak32"],
+                     "peak_source": "measured in this run (FP32 FMA probe; not in MEASURED_PEAKS.json)",
+                     "flops_per_launch": res["flops"], "flops_per_pair": res["per_pair"],
+                     "flops_per_atom": res["per_atom"], "traffic": None},
+        "gpu_launches": res["launches"],
+        "clocks": res["clocks"],
+    }
+    if "ms_e2e" in res:
+        line["e2e"] = {"value": world * M / (res["ms_e2e"] * 1e-3), "unit": "design rows/s",
+                       "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],
+                       "ms_per_step": res["ms_e2e"], "host_wall_ms_per_step": res["wall_e2e"]}
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -141,6 +141,33 @@ int mld_gpu_predict(mld_gpu_handle* h, const double* w_params, double* E, double
 /* Block until the handle's stream has finished. */
 int mld_gpu_synchronize(mld_gpu_handle* h);
 
+/* ---- measurement (the reference's phase timers, time_check_general / repport_time,
+ *      ml_in_ndm_module.F90:271-320, re-done with CUDA events on the handle's stream) ---- */
+#define MLD_NPHASE 6
+#define MLD_PHASE_NEIGHBOURS 0   /* count, scan, fill */
+#define MLD_PHASE_ROWS 1         /* zero the design matrix, labels and weights */
+#define MLD_PHASE_DESCRIPTORS 2  /* fused bispectrum + design-row kernel */
+#define MLD_PHASE_GRAM 3         /* weighted Gram and right-hand side */
+#define MLD_PHASE_SOLVE 4        /* ridge / min-norm solve */
+#define MLD_PHASE_PREDICT 5      /* train predictions and squared errors */
+
+/* Record CUDA events around each phase of mld_gpu_fit (on = 1) and accumulate their times. */
+int mld_gpu_set_profiling(mld_gpu_handle* h, int on);
+/* Accumulated per-phase device time [ms], kernel launches and fits (arrays of MLD_NPHASE;
+ * any may be NULL); reset != 0 clears the accumulators after reading. */
+int mld_gpu_profile(mld_gpu_handle* h, double* ms, long long* launches, long long* calls, int reset);
+/* Event-based interval timer on the handle's stream (stop synchronises on its event). */
+int mld_gpu_timer_start(mld_gpu_handle* h);
+int mld_gpu_timer_stop(mld_gpu_handle* h, double* ms);
+/* Sizes behind the algorithmic work model of the descriptor kernel, out[12] =
+ * {NU, one-term U entries, two-term U entries, CG terms (ZA+ZB+ZC), sum of Z row extents,
+ *  Z outputs, merged Y slots, Y slots carrying ZA, K, channels, neighbour pairs, atoms}. */
+int mld_gpu_work_counts(const mld_gpu_handle* h, long long* out);
+/* Measured CUDA-core FMA throughput [TFLOP/s] of this GPU for the precision's descriptor type
+ * (FP64 for MLD_PRECISION_PLAIN_FP64, FP32 for MLD_PRECISION_MIXED): the roofline denominator
+ * of the descriptor kernel. */
+int mld_gpu_peak_flops(mld_gpu_handle* h, int precision, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

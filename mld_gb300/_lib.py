@@ -24,7 +24,11 @@ MAX_ELEMENTS = 8
 EXPORTED = ["mld_gpu_config_defaults", "mld_gpu_create", "mld_gpu_destroy", "mld_gpu_last_error", "mld_gpu_dims",
             "mld_gpu_set_structures", "mld_gpu_set_labels", "mld_gpu_descriptors",
             "mld_gpu_descriptor_derivatives", "mld_gpu_num_rows", "mld_gpu_design_matrix", "mld_gpu_gram",
-            "mld_gpu_solve", "mld_gpu_fit", "mld_gpu_predict", "mld_gpu_synchronize"]
+            "mld_gpu_solve", "mld_gpu_fit", "mld_gpu_predict", "mld_gpu_synchronize", "mld_gpu_set_profiling",
+            "mld_gpu_profile", "mld_gpu_timer_start", "mld_gpu_timer_stop", "mld_gpu_work_counts",
+            "mld_gpu_peak_flops"]
+NPHASE = 6
+PHASES = ["neighbours", "rows", "descriptors", "gram", "solve", "predict"]
 
 
 class MldGpuConfig(ctypes.Structure):
@@ -89,6 +93,12 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.mld_gpu_fit.argtypes = [P, P, P]
     L.mld_gpu_predict.argtypes = [P, P, P, P, P]
     L.mld_gpu_synchronize.argtypes = [P]
+    L.mld_gpu_set_profiling.argtypes = [P, I]
+    L.mld_gpu_profile.argtypes = [P, P, P, P, I]
+    L.mld_gpu_timer_start.argtypes = [P]
+    L.mld_gpu_timer_stop.argtypes = [P, ctypes.POINTER(D)]
+    L.mld_gpu_work_counts.argtypes = [P, P]
+    L.mld_gpu_peak_flops.argtypes = [P, I, ctypes.POINTER(D)]
     for n in EXPORTED:
         if n not in ("mld_gpu_config_defaults", "mld_gpu_destroy", "mld_gpu_last_error"):
             getattr(L, n).restype = I
@@ -220,3 +230,33 @@ class Handle:
 
     def synchronize(self):
         self._check(self._L.mld_gpu_synchronize(self._h))
+
+    def set_profiling(self, on: bool = True):
+        self._check(self._L.mld_gpu_set_profiling(self._h, int(on)))
+
+    def profile(self, reset: bool = False):
+        ms = np.zeros(NPHASE)
+        la = np.zeros(NPHASE, np.int64)
+        ca = np.zeros(NPHASE, np.int64)
+        self._check(self._L.mld_gpu_profile(self._h, _p(ms), _p(la), _p(ca), int(reset)))
+        return {k: (ms[i], int(la[i]), int(ca[i])) for i, k in enumerate(PHASES)}
+
+    def timer_start(self):
+        self._check(self._L.mld_gpu_timer_start(self._h))
+
+    def timer_stop(self) -> float:
+        t = ctypes.c_double()
+        self._check(self._L.mld_gpu_timer_stop(self._h, ctypes.byref(t)))
+        return t.value
+
+    def peak_flops(self, precision: int) -> float:
+        t = ctypes.c_double()
+        self._check(self._L.mld_gpu_peak_flops(self._h, int(precision), ctypes.byref(t)))
+        return t.value
+
+    def work_counts(self):
+        out = np.zeros(12, np.int64)
+        self._check(self._L.mld_gpu_work_counts(self._h, _p(out)))
+        keys = ["NU", "u_one_term", "u_two_term", "cg_terms", "z_row_extents", "z_outputs", "y_slots",
+                "y_slots_za", "K", "nch", "pairs", "atoms"]
+        return dict(zip(keys, (int(v) for v in out)))

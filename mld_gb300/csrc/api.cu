@@ -61,6 +61,14 @@ struct mld_gpu_handle {
   std::vector<int> h_has;  // 3*S
   RowLayout fit_rows;
 
+  // profiling: CUDA events around each phase of a fit, accumulated after its final sync
+  bool prof = false;
+  cudaEvent_t ev[2 * MLD_NPHASE] = {};
+  cudaEvent_t tev[2] = {};
+  double ms[MLD_NPHASE] = {0};
+  long long launches[MLD_NPHASE] = {0};
+  long long calls[MLD_NPHASE] = {0};
+
   std::vector<void*> owned;  // table allocations
   Buf bufs[40];
   enum {
@@ -166,6 +174,10 @@ RowLayout make_layout(const mld_gpu_handle* h, const std::vector<int>& has, bool
   return L;
 }
 
+void mark(mld_gpu_handle* h, int phase, int end) {
+  if (h->prof) cudaEventRecord(h->ev[2 * phase + end], h->st);
+}
+
 int build_neighbours(mld_gpu_handle* h) {
   if (!h->has_batch) return fail(h, MLD_ERR_STATE, "no structures staged");
   DevBatch& b = h->b;
@@ -215,6 +227,7 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
   CK(ensure(h, mld_gpu_handle::B_WROW, sizeof(double) * std::max<long long>(L.M, 1)));
   CK(ensure(h, mld_gpu_handle::B_KIND, sizeof(int) * std::max<long long>(L.M, 1)));
   T* X = bp_<T>(h, mld_gpu_handle::B_X);
+  mark(h, MLD_PHASE_ROWS, 0);
   CK(cudaMemsetAsync(X, 0, xbytes, h->st));
   const double* dE = with_labels ? bp_<double>(h, mld_gpu_handle::B_E) : nullptr;
   if (with_labels) {
@@ -236,15 +249,36 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
                            bp_<double>(h, mld_gpu_handle::B_WEFS), X, bp_<double>(h, mld_gpu_handle::B_Y),
                            bp_<double>(h, mld_gpu_handle::B_WROW), bp_<int>(h, mld_gpu_handle::B_KIND), h->st));
   }
+  mark(h, MLD_PHASE_ROWS, 1);
+  mark(h, MLD_PHASE_DESCRIPTORS, 0);
   CK(launch_bso4_rows<T>(h->dt, h->b, rows, h->bp, X, (T*)nullptr, (T*)nullptr, 1, h->st));
+  mark(h, MLD_PHASE_DESCRIPTORS, 1);
   *Xout = X;
   return MLD_OK;
 }
 
+// Kernel launches per phase of one fit (neighbours: count, 3 scan kernels, fill; rows: labels
+// kernel; descriptors: fused bispectrum kernel; Gram: tiles, rhs, symmetrise; solve; predict).
+const int kLaunchesPerPhase[MLD_NPHASE] = {5, 1, 1, 3, 1, 1};
+
+void accumulate_profile(mld_gpu_handle* h) {
+  if (!h->prof) return;
+  for (int p = 0; p < MLD_NPHASE; ++p) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, h->ev[2 * p], h->ev[2 * p + 1]) == cudaSuccess) {
+      h->ms[p] += t;
+      h->launches[p] += kLaunchesPerPhase[p];
+      h->calls[p] += 1;
+    }
+  }
+}
+
 template <typename T>
 int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
+  mark(h, MLD_PHASE_NEIGHBOURS, 0);
   int rc = build_neighbours(h);
   if (rc) return rc;
+  mark(h, MLD_PHASE_NEIGHBOURS, 1);
   T* X = nullptr;
   rc = run_rows<T>(h, h->fit_rows, true, &X);
   if (rc) return rc;
@@ -259,18 +293,25 @@ int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
   double* G = bp_<double>(h, mld_gpu_handle::B_G);
   double* hv = bp_<double>(h, mld_gpu_handle::B_H);
   double* w = bp_<double>(h, mld_gpu_handle::B_W);
+  mark(h, MLD_PHASE_GRAM, 0);
   CK(launch_gram<T>(X, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D, G, hv,
                     h->st));
+  mark(h, MLD_PHASE_GRAM, 1);
+  mark(h, MLD_PHASE_SOLVE, 0);
   CK(launch_solve_sym(G, hv, D, h->cfg.lambda_krr, h->cfg.svd_rcond, w, bp_<double>(h, mld_gpu_handle::B_EVALS),
                       bp_<int>(h, mld_gpu_handle::B_INFO), h->st));
+  mark(h, MLD_PHASE_SOLVE, 1);
   double* sq = bp_<double>(h, mld_gpu_handle::B_SQ);
+  mark(h, MLD_PHASE_PREDICT, 0);
   CK(cudaMemsetAsync(sq, 0, sizeof(double) * 6, h->st));
   CK(launch_predict_sq<T>(X, w, M, D, nullptr, bp_<double>(h, mld_gpu_handle::B_Y), bp_<int>(h, mld_gpu_handle::B_KIND),
                           sq, h->st));
+  mark(h, MLD_PHASE_PREDICT, 1);
   double hsq[6];
   if (w_params) CK(cudaMemcpyAsync(w_params, w, sizeof(double) * D, cudaMemcpyDeviceToHost, h->st));
   CK(cudaMemcpyAsync(hsq, sq, sizeof(double) * 6, cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
+  accumulate_profile(h);
   if (rmse)
     for (int k = 0; k < 3; ++k) rmse[k] = hsq[3 + k] > 0 ? std::sqrt(hsq[k] / hsq[3 + k]) : 0.0;
   return MLD_OK;
@@ -439,6 +480,10 @@ void mld_gpu_destroy(mld_gpu_handle* h) {
   for (auto& bf : h->bufs)
     if (bf.p) cudaFree(bf.p);
   for (void* p : h->owned) cudaFree(p);
+  for (auto& e : h->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : h->tev)
+    if (e) cudaEventDestroy(e);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
 }
@@ -761,6 +806,82 @@ int mld_gpu_predict(mld_gpu_handle* h, const double* w_params, double* E, double
   return MLD_OK;
 }
 
+int mld_gpu_set_profiling(mld_gpu_handle* h, int on) {
+  if (!h) return MLD_ERR_INVALID;
+  if (on && !h->ev[0]) {
+    for (auto& e : h->ev) CK(cudaEventCreate(&e));
+  }
+  h->prof = on != 0;
+  return MLD_OK;
+}
+
+int mld_gpu_profile(mld_gpu_handle* h, double* ms, long long* launches, long long* calls, int reset) {
+  if (!h) return MLD_ERR_INVALID;
+  for (int p = 0; p < MLD_NPHASE; ++p) {
+    if (ms) ms[p] = h->ms[p];
+    if (launches) launches[p] = h->launches[p];
+    if (calls) calls[p] = h->calls[p];
+    if (reset) {
+      h->ms[p] = 0;
+      h->launches[p] = 0;
+      h->calls[p] = 0;
+    }
+  }
+  return MLD_OK;
+}
+
+int mld_gpu_timer_start(mld_gpu_handle* h) {
+  if (!h) return MLD_ERR_INVALID;
+  if (!h->tev[0]) {
+    CK(cudaEventCreate(&h->tev[0]));
+    CK(cudaEventCreate(&h->tev[1]));
+  }
+  CK(cudaEventRecord(h->tev[0], h->st));
+  return MLD_OK;
+}
+
+int mld_gpu_timer_stop(mld_gpu_handle* h, double* ms) {
+  if (!h || !ms || !h->tev[0]) return MLD_ERR_INVALID;
+  CK(cudaEventRecord(h->tev[1], h->st));
+  CK(cudaEventSynchronize(h->tev[1]));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, h->tev[0], h->tev[1]));
+  *ms = t;
+  return MLD_OK;
+}
+
+int mld_gpu_work_counts(const mld_gpu_handle* h, long long* out) {
+  if (!h || !out) return MLD_ERR_INVALID;
+  const Bso4Tables& t = h->tab;
+  long long one = 0, two = 0;
+  for (int j = 1; j <= t.J; ++j)
+    for (int p = -j; p <= j; p += 2)
+      for (int q = -j; q <= j; q += 2) {
+        // entries on the edge of the layer have one source term, the rest two
+        int nterm = 0;
+        if (q != -j) nterm = (p != -j) + (p != j);
+        else nterm = (p != j) + (p != -j);
+        (nterm == 1 ? one : two) += 1;
+      }
+  long long cgsum = t.cg_terms_A + t.cg_terms_B + t.cg_terms_C;
+  long long na_sum = 0, is_a = 0;
+  for (const auto& z : t.zterms) na_sum += z.na;
+  for (const auto& s : t.yslots) is_a += s.is_a;
+  out[0] = t.NU;
+  out[1] = one;
+  out[2] = two;
+  out[3] = cgsum;
+  out[4] = na_sum;
+  out[5] = (long long)t.zterms.size();
+  out[6] = (long long)t.yslots.size();
+  out[7] = is_a;
+  out[8] = t.K;
+  out[9] = h->nch;
+  out[10] = h->b.P;
+  out[11] = h->A;
+  return MLD_OK;
+}
+
 int mld_gpu_synchronize(mld_gpu_handle* h) {
   if (!h) return MLD_ERR_INVALID;
   cudaError_t e = cudaStreamSynchronize(h->st);
@@ -768,3 +889,15 @@ int mld_gpu_synchronize(mld_gpu_handle* h) {
 }
 
 }  // extern "C"
+
+namespace mld {
+template <typename T>
+cudaError_t measure_fma_peak(cudaStream_t st, double* tflops);
+}
+
+extern "C" int mld_gpu_peak_flops(mld_gpu_handle* h, int precision, double* tflops) {
+  if (!h || !tflops) return MLD_ERR_INVALID;
+  cudaError_t e = precision == MLD_PRECISION_MIXED ? mld::measure_fma_peak<float>(h->st, tflops)
+                                                   : mld::measure_fma_peak<double>(h->st, tflops);
+  return e == cudaSuccess ? MLD_OK : cuda_fail(h, e, "mld_gpu_peak_flops");
+}

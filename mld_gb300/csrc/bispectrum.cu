@@ -354,8 +354,9 @@ __global__ void __launch_bounds__(NW * 32) k_bso4(KernelArgs<T> args, T* __restr
             cx<T> cv = cc[sl.uidx];
             atomicAdd(&Bk[sl.k], cv.x * zs.x + cv.y * zs.y);  // Re(conj(c) * ZA)
           }
-          acc.x = fma((T)z.scale, zs.x, acc.x);
-          acc.y = fma((T)z.scale, zs.y, acc.y);
+          const T sc = (T)z.snum / (T)z.sden;
+          acc.x = fma(sc, zs.x, acc.x);
+          acc.y = fma(sc, zs.y, acc.y);
         }
         Y[sidx] = acc;
       }

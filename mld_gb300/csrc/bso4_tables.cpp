@@ -89,13 +89,11 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
   };
 
   // ZTerm list per (k, block) and per (m1,m2)
-  struct Block { int jA, jB, jO; double scale; int first; };
+  struct Block { int jA, jB, jO, snum, sden; int first; };
   std::vector<std::vector<Block>> kblocks(t->K);
   for (int k = 0; k < t->K; ++k) {
     int l1 = t->l1[k], l2 = t->l2[k], l = t->l[k];
-    Block bl[3] = {{l1, l2, l, 1.0, 0},
-                   {l, l2, l1, (double)(l + 1) / (double)(l1 + 1), 0},
-                   {l1, l, l2, (double)(l + 1) / (double)(l2 + 1), 0}};
+    Block bl[3] = {{l1, l2, l, 1, 1, 0}, {l, l2, l1, l + 1, l1 + 1, 0}, {l1, l, l2, l + 1, l2 + 1, 0}};
     for (int b = 0; b < 3; ++b) {
       Block& B = bl[b];
       B.first = (int)t->zterms.size();
@@ -112,7 +110,9 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
           z.i2 = (uint16_t)uidx(B.jB, m1 - malo, m2 - mblo);
           z.cg1 = (uint16_t)cglist(B.jA, B.jB, B.jO, m1);
           z.cg2 = (uint16_t)cglist(B.jA, B.jB, B.jO, m2);
-          z.scale = (float)B.scale;
+          z.snum = (uint8_t)B.snum;
+          z.sden = (uint8_t)B.sden;
+          z.pad = 0;
           long long nt = (long long)z.na * z.nb;
           (b == 0 ? t->cg_terms_A : b == 1 ? t->cg_terms_B : t->cg_terms_C) += nt;
           t->zterms.push_back(z);

@@ -367,3 +367,63 @@ template cudaError_t launch_rows_prep<float>(int, const int*, const DevRows&, co
                                              cudaStream_t);
 
 }  // namespace mld
+
+namespace mld {
+
+// CUDA-core FMA throughput probe: 8 independent FMA chains per thread, all SMs busy.  Used as
+// the measured denominator of the descriptor kernel's roofline (FP64 or FP32 pipe).
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_peak(int iters, T seed, T* out) {
+  T a0 = seed + threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6,
+    a7 = a0 + 7;
+  const T m = (T)0.999999, c = (T)1e-7;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      a0 = fma(a0, m, c);
+      a1 = fma(a1, m, c);
+      a2 = fma(a2, m, c);
+      a3 = fma(a3, m, c);
+      a4 = fma(a4, m, c);
+      a5 = fma(a5, m, c);
+      a6 = fma(a6, m, c);
+      a7 = fma(a7, m, c);
+    }
+  }
+  T s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == (T)-1) out[0] = s;  // never true; keeps the chains alive
+}
+
+template <typename T>
+cudaError_t measure_fma_peak(cudaStream_t st, double* tflops) {
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  T* out = nullptr;
+  cudaError_t e = cudaMalloc(&out, sizeof(T));
+  if (e != cudaSuccess) return e;
+  const int blocks = nsm * 8, threads = 256;
+  const int iters = sizeof(T) == 8 ? 64 : 2048;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  k_fma_peak<T><<<blocks, threads, 0, st>>>(iters, (T)1, out);  // warm-up
+  cudaEventRecord(a, st);
+  const int reps = 5;
+  for (int r = 0; r < reps; ++r) k_fma_peak<T><<<blocks, threads, 0, st>>>(iters, (T)1, out);
+  cudaEventRecord(b, st);
+  e = cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  const double flops = 2.0 * 8 * 16 * (double)iters * threads * blocks * reps;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
+template cudaError_t measure_fma_peak<double>(cudaStream_t, double*);
+template cudaError_t measure_fma_peak<float>(cudaStream_t, double*);
+
+}  // namespace mld

@@ -19,7 +19,8 @@ struct ZTerm {
   uint16_t i1, i2;       // flattened c index of the first (ma,mb) / matching second factor
   uint16_t cg1, cg2;     // offsets into the 1-D CG coefficient table
   uint8_t na, nb, s1, s2;  // loop extents and layer strides (j+1)
-  float scale;           // 1 for ZA, (l+1)/(l1+1) for ZB, (l+1)/(l2+1) for ZC
+  uint8_t snum, sden;    // scale snum/sden: 1 for ZA, (l+1)/(l1+1) for ZB, (l+1)/(l2+1) for ZC
+  uint16_t pad;
 };
 
 // One slot of the merged Y array: for triple k and layer j, the sum of the scaled Z blocks

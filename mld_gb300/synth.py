@@ -88,9 +88,9 @@ def morse_labels(pos: np.ndarray, cell: np.ndarray, types: np.ndarray, rcut: flo
 def bcc(n: int, m: int, k: int, a: float) -> Tuple[np.ndarray, np.ndarray]:
     base = np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.5]])
     g = np.stack(np.meshgrid(np.arange(n), np.arange(m), np.arange(k), indexing="ij"), -1).reshape(-1, 3)
-    frac = (g[:, None, :] + base[None, :, :]).reshape(-1, 3)
+    sites = (g[:, None, :] + base[None, :, :]).reshape(-1, 3)   # in units of the cubic cell
     cell = np.diag([n * a, m * a, k * a])
-    return frac @ cell, cell
+    return sites * a, cell
 
 
 def strain_cell(rng: np.random.Generator, cell: np.ndarray, amp: float) -> np.ndarray:
@@ -152,24 +152,36 @@ def fe_bcc_fixed(n_struct: int = 100, reps: int = 4, sigma: float = 0.05, strain
     return Dataset(out, rcut, "fe_bcc_128x100")
 
 
+def _batched_one(args):
+    s, seed, nmin, nmax, sigma, strain, rcut, max_vac = args
+    rng = np.random.default_rng(np.random.SeedSequence([seed, s]))
+    N = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+    nvac = int(rng.integers(0, max_vac + 1))
+    n, m, k = _dims_for(N + nvac)
+    pos, cell = bcc(n, m, k, FE_A)
+    keep = np.sort(rng.choice(pos.shape[0], size=N, replace=False))
+    pos = pos[keep]
+    cell2 = strain_cell(rng, cell, strain)
+    pos = pos @ np.linalg.solve(cell, cell2)
+    pos = pos + rng.normal(0.0, sigma, size=pos.shape)
+    types = np.zeros(N, np.int32)
+    E, F, S = morse_labels(pos, cell2, types, rcut)
+    return Structure(cell=cell2, positions=pos, types=types, elements=["Fe"],
+                     energies=np.array([E, E, E]), forces=F, stress=S, name=f"feb_{s:05d}")
+
+
 def fe_bcc_batched(n_struct: int = 2000, nmin: int = 16, nmax: int = 1024, sigma: float = 0.08,
                    strain: float = 0.02, rcut: float = 4.7, seed: int = 20240602,
-                   max_vac: int = 3) -> Dataset:
-    """Fe bcc supercells with log-uniform atom counts, trimmed to size, 0..max_vac extra vacancies."""
-    rng = np.random.default_rng(seed)
-    out = []
-    for s in range(n_struct):
-        N = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
-        nvac = int(rng.integers(0, max_vac + 1))
-        n, m, k = _dims_for(N + nvac)
-        pos, cell = bcc(n, m, k, FE_A)
-        keep = np.sort(rng.choice(pos.shape[0], size=N, replace=False))
-        pos = pos[keep]
-        cell2 = strain_cell(rng, cell, strain)
-        pos = pos @ np.linalg.solve(cell, cell2)
-        pos = pos + rng.normal(0.0, sigma, size=pos.shape)
-        types = np.zeros(N, np.int32)
-        E, F, S = morse_labels(pos, cell2, types, rcut)
-        out.append(Structure(cell=cell2, positions=pos, types=types, elements=["Fe"],
-                             energies=np.array([E, E, E]), forces=F, stress=S, name=f"feb_{s:05d}"))
+                   max_vac: int = 3, workers: int = 0) -> Dataset:
+    """Fe bcc supercells with log-uniform atom counts in [nmin, nmax], trimmed to size with
+    0..max_vac extra vacancies.  Structure s draws from its own seeded stream, so the set does
+    not depend on ``workers`` (0 = serial; >0 = that many spawned processes)."""
+    jobs = [(s, seed, nmin, nmax, sigma, strain, rcut, max_vac) for s in range(n_struct)]
+    if workers and workers > 1 and n_struct > 8:
+        import concurrent.futures as cf
+        import multiprocessing as mp
+        with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            out = list(ex.map(_batched_one, jobs, chunksize=max(1, n_struct // (4 * workers))))
+    else:
+        out = [_batched_one(j) for j in jobs]
     return Dataset(out, rcut, f"fe_bcc_batched_{n_struct}")

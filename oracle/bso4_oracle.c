@@ -174,7 +174,7 @@ static void orc_fcut(int type, double r, double rc, double width, double *f, dou
 /* angular_functions.f90:41-273 (spherical_4d).  Writes U (NU), and vec (3*NU) with
  * vec[a*NU + idx] = conj(U)*dfc*x_a/r + fc*conj(dU_a) -- the reference's class_mml%vecall. */
 static void orc_spherical_4d(const double x[3], double rr, double rcut, double fc, double dfc,
-                             cplx *U, cplx *dU /*3*NU scratch*/, cplx *vec) {
+                             cplx *U, cplx *dU /*3*NU scratch*/, cplx *vec, long vs) {
     const int NU = g_NU, J = g_J;
     double r0 = rcut / g_inv_r0;
     double th0 = rr / r0;
@@ -197,7 +197,7 @@ static void orc_spherical_4d(const double x[3], double rr, double rcut, double f
     dxm[0] += l0i; dxm[1] -= I * l0i;
 
     U[0] = 1.0;
-    for (int a = 0; a < 3; a++) { dU[a * NU] = 0.0; vec[a * NU] = dfc * drr[a]; }
+    for (int a = 0; a < 3; a++) { dU[a * NU] = 0.0; vec[a] = dfc * drr[a]; }
     for (int j = 1; j <= J; j++) {
         for (int q = -j; q <= j; q += 2) {
             for (int p = -j; p <= j; p += 2) {
@@ -238,7 +238,7 @@ static void orc_spherical_4d(const double x[3], double rr, double rcut, double f
                 cplx cu = conj(u);
                 for (int a = 0; a < 3; a++) {
                     dU[a * NU + d] = du[a];
-                    vec[a * NU + d] = cu * (dfc * drr[a]) + fc * conj(du[a]);
+                    vec[(long)d * vs + a] = cu * (dfc * drr[a]) + fc * conj(du[a]);
                 }
             }
         }
@@ -357,7 +357,9 @@ int orc_bispectrum(int nat, const int *itype, int ntypes, int nch, const double 
     const int NU = g_NU, K = g_K, J = g_J;
     const int KK = nch * K;
     cplx *U = malloc(sizeof(cplx) * NU), *dUs = malloc(sizeof(cplx) * 3 * NU);
-    cplx *vec = malloc(sizeof(cplx) * (size_t)3 * NU * (cap > 0 ? cap : 1));  /* vec[(n*3+a)*NU+idx] */
+    const long vs = 3L * (cap > 0 ? cap : 1);   /* class_mml(m1,m2,j)%vecall(1:3n): vec[idx*vs + 3n + a] */
+    cplx *vec = malloc(sizeof(cplx) * (size_t)vs * NU);
+    cplx *dsum = malloc(sizeof(cplx) * (size_t)vs);
     double *nw = malloc(sizeof(double) * (size_t)nch * (cap > 0 ? cap : 1));
     cplx *cm = malloc(sizeof(cplx) * NU * nch);
     /* ZA/ZB/ZC stored per triple at offsets by layer sizes */
@@ -382,7 +384,7 @@ int orc_bispectrum(int nat, const int *itype, int ntypes, int nch, const double 
             }
             double fc = (1.0 - fi) * fo;
             double dfc = -dfi * fo + (1.0 - fi) * dfo;
-            orc_spherical_4d(x, r, rcut, fc, dfc, U, dUs, vec + (size_t)n * 3 * NU);
+            orc_spherical_4d(x, r, rcut, fc, dfc, U, dUs, vec + (size_t)n * 3, vs);
             for (int ch = 0; ch < nch; ch++) {
                 double w = chw[ch * ntypes + tn];
                 nw[ch * (cap > 0 ? cap : 1) + n] = w;
@@ -439,28 +441,37 @@ int orc_bispectrum(int nat, const int *itype, int ntypes, int nch, const double 
                 B[((size_t)i * nch + ch) * K + k] = (n_i == 0) ? 0.0 : e;
                 if (!dB) continue;
                 double fB = (double)(1 + l) / (double)(1 + l1), fC = (double)(1 + l) / (double)(1 + l2);
+                /* zaxpy over the contiguous 3n vecall of each (m1,m2,layer), as :560-690 */
+                const int n3 = 3 * n_i;
+                for (int e = 0; e < n3; e++) dsum[e] = 0.0;
+                t = 0;
+                for (int m1 = -l; m1 <= l; m1 += 2) for (int m2 = -l; m2 <= l; m2 += 2, t++) {
+                    const cplx zz = zA[t];
+                    const cplx *v = vec + (long)uidx(l, m1, m2) * vs;
+                    for (int e = 0; e < n3; e++) dsum[e] += zz * v[e];
+                }
+                t = 0;
+                for (int m1 = -l1; m1 <= l1; m1 += 2) for (int m2 = -l1; m2 <= l1; m2 += 2, t++) {
+                    const cplx zz = zB[t] * fB;
+                    const cplx *v = vec + (long)uidx(l1, m1, m2) * vs;
+                    for (int e = 0; e < n3; e++) dsum[e] += zz * v[e];
+                }
+                t = 0;
+                for (int m1 = -l2; m1 <= l2; m1 += 2) for (int m2 = -l2; m2 <= l2; m2 += 2, t++) {
+                    const cplx zz = zC[t] * fC;
+                    const cplx *v = vec + (long)uidx(l2, m1, m2) * vs;
+                    for (int e = 0; e < n3; e++) dsum[e] += zz * v[e];
+                }
                 for (int n = 0; n < n_i; n++) {
+                    /* vecall of a weighted channel is the plain one scaled by the neighbour weight */
                     double w = nw[ch * (cap > 0 ? cap : 1) + n];
-                    for (int a = 0; a < 3; a++) {
-                        const cplx *v = vec + ((size_t)n * 3 + a) * NU;
-                        cplx s = 0.0;
-                        t = 0;
-                        for (int m1 = -l; m1 <= l; m1 += 2) for (int m2 = -l; m2 <= l; m2 += 2, t++)
-                            s += zA[t] * v[uidx(l, m1, m2)];
-                        t = 0;
-                        for (int m1 = -l1; m1 <= l1; m1 += 2) for (int m2 = -l1; m2 <= l1; m2 += 2, t++)
-                            s += (zB[t] * fB) * v[uidx(l1, m1, m2)];
-                        t = 0;
-                        for (int m1 = -l2; m1 <= l2; m1 += 2) for (int m2 = -l2; m2 <= l2; m2 += 2, t++)
-                            s += (zC[t] * fC) * v[uidx(l2, m1, m2)];
-                        /* vecall of a weighted channel is the plain one scaled by the neighbour weight */
-                        dB[(((size_t)i * cap + n) * 3 + a) * KK + (size_t)ch * K + k] = w * creal(s);
-                    }
+                    for (int a = 0; a < 3; a++)
+                        dB[(((size_t)i * cap + n) * 3 + a) * KK + (size_t)ch * K + k] = w * creal(dsum[3 * n + a]);
                 }
             }
         }
     }
-    free(U); free(dUs); free(vec); free(nw); free(cm); free(Z);
+    free(U); free(dUs); free(vec); free(dsum); free(nw); free(cm); free(Z);
     return 0;
 }
 
@@ -517,4 +528,44 @@ int orc_rows_linear(int nat, int KK, const double *B, const double *dB, const in
         for (int s = 0; s < 6; s++) for (int k = 0; k < KK; k++) rowS[s * D + 1 + k] *= sc;
     }
     return 0;
+}
+
+/* Batch driver for the CPU baseline: neighbours + descriptors + linear design rows of many
+ * structures, OpenMP-parallel over structures (the reference parallelises over configurations
+ * with MPI subworlds, mld_mpi.F90:536-610).  Rows are written in the design-matrix order
+ * E, 3*nat F, 6 S per structure: A[(row)*(1+KK) + col].  Returns 0 or the first error. */
+int orc_rows_batch(int nstruct, const int *nat, const double *pos, const double *cell, const int *types,
+                   int ntypes, int nch, const double *chw, double rcut, int cap,
+                   double sign_stress, double sign_big, double *A) {
+    const int K = g_K, KK = nch * K, D = 1 + KK;
+    long *atom0 = malloc(sizeof(long) * (nstruct + 1));
+    long *row0 = malloc(sizeof(long) * (nstruct + 1));
+    atom0[0] = 0; row0[0] = 0;
+    for (int s = 0; s < nstruct; s++) {
+        atom0[s + 1] = atom0[s] + nat[s];
+        row0[s + 1] = row0[s] + 1 + 3L * nat[s] + 6;
+    }
+    int err = 0;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int s = 0; s < nstruct; s++) {
+        int n = nat[s];
+        int *nn = malloc(sizeof(int) * n), *nb = malloc(sizeof(int) * (size_t)n * cap);
+        double *u = malloc(sizeof(double) * (size_t)n * cap * 3);
+        double *B = malloc(sizeof(double) * (size_t)n * KK);
+        double *dB = malloc(sizeof(double) * (size_t)n * cap * 3 * KK);
+        int small = 0;
+        const double *cl = cell + 9L * s;
+        if (orc_neighbours(n, pos + 3 * atom0[s], cl, rcut, cap, nn, nb, u, &small) != 0) {
+#pragma omp atomic write
+            err = 1;
+        } else {
+            orc_bispectrum(n, types + atom0[s], ntypes, nch, chw, NULL, 0.4, rcut, nn, nb, u, cap, B, dB);
+            double *Ar = A + (size_t)row0[s] * D;
+            orc_rows_linear(n, KK, B, dB, nn, nb, u, cap, small, sign_stress, sign_big, orc_volume(cl),
+                            Ar, Ar + D, Ar + (size_t)(1 + 3 * n) * D);
+        }
+        free(nn); free(nb); free(u); free(B); free(dB);
+    }
+    free(atom0); free(row0);
+    return err;
 }
