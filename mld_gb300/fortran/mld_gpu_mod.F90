@@ -1,0 +1,124 @@
+! ISO_C_BINDING interface to libmld_gpu (include/mld_gpu.h) for the MILADY Fortran host.
+!
+! A MILADY build links this module and libmld_gpu.so; the call sites that replace the
+! reference's own routines are shown in INTEGRATION.md.  Arrays keep the reference's
+! column-major shapes (pos_cart(3,nat), cell(3,3), force(3,nat), stress(6), energy(dim,nat),
+! Amat(D,M)) and are passed with c_loc, so no copies are made on the host side.
+module mld_gpu_mod
+  use iso_c_binding
+  implicit none
+  private
+
+  integer(c_int), parameter, public :: MLD_OK = 0
+  integer(c_int), parameter, public :: MLD_PRECISION_PLAIN_FP64 = 0
+  integer(c_int), parameter, public :: MLD_PRECISION_MIXED = 1
+  integer, parameter, public :: MLD_MAX_ELEMENTS = 8
+
+  type, bind(C), public :: mld_gpu_config
+    integer(c_int) :: descriptor_type
+    real(c_double) :: j_max
+    real(c_double) :: r_cut
+    real(c_double) :: inv_r0_input
+    integer(c_int) :: weighted
+    integer(c_int) :: weighted_3ch
+    integer(c_int) :: n_elements
+    real(c_double) :: weight_per_element(MLD_MAX_ELEMENTS)
+    real(c_double) :: weight_per_element_3ch(MLD_MAX_ELEMENTS)
+    real(c_double) :: r_cut_pair_in(MLD_MAX_ELEMENTS * MLD_MAX_ELEMENTS)
+    real(c_double) :: r_cut_width_in
+    integer(c_int) :: desc_forces
+    integer(c_int) :: ml_type
+    integer(c_int) :: mld_order
+    real(c_double) :: lambda_krr
+    real(c_double) :: svd_rcond
+    real(c_double) :: sign_stress
+    real(c_double) :: sign_stress_big_box
+    integer(c_int) :: imm_neigh
+    integer(c_int) :: precision
+  end type mld_gpu_config
+
+  public :: mld_gpu_config_defaults, mld_gpu_create, mld_gpu_destroy, mld_gpu_dims, &
+            mld_gpu_set_structures, mld_gpu_set_labels, mld_gpu_descriptors, mld_gpu_num_rows, &
+            mld_gpu_design_matrix, mld_gpu_gram, mld_gpu_solve, mld_gpu_fit, mld_gpu_predict, &
+            mld_gpu_synchronize
+
+  interface
+    subroutine mld_gpu_config_defaults(cfg) bind(C, name="mld_gpu_config_defaults")
+      import :: mld_gpu_config
+      type(mld_gpu_config), intent(out) :: cfg
+    end subroutine
+
+    integer(c_int) function mld_gpu_create(cfg, h) bind(C, name="mld_gpu_create")
+      import :: c_int, c_ptr, mld_gpu_config
+      type(mld_gpu_config), intent(in) :: cfg
+      type(c_ptr), intent(out) :: h
+    end function
+
+    subroutine mld_gpu_destroy(h) bind(C, name="mld_gpu_destroy")
+      import :: c_ptr
+      type(c_ptr), value :: h
+    end subroutine
+
+    integer(c_int) function mld_gpu_dims(h, k, dim_desc, dim_design_line) bind(C, name="mld_gpu_dims")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+      integer(c_int), intent(out) :: k, dim_desc, dim_design_line
+    end function
+
+    integer(c_int) function mld_gpu_set_structures(h, nstruct, nat, pos, cell, types) &
+        bind(C, name="mld_gpu_set_structures")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+      integer(c_int), value :: nstruct
+      type(c_ptr), value :: nat, pos, cell, types
+    end function
+
+    integer(c_int) function mld_gpu_set_labels(h, energy, force, stress, has_efs, w_efs) &
+        bind(C, name="mld_gpu_set_labels")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, energy, force, stress, has_efs, w_efs
+    end function
+
+    integer(c_int) function mld_gpu_descriptors(h, b_out, n_neigh_out) bind(C, name="mld_gpu_descriptors")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, b_out, n_neigh_out
+    end function
+
+    integer(c_int) function mld_gpu_num_rows(h, m) bind(C, name="mld_gpu_num_rows")
+      import :: c_int, c_ptr, c_long_long
+      type(c_ptr), value :: h
+      integer(c_long_long), intent(out) :: m
+    end function
+
+    integer(c_int) function mld_gpu_design_matrix(h, a, y, w) bind(C, name="mld_gpu_design_matrix")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, a, y, w
+    end function
+
+    integer(c_int) function mld_gpu_gram(h, g, rhs) bind(C, name="mld_gpu_gram")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, g, rhs
+    end function
+
+    integer(c_int) function mld_gpu_solve(h, g, rhs, d, w, rank) bind(C, name="mld_gpu_solve")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, g, rhs, w, rank
+      integer(c_int), value :: d
+    end function
+
+    integer(c_int) function mld_gpu_fit(h, w_params, rmse_efs) bind(C, name="mld_gpu_fit")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, w_params, rmse_efs
+    end function
+
+    integer(c_int) function mld_gpu_predict(h, w_params, e, f, s) bind(C, name="mld_gpu_predict")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, w_params, e, f, s
+    end function
+
+    integer(c_int) function mld_gpu_synchronize(h) bind(C, name="mld_gpu_synchronize")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+  end interface
+end module mld_gpu_mod
