@@ -13,7 +13,7 @@
 
 namespace mld {
 template <typename T>
-cudaError_t launch_predict_sq(const T* X, const double* w, long long M, int D, double* pred, const double* y,
+cudaError_t launch_predict_sq(const T* X, int ldx, const double* w, long long M, int D, double* pred, const double* y,
                               const int* kind, double* sq, cudaStream_t st);
 template <typename T>
 cudaError_t launch_rows_prep(int S, const int* atom_start, const DevRows& rows, const double* E, const double* F,
@@ -45,7 +45,7 @@ struct mld_gpu_handle {
   Bso4Tables tab;
   DevTables dt;
   BsoParams bp;
-  int nch = 1, K = 0, KK = 0, D = 0;
+  int nch = 1, K = 0, KK = 0, D = 0, ldx = 0;
   bool mixed = false;
 
   // staged batch
@@ -215,13 +215,14 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
   DevRows rows;
   rows.M = L.M;
   rows.D = h->D;
+  rows.ldx = h->ldx;
   CK(upload(h, mld_gpu_handle::B_ROWE, L.rowE.data(), h->S));
   CK(upload(h, mld_gpu_handle::B_ROWF, L.rowF.data(), h->S));
   CK(upload(h, mld_gpu_handle::B_ROWS, L.rowS.data(), h->S));
   rows.rowE = bp_<long long>(h, mld_gpu_handle::B_ROWE);
   rows.rowF = bp_<long long>(h, mld_gpu_handle::B_ROWF);
   rows.rowS = bp_<long long>(h, mld_gpu_handle::B_ROWS);
-  size_t xbytes = sizeof(T) * (size_t)std::max<long long>(L.M, 1) * h->D;
+  size_t xbytes = sizeof(T) * (size_t)std::max<long long>(L.M, 1) * h->ldx;
   CK(ensure(h, mld_gpu_handle::B_X, xbytes));
   CK(ensure(h, mld_gpu_handle::B_Y, sizeof(double) * std::max<long long>(L.M, 1)));
   CK(ensure(h, mld_gpu_handle::B_WROW, sizeof(double) * std::max<long long>(L.M, 1)));
@@ -294,7 +295,7 @@ int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
   double* hv = bp_<double>(h, mld_gpu_handle::B_H);
   double* w = bp_<double>(h, mld_gpu_handle::B_W);
   mark(h, MLD_PHASE_GRAM, 0);
-  CK(launch_gram<T>(X, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D, G, hv,
+  CK(launch_gram<T>(X, h->ldx, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D, G, hv,
                     h->st));
   mark(h, MLD_PHASE_GRAM, 1);
   mark(h, MLD_PHASE_SOLVE, 0);
@@ -304,7 +305,7 @@ int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
   double* sq = bp_<double>(h, mld_gpu_handle::B_SQ);
   mark(h, MLD_PHASE_PREDICT, 0);
   CK(cudaMemsetAsync(sq, 0, sizeof(double) * 6, h->st));
-  CK(launch_predict_sq<T>(X, w, M, D, nullptr, bp_<double>(h, mld_gpu_handle::B_Y), bp_<int>(h, mld_gpu_handle::B_KIND),
+  CK(launch_predict_sq<T>(X, h->ldx, w, M, D, nullptr, bp_<double>(h, mld_gpu_handle::B_Y), bp_<int>(h, mld_gpu_handle::B_KIND),
                           sq, h->st));
   mark(h, MLD_PHASE_PREDICT, 1);
   double hsq[6];
@@ -378,70 +379,45 @@ int mld_gpu_create(const mld_gpu_config* cfg, mld_gpu_handle** out) {
   h->K = t.K;
   h->KK = h->nch * t.K;
   h->D = 1 + h->KK;
+  h->ldx = round_up4(h->D);
   // device tables
   DevTables& d = h->dt;
   d.J = t.J;
   d.NU = t.NU;
+  d.HU = t.HU;
   d.K = t.K;
-  d.NY = (int)t.yslots.size();
-  std::vector<float> cg32(t.cg.begin(), t.cg.end());
-  std::vector<double> tz(t.NU, 0.0), tx(t.NU, 0.0);
-  std::vector<int16_t> sz(t.NU, -1), sx(t.NU, -1), uj(t.NU), up(t.NU), uq(t.NU);
-  std::vector<int8_t> qn(t.NU, 0);
-  for (int j = 0; j <= t.J; ++j) {
-    int e2 = 0;
-    for (int p = -j; p <= j; p += 2)
-      for (int q = -j; q <= j; q += 2, ++e2) {
-        int idx = t.off[j] + e2;
-        uj[idx] = (int16_t)j;
-        up[idx] = (int16_t)p;
-        uq[idx] = (int16_t)q;
-        if (j == 0) continue;
-        auto loc = [&](int pp, int qq) { return ((pp + j - 1) / 2) * j + (qq + j - 1) / 2; };
-        if (q != -j) {
-          double den = (double)(j + q);
-          if (p != -j) {
-            tz[idx] = std::sqrt((double)(j + p) / den);
-            sz[idx] = (int16_t)loc(p - 1, q - 1);
-          }
-          if (p != j) {
-            tx[idx] = std::sqrt((double)(j - p) / den);
-            sx[idx] = (int16_t)loc(p + 1, q - 1);
-          }
-        } else {
-          qn[idx] = 1;
-          double den = (double)(j - q);
-          if (p != j) {
-            tz[idx] = std::sqrt((double)(j - p) / den);
-            sz[idx] = (int16_t)loc(p + 1, q + 1);
-          }
-          if (p != -j) {
-            tx[idx] = std::sqrt((double)(j + p) / den);
-            sx[idx] = (int16_t)loc(p - 1, q + 1);
-          }
-        }
-      }
+  d.NS = (int)t.yslots.size();
+  d.NYP = t.NYP;
+  d.NTILE = (int)t.tiles.size();
+  for (int j = 0; j <= t.J + 1; ++j) {
+    d.hoff[j] = t.hoff[j];
+    d.rowk_off[j] = t.rowk_off[j];
   }
-  std::vector<float> tz32(tz.begin(), tz.end()), tx32(tx.begin(), tx.end());
+  for (int j = 0; j <= t.J; ++j) {
+    d.Mp[j] = t.Mp[j];
+    d.yoff[j] = t.yoff[j];
+  }
+  std::vector<float> cg32(t.cg.begin(), t.cg.end());
+  std::vector<float> tz32(t.rec_tz.begin(), t.rec_tz.end()), tx32(t.rec_tx.begin(), t.rec_tx.end());
   e = cudaSuccess;
 #define UP(dst, vec) \
   if (e == cudaSuccess) e = dev_alloc_copy(h, &dst, vec.data(), vec.size())
   UP(d.zterms, t.zterms);
   UP(d.yslots, t.yslots);
-  UP(d.kslot_begin, t.kslot_begin);
   UP(d.yorder, t.yorder);
+  UP(d.rowk, t.rowk);
+  UP(d.tiles, t.tiles);
   UP(d.cg64, t.cg);
   UP(d.cg32, cg32);
-  UP(d.rec_tz64, tz);
-  UP(d.rec_tx64, tx);
+  UP(d.rec_tz64, t.rec_tz);
+  UP(d.rec_tx64, t.rec_tx);
   UP(d.rec_tz32, tz32);
   UP(d.rec_tx32, tx32);
-  UP(d.rec_sz, sz);
-  UP(d.rec_sx, sx);
-  UP(d.rec_qneg, qn);
-  UP(d.uj, uj);
-  UP(d.up, up);
-  UP(d.uq, uq);
+  UP(d.rec_sz, t.rec_sz);
+  UP(d.rec_sx, t.rec_sx);
+  UP(d.rec_qneg, t.rec_qneg);
+  UP(d.expand, t.expand);
+  UP(d.half_diag, t.half_diag);
 #undef UP
   if (e != cudaSuccess) {
     int code = cuda_fail(h, e, "table upload");
@@ -686,22 +662,24 @@ int mld_gpu_design_matrix(mld_gpu_handle* h, double* A, double* y, double* w) {
   int rc = build_neighbours(h);
   if (rc) return rc;
   const long long M = h->fit_rows.M;
-  const size_t n = (size_t)M * h->D;
   if (h->mixed) {
     float* X = nullptr;
     rc = run_rows<float>(h, h->fit_rows, true, &X);
     if (rc) return rc;
     if (A) {
-      std::vector<float> tmp(n);
-      CK(cudaMemcpyAsync(tmp.data(), X, sizeof(float) * n, cudaMemcpyDeviceToHost, h->st));
+      std::vector<float> tmp((size_t)M * h->ldx);
+      CK(cudaMemcpyAsync(tmp.data(), X, sizeof(float) * tmp.size(), cudaMemcpyDeviceToHost, h->st));
       CK(cudaStreamSynchronize(h->st));
-      for (size_t i = 0; i < n; ++i) A[i] = tmp[i];
+      for (long long r = 0; r < M; ++r)
+        for (int c = 0; c < h->D; ++c) A[(size_t)r * h->D + c] = tmp[(size_t)r * h->ldx + c];
     }
   } else {
     double* X = nullptr;
     rc = run_rows<double>(h, h->fit_rows, true, &X);
     if (rc) return rc;
-    if (A) CK(cudaMemcpyAsync(A, X, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+    if (A && M > 0)
+      CK(cudaMemcpy2DAsync(A, sizeof(double) * h->D, X, sizeof(double) * h->ldx, sizeof(double) * h->D, (size_t)M,
+                           cudaMemcpyDeviceToHost, h->st));
   }
   if (y) CK(cudaMemcpyAsync(y, bp_<double>(h, mld_gpu_handle::B_Y), sizeof(double) * M, cudaMemcpyDeviceToHost, h->st));
   if (w)
@@ -723,13 +701,13 @@ int mld_gpu_gram(mld_gpu_handle* h, double* G, double* rhs) {
     float* X = nullptr;
     rc = run_rows<float>(h, h->fit_rows, true, &X);
     if (rc) return rc;
-    CK(launch_gram<float>(X, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D,
+    CK(launch_gram<float>(X, h->ldx, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D,
                           bp_<double>(h, mld_gpu_handle::B_G), bp_<double>(h, mld_gpu_handle::B_H), h->st));
   } else {
     double* X = nullptr;
     rc = run_rows<double>(h, h->fit_rows, true, &X);
     if (rc) return rc;
-    CK(launch_gram<double>(X, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D,
+    CK(launch_gram<double>(X, h->ldx, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D,
                            bp_<double>(h, mld_gpu_handle::B_G), bp_<double>(h, mld_gpu_handle::B_H), h->st));
   }
   if (G) CK(cudaMemcpyAsync(G, bp_<double>(h, mld_gpu_handle::B_G), sizeof(double) * D * D, cudaMemcpyDeviceToHost, h->st));
@@ -785,12 +763,12 @@ int mld_gpu_predict(mld_gpu_handle* h, const double* w_params, double* E, double
     float* X = nullptr;
     rc = run_rows<float>(h, L, false, &X);
     if (rc) return rc;
-    CK(launch_predict_sq<float>(X, dw, L.M, D, pred, nullptr, nullptr, nullptr, h->st));
+    CK(launch_predict_sq<float>(X, h->ldx, dw, L.M, D, pred, nullptr, nullptr, nullptr, h->st));
   } else {
     double* X = nullptr;
     rc = run_rows<double>(h, L, false, &X);
     if (rc) return rc;
-    CK(launch_predict_sq<double>(X, dw, L.M, D, pred, nullptr, nullptr, nullptr, h->st));
+    CK(launch_predict_sq<double>(X, h->ldx, dw, L.M, D, pred, nullptr, nullptr, nullptr, h->st));
   }
   std::vector<double> hp(L.M);
   CK(cudaMemcpyAsync(hp.data(), pred, sizeof(double) * L.M, cudaMemcpyDeviceToHost, h->st));
@@ -853,24 +831,13 @@ int mld_gpu_timer_stop(mld_gpu_handle* h, double* ms) {
 int mld_gpu_work_counts(const mld_gpu_handle* h, long long* out) {
   if (!h || !out) return MLD_ERR_INVALID;
   const Bso4Tables& t = h->tab;
-  long long one = 0, two = 0;
-  for (int j = 1; j <= t.J; ++j)
-    for (int p = -j; p <= j; p += 2)
-      for (int q = -j; q <= j; q += 2) {
-        // entries on the edge of the layer have one source term, the rest two
-        int nterm = 0;
-        if (q != -j) nterm = (p != -j) + (p != j);
-        else nterm = (p != j) + (p != -j);
-        (nterm == 1 ? one : two) += 1;
-      }
-  long long cgsum = t.cg_terms_A + t.cg_terms_B + t.cg_terms_C;
   long long na_sum = 0, is_a = 0;
   for (const auto& z : t.zterms) na_sum += z.na;
   for (const auto& s : t.yslots) is_a += s.is_a;
-  out[0] = t.NU;
-  out[1] = one;
-  out[2] = two;
-  out[3] = cgsum;
+  out[0] = t.HU;
+  out[1] = t.u_one;
+  out[2] = t.u_two;
+  out[3] = t.cg_terms;
   out[4] = na_sum;
   out[5] = (long long)t.zterms.size();
   out[6] = (long long)t.yslots.size();

@@ -6,7 +6,10 @@
 // src/mld/angular_functions.f90:432-483 (cg / wigner3j with doubled indices).
 // Instead of one flattened list of CG products per term (the reference's cg_A/cg_B/cg_C),
 // each Z output stores its two 1-D coefficient lists and the strided c indices, so the GPU
-// derives the 34 946 products per block from a table of a few thousand entries.
+// derives the products from a table of a few thousand entries.  Only half of every layer is
+// evaluated: U, c, Z and vecall all satisfy X(-p,-q) = (-1)^((p-q)/2) conj(X(p,q)), so the
+// other half follows by conjugation and the sums over a full layer fold into 2*Re over the half
+// (plus the self-symmetric centre of even layers).
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -56,14 +59,28 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
   }
   *t = Bso4Tables();
   t->J = J;
-  int NU = 0;
+  int NU = 0, HU = 0;
   for (int j = 0; j <= J; ++j) {
     t->off[j] = NU;
+    t->hoff[j] = HU;
     NU += (j + 1) * (j + 1);
+    HU += ((j + 1) * (j + 1) + 1) / 2;
   }
   t->off[J + 1] = NU;
+  t->hoff[J + 1] = HU;
   t->NU = NU;
-  auto uidx = [&](int j, int p, int q) { return t->off[j] + ((p + j) / 2) * (j + 1) + (q + j) / 2; };
+  t->HU = HU;
+  auto H = [&](int j) { return ((j + 1) * (j + 1) + 1) / 2; };
+  auto loc = [&](int j, int p, int q) { return ((p + j) / 2) * (j + 1) + (q + j) / 2; };  // row-major in layer
+  auto uidx = [&](int j, int p, int q) { return t->off[j] + loc(j, p, q); };
+  // encoded reference to entry (p,q) of layer j through its stored half
+  auto enc = [&](int j, int p, int q) -> int16_t {
+    int e = loc(j, p, q);
+    if (e < H(j)) return (int16_t)(e << 2);
+    int partner = (j + 1) * (j + 1) - 1 - e;  // (-p,-q)
+    int neg = (((p - q) / 2) % 2 != 0) ? 1 : 0;
+    return (int16_t)((partner << 2) | 2 | neg);
+  };
 
   for (int l1 = 0; l1 <= J; ++l1)
     for (int l2 = 0; l2 <= l1; ++l2)
@@ -75,6 +92,54 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
         t->l.push_back(l);
       }
   t->K = (int)t->l.size();
+
+  // recursion and expansion tables on half layers (angular_functions.f90:108-272)
+  t->rec_tz.assign(HU, 0.0);
+  t->rec_tx.assign(HU, 0.0);
+  t->rec_sz.assign(HU, -1);
+  t->rec_sx.assign(HU, -1);
+  t->rec_qneg.assign(HU, 0);
+  t->half_diag.assign(HU, 0);
+  t->expand.assign(NU, 0);
+  for (int j = 0; j <= J; ++j) {
+    for (int p = -j; p <= j; p += 2)
+      for (int q = -j; q <= j; q += 2) {
+        int e = loc(j, p, q);
+        t->expand[t->off[j] + e] = enc(j, p, q);
+        if (e >= H(j)) continue;
+        int hi = t->hoff[j] + e;
+        if (p == q) t->half_diag[hi] = 1;
+        if (j == 0) continue;
+        int nterm = 0;
+        if (q != -j) {
+          double den = (double)(j + q);
+          if (p != -j) {
+            t->rec_tz[hi] = std::sqrt((double)(j + p) / den);
+            t->rec_sz[hi] = enc(j - 1, p - 1, q - 1);
+            ++nterm;
+          }
+          if (p != j) {
+            t->rec_tx[hi] = std::sqrt((double)(j - p) / den);
+            t->rec_sx[hi] = enc(j - 1, p + 1, q - 1);
+            ++nterm;
+          }
+        } else {
+          t->rec_qneg[hi] = 1;
+          double den = (double)(j - q);
+          if (p != j) {
+            t->rec_tz[hi] = std::sqrt((double)(j - p) / den);
+            t->rec_sz[hi] = enc(j - 1, p + 1, q + 1);
+            ++nterm;
+          }
+          if (p != -j) {
+            t->rec_tx[hi] = std::sqrt((double)(j + p) / den);
+            t->rec_sx[hi] = enc(j - 1, p - 1, q + 1);
+            ++nterm;
+          }
+        }
+        (nterm == 1 ? t->u_one : t->u_two) += 1;
+      }
+  }
 
   std::map<std::tuple<int, int, int, int>, int> cgoff;  // (jA,jB,jOut,m) -> offset
   auto cglist = [&](int jA, int jB, int jO, int m) -> int {
@@ -88,8 +153,8 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
     return o;
   };
 
-  // ZTerm list per (k, block) and per (m1,m2)
-  struct Block { int jA, jB, jO, snum, sden; int first; };
+  // Z outputs on half layers; per (k, block) the index of its first half output
+  struct Block { int jA, jB, jO, snum, sden, first; };
   std::vector<std::vector<Block>> kblocks(t->K);
   for (int k = 0; k < t->K; ++k) {
     int l1 = t->l1[k], l2 = t->l2[k], l = t->l[k];
@@ -101,7 +166,10 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
         for (int m2 = -B.jO; m2 <= B.jO; m2 += 2) {
           int malo = std::max(-B.jA, m1 - B.jB), mahi = std::min(B.jA, m1 + B.jB);
           int mblo = std::max(-B.jA, m2 - B.jB), mbhi = std::min(B.jA, m2 + B.jB);
-          ZTerm z;
+          long long nt = (long long)((mahi - malo) / 2 + 1) * ((mbhi - mblo) / 2 + 1);
+          t->cg_terms_full += nt;
+          if (loc(B.jO, m1, m2) >= H(B.jO)) continue;
+          ZTerm z{};
           z.na = (uint8_t)((mahi - malo) / 2 + 1);
           z.nb = (uint8_t)((mbhi - mblo) / 2 + 1);
           z.s1 = (uint8_t)(B.jA + 1);
@@ -112,9 +180,7 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
           z.cg2 = (uint16_t)cglist(B.jA, B.jB, B.jO, m2);
           z.snum = (uint8_t)B.snum;
           z.sden = (uint8_t)B.sden;
-          z.pad = 0;
-          long long nt = (long long)z.na * z.nb;
-          (b == 0 ? t->cg_terms_A : b == 1 ? t->cg_terms_B : t->cg_terms_C) += nt;
+          t->cg_terms += nt;
           t->zterms.push_back(z);
         }
       kblocks[k].push_back(B);
@@ -125,41 +191,65 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
     return false;
   }
 
-  // merged Y slots: per k, per distinct layer
-  t->kslot_begin.assign(t->K + 1, 0);
-  std::vector<long long> cost;
+  // layer-blocked Y: rows of layer j are the triples using layer j (any of l, l1, l2)
+  std::vector<std::vector<int>> rows(J + 1);
   for (int k = 0; k < t->K; ++k) {
-    t->kslot_begin[k] = (int)t->yslots.size();
-    const auto& bl = kblocks[k];
-    std::vector<int> layers;
-    for (int b = 0; b < 3; ++b)
-      if (std::find(layers.begin(), layers.end(), bl[b].jO) == layers.end()) layers.push_back(bl[b].jO);
-    for (int j : layers) {
-      int pos = 0;
-      for (int p = -j; p <= j; p += 2)
-        for (int q = -j; q <= j; q += 2, ++pos) {
-          YSlot s{};
-          s.nterm = 0;
-          s.is_a = 0;
-          long long c = 0;
-          for (int b = 0; b < 3; ++b) {
-            if (bl[b].jO != j) continue;
-            if (b == 0) s.is_a = 1;
-            int zi = bl[b].first + pos;
-            s.term[s.nterm++] = (uint16_t)zi;
-            c += (long long)t->zterms[zi].na * t->zterms[zi].nb;
-          }
-          s.uidx = (uint16_t)uidx(j, p, q);
-          s.k = (uint16_t)k;
-          t->yslots.push_back(s);
-          cost.push_back(c);
-        }
+    int js[3] = {t->l[k], t->l1[k], t->l2[k]};
+    for (int b = 0; b < 3; ++b) {
+      bool seen = false;
+      for (int c = 0; c < b; ++c) seen |= js[c] == js[b];
+      if (!seen) rows[js[b]].push_back(k);
     }
   }
-  t->kslot_begin[t->K] = (int)t->yslots.size();
+  int ypos = 0, rk = 0;
+  for (int j = 0; j <= J; ++j) {
+    t->Mp[j] = ((int)rows[j].size() + kRowTile - 1) / kRowTile * kRowTile;
+    t->yoff[j] = ypos;
+    ypos += t->Mp[j] * H(j);
+    t->rowk_off[j] = rk;
+    for (int r = 0; r < t->Mp[j]; ++r) t->rowk.push_back(r < (int)rows[j].size() ? (int16_t)rows[j][r] : -1);
+    rk += t->Mp[j];
+  }
+  t->rowk_off[J + 1] = rk;
+  t->NYP = ypos;
+  if (ypos >= 65535) {
+    *err = "Y table exceeds 16-bit offsets";
+    return false;
+  }
+
+  // folded slots
+  std::vector<long long> cost;
+  for (int j = 0; j <= J; ++j) {
+    for (int r = 0; r < (int)rows[j].size(); ++r) {
+      const int k = rows[j][r];
+      const auto& bl = kblocks[k];
+      for (int e = 0; e < H(j); ++e) {
+        int p = -j + 2 * (e / (j + 1)), q = -j + 2 * (e % (j + 1));
+        YSlot s{};
+        long long c = 0;
+        for (int b = 0; b < 3; ++b) {
+          if (bl[b].jO != j) continue;
+          if (b == 0) s.is_a = 1;
+          int zi = bl[b].first + e;  // half outputs are stored in row-major order of the layer
+          s.term[s.nterm++] = (uint16_t)zi;
+          c += (long long)t->zterms[zi].na * t->zterms[zi].nb;
+        }
+        s.ufull = (uint16_t)uidx(j, p, q);
+        s.k = (uint16_t)k;
+        s.ypos = (uint16_t)(t->yoff[j] + e * t->Mp[j] + r);
+        s.wgt = (uint8_t)((p == 0 && q == 0) ? 1 : 2);
+        t->yslots.push_back(s);
+        cost.push_back(c);
+      }
+    }
+  }
   t->yorder.resize(t->yslots.size());
   for (size_t i = 0; i < t->yorder.size(); ++i) t->yorder[i] = (int)i;
   std::stable_sort(t->yorder.begin(), t->yorder.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+
+  // row tiles of the dB contraction, heaviest layers first
+  for (int j = J; j >= 0; --j)
+    for (int rt = 0; rt < t->Mp[j] / kRowTile; ++rt) t->tiles.push_back((j << 8) | rt);
   return true;
 }
 

@@ -57,8 +57,8 @@ constexpr int GT = 32;   // tile edge
 constexpr int GR = 32;   // rows per smem stage
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_gram(const T* __restrict__ X, const double* __restrict__ w, long long M,
-                                              int D, long long rows_per_block, double* __restrict__ G) {
+__global__ void __launch_bounds__(256) k_gram(const T* __restrict__ X, int ldx, const double* __restrict__ w,
+                                              long long M, int D, long long rows_per_block, double* __restrict__ G) {
   const int nt = (D + GT - 1) / GT;
   // decode upper-triangular tile pair from blockIdx.x
   int t = blockIdx.x, ti = 0;
@@ -81,8 +81,8 @@ __global__ void __launch_bounds__(256) k_gram(const T* __restrict__ X, const dou
       double va = 0, vb = 0;
       if (r < r1) {
         const double wr = w[r];
-        if (i0 + cc < D) va = (double)X[r * D + i0 + cc] * wr;
-        if (j0 + cc < D) vb = (double)X[r * D + j0 + cc];
+        if (i0 + cc < D) va = (double)X[r * ldx + i0 + cc] * wr;
+        if (j0 + cc < D) vb = (double)X[r * ldx + j0 + cc];
       }
       sa[rr][cc] = va;
       sb[rr][cc] = vb;
@@ -107,14 +107,14 @@ __global__ void __launch_bounds__(256) k_gram(const T* __restrict__ X, const dou
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_rhs(const T* __restrict__ X, const double* __restrict__ w,
+__global__ void __launch_bounds__(256) k_rhs(const T* __restrict__ X, int ldx, const double* __restrict__ w,
                                              const double* __restrict__ y, long long M, int D,
                                              long long rows_per_block, double* __restrict__ h) {
   const long long r0 = (long long)blockIdx.x * rows_per_block;
   const long long r1 = min(M, r0 + rows_per_block);
   for (int c = threadIdx.x; c < D; c += blockDim.x) {
     double acc = 0;
-    for (long long r = r0; r < r1; ++r) acc = fma((double)X[r * D + c], w[r] * y[r], acc);
+    for (long long r = r0; r < r1; ++r) acc = fma((double)X[r * ldx + c], w[r] * y[r], acc);
     atomicAdd(&h[c], acc);
   }
 }
@@ -126,8 +126,8 @@ __global__ void k_symmetrize(double* G, int D) {
 }
 
 template <typename T>
-cudaError_t launch_gram(const T* X, const double* w, const double* y, long long M, int D, double* G, double* h,
-                        cudaStream_t st) {
+cudaError_t launch_gram(const T* X, int ldx, const double* w, const double* y, long long M, int D, double* G,
+                        double* h, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(G, 0, sizeof(double) * (size_t)D * D, st);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(h, 0, sizeof(double) * (size_t)D, st);
@@ -148,11 +148,11 @@ cudaError_t launch_gram(const T* X, const double* w, const double* y, long long 
     chunks = 65535;
     rpb = (M + chunks - 1) / chunks;
   }
-  k_gram<T><<<dim3(npairs, (unsigned)chunks), 256, 0, st>>>(X, w, M, D, rpb, G);
+  k_gram<T><<<dim3(npairs, (unsigned)chunks), 256, 0, st>>>(X, ldx, w, M, D, rpb, G);
   long long hch = (long long)nsm * 4;
   long long hrpb = (M + hch - 1) / hch;
   hch = (M + hrpb - 1) / hrpb;
-  k_rhs<T><<<(unsigned)hch, 128, 0, st>>>(X, w, y, M, D, hrpb, h);
+  k_rhs<T><<<(unsigned)hch, 128, 0, st>>>(X, ldx, w, y, M, D, hrpb, h);
   k_symmetrize<<<D, 128, 0, st>>>(G, D);
   return cudaGetLastError();
 }
@@ -311,14 +311,14 @@ cudaError_t launch_solve_sym(double* G, const double* h, int D, double lambda, d
 // predictions and squared-error sums per row kind (0 energy, 1 force, 2 stress)
 // ------------------------------------------------------------------------------------
 template <typename T>
-__global__ void k_predict(const T* __restrict__ X, const double* __restrict__ w, long long M, int D,
+__global__ void k_predict(const T* __restrict__ X, int ldx, const double* __restrict__ w, long long M, int D,
                           double* __restrict__ pred, const double* __restrict__ y, const int* __restrict__ kind,
                           double* __restrict__ sq /*3 sums + 3 counts*/) {
   const int lane = threadIdx.x & 31;
   const long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (r >= M) return;
   double acc = 0;
-  for (int c = lane; c < D; c += 32) acc = fma((double)X[r * D + c], w[c], acc);
+  for (int c = lane; c < D; c += 32) acc = fma((double)X[r * ldx + c], w[c], acc);
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if (lane == 0) {
     if (pred) pred[r] = acc;
@@ -332,12 +332,12 @@ __global__ void k_predict(const T* __restrict__ X, const double* __restrict__ w,
 }
 
 template <typename T>
-cudaError_t launch_predict_sq(const T* X, const double* w, long long M, int D, double* pred, const double* y,
-                              const int* kind, double* sq, cudaStream_t st) {
+cudaError_t launch_predict_sq(const T* X, int ldx, const double* w, long long M, int D, double* pred,
+                              const double* y, const int* kind, double* sq, cudaStream_t st) {
   if (M == 0) return cudaSuccess;
   long long threads = M * 32;
   unsigned blocks = (unsigned)((threads + 255) / 256);
-  k_predict<T><<<blocks, 256, 0, st>>>(X, w, M, D, pred, y, kind, sq);
+  k_predict<T><<<blocks, 256, 0, st>>>(X, ldx, w, M, D, pred, y, kind, sq);
   return cudaGetLastError();
 }
 
@@ -346,18 +346,18 @@ cudaError_t launch_rows_prep(int S, const int* atom_start, const DevRows& rows, 
                              const double* Sv, const double* wefs, T* X, double* y, double* wrow, int* kind,
                              cudaStream_t st) {
   if (S == 0) return cudaSuccess;
-  k_rows_prep<T><<<S, 128, 0, st>>>(S, atom_start, rows.rowE, rows.rowF, rows.rowS, E, F, Sv, wefs, rows.D, X, y,
+  k_rows_prep<T><<<S, 128, 0, st>>>(S, atom_start, rows.rowE, rows.rowF, rows.rowS, E, F, Sv, wefs, rows.ldx, X, y,
                                     wrow, kind);
   return cudaGetLastError();
 }
 
-template cudaError_t launch_gram<double>(const double*, const double*, const double*, long long, int, double*,
+template cudaError_t launch_gram<double>(const double*, int, const double*, const double*, long long, int, double*,
                                          double*, cudaStream_t);
-template cudaError_t launch_gram<float>(const float*, const double*, const double*, long long, int, double*, double*,
-                                        cudaStream_t);
-template cudaError_t launch_predict_sq<double>(const double*, const double*, long long, int, double*, const double*,
-                                               const int*, double*, cudaStream_t);
-template cudaError_t launch_predict_sq<float>(const float*, const double*, long long, int, double*, const double*,
+template cudaError_t launch_gram<float>(const float*, int, const double*, const double*, long long, int, double*,
+                                        double*, cudaStream_t);
+template cudaError_t launch_predict_sq<double>(const double*, int, const double*, long long, int, double*,
+                                               const double*, const int*, double*, cudaStream_t);
+template cudaError_t launch_predict_sq<float>(const float*, int, const double*, long long, int, double*, const double*,
                                               const int*, double*, cudaStream_t);
 template cudaError_t launch_rows_prep<double>(int, const int*, const DevRows&, const double*, const double*,
                                               const double*, const double*, double*, double*, double*, int*,

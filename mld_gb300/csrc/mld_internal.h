@@ -11,39 +11,62 @@ namespace mld {
 constexpr int kMaxJ = 10;          // doubled angular momentum bound (j_max <= 5)
 constexpr int kMaxTypes = 8;       // element types per handle
 constexpr int kMaxCh = 3;          // plain, weighted, weighted_3ch
+constexpr int kRowTile = 4;        // rows (triples) per register tile of the dB contraction
+constexpr int kColTile = 4;        // columns (neighbour, component) per register tile
+
+// Symmetry used throughout: U^j(-p,-q) = (-1)^((p-q)/2) conj(U^j(p,q)); the same holds for c,
+// the Z blocks and vecall.  Only the "half" of each layer is stored: the first
+// H_j = ceil((j+1)^2/2) entries in row-major (p, q) order.  A source reference into a half
+// layer is encoded as (half_index << 2) | (conj << 1) | negate, or -1 when absent.
 
 // One output element of the Z contraction (compute_bispectrum_so4.F90:1014-1143).
 // Z(m1,m2) = sum_{a<na, b<nb} cg1[a]*cg2[b] * c[i1 + a*s1 + b] * c[i2 - a*s2 - b]
-// where layer jA supplies the first factor and layer jB the second.
+// (full-layer indices of c) where layer jA supplies the first factor and jB the second.
 struct ZTerm {
-  uint16_t i1, i2;       // flattened c index of the first (ma,mb) / matching second factor
-  uint16_t cg1, cg2;     // offsets into the 1-D CG coefficient table
+  uint16_t i1, i2;         // flattened c index of the first (ma,mb) / matching second factor
+  uint16_t cg1, cg2;       // offsets into the 1-D CG coefficient table
   uint8_t na, nb, s1, s2;  // loop extents and layer strides (j+1)
-  uint8_t snum, sden;    // scale snum/sden: 1 for ZA, (l+1)/(l1+1) for ZB, (l+1)/(l2+1) for ZC
+  uint8_t snum, sden;      // scale snum/sden: 1 for ZA, (l+1)/(l1+1) for ZB, (l+1)/(l2+1) for ZC
   uint16_t pad;
 };
 
-// One slot of the merged Y array: for triple k and layer j, the sum of the scaled Z blocks
-// of k living on layer j at entry (p,q).  nterm in {1,2,3}; term[] index ZTerm entries.
+// One slot of the folded Y array: triple k, layer j, half entry e.  Y = wgt * sum of the scaled
+// Z blocks of k living on layer j at that entry; wgt = 2 off the symmetry centre, 1 on it.
 struct YSlot {
   uint16_t term[3];
   uint8_t nterm;
-  uint8_t is_a;          // first term is the ZA block (contributes to B_k)
-  uint16_t uidx;         // flattened (j,p,q) index into c / V
-  uint16_t k;            // triple index
+  uint8_t is_a;            // term[0] is the ZA block (contributes to B_k)
+  uint16_t ufull;          // full (j,p,q) index into c
+  uint16_t k;              // triple index
+  uint16_t ypos;           // position in the layer-blocked Y array
+  uint8_t wgt;             // 2 or 1
+  uint8_t pad;
 };
 
 // Host-built constant tables of the SO(4) bispectrum for a given j_max.
 struct Bso4Tables {
-  int J = 0, NU = 0, K = 0;
-  int off[kMaxJ + 2] = {0};
-  std::vector<int> l1, l2, l;           // triples (reference order)
-  std::vector<double> cg;               // 1-D CG coefficient lists
-  std::vector<ZTerm> zterms;            // all ZA/ZB/ZC outputs
-  std::vector<YSlot> yslots;            // merged slots, grouped by k (contiguous per k)
-  std::vector<int> kslot_begin;         // K+1 offsets into yslots
-  std::vector<int> yorder;              // yslot evaluation order (cost-descending)
-  long long cg_terms_A = 0, cg_terms_B = 0, cg_terms_C = 0;
+  int J = 0, NU = 0, HU = 0, K = 0, NYP = 0;
+  int off[kMaxJ + 2] = {0};     // full-layer offsets
+  int hoff[kMaxJ + 2] = {0};    // half-layer offsets
+  int Mp[kMaxJ + 1] = {0};      // padded row count per layer (multiple of kRowTile)
+  int yoff[kMaxJ + 1] = {0};    // Y offset of each layer block (complex elements)
+  std::vector<int> l1, l2, l;   // triples (reference order)
+  std::vector<double> cg;       // 1-D CG coefficient lists
+  std::vector<ZTerm> zterms;    // ZA/ZB/ZC outputs on half layers
+  std::vector<YSlot> yslots;    // folded slots
+  std::vector<int> yorder;      // slot evaluation order (cost-descending)
+  std::vector<int16_t> rowk;    // per layer-block row: triple index or -1 (padding)
+  int rowk_off[kMaxJ + 2] = {0};  // offset of each layer's rows in rowk
+  std::vector<int> tiles;       // row tiles (j << 8 | rt), cost-descending
+  // recursion on half layers: U = tz*Zsel*U[src_z] + tx*(-i)*Xsel*U[src_x]
+  std::vector<double> rec_tz, rec_tx;
+  std::vector<int16_t> rec_sz, rec_sx;
+  std::vector<int8_t> rec_qneg;
+  std::vector<int16_t> expand;  // full index -> encoded half source
+  std::vector<int8_t> half_diag;  // half entries on the diagonal p == q (get the +1 of c)
+  long long cg_terms = 0;       // CG products evaluated per channel (half outputs)
+  long long cg_terms_full = 0;  // CG products of the unfolded contraction (reference count)
+  long long u_one = 0, u_two = 0;  // half-layer recursion entries with one / two source terms
 };
 
 bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err);
@@ -51,14 +74,18 @@ double cg_coefficient(int j1, int m1, int j2, int m2, int j, int m);  // doubled
 
 // Device copies of the tables.
 struct DevTables {
-  int J = 0, NU = 0, K = 0, NY = 0;
+  int J = 0, NU = 0, HU = 0, K = 0, NS = 0, NYP = 0, NTILE = 0;
+  int hoff[kMaxJ + 2] = {0};
+  int Mp[kMaxJ + 1] = {0};
+  int yoff[kMaxJ + 1] = {0};
+  int rowk_off[kMaxJ + 2] = {0};
   ZTerm* zterms = nullptr;
   YSlot* yslots = nullptr;
-  int* kslot_begin = nullptr;
   int* yorder = nullptr;
+  int16_t* rowk = nullptr;
+  int* tiles = nullptr;
   double* cg64 = nullptr;
   float* cg32 = nullptr;
-  // U-recursion coefficients per flattened index: U = tz*Zsel*U[sz] - i*tx*Xsel*U[sx]
   double* rec_tz64 = nullptr;
   double* rec_tx64 = nullptr;
   float* rec_tz32 = nullptr;
@@ -66,9 +93,8 @@ struct DevTables {
   int16_t* rec_sz = nullptr;
   int16_t* rec_sx = nullptr;
   int8_t* rec_qneg = nullptr;
-  int16_t* uj = nullptr;     // layer j of each flattened index
-  int16_t* up = nullptr;     // p of each flattened index
-  int16_t* uq = nullptr;     // q of each flattened index
+  int16_t* expand = nullptr;
+  int8_t* half_diag = nullptr;
 };
 
 // Per-batch structure description on the device.
@@ -90,13 +116,13 @@ struct DevBatch {
   int* nbr_idx = nullptr;    // P
   double* nbr_u = nullptr;   // 3P  (x_neighbour - x_centre, FP64)
   long long P = 0;
-  size_t P_cap = 0;
 };
 
 // Design-row placement of each structure (-1 when a block is absent).
 struct DevRows {
   long long M = 0;           // rows
   int D = 0;                 // row width (1 + nch*K for linear)
+  int ldx = 0;               // row stride of the design matrix (D rounded up to 4)
   long long* rowE = nullptr; // S
   long long* rowF = nullptr; // S (first of 3*nat force rows)
   long long* rowS = nullptr; // S (first of 6 stress rows)
@@ -112,6 +138,8 @@ struct BsoParams {
   double sign_stress, sign_big;
 };
 
+inline int round_up4(int d) { return (d + 3) & ~3; }
+
 // Kernels / launchers (return cudaError_t of the launch).
 cudaError_t launch_neighbours(const DevBatch& b, double rcut, int* counts, int* maxcount, cudaStream_t st,
                               int pass /*0 count, 1 fill*/);
@@ -122,13 +150,9 @@ cudaError_t launch_bso4_rows(const DevTables& tb, const DevBatch& b, const DevRo
                              T* X, T* Bout, T* dBout, int want_rows, cudaStream_t st);
 
 template <typename T>
-cudaError_t launch_gram(const T* X, const double* w, const double* y, long long M, int D, double* G, double* h,
-                        cudaStream_t st);
+cudaError_t launch_gram(const T* X, int ldx, const double* w, const double* y, long long M, int D, double* G,
+                        double* h, cudaStream_t st);
 cudaError_t launch_solve_sym(double* G, const double* h, int D, double lambda, double rcond, double* wout,
-                             double* work, int* info, cudaStream_t st);
-template <typename T>
-cudaError_t launch_predict(const T* X, const double* w, long long M, int D, double* pred, cudaStream_t st);
-
-size_t bso4_smem_bytes(int NU, int NY, int K, int nch, int elem_bytes, int nwarps);
+                             double* evals, int* info, cudaStream_t st);
 
 }  // namespace mld
