@@ -105,7 +105,11 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
     for (int p = -j; p <= j; p += 2)
       for (int q = -j; q <= j; q += 2) {
         int e = loc(j, p, q);
-        t->expand[t->off[j] + e] = enc(j, p, q);
+        {
+          // expansion reads the concatenated half layers: shift the local index by hoff[j]
+          const int16_t code = enc(j, p, q);
+          t->expand[t->off[j] + e] = (int16_t)((((code >> 2) + t->hoff[j]) << 2) | (code & 3));
+        }
         if (e >= H(j)) continue;
         int hi = t->hoff[j] + e;
         if (p == q) t->half_diag[hi] = 1;

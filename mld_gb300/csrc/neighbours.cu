@@ -44,6 +44,10 @@ __global__ void k_neighbours(int A, const int* __restrict__ atom_struct, const i
     double u0 = 0, u1 = 0, u2 = 0;
     int jj = 0;
     if (cidx < ncand) {
+      // FP32 pre-filter: candidates clearly inside or outside r_cut are classified in FP32;
+      // only accepted pairs and those within kBand of the cut take the exact FP64 test.
+      constexpr float kBand = 1e-3f;
+      const float rcf = (float)rcut;
       if (sm) {
         jj = (int)(cidx / nimg);
         int im = (int)(cidx - (long long)jj * nimg);
@@ -52,29 +56,48 @@ __global__ void k_neighbours(int A, const int* __restrict__ atom_struct, const i
         int n2 = im % (2 * n2s + 1) - n2s;
         int n1 = im / (2 * n2s + 1) - n1s;
         const double* xj = pos + 3 * (size_t)(a0 + jj);
-        double t0 = xi0 - (xj[0] + cl[0] * n1 + cl[3] * n2 + cl[6] * n3);
-        double t1 = xi1 - (xj[1] + cl[1] * n1 + cl[4] * n2 + cl[7] * n3);
-        double t2 = xi2 - (xj[2] + cl[2] * n1 + cl[5] * n2 + cl[8] * n3);
-        double r2 = t0 * t0 + t1 * t1 + t2 * t2;
-        ok = (r2 >= 1e-15) && (r2 <= rc2) && (sqrt(r2) < rcut);
-        u0 = -t0;
-        u1 = -t1;
-        u2 = -t2;
+        const float f0 = (float)(xi0 - xj[0]) - ((float)cl[0] * n1 + (float)cl[3] * n2 + (float)cl[6] * n3);
+        const float f1 = (float)(xi1 - xj[1]) - ((float)cl[1] * n1 + (float)cl[4] * n2 + (float)cl[7] * n3);
+        const float f2 = (float)(xi2 - xj[2]) - ((float)cl[2] * n1 + (float)cl[5] * n2 + (float)cl[8] * n3);
+        const float rf = sqrtf(f0 * f0 + f1 * f1 + f2 * f2);
+        if (rf < rcf + kBand) {
+          double t0 = xi0 - (xj[0] + cl[0] * n1 + cl[3] * n2 + cl[6] * n3);
+          double t1 = xi1 - (xj[1] + cl[1] * n1 + cl[4] * n2 + cl[7] * n3);
+          double t2 = xi2 - (xj[2] + cl[2] * n1 + cl[5] * n2 + cl[8] * n3);
+          double r2 = t0 * t0 + t1 * t1 + t2 * t2;
+          ok = (r2 >= 1e-15) && (r2 <= rc2) && (sqrt(r2) < rcut);
+          u0 = -t0;
+          u1 = -t1;
+          u2 = -t2;
+        }
       } else {
         jj = (int)cidx;
         if (a0 + jj != g) {
           const double* xj = pos + 3 * (size_t)(a0 + jj);
-          double d0 = xj[0] - xi0, d1 = xj[1] - xi1, d2 = xj[2] - xi2;
-          double ds[3];
+          const float e0 = (float)(xj[0] - xi0), e1 = (float)(xj[1] - xi1), e2 = (float)(xj[2] - xi2);
+          float fs[3];
           for (int k = 0; k < 3; ++k) {
-            double v = d0 * bg[3 * k] + d1 * bg[3 * k + 1] + d2 * bg[3 * k + 2];
-            if (v > 0.5 || v < -0.5) v -= round(v);
-            ds[k] = v;
+            float v = e0 * (float)bg[3 * k] + e1 * (float)bg[3 * k + 1] + e2 * (float)bg[3 * k + 2];
+            fs[k] = v - rintf(v);
           }
-          u0 = cl[0] * ds[0] + cl[3] * ds[1] + cl[6] * ds[2];
-          u1 = cl[1] * ds[0] + cl[4] * ds[1] + cl[7] * ds[2];
-          u2 = cl[2] * ds[0] + cl[5] * ds[1] + cl[8] * ds[2];
-          ok = sqrt(u0 * u0 + u1 * u1 + u2 * u2) < rcut;
+          const float g0 = (float)cl[0] * fs[0] + (float)cl[3] * fs[1] + (float)cl[6] * fs[2];
+          const float g1 = (float)cl[1] * fs[0] + (float)cl[4] * fs[1] + (float)cl[7] * fs[2];
+          const float g2 = (float)cl[2] * fs[0] + (float)cl[5] * fs[1] + (float)cl[8] * fs[2];
+          // the FP32 image can differ from the reference's only when a component sits at +-0.5,
+          // i.e. at half a cell width (> r_cut for a large box), so its distance is a lower bound
+          if (sqrtf(g0 * g0 + g1 * g1 + g2 * g2) < rcf + kBand) {
+            double d0 = xj[0] - xi0, d1 = xj[1] - xi1, d2 = xj[2] - xi2;
+            double ds[3];
+            for (int k = 0; k < 3; ++k) {
+              double v = d0 * bg[3 * k] + d1 * bg[3 * k + 1] + d2 * bg[3 * k + 2];
+              if (v > 0.5 || v < -0.5) v -= round(v);
+              ds[k] = v;
+            }
+            u0 = cl[0] * ds[0] + cl[3] * ds[1] + cl[6] * ds[2];
+            u1 = cl[1] * ds[0] + cl[4] * ds[1] + cl[7] * ds[2];
+            u2 = cl[2] * ds[0] + cl[5] * ds[1] + cl[8] * ds[2];
+            ok = sqrt(u0 * u0 + u1 * u1 + u2 * u2) < rcut;
+          }
         }
       }
     }
