@@ -1,0 +1,139 @@
+"""``milady_run``: the Python entry of the MILADY fit, driving the GPU path through the C ABI.
+
+Mirrors the documented surface ``milady_run(input, db_model, DB, workdir, output, check)`` of the
+reference's Python wrapper (README of the MILADY project): it reads the ``&input_ml`` namelist,
+``db_model.in`` and the POSCAR database, fits with ``mld_gpu_fit`` and writes the predictions of
+the training and test configurations in the reference's ``train_*.out`` / ``test_*.out`` layout
+(``es20.10`` predicted and reference values, class and file name; mld.F90:944-1020).
+Only descriptor_type = 9 with ml_type = 0 and mld_order = 1 is supported by this build.
+"""
+from __future__ import annotations
+
+import dataclasses
+import os
+from typing import Dict, List, Optional
+
+import numpy as np
+
+from . import _lib, db_model, namelist, poscar
+
+
+@dataclasses.dataclass
+class FitResult:
+    w: np.ndarray
+    rmse_train: np.ndarray
+    rmse_test: Optional[np.ndarray]
+    n_train: int
+    n_test: int
+    files: Dict[str, str]
+
+
+def _config(nl: dict, precision: int) -> _lib.MldGpuConfig:
+    if int(nl["descriptor_type"]) != 9:
+        raise ValueError("this build implements descriptor_type = 9 (bispectrum SO(4)) only")
+    if int(nl["ml_type"]) != 0 or int(nl["mld_order"]) != 1:
+        raise ValueError("this build implements ml_type = 0 with mld_order = 1")
+    c = _lib.default_config()
+    c.j_max = float(nl["j_max"])
+    c.r_cut = float(nl["r_cut"])
+    c.inv_r0_input = float(nl["inv_r0_input"])
+    c.weighted = int(bool(nl["weighted"]))
+    c.weighted_3ch = int(bool(nl["weighted_3ch"]))
+    els = namelist.elements(nl) or ["X"]
+    c.n_elements = len(els)
+    w1 = namelist.element_weights(nl, "weight_per_element")
+    w2 = namelist.element_weights(nl, "weight_per_element_3ch")
+    if nl.get("weighted_auto"):
+        # fix_poscar_weights (build_subdata.F90:2953-2999): channel weights renormalised
+        r1 = float(np.sqrt(np.mean(np.square(w1)))) if w1 else 1.0
+        r2 = float(np.mean(w2)) if w2 else 1.0
+        w1 = [x / r1 for x in w1]
+        w2 = [x / r2 for x in w2]
+    for i, x in enumerate(w1[: _lib.MAX_ELEMENTS]):
+        c.weight_per_element[i] = x
+    for i, x in enumerate(w2[: _lib.MAX_ELEMENTS]):
+        c.weight_per_element_3ch[i] = x
+    c.desc_forces = int(bool(nl["desc_forces"]))
+    c.lambda_krr = float(nl["lambda_krr"])
+    c.svd_rcond = float(nl["svd_rcond"])
+    c.sign_stress = float(nl["sign_stress"])
+    c.sign_stress_big_box = float(nl["sign_stress_big_box"])
+    c.precision = precision
+    return c
+
+
+def _load(cfgs: List[db_model.Config], root: str, els: List[str], iread_energy: int, want_forces: bool):
+    ss = []
+    for c in cfgs:
+        s = poscar.read_poscar(os.path.join(root, c.filename), want_forces=want_forces)
+        # map POSCAR species onto the namelist element list (itype_to_global)
+        m = np.array([els.index(e) if e in els else 0 for e in s.elements], np.int32)
+        s.types = m[s.types]
+        ss.append(s)
+    nat = np.array([s.nat for s in ss], np.int32)
+    pos = np.concatenate([s.positions for s in ss])
+    cell = np.stack([s.cell for s in ss])
+    types = np.concatenate([s.types for s in ss])
+    E = np.array([s.energies[iread_energy - 1] for s in ss])
+    F = np.concatenate([s.forces if s.forces is not None else np.zeros((s.nat, 3)) for s in ss])
+    S = np.stack([s.stress if s.stress is not None else np.zeros(6) for s in ss])
+    has = np.array([[c.has_e and s.has_energy, c.has_f and s.has_force, c.has_s and s.has_stress]
+                    for c, s in zip(cfgs, ss)], np.int32)
+    w = np.array([[c.w_e, c.w_f, c.w_s] for c in cfgs])
+    return ss, nat, pos, cell, types, E, F, S, has, w
+
+
+def _write(path: str, rows: List[tuple]):
+    with open(path, "w") as fh:
+        for pred, ref, cls, name in rows:
+            fh.write("%20.10E%20.10E %s %s\n" % (pred, ref, cls, name))
+
+
+def milady_run(input: str, db_model_file: str = "db_model.in", DB: str = "DB/", workdir: str = ".",
+               output: str = "out", check: bool = False, precision: int = _lib.MIXED) -> FitResult:
+    nl = namelist.read_input_ml(input)
+    lines = db_model.read_db_model(db_model_file, int(nl["selection_type"]))
+    cfgs = db_model.select(lines, int(nl["selection_type"]), int(nl["seed"]), db_path="",
+                           factors=(float(nl["factor_energy_error"]), float(nl["factor_force_error"]),
+                                    float(nl["factor_stress_error"])))
+    els = namelist.elements(nl)
+    train = [c for c in cfgs if c.train]
+    test = [c for c in cfgs if not c.train]
+    os.makedirs(os.path.join(workdir, output), exist_ok=True)
+    files: Dict[str, str] = {}
+    with _lib.Handle(_config(nl, precision)) as h:
+        ss, nat, pos, cell, types, E, F, S, has, w = _load(train, DB, els, int(nl["iread_energy"]), True)
+        h.set_structures(nat, pos, cell, types)
+        h.set_labels(E, F, S, has, w)
+        coef, rmse = h.fit()
+        rmse_test = None
+        for tag, group in (("train", train), ("test", test)):
+            if not group or (tag == "test" and nl.get("train_only")):
+                continue
+            if tag == "test":
+                ss, nat, pos, cell, types, E, F, S, has, w = _load(group, DB, els, int(nl["iread_energy"]), True)
+                h.set_structures(nat, pos, cell, types)
+            Ep, Fp, Sp = h.predict(coef)
+            er, fr, sr = [], [], []
+            a0 = 0
+            for i, (c, s) in enumerate(zip(group, ss)):
+                nm = os.path.basename(c.filename)
+                cls = nm.split("_")[0]
+                if has[i, 0]:
+                    er.append((Ep[i], E[i], cls, nm))
+                if has[i, 1]:
+                    for a in range(s.nat):
+                        for k in range(3):
+                            fr.append((Fp[a0 + a, k], F[a0 + a, k], cls, nm))
+                if has[i, 2]:
+                    for k in range(6):
+                        sr.append((Sp[i, k], S[i, k], cls, nm))
+                a0 += s.nat
+            for kind, rows in (("energy", er), ("force", fr), ("stress", sr)):
+                p = os.path.join(workdir, output, f"{tag}_{kind}.out")
+                _write(p, rows)
+                files[f"{tag}_{kind}"] = p
+            if tag == "test":
+                rmse_test = np.array([np.sqrt(np.mean([(a - b) ** 2 for a, b, *_ in r])) if r else 0.0
+                                      for r in (er, fr, sr)])
+    return FitResult(coef, rmse, rmse_test, len(train), len(test), files)
