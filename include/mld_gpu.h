@@ -168,6 +168,36 @@ int mld_gpu_work_counts(const mld_gpu_handle* h, long long* out);
  * of the descriptor kernel. */
 int mld_gpu_peak_flops(mld_gpu_handle* h, int precision, double* tflops);
 
+/* ---- descriptors without device allocation --------------------------------------------
+ * No counterpart in the MILADY reference.  Some callers cannot call cudaMalloc: it
+ * synchronises the device, and hosts whose device memory is owned by another runtime's pool
+ * have nothing to call it with.  Examples are MD steps, serving loops and such pool-managed
+ * hosts.  This entry point computes the bispectrum descriptors of ONE structure on the
+ * current device and allocates nothing.  Its scratch (contraction tables, neighbour list, scan
+ * and FP32 staging) lives in one static device array of MLD_NOALLOC_SCRATCH_MIB MiB, which
+ * every GPU that loads the library holds until the process exits.
+ *   cfg    configuration as for mld_gpu_create (descriptor_type 9; both precisions)
+ *   pos    DEVICE pointer, 3*nat doubles (pos_cart(3,nat))
+ *   cell   HOST pointer, 9 doubles (cell(3,3), columns = lattice vectors)
+ *   types  DEVICE pointer, nat ints (0-based element index)
+ *   B      DEVICE pointer, nat*dim_desc doubles (energy(dim_desc, nat)), written on `stream`
+ *   stream cudaStream_t or NULL for the default stream
+ *   err    optional buffer of err_len bytes that receives a message when the call fails
+ * Limits: nat <= MLD_NOALLOC_MAX_ATOMS and at most MLD_NOALLOC_MAX_PAIRS neighbour pairs
+ * (fewer when many channels need FP32 staging).  Larger inputs return MLD_ERR_NOALLOC_LIMIT.
+ * The first call on a device resolves the array's address (cudaGetSymbolAddress) and uploads
+ * the tables; make that first call before any stream capture.  Every call shares the array
+ * and it keeps the last call's contents.  Counters that must start at zero are cleared on
+ * every call.  Calls that overlap on the GPU (two streams, or two host threads on one device)
+ * race on the array: serialise them.  The call synchronises once on `stream` to read the pair
+ * count; B is complete when `stream` is next synchronised. */
+#define MLD_NOALLOC_SCRATCH_MIB 48
+#define MLD_NOALLOC_MAX_ATOMS 16384
+#define MLD_NOALLOC_MAX_PAIRS 1048576
+#define MLD_ERR_NOALLOC_LIMIT 8  /* input larger than the static scratch array allows */
+int mld_gpu_descriptors_noalloc(const mld_gpu_config* cfg, int nat, const double* pos, const double* cell,
+                                const int* types, double* B, void* stream, char* err, int err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(HERE, "libmld_gpu.so")
 
 MLD_OK = 0
 ERRORS = {1: "MLD_ERR_INVALID", 2: "MLD_ERR_CUDA", 3: "MLD_ERR_NEIGHBOUR_CAP", 4: "MLD_ERR_OOM",
-          5: "MLD_ERR_SOLVE", 6: "MLD_ERR_STATE", 7: "MLD_ERR_UNSUPPORTED"}
+          5: "MLD_ERR_SOLVE", 6: "MLD_ERR_STATE", 7: "MLD_ERR_UNSUPPORTED", 8: "MLD_ERR_NOALLOC_LIMIT"}
 PLAIN_FP64 = 0
 MIXED = 1
 MAX_ELEMENTS = 8
@@ -26,7 +26,7 @@ EXPORTED = ["mld_gpu_config_defaults", "mld_gpu_create", "mld_gpu_destroy", "mld
             "mld_gpu_descriptor_derivatives", "mld_gpu_num_rows", "mld_gpu_design_matrix", "mld_gpu_gram",
             "mld_gpu_solve", "mld_gpu_fit", "mld_gpu_predict", "mld_gpu_synchronize", "mld_gpu_set_profiling",
             "mld_gpu_profile", "mld_gpu_timer_start", "mld_gpu_timer_stop", "mld_gpu_work_counts",
-            "mld_gpu_peak_flops"]
+            "mld_gpu_peak_flops", "mld_gpu_descriptors_noalloc"]
 NPHASE = 6
 PHASES = ["neighbours", "rows", "descriptors", "gram", "solve", "predict"]
 
@@ -99,6 +99,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.mld_gpu_timer_stop.argtypes = [P, ctypes.POINTER(D)]
     L.mld_gpu_work_counts.argtypes = [P, P]
     L.mld_gpu_peak_flops.argtypes = [P, I, ctypes.POINTER(D)]
+    L.mld_gpu_descriptors_noalloc.argtypes = [ctypes.POINTER(MldGpuConfig), I, P, P, P, P, P, ctypes.c_char_p, I]
     for n in EXPORTED:
         if n not in ("mld_gpu_config_defaults", "mld_gpu_destroy", "mld_gpu_last_error"):
             getattr(L, n).restype = I
