@@ -418,6 +418,13 @@ int mld_gpu_create(const mld_gpu_config* cfg, mld_gpu_handle** out) {
   UP(d.rec_qneg, t.rec_qneg);
   UP(d.expand, t.expand);
   UP(d.half_diag, t.half_diag);
+  std::vector<RecEntry32> r32;
+  std::vector<RecEntry64> r64;
+  pack_recursion(t, &r32, &r64);
+  UP(d.rec32, r32);
+  UP(d.rec64, r64);
+  UP(d.zitems, t.zitems);
+  UP(d.zitem_off, t.zitem_off);
 #undef UP
   if (e != cudaSuccess) {
     int code = cuda_fail(h, e, "table upload");

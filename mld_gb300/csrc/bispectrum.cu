@@ -9,8 +9,9 @@
 //            scattered straight into the energy / force / stress design rows           (mld_energy.F90:91-117,
 //            mld_forces.F90:222-263, mld_stress.F90:272-756)
 // Only half of every layer is computed (X(-p,-q) = (-1)^((p-q)/2) conj X(p,q) for U, c, Z, V);
-// full-layer sums fold into weighted sums over the half.
-// T = double (plain FP64 method) or float (mixed method: FP32 descriptors).
+// full-layer sums fold into weighted sums over the half.  The layer recursions run on lane
+// groups (8 lanes per neighbour for c, 16 for U+dU), phase 2 follows a host-balanced per-thread
+// schedule.  T = double (plain FP64 method) or float (mixed method: FP32 descriptors).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,14 +36,22 @@ __device__ __forceinline__ cx<T> cfma(cx<T> a, cx<T> b, cx<T> c) {  // a*b + c
 // decode an encoded half-layer reference: (idx << 2) | (conj << 1) | neg
 template <typename T>
 __device__ __forceinline__ cx<T> fetch(const cx<T>* base, int code) {
-  cx<T> v = base[code >> 2];
-  if (code & 2) v.y = -v.y;
-  if (code & 1) {
-    v.x = -v.x;
-    v.y = -v.y;
-  }
-  return v;
+  const cx<T> v = base[code >> 2];
+  const T sy = (code & 2) ? T(-1) : T(1);
+  const T sn = (code & 1) ? T(-1) : T(1);
+  return {sn * v.x, sn * sy * v.y};
 }
+
+template <typename T>
+struct RecEntry;
+template <>
+struct RecEntry<float> {
+  using type = RecEntry32;
+};
+template <>
+struct RecEntry<double> {
+  using type = RecEntry64;
+};
 
 template <typename T>
 struct NbrGeom {
@@ -115,135 +124,115 @@ __device__ void nbr_geometry(const double* u3, T rcut, T inv_r0, double rin, dou
   for (int a = 0; a < 3; ++a) g->dfr[a] = dfc * drr[a];
 }
 
-template <typename T>
-struct Tabs {
-  const T* tz;
-  const T* tx;
-  const int16_t* sz;
-  const int16_t* sx;
-  const int8_t* qneg;
-  const T* cg;
-};
-
-// Phase-1 recursion of one neighbour by one warp on half layers, U only; accumulates
-// f_c*w_ch*U into cpart[ch*HU + h].
-template <typename T>
-__device__ void warp_u_accumulate(const NbrGeom<T>& g, const Tabs<T>& tb, int J, const int* hoff, const T* wch,
-                                  int nch, cx<T>* ubuf, int LH, cx<T>* cpart, int HU, int lane) {
+// Layer recursion of one neighbour by a group of G lanes (sl = lane within the group) on half
+// layers.  WITH_DU: U and dU, vecall written to V[a*HU + h] (dU of layer j-1 stays raw in V
+// until layer j is formed, then is converted).  Otherwise U only, f_c*w_ch*U added atomically to
+// cpart[ch*HU + h] (the groups of a warp share cpart).  Every group of the warp calls this with
+// the same J so the warp-wide __syncwarp calls line up; inactive groups pass active = false.
+template <typename T, int G, bool WITH_DU>
+__device__ void group_recursion(const NbrGeom<T>& g, const typename RecEntry<T>::type* __restrict__ rec, int J,
+                                const int* hoff, cx<T>* ubuf, int LH, cx<T>* V, cx<T>* cpart, const T* wch, int nch,
+                                int HU, int sl, bool active) {
   cx<T>* prev = ubuf;
   cx<T>* cur = ubuf + LH;
-  if (lane == 0) {
+  if (active && sl == 0) {
     prev[0] = {T(1), T(0)};
-    for (int ch = 0; ch < nch; ++ch) cpart[ch * HU].x += g.fc * wch[ch];
-  }
-  __syncwarp();
-  for (int j = 1; j <= J; ++j) {
-    const int ne = hoff[j + 1] - hoff[j];
-    for (int e = lane; e < ne; e += 32) {
-      const int idx = hoff[j] + e;
-      const T tz = __ldg(tb.tz + idx), tx = __ldg(tb.tx + idx);
-      const int sz = __ldg(tb.sz + idx), sx = __ldg(tb.sx + idx);
-      const bool qn = __ldg(tb.qneg + idx) != 0;
-      const cx<T> Z = qn ? g.zp : g.zm;
-      const cx<T> X = qn ? g.xm : g.xp;
-      cx<T> u = {T(0), T(0)};
-      if (sz >= 0) u = cmul(cx<T>{tz * Z.x, tz * Z.y}, fetch(prev, sz));
-      if (sx >= 0) u = cfma(cx<T>{tx * X.y, -tx * X.x}, fetch(prev, sx), u);  // (-i*tx*X)*U
-      cur[e] = u;
-      for (int ch = 0; ch < nch; ++ch) {
-        const T f = g.fc * wch[ch];
-        cx<T> v = cpart[ch * HU + idx];
-        cpart[ch * HU + idx] = {fma(f, u.x, v.x), fma(f, u.y, v.y)};
-      }
+    if constexpr (WITH_DU) {
+      for (int a = 0; a < 3; ++a) V[a * HU] = {T(0), T(0)};
+    } else {
+      for (int ch = 0; ch < nch; ++ch) atomicAdd(&cpart[ch * HU].x, g.fc * wch[ch]);
     }
-    __syncwarp();
-    cx<T>* t = prev;
-    prev = cur;
-    cur = t;
-  }
-}
-
-// Phase-3 recursion of one neighbour by one warp on half layers: U and dU, writing vecall into
-// V[a*HU + h].  dU of layer j-1 stays raw in V until layer j is formed, then is converted.
-template <typename T>
-__device__ void warp_u_du_vecall(const NbrGeom<T>& g, const Tabs<T>& tb, int J, const int* hoff, cx<T>* ubuf,
-                                 int LH, cx<T>* V, int HU, int lane) {
-  cx<T>* prev = ubuf;
-  cx<T>* cur = ubuf + LH;
-  if (lane == 0) {
-    prev[0] = {T(1), T(0)};
-    for (int a = 0; a < 3; ++a) V[a * HU] = {T(0), T(0)};
   }
   __syncwarp();
   for (int j = 1; j <= J; ++j) {
-    const int ne = hoff[j + 1] - hoff[j];
+    const int h0 = hoff[j], ne = hoff[j + 1] - h0;
     const int pbase = hoff[j - 1];
-    for (int e = lane; e < ne; e += 32) {
-      const int idx = hoff[j] + e;
-      const T tz = __ldg(tb.tz + idx), tx = __ldg(tb.tx + idx);
-      const int sz = __ldg(tb.sz + idx), sx = __ldg(tb.sx + idx);
-      const bool qn = __ldg(tb.qneg + idx) != 0;
-      const cx<T> Z = qn ? g.zp : g.zm;
-      const cx<T> X = qn ? g.xm : g.xp;
-      const cx<T> A = {tz * Z.x, tz * Z.y};
-      const cx<T> Bc = {tx * X.y, -tx * X.x};
-      cx<T> u = {T(0), T(0)};
-      cx<T> du[3] = {{T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}};
-      if (sz >= 0) {
-        const cx<T> Uz = fetch(prev, sz);
-        u = cmul(A, Uz);
+    if (active) {
+      for (int e = sl; e < ne; e += G) {
+        const int idx = h0 + e;
+        const auto r = rec[idx];
+        const T tz = (T)r.tz, tx = (T)r.tx;
+        const int sz = r.sz, sx = r.sx;
+        const bool qn = r.qneg != 0;
+        const cx<T> Z = qn ? g.zp : g.zm;
+        const cx<T> X = qn ? g.xm : g.xp;
+        const cx<T> A = {tz * Z.x, tz * Z.y};
+        const cx<T> Bc = {tx * X.y, -tx * X.x};  // -i*tx*X
+        cx<T> u = {T(0), T(0)};
+        if constexpr (WITH_DU) {
+          cx<T> du[3] = {{T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}};
+          if (sz >= 0) {
+            const cx<T> Uz = fetch(prev, sz);
+            u = cmul(A, Uz);
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          const cx<T> dZ = qn ? g.dzp[a] : g.dzm[a];
-          du[a] = cfma(A, fetch(V + a * HU + pbase, sz), cmul(cx<T>{tz * dZ.x, tz * dZ.y}, Uz));
+            for (int a = 0; a < 3; ++a) {
+              const cx<T> dZ = qn ? g.dzp[a] : g.dzm[a];
+              du[a] = cfma(A, fetch(V + a * HU + pbase, sz), cmul(cx<T>{tz * dZ.x, tz * dZ.y}, Uz));
+            }
+          }
+          if (sx >= 0) {
+            const cx<T> Ux = fetch(prev, sx);
+            u = cfma(Bc, Ux, u);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+              const cx<T> dX = qn ? g.dxm[a] : g.dxp[a];
+              du[a] = cfma(Bc, fetch(V + a * HU + pbase, sx), cfma(cx<T>{tx * dX.y, -tx * dX.x}, Ux, du[a]));
+            }
+          }
+#pragma unroll
+          for (int a = 0; a < 3; ++a) V[a * HU + idx] = du[a];
+        } else {
+          if (sz >= 0) u = cmul(A, fetch(prev, sz));
+          if (sx >= 0) u = cfma(Bc, fetch(prev, sx), u);
+          for (int ch = 0; ch < nch; ++ch) {
+            const T f = g.fc * wch[ch];
+            atomicAdd(&cpart[ch * HU + idx].x, f * u.x);
+            atomicAdd(&cpart[ch * HU + idx].y, f * u.y);
+          }
         }
+        cur[e] = u;
       }
-      if (sx >= 0) {
-        const cx<T> Ux = fetch(prev, sx);
-        u = cfma(Bc, Ux, u);
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          const cx<T> dX = qn ? g.dxm[a] : g.dxp[a];
-          du[a] = cfma(Bc, fetch(V + a * HU + pbase, sx), cfma(cx<T>{tx * dX.y, -tx * dX.x}, Ux, du[a]));
-        }
-      }
-      cur[e] = u;
-#pragma unroll
-      for (int a = 0; a < 3; ++a) V[a * HU + idx] = du[a];
     }
     __syncwarp();
-    const int np = hoff[j] - hoff[j - 1];
-    for (int e = lane; e < np; e += 32) {
-      const cx<T> U = prev[e];
+    if constexpr (WITH_DU) {
+      if (active) {
+        const int np = h0 - pbase;
+        for (int e = sl; e < np; e += G) {
+          const cx<T> U = prev[e];
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const cx<T> d = V[a * HU + pbase + e];
-        V[a * HU + pbase + e] = {fma(U.x, g.dfr[a], g.fc * d.x), fma(-U.y, g.dfr[a], -g.fc * d.y)};
+          for (int a = 0; a < 3; ++a) {
+            const cx<T> d = V[a * HU + pbase + e];
+            V[a * HU + pbase + e] = {fma(U.x, g.dfr[a], g.fc * d.x), fma(-U.y, g.dfr[a], -g.fc * d.y)};
+          }
+        }
       }
+      __syncwarp();
     }
-    __syncwarp();
     cx<T>* t = prev;
     prev = cur;
     cur = t;
   }
-  {
-    const int np = hoff[J + 1] - hoff[J];
-    for (int e = lane; e < np; e += 32) {
-      const cx<T> U = prev[e];
+  if constexpr (WITH_DU) {
+    if (active) {
+      const int np = hoff[J + 1] - hoff[J];
+      for (int e = sl; e < np; e += G) {
+        const cx<T> U = prev[e];
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const cx<T> d = V[a * HU + hoff[J] + e];
-        V[a * HU + hoff[J] + e] = {fma(U.x, g.dfr[a], g.fc * d.x), fma(-U.y, g.dfr[a], -g.fc * d.y)};
+        for (int a = 0; a < 3; ++a) {
+          const cx<T> d = V[a * HU + hoff[J] + e];
+          V[a * HU + hoff[J] + e] = {fma(U.x, g.dfr[a], g.fc * d.x), fma(-U.y, g.dfr[a], -g.fc * d.y)};
+        }
       }
     }
+    __syncwarp();
   }
-  __syncwarp();
 }
 
 template <typename T>
 struct KernelArgs {
   DevTables tb;
-  Tabs<T> t;
+  const typename RecEntry<T>::type* rec;
+  const T* cg;
   // batch
   const int* atom_struct;
   const int* atom_start;
@@ -259,29 +248,33 @@ struct KernelArgs {
   const long long* rowS;
   int D, ldx;
   int want_rows;
-  int NB;  // neighbours per phase-3 chunk
+  int NB;  // neighbours per phase-3 chunk (2 per warp)
   BsoParams p;
 };
 
-template <typename T, int NW>
-__global__ void __launch_bounds__(NW * 32) k_bso4(KernelArgs<T> args, T* __restrict__ X, T* __restrict__ Bout,
-                                                   T* __restrict__ dBout, int A) {
+constexpr int kNW = 8;           // warps per CTA (kNW*32 == kZThreads)
+constexpr int kG1 = 8;           // lanes per neighbour in phase 1
+constexpr int kG3 = 16;          // lanes per neighbour in phase 3
+
+template <typename T>
+__global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __restrict__ X, T* __restrict__ Bout,
+                                                    T* __restrict__ dBout, int A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const DevTables& tb = args.tb;
   const int J = tb.J, NU = tb.NU, HU = tb.HU, K = tb.K, NYP = tb.NYP;
   const int nch = args.p.nch;
   const int NB = args.NB;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  constexpr int nth = NW * 32;
+  constexpr int nth = kNW * 32;
   const int LH = tb.hoff[J + 1] - tb.hoff[J];  // largest half layer
 
   // shared-memory carve-up
   cx<T>* cfull = reinterpret_cast<cx<T>*>(smem_raw);              // nch*NU
   cx<T>* Y = cfull + nch * NU;                                      // nch*NYP
-  cx<T>* V = Y + (size_t)nch * NYP;                                 // max(NB*3, NW*nch)*HU
-  const size_t vblock = (size_t)max(NB * 3, NW * nch) * HU;
-  cx<T>* ubuf = V + vblock;                                         // NW*2*LH
-  T* dBs = reinterpret_cast<T*>(ubuf + (size_t)NW * 2 * LH);        // 3*NB*K  [col][k]
+  cx<T>* V = Y + (size_t)nch * NYP;                                 // max(NB*3, kNW*nch)*HU
+  const size_t vblock = (size_t)max(NB * 3, kNW * nch) * HU;
+  cx<T>* ubuf = V + vblock;                                         // (32/kG1)*kNW*2*LH
+  T* dBs = reinterpret_cast<T*>(ubuf + (size_t)(32 / kG1) * kNW * 2 * LH);  // 3*NB*K  [col][k]
   T* Bk = dBs + (size_t)3 * NB * K;                                 // nch*K
   T* selfacc = Bk + nch * K;                                        // nch*3*K
   T* stacc = selfacc + nch * 3 * K;                                 // nch*6*K
@@ -304,30 +297,36 @@ __global__ void __launch_bounds__(NW * 32) k_bso4(KernelArgs<T> args, T* __restr
     const int a0 = args.atom_start[s];
     const int ldx = args.ldx;
 
-    // ---------------- phase 1: c^j on half layers ----------------------------------
-    for (int e = tid; e < NW * nch * HU; e += nth) V[e] = {T(0), T(0)};
+    // ---------------- phase 1: c^j on half layers, 8 lanes per neighbour --------------
+    for (int e = tid; e < kNW * nch * HU; e += nth) V[e] = {T(0), T(0)};
     for (int e = tid; e < nch * K * 10; e += nth) Bk[e] = T(0);  // Bk, selfacc, stacc
+    for (int e = tid; e < nch * NYP; e += nth) Y[e] = {T(0), T(0)};
     __syncthreads();
     {
+      constexpr int GPW = 32 / kG1;  // groups per warp
+      const int grp = lane / kG1, sl = lane % kG1;
       cx<T>* cpart = V + (size_t)warp * nch * HU;
-      cx<T>* ub = ubuf + (size_t)warp * 2 * LH;
-      for (int n = warp; n < nn; n += NW) {
+      cx<T>* ub = ubuf + (size_t)(warp * GPW + grp) * 2 * LH;
+      for (int nb0 = warp * GPW; nb0 < nn; nb0 += kNW * GPW) {
+        const int n = nb0 + grp;
+        const bool active = n < nn;
         NbrGeom<T> g;
-        const int nb = args.nbr_idx[p0 + n];
-        const int tn = args.types[nb];
-        const double rin = args.p.has_rin ? args.p.rin[ti * args.p.ntypes + tn] : 0.0;
-        nbr_geometry<T>(args.nbr_u + 3 * (size_t)(p0 + n), rcut, inv_r0, rin, args.p.rin_width, &g);
-        T wch[kMaxCh];
-        for (int ch = 0; ch < nch; ++ch) wch[ch] = (T)args.p.chw[ch * args.p.ntypes + tn];
-        warp_u_accumulate<T>(g, args.t, J, tb.hoff, wch, nch, ub, LH, cpart, HU, lane);
+        T wch[kMaxCh] = {T(0), T(0), T(0)};
+        if (active) {
+          const int nb = args.nbr_idx[p0 + n];
+          const int tn = args.types[nb];
+          const double rin = args.p.has_rin ? args.p.rin[ti * args.p.ntypes + tn] : 0.0;
+          nbr_geometry<T>(args.nbr_u + 3 * (size_t)(p0 + n), rcut, inv_r0, rin, args.p.rin_width, &g);
+          for (int ch = 0; ch < nch; ++ch) wch[ch] = (T)args.p.chw[ch * args.p.ntypes + tn];
+        }
+        group_recursion<T, kG1, false>(g, args.rec, J, tb.hoff, ub, LH, nullptr, cpart, wch, nch, HU, sl, active);
       }
     }
     __syncthreads();
-    // reduce the warp partials (each thread owns element e of every warp block, so writing
-    // the sum back into warp 0's block is race free), then expand to full layers
+    // reduce the warp partials into warp 0's block (thread-owned elements), expand to full layers
     for (int e = tid; e < nch * HU; e += nth) {
       cx<T> v = {T(0), T(0)};
-      for (int w = 0; w < NW; ++w) {
+      for (int w = 0; w < kNW; ++w) {
         const cx<T> q = V[(size_t)w * nch * HU + e];
         v.x += q.x;
         v.y += q.y;
@@ -342,52 +341,41 @@ __global__ void __launch_bounds__(NW * 32) k_bso4(KernelArgs<T> args, T* __restr
     }
     __syncthreads();
 
-    // ---------------- phase 2: folded Z -> Y, B --------------------------------------
-    for (int t = tid; t < tb.NS; t += nth) {
-      const int sidx = tb.yorder[t];
-      const YSlot sl = tb.yslots[sidx];
-      for (int ch = 0; ch < nch; ++ch) {
-        const cx<T>* cc = cfull + ch * NU;
-        cx<T> acc = {T(0), T(0)};
-        for (int tt = 0; tt < sl.nterm; ++tt) {
-          const ZTerm z = tb.zterms[sl.term[tt]];
+    // ---------------- phase 2: folded Z -> Y, B on the balanced schedule ---------------
+    {
+      const int i0 = tb.zitem_off[tid], i1 = tb.zitem_off[tid + 1];
+      for (int it = i0; it < i1; ++it) {
+        const ZItem zi = tb.zitems[it];
+        const ZTerm z = tb.zterms[zi.zt];
+        const T sc = (T)zi.snum / (T)zi.sden * (T)zi.wgt;
+        for (int ch = 0; ch < nch; ++ch) {
+          const cx<T>* cc = cfull + ch * NU;
           cx<T> zs = {T(0), T(0)};
           int i1a = z.i1, i2a = z.i2;
           for (int a = 0; a < z.na; ++a) {
-            const T c1 = __ldg(args.t.cg + z.cg1 + a);
+            const T c1 = __ldg(args.cg + z.cg1 + a);
             cx<T> part = {T(0), T(0)};
-            int i1 = i1a, i2 = i2a;
+            const T* cg2 = args.cg + z.cg2;
+#pragma unroll 3
             for (int b = 0; b < z.nb; ++b) {
-              const T c2 = __ldg(args.t.cg + z.cg2 + b);
-              const cx<T> pr = cmul(cc[i1], cc[i2]);
+              const cx<T> pr = cmul(cc[i1a + b], cc[i2a - b]);
+              const T c2 = __ldg(cg2 + b);
               part.x = fma(c2, pr.x, part.x);
               part.y = fma(c2, pr.y, part.y);
-              ++i1;
-              --i2;
             }
             zs.x = fma(c1, part.x, zs.x);
             zs.y = fma(c1, part.y, zs.y);
             i1a += z.s1;
             i2a -= z.s2;
           }
-          if (tt == 0 && sl.is_a) {
-            const cx<T> cv = cc[sl.ufull];
-            atomicAdd(&Bk[ch * K + sl.k], (T)sl.wgt * (cv.x * zs.x + cv.y * zs.y));  // w * Re(conj(c) ZA)
+          if (zi.is_a) {
+            const cx<T> cv = cc[zi.ufull];
+            atomicAdd(&Bk[ch * K + zi.k], (T)zi.wgt * (cv.x * zs.x + cv.y * zs.y));  // w * Re(conj(c) ZA)
           }
-          const T sc = (T)z.snum / (T)z.sden;
-          acc.x = fma(sc, zs.x, acc.x);
-          acc.y = fma(sc, zs.y, acc.y);
+          cx<T>* yp = Y + (size_t)ch * NYP + zi.ypos;
+          atomicAdd(&yp->x, sc * zs.x);
+          atomicAdd(&yp->y, sc * zs.y);
         }
-        Y[(size_t)ch * NYP + sl.ypos] = {(T)sl.wgt * acc.x, (T)sl.wgt * acc.y};
-      }
-    }
-    // padding rows of the layer blocks must be zero
-    for (int j = 0; j <= J; ++j) {
-      const int Mp = tb.Mp[j], H = tb.hoff[j + 1] - tb.hoff[j];
-      for (int e = tid; e < Mp * H; e += nth) {
-        const int r = e % Mp;
-        if (tb.rowk[tb.rowk_off[j] + r] < 0)
-          for (int ch = 0; ch < nch; ++ch) Y[(size_t)ch * NYP + tb.yoff[j] + e] = {T(0), T(0)};
       }
     }
     __syncthreads();
@@ -402,28 +390,36 @@ __global__ void __launch_bounds__(NW * 32) k_bso4(KernelArgs<T> args, T* __restr
     }
 
     // ---------------- phase 3: dB per neighbour chunk, scattered into rows -----------
-    for (int base = 0; base < nn; base += NB) {
-      const int nb_here = min(NB, nn - base);
-      for (int n = warp; n < nb_here; n += NW) {
+    const int nchunk = (nn + NB - 1) / NB;
+    const int csz = (nn + nchunk - 1) / nchunk;  // balanced chunk size <= NB
+    for (int base = 0; base < nn; base += csz) {
+      const int nb_here = min(csz, nn - base);
+      {
+        constexpr int GPW = 32 / kG3;
+        const int grp = lane / kG3, sl = lane % kG3;
+        const int n = warp * GPW + grp;  // NB = kNW*GPW
+        const bool active = n < nb_here;
         NbrGeom<T> g;
-        const int nbi = args.nbr_idx[p0 + base + n];
-        const int tn = args.types[nbi];
-        const double rin = args.p.has_rin ? args.p.rin[ti * args.p.ntypes + tn] : 0.0;
-        const double* u3 = args.nbr_u + 3 * (size_t)(p0 + base + n);
-        nbr_geometry<T>(u3, rcut, inv_r0, rin, args.p.rin_width, &g);
-        warp_u_du_vecall<T>(g, args.t, J, tb.hoff, ubuf + (size_t)warp * 2 * LH, LH, V + (size_t)n * 3 * HU, HU,
-                            lane);
-        if (lane == 0) {
-          for (int ch = 0; ch < nch; ++ch) nwt[ch * NB + n] = (T)args.p.chw[ch * args.p.ntypes + tn];
-          nidx[n] = nbi;
-          const double r = sqrt(u3[0] * u3[0] + u3[1] * u3[1] + u3[2] * u3[2]);
-          // stress lever arm: x_n - x_i (small box) or sign_big*(x_i - x_n) (large box)
-          const double sg = args.small[s] ? 1.0 : -args.p.sign_big;
-          nuu[n * 4 + 0] = (T)(sg * u3[0]);
-          nuu[n * 4 + 1] = (T)(sg * u3[1]);
-          nuu[n * 4 + 2] = (T)(sg * u3[2]);
-          nuu[n * 4 + 3] = (T)(1.0 / r);
+        const double* u3 = args.nbr_u + 3 * (size_t)(p0 + base + min(n, nb_here - 1));
+        if (active) {
+          const int nbi = args.nbr_idx[p0 + base + n];
+          const int tn = args.types[nbi];
+          const double rin = args.p.has_rin ? args.p.rin[ti * args.p.ntypes + tn] : 0.0;
+          nbr_geometry<T>(u3, rcut, inv_r0, rin, args.p.rin_width, &g);
+          if (sl == 0) {
+            for (int ch = 0; ch < nch; ++ch) nwt[ch * NB + n] = (T)args.p.chw[ch * args.p.ntypes + tn];
+            nidx[n] = nbi;
+            const double r = sqrt(u3[0] * u3[0] + u3[1] * u3[1] + u3[2] * u3[2]);
+            // stress lever arm: x_n - x_i (small box) or sign_big*(x_i - x_n) (large box)
+            const double sg = args.small[s] ? 1.0 : -args.p.sign_big;
+            nuu[n * 4 + 0] = (T)(sg * u3[0]);
+            nuu[n * 4 + 1] = (T)(sg * u3[1]);
+            nuu[n * 4 + 2] = (T)(sg * u3[2]);
+            nuu[n * 4 + 3] = (T)(1.0 / r);
+          }
         }
+        group_recursion<T, kG3, true>(g, args.rec, J, tb.hoff, ubuf + (size_t)(warp * GPW + grp) * 2 * LH, LH,
+                                      V + (size_t)min(n, NB - 1) * 3 * HU, nullptr, nullptr, nch, HU, sl, active);
       }
       const int ncols = 3 * nb_here;
       const int ncolt = (ncols + kColTile - 1) / kColTile;
@@ -451,6 +447,7 @@ __global__ void __launch_bounds__(NW * 32) k_bso4(KernelArgs<T> args, T* __restr
           for (int r = 0; r < kRowTile; ++r)
 #pragma unroll
             for (int c = 0; c < kColTile; ++c) acc[r][c] = T(0);
+#pragma unroll 2
           for (int e = 0; e < H; ++e) {
             cx<T> y[kRowTile], v[kColTile];
 #pragma unroll
@@ -472,15 +469,12 @@ __global__ void __launch_bounds__(NW * 32) k_bso4(KernelArgs<T> args, T* __restr
           }
         }
         __syncthreads();
-        // neighbour weights of this channel
-        for (int e = tid; e < ncols * K; e += nth) dBs[e] *= nwt[ch * NB + e / (3 * K)];
-        __syncthreads();
         // scatter: neighbour force rows (atomic), self force and stress accumulators
         for (int it = tid; it < 3 * K; it += nth) {
           const int a = it / K, k = it - a * K;
           T self = selfacc[ch * 3 * K + it];
           for (int n = 0; n < nb_here; ++n) {
-            const T v = dBs[(n * 3 + a) * K + k];
+            const T v = dBs[(n * 3 + a) * K + k] * nwt[ch * NB + n];
             self += v;
             if (rF >= 0) {
               const long long row = rF + 3LL * (nidx[n] - a0) + a;
@@ -496,7 +490,8 @@ __global__ void __launch_bounds__(NW * 32) k_bso4(KernelArgs<T> args, T* __restr
             const int aa = sidx < 3 ? sidx : (sidx == 3 ? 1 : 0);
             const int bb = sidx < 3 ? sidx : (sidx == 5 ? 1 : 2);
             T acc = stacc[ch * 6 * K + it];
-            for (int n = 0; n < nb_here; ++n) acc += dBs[(n * 3 + aa) * K + k] * nuu[n * 4 + bb] * nuu[n * 4 + 3];
+            for (int n = 0; n < nb_here; ++n)
+              acc += dBs[(n * 3 + aa) * K + k] * nwt[ch * NB + n] * nuu[n * 4 + bb] * nuu[n * 4 + 3];
             stacc[ch * 6 * K + it] = acc;
           }
         }
@@ -524,11 +519,11 @@ __global__ void __launch_bounds__(NW * 32) k_bso4(KernelArgs<T> args, T* __restr
   }
 }
 
-static size_t smem_bytes(const DevTables& tb, int nch, int eb, int NW, int NB) {
+static size_t smem_bytes(const DevTables& tb, int nch, int eb, int NB) {
   const size_t LH = tb.hoff[tb.J + 1] - tb.hoff[tb.J];
   const size_t cxb = 2 * (size_t)eb;
-  const size_t vblock = (size_t)std::max(NB * 3, NW * nch) * tb.HU;
-  size_t b = cxb * ((size_t)nch * tb.NU + (size_t)nch * tb.NYP + vblock + (size_t)NW * 2 * LH);
+  const size_t vblock = (size_t)std::max(NB * 3, kNW * nch) * tb.HU;
+  size_t b = cxb * ((size_t)nch * tb.NU + (size_t)nch * tb.NYP + vblock + (size_t)(32 / kG1) * kNW * 2 * LH);
   b += (size_t)eb * ((size_t)3 * NB * tb.K + (size_t)nch * 10 * tb.K + (size_t)nch * NB + (size_t)NB * 4);
   b += sizeof(int) * NB;
   return b;
@@ -537,23 +532,17 @@ static size_t smem_bytes(const DevTables& tb, int nch, int eb, int NW, int NB) {
 template <typename T>
 cudaError_t launch_bso4_rows(const DevTables& tb, const DevBatch& b, const DevRows& rows, const BsoParams& p, T* X,
                              T* Bout, T* dBout, int want_rows, cudaStream_t st) {
-  constexpr int NW = 8;
-  const int NB = sizeof(T) == 8 ? 8 : 16;
+  const int NB = kNW * (32 / kG3);
   if (b.A == 0) return cudaSuccess;
   KernelArgs<T> a{};
   a.tb = tb;
   if constexpr (sizeof(T) == 8) {
-    a.t.tz = reinterpret_cast<const T*>(tb.rec_tz64);
-    a.t.tx = reinterpret_cast<const T*>(tb.rec_tx64);
-    a.t.cg = reinterpret_cast<const T*>(tb.cg64);
+    a.rec = reinterpret_cast<const RecEntry64*>(tb.rec64);
+    a.cg = reinterpret_cast<const T*>(tb.cg64);
   } else {
-    a.t.tz = reinterpret_cast<const T*>(tb.rec_tz32);
-    a.t.tx = reinterpret_cast<const T*>(tb.rec_tx32);
-    a.t.cg = reinterpret_cast<const T*>(tb.cg32);
+    a.rec = reinterpret_cast<const RecEntry32*>(tb.rec32);
+    a.cg = reinterpret_cast<const T*>(tb.cg32);
   }
-  a.t.sz = tb.rec_sz;
-  a.t.sx = tb.rec_sx;
-  a.t.qneg = tb.rec_qneg;
   a.atom_struct = b.atom_struct;
   a.atom_start = b.atom_start;
   a.types = b.types;
@@ -570,13 +559,13 @@ cudaError_t launch_bso4_rows(const DevTables& tb, const DevBatch& b, const DevRo
   a.want_rows = want_rows;
   a.NB = NB;
   a.p = p;
-  size_t smem = smem_bytes(tb, p.nch, sizeof(T), NW, NB);
-  cudaError_t e = cudaFuncSetAttribute(k_bso4<T, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  size_t smem = smem_bytes(tb, p.nch, sizeof(T), NB);
+  cudaError_t e = cudaFuncSetAttribute(k_bso4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bso4<T, NW>, NW * 32, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bso4<T>, kNW * 32, smem);
   if (occ < 1) return cudaErrorInvalidConfiguration;
-  k_bso4<T, NW><<<b.A, NW * 32, smem, st>>>(a, X, Bout, dBout, b.A);
+  k_bso4<T><<<b.A, kNW * 32, smem, st>>>(a, X, Bout, dBout, b.A);
   return cudaGetLastError();
 }
 

@@ -254,6 +254,43 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
   // row tiles of the dB contraction, heaviest layers first
   for (int j = J; j >= 0; --j)
     for (int rt = 0; rt < t->Mp[j] / kRowTile; ++rt) t->tiles.push_back((j << 8) | rt);
+
+  // phase-2 schedule: every (slot, term) is one item; longest-processing-time-first assignment
+  // of items to kZThreads threads, so that each thread's total CG work is nearly equal.
+  {
+    struct It { ZItem z; long long cost; };
+    std::vector<It> items;
+    for (const YSlot& s : t->yslots)
+      for (int tt = 0; tt < s.nterm; ++tt) {
+        const ZTerm& z = t->zterms[s.term[tt]];
+        ZItem zi{};
+        zi.zt = s.term[tt];
+        zi.ypos = s.ypos;
+        zi.ufull = s.ufull;
+        zi.k = s.k;
+        zi.snum = z.snum;
+        zi.sden = z.sden;
+        zi.wgt = s.wgt;
+        zi.is_a = (tt == 0 && s.is_a) ? 1 : 0;
+        items.push_back({zi, (long long)z.na * z.nb + 4});
+      }
+    std::stable_sort(items.begin(), items.end(), [](const It& a, const It& b) { return a.cost > b.cost; });
+    std::vector<long long> load(kZThreads, 0);
+    std::vector<std::vector<ZItem>> per(kZThreads);
+    for (const It& it : items) {
+      int best = 0;
+      for (int th = 1; th < kZThreads; ++th)
+        if (load[th] < load[best]) best = th;
+      load[best] += it.cost;
+      per[best].push_back(it.z);
+    }
+    t->zitem_off.assign(kZThreads + 1, 0);
+    for (int th = 0; th < kZThreads; ++th) {
+      t->zitem_off[th] = (int)t->zitems.size();
+      t->zitems.insert(t->zitems.end(), per[th].begin(), per[th].end());
+    }
+    t->zitem_off[kZThreads] = (int)t->zitems.size();
+  }
   return true;
 }
 

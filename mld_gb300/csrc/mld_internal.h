@@ -43,8 +43,35 @@ struct YSlot {
   uint8_t pad;
 };
 
+// One Z-term work item of the balanced phase-2 schedule: term `zt` of the slot at `ypos`.
+struct ZItem {
+  uint16_t zt;             // ZTerm index
+  uint16_t ypos;           // Y position of its slot
+  uint16_t ufull;          // c index of the slot's (j,p,q) (for B)
+  uint16_t k;              // triple
+  uint8_t snum, sden, wgt, is_a;  // scale, fold weight, ZA flag
+  uint32_t pad;
+};
+
+// Packed per-entry recursion record of the half layers (one 16-byte load per entry).
+struct RecEntry32 {
+  float tz, tx;
+  int16_t sz, sx;
+  int32_t qneg;
+};
+struct RecEntry64 {
+  double tz, tx;
+  int16_t sz, sx;
+  int32_t qneg;
+  int64_t pad;
+};
+
+constexpr int kZThreads = 256;  // threads of the phase-2 schedule (= CTA size of k_bso4)
+
 // Host-built constant tables of the SO(4) bispectrum for a given j_max.
 struct Bso4Tables {
+  std::vector<ZItem> zitems;    // phase-2 work, grouped per thread (LPT-balanced)
+  std::vector<int> zitem_off;   // kZThreads + 1 offsets into zitems
   int J = 0, NU = 0, HU = 0, K = 0, NYP = 0;
   int off[kMaxJ + 2] = {0};     // full-layer offsets
   int hoff[kMaxJ + 2] = {0};    // half-layer offsets
@@ -95,7 +122,21 @@ struct DevTables {
   int8_t* rec_qneg = nullptr;
   int16_t* expand = nullptr;
   int8_t* half_diag = nullptr;
+  RecEntry32* rec32 = nullptr;  // packed recursion records (FP32 method)
+  RecEntry64* rec64 = nullptr;  // packed recursion records (FP64 method)
+  ZItem* zitems = nullptr;
+  int* zitem_off = nullptr;     // kZThreads + 1
 };
+
+// Packed recursion records from the table vectors.
+inline void pack_recursion(const Bso4Tables& t, std::vector<RecEntry32>* r32, std::vector<RecEntry64>* r64) {
+  r32->resize(t.HU);
+  r64->resize(t.HU);
+  for (int h = 0; h < t.HU; ++h) {
+    (*r32)[h] = RecEntry32{(float)t.rec_tz[h], (float)t.rec_tx[h], t.rec_sz[h], t.rec_sx[h], (int32_t)t.rec_qneg[h]};
+    (*r64)[h] = RecEntry64{t.rec_tz[h], t.rec_tx[h], t.rec_sz[h], t.rec_sx[h], (int32_t)t.rec_qneg[h], 0};
+  }
+}
 
 // Per-batch structure description on the device.
 struct DevBatch {

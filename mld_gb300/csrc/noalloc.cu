@@ -124,6 +124,13 @@ int noalloc_setup(int dev, double j_max, DeviceState** out, std::string* msg) {
     PUT(t.rec_qneg, d.rec_qneg);
     PUT(t.expand, d.expand);
     PUT(t.half_diag, d.half_diag);
+    std::vector<RecEntry32> r32;
+    std::vector<RecEntry64> r64;
+    pack_recursion(t, &r32, &r64);
+    PUT(r32, d.rec32);
+    PUT(r64, d.rec64);
+    PUT(t.zitems, d.zitems);
+    PUT(t.zitem_off, d.zitem_off);
 #undef PUT
     if (e != cudaSuccess) {
       *msg = std::string("table upload into the scratch array: ") + cudaGetErrorString(e);
