@@ -132,7 +132,7 @@ __device__ void nbr_geometry(const double* u3, T rcut, T inv_r0, double rin, dou
 template <typename T, int G, bool WITH_DU>
 __device__ void group_recursion(const NbrGeom<T>& g, const typename RecEntry<T>::type* __restrict__ rec, int J,
                                 const int* hoff, cx<T>* ubuf, int LH, cx<T>* V, cx<T>* cpart, const T* wch, int nch,
-                                int HU, int sl, bool active) {
+                                int HU, int sl, bool active, bool private_part = false) {
   cx<T>* prev = ubuf;
   cx<T>* cur = ubuf + LH;
   if (active && sl == 0) {
@@ -140,7 +140,10 @@ __device__ void group_recursion(const NbrGeom<T>& g, const typename RecEntry<T>:
     if constexpr (WITH_DU) {
       for (int a = 0; a < 3; ++a) V[a * HU] = {T(0), T(0)};
     } else {
-      for (int ch = 0; ch < nch; ++ch) atomicAdd(&cpart[ch * HU].x, g.fc * wch[ch]);
+      for (int ch = 0; ch < nch; ++ch) {
+        if (private_part) cpart[ch * HU].x += g.fc * wch[ch];
+        else atomicAdd(&cpart[ch * HU].x, g.fc * wch[ch]);
+      }
     }
   }
   __syncwarp();
@@ -186,8 +189,13 @@ __device__ void group_recursion(const NbrGeom<T>& g, const typename RecEntry<T>:
           if (sx >= 0) u = cfma(Bc, fetch(prev, sx), u);
           for (int ch = 0; ch < nch; ++ch) {
             const T f = g.fc * wch[ch];
-            atomicAdd(&cpart[ch * HU + idx].x, f * u.x);
-            atomicAdd(&cpart[ch * HU + idx].y, f * u.y);
+            if (private_part) {
+              cx<T> v = cpart[ch * HU + idx];
+              cpart[ch * HU + idx] = {fma(f, u.x, v.x), fma(f, u.y, v.y)};
+            } else {
+              atomicAdd(&cpart[ch * HU + idx].x, f * u.x);
+              atomicAdd(&cpart[ch * HU + idx].y, f * u.y);
+            }
           }
         }
         cur[e] = u;
@@ -298,14 +306,17 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
     const int ldx = args.ldx;
 
     // ---------------- phase 1: c^j on half layers, 8 lanes per neighbour --------------
-    for (int e = tid; e < kNW * nch * HU; e += nth) V[e] = {T(0), T(0)};
+    // each lane group accumulates privately when the V block holds one partial per group
+    const bool gpriv = (size_t)32 * nch * HU <= vblock;
+    const int nparts = gpriv ? kNW * (32 / kG1) : kNW;
+    for (int e = tid; e < nparts * nch * HU; e += nth) V[e] = {T(0), T(0)};
     for (int e = tid; e < nch * K * 10; e += nth) Bk[e] = T(0);  // Bk, selfacc, stacc
     for (int e = tid; e < nch * NYP; e += nth) Y[e] = {T(0), T(0)};
     __syncthreads();
     {
       constexpr int GPW = 32 / kG1;  // groups per warp
       const int grp = lane / kG1, sl = lane % kG1;
-      cx<T>* cpart = V + (size_t)warp * nch * HU;
+      cx<T>* cpart = V + (size_t)(gpriv ? warp * GPW + grp : warp) * nch * HU;
       cx<T>* ub = ubuf + (size_t)(warp * GPW + grp) * 2 * LH;
       for (int nb0 = warp * GPW; nb0 < nn; nb0 += kNW * GPW) {
         const int n = nb0 + grp;
@@ -319,14 +330,15 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
           nbr_geometry<T>(args.nbr_u + 3 * (size_t)(p0 + n), rcut, inv_r0, rin, args.p.rin_width, &g);
           for (int ch = 0; ch < nch; ++ch) wch[ch] = (T)args.p.chw[ch * args.p.ntypes + tn];
         }
-        group_recursion<T, kG1, false>(g, args.rec, J, tb.hoff, ub, LH, nullptr, cpart, wch, nch, HU, sl, active);
+        group_recursion<T, kG1, false>(g, args.rec, J, tb.hoff, ub, LH, nullptr, cpart, wch, nch, HU, sl, active,
+                                       gpriv);
       }
     }
     __syncthreads();
     // reduce the warp partials into warp 0's block (thread-owned elements), expand to full layers
     for (int e = tid; e < nch * HU; e += nth) {
       cx<T> v = {T(0), T(0)};
-      for (int w = 0; w < kNW; ++w) {
+      for (int w = 0; w < nparts; ++w) {
         const cx<T> q = V[(size_t)w * nch * HU + e];
         v.x += q.x;
         v.y += q.y;
@@ -342,20 +354,26 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
     __syncthreads();
 
     // ---------------- phase 2: folded Z -> Y, B on the balanced schedule ---------------
+    // a thread owns whole slots (their terms are consecutive items), so Y is stored once
     {
       const int i0 = tb.zitem_off[tid], i1 = tb.zitem_off[tid + 1];
-      for (int it = i0; it < i1; ++it) {
-        const ZItem zi = tb.zitems[it];
-        const ZTerm z = tb.zterms[zi.zt];
-        const T sc = (T)zi.snum / (T)zi.sden * (T)zi.wgt;
-        for (int ch = 0; ch < nch; ++ch) {
-          const cx<T>* cc = cfull + ch * NU;
+      for (int ch = 0; ch < nch; ++ch) {
+        const cx<T>* cc = cfull + ch * NU;
+        cx<T> acc = {T(0), T(0)};
+        int left = 0;
+        for (int it = i0; it < i1; ++it) {
+          const ZItem zi = tb.zitems[it];
+          if (zi.pad) {
+            left = (int)zi.pad;
+            acc = {T(0), T(0)};
+          }
+          const ZTerm z = tb.zterms[zi.zt];
           cx<T> zs = {T(0), T(0)};
           int i1a = z.i1, i2a = z.i2;
+          const T* cg2 = args.cg + z.cg2;
           for (int a = 0; a < z.na; ++a) {
             const T c1 = __ldg(args.cg + z.cg1 + a);
             cx<T> part = {T(0), T(0)};
-            const T* cg2 = args.cg + z.cg2;
 #pragma unroll 3
             for (int b = 0; b < z.nb; ++b) {
               const cx<T> pr = cmul(cc[i1a + b], cc[i2a - b]);
@@ -372,9 +390,10 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
             const cx<T> cv = cc[zi.ufull];
             atomicAdd(&Bk[ch * K + zi.k], (T)zi.wgt * (cv.x * zs.x + cv.y * zs.y));  // w * Re(conj(c) ZA)
           }
-          cx<T>* yp = Y + (size_t)ch * NYP + zi.ypos;
-          atomicAdd(&yp->x, sc * zs.x);
-          atomicAdd(&yp->y, sc * zs.y);
+          const T sc = (T)zi.snum / (T)zi.sden * (T)zi.wgt;
+          acc.x = fma(sc, zs.x, acc.x);
+          acc.y = fma(sc, zs.y, acc.y);
+          if (--left == 0) Y[(size_t)ch * NYP + zi.ypos] = acc;
         }
       }
     }

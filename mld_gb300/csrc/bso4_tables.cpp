@@ -255,12 +255,28 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
   for (int j = J; j >= 0; --j)
     for (int rt = 0; rt < t->Mp[j] / kRowTile; ++rt) t->tiles.push_back((j << 8) | rt);
 
-  // phase-2 schedule: every (slot, term) is one item; longest-processing-time-first assignment
-  // of items to kZThreads threads, so that each thread's total CG work is nearly equal.
+  // phase-2 schedule: one item per slot (all of its terms, so Y is written once without
+  // atomics); longest-processing-time-first assignment of slots to kZThreads threads, so that
+  // each thread's total CG work is nearly equal.  Items of a slot are consecutive: the first
+  // carries the slot's term count in `pad`.
   {
-    struct It { ZItem z; long long cost; };
+    struct It { int slot; long long cost; };
     std::vector<It> items;
-    for (const YSlot& s : t->yslots)
+    for (size_t si = 0; si < t->yslots.size(); ++si) {
+      const YSlot& s = t->yslots[si];
+      long long c = 4;
+      for (int tt = 0; tt < s.nterm; ++tt) c += (long long)t->zterms[s.term[tt]].na * t->zterms[s.term[tt]].nb;
+      items.push_back({(int)si, c});
+    }
+    std::stable_sort(items.begin(), items.end(), [](const It& a, const It& b) { return a.cost > b.cost; });
+    std::vector<long long> load(kZThreads, 0);
+    std::vector<std::vector<ZItem>> per(kZThreads);
+    for (const It& it : items) {
+      int best = 0;
+      for (int th = 1; th < kZThreads; ++th)
+        if (load[th] < load[best]) best = th;
+      load[best] += it.cost;
+      const YSlot& s = t->yslots[it.slot];
       for (int tt = 0; tt < s.nterm; ++tt) {
         const ZTerm& z = t->zterms[s.term[tt]];
         ZItem zi{};
@@ -272,17 +288,9 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
         zi.sden = z.sden;
         zi.wgt = s.wgt;
         zi.is_a = (tt == 0 && s.is_a) ? 1 : 0;
-        items.push_back({zi, (long long)z.na * z.nb + 4});
+        zi.pad = (tt == 0) ? (uint32_t)s.nterm : 0u;
+        per[best].push_back(zi);
       }
-    std::stable_sort(items.begin(), items.end(), [](const It& a, const It& b) { return a.cost > b.cost; });
-    std::vector<long long> load(kZThreads, 0);
-    std::vector<std::vector<ZItem>> per(kZThreads);
-    for (const It& it : items) {
-      int best = 0;
-      for (int th = 1; th < kZThreads; ++th)
-        if (load[th] < load[best]) best = th;
-      load[best] += it.cost;
-      per[best].push_back(it.z);
     }
     t->zitem_off.assign(kZThreads + 1, 0);
     for (int th = 0; th < kZThreads; ++th) {

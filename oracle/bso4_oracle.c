@@ -569,3 +569,72 @@ int orc_rows_batch(int nstruct, const int *nat, const double *pos, const double 
     free(atom0); free(row0);
     return err;
 }
+
+/* Quadratic (mld_order=2, QML full layout) design rows of one structure, D = 1 + KK + KK*KK:
+ *   energy row   [nat, sum_i B_i, sum_i B_i (x) B_i]            (mld_energy.F90:170-266, :364-461;
+ *                index of (id1,id2) = 1 + KK + KK*id1 + id2, 0-based)
+ *   force rows   linear part as orc_rows_linear; quadratic part
+ *                row(atom) -= sum_centres [f(id1) B_c(id2) + f(id2) B_c(id1)] with f the
+ *                post-flip derivative force(:, c, n, :) and B_c the CENTRE's descriptor
+ *                (mld_forces.F90:410-500)
+ *   stress rows  sign_stress*3/V * sum_{i,n} [f(id1) B_nb(id2) + f(id2) B_nb(id1)] uu/r with B_nb
+ *                the NEIGHBOUR's descriptor, as in mld_stress.F90:340-356/:580-603 where
+ *                ik = kind_neigh(ia, ia_n). */
+int orc_rows_quadratic(int nat, int KK, const double *B, const double *dB, const int *nn, const int *nbr,
+                       const double *u, int cap, int is_small, double sign_stress, double sign_big, double volume,
+                       double *rowE, double *rowF, double *rowS) {
+    const int D = 1 + KK + KK * KK;
+    static const int sa[6] = {0, 1, 2, 1, 0, 0}, sb[6] = {0, 1, 2, 2, 2, 1};
+    if (rowE) {
+        memset(rowE, 0, sizeof(double) * D);
+        rowE[0] = (double)nat;
+        for (int i = 0; i < nat; i++) {
+            const double *b = B + (size_t)i * KK;
+            for (int k = 0; k < KK; k++) rowE[1 + k] += b[k];
+            for (int p = 0; p < KK; p++)
+                for (int q = 0; q < KK; q++) rowE[1 + KK + KK * p + q] += b[p] * b[q];
+        }
+    }
+    if (rowF) {
+        memset(rowF, 0, sizeof(double) * (size_t)3 * nat * D);
+        for (int i = 0; i < nat; i++) {
+            const double *bc = B + (size_t)i * KK;
+            for (int n = 0; n < nn[i]; n++) {
+                int ia = nbr[i * cap + n];
+                for (int a = 0; a < 3; a++) {
+                    const double *d = dB + (((size_t)i * cap + n) * 3 + a) * KK;
+                    double *self = rowF + ((size_t)i * 3 + a) * D;
+                    double *other = rowF + ((size_t)ia * 3 + a) * D;
+                    for (int k = 0; k < KK; k++) { self[1 + k] += d[k]; other[1 + k] -= d[k]; }
+                    for (int p = 0; p < KK; p++)
+                        for (int q = 0; q < KK; q++) {
+                            double v = d[p] * bc[q] + d[q] * bc[p];
+                            self[1 + KK + KK * p + q] += v;
+                            other[1 + KK + KK * p + q] -= v;
+                        }
+                }
+            }
+        }
+    }
+    if (rowS) {
+        memset(rowS, 0, sizeof(double) * 6 * D);
+        for (int i = 0; i < nat; i++)
+            for (int n = 0; n < nn[i]; n++) {
+                const double *x = u + ((size_t)i * cap + n) * 3;
+                const double *bn = B + (size_t)nbr[i * cap + n] * KK;
+                double r = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+                double uu[3];
+                for (int c = 0; c < 3; c++) uu[c] = is_small ? x[c] : -sign_big * x[c];
+                for (int s = 0; s < 6; s++) {
+                    const double *d = dB + (((size_t)i * cap + n) * 3 + sa[s]) * KK;
+                    double f = uu[sb[s]] / r;
+                    for (int k = 0; k < KK; k++) rowS[s * D + 1 + k] += d[k] * f;
+                    for (int p = 0; p < KK; p++)
+                        for (int q = 0; q < KK; q++) rowS[s * D + 1 + KK + KK * p + q] += (d[p] * bn[q] + d[q] * bn[p]) * f;
+                }
+            }
+        double sc = sign_stress * 3.0 / volume;
+        for (int s = 0; s < 6; s++) for (int k = 1; k < D; k++) rowS[s * D + k] *= sc;
+    }
+    return 0;
+}
