@@ -19,6 +19,15 @@ template <typename T>
 cudaError_t launch_rows_prep(int S, const int* atom_start, const DevRows& rows, const double* E, const double* F,
                              const double* Sv, const double* wefs, T* X, double* y, double* wrow, int* kind,
                              cudaStream_t st);
+template <typename T>
+cudaError_t launch_quad_rows(const DevBatch& b, const DevRows& rows, const BsoParams& p, int KK, const int* rev,
+                             const T* B, const T* dB, T* H, T* X, int qoff, cudaStream_t st);
+cudaError_t launch_reverse_pairs(const DevBatch& b, int* rev, cudaStream_t st);
+cudaError_t launch_cholesky(double* A, int D, double shift, int* info, cudaStream_t st);
+cudaError_t launch_chol_solve(const double* L, int D, const double* b, double* x, cudaStream_t st);
+cudaError_t launch_residual(const double* G, int D, double lambda, const double* w, const double* h, double* r,
+                            cudaStream_t st);
+cudaError_t launch_axpy(int n, double a, const double* x, double* y, cudaStream_t st);
 }  // namespace mld
 
 using namespace mld;
@@ -46,6 +55,9 @@ struct mld_gpu_handle {
   DevTables dt;
   BsoParams bp;
   int nch = 1, K = 0, KK = 0, D = 0, ldx = 0;
+  // quadratic model (mld_order = 2): linear block DL = 1 + KK, upper-triangle quadratic block DQ
+  bool quad = false;
+  int DL = 0, DQ = 0, Dfull = 0;
   bool mixed = false;
 
   // staged batch
@@ -70,13 +82,14 @@ struct mld_gpu_handle {
   long long calls[MLD_NPHASE] = {0};
 
   std::vector<void*> owned;  // table allocations
-  Buf bufs[40];
+  Buf bufs[48];
   enum {
     B_ATOM_START, B_ATOM_STRUCT, B_TYPES, B_POS, B_CELL, B_RECIP, B_SMALL, B_NSIZE, B_VOL,
     B_NN, B_NBR_OFF, B_NBR_IDX, B_NBR_U, B_SCAN_TMP, B_MAXNN,
     B_E, B_F, B_S, B_WEFS,
     B_ROWE, B_ROWF, B_ROWS, B_X, B_Y, B_WROW, B_KIND,
     B_G, B_H, B_W, B_EVALS, B_INFO, B_SQ, B_PRED, B_BOUT, B_DBOUT,
+    B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
     B_COUNT
   };
 };
@@ -252,10 +265,108 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
   }
   mark(h, MLD_PHASE_ROWS, 1);
   mark(h, MLD_PHASE_DESCRIPTORS, 0);
-  CK(launch_bso4_rows<T>(h->dt, h->b, rows, h->bp, X, (T*)nullptr, (T*)nullptr, 1, h->st));
+  if (!h->quad) {
+    CK(launch_bso4_rows<T>(h->dt, h->b, rows, h->bp, X, (T*)nullptr, (T*)nullptr, 1, h->st));
+  } else {
+    // quadratic rows need every atom's B and every pair's dB (mld_forces.F90:410-500)
+    const size_t nB = (size_t)std::max(1, h->A) * h->KK, nd = (size_t)std::max<long long>(1, h->b.P) * 3 * h->KK;
+    CK(ensure(h, mld_gpu_handle::B_BOUT, sizeof(T) * nB));
+    CK(ensure(h, mld_gpu_handle::B_DBOUT, sizeof(T) * nd));
+    CK(ensure(h, mld_gpu_handle::B_REV, sizeof(int) * (size_t)std::max<long long>(1, h->b.P)));
+    CK(ensure(h, mld_gpu_handle::B_HQ, sizeof(T) * (size_t)std::max(1, h->A) * 6 * h->KK));
+    T* Bq = bp_<T>(h, mld_gpu_handle::B_BOUT);
+    T* dBq = bp_<T>(h, mld_gpu_handle::B_DBOUT);
+    CK(launch_bso4_rows<T>(h->dt, h->b, rows, h->bp, X, Bq, dBq, 1, h->st));
+    CK(launch_reverse_pairs(h->b, bp_<int>(h, mld_gpu_handle::B_REV), h->st));
+    CK(launch_quad_rows<T>(h->b, rows, h->bp, h->KK, bp_<int>(h, mld_gpu_handle::B_REV), Bq, dBq,
+                           bp_<T>(h, mld_gpu_handle::B_HQ), X, h->DL, h->st));
+  }
   mark(h, MLD_PHASE_DESCRIPTORS, 1);
   *Xout = X;
   return MLD_OK;
+}
+
+// Symmetric solve of (G + lambda I) w = rhs: min-norm Jacobi (gelsd semantics) up to
+// kJacobiMax, blocked Cholesky with two FP64 refinement steps above (diagonal shift
+// lambda, or a 1e-12 relative jitter when lambda <= 0).  G is left intact.
+int solve_any(mld_gpu_handle* h, double* G, const double* rhs, int D, double* w) {
+  if (D <= 112) {
+    CK(launch_solve_sym(G, rhs, D, h->cfg.lambda_krr, h->cfg.svd_rcond, w, bp_<double>(h, mld_gpu_handle::B_EVALS),
+                        bp_<int>(h, mld_gpu_handle::B_INFO), h->st));
+    return MLD_OK;
+  }
+  CK(ensure(h, mld_gpu_handle::B_GF, sizeof(double) * (size_t)D * D));
+  CK(ensure(h, mld_gpu_handle::B_RES, sizeof(double) * D));
+  CK(ensure(h, mld_gpu_handle::B_DW, sizeof(double) * D));
+  CK(ensure(h, mld_gpu_handle::B_INFO, sizeof(int) * 4));
+  double* Lf = bp_<double>(h, mld_gpu_handle::B_GF);
+  double* r = bp_<double>(h, mld_gpu_handle::B_RES);
+  double* dw = bp_<double>(h, mld_gpu_handle::B_DW);
+  double shift = h->cfg.lambda_krr > 0 ? h->cfg.lambda_krr : 0.0;
+  if (shift <= 0) {
+    std::vector<double> diag(D);
+    CK(cudaMemcpy2DAsync(diag.data(), sizeof(double), G, sizeof(double) * (D + 1), sizeof(double), D,
+                         cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    double mx = 0;
+    for (double v : diag) mx = std::max(mx, std::fabs(v));
+    shift = 1e-12 * (mx > 0 ? mx : 1.0);
+  }
+  CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)D * D, cudaMemcpyDeviceToDevice, h->st));
+  int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
+  CK(launch_cholesky(Lf, D, shift, info, h->st));
+  CK(launch_chol_solve(Lf, D, rhs, w, h->st));
+  for (int it = 0; it < 2; ++it) {
+    CK(launch_residual(G, D, shift, w, rhs, r, h->st));
+    CK(launch_chol_solve(Lf, D, r, dw, h->st));
+    CK(launch_axpy(D, 1.0, dw, w, h->st));
+  }
+  int hinfo = 0;
+  CK(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (hinfo != 0)
+    return fail(h, MLD_ERR_SOLVE, "normal matrix not positive definite at column " + std::to_string(hinfo));
+  return MLD_OK;
+}
+
+// weights of the reference's full quadratic layout <-> the deduplicated working layout
+void dedup_to_full(const mld_gpu_handle* h, const double* wd, double* wf) {
+  const int KK = h->KK, DL = h->DL;
+  for (int c = 0; c < DL; ++c) wf[c] = wd[c];
+  const double r2 = std::sqrt(2.0);
+  for (int i = 0, q = 0; i < KK; ++i)
+    for (int j = i; j < KK; ++j, ++q) {
+      const double v = wd[DL + q];
+      if (i == j) wf[DL + KK * i + j] = v;
+      else wf[DL + KK * i + j] = wf[DL + KK * j + i] = v / r2;
+    }
+}
+void full_to_dedup(const mld_gpu_handle* h, const double* wf, double* wd) {
+  const int KK = h->KK, DL = h->DL;
+  for (int c = 0; c < DL; ++c) wd[c] = wf[c];
+  const double r2 = std::sqrt(2.0);
+  for (int i = 0, q = 0; i < KK; ++i)
+    for (int j = i; j < KK; ++j, ++q)
+      wd[DL + q] = (i == j) ? wf[DL + KK * i + j] : (wf[DL + KK * i + j] + wf[DL + KK * j + i]) / r2;
+}
+
+// a working-layout design row -> the reference's row (full K*K quadratic block)
+void export_row(const mld_gpu_handle* h, const double* xd, double* xf) {
+  const int KK = h->KK, DL = h->DL;
+  for (int c = 0; c < DL; ++c) xf[c] = xd[c];
+  if (!h->quad) return;
+  const double r2 = std::sqrt(2.0);
+  for (int i = 0, q = 0; i < KK; ++i)
+    for (int j = i; j < KK; ++j, ++q) {
+      const double v = xd[DL + q];
+      if (i == j) xf[DL + KK * i + j] = v;
+      else xf[DL + KK * i + j] = xf[DL + KK * j + i] = v / r2;
+    }
+}
+
+__global__ void k_sub(long long n, const double* a, const double* b, double* out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i] - b[i];
 }
 
 // Kernel launches per phase of one fit (neighbours: count, 3 scan kernels, fill; rows: labels
@@ -285,23 +396,40 @@ int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
   if (rc) return rc;
   const long long M = h->fit_rows.M;
   const int D = h->D;
-  CK(ensure(h, mld_gpu_handle::B_G, sizeof(double) * D * D));
-  CK(ensure(h, mld_gpu_handle::B_H, sizeof(double) * D));
+  const size_t gdim = (size_t)std::max(h->DL, h->DQ);
+  CK(ensure(h, mld_gpu_handle::B_G, sizeof(double) * gdim * gdim));
+  CK(ensure(h, mld_gpu_handle::B_H, sizeof(double) * gdim));
   CK(ensure(h, mld_gpu_handle::B_W, sizeof(double) * D));
-  CK(ensure(h, mld_gpu_handle::B_EVALS, sizeof(double) * D));
+  CK(ensure(h, mld_gpu_handle::B_EVALS, sizeof(double) * gdim));
   CK(ensure(h, mld_gpu_handle::B_INFO, sizeof(int) * 4));
   CK(ensure(h, mld_gpu_handle::B_SQ, sizeof(double) * 6));
   double* G = bp_<double>(h, mld_gpu_handle::B_G);
   double* hv = bp_<double>(h, mld_gpu_handle::B_H);
   double* w = bp_<double>(h, mld_gpu_handle::B_W);
+  double* y = bp_<double>(h, mld_gpu_handle::B_Y);
+  double* wrow = bp_<double>(h, mld_gpu_handle::B_WROW);
+  // linear block (QNML stage 1, or the whole linear model): parameters.F90:1018-1099
   mark(h, MLD_PHASE_GRAM, 0);
-  CK(launch_gram<T>(X, h->ldx, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D, G, hv,
-                    h->st));
+  CK(launch_gram<T>(X, h->ldx, wrow, y, M, h->DL, G, hv, h->st));
   mark(h, MLD_PHASE_GRAM, 1);
   mark(h, MLD_PHASE_SOLVE, 0);
-  CK(launch_solve_sym(G, hv, D, h->cfg.lambda_krr, h->cfg.svd_rcond, w, bp_<double>(h, mld_gpu_handle::B_EVALS),
-                      bp_<int>(h, mld_gpu_handle::B_INFO), h->st));
+  rc = solve_any(h, G, hv, h->DL, w);
+  if (rc) return rc;
   mark(h, MLD_PHASE_SOLVE, 1);
+  if (h->quad) {
+    // QNML stage 2 (parameters.F90:404-421, 476-1015): the quadratic block is fitted to the
+    // residual of the linear fit with the same ridge solver
+    CK(ensure(h, mld_gpu_handle::B_PRED, sizeof(double) * std::max<long long>(M, 1)));
+    CK(ensure(h, mld_gpu_handle::B_YQ, sizeof(double) * std::max<long long>(M, 1)));
+    double* pred = bp_<double>(h, mld_gpu_handle::B_PRED);
+    double* yq = bp_<double>(h, mld_gpu_handle::B_YQ);
+    CK(launch_predict_sq<T>(X, h->ldx, w, M, h->DL, pred, nullptr, nullptr, nullptr, h->st));
+    k_sub<<<(unsigned)((M + 255) / 256), 256, 0, h->st>>>(M, y, pred, yq);
+    CK(cudaGetLastError());
+    CK(launch_gram<T>(X + h->DL, h->ldx, wrow, yq, M, h->DQ, G, hv, h->st));
+    rc = solve_any(h, G, hv, h->DQ, w + h->DL);
+    if (rc) return rc;
+  }
   double* sq = bp_<double>(h, mld_gpu_handle::B_SQ);
   mark(h, MLD_PHASE_PREDICT, 0);
   CK(cudaMemsetAsync(sq, 0, sizeof(double) * 6, h->st));
@@ -309,9 +437,14 @@ int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
                           sq, h->st));
   mark(h, MLD_PHASE_PREDICT, 1);
   double hsq[6];
-  if (w_params) CK(cudaMemcpyAsync(w_params, w, sizeof(double) * D, cudaMemcpyDeviceToHost, h->st));
+  std::vector<double> wd(D);
+  CK(cudaMemcpyAsync(wd.data(), w, sizeof(double) * D, cudaMemcpyDeviceToHost, h->st));
   CK(cudaMemcpyAsync(hsq, sq, sizeof(double) * 6, cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
+  if (w_params) {
+    if (h->quad) dedup_to_full(h, wd.data(), w_params);
+    else std::copy(wd.begin(), wd.end(), w_params);
+  }
   accumulate_profile(h);
   if (rmse)
     for (int k = 0; k < 3; ++k) rmse[k] = hsq[3 + k] > 0 ? std::sqrt(hsq[k] / hsq[3 + k]) : 0.0;
@@ -354,7 +487,7 @@ int mld_gpu_create(const mld_gpu_config* cfg, mld_gpu_handle** out) {
   if (!cfg || !out) return MLD_ERR_INVALID;
   *out = nullptr;
   if (cfg->descriptor_type != 9) return MLD_ERR_UNSUPPORTED;
-  if (cfg->ml_type != 0 || cfg->mld_order != 1) return MLD_ERR_UNSUPPORTED;
+  if (cfg->ml_type != 0 || (cfg->mld_order != 1 && cfg->mld_order != 2)) return MLD_ERR_UNSUPPORTED;
   if (!(cfg->inv_r0_input > 0.0 && cfg->inv_r0_input < 1.0)) return MLD_ERR_INVALID;  // test_parameters_bso4
   if (cfg->j_max < 0 || !(cfg->r_cut > 0)) return MLD_ERR_INVALID;
   if (cfg->n_elements < 1 || cfg->n_elements > MLD_MAX_ELEMENTS) return MLD_ERR_INVALID;
@@ -378,7 +511,11 @@ int mld_gpu_create(const mld_gpu_config* cfg, mld_gpu_handle** out) {
   h->nch = cfg->weighted ? (cfg->weighted_3ch ? 3 : 2) : 1;
   h->K = t.K;
   h->KK = h->nch * t.K;
-  h->D = 1 + h->KK;
+  h->DL = 1 + h->KK;
+  h->quad = cfg->mld_order == 2;
+  h->DQ = h->quad ? h->KK * (h->KK + 1) / 2 : 0;
+  h->D = h->DL + h->DQ;                                       // working (deduplicated) row width
+  h->Dfull = h->DL + (h->quad ? h->KK * h->KK : 0);           // reference layout (dim_design_line)
   h->ldx = round_up4(h->D);
   // device tables
   DevTables& d = h->dt;
@@ -475,7 +612,7 @@ int mld_gpu_dims(const mld_gpu_handle* h, int* K, int* dim_desc, int* dim_design
   if (!h) return MLD_ERR_INVALID;
   if (K) *K = h->K;
   if (dim_desc) *dim_desc = h->KK;
-  if (dim_design_line) *dim_design_line = h->D;
+  if (dim_design_line) *dim_design_line = h->Dfull;
   return MLD_OK;
 }
 
@@ -677,16 +814,22 @@ int mld_gpu_design_matrix(mld_gpu_handle* h, double* A, double* y, double* w) {
       std::vector<float> tmp((size_t)M * h->ldx);
       CK(cudaMemcpyAsync(tmp.data(), X, sizeof(float) * tmp.size(), cudaMemcpyDeviceToHost, h->st));
       CK(cudaStreamSynchronize(h->st));
-      for (long long r = 0; r < M; ++r)
-        for (int c = 0; c < h->D; ++c) A[(size_t)r * h->D + c] = tmp[(size_t)r * h->ldx + c];
+      std::vector<double> row(h->D);
+      for (long long r = 0; r < M; ++r) {
+        for (int c = 0; c < h->D; ++c) row[c] = tmp[(size_t)r * h->ldx + c];
+        export_row(h, row.data(), A + (size_t)r * h->Dfull);
+      }
     }
   } else {
     double* X = nullptr;
     rc = run_rows<double>(h, h->fit_rows, true, &X);
     if (rc) return rc;
-    if (A && M > 0)
-      CK(cudaMemcpy2DAsync(A, sizeof(double) * h->D, X, sizeof(double) * h->ldx, sizeof(double) * h->D, (size_t)M,
-                           cudaMemcpyDeviceToHost, h->st));
+    if (A && M > 0) {
+      std::vector<double> tmp((size_t)M * h->ldx);
+      CK(cudaMemcpyAsync(tmp.data(), X, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+      for (long long r = 0; r < M; ++r) export_row(h, tmp.data() + (size_t)r * h->ldx, A + (size_t)r * h->Dfull);
+    }
   }
   if (y) CK(cudaMemcpyAsync(y, bp_<double>(h, mld_gpu_handle::B_Y), sizeof(double) * M, cudaMemcpyDeviceToHost, h->st));
   if (w)
@@ -725,23 +868,21 @@ int mld_gpu_gram(mld_gpu_handle* h, double* G, double* rhs) {
 
 int mld_gpu_solve(mld_gpu_handle* h, const double* G, const double* rhs, int D, double* w, int* rank_out) {
   if (!h || !G || !rhs || !w || D < 1) return MLD_ERR_INVALID;
-  if (D > 112) return fail(h, MLD_ERR_UNSUPPORTED, "symmetric solve limited to D <= 112 in this build");
-  double *dG = nullptr, *dh = nullptr, *dw = nullptr;
-  int* dinfo = nullptr;
-  CK(ensure(h, mld_gpu_handle::B_G, sizeof(double) * D * D));
+  CK(ensure(h, mld_gpu_handle::B_G, sizeof(double) * (size_t)D * D));
   CK(ensure(h, mld_gpu_handle::B_H, sizeof(double) * D));
   CK(ensure(h, mld_gpu_handle::B_W, sizeof(double) * D));
+  CK(ensure(h, mld_gpu_handle::B_EVALS, sizeof(double) * D));
   CK(ensure(h, mld_gpu_handle::B_INFO, sizeof(int) * 4));
-  dG = bp_<double>(h, mld_gpu_handle::B_G);
-  dh = bp_<double>(h, mld_gpu_handle::B_H);
-  dw = bp_<double>(h, mld_gpu_handle::B_W);
-  dinfo = bp_<int>(h, mld_gpu_handle::B_INFO);
-  CK(cudaMemcpyAsync(dG, G, sizeof(double) * D * D, cudaMemcpyHostToDevice, h->st));
+  double* dG = bp_<double>(h, mld_gpu_handle::B_G);
+  double* dh = bp_<double>(h, mld_gpu_handle::B_H);
+  double* dw = bp_<double>(h, mld_gpu_handle::B_W);
+  CK(cudaMemcpyAsync(dG, G, sizeof(double) * (size_t)D * D, cudaMemcpyHostToDevice, h->st));
   CK(cudaMemcpyAsync(dh, rhs, sizeof(double) * D, cudaMemcpyHostToDevice, h->st));
-  CK(launch_solve_sym(dG, dh, D, h->cfg.lambda_krr, h->cfg.svd_rcond, dw, nullptr, dinfo, h->st));
-  int info[2];
+  int rc = solve_any(h, dG, dh, D, dw);
+  if (rc) return rc;
+  int info[2] = {0, D};
   CK(cudaMemcpyAsync(w, dw, sizeof(double) * D, cudaMemcpyDeviceToHost, h->st));
-  CK(cudaMemcpyAsync(info, dinfo, sizeof(int) * 2, cudaMemcpyDeviceToHost, h->st));
+  if (D <= 112) CK(cudaMemcpyAsync(info, bp_<int>(h, mld_gpu_handle::B_INFO), sizeof(int) * 2, cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   if (rank_out) *rank_out = info[1];
   return MLD_OK;
@@ -750,7 +891,6 @@ int mld_gpu_solve(mld_gpu_handle* h, const double* G, const double* rhs, int D, 
 int mld_gpu_fit(mld_gpu_handle* h, double* w_params, double* rmse_efs) {
   if (!h) return MLD_ERR_INVALID;
   if (!h->has_labels) return fail(h, MLD_ERR_STATE, "labels not set");
-  if (h->D > 112) return fail(h, MLD_ERR_UNSUPPORTED, "symmetric solve limited to D <= 112 in this build");
   return h->mixed ? fit_impl<float>(h, w_params, rmse_efs) : fit_impl<double>(h, w_params, rmse_efs);
 }
 
@@ -765,7 +905,10 @@ int mld_gpu_predict(mld_gpu_handle* h, const double* w_params, double* E, double
   CK(ensure(h, mld_gpu_handle::B_PRED, sizeof(double) * std::max<long long>(L.M, 1)));
   double* dw = bp_<double>(h, mld_gpu_handle::B_W);
   double* pred = bp_<double>(h, mld_gpu_handle::B_PRED);
-  CK(cudaMemcpyAsync(dw, w_params, sizeof(double) * D, cudaMemcpyHostToDevice, h->st));
+  std::vector<double> wd(D);
+  if (h->quad) full_to_dedup(h, w_params, wd.data());
+  else std::copy(w_params, w_params + D, wd.begin());
+  CK(cudaMemcpyAsync(dw, wd.data(), sizeof(double) * D, cudaMemcpyHostToDevice, h->st));
   if (h->mixed) {
     float* X = nullptr;
     rc = run_rows<float>(h, L, false, &X);

@@ -1,0 +1,207 @@
+// Blocked FP64 Cholesky factorisation and triangular solves for large normal matrices
+// (D > kJacobiMax, e.g. the quadratic block of the QNML fit).
+//
+// The reference solves the regularised normal equations (A W A^T + lambda I) w = A W y with
+// LAPACK dgelsd (parameters.F90:1018-1099, stats_tools.F90:1153-1213).  For a symmetric
+// positive-definite normal matrix the Cholesky solution is the same solution; a rank-deficient
+// matrix without ridge gets a relative diagonal shift `jitter * max(diag)` (the min-norm
+// solution differs only in the null space, predictions agree).  Iterative refinement with FP64
+// residuals (driven from api.cu) recovers FP64-level coefficients.
+//
+// Right-looking blocked algorithm, block size kCB, lower triangle, row-major D x D (lda):
+//   for each block column k: factor the diagonal block (one CTA), solve the panel below it
+//   (L21 = A21 L11^-T), update the trailing lower triangle A22 -= L21 L21^T.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "mld_internal.h"
+
+namespace mld {
+
+constexpr int kCB = 32;
+
+// Factor the diagonal block [k0, k0+nb) in place; info[0] = first failing column + 1.
+__global__ void __launch_bounds__(256) k_potrf_diag(double* A, int lda, int k0, int nb, double shift, int* info) {
+  __shared__ double L[kCB][kCB + 1];
+  const int tid = threadIdx.x;
+  for (int e = tid; e < nb * nb; e += blockDim.x) {
+    const int i = e / nb, j = e % nb;
+    double v = A[(size_t)(k0 + i) * lda + (k0 + j)];
+    if (i == j) v += shift;
+    L[i][j] = v;
+  }
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    if (tid == 0) {
+      double d = L[j][j];
+      if (!(d > 0.0)) {
+        if (info[0] == 0) info[0] = k0 + j + 1;
+        d = 1e-300;
+      }
+      L[j][j] = sqrt(d);
+    }
+    __syncthreads();
+    const double djj = L[j][j];
+    for (int i = j + 1 + tid; i < nb; i += blockDim.x) L[i][j] /= djj;
+    __syncthreads();
+    for (int e = tid; e < (nb - j - 1) * (nb - j - 1); e += blockDim.x) {
+      const int i = j + 1 + e / (nb - j - 1), c = j + 1 + e % (nb - j - 1);
+      if (c <= i) L[i][c] -= L[i][j] * L[c][j];
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < nb * nb; e += blockDim.x) {
+    const int i = e / nb, j = e % nb;
+    if (j <= i) A[(size_t)(k0 + i) * lda + (k0 + j)] = L[i][j];
+  }
+}
+
+// Panel: rows r in [k0+nb, D): A[r][k0..k0+nb) <- A[r][..] L11^-T  (one thread per row)
+__global__ void __launch_bounds__(128) k_trsm_panel(double* A, int lda, int D, int k0, int nb) {
+  __shared__ double L[kCB][kCB + 1];
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int i = e / nb, j = e % nb;
+    L[i][j] = (j <= i) ? A[(size_t)(k0 + i) * lda + (k0 + j)] : 0.0;
+  }
+  __syncthreads();
+  const int r = k0 + nb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= D) return;
+  double x[kCB];
+  for (int j = 0; j < nb; ++j) x[j] = A[(size_t)r * lda + k0 + j];
+  for (int j = 0; j < nb; ++j) {
+    double v = x[j];
+    for (int c = 0; c < j; ++c) v -= x[c] * L[j][c];
+    x[j] = v / L[j][j];
+  }
+  for (int j = 0; j < nb; ++j) A[(size_t)r * lda + k0 + j] = x[j];
+}
+
+// Trailing update of the lower triangle: A[i][j] -= sum_c L[i][c] L[j][c], i, j >= k1, j <= i.
+// 32x32 tiles, 16x16 threads with 2x2 outputs.
+__global__ void __launch_bounds__(256) k_syrk_update(double* A, int lda, int D, int k0, int nb, int k1) {
+  const int ntile = (D - k1 + 31) / 32;
+  int t = blockIdx.x, ti = 0;
+  while (t >= ti + 1) {  // lower-triangular tile pairs (tj <= ti)
+    t -= ti + 1;
+    ++ti;
+  }
+  const int tj = t;
+  if (ti >= ntile) return;
+  const int i0 = k1 + ti * 32, j0 = k1 + tj * 32;
+  __shared__ double Li[32][kCB + 1], Lj[32][kCB + 1];
+  for (int e = threadIdx.x; e < 32 * nb; e += blockDim.x) {
+    const int r = e / nb, c = e % nb;
+    Li[r][c] = (i0 + r < D) ? A[(size_t)(i0 + r) * lda + k0 + c] : 0.0;
+    Lj[r][c] = (j0 + r < D) ? A[(size_t)(j0 + r) * lda + k0 + c] : 0.0;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[2][2] = {{0, 0}, {0, 0}};
+  for (int c = 0; c < nb; ++c) {
+    const double a0 = Li[ty][c], a1 = Li[ty + 16][c];
+    const double b0 = Lj[tx][c], b1 = Lj[tx + 16][c];
+    acc[0][0] = fma(a0, b0, acc[0][0]);
+    acc[0][1] = fma(a0, b1, acc[0][1]);
+    acc[1][0] = fma(a1, b0, acc[1][0]);
+    acc[1][1] = fma(a1, b1, acc[1][1]);
+  }
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) {
+      const int i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
+      if (i < D && j < D && j <= i) A[(size_t)i * lda + j] -= acc[a][b];
+    }
+}
+
+// Solve L L^T x = b in one CTA (forward then backward substitution, blocked by kCB rows).
+__global__ void __launch_bounds__(1024) k_chol_solve(const double* L, int lda, int D, const double* b, double* x) {
+  extern __shared__ double sx[];  // D
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int i = tid; i < D; i += nth) sx[i] = b[i];
+  __syncthreads();
+  __shared__ double red[32];
+  // forward: L y = b
+  for (int i = 0; i < D; ++i) {
+    double part = 0.0;
+    for (int c = tid; c < i; c += nth) part = fma(L[(size_t)i * lda + c], sx[c], part);
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((tid & 31) == 0) red[tid >> 5] = part;
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0;
+      for (int w = 0; w < (nth + 31) / 32; ++w) s += red[w];
+      sx[i] = (sx[i] - s) / L[(size_t)i * lda + i];
+    }
+    __syncthreads();
+  }
+  // backward: L^T x = y
+  for (int i = D - 1; i >= 0; --i) {
+    double part = 0.0;
+    for (int c = i + 1 + tid; c < D; c += nth) part = fma(L[(size_t)c * lda + i], sx[c], part);
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((tid & 31) == 0) red[tid >> 5] = part;
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0;
+      for (int w = 0; w < (nth + 31) / 32; ++w) s += red[w];
+      sx[i] = (sx[i] - s) / L[(size_t)i * lda + i];
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < D; i += nth) x[i] = sx[i];
+}
+
+// r = h - (G + lambda I) w (full symmetric G, row-major), FP64.
+__global__ void k_residual(const double* G, int D, double lambda, const double* w, const double* h, double* r) {
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= D) return;
+  double acc = 0.0;
+  for (int c = lane; c < D; c += 32) acc = fma(G[(size_t)i * D + c], w[c], acc);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) r[i] = h[i] - acc - lambda * w[i];
+}
+
+__global__ void k_axpy(int n, double a, const double* x, double* y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] += a * x[i];
+}
+
+cudaError_t launch_cholesky(double* A, int D, double shift, int* info, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(info, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  for (int k0 = 0; k0 < D; k0 += kCB) {
+    const int nb = min(kCB, D - k0);
+    k_potrf_diag<<<1, 256, 0, st>>>(A, D, k0, nb, shift, info);
+    const int k1 = k0 + nb;
+    if (k1 < D) {
+      const int rows = D - k1;
+      k_trsm_panel<<<(rows + 127) / 128, 128, 0, st>>>(A, D, D, k0, nb);
+      const int nt = (rows + 31) / 32;
+      k_syrk_update<<<nt * (nt + 1) / 2, 256, 0, st>>>(A, D, D, k0, nb, k1);
+    }
+    // the shift applies to the diagonal blocks only once: later blocks still hold raw values
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_chol_solve(const double* L, int D, const double* b, double* x, cudaStream_t st) {
+  const size_t smem = sizeof(double) * (size_t)D;
+  cudaError_t e = cudaFuncSetAttribute(k_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_chol_solve<<<1, 1024, smem, st>>>(L, D, D, b, x);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_residual(const double* G, int D, double lambda, const double* w, const double* h, double* r,
+                            cudaStream_t st) {
+  const long long threads = (long long)D * 32;
+  k_residual<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(G, D, lambda, w, h, r);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_axpy(int n, double a, const double* x, double* y, cudaStream_t st) {
+  k_axpy<<<(n + 255) / 256, 256, 0, st>>>(n, a, x, y);
+  return cudaGetLastError();
+}
+
+}  // namespace mld

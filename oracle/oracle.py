@@ -160,3 +160,31 @@ def fit_linear(A: np.ndarray, y: np.ndarray, wts: np.ndarray, lam: float, rcond:
 def rmse(pred: np.ndarray, ref: np.ndarray) -> float:
     d = np.asarray(pred) - np.asarray(ref)
     return float(np.sqrt(np.mean(d * d))) if d.size else 0.0
+
+
+def quadratic_rows(desc: Dict[str, np.ndarray], cell: np.ndarray, *, sign_stress: float = 1.0,
+                   sign_big: float = 1.0):
+    """Quadratic design rows in the reference's full layout (1 + KK + KK*KK columns)."""
+    L = lib()
+    L.orc_rows_quadratic.argtypes = L.orc_rows_linear.argtypes
+    B, dB = desc["B"], desc["dB"]
+    nat, KK = B.shape
+    D = 1 + KK + KK * KK
+    rowE = np.zeros(D)
+    rowF = np.zeros((3 * nat, D))
+    rowS = np.zeros((6, D))
+    vol = L.orc_volume(_ptr(np.ascontiguousarray(cell, dtype=np.float64)))
+    L.orc_rows_quadratic(nat, KK, _ptr(B), _ptr(dB), _ptr(desc["nn"]), _ptr(desc["nbr"]), _ptr(desc["u"]),
+                         desc["cap"], int(desc["small"]), float(sign_stress), float(sign_big), float(vol),
+                         _ptr(rowE), _ptr(rowF), _ptr(rowS))
+    return rowE, rowF, rowS
+
+
+def fit_qnml(A: np.ndarray, y: np.ndarray, wts: np.ndarray, lam: float, n_linear: int, rcond: float = -1.0):
+    """QNML two-stage fit (parameters.F90:404-421, 476-1015): linear block first, then the
+    quadratic block on the residual, both with the linear ridge/gelsd solver."""
+    AL, AQ = A[:, :n_linear], A[:, n_linear:]
+    wL = fit_linear(AL, y, wts, lam, rcond)
+    res = y - AL @ wL
+    wQ = fit_linear(AQ, res, wts, lam, rcond)
+    return np.concatenate([wL, wQ])
