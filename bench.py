@@ -159,7 +159,8 @@ def run_ours(a, rank, world):
     flops, per_pair, per_atom = flops_model(wc, wc["pairs"], wc["atoms"])
     t_desc = prof["descriptors"][0] / max(prof["descriptors"][2], 1)
     peak32 = h.peak_flops(_lib.MIXED)
-    launches = sum(v[1] for v in prof.values())
+    launches = int(sum(v[1] for v in prof.values()))
+    res["solve_info"] = h.solve_info()
     res.update(M=M, A=A, ms_step=ms_step, rmse_mixed=rmse_mixed.tolist(), prof=prof, wc=wc, flops=flops,
                t_desc=t_desc, peak32=peak32, launches=launches, clocks=clk.summary(),
                per_pair=per_pair, per_atom=per_atom)
@@ -198,18 +199,21 @@ def run_ours(a, rank, world):
     h.close()
 
     # ---------------- plain FP64 method on the same data ----------------------------------
-    h64 = handle(_lib.PLAIN_FP64)
-    w64, rmse64 = h64.fit()
-    h64.set_profiling(True)
-    h64.profile(reset=True)
-    h64.timer_start()
-    for _ in range(a.plain_steps):
+    if a.plain_steps > 0:
+        h64 = handle(_lib.PLAIN_FP64)
         w64, rmse64 = h64.fit()
-    ms64 = h64.timer_stop() / a.plain_steps
-    prof64 = h64.profile(reset=True)
-    peak64 = h64.peak_flops(_lib.PLAIN_FP64)
-    h64.close()
-    res.update(ms64=ms64, rmse64=rmse64.tolist(), prof64=prof64, peak64=peak64)
+        h64.set_profiling(True)
+        h64.profile(reset=True)
+        h64.timer_start()
+        for _ in range(a.plain_steps):
+            w64, rmse64 = h64.fit()
+        ms64 = h64.timer_stop() / a.plain_steps
+        prof64 = h64.profile(reset=True)
+        peak64 = h64.peak_flops(_lib.PLAIN_FP64)
+        h64.close()
+        res.update(ms64=ms64, rmse64=rmse64.tolist(), prof64=prof64, peak64=peak64)
+    else:
+        res.update(ms64=None, rmse64=None, prof64=None, peak64=None)
     res["ds"] = ds
     return res
 
@@ -324,12 +328,13 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single"},
         "atom_evals_per_s": world * A / (ms_step * 1e-3),
         "rmse_efs": res["rmse_mixed"],
-        "plain_fp64": {"value": M / (res["ms64"] * 1e-3), "ms_per_step": res["ms64"], "rmse_efs": res["rmse64"],
+        "plain_fp64": None if res["ms64"] is None else {"value": M / (res["ms64"] * 1e-3), "ms_per_step": res["ms64"], "rmse_efs": res["rmse64"],
                        "steps": a.plain_steps,
-                       "phase_ms": {k: v[0] / max(v[2], 1) for k, v in res["prof64"].items()},
+                       "phase_ms": {k: v[0] / a.plain_steps for k, v in res["prof64"].items()},
                        "fp64_peak_tflops_measured": res["peak64"]},
-        "speedup_vs_plain_fp64": res["ms64"] / ms_step,
-        "phase_ms": {k: v[0] / max(v[2], 1) for k, v in res["prof"].items()},
+        "speedup_vs_plain_fp64": None if res["ms64"] is None else res["ms64"] / ms_step,
+        "phase_ms": {k: v[0] / a.steps for k, v in res["prof"].items()},
+        "mixed_solve": res["solve_info"],
         "roofline": {"kernel": "k_bso4<float> (fused descriptor + design rows)", "bound": "fp32",
                      "achieved": achieved, "peak": res["peak32"], "unit": "TFLOP/s", "frac": achieved / res["peak32"],
                      "peak_source": "measured in this run (FP32 FMA probe; not in MEASURED_PEAKS.json)",

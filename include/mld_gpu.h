@@ -43,6 +43,7 @@ extern "C" {
 #define MLD_ERR_SOLVE 5          /* the normal matrix could not be solved */
 #define MLD_ERR_STATE 6          /* call order: e.g. fit before structures were staged */
 #define MLD_ERR_UNSUPPORTED 7    /* option outside this build (e.g. descriptor_type != 9) */
+#define MLD_ERR_TIMEOUT 9        /* a bounded device-side wait expired (kernel returned early) */
 
 #define MLD_PRECISION_PLAIN_FP64 0  /* all-FP64 on the GPU */
 #define MLD_PRECISION_MIXED 1       /* FP32 descriptors/rows, FP64 Gram accumulation and solve */
@@ -167,6 +168,25 @@ int mld_gpu_work_counts(const mld_gpu_handle* h, long long* out);
  * (FP64 for MLD_PRECISION_PLAIN_FP64, FP32 for MLD_PRECISION_MIXED): the roofline denominator
  * of the descriptor kernel. */
 int mld_gpu_peak_flops(mld_gpu_handle* h, int precision, double* tflops);
+
+/* Solver record of the last mixed-method fit: conjugate-gradient iterations and final relative
+ * preconditioned residual per stage (0 = linear block, 1 = quadratic block of QNML), and how
+ * often the Cholesky preconditioner had to be re-factorised with a larger diagonal shift.
+ * (No reference counterpart: the reference solves with dgelsd, stats_tools.F90:1153-1213.) */
+int mld_gpu_solve_info(const mld_gpu_handle* h, int* pcg_iterations /*[2]*/, double* pcg_residual /*[2]*/,
+                       int* chol_retries);
+
+/* Weighted Gram matrix and right-hand side of caller-owned DEVICE rows, the per-block
+ * accumulation of the online fit (gram%accumulate, module_online_fit.F90:49-53,138-265):
+ *   G   (D x D, row-major FP64, device)   = sum_r w[r] x_r x_r^T
+ *   rhs (D, FP64, device; may be NULL)    = sum_r w[r] y[r] x_r
+ * X holds M rows of D values with a row stride of ldx elements, FP64 (x_is_fp32 = 0) or FP32.
+ * method MLD_PRECISION_PLAIN_FP64: FP64 accumulation on the CUDA cores; MLD_PRECISION_MIXED:
+ * tensor cores in BF16 split precision (x = hi + lo, hi*hi + hi*lo + lo*hi) with FP32
+ * accumulation per row split and FP64 accumulation across splits.  Allocates and frees its own
+ * workspace; `stream` may be NULL; returns after the stream has synchronised. */
+int mld_gpu_gram_rows(int method, const void* X, int x_is_fp32, long long M, int D, int ldx, const double* w,
+                      const double* y, double* G, double* rhs, void* stream, char* err, int err_len);
 
 /* ---- descriptors without device allocation --------------------------------------------
  * No counterpart in the MILADY reference.  Some callers cannot call cudaMalloc: it

@@ -16,7 +16,8 @@ LIB_PATH = os.path.join(HERE, "libmld_gpu.so")
 
 MLD_OK = 0
 ERRORS = {1: "MLD_ERR_INVALID", 2: "MLD_ERR_CUDA", 3: "MLD_ERR_NEIGHBOUR_CAP", 4: "MLD_ERR_OOM",
-          5: "MLD_ERR_SOLVE", 6: "MLD_ERR_STATE", 7: "MLD_ERR_UNSUPPORTED", 8: "MLD_ERR_NOALLOC_LIMIT"}
+          5: "MLD_ERR_SOLVE", 6: "MLD_ERR_STATE", 7: "MLD_ERR_UNSUPPORTED", 8: "MLD_ERR_NOALLOC_LIMIT",
+          9: "MLD_ERR_TIMEOUT"}
 PLAIN_FP64 = 0
 MIXED = 1
 MAX_ELEMENTS = 8
@@ -26,7 +27,7 @@ EXPORTED = ["mld_gpu_config_defaults", "mld_gpu_create", "mld_gpu_destroy", "mld
             "mld_gpu_descriptor_derivatives", "mld_gpu_num_rows", "mld_gpu_design_matrix", "mld_gpu_gram",
             "mld_gpu_solve", "mld_gpu_fit", "mld_gpu_predict", "mld_gpu_synchronize", "mld_gpu_set_profiling",
             "mld_gpu_profile", "mld_gpu_timer_start", "mld_gpu_timer_stop", "mld_gpu_work_counts",
-            "mld_gpu_peak_flops", "mld_gpu_descriptors_noalloc"]
+            "mld_gpu_peak_flops", "mld_gpu_descriptors_noalloc", "mld_gpu_solve_info", "mld_gpu_gram_rows"]
 NPHASE = 6
 PHASES = ["neighbours", "rows", "descriptors", "gram", "solve", "predict"]
 
@@ -261,3 +262,24 @@ class Handle:
         keys = ["NU", "u_one_term", "u_two_term", "cg_terms", "z_row_extents", "z_outputs", "y_slots",
                 "y_slots_za", "K", "nch", "pairs", "atoms"]
         return dict(zip(keys, (int(v) for v in out)))
+
+    def solve_info(self):
+        it = np.zeros(2, np.int32)
+        res = np.zeros(2)
+        rt = ctypes.c_int()
+        self._check(self._L.mld_gpu_solve_info(self._h, _p(it), _p(res), ctypes.byref(rt)))
+        return {"pcg_iterations": [int(v) for v in it], "pcg_residual": [float(v) for v in res],
+                "chol_retries": int(rt.value)}
+
+
+def gram_rows(method: int, X_ptr: int, x_is_fp32: bool, M: int, D: int, ldx: int, w_ptr: int, y_ptr: int,
+              G_ptr: int, rhs_ptr: int = 0, stream: int = 0) -> None:
+    """G = X^T W X (and rhs = X^T W y) of device rows given as raw device addresses."""
+    L = load()
+    err = ctypes.create_string_buffer(512)
+    vp = ctypes.c_void_p
+    rc = L.mld_gpu_gram_rows(int(method), vp(X_ptr), int(bool(x_is_fp32)), ctypes.c_longlong(M), int(D), int(ldx),
+                             vp(w_ptr), vp(y_ptr or None), vp(G_ptr), vp(rhs_ptr or None), vp(stream or None), err,
+                             512)
+    if rc != 0:
+        raise MldError(rc, err.value.decode(errors="replace"))

@@ -11,24 +11,6 @@
 #include "../../include/mld_gpu.h"
 #include "mld_internal.h"
 
-namespace mld {
-template <typename T>
-cudaError_t launch_predict_sq(const T* X, int ldx, const double* w, long long M, int D, double* pred, const double* y,
-                              const int* kind, double* sq, cudaStream_t st);
-template <typename T>
-cudaError_t launch_rows_prep(int S, const int* atom_start, const DevRows& rows, const double* E, const double* F,
-                             const double* Sv, const double* wefs, T* X, double* y, double* wrow, int* kind,
-                             cudaStream_t st);
-template <typename T>
-cudaError_t launch_quad_rows(const DevBatch& b, const DevRows& rows, const BsoParams& p, int KK, const int* rev,
-                             const T* B, const T* dB, T* H, T* X, int qoff, cudaStream_t st);
-cudaError_t launch_reverse_pairs(const DevBatch& b, int* rev, cudaStream_t st);
-cudaError_t launch_cholesky(double* A, int D, double shift, int* info, cudaStream_t st);
-cudaError_t launch_chol_solve(const double* L, int D, const double* b, double* x, cudaStream_t st);
-cudaError_t launch_residual(const double* G, int D, double lambda, const double* w, const double* h, double* r,
-                            cudaStream_t st);
-cudaError_t launch_axpy(int n, double a, const double* x, double* y, cudaStream_t st);
-}  // namespace mld
 
 using namespace mld;
 
@@ -73,13 +55,27 @@ struct mld_gpu_handle {
   std::vector<int> h_has;  // 3*S
   RowLayout fit_rows;
 
-  // profiling: CUDA events around each phase of a fit, accumulated after its final sync
+  // profiling: CUDA event pairs around each phase interval of a fit, accumulated after its
+  // final sync; kernel launches are counted per interval at the launch sites
   bool prof = false;
-  cudaEvent_t ev[2 * MLD_NPHASE] = {};
+  std::vector<cudaEvent_t> evpool;
+  struct Interval {
+    int phase, ev;
+    long long launches;
+  };
+  std::vector<Interval> pending;
+  int cur_phase = -1, cur_ev = -1;
+  long long cur_launches = 0;
   cudaEvent_t tev[2] = {};
   double ms[MLD_NPHASE] = {0};
   long long launches[MLD_NPHASE] = {0};
   long long calls[MLD_NPHASE] = {0};
+
+  // device properties and the last mixed-method solve
+  int nsm = 0;
+  int pcg_iters[2] = {0, 0};
+  double pcg_rel[2] = {0, 0};
+  int chol_retries = 0;
 
   std::vector<void*> owned;  // table allocations
   Buf bufs[48];
@@ -90,6 +86,7 @@ struct mld_gpu_handle {
     B_ROWE, B_ROWF, B_ROWS, B_X, B_Y, B_WROW, B_KIND,
     B_G, B_H, B_W, B_EVALS, B_INFO, B_SQ, B_PRED, B_BOUT, B_DBOUT,
     B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
+    B_GWS, B_TERR, B_PCG, B_POS32,
     B_COUNT
   };
 };
@@ -187,9 +184,30 @@ RowLayout make_layout(const mld_gpu_handle* h, const std::vector<int>& has, bool
   return L;
 }
 
+// Phase intervals: mark(h, p, 0) opens an interval of phase p, mark(h, p, 1) closes it; a
+// phase may be entered several times per fit.  nl() counts the kernels launched inside.
 void mark(mld_gpu_handle* h, int phase, int end) {
-  if (h->prof) cudaEventRecord(h->ev[2 * phase + end], h->st);
+  if (!h->prof) return;
+  if (!end) {
+    const int idx = (int)h->pending.size();
+    while ((int)h->evpool.size() < 2 * (idx + 1)) {
+      cudaEvent_t e = nullptr;
+      if (cudaEventCreate(&e) != cudaSuccess) return;
+      h->evpool.push_back(e);
+    }
+    cudaEventRecord(h->evpool[2 * idx], h->st);
+    h->cur_phase = phase;
+    h->cur_ev = idx;
+    h->cur_launches = 0;
+  } else if (h->cur_phase == phase && h->cur_ev >= 0) {
+    cudaEventRecord(h->evpool[2 * h->cur_ev + 1], h->st);
+    h->pending.push_back({phase, h->cur_ev, h->cur_launches});
+    h->cur_phase = -1;
+    h->cur_ev = -1;
+  }
 }
+
+inline void nl(mld_gpu_handle* h, long long n) { h->cur_launches += n; }
 
 int build_neighbours(mld_gpu_handle* h) {
   if (!h->has_batch) return fail(h, MLD_ERR_STATE, "no structures staged");
@@ -198,12 +216,16 @@ int build_neighbours(mld_gpu_handle* h) {
   CK(ensure(h, mld_gpu_handle::B_NBR_OFF, sizeof(int) * (h->A + 1)));
   CK(ensure(h, mld_gpu_handle::B_SCAN_TMP, sizeof(int) * ((h->A + 1023) / 1024 + 2)));
   CK(ensure(h, mld_gpu_handle::B_MAXNN, sizeof(int) * 2));
+  CK(ensure(h, mld_gpu_handle::B_POS32, sizeof(float4) * 2 * (size_t)std::max(1, h->A)));
+  b.pos32 = bp_<float4>(h, mld_gpu_handle::B_POS32);
+  b.frac32 = b.pos32 + std::max(1, h->A);
   b.nn = bp_<int>(h, mld_gpu_handle::B_NN);
   b.nbr_off = bp_<int>(h, mld_gpu_handle::B_NBR_OFF);
   int* dmax = bp_<int>(h, mld_gpu_handle::B_MAXNN);
   CK(cudaMemsetAsync(dmax, 0, sizeof(int), h->st));
   CK(launch_neighbours(b, h->cfg.r_cut, b.nn, dmax, h->st, 0));
   CK(launch_scan(b.nn, b.nbr_off, h->A, bp_<int>(h, mld_gpu_handle::B_SCAN_TMP), h->st));
+  nl(h, 5);
   int hv[2] = {0, 0};
   CK(cudaMemcpyAsync(&hv[0], b.nbr_off + h->A, sizeof(int), cudaMemcpyDeviceToHost, h->st));
   CK(cudaMemcpyAsync(&hv[1], dmax, sizeof(int), cudaMemcpyDeviceToHost, h->st));
@@ -219,6 +241,7 @@ int build_neighbours(mld_gpu_handle* h) {
   b.nbr_idx = bp_<int>(h, mld_gpu_handle::B_NBR_IDX);
   b.nbr_u = bp_<double>(h, mld_gpu_handle::B_NBR_U);
   CK(launch_neighbours(b, h->cfg.r_cut, b.nn, dmax, h->st, 1));
+  nl(h, 1);
   h->nbr_valid = true;
   return MLD_OK;
 }
@@ -263,10 +286,12 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
                            bp_<double>(h, mld_gpu_handle::B_WEFS), X, bp_<double>(h, mld_gpu_handle::B_Y),
                            bp_<double>(h, mld_gpu_handle::B_WROW), bp_<int>(h, mld_gpu_handle::B_KIND), h->st));
   }
+  nl(h, 1);
   mark(h, MLD_PHASE_ROWS, 1);
   mark(h, MLD_PHASE_DESCRIPTORS, 0);
   if (!h->quad) {
     CK(launch_bso4_rows<T>(h->dt, h->b, rows, h->bp, X, (T*)nullptr, (T*)nullptr, 1, h->st));
+    nl(h, 1);
   } else {
     // quadratic rows need every atom's B and every pair's dB (mld_forces.F90:410-500)
     const size_t nB = (size_t)std::max(1, h->A) * h->KK, nd = (size_t)std::max<long long>(1, h->b.P) * 3 * h->KK;
@@ -280,6 +305,7 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
     CK(launch_reverse_pairs(h->b, bp_<int>(h, mld_gpu_handle::B_REV), h->st));
     CK(launch_quad_rows<T>(h->b, rows, h->bp, h->KK, bp_<int>(h, mld_gpu_handle::B_REV), Bq, dBq,
                            bp_<T>(h, mld_gpu_handle::B_HQ), X, h->DL, h->st));
+    nl(h, 4);
   }
   mark(h, MLD_PHASE_DESCRIPTORS, 1);
   *Xout = X;
@@ -293,15 +319,17 @@ int solve_any(mld_gpu_handle* h, double* G, const double* rhs, int D, double* w)
   if (D <= 112) {
     CK(launch_solve_sym(G, rhs, D, h->cfg.lambda_krr, h->cfg.svd_rcond, w, bp_<double>(h, mld_gpu_handle::B_EVALS),
                         bp_<int>(h, mld_gpu_handle::B_INFO), h->st));
+    nl(h, 1);
     return MLD_OK;
   }
   CK(ensure(h, mld_gpu_handle::B_GF, sizeof(double) * (size_t)D * D));
   CK(ensure(h, mld_gpu_handle::B_RES, sizeof(double) * D));
-  CK(ensure(h, mld_gpu_handle::B_DW, sizeof(double) * D));
+  CK(ensure(h, mld_gpu_handle::B_DW, sizeof(double) * 3 * (size_t)D));
   CK(ensure(h, mld_gpu_handle::B_INFO, sizeof(int) * 4));
   double* Lf = bp_<double>(h, mld_gpu_handle::B_GF);
   double* r = bp_<double>(h, mld_gpu_handle::B_RES);
   double* dw = bp_<double>(h, mld_gpu_handle::B_DW);
+  double* tmp = dw + D;
   double shift = h->cfg.lambda_krr > 0 ? h->cfg.lambda_krr : 0.0;
   if (shift <= 0) {
     std::vector<double> diag(D);
@@ -315,12 +343,13 @@ int solve_any(mld_gpu_handle* h, double* G, const double* rhs, int D, double* w)
   CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)D * D, cudaMemcpyDeviceToDevice, h->st));
   int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
   CK(launch_cholesky(Lf, D, shift, info, h->st));
-  CK(launch_chol_solve(Lf, D, rhs, w, h->st));
+  CK(launch_chol_solve_blocked(Lf, D, rhs, w, tmp, h->st));
   for (int it = 0; it < 2; ++it) {
     CK(launch_residual(G, D, shift, w, rhs, r, h->st));
-    CK(launch_chol_solve(Lf, D, r, dw, h->st));
+    CK(launch_chol_solve_blocked(Lf, D, r, dw, tmp, h->st));
     CK(launch_axpy(D, 1.0, dw, w, h->st));
   }
+  nl(h, cholesky_launches(D) + 3 * chol_solve_launches(D) + 4);
   int hinfo = 0;
   CK(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
@@ -371,22 +400,167 @@ __global__ void k_sub(long long n, const double* a, const double* b, double* out
 
 // Kernel launches per phase of one fit (neighbours: count, 3 scan kernels, fill; rows: labels
 // kernel; descriptors: fused bispectrum kernel; Gram: tiles, rhs, symmetrise; solve; predict).
-const int kLaunchesPerPhase[MLD_NPHASE] = {5, 1, 1, 3, 1, 1};
-
 void accumulate_profile(mld_gpu_handle* h) {
   if (!h->prof) return;
-  for (int p = 0; p < MLD_NPHASE; ++p) {
+  for (const auto& iv : h->pending) {
     float t = 0.f;
-    if (cudaEventElapsedTime(&t, h->ev[2 * p], h->ev[2 * p + 1]) == cudaSuccess) {
-      h->ms[p] += t;
-      h->launches[p] += kLaunchesPerPhase[p];
-      h->calls[p] += 1;
+    if (cudaEventElapsedTime(&t, h->evpool[2 * iv.ev], h->evpool[2 * iv.ev + 1]) == cudaSuccess) {
+      h->ms[iv.phase] += t;
+      h->launches[iv.phase] += iv.launches;
+      h->calls[iv.phase] += 1;
     }
   }
+  h->pending.clear();
+}
+
+// Plain method, one block of columns [c0, c0 + Db): FP64 Gram on the CUDA cores and the
+// symmetric solve (min-norm Jacobi / Cholesky), parameters.F90:1018-1099.
+int fit_block_plain(mld_gpu_handle* h, const double* X, int c0, int Db, const double* y, long long M, double* w) {
+  double* G = bp_<double>(h, mld_gpu_handle::B_G);
+  double* hv = bp_<double>(h, mld_gpu_handle::B_H);
+  mark(h, MLD_PHASE_GRAM, 0);
+  CK(launch_gram<double>(X + c0, h->ldx, bp_<double>(h, mld_gpu_handle::B_WROW), y, M, Db, G, hv, h->st));
+  nl(h, 3);
+  mark(h, MLD_PHASE_GRAM, 1);
+  mark(h, MLD_PHASE_SOLVE, 0);
+  int rc = solve_any(h, G, hv, Db, w);
+  if (rc) return rc;
+  mark(h, MLD_PHASE_SOLVE, 1);
+  return MLD_OK;
+}
+
+constexpr size_t kGramWorkspaceCap = size_t(8) << 30;  // bf16 planes of one row chunk
+constexpr int kPcgMaxIter = 40;
+constexpr double kPcgTol2 = 1e-22;   // (preconditioned residual / initial)^2 that ends the iteration
+constexpr double kPcgFloor2 = 1e-14; // below this, stagnation also ends it
+
+// Mixed method, one block of columns [c0, c0 + Db) of the FP32 design matrix.
+//  * normal matrix G~ = X^T W X on the tensor cores in BF16 split precision (gram_tc.cu) and
+//    rhs = X^T W y with FP64 accumulation;
+//  * preconditioner: FP64 Cholesky of G~ + diag(max(lambda, rel * G~_ii)), rel = 1e-6 (x10 on
+//    a failed factorisation);
+//  * conjugate gradients on (X^T W X + lambda I) w = X^T W y with FP64-accumulated matvecs
+//    over X itself, so the converged coefficients are those of the FP64 normal equations of
+//    this X, whatever the precision of G~.
+int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const double* y, long long M, double* w,
+                    int stage) {
+  double* G = bp_<double>(h, mld_gpu_handle::B_G);
+  double* hv = bp_<double>(h, mld_gpu_handle::B_H);
+  const double* wrow = bp_<double>(h, mld_gpu_handle::B_WROW);
+  const double lam = h->cfg.lambda_krr > 0 ? h->cfg.lambda_krr : 0.0;
+  mark(h, MLD_PHASE_GRAM, 0);
+  const size_t need = (size_t)4 * Db * (size_t)((std::max<long long>(M, 1) + 63) / 64 * 64) + 256;
+  const size_t wsb = std::max(gram_tc_min_workspace(Db), std::min(need, kGramWorkspaceCap));
+  CK(ensure(h, mld_gpu_handle::B_GWS, wsb));
+  CK(ensure(h, mld_gpu_handle::B_TERR, sizeof(int)));
+  int* terr = bp_<int>(h, mld_gpu_handle::B_TERR);
+  CK(cudaMemsetAsync(G, 0, sizeof(double) * (size_t)Db * Db, h->st));
+  CK(cudaMemsetAsync(terr, 0, sizeof(int), h->st));
+  if (!gram_tc_available()) return fail(h, MLD_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  CK(launch_gram_tc<float>(X, h->ldx, c0, Db, wrow, M, G, bp_<void>(h, mld_gpu_handle::B_GWS), wsb, terr, h->nsm,
+                           h->st));
+  const long long chunk = (long long)((wsb - 256) / (4 * (size_t)Db)) / 64 * 64;
+  nl(h, 2 * ((M + chunk - 1) / chunk));
+  CK(launch_symmetrize(G, Db, h->st));
+  CK(ensure(h, mld_gpu_handle::B_PRED, sizeof(double) * (size_t)std::max<long long>(M, 1)));
+  CK(launch_rhs<float>(X + c0, h->ldx, wrow, y, M, Db, hv, h->nsm, h->st,
+                       bp_<float2>(h, mld_gpu_handle::B_PRED)));
+  nl(h, 2);
+  mark(h, MLD_PHASE_GRAM, 1);
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, terr, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (herr) return fail(h, MLD_ERR_TIMEOUT, "tensor-core Gram: a pipeline wait timed out");
+
+  mark(h, MLD_PHASE_SOLVE, 0);
+  CK(ensure(h, mld_gpu_handle::B_GF, sizeof(double) * (size_t)Db * Db));
+  CK(ensure(h, mld_gpu_handle::B_PCG, sizeof(double) * (7 * (size_t)Db + 8)));
+  CK(ensure(h, mld_gpu_handle::B_INFO, sizeof(int) * 4));
+  CK(ensure(h, mld_gpu_handle::B_PRED, sizeof(double) * (size_t)std::max<long long>(M, 1)));
+  double* Lf = bp_<double>(h, mld_gpu_handle::B_GF);
+  double* r = bp_<double>(h, mld_gpu_handle::B_PCG);
+  double* z = r + Db;
+  double* p = z + Db;
+  double* q = p + Db;
+  double* tmp = q + Db;  // 2 Db
+  double* scal = tmp + 2 * (size_t)Db;
+  float2* sv = bp_<float2>(h, mld_gpu_handle::B_PRED);  // per-row double-FP32 scratch
+  int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
+  double rel = 1e-6;
+  int retries = 0;
+  for (;; ++retries) {
+    CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)Db * Db, cudaMemcpyDeviceToDevice, h->st));
+    CK(launch_shift_diag_rel(Lf, Db, lam, rel, h->st));
+    CK(launch_cholesky(Lf, Db, 0.0, info, h->st));
+    nl(h, 1 + cholesky_launches(Db));
+    int hinfo = 0;
+    CK(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (hinfo == 0) break;
+    if (retries >= 3)
+      return fail(h, MLD_ERR_SOLVE, "preconditioner not positive definite at column " + std::to_string(hinfo));
+    rel *= 10.0;
+  }
+  h->chol_retries += retries;
+  // x0 = 0, r0 = rhs
+  CK(cudaMemsetAsync(w, 0, sizeof(double) * Db, h->st));
+  CK(cudaMemcpyAsync(r, hv, sizeof(double) * Db, cudaMemcpyDeviceToDevice, h->st));
+  CK(launch_chol_solve_blocked(Lf, Db, r, z, tmp, h->st));
+  CK(launch_pcg_beta(Db, z, r, p, scal, 1, h->st));
+  nl(h, chol_solve_launches(Db) + 1);
+  if (Db <= 256) {
+    CK(launch_split_weights(wrow, M, sv, h->st));  // the fused narrow matvec reads w as pairs
+    nl(h, 1);
+  }
+  double hs[2] = {0, 0};
+  double prev = 0.0;
+  int it = 0, slow = 0;
+  for (; it < kPcgMaxIter; ++it) {
+    int nmv = 0;
+    CK(launch_normal_matvec(X + c0, h->ldx, Db, wrow, p, M, lam, sv, q, h->nsm, h->st, &nmv));
+    CK(launch_pcg_alpha(Db, p, q, w, r, scal, h->st));
+    CK(launch_chol_solve_blocked(Lf, Db, r, z, tmp, h->st));
+    CK(launch_pcg_beta(Db, z, r, p, scal, 0, h->st));
+    nl(h, nmv + 2 + chol_solve_launches(Db));
+    CK(cudaMemcpyAsync(hs, scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    const double ratio = hs[1] > 0 ? hs[0] / hs[1] : 0.0;
+    if (!(ratio > kPcgTol2)) {
+      ++it;
+      break;
+    }
+    // stagnation at the FP64 rounding floor of the matvec: three steps without halving r.z
+    slow = (it > 0 && ratio < kPcgFloor2 && hs[0] > 0.5 * prev) ? slow + 1 : 0;
+    prev = hs[0];
+    if (slow >= 3) {
+      ++it;
+      break;
+    }
+  }
+  h->pcg_iters[stage] = it;
+  h->pcg_rel[stage] = hs[1] > 0 ? std::sqrt(std::max(hs[0], 0.0) / hs[1]) : 0.0;
+  mark(h, MLD_PHASE_SOLVE, 1);
+  return MLD_OK;
+}
+
+template <typename T>
+int fit_block(mld_gpu_handle* h, const T* X, int c0, int Db, const double* y, long long M, double* w, int stage);
+template <>
+int fit_block<double>(mld_gpu_handle* h, const double* X, int c0, int Db, const double* y, long long M, double* w,
+                      int) {
+  return fit_block_plain(h, X, c0, Db, y, M, w);
+}
+template <>
+int fit_block<float>(mld_gpu_handle* h, const float* X, int c0, int Db, const double* y, long long M, double* w,
+                     int stage) {
+  return fit_block_mixed(h, X, c0, Db, y, M, w, stage);
 }
 
 template <typename T>
 int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
+  h->pending.clear();
+  h->pcg_iters[0] = h->pcg_iters[1] = 0;
+  h->chol_retries = 0;
   mark(h, MLD_PHASE_NEIGHBOURS, 0);
   int rc = build_neighbours(h);
   if (rc) return rc;
@@ -403,19 +577,11 @@ int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
   CK(ensure(h, mld_gpu_handle::B_EVALS, sizeof(double) * gdim));
   CK(ensure(h, mld_gpu_handle::B_INFO, sizeof(int) * 4));
   CK(ensure(h, mld_gpu_handle::B_SQ, sizeof(double) * 6));
-  double* G = bp_<double>(h, mld_gpu_handle::B_G);
-  double* hv = bp_<double>(h, mld_gpu_handle::B_H);
   double* w = bp_<double>(h, mld_gpu_handle::B_W);
   double* y = bp_<double>(h, mld_gpu_handle::B_Y);
-  double* wrow = bp_<double>(h, mld_gpu_handle::B_WROW);
   // linear block (QNML stage 1, or the whole linear model): parameters.F90:1018-1099
-  mark(h, MLD_PHASE_GRAM, 0);
-  CK(launch_gram<T>(X, h->ldx, wrow, y, M, h->DL, G, hv, h->st));
-  mark(h, MLD_PHASE_GRAM, 1);
-  mark(h, MLD_PHASE_SOLVE, 0);
-  rc = solve_any(h, G, hv, h->DL, w);
+  rc = fit_block<T>(h, X, 0, h->DL, y, M, w, 0);
   if (rc) return rc;
-  mark(h, MLD_PHASE_SOLVE, 1);
   if (h->quad) {
     // QNML stage 2 (parameters.F90:404-421, 476-1015): the quadratic block is fitted to the
     // residual of the linear fit with the same ridge solver
@@ -423,11 +589,13 @@ int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
     CK(ensure(h, mld_gpu_handle::B_YQ, sizeof(double) * std::max<long long>(M, 1)));
     double* pred = bp_<double>(h, mld_gpu_handle::B_PRED);
     double* yq = bp_<double>(h, mld_gpu_handle::B_YQ);
+    mark(h, MLD_PHASE_PREDICT, 0);
     CK(launch_predict_sq<T>(X, h->ldx, w, M, h->DL, pred, nullptr, nullptr, nullptr, h->st));
     k_sub<<<(unsigned)((M + 255) / 256), 256, 0, h->st>>>(M, y, pred, yq);
     CK(cudaGetLastError());
-    CK(launch_gram<T>(X + h->DL, h->ldx, wrow, yq, M, h->DQ, G, hv, h->st));
-    rc = solve_any(h, G, hv, h->DQ, w + h->DL);
+    nl(h, 2);
+    mark(h, MLD_PHASE_PREDICT, 1);
+    rc = fit_block<T>(h, X, h->DL, h->DQ, yq, M, w + h->DL, 1);
     if (rc) return rc;
   }
   double* sq = bp_<double>(h, mld_gpu_handle::B_SQ);
@@ -435,6 +603,7 @@ int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
   CK(cudaMemsetAsync(sq, 0, sizeof(double) * 6, h->st));
   CK(launch_predict_sq<T>(X, h->ldx, w, M, D, nullptr, bp_<double>(h, mld_gpu_handle::B_Y), bp_<int>(h, mld_gpu_handle::B_KIND),
                           sq, h->st));
+  nl(h, 1);
   mark(h, MLD_PHASE_PREDICT, 1);
   double hsq[6];
   std::vector<double> wd(D);
@@ -502,6 +671,7 @@ int mld_gpu_create(const mld_gpu_config* cfg, mld_gpu_handle** out) {
     return MLD_ERR_INVALID;
   }
   cudaError_t e = cudaGetDevice(&h->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete h;
@@ -600,7 +770,7 @@ void mld_gpu_destroy(mld_gpu_handle* h) {
   for (auto& bf : h->bufs)
     if (bf.p) cudaFree(bf.p);
   for (void* p : h->owned) cudaFree(p);
-  for (auto& e : h->ev)
+  for (auto& e : h->evpool)
     if (e) cudaEventDestroy(e);
   for (auto& e : h->tev)
     if (e) cudaEventDestroy(e);
@@ -848,11 +1018,29 @@ int mld_gpu_gram(mld_gpu_handle* h, double* G, double* rhs) {
   CK(ensure(h, mld_gpu_handle::B_G, sizeof(double) * D * D));
   CK(ensure(h, mld_gpu_handle::B_H, sizeof(double) * D));
   if (h->mixed) {
+    // tensor-core BF16 split-precision Gram (the mixed method's normal matrix)
     float* X = nullptr;
     rc = run_rows<float>(h, h->fit_rows, true, &X);
     if (rc) return rc;
-    CK(launch_gram<float>(X, h->ldx, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D,
-                          bp_<double>(h, mld_gpu_handle::B_G), bp_<double>(h, mld_gpu_handle::B_H), h->st));
+    double* dG = bp_<double>(h, mld_gpu_handle::B_G);
+    const size_t need = (size_t)4 * D * (size_t)((std::max<long long>(M, 1) + 63) / 64 * 64) + 256;
+    const size_t wsb = std::max(gram_tc_min_workspace(D), std::min(need, kGramWorkspaceCap));
+    CK(ensure(h, mld_gpu_handle::B_GWS, wsb));
+    CK(ensure(h, mld_gpu_handle::B_TERR, sizeof(int)));
+    int* terr = bp_<int>(h, mld_gpu_handle::B_TERR);
+    CK(cudaMemsetAsync(dG, 0, sizeof(double) * (size_t)D * D, h->st));
+    CK(cudaMemsetAsync(terr, 0, sizeof(int), h->st));
+    if (!gram_tc_available()) return fail(h, MLD_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    CK(launch_gram_tc<float>(X, h->ldx, 0, D, bp_<double>(h, mld_gpu_handle::B_WROW), M, dG,
+                             bp_<void>(h, mld_gpu_handle::B_GWS), wsb, terr, h->nsm, h->st));
+    CK(launch_symmetrize(dG, D, h->st));
+    CK(ensure(h, mld_gpu_handle::B_PRED, sizeof(double) * (size_t)std::max<long long>(M, 1)));
+    CK(launch_rhs<float>(X, h->ldx, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D,
+                         bp_<double>(h, mld_gpu_handle::B_H), h->nsm, h->st, bp_<float2>(h, mld_gpu_handle::B_PRED)));
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, terr, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (herr) return fail(h, MLD_ERR_TIMEOUT, "tensor-core Gram: a pipeline wait timed out");
   } else {
     double* X = nullptr;
     rc = run_rows<double>(h, h->fit_rows, true, &X);
@@ -936,10 +1124,9 @@ int mld_gpu_predict(mld_gpu_handle* h, const double* w_params, double* E, double
 
 int mld_gpu_set_profiling(mld_gpu_handle* h, int on) {
   if (!h) return MLD_ERR_INVALID;
-  if (on && !h->ev[0]) {
-    for (auto& e : h->ev) CK(cudaEventCreate(&e));
-  }
   h->prof = on != 0;
+  h->pending.clear();
+  h->cur_phase = h->cur_ev = -1;
   return MLD_OK;
 }
 
@@ -1017,4 +1204,105 @@ extern "C" int mld_gpu_peak_flops(mld_gpu_handle* h, int precision, double* tflo
   cudaError_t e = precision == MLD_PRECISION_MIXED ? mld::measure_fma_peak<float>(h->st, tflops)
                                                    : mld::measure_fma_peak<double>(h->st, tflops);
   return e == cudaSuccess ? MLD_OK : cuda_fail(h, e, "mld_gpu_peak_flops");
+}
+
+extern "C" int mld_gpu_solve_info(const mld_gpu_handle* h, int* pcg_iterations, double* pcg_residual,
+                                  int* chol_retries) {
+  if (!h) return MLD_ERR_INVALID;
+  for (int s = 0; s < 2; ++s) {
+    if (pcg_iterations) pcg_iterations[s] = h->pcg_iters[s];
+    if (pcg_residual) pcg_residual[s] = h->pcg_rel[s];
+  }
+  if (chol_retries) *chol_retries = h->chol_retries;
+  return MLD_OK;
+}
+
+namespace {
+int set_err(char* err, int err_len, int code, const std::string& msg) {
+  if (err && err_len > 0) {
+    std::strncpy(err, msg.c_str(), (size_t)err_len - 1);
+    err[err_len - 1] = 0;
+  }
+  return code;
+}
+}  // namespace
+
+extern "C" int mld_gpu_gram_rows(int method, const void* X, int x_is_fp32, long long M, int D, int ldx,
+                                 const double* w, const double* y, double* G, double* rhs, void* stream, char* err,
+                                 int err_len) {
+  if (!X || !w || !G || D < 1 || M < 0 || ldx < D || (rhs && !y))
+    return set_err(err, err_len, MLD_ERR_INVALID, "invalid argument");
+  if (method != MLD_PRECISION_PLAIN_FP64 && method != MLD_PRECISION_MIXED)
+    return set_err(err, err_len, MLD_ERR_INVALID, "method must be MLD_PRECISION_PLAIN_FP64 or MLD_PRECISION_MIXED");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int dev = 0, nsm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  void* ws = nullptr;
+  double* hbuf = nullptr;
+  int* terr = nullptr;
+  auto cleanup = [&]() {
+    if (ws) cudaFree(ws);
+    if (hbuf) cudaFree(hbuf);
+    if (terr) cudaFree(terr);
+  };
+  auto cuda_err = [&](cudaError_t ce, const char* where) {
+    cleanup();
+    return set_err(err, err_len, ce == cudaErrorMemoryAllocation ? MLD_ERR_OOM : MLD_ERR_CUDA,
+                   std::string(where) + ": " + cudaGetErrorString(ce));
+  };
+  if (e != cudaSuccess) return cuda_err(e, "device query");
+  if (method == MLD_PRECISION_PLAIN_FP64) {
+    double* hv = rhs;
+    const double* yy = y;
+    if (!hv) {
+      e = cudaMalloc(&hbuf, sizeof(double) * (size_t)D + sizeof(double) * (size_t)std::max<long long>(M, 1));
+      if (e != cudaSuccess) return cuda_err(e, "cudaMalloc");
+      hv = hbuf;
+      double* yz = hbuf + D;
+      e = cudaMemsetAsync(yz, 0, sizeof(double) * (size_t)std::max<long long>(M, 1), st);
+      if (e != cudaSuccess) return cuda_err(e, "cudaMemsetAsync");
+      yy = yz;
+    }
+    e = x_is_fp32 ? launch_gram<float>(static_cast<const float*>(X), ldx, w, yy, M, D, G, hv, st)
+                  : launch_gram<double>(static_cast<const double*>(X), ldx, w, yy, M, D, G, hv, st);
+    if (e != cudaSuccess) return cuda_err(e, "launch_gram");
+  } else {
+    if (!gram_tc_available())
+      return set_err(err, err_len, MLD_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    const size_t need = (size_t)4 * D * (size_t)((std::max<long long>(M, 1) + 63) / 64 * 64) + 256;
+    const size_t wsb = std::max(gram_tc_min_workspace(D), std::min(need, kGramWorkspaceCap));
+    e = cudaMalloc(&ws, wsb);
+    if (e == cudaSuccess) e = cudaMalloc(&terr, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(terr, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(G, 0, sizeof(double) * (size_t)D * D, st);
+    if (e != cudaSuccess) return cuda_err(e, "workspace");
+    e = x_is_fp32 ? launch_gram_tc<float>(static_cast<const float*>(X), ldx, 0, D, w, M, G, ws, wsb, terr, nsm, st)
+                  : launch_gram_tc<double>(static_cast<const double*>(X), ldx, 0, D, w, M, G, ws, wsb, terr, nsm, st);
+    if (e == cudaSuccess) e = launch_symmetrize(G, D, st);
+    float2* sv = nullptr;
+    if (e == cudaSuccess && rhs && x_is_fp32) {
+      e = cudaMalloc(&sv, sizeof(float2) * (size_t)std::max<long long>(M, 1));
+      if (e == cudaSuccess) e = launch_rhs<float>(static_cast<const float*>(X), ldx, w, y, M, D, rhs, nsm, st, sv);
+    } else if (e == cudaSuccess && rhs) {
+      e = launch_rhs<double>(static_cast<const double*>(X), ldx, w, y, M, D, rhs, nsm, st, nullptr);
+    }
+    if (sv) {
+      cudaStreamSynchronize(st);
+      cudaFree(sv);
+    }
+    if (e != cudaSuccess) return cuda_err(e, "launch_gram_tc");
+    int herr = 0;
+    e = cudaMemcpyAsync(&herr, terr, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_err(e, "synchronize");
+    if (herr) {
+      cleanup();
+      return set_err(err, err_len, MLD_ERR_TIMEOUT, "tensor-core Gram: a pipeline wait timed out");
+    }
+  }
+  e = cudaStreamSynchronize(st);
+  cleanup();
+  if (e != cudaSuccess) return set_err(err, err_len, MLD_ERR_CUDA, cudaGetErrorString(e));
+  return set_err(err, err_len, MLD_OK, "");
 }

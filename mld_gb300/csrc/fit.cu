@@ -11,6 +11,9 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <algorithm>
+#include <type_traits>
+
 #include "mld_internal.h"
 
 namespace mld {
@@ -106,19 +109,6 @@ __global__ void __launch_bounds__(256) k_gram(const T* __restrict__ X, int ldx, 
     }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) k_rhs(const T* __restrict__ X, int ldx, const double* __restrict__ w,
-                                             const double* __restrict__ y, long long M, int D,
-                                             long long rows_per_block, double* __restrict__ h) {
-  const long long r0 = (long long)blockIdx.x * rows_per_block;
-  const long long r1 = min(M, r0 + rows_per_block);
-  for (int c = threadIdx.x; c < D; c += blockDim.x) {
-    double acc = 0;
-    for (long long r = r0; r < r1; ++r) acc = fma((double)X[r * ldx + c], w[r] * y[r], acc);
-    atomicAdd(&h[c], acc);
-  }
-}
-
 __global__ void k_symmetrize(double* G, int D) {
   const int i = blockIdx.x, j = threadIdx.x;
   for (int jj = j; jj < D; jj += blockDim.x)
@@ -149,13 +139,326 @@ cudaError_t launch_gram(const T* X, int ldx, const double* w, const double* y, l
     rpb = (M + chunks - 1) / chunks;
   }
   k_gram<T><<<dim3(npairs, (unsigned)chunks), 256, 0, st>>>(X, ldx, w, M, D, rpb, G);
-  long long hch = (long long)nsm * 4;
-  long long hrpb = (M + hch - 1) / hch;
-  hch = (M + hrpb - 1) / hrpb;
-  k_rhs<T><<<(unsigned)hch, 128, 0, st>>>(X, ldx, w, y, M, D, hrpb, h);
+  e = launch_rhs<T>(X, ldx, w, y, M, D, h, nsm, st, nullptr);
+  if (e != cudaSuccess) return e;
   k_symmetrize<<<D, 128, 0, st>>>(G, D);
   return cudaGetLastError();
 }
+
+// q[c] = sum_r w[r] v[r] X[r][c] (FP64 accumulation).  Columns in blocks of 256 (8 per lane,
+// blockIdx.y), design rows in chunks (blockIdx.x) walked by the 8 warps; per-CTA partial sums
+// are reduced in shared memory and added to q with one atomic per column.
+template <typename T>
+__global__ void __launch_bounds__(256) k_xtv(const T* __restrict__ X, int ldx, int D, const double* __restrict__ w,
+                                             const double* __restrict__ v, long long M, long long rpb,
+                                             double* __restrict__ q) {
+  __shared__ double red[8][256];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int cb = blockIdx.y * 256;
+  const long long r0 = (long long)blockIdx.x * rpb, r1 = min(M, r0 + rpb);
+  double acc[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc[k] = 0.0;
+  for (long long r = r0 + warp; r < r1; r += 8) {
+    const double s = w[r] * v[r];
+    const T* xr = X + r * ldx + cb;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int c = lane + 32 * k;
+      if (cb + c < D) acc[k] = fma((double)xr[c], s, acc[k]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) red[warp][lane + 32 * k] = acc[k];
+  __syncthreads();
+  double sum = 0.0;
+#pragma unroll
+  for (int w8 = 0; w8 < 8; ++w8) sum += red[w8][threadIdx.x];
+  if (cb + threadIdx.x < D && sum != 0.0) atomicAdd(&q[cb + threadIdx.x], sum);
+}
+
+// ------------------------------------------------------------------------------------
+// Double-FP32 ("double-single") arithmetic for the refinement matvecs of the mixed method.
+// GB300 issues FP64 at 1/64 of its FP32 rate, so the FP64-accumulated products of the
+// refinement are formed from FP32 error-free transformations instead: TwoSum (Knuth) and
+// TwoProd via fmaf give sums and products as unevaluated pairs hi + lo, about 2^-44 relative
+// to the sum of the magnitudes.  X is FP32, so x * (p_hi + p_lo) is formed exactly up to the
+// x * p_lo term.
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+// (sh, sl) += x * (ph + pl)
+__device__ __forceinline__ void ds_fma(float& sh, float& sl, float x, float ph, float pl) {
+  const float p = x * ph;
+  const float pe = fmaf(x, pl, fmaf(x, ph, -p));
+  float t, e;
+  two_sum(sh, p, t, e);
+  sh = t;
+  sl += e + pe;
+}
+// (sh, sl) += (oh, ol)
+__device__ __forceinline__ void ds_add(float& sh, float& sl, float oh, float ol) {
+  float t, e;
+  two_sum(sh, oh, t, e);
+  sh = t;
+  sl += e + ol;
+}
+__device__ __forceinline__ void ds_norm(float& sh, float& sl) {
+  const float t = sh + sl;
+  sl = sl - (t - sh);
+  sh = t;
+}
+__device__ __forceinline__ void ds_split(double v, float& h, float& l) {
+  h = (float)v;
+  l = (float)(v - (double)h);
+}
+
+// Normal-equation matvec of a narrow block (D <= 32*NK <= 256) in one pass over X:
+// q = sum_r w[r] (x_r . p) x_r, the row held in registers between the dot and the update.
+template <int NK>
+__global__ void __launch_bounds__(256) k_normal_matvec_narrow(const float* __restrict__ X, int ldx, int D,
+                                                              const float2* __restrict__ wds,
+                                                              const double* __restrict__ p, long long M, long long rpb,
+                                                              double* __restrict__ q) {
+  __shared__ double red[8][32 * NK];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float ph[NK], pl[NK], ah[NK], al[NK];
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
+    const int c = lane + 32 * k;
+    ds_split(c < D ? p[c] : 0.0, ph[k], pl[k]);
+    ah[k] = al[k] = 0.f;
+  }
+  // four design rows per warp step keep four row loads in flight
+  constexpr int RU = 4;
+  const long long r0 = (long long)blockIdx.x * rpb, r1 = min(M, r0 + rpb);
+  int step = 0;
+  for (long long rb = r0 + RU * warp; rb < r1; rb += RU * 8, ++step) {
+    float x[RU][NK];
+    float dh[RU], dl[RU];
+#pragma unroll
+    for (int u = 0; u < RU; ++u) {
+      const long long r = rb + u;
+      const float* xr = X + min(r, r1 - 1) * ldx;
+#pragma unroll
+      for (int k = 0; k < NK; ++k) {
+        const int c = lane + 32 * k;
+        x[u][k] = (c < D && r < r1) ? xr[c] : 0.f;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < RU; ++u) {
+      dh[u] = dl[u] = 0.f;
+#pragma unroll
+      for (int k = 0; k < NK; ++k) ds_fma(dh[u], dl[u], x[u][k], ph[k], pl[k]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int u = 0; u < RU; ++u) {
+        const float oh = __shfl_xor_sync(0xffffffffu, dh[u], o), ol = __shfl_xor_sync(0xffffffffu, dl[u], o);
+        ds_add(dh[u], dl[u], oh, ol);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < RU; ++u) {
+      const long long r = rb + u;
+      // s = w_r * d as a pair (zero past the chunk)
+      const float2 wv = r < r1 ? wds[r] : make_float2(0.f, 0.f);
+      const float wh = wv.x, wl = wv.y;
+      const float sp = dh[u] * wh;
+      const float se = fmaf(dh[u], wl, fmaf(dl[u], wh, fmaf(dh[u], wh, -sp)));
+      const float sh = sp + se;
+      const float sl = se - (sh - sp);
+#pragma unroll
+      for (int k = 0; k < NK; ++k) ds_fma(ah[k], al[k], x[u][k], sh, sl);
+    }
+    if ((step & 63) == 63) {
+#pragma unroll
+      for (int k = 0; k < NK; ++k) ds_norm(ah[k], al[k]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NK; ++k) red[warp][lane + 32 * k] = (double)ah[k] + (double)al[k];
+  __syncthreads();
+  for (int c = threadIdx.x; c < 32 * NK; c += 256) {
+    double sum = 0.0;
+#pragma unroll
+    for (int w8 = 0; w8 < 8; ++w8) sum += red[w8][c];
+    if (c < D && sum != 0.0) atomicAdd(&q[c], sum);
+  }
+}
+
+// sv[r] = w[r] * (x_r . p) as a double-FP32 pair (warp per design row)
+__global__ void __launch_bounds__(256) k_xp_ds(const float* __restrict__ X, int ldx, int D,
+                                               const double* __restrict__ w, const double* __restrict__ p, long long M,
+                                               float2* __restrict__ sv) {
+  extern __shared__ float pp[];  // [2][D]
+  for (int c = threadIdx.x; c < D; c += blockDim.x) ds_split(p[c], pp[c], pp[D + c]);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long r = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < M; r += nw) {
+    const float* xr = X + r * ldx;
+    float dh = 0.f, dl = 0.f;
+    for (int c = lane; c < D; c += 32) ds_fma(dh, dl, xr[c], pp[c], pp[D + c]);
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, dh, o), ol = __shfl_xor_sync(0xffffffffu, dl, o);
+      ds_add(dh, dl, oh, ol);
+    }
+    if (lane == 0) {
+      const double s = ((double)dh + (double)dl) * w[r];
+      float h, l;
+      ds_split(s, h, l);
+      sv[r] = make_float2(h, l);
+    }
+  }
+}
+
+// wds[r] = w[r] as a double-FP32 pair
+__global__ void k_w_ds(const double* __restrict__ w, long long M, float2* __restrict__ wds) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= M) return;
+  float h, l;
+  ds_split(w[r], h, l);
+  wds[r] = make_float2(h, l);
+}
+
+// sv[r] = w[r] * y[r] as a double-FP32 pair
+__global__ void k_wy_ds(const double* __restrict__ w, const double* __restrict__ y, long long M,
+                        float2* __restrict__ sv) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= M) return;
+  float h, l;
+  ds_split(w[r] * y[r], h, l);
+  sv[r] = make_float2(h, l);
+}
+
+// q[c] = sum_r sv[r] X[r][c] with double-FP32 accumulation; columns in blocks of 256
+// (blockIdx.y), design rows in chunks (blockIdx.x) walked by the 8 warps.
+__global__ void __launch_bounds__(256) k_xtv_ds(const float* __restrict__ X, int ldx, int D,
+                                                const float2* __restrict__ sv, long long M, long long rpb,
+                                                double* __restrict__ q) {
+  __shared__ double red[8][256];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int cb = blockIdx.y * 256;
+  const long long r0 = (long long)blockIdx.x * rpb, r1 = min(M, r0 + rpb);
+  float ah[8], al[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) ah[k] = al[k] = 0.f;
+  for (long long r = r0 + warp; r < r1; r += 8) {
+    const float2 s = sv[r];
+    const float* xr = X + r * ldx + cb;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int c = lane + 32 * k;
+      if (cb + c < D) ds_fma(ah[k], al[k], xr[c], s.x, s.y);
+    }
+    if (((r - r0) & 511) == 504) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) ds_norm(ah[k], al[k]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) red[warp][lane + 32 * k] = (double)ah[k] + (double)al[k];
+  __syncthreads();
+  double sum = 0.0;
+#pragma unroll
+  for (int w8 = 0; w8 < 8; ++w8) sum += red[w8][threadIdx.x];
+  if (cb + threadIdx.x < D && sum != 0.0) atomicAdd(&q[cb + threadIdx.x], sum);
+}
+
+namespace {
+// design-row chunk per CTA so that about 8 CTAs per SM run over all column blocks
+long long rows_per_cta(long long M, int ncb, int nsm) {
+  long long ctas = std::max<long long>(1, (long long)nsm * 8 / std::max(1, ncb));
+  long long rpb = (M + ctas - 1) / ctas;
+  return std::max<long long>(64, rpb);
+}
+}  // namespace
+
+// h = X^T diag(w) y: double-FP32 accumulation for an FP32 X when `sv` (M float2 of scratch) is
+// given, FP64 accumulation otherwise
+template <typename T>
+cudaError_t launch_rhs(const T* X, int ldx, const double* w, const double* y, long long M, int D, double* h,
+                       int nsm, cudaStream_t st, float2* sv) {
+  cudaError_t e = cudaMemsetAsync(h, 0, sizeof(double) * (size_t)D, st);
+  if (e != cudaSuccess || M == 0) return e;
+  const int ncb = (D + 255) / 256;
+  const long long rpb = rows_per_cta(M, ncb, nsm);
+  const long long nrb = (M + rpb - 1) / rpb;
+  if constexpr (std::is_same<T, float>::value) {
+    if (sv) {
+      k_wy_ds<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(w, y, M, sv);
+      k_xtv_ds<<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(X, ldx, D, sv, M, rpb, h);
+      return cudaGetLastError();
+    }
+  }
+  k_xtv<T><<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(X, ldx, D, w, y, M, rpb, h);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_split_weights(const double* w, long long M, float2* wds, cudaStream_t st) {
+  if (M > 0) k_w_ds<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(w, M, wds);
+  return cudaGetLastError();
+}
+
+// q = X^T W X p (+ lambda p) for an FP32 X in double-FP32 arithmetic: one fused pass for
+// D <= 256 (weights as pairs in sv, from launch_split_weights), else sv = W X p then X^T sv
+// (sv: M float2 of scratch).  *launches: kernels issued.
+cudaError_t launch_normal_matvec(const float* X, int ldx, int D, const double* w, const double* p, long long M,
+                                 double lambda, float2* sv, double* q, int nsm, cudaStream_t st, int* launches) {
+  cudaError_t e = cudaMemsetAsync(q, 0, sizeof(double) * (size_t)D, st);
+  if (e != cudaSuccess) return e;
+  *launches = 0;
+  if (M > 0 && D <= 256) {
+    const long long rpb = rows_per_cta(M, 1, nsm);
+    const unsigned nrb = (unsigned)((M + rpb - 1) / rpb);
+    switch ((D + 31) / 32) {
+      case 1: k_normal_matvec_narrow<1><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
+      case 2: k_normal_matvec_narrow<2><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
+      case 3: k_normal_matvec_narrow<3><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
+      case 4: k_normal_matvec_narrow<4><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
+      case 5: k_normal_matvec_narrow<5><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
+      case 6: k_normal_matvec_narrow<6><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
+      case 7: k_normal_matvec_narrow<7><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
+      default: k_normal_matvec_narrow<8><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
+    }
+    *launches = 1;
+  } else if (M > 0) {
+    const size_t smem = sizeof(float) * 2 * (size_t)D;
+    if (smem > 48 * 1024) {
+      e = cudaFuncSetAttribute(k_xp_ds, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    k_xp_ds<<<(unsigned)(nsm * 8), 256, smem, st>>>(X, ldx, D, w, p, M, sv);
+    const int ncb = (D + 255) / 256;
+    const long long rpb = rows_per_cta(M, ncb, nsm);
+    const long long nrb = (M + rpb - 1) / rpb;
+    k_xtv_ds<<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(X, ldx, D, sv, M, rpb, q);
+    *launches = 2;
+  }
+  if (lambda > 0) {
+    e = launch_axpy(D, lambda, p, q, st);
+    *launches += 1;
+  }
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_rhs<double>(const double*, int, const double*, const double*, long long, int, double*, int,
+                                        cudaStream_t, float2*);
+template cudaError_t launch_rhs<float>(const float*, int, const double*, const double*, long long, int, double*, int,
+                                       cudaStream_t, float2*);
+
+// lower triangle <- upper triangle
+cudaError_t launch_symmetrize(double* G, int D, cudaStream_t st) {
+  k_symmetrize<<<D, 128, 0, st>>>(G, D);
+  return cudaGetLastError();
+}
+
 
 // ------------------------------------------------------------------------------------
 // Symmetric min-norm solve by parallel cyclic Jacobi (one CTA, D <= kJacobiMax).
@@ -310,24 +613,59 @@ cudaError_t launch_solve_sym(double* G, const double* h, int D, double lambda, d
 // ------------------------------------------------------------------------------------
 // predictions and squared-error sums per row kind (0 energy, 1 force, 2 stress)
 // ------------------------------------------------------------------------------------
+// Predictions X w (warp per design row, grid-stride) and per-kind squared errors: FP64 dot for
+// an FP64 X, double-FP32 dot for an FP32 X (w split into FP32 pairs in shared memory).  The
+// squared errors are reduced per block before six FP64 atomics.
 template <typename T>
-__global__ void k_predict(const T* __restrict__ X, int ldx, const double* __restrict__ w, long long M, int D,
-                          double* __restrict__ pred, const double* __restrict__ y, const int* __restrict__ kind,
-                          double* __restrict__ sq /*3 sums + 3 counts*/) {
-  const int lane = threadIdx.x & 31;
-  const long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (r >= M) return;
-  double acc = 0;
-  for (int c = lane; c < D; c += 32) acc = fma((double)X[r * ldx + c], w[c], acc);
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) {
-    if (pred) pred[r] = acc;
-    if (sq) {
-      double d = acc - y[r];
-      int k = kind[r];
-      atomicAdd(&sq[k], d * d);
-      atomicAdd(&sq[3 + k], 1.0);
+__global__ void __launch_bounds__(256) k_predict(const T* __restrict__ X, int ldx, const double* __restrict__ w,
+                                                 long long M, int D, double* __restrict__ pred,
+                                                 const double* __restrict__ y, const int* __restrict__ kind,
+                                                 double* __restrict__ sq /*3 sums + 3 counts*/) {
+  extern __shared__ float wsp[];  // [2][D] for FP32 X
+  __shared__ double red[8][6];
+  constexpr bool kDs = std::is_same<T, float>::value;
+  if (kDs) {
+    for (int c = threadIdx.x; c < D; c += blockDim.x) ds_split(w[c], wsp[c], wsp[D + c]);
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double acc6[6] = {0, 0, 0, 0, 0, 0};
+  const long long nw = (long long)gridDim.x * 8;
+  for (long long r = (long long)blockIdx.x * 8 + warp; r < M; r += nw) {
+    const T* xr = X + r * ldx;
+    double v;
+    if constexpr (kDs) {
+      float dh = 0.f, dl = 0.f;
+      for (int c = lane; c < D; c += 32) ds_fma(dh, dl, xr[c], wsp[c], wsp[D + c]);
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, dh, o), ol = __shfl_xor_sync(0xffffffffu, dl, o);
+        ds_add(dh, dl, oh, ol);
+      }
+      v = (double)dh + (double)dl;
+    } else {
+      double a = 0.0;
+      for (int c = lane; c < D; c += 32) a = fma((double)xr[c], w[c], a);
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      v = a;
     }
+    if (lane == 0) {
+      if (pred) pred[r] = v;
+      if (sq) {
+        const double d = v - y[r];
+        const int k = kind[r];
+        acc6[k] += d * d;
+        acc6[3 + k] += 1.0;
+      }
+    }
+  }
+  if (!sq) return;
+  if (lane == 0)
+    for (int k = 0; k < 6; ++k) red[warp][k] = acc6[k];
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double t = 0.0;
+    for (int w8 = 0; w8 < 8; ++w8) t += red[w8][threadIdx.x];
+    if (t != 0.0) atomicAdd(&sq[threadIdx.x], t);
   }
 }
 
@@ -335,9 +673,20 @@ template <typename T>
 cudaError_t launch_predict_sq(const T* X, int ldx, const double* w, long long M, int D, double* pred,
                               const double* y, const int* kind, double* sq, cudaStream_t st) {
   if (M == 0) return cudaSuccess;
-  long long threads = M * 32;
-  unsigned blocks = (unsigned)((threads + 255) / 256);
-  k_predict<T><<<blocks, 256, 0, st>>>(X, ldx, w, M, D, pred, y, kind, sq);
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (M + 7) / 8;
+  const unsigned blocks = (unsigned)std::min<long long>(want, (long long)nsm * 8);
+  size_t smem = 0;
+  if (std::is_same<T, float>::value) {
+    smem = sizeof(float) * 2 * (size_t)D;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k_predict<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  k_predict<T><<<blocks, 256, smem, st>>>(X, ldx, w, M, D, pred, y, kind, sq);
   return cudaGetLastError();
 }
 

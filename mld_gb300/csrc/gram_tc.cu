@@ -1,0 +1,391 @@
+// Weighted Gram matrix G = X^T W X on the 5th-generation tensor cores (tcgen05) in BF16 split
+// precision with FP32 accumulation: the mixed method's normal matrix (parameters.F90:1018-1099
+// for the linear block, :404-421,476-1015 for the quadratic block of the QNML fit).
+//
+//   x' = sqrt(w_r) x_r,  x' = hi + lo  (hi = bf16(x'), lo = bf16(x' - hi)),
+//   x'_i x'_j ~= hi_i hi_j + hi_i lo_j + lo_i hi_j      (three bf16 MMAs per K step)
+//
+// A row chunk of X is first transposed into K-major bf16 planes Xt_hi / Xt_lo (D x Mp, the design
+// row index contiguous), so both MMA operands of an output tile (features i, features j) are
+// 128 x 64 K-major slices of the same planes, fetched by TMA with 128-byte swizzle.  Feature rows
+// beyond D and design rows beyond the chunk are zero-filled by TMA.
+//
+// Grid: (upper-triangle tile pairs) x (row splits), split-major so that the CTAs resident at one
+// time read the same rows (L2 reuse).  Per CTA: warp 0 issues TMA loads into a 3-stage ring,
+// warp 1 allocates two 128-column TMEM accumulators and issues tcgen05.mma from one thread,
+// warps 2-17 drain the accumulators with tcgen05.ld into compensated FP32 sums and finally add
+// them into the FP64 Gram with atomics (one FP64 add per element and split).  Every mbarrier wait
+// is bounded: on expiry the CTA sets *err, waits (bounded) for its copies in flight and still
+// frees its TMEM.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "mld_internal.h"
+
+namespace mld {
+
+namespace {
+
+constexpr int kTM = 128;                       // tile rows (i) = tile columns (j)
+constexpr int kTK = 64;                        // design rows per stage: 128 bytes of bf16, one swizzle row
+constexpr int kStages = 3;
+constexpr int kTileBytes = kTM * kTK * 2;      // 16 KB per operand tile
+constexpr int kStageBytes = 4 * kTileBytes;    // A_hi, A_lo, B_hi, B_lo
+constexpr int kFlush = 2;                      // K slices per TMEM accumulation (128 design rows)
+constexpr int kEpiWarps = 16;                  // four per TMEM lane quarter, 32 columns each
+constexpr int kGramThreads = 32 * (2 + kEpiWarps);
+constexpr size_t kGramSmem = (size_t)kStages * kStageBytes + 1024 + 256;
+constexpr long long kWaitLimit = 2000000000LL;  // SM clocks (about one second)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait for the phase of the given parity; false on expiry
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > kWaitLimit) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major tile written by TMA with 128-byte swizzle:
+// rows of 128 bytes, 8-row core groups 1024 bytes apart (stride byte offset), version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);  // start address, bits 0-13
+  d |= (uint64_t)1 << 16;                    // leading byte offset (not used by swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset, bits 32-45
+  d |= (uint64_t)1 << 46;                    // descriptor version
+  d |= (uint64_t)2 << 61;                    // 128-byte swizzle
+  return d;
+}
+
+// kind::f16 instruction descriptor: D FP32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1),
+// both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28; M = N = 128.
+constexpr uint32_t kIdesc =
+    (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTM >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+}  // namespace
+
+// Transpose rows [r0, r0 + rows) of X (row stride ldx, columns [c0, c0 + D)) into the K-major
+// bf16 planes hi/lo (D x Mp), scaling row r by sqrt(w[r]); design rows [rows, Mp) are zeroed.
+// grid.x: 32-row blocks of the chunk, grid.y: 32-column blocks.
+template <typename T>
+__global__ void __launch_bounds__(256) k_split_bf16(const T* __restrict__ X, int ldx, int c0, int D,
+                                                    const double* __restrict__ w, long long r0, long long rows,
+                                                    long long Mp, __nv_bfloat16* __restrict__ hi,
+                                                    __nv_bfloat16* __restrict__ lo) {
+  __shared__ float tile[32][33];
+  __shared__ double sw[32];
+  const long long rb = (long long)blockIdx.x * 32;
+  const int cb = blockIdx.y * 32;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  if (tid < 32) sw[tid] = (rb + tid < rows) ? sqrt(w[r0 + rb + tid]) : 0.0;
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const long long r = rb + y;
+    const int c = cb + threadIdx.x;
+    float v = 0.f;
+    if (r < rows && c < D) v = (float)((double)X[(r0 + r) * ldx + c0 + c] * sw[y]);
+    tile[y][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int c = cb + y;
+    const long long r = rb + threadIdx.x;
+    if (c < D && r < Mp) {
+      const float v = tile[threadIdx.x][y];
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      hi[(size_t)c * Mp + r] = h;
+      lo[(size_t)c * Mp + r] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+  }
+}
+
+// blockIdx.x = tile + ntile * split; tile enumerates the upper-triangle pairs ti <= tj.
+// Row split s covers K slices [s * kps, min(nk, (s + 1) * kps)) of 64 design rows.
+//
+// The FP32 accumulator lives in TMEM for `flush` K slices only (kFlush = 2: 128 design rows), because
+// the tensor core rounds its FP32 accumulation toward zero (a bias that grows with the chain): the MMA issuer
+// alternates between two 128-column TMEM buffers, and the epilogue warps drain the idle buffer
+// into compensated (Kahan) FP32 register sums, so the error of the whole split stays at the
+// level of one short FP32 accumulation.  Epilogue warp w reads TMEM lane quarter w % 4 and one
+// quarter (32 columns) of the tile.
+__global__ void __launch_bounds__(kGramThreads, 1)
+    k_gram_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo, int nt,
+              int ntile, int nk, int kps, int flush, int D, double* __restrict__ G, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* tiles = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = reinterpret_cast<uint64_t*>(tiles + kStages * kStageBytes);
+  uint64_t* empty = full + kStages;
+  uint64_t* tfull = empty + kStages;  // [2] accumulator buffer ready for the epilogue
+  uint64_t* tempty = tfull + 2;       // [2] accumulator buffer drained
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
+
+  int t = blockIdx.x % ntile, ti = 0;
+  const int split = blockIdx.x / ntile;
+  while (t >= nt - ti) {
+    t -= nt - ti;
+    ++ti;
+  }
+  const int tj = ti + t;
+  const int kb = split * kps;
+  const int nkl = min(nk, kb + kps) - kb;  // >= 1 by construction of the grid
+  const int ngrp = (nkl + flush - 1) / flush;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], kEpiWarps);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(2 * kTM));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+  bool ok = true;
+
+  if (warp == 0 && lane == 0) {
+    // producer: A = features of tile ti, B = features of tile tj
+    int issued = 0;
+    for (int k = 0; k < nkl; ++k) {
+      const int s = k % kStages;
+      if (k >= kStages && !mbar_wait(&empty[s], ((k / kStages) - 1) & 1)) {
+        ok = false;
+        break;
+      }
+      unsigned char* st = tiles + s * kStageBytes;
+      const int x = (kb + k) * kTK;
+      mbar_expect_tx(&full[s], kStageBytes);
+      tma_load_2d(st, &map_hi, x, ti * kTM, &full[s]);
+      tma_load_2d(st + kTileBytes, &map_lo, x, ti * kTM, &full[s]);
+      tma_load_2d(st + 2 * kTileBytes, &map_hi, x, tj * kTM, &full[s]);
+      tma_load_2d(st + 3 * kTileBytes, &map_lo, x, tj * kTM, &full[s]);
+      issued = k + 1;
+    }
+    // the copies issued last may still be in flight: wait for them (bounded) before leaving
+    for (int k = max(0, issued - kStages); k < issued; ++k) mbar_wait(&full[k % kStages], (k / kStages) & 1);
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer: K-slice group g accumulates into TMEM buffer g & 1
+    for (int g = 0; g < ngrp && ok; ++g) {
+      const int b = g & 1;
+      if (g >= 2 && !mbar_wait(&tempty[b], ((g >> 1) - 1) & 1)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t acc = tmem + (uint32_t)(b * kTM);
+      const int k1 = min(nkl, (g + 1) * flush);
+      for (int k = g * flush; k < k1; ++k) {
+        const int s = k % kStages;
+        if (!mbar_wait(&full[s], (k / kStages) & 1)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t st = smem_u32(tiles + s * kStageBytes);
+#pragma unroll
+        for (int kk = 0; kk < kTK / 16; ++kk) {
+          const uint32_t off = kk * 32;  // 16 bf16 along K inside the 128-byte swizzle row
+          const uint64_t ahi = sw128_desc(st + off), alo = sw128_desc(st + kTileBytes + off);
+          const uint64_t bhi = sw128_desc(st + 2 * kTileBytes + off), blo = sw128_desc(st + 3 * kTileBytes + off);
+          mma_bf16(acc, ahi, bhi, (k > g * flush || kk > 0) ? 1u : 0u);
+          mma_bf16(acc, ahi, blo, 1u);
+          mma_bf16(acc, alo, bhi, 1u);
+        }
+        mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
+      }
+      mma_commit(&tfull[b]);
+    }
+  } else if (warp >= 2) {
+    // epilogue: Kahan sums of 32 columns of one TMEM lane quarter
+    const int q = warp & 3, cq = (warp - 2) >> 2;
+    float sum[32], cmp[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) sum[c] = cmp[c] = 0.f;
+    bool got = true;
+    for (int g = 0; g < ngrp; ++g) {
+      const int b = g & 1;
+      if (!mbar_wait(&tfull[b], (g >> 1) & 1)) {
+        got = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+      for (int h2 = 0; h2 < 4; ++h2) {
+        uint32_t v[8];
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kTM + cq * 32 + h2 * 8);
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+                     : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const int e = h2 * 8 + c;
+          const float y = __uint_as_float(v[c]) - cmp[e];
+          const float tt = sum[e] + y;
+          cmp[e] = (tt - sum[e]) - y;
+          sum[e] = tt;
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+    }
+    if (got) {
+      const int i = ti * kTM + q * 32 + lane;
+      if (i < D) {
+#pragma unroll
+        for (int c = 0; c < 32; ++c) {
+          const int j = tj * kTM + cq * 32 + c;
+          if (j < D && j >= i) atomicAdd(&G[(size_t)i * D + j], (double)sum[c] - (double)cmp[c]);
+        }
+      }
+    } else if (lane == 0) {
+      atomicExch(err, 1);
+    }
+  }
+  if (!ok) atomicExch(err, 1);
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kTM));
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+namespace {
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+// plane of D feature rows x Mp design rows (bf16, row stride Mp * 2 bytes); box 64 x 128
+bool make_plane_map(CUtensorMap* m, void* base, long long Mp, int D) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)Mp, (cuuint64_t)D};
+  cuuint64_t strides[1] = {(cuuint64_t)Mp * 2};
+  cuuint32_t box[2] = {(cuuint32_t)kTK, (cuuint32_t)kTM};
+  cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+}  // namespace
+
+size_t gram_tc_min_workspace(int D) { return (size_t)4 * D * kTK + 256; }
+
+bool gram_tc_available() { return encode_fn() != nullptr; }
+
+// G (FP64, D x D, upper triangle) += sum over rows r of w_r x_r x_r^T for columns [c0, c0 + D)
+// of X (M rows, stride ldx).  `ws` holds ws_bytes >= gram_tc_min_workspace(D) bytes; the rows
+// are processed in chunks that fit it.  The caller zeroes G and *err and symmetrises G.
+template <typename T>
+cudaError_t launch_gram_tc(const T* X, int ldx, int c0, int D, const double* w, long long M, double* G, void* ws,
+                           size_t ws_bytes, int* err, int nsm, cudaStream_t st) {
+  if (M <= 0 || D <= 0) return cudaSuccess;
+  if (ws_bytes < gram_tc_min_workspace(D) || ((uintptr_t)ws & 15)) return cudaErrorInvalidValue;
+  // chunk rows: a multiple of 64 whose two planes fit the workspace
+  long long chunk = (long long)((ws_bytes - 256) / (4 * (size_t)D)) / kTK * kTK;
+  chunk = std::min(chunk, (M + kTK - 1) / kTK * kTK);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGramSmem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const int nt = (D + kTM - 1) / kTM;
+  const int ntile = nt * (nt + 1) / 2;
+  __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(ws);
+  for (long long r0 = 0; r0 < M; r0 += chunk) {
+    const long long rows = std::min(chunk, M - r0);
+    const long long Mp = (rows + 7) / 8 * 8;  // 16-byte plane row stride
+    __nv_bfloat16* lo = hi + (size_t)D * Mp;
+    dim3 g1((unsigned)((Mp + 31) / 32), (unsigned)((D + 31) / 32));
+    k_split_bf16<T><<<g1, dim3(32, 8), 0, st>>>(X, ldx, c0, D, w, r0, rows, Mp, hi, lo);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    CUtensorMap mh, ml;
+    if (!make_plane_map(&mh, hi, Mp, D) || !make_plane_map(&ml, lo, Mp, D)) return cudaErrorInvalidValue;
+    const int nk = (int)((rows + kTK - 1) / kTK);
+    // row splits: at least two waves of CTAs where the tile count alone does not give them
+    int nsplit = std::max(1, std::min(nk, (2 * nsm + ntile - 1) / ntile));
+    const int kps = (nk + nsplit - 1) / nsplit;
+    nsplit = (nk + kps - 1) / kps;  // every split non-empty
+    k_gram_tc<<<(unsigned)(ntile * nsplit), kGramThreads, kGramSmem, st>>>(mh, ml, nt, ntile, nk, kps, kFlush, D, G,
+                                                                           err);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+template cudaError_t launch_gram_tc<float>(const float*, int, int, int, const double*, long long, double*, void*,
+                                           size_t, int*, int, cudaStream_t);
+template cudaError_t launch_gram_tc<double>(const double*, int, int, int, const double*, long long, double*, void*,
+                                            size_t, int*, int, cudaStream_t);
+
+}  // namespace mld

@@ -151,6 +151,9 @@ struct DevBatch {
   int* small = nullptr;      // S
   int* nsize = nullptr;      // 3S
   double* volume = nullptr;  // S
+  // FP32 copies for the neighbour pre-filter (written by the counting pass)
+  float4* pos32 = nullptr;   // A  (x, y, z, 0)
+  float4* frac32 = nullptr;  // A  (fractional coordinates b_k . x, 0)
   // neighbour list (CSR over atoms)
   int* nn = nullptr;         // A
   int* nbr_off = nullptr;    // A+1
@@ -195,5 +198,46 @@ cudaError_t launch_gram(const T* X, int ldx, const double* w, const double* y, l
                         double* h, cudaStream_t st);
 cudaError_t launch_solve_sym(double* G, const double* h, int D, double lambda, double rcond, double* wout,
                              double* evals, int* info, cudaStream_t st);
+template <typename T>
+cudaError_t launch_rhs(const T* X, int ldx, const double* w, const double* y, long long M, int D, double* h,
+                       int nsm, cudaStream_t st, float2* sv);
+cudaError_t launch_symmetrize(double* G, int D, cudaStream_t st);
+cudaError_t launch_split_weights(const double* w, long long M, float2* wds, cudaStream_t st);
+cudaError_t launch_normal_matvec(const float* X, int ldx, int D, const double* w, const double* p, long long M,
+                                 double lambda, float2* sv, double* q, int nsm, cudaStream_t st, int* launches);
+template <typename T>
+cudaError_t launch_predict_sq(const T* X, int ldx, const double* w, long long M, int D, double* pred, const double* y,
+                              const int* kind, double* sq, cudaStream_t st);
+template <typename T>
+cudaError_t launch_rows_prep(int S, const int* atom_start, const DevRows& rows, const double* E, const double* F,
+                             const double* Sv, const double* wefs, T* X, double* y, double* wrow, int* kind,
+                             cudaStream_t st);
+template <typename T>
+cudaError_t launch_quad_rows(const DevBatch& b, const DevRows& rows, const BsoParams& p, int KK, const int* rev,
+                             const T* B, const T* dB, T* H, T* X, int qoff, cudaStream_t st);
+cudaError_t launch_reverse_pairs(const DevBatch& b, int* rev, cudaStream_t st);
+
+// dense FP64 factorisation / solves (solve.cu)
+cudaError_t launch_cholesky(double* A, int D, double shift, int* info, cudaStream_t st);
+cudaError_t launch_chol_solve(const double* L, int D, const double* b, double* x, cudaStream_t st);
+cudaError_t launch_chol_solve_blocked(const double* L, int D, const double* b, double* x, double* tmp,
+                                      cudaStream_t st);
+inline int chol_solve_launches(int D) { return 2 * ((D + 63) / 64); }
+inline int cholesky_launches(int D) { return 3 * ((D + 31) / 32) - 2; }
+cudaError_t launch_residual(const double* G, int D, double lambda, const double* w, const double* h, double* r,
+                            cudaStream_t st);
+cudaError_t launch_axpy(int n, double a, const double* x, double* y, cudaStream_t st);
+cudaError_t launch_shift_diag_rel(double* A, int D, double lambda, double rel, cudaStream_t st);
+cudaError_t launch_pcg_alpha(int D, const double* p, const double* q, double* x, double* r, double* scal,
+                             cudaStream_t st);
+cudaError_t launch_pcg_beta(int D, const double* z, const double* r, double* p, double* scal, int first,
+                            cudaStream_t st);
+
+// tensor-core Gram in BF16 split precision (gram_tc.cu)
+size_t gram_tc_min_workspace(int D);
+bool gram_tc_available();
+template <typename T>
+cudaError_t launch_gram_tc(const T* X, int ldx, int c0, int D, const double* w, long long M, double* G, void* ws,
+                           size_t ws_bytes, int* err, int nsm, cudaStream_t st);
 
 }  // namespace mld

@@ -7,17 +7,38 @@
 // coordinates, wrapping components with |ds| > 0.5 by nint (neighbours.F90:315-324).
 // Candidates are scanned in (j, n1, n2, n3) order and compacted with a warp ballot, so the
 // neighbour order (and hence every floating-point sum over neighbours) is deterministic.
+// The counting pass (pass 0) also writes the FP32 copies of positions and fractional
+// coordinates that both passes use for their pre-filter.
 #include <cuda_runtime.h>
 
 #include "mld_internal.h"
 
 namespace mld {
 
-__global__ void k_neighbours(int A, const int* __restrict__ atom_struct, const int* __restrict__ atom_start,
-                             const double* __restrict__ pos, const double* __restrict__ cell,
-                             const double* __restrict__ recip, const int* __restrict__ small,
-                             const int* __restrict__ nsize, double rcut, int pass, int* __restrict__ counts, int* __restrict__ maxcount,
-                             const int* __restrict__ offsets, int* __restrict__ nbr_idx, double* __restrict__ nbr_u) {
+// FP32 positions and fractional coordinates of every atom for the pre-filter.
+__global__ void k_nbr_prep(int A, const int* __restrict__ atom_struct, const double* __restrict__ pos,
+                           const double* __restrict__ recip, float4* __restrict__ pos32,
+                           float4* __restrict__ frac32) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A) return;
+  const double* bg = recip + 9 * (size_t)atom_struct[i];
+  const double x0 = pos[3 * (size_t)i], x1 = pos[3 * (size_t)i + 1], x2 = pos[3 * (size_t)i + 2];
+  pos32[i] = make_float4((float)x0, (float)x1, (float)x2, 0.f);
+  frac32[i] = make_float4((float)(x0 * bg[0] + x1 * bg[1] + x2 * bg[2]), (float)(x0 * bg[3] + x1 * bg[4] + x2 * bg[5]),
+                          (float)(x0 * bg[6] + x1 * bg[7] + x2 * bg[8]), 0.f);
+}
+
+// One warp per centre atom; lanes take candidates (j, image) in order.  Candidates clearly
+// inside or outside r_cut are classified in FP32 from the prepared copies (position error of
+// order 1e-6 A against a band of 1e-3 A); only candidates within r_cut + band take the exact
+// FP64 test of the reference, so the list is the FP64 list.
+__global__ void __launch_bounds__(256) k_neighbours(
+    int A, const int* __restrict__ atom_struct, const int* __restrict__ atom_start, const double* __restrict__ pos,
+    const float4* __restrict__ pos32, const float4* __restrict__ frac32, const double* __restrict__ cell,
+    const double* __restrict__ recip, const int* __restrict__ small, const int* __restrict__ nsize, double rcut,
+    int pass, int* __restrict__ counts, int* __restrict__ maxcount, const int* __restrict__ offsets,
+    int* __restrict__ nbr_idx, double* __restrict__ nbr_u) {
+  constexpr float kBand = 1e-3f;
   const int lane = threadIdx.x & 31;
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (g >= A) return;
@@ -25,8 +46,13 @@ __global__ void k_neighbours(int A, const int* __restrict__ atom_struct, const i
   const int a0 = atom_start[s], nat = atom_start[s + 1] - a0;
   const double* cl = cell + 9 * (size_t)s;
   const double* bg = recip + 9 * (size_t)s;
+  float c32[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) c32[k] = (float)cl[k];
+  const float4 pi = pos32[g], fi = frac32[g];
   const double xi0 = pos[3 * (size_t)g], xi1 = pos[3 * (size_t)g + 1], xi2 = pos[3 * (size_t)g + 2];
   const double rc2 = rcut * rcut;
+  const float rcb = (float)rcut + kBand, rcb2 = rcb * rcb;
   const int sm = small[s];
   int n1s = 0, n2s = 0, n3s = 0, nimg = 1;
   if (sm) {
@@ -44,27 +70,23 @@ __global__ void k_neighbours(int A, const int* __restrict__ atom_struct, const i
     double u0 = 0, u1 = 0, u2 = 0;
     int jj = 0;
     if (cidx < ncand) {
-      // FP32 pre-filter: candidates clearly inside or outside r_cut are classified in FP32;
-      // only accepted pairs and those within kBand of the cut take the exact FP64 test.
-      constexpr float kBand = 1e-3f;
-      const float rcf = (float)rcut;
       if (sm) {
         jj = (int)(cidx / nimg);
         int im = (int)(cidx - (long long)jj * nimg);
-        int n3 = im % (2 * n3s + 1) - n3s;
+        const int n3 = im % (2 * n3s + 1) - n3s;
         im /= (2 * n3s + 1);
-        int n2 = im % (2 * n2s + 1) - n2s;
-        int n1 = im / (2 * n2s + 1) - n1s;
-        const double* xj = pos + 3 * (size_t)(a0 + jj);
-        const float f0 = (float)(xi0 - xj[0]) - ((float)cl[0] * n1 + (float)cl[3] * n2 + (float)cl[6] * n3);
-        const float f1 = (float)(xi1 - xj[1]) - ((float)cl[1] * n1 + (float)cl[4] * n2 + (float)cl[7] * n3);
-        const float f2 = (float)(xi2 - xj[2]) - ((float)cl[2] * n1 + (float)cl[5] * n2 + (float)cl[8] * n3);
-        const float rf = sqrtf(f0 * f0 + f1 * f1 + f2 * f2);
-        if (rf < rcf + kBand) {
-          double t0 = xi0 - (xj[0] + cl[0] * n1 + cl[3] * n2 + cl[6] * n3);
-          double t1 = xi1 - (xj[1] + cl[1] * n1 + cl[4] * n2 + cl[7] * n3);
-          double t2 = xi2 - (xj[2] + cl[2] * n1 + cl[5] * n2 + cl[8] * n3);
-          double r2 = t0 * t0 + t1 * t1 + t2 * t2;
+        const int n2 = im % (2 * n2s + 1) - n2s;
+        const int n1 = im / (2 * n2s + 1) - n1s;
+        const float4 pj = pos32[a0 + jj];
+        const float f0 = (pi.x - pj.x) - (c32[0] * n1 + c32[3] * n2 + c32[6] * n3);
+        const float f1 = (pi.y - pj.y) - (c32[1] * n1 + c32[4] * n2 + c32[7] * n3);
+        const float f2 = (pi.z - pj.z) - (c32[2] * n1 + c32[5] * n2 + c32[8] * n3);
+        if (f0 * f0 + f1 * f1 + f2 * f2 < rcb2) {
+          const double* xj = pos + 3 * (size_t)(a0 + jj);
+          const double t0 = xi0 - (xj[0] + cl[0] * n1 + cl[3] * n2 + cl[6] * n3);
+          const double t1 = xi1 - (xj[1] + cl[1] * n1 + cl[4] * n2 + cl[7] * n3);
+          const double t2 = xi2 - (xj[2] + cl[2] * n1 + cl[5] * n2 + cl[8] * n3);
+          const double r2 = t0 * t0 + t1 * t1 + t2 * t2;
           ok = (r2 >= 1e-15) && (r2 <= rc2) && (sqrt(r2) < rcut);
           u0 = -t0;
           u1 = -t1;
@@ -73,23 +95,22 @@ __global__ void k_neighbours(int A, const int* __restrict__ atom_struct, const i
       } else {
         jj = (int)cidx;
         if (a0 + jj != g) {
-          const double* xj = pos + 3 * (size_t)(a0 + jj);
-          const float e0 = (float)(xj[0] - xi0), e1 = (float)(xj[1] - xi1), e2 = (float)(xj[2] - xi2);
-          float fs[3];
-          for (int k = 0; k < 3; ++k) {
-            float v = e0 * (float)bg[3 * k] + e1 * (float)bg[3 * k + 1] + e2 * (float)bg[3 * k + 2];
-            fs[k] = v - rintf(v);
-          }
-          const float g0 = (float)cl[0] * fs[0] + (float)cl[3] * fs[1] + (float)cl[6] * fs[2];
-          const float g1 = (float)cl[1] * fs[0] + (float)cl[4] * fs[1] + (float)cl[7] * fs[2];
-          const float g2 = (float)cl[2] * fs[0] + (float)cl[5] * fs[1] + (float)cl[8] * fs[2];
+          const float4 fj = frac32[a0 + jj];
+          float d0 = fj.x - fi.x, d1 = fj.y - fi.y, d2 = fj.z - fi.z;
+          d0 -= rintf(d0);
+          d1 -= rintf(d1);
+          d2 -= rintf(d2);
+          const float g0 = c32[0] * d0 + c32[3] * d1 + c32[6] * d2;
+          const float g1 = c32[1] * d0 + c32[4] * d1 + c32[7] * d2;
+          const float g2 = c32[2] * d0 + c32[5] * d1 + c32[8] * d2;
           // the FP32 image can differ from the reference's only when a component sits at +-0.5,
           // i.e. at half a cell width (> r_cut for a large box), so its distance is a lower bound
-          if (sqrtf(g0 * g0 + g1 * g1 + g2 * g2) < rcf + kBand) {
-            double d0 = xj[0] - xi0, d1 = xj[1] - xi1, d2 = xj[2] - xi2;
+          if (g0 * g0 + g1 * g1 + g2 * g2 < rcb2) {
+            const double* xj = pos + 3 * (size_t)(a0 + jj);
+            const double e0 = xj[0] - xi0, e1 = xj[1] - xi1, e2 = xj[2] - xi2;
             double ds[3];
             for (int k = 0; k < 3; ++k) {
-              double v = d0 * bg[3 * k] + d1 * bg[3 * k + 1] + d2 * bg[3 * k + 2];
+              double v = e0 * bg[3 * k] + e1 * bg[3 * k + 1] + e2 * bg[3 * k + 2];
               if (v > 0.5 || v < -0.5) v -= round(v);
               ds[k] = v;
             }
@@ -182,8 +203,11 @@ cudaError_t launch_neighbours(const DevBatch& b, double rcut, int* counts, int* 
   const int threads = 256;
   const long long warps = b.A;
   const int blocks = (int)((warps * 32 + threads - 1) / threads);
-  k_neighbours<<<blocks, threads, 0, st>>>(b.A, b.atom_struct, b.atom_start, b.pos, b.cell, b.recip, b.small,
-                                           b.nsize, rcut, pass, counts, maxcount, b.nbr_off, b.nbr_idx, b.nbr_u);
+  if (!b.pos32 || !b.frac32) return cudaErrorInvalidValue;
+  if (pass == 0) k_nbr_prep<<<(b.A + 255) / 256, 256, 0, st>>>(b.A, b.atom_struct, b.pos, b.recip, b.pos32, b.frac32);
+  k_neighbours<<<blocks, threads, 0, st>>>(b.A, b.atom_struct, b.atom_start, b.pos, b.pos32, b.frac32, b.cell,
+                                           b.recip, b.small, b.nsize, rcut, pass, counts, maxcount, b.nbr_off,
+                                           b.nbr_idx, b.nbr_u);
   return cudaGetLastError();
 }
 

@@ -256,6 +256,8 @@ extern "C" int mld_gpu_descriptors_noalloc(const mld_gpu_config* cfg, int nat, c
   b.atom_struct = reinterpret_cast<int*>(take(sizeof(int) * nat));
   b.nn = reinterpret_cast<int*>(take(sizeof(int) * nat));
   b.nbr_off = reinterpret_cast<int*>(take(sizeof(int) * (nat + 1)));
+  b.pos32 = reinterpret_cast<float4*>(take(sizeof(float4) * nat));   // neighbour pre-filter copies
+  b.frac32 = reinterpret_cast<float4*>(take(sizeof(float4) * nat));
   int* scan_tmp = reinterpret_cast<int*>(take(sizeof(int) * ((nat + 1023) / 1024 + 2)));
   int* dmax = reinterpret_cast<int*>(take(sizeof(int) * 2));
   float* bstage = mixed ? reinterpret_cast<float*>(take(sizeof(float) * (size_t)nat * KK)) : nullptr;

@@ -166,6 +166,170 @@ __global__ void k_axpy(int n, double a, const double* x, double* y) {
   if (i < n) y[i] += a * x[i];
 }
 
+// ------------------------------------------------------------------------------------
+// Blocked triangular solves with the Cholesky factor, one launch per 64-row block step.
+// Every CTA of a step solves the 64 x 64 diagonal block itself (cheap), so the block's
+// solution never has to be published between CTAs; the running right-hand side `r` is only
+// written outside the block being solved.
+// ------------------------------------------------------------------------------------
+constexpr int kTB = 64;
+
+// forward, L y = r: y[k0..k0+nb) from the diagonal block, r[i] -= L[i][blk] . y[blk] for i below
+__global__ void __launch_bounds__(256) k_trsv_fwd(const double* __restrict__ L, int D, int k0, int nb,
+                                                  double* __restrict__ r, double* __restrict__ y) {
+  __shared__ double Ld[kTB][kTB + 1];
+  __shared__ double xs[kTB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int i = e / nb, j = e % nb;
+    Ld[i][j] = (j <= i) ? L[(size_t)(k0 + i) * D + k0 + j] : 0.0;
+  }
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) xs[i] = r[k0 + i];
+  __syncthreads();
+  if (warp == 0) {
+    for (int j = 0; j < nb; ++j) {
+      const double xj = xs[j] / Ld[j][j];
+      __syncwarp();
+      for (int i = j + 1 + lane; i < nb; i += 32) xs[i] -= Ld[i][j] * xj;
+      if (lane == 0) xs[j] = xj;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) y[k0 + i] = xs[i];
+  for (int i = k0 + nb + blockIdx.x * nw + warp; i < D; i += gridDim.x * nw) {
+    double acc = 0.0;
+    for (int c = lane; c < nb; c += 32) acc = fma(L[(size_t)i * D + k0 + c], xs[c], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) r[i] -= acc;
+  }
+}
+
+// backward, L^T x = r: x[k0..k0+nb) from the diagonal block, r[i] -= sum_c L[k0+c][i] x[k0+c] for i < k0
+__global__ void __launch_bounds__(256) k_trsv_bwd(const double* __restrict__ L, int D, int k0, int nb,
+                                                  double* __restrict__ r, double* __restrict__ x) {
+  __shared__ double Ld[kTB][kTB + 1];
+  __shared__ double xs[kTB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int i = e / nb, j = e % nb;
+    Ld[i][j] = (j <= i) ? L[(size_t)(k0 + i) * D + k0 + j] : 0.0;
+  }
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) xs[i] = r[k0 + i];
+  __syncthreads();
+  if (warp == 0) {
+    for (int j = nb - 1; j >= 0; --j) {
+      const double xj = xs[j] / Ld[j][j];
+      __syncwarp();
+      for (int i = lane; i < j; i += 32) xs[i] -= Ld[j][i] * xj;
+      if (lane == 0) xs[j] = xj;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) x[k0 + i] = xs[i];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k0; i += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int c = 0; c < nb; ++c) acc = fma(L[(size_t)(k0 + c) * D + i], xs[c], acc);
+    r[i] -= acc;
+  }
+}
+
+// A[i][i] += max(lambda, rel * A[i][i]); an empty (zero) diagonal entry gets 1
+__global__ void k_shift_diag_rel(double* A, int D, double lambda, double rel) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= D) return;
+  double* d = A + (size_t)i * D + i;
+  *d += (*d > 0.0) ? fmax(lambda, rel * *d) : 1.0;
+}
+
+// ------------------------------------------------------------------------------------
+// Preconditioned conjugate gradients on the normal equations, vector updates in one CTA.
+// scal[0] = r.z of the current iterate, scal[1] = r.z of the first iterate, scal[2] = alpha.
+// ------------------------------------------------------------------------------------
+__device__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+  return s;
+}
+
+// x += alpha p, r -= alpha q with alpha = (r.z) / (p.q)
+__global__ void __launch_bounds__(1024) k_pcg_alpha(int D, const double* __restrict__ p, const double* __restrict__ q,
+                                                    double* __restrict__ x, double* __restrict__ r,
+                                                    double* __restrict__ scal) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < D; i += blockDim.x) s = fma(p[i], q[i], s);
+  const double pq = block_sum(s, red);
+  const double alpha = (pq > 0.0) ? scal[0] / pq : 0.0;
+  for (int i = threadIdx.x; i < D; i += blockDim.x) {
+    x[i] = fma(alpha, p[i], x[i]);
+    r[i] = fma(-alpha, q[i], r[i]);
+  }
+  if (threadIdx.x == 0) scal[2] = alpha;
+}
+
+// p = z + beta p with beta = (r.z)_new / (r.z)_old; first: p = z
+__global__ void __launch_bounds__(1024) k_pcg_beta(int D, const double* __restrict__ z, const double* __restrict__ r,
+                                                   double* __restrict__ p, double* __restrict__ scal, int first) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < D; i += blockDim.x) s = fma(r[i], z[i], s);
+  const double rz = block_sum(s, red);
+  const double beta = (first || !(scal[0] > 0.0)) ? 0.0 : rz / scal[0];
+  for (int i = threadIdx.x; i < D; i += blockDim.x) p[i] = fma(beta, p[i], z[i]);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    scal[0] = rz;
+    if (first) scal[1] = rz;
+  }
+}
+
+cudaError_t launch_shift_diag_rel(double* A, int D, double lambda, double rel, cudaStream_t st) {
+  k_shift_diag_rel<<<(D + 255) / 256, 256, 0, st>>>(A, D, lambda, rel);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pcg_alpha(int D, const double* p, const double* q, double* x, double* r, double* scal,
+                             cudaStream_t st) {
+  k_pcg_alpha<<<1, 1024, 0, st>>>(D, p, q, x, r, scal);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pcg_beta(int D, const double* z, const double* r, double* p, double* scal, int first,
+                            cudaStream_t st) {
+  k_pcg_beta<<<1, 1024, 0, st>>>(D, z, r, p, scal, first);
+  return cudaGetLastError();
+}
+
+// x = (L L^T)^-1 b; tmp holds 2*D doubles
+cudaError_t launch_chol_solve_blocked(const double* L, int D, const double* b, double* x, double* tmp,
+                                      cudaStream_t st) {
+  double* r = tmp;
+  double* y = tmp + D;
+  cudaError_t e = cudaMemcpyAsync(r, b, sizeof(double) * (size_t)D, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  for (int k0 = 0; k0 < D; k0 += kTB) {
+    const int nb = min(kTB, D - k0);
+    const int below = D - k0 - nb;
+    const int grid = max(1, min((below + 7) / 8, 296));
+    k_trsv_fwd<<<grid, 256, 0, st>>>(L, D, k0, nb, r, y);
+  }
+  const int nblk = (D + kTB - 1) / kTB;
+  for (int b0 = nblk - 1; b0 >= 0; --b0) {
+    const int k0 = b0 * kTB, nb = min(kTB, D - k0);
+    const int grid = max(1, min((k0 + 255) / 256, 296));
+    k_trsv_bwd<<<grid, 256, 0, st>>>(L, D, k0, nb, y, x);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_cholesky(double* A, int D, double shift, int* info, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(info, 0, sizeof(int), st);
   if (e != cudaSuccess) return e;
