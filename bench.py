@@ -47,6 +47,11 @@ def _args():
     p.add_argument("--plain-steps", type=int, default=2)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--workload", choices=["fe_linear", "hea_qnml"], default="fe_linear",
+                   help="fe_linear: batched linear Fe fit (default); hea_qnml: quadratic QNML fit of the "
+                        "5-element alloy (4,000 x 250 atoms, weighted two-channel bispectrum)")
+    p.add_argument("--plain-structures", type=int, default=200,
+                   help="hea_qnml: structures of the sample on which mixed and plain FP64 are compared")
     return p.parse_args()
 
 
@@ -218,6 +223,80 @@ def run_ours(a, rank, world):
     return res
 
 
+def run_hea(a):
+    """QNML quadratic fit of the 5-element bcc alloy: one step = one full mixed-method fit of
+    the whole set (neighbours, two-channel descriptors, quadratic rows, tensor-core Gram of the
+    linear and quadratic blocks, Cholesky-preconditioned CG).  The plain FP64 method is timed on
+    the first --plain-structures structures (its FP64 Gram grows as rows x D^2 and takes
+    minutes on the whole set); both methods are fitted on that sample for the RMSE comparison."""
+    from mld_gb300 import _lib, synth
+    n_struct = a.structures if a.structures != N_STRUCT else 4000
+    ds = synth.hea_bcc_batched(n_struct=n_struct, workers=min(16, os.cpu_count() or 1))
+    lam = 1e-8
+
+    def handle(precision, idx=None):
+        c = _lib.default_config()
+        c.j_max, c.r_cut, c.lambda_krr, c.precision, c.mld_order = 4.0, 5.0, lam, precision, 2
+        c.weighted = 1
+        c.n_elements = len(synth.HEA_ELEMENTS)
+        for i, wv in enumerate(synth.HEA_WEIGHTS):
+            c.weight_per_element[i] = wv
+        h = _lib.Handle(c)
+        sub = ds if idx is None else synth.Dataset([ds.structures[i] for i in idx], ds.rcut, ds.name)
+        nat, pos, cell, types = sub.arrays()
+        E, F, S, has = sub.labels()
+        h.set_structures(nat, pos, cell, types)
+        h.set_labels(E, F, S, has, np.ones((len(nat), 3)))
+        return h, int(nat.sum())
+
+    out = {}
+    h, A = handle(_lib.MIXED)
+    M = h.num_rows()
+    for _ in range(a.warmup):
+        h.fit()
+    h.set_profiling(True)
+    h.profile(reset=True)
+    with Clocks() as clk:
+        h.timer_start()
+        for _ in range(a.steps):
+            w, rmse = h.fit()
+        ms = h.timer_stop() / a.steps
+    prof = h.profile(reset=True)
+    out.update(ms=ms, rmse=rmse.tolist(), prof={k: v[0] / a.steps for k, v in prof.items()},
+               launches=int(sum(v[1] for v in prof.values())), solve=h.solve_info(), clocks=clk.summary(),
+               D=h.dim_design_line)
+    h.close()
+    sample = {}
+    if a.plain_structures > 0:
+        idx = list(range(min(a.plain_structures, n_struct)))
+        for name, prec in (("mixed", _lib.MIXED), ("plain_fp64", _lib.PLAIN_FP64)):
+            hs, As = handle(prec, idx)
+            Ms = hs.num_rows()
+            hs.fit()
+            hs.timer_start()
+            ws, rs = hs.fit()
+            t = hs.timer_stop()
+            sample[name] = {"ms_per_fit": t, "design_rows": Ms, "rows_per_s": Ms / (t * 1e-3), "rmse_efs": rs.tolist()}
+            hs.close()
+        mx, pl = sample["mixed"], sample["plain_fp64"]
+        sample["force_rmse_rel_diff"] = abs(mx["rmse_efs"][1] - pl["rmse_efs"][1]) / pl["rmse_efs"][1]
+        sample["speedup_rows_per_s_vs_plain_fp64"] = (M / (ms * 1e-3)) / pl["rows_per_s"]
+    line = {
+        "metric": "design rows/s (QNML quadratic fit, 5-element bcc alloy, weighted bispectrum j_max=4)",
+        "value": M / (ms * 1e-3), "unit": "design rows/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 descriptors/rows + bf16x3 tensor-core Gram (fp32 acc) + fp64 Cholesky / double-fp32 CG",
+        "data": "synthetic",
+        "config": {"workload": "hea_bcc_MoNbTaVCr_4000x250_qnml_weighted_jmax4", "structures": n_struct,
+                   "atoms": A, "design_rows": M, "dim_design_line_full": out["D"], "r_cut": 5.0, "lambda_krr": lam,
+                   "l2": "working set above L2 every step", "parallelism": "single"},
+        "atom_evals_per_s": A / (ms * 1e-3), "rmse_efs": out["rmse"], "phase_ms": out["prof"],
+        "mixed_solve": out["solve"], "gpu_launches": out["launches"], "clocks": out["clocks"],
+        "sample_comparison": sample or None,
+    }
+    print(json.dumps(line))
+
+
 def cpu_sample(ds, target_s=15.0, threads=None):
     """Time the oracle (CPU restatement of the reference) on a bounded sample of the same set:
     neighbours + descriptors + rows in C (OpenMP over structures), Gram + gelsd in NumPy/LAPACK."""
@@ -292,6 +371,10 @@ def main():
         print(json.dumps(line))
         return
 
+    if a.workload == "hea_qnml":
+        if rank == 0:
+            run_hea(a)
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")

@@ -169,12 +169,13 @@ int mld_gpu_work_counts(const mld_gpu_handle* h, long long* out);
  * of the descriptor kernel. */
 int mld_gpu_peak_flops(mld_gpu_handle* h, int precision, double* tflops);
 
-/* Solver record of the last mixed-method fit: conjugate-gradient iterations and final relative
- * preconditioned residual per stage (0 = linear block, 1 = quadratic block of QNML), and how
- * often the Cholesky preconditioner had to be re-factorised with a larger diagonal shift.
+/* Solver record of the last mixed-method fit: conjugate-gradient iterations, final relative
+ * preconditioned residual and the relative diagonal shift of the Cholesky preconditioner, per
+ * stage (0 = linear block, 1 = quadratic block of QNML), and how often the preconditioner had
+ * to be re-factorised with a larger shift.
  * (No reference counterpart: the reference solves with dgelsd, stats_tools.F90:1153-1213.) */
 int mld_gpu_solve_info(const mld_gpu_handle* h, int* pcg_iterations /*[2]*/, double* pcg_residual /*[2]*/,
-                       int* chol_retries);
+                       double* precond_shift /*[2]*/, int* chol_retries);
 
 /* Weighted Gram matrix and right-hand side of caller-owned DEVICE rows, the per-block
  * accumulation of the online fit (gram%accumulate, module_online_fit.F90:49-53,138-265):

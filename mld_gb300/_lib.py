@@ -266,10 +266,11 @@ class Handle:
     def solve_info(self):
         it = np.zeros(2, np.int32)
         res = np.zeros(2)
+        sh = np.zeros(2)
         rt = ctypes.c_int()
-        self._check(self._L.mld_gpu_solve_info(self._h, _p(it), _p(res), ctypes.byref(rt)))
+        self._check(self._L.mld_gpu_solve_info(self._h, _p(it), _p(res), _p(sh), ctypes.byref(rt)))
         return {"pcg_iterations": [int(v) for v in it], "pcg_residual": [float(v) for v in res],
-                "chol_retries": int(rt.value)}
+                "precond_shift": [float(v) for v in sh], "chol_retries": int(rt.value)}
 
 
 def gram_rows(method: int, X_ptr: int, x_is_fp32: bool, M: int, D: int, ldx: int, w_ptr: int, y_ptr: int,

@@ -74,6 +74,7 @@ struct mld_gpu_handle {
   // device properties and the last mixed-method solve
   int nsm = 0;
   int pcg_iters[2] = {0, 0};
+  double precond_shift[2] = {0, 0};
   double pcg_rel[2] = {0, 0};
   int chol_retries = 0;
 
@@ -86,9 +87,10 @@ struct mld_gpu_handle {
     B_ROWE, B_ROWF, B_ROWS, B_X, B_Y, B_WROW, B_KIND,
     B_G, B_H, B_W, B_EVALS, B_INFO, B_SQ, B_PRED, B_BOUT, B_DBOUT,
     B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
-    B_GWS, B_TERR, B_PCG, B_POS32,
+    B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV,
     B_COUNT
   };
+  static_assert(B_COUNT <= 48, "buffer table too small");
 };
 
 namespace {
@@ -246,6 +248,18 @@ int build_neighbours(mld_gpu_handle* h) {
   return MLD_OK;
 }
 
+// global Y scratch of the descriptor kernel when its per-atom Y does not fit in shared memory
+template <typename T>
+int y_scratch(mld_gpu_handle* h, void** p, size_t* bytes) {
+  *bytes = bso4_y_scratch_bytes(h->dt, h->nch, (int)sizeof(T), 2 * std::max(1, h->nsm));
+  *p = nullptr;
+  if (*bytes) {
+    CK(ensure(h, mld_gpu_handle::B_YSCR, *bytes));
+    *p = bp_<void>(h, mld_gpu_handle::B_YSCR);
+  }
+  return MLD_OK;
+}
+
 template <typename T>
 int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) {
   DevRows rows;
@@ -290,7 +304,11 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
   mark(h, MLD_PHASE_ROWS, 1);
   mark(h, MLD_PHASE_DESCRIPTORS, 0);
   if (!h->quad) {
-    CK(launch_bso4_rows<T>(h->dt, h->b, rows, h->bp, X, (T*)nullptr, (T*)nullptr, 1, h->st));
+    void* ys = nullptr;
+    size_t ysb = 0;
+    int rcy = y_scratch<T>(h, &ys, &ysb);
+    if (rcy) return rcy;
+    CK(launch_bso4_rows<T>(h->dt, h->b, rows, h->bp, X, (T*)nullptr, (T*)nullptr, 1, h->st, ys, ysb));
     nl(h, 1);
   } else {
     // quadratic rows need every atom's B and every pair's dB (mld_forces.F90:410-500)
@@ -301,7 +319,11 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
     CK(ensure(h, mld_gpu_handle::B_HQ, sizeof(T) * (size_t)std::max(1, h->A) * 6 * h->KK));
     T* Bq = bp_<T>(h, mld_gpu_handle::B_BOUT);
     T* dBq = bp_<T>(h, mld_gpu_handle::B_DBOUT);
-    CK(launch_bso4_rows<T>(h->dt, h->b, rows, h->bp, X, Bq, dBq, 1, h->st));
+    void* ys = nullptr;
+    size_t ysb = 0;
+    int rcy = y_scratch<T>(h, &ys, &ysb);
+    if (rcy) return rcy;
+    CK(launch_bso4_rows<T>(h->dt, h->b, rows, h->bp, X, Bq, dBq, 1, h->st, ys, ysb));
     CK(launch_reverse_pairs(h->b, bp_<int>(h, mld_gpu_handle::B_REV), h->st));
     CK(launch_quad_rows<T>(h->b, rows, h->bp, h->KK, bp_<int>(h, mld_gpu_handle::B_REV), Bq, dBq,
                            bp_<T>(h, mld_gpu_handle::B_HQ), X, h->DL, h->st));
@@ -430,15 +452,20 @@ int fit_block_plain(mld_gpu_handle* h, const double* X, int c0, int Db, const do
 }
 
 constexpr size_t kGramWorkspaceCap = size_t(8) << 30;  // bf16 planes of one row chunk
-constexpr int kPcgMaxIter = 40;
+constexpr int kPcgMaxIter = 150;
+constexpr double kPcgObjTol = 1e-7;  // relative objective decrease over three steps that ends CG
+// relative diagonal shift of the preconditioner: max(min, per_column * D), x3 while not SPD
+constexpr double kPrecondShiftMin = 1e-6;
+constexpr double kPrecondShiftPerColumn = 2e-7;
 constexpr double kPcgTol2 = 1e-22;   // (preconditioned residual / initial)^2 that ends the iteration
 constexpr double kPcgFloor2 = 1e-14; // below this, stagnation also ends it
 
 // Mixed method, one block of columns [c0, c0 + Db) of the FP32 design matrix.
 //  * normal matrix G~ = X^T W X on the tensor cores in BF16 split precision (gram_tc.cu) and
 //    rhs = X^T W y with FP64 accumulation;
-//  * preconditioner: FP64 Cholesky of G~ + diag(max(lambda, rel * G~_ii)), rel = 1e-6 (x10 on
-//    a failed factorisation);
+//  * preconditioner: FP64 Cholesky of G~ + diag(max(lambda, rel * G~_ii)), rel = max(1e-6,
+//    2e-7 * D) (x3 on a failed factorisation);
+//    applied through the explicit inverse of the factor (two dense FP64 triangular matvecs);
 //  * conjugate gradients on (X^T W X + lambda I) w = X^T W y with FP64-accumulated matvecs
 //    over X itself, so the converged coefficients are those of the FP64 normal equations of
 //    this X, whatever the precision of G~.
@@ -483,10 +510,12 @@ int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const dou
   double* p = z + Db;
   double* q = p + Db;
   double* tmp = q + Db;  // 2 Db
-  double* scal = tmp + 2 * (size_t)Db;
+  double* scal = tmp + 2 * (size_t)Db;  // [0..3] CG scalars, [4] objective at w = 0
   float2* sv = bp_<float2>(h, mld_gpu_handle::B_PRED);  // per-row double-FP32 scratch
   int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
-  double rel = 1e-6;
+  // the error of the BF16x3 Gram is coherent across the matrix (the tensor core truncates its
+  // FP32 sums), so the shift that keeps G~ positive definite grows with D
+  double rel = std::max(kPrecondShiftMin, kPrecondShiftPerColumn * Db);
   int retries = 0;
   for (;; ++retries) {
     CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)Db * Db, cudaMemcpyDeviceToDevice, h->st));
@@ -497,35 +526,56 @@ int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const dou
     CK(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     if (hinfo == 0) break;
-    if (retries >= 3)
+    if (retries >= 6)
       return fail(h, MLD_ERR_SOLVE, "preconditioner not positive definite at column " + std::to_string(hinfo));
-    rel *= 10.0;
+    rel *= 3.0;
   }
+  h->precond_shift[stage] = rel;
   h->chol_retries += retries;
+  // explicit inverse of the factor: each preconditioner application is two dense matvecs
+  CK(ensure(h, mld_gpu_handle::B_RINV, sizeof(double) * 2 * (size_t)Db * Db));
+  double* Rinv = bp_<double>(h, mld_gpu_handle::B_RINV);
+  double* Rinvt = Rinv + (size_t)Db * Db;
+  {
+    int ninv = 0;
+    CK(launch_cholesky_inverse(Lf, Db, Rinv, Rinvt, h->st, &ninv));
+    nl(h, ninv);
+  }
+  // objective sum_r w_r y_r^2 at w = 0, for the stopping test on its decrease
+  CK(launch_weighted_sumsq(wrow, y, M, scal + 4, h->st));
+  nl(h, 1);
   // x0 = 0, r0 = rhs
   CK(cudaMemsetAsync(w, 0, sizeof(double) * Db, h->st));
   CK(cudaMemcpyAsync(r, hv, sizeof(double) * Db, cudaMemcpyDeviceToDevice, h->st));
-  CK(launch_chol_solve_blocked(Lf, Db, r, z, tmp, h->st));
+  CK(launch_precond_apply(Rinv, Rinvt, Db, r, z, tmp, h->st));
   CK(launch_pcg_beta(Db, z, r, p, scal, 1, h->st));
-  nl(h, chol_solve_launches(Db) + 1);
-  if (Db <= 256) {
-    CK(launch_split_weights(wrow, M, sv, h->st));  // the fused narrow matvec reads w as pairs
-    nl(h, 1);
-  }
-  double hs[2] = {0, 0};
-  double prev = 0.0;
+  nl(h, 3);
+  CK(launch_split_weights(wrow, M, sv, h->st));  // the fused matvecs read w as pairs
+  CK(cudaMemsetAsync(terr, 0, sizeof(int), h->st));
+  nl(h, 1);
+  double hs[5] = {0, 0, 0, 0, 0};
+  double prev = 0.0, fobj = -1.0, dec_hist[3] = {0, 0, 0};
   int it = 0, slow = 0;
   for (; it < kPcgMaxIter; ++it) {
     int nmv = 0;
-    CK(launch_normal_matvec(X + c0, h->ldx, Db, wrow, p, M, lam, sv, q, h->nsm, h->st, &nmv));
+    CK(launch_normal_matvec(X, h->ldx, c0, Db, wrow, p, M, lam, sv, q, h->nsm, h->st, &nmv, terr));
     CK(launch_pcg_alpha(Db, p, q, w, r, scal, h->st));
-    CK(launch_chol_solve_blocked(Lf, Db, r, z, tmp, h->st));
+    CK(launch_precond_apply(Rinv, Rinvt, Db, r, z, tmp, h->st));
     CK(launch_pcg_beta(Db, z, r, p, scal, 0, h->st));
-    nl(h, nmv + 2 + chol_solve_launches(Db));
-    CK(cudaMemcpyAsync(hs, scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, h->st));
+    nl(h, nmv + 4);
+    CK(cudaMemcpyAsync(hs, scal, sizeof(double) * 5, cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     const double ratio = hs[1] > 0 ? hs[0] / hs[1] : 0.0;
     if (!(ratio > kPcgTol2)) {
+      ++it;
+      break;
+    }
+    // least-squares objective: f_k = f_0 - sum of the step decreases alpha_j (r.z)_j; stop once
+    // three steps together lower it by less than kPcgObjTol of its value
+    if (fobj < 0) fobj = hs[4];
+    fobj -= hs[3];
+    dec_hist[it % 3] = hs[3];
+    if (it >= 2 && fobj > 0 && dec_hist[0] + dec_hist[1] + dec_hist[2] < kPcgObjTol * fobj) {
       ++it;
       break;
     }
@@ -537,6 +587,9 @@ int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const dou
       break;
     }
   }
+  CK(cudaMemcpyAsync(&herr, terr, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (herr) return fail(h, MLD_ERR_TIMEOUT, "normal-equation matvec: a pipeline wait timed out");
   h->pcg_iters[stage] = it;
   h->pcg_rel[stage] = hs[1] > 0 ? std::sqrt(std::max(hs[0], 0.0) / hs[1]) : 0.0;
   mark(h, MLD_PHASE_SOLVE, 1);
@@ -910,8 +963,12 @@ int mld_gpu_descriptors(mld_gpu_handle* h, double* B_out, int* n_neigh_out) {
   if (h->mixed) {
     CK(ensure(h, mld_gpu_handle::B_BOUT, sizeof(float) * std::max<size_t>(nB, 1)));
     CK(ensure(h, mld_gpu_handle::B_DBOUT, sizeof(float) * std::max<size_t>(nd, 1)));
+    void* ys = nullptr;
+    size_t ysb = 0;
+    int rcy = y_scratch<float>(h, &ys, &ysb);
+    if (rcy) return rcy;
     CK(launch_bso4_rows<float>(h->dt, h->b, rows, h->bp, (float*)nullptr, bp_<float>(h, mld_gpu_handle::B_BOUT),
-                               bp_<float>(h, mld_gpu_handle::B_DBOUT), 0, h->st));
+                               bp_<float>(h, mld_gpu_handle::B_DBOUT), 0, h->st, ys, ysb));
     if (B_out) {
       std::vector<float> tmp(nB);
       CK(cudaMemcpyAsync(tmp.data(), bp_<float>(h, mld_gpu_handle::B_BOUT), sizeof(float) * nB,
@@ -922,8 +979,12 @@ int mld_gpu_descriptors(mld_gpu_handle* h, double* B_out, int* n_neigh_out) {
   } else {
     CK(ensure(h, mld_gpu_handle::B_BOUT, sizeof(double) * std::max<size_t>(nB, 1)));
     CK(ensure(h, mld_gpu_handle::B_DBOUT, sizeof(double) * std::max<size_t>(nd, 1)));
+    void* ys = nullptr;
+    size_t ysb = 0;
+    int rcy = y_scratch<double>(h, &ys, &ysb);
+    if (rcy) return rcy;
     CK(launch_bso4_rows<double>(h->dt, h->b, rows, h->bp, (double*)nullptr, bp_<double>(h, mld_gpu_handle::B_BOUT),
-                                bp_<double>(h, mld_gpu_handle::B_DBOUT), 0, h->st));
+                                bp_<double>(h, mld_gpu_handle::B_DBOUT), 0, h->st, ys, ysb));
     if (B_out)
       CK(cudaMemcpyAsync(B_out, bp_<double>(h, mld_gpu_handle::B_BOUT), sizeof(double) * nB, cudaMemcpyDeviceToHost,
                          h->st));
@@ -1207,11 +1268,12 @@ extern "C" int mld_gpu_peak_flops(mld_gpu_handle* h, int precision, double* tflo
 }
 
 extern "C" int mld_gpu_solve_info(const mld_gpu_handle* h, int* pcg_iterations, double* pcg_residual,
-                                  int* chol_retries) {
+                                  double* precond_shift, int* chol_retries) {
   if (!h) return MLD_ERR_INVALID;
   for (int s = 0; s < 2; ++s) {
     if (pcg_iterations) pcg_iterations[s] = h->pcg_iters[s];
     if (pcg_residual) pcg_residual[s] = h->pcg_rel[s];
+    if (precond_shift) precond_shift[s] = h->precond_shift[s];
   }
   if (chol_retries) *chol_retries = h->chol_retries;
   return MLD_OK;

@@ -258,13 +258,19 @@ struct KernelArgs {
   int want_rows;
   int NB;  // neighbours per phase-3 chunk (2 per warp)
   BsoParams p;
+  // Y (the contracted Z blocks, nch * NYP complex per atom) in global memory, one slice per CTA,
+  // when it does not fit in shared memory next to the rest (FP64 with several channels)
+  void* yglobal;
 };
 
 constexpr int kNW = 8;           // warps per CTA (kNW*32 == kZThreads)
 constexpr int kG1 = 8;           // lanes per neighbour in phase 1
 constexpr int kG3 = 16;          // lanes per neighbour in phase 3
 
-template <typename T>
+// kYShared: Y lives in shared memory (the common case); otherwise in the per-CTA global slice
+// args.yglobal (FP64 with several channels), a separate instantiation so that the shared-memory
+// variant keeps shared-memory addressing.
+template <typename T, bool kYShared>
 __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __restrict__ X, T* __restrict__ Bout,
                                                     T* __restrict__ dBout, int A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -278,8 +284,9 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
 
   // shared-memory carve-up
   cx<T>* cfull = reinterpret_cast<cx<T>*>(smem_raw);              // nch*NU
-  cx<T>* Y = cfull + nch * NU;                                      // nch*NYP
-  cx<T>* V = Y + (size_t)nch * NYP;                                 // max(NB*3, kNW*nch)*HU
+  cx<T>* Y = kYShared ? cfull + nch * NU
+                      : reinterpret_cast<cx<T>*>(args.yglobal) + (size_t)blockIdx.x * nch * NYP;  // nch*NYP
+  cx<T>* V = kYShared ? Y + (size_t)nch * NYP : cfull + nch * NU;  // max(NB*3, kNW*nch)*HU
   const size_t vblock = (size_t)max(NB * 3, kNW * nch) * HU;
   cx<T>* ubuf = V + vblock;                                         // (32/kG1)*kNW*2*LH
   T* dBs = reinterpret_cast<T*>(ubuf + (size_t)(32 / kG1) * kNW * 2 * LH);  // 3*NB*K  [col][k]
@@ -538,19 +545,36 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
   }
 }
 
-static size_t smem_bytes(const DevTables& tb, int nch, int eb, int NB) {
+static size_t smem_bytes(const DevTables& tb, int nch, int eb, int NB, bool y_in_smem) {
   const size_t LH = tb.hoff[tb.J + 1] - tb.hoff[tb.J];
   const size_t cxb = 2 * (size_t)eb;
   const size_t vblock = (size_t)std::max(NB * 3, kNW * nch) * tb.HU;
-  size_t b = cxb * ((size_t)nch * tb.NU + (size_t)nch * tb.NYP + vblock + (size_t)(32 / kG1) * kNW * 2 * LH);
+  size_t b = cxb * ((size_t)nch * tb.NU + (y_in_smem ? (size_t)nch * tb.NYP : 0) + vblock +
+                    (size_t)(32 / kG1) * kNW * 2 * LH);
   b += (size_t)eb * ((size_t)3 * NB * tb.K + (size_t)nch * 10 * tb.K + (size_t)nch * NB + (size_t)NB * 4);
   b += sizeof(int) * NB;
   return b;
 }
 
+static int max_optin_smem() {
+  static int v = 0;
+  if (!v) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  }
+  return v;
+}
+
+size_t bso4_y_scratch_bytes(const DevTables& tb, int nch, int eb, int max_ctas) {
+  const int NB = kNW * (32 / kG3);
+  if (smem_bytes(tb, nch, eb, NB, true) <= (size_t)max_optin_smem()) return 0;
+  return (size_t)max_ctas * nch * tb.NYP * 2 * eb;
+}
+
 template <typename T>
 cudaError_t launch_bso4_rows(const DevTables& tb, const DevBatch& b, const DevRows& rows, const BsoParams& p, T* X,
-                             T* Bout, T* dBout, int want_rows, cudaStream_t st) {
+                             T* Bout, T* dBout, int want_rows, cudaStream_t st, void* yscratch, size_t yscratch_bytes) {
   const int NB = kNW * (32 / kG3);
   if (b.A == 0) return cudaSuccess;
   KernelArgs<T> a{};
@@ -578,19 +602,34 @@ cudaError_t launch_bso4_rows(const DevTables& tb, const DevBatch& b, const DevRo
   a.want_rows = want_rows;
   a.NB = NB;
   a.p = p;
-  size_t smem = smem_bytes(tb, p.nch, sizeof(T), NB);
-  cudaError_t e = cudaFuncSetAttribute(k_bso4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const bool y_in_smem = smem_bytes(tb, p.nch, sizeof(T), NB, true) <= (size_t)max_optin_smem();
+  size_t smem = smem_bytes(tb, p.nch, sizeof(T), NB, y_in_smem);
+  a.yglobal = nullptr;
+  auto kern = y_in_smem ? k_bso4<T, true> : k_bso4<T, false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bso4<T>, kNW * 32, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kNW * 32, smem);
   if (occ < 1) return cudaErrorInvalidConfiguration;
-  k_bso4<T><<<b.A, kNW * 32, smem, st>>>(a, X, Bout, dBout, b.A);
+  int grid = b.A;
+  if (!y_in_smem) {
+    // persistent CTAs (the kernel strides over atoms), one Y slice each
+    const size_t per_cta = (size_t)p.nch * tb.NYP * 2 * sizeof(T);
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const long long fit = yscratch ? (long long)(yscratch_bytes / per_cta) : 0;
+    grid = (int)std::min<long long>({(long long)b.A, (long long)nsm * occ, fit});
+    if (grid < 1) return cudaErrorInvalidValue;  // Y scratch required and not given
+    a.yglobal = yscratch;
+  }
+  kern<<<grid, kNW * 32, smem, st>>>(a, X, Bout, dBout, b.A);
   return cudaGetLastError();
 }
 
 template cudaError_t launch_bso4_rows<double>(const DevTables&, const DevBatch&, const DevRows&, const BsoParams&,
-                                              double*, double*, double*, int, cudaStream_t);
+                                              double*, double*, double*, int, cudaStream_t, void*, size_t);
 template cudaError_t launch_bso4_rows<float>(const DevTables&, const DevBatch&, const DevRows&, const BsoParams&,
-                                             float*, float*, float*, int, cudaStream_t);
+                                             float*, float*, float*, int, cudaStream_t, void*, size_t);
 
 }  // namespace mld

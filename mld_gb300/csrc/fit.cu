@@ -15,6 +15,7 @@
 #include <type_traits>
 
 #include "mld_internal.h"
+#include "ptx.cuh"
 
 namespace mld {
 
@@ -370,6 +371,154 @@ __global__ void __launch_bounds__(256) k_xtv_ds(const float* __restrict__ X, int
   if (cb + threadIdx.x < D && sum != 0.0) atomicAdd(&q[cb + threadIdx.x], sum);
 }
 
+// ------------------------------------------------------------------------------------
+// Normal-equation matvec of a wide block (D > 256) in one pass over X.  Design rows stream
+// through a ring of shared-memory stages by 1-D bulk copies issued from one producer thread;
+// eight consumer warps form the dot x_r . p over column slices (double-FP32), combine the
+// slices, and add w_r (x_r . p) x_r into per-column double-FP32 sums held in shared memory.
+// Every wait is bounded: on expiry the CTA sets *err and leaves the loop uniformly.
+// ------------------------------------------------------------------------------------
+constexpr int kWConsumers = 256;
+constexpr int kWThreads = kWConsumers + 32;
+
+// CPT columns per consumer thread (c = tid + 256 k): p as pairs and the column sums live in
+// registers; the row ring and the per-warp dot partials are in shared memory.
+template <int CPT>
+__global__ void __launch_bounds__(kWThreads, 1)
+    k_normal_matvec_wide(const float* __restrict__ X, long long ldx, int c0, int D, const float2* __restrict__ wds,
+                         const double* __restrict__ p, long long M, long long rpb, int rowf, int stages,
+                         double* __restrict__ q, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char wsm[];
+  float* rows = reinterpret_cast<float*>(wsm);                             // stages * rowf
+  float2* part = reinterpret_cast<float2*>(rows + (size_t)stages * rowf);  // stages * 8
+  uint64_t* full = reinterpret_cast<uint64_t*>(part + stages * 8);
+  uint64_t* empty = full + stages;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int a0 = c0 & ~3, off = c0 - a0;
+  const uint32_t bytes = (uint32_t)rowf * 4u;
+  const long long r0 = (long long)blockIdx.x * rpb;
+  const long long nr = min(M, r0 + rpb) - r0;
+  if (nr <= 0) return;
+  if (tid == 0) {
+    for (int s = 0; s < stages; ++s) {
+      ptx::mbar_init(&full[s], 1);
+      ptx::mbar_init(&empty[s], kWConsumers / 32);
+    }
+    ptx::mbar_init_fence();
+  }
+  __syncthreads();
+  if (warp == kWConsumers / 32) {
+    // producer
+    if (lane == 0) {
+      long long issued = 0;
+      for (long long k = 0; k < nr; ++k) {
+        const int s = (int)(k % stages);
+        if (k >= stages && !ptx::mbar_wait(&empty[s], (uint32_t)(((k / stages) - 1) & 1))) {
+          atomicExch(err, 1);
+          break;
+        }
+        ptx::mbar_expect_tx(&full[s], bytes);
+        ptx::bulk_load(rows + (size_t)s * rowf, X + (r0 + k) * ldx + a0, bytes, &full[s]);
+        issued = k + 1;
+      }
+      for (long long k = max(0LL, issued - stages); k < issued; ++k)
+        ptx::mbar_wait(&full[k % stages], (uint32_t)((k / stages) & 1));
+    }
+    return;
+  }
+  // consumers
+  float ph[CPT], pl[CPT], ah[CPT], al[CPT];
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) {
+    const int c = tid + kWConsumers * k;
+    ds_split(c < D ? p[c] : 0.0, ph[k], pl[k]);
+    ah[k] = al[k] = 0.f;
+  }
+  // two design rows per step: independent dot chains and one pass over the sums for both
+  for (long long k = 0; k < nr; k += 2) {
+    const bool two = k + 1 < nr;
+    const int s0 = (int)(k % stages), s1 = (int)((k + 1) % stages);
+    const float2 wv0 = wds[r0 + k];
+    const float2 wv1 = two ? wds[r0 + k + 1] : make_float2(0.f, 0.f);
+    bool ok = ptx::mbar_wait(&full[s0], (uint32_t)((k / stages) & 1));
+    if (two) ok = ok && ptx::mbar_wait(&full[s1], (uint32_t)(((k + 1) / stages) & 1));
+    const float* xr0 = rows + (size_t)s0 * rowf + off;
+    const float* xr1 = rows + (size_t)s1 * rowf + off;
+    float d0h = 0.f, d0l = 0.f, d1h = 0.f, d1l = 0.f;
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) {
+      const int c = tid + kWConsumers * j;
+      const float v0 = (ok && c < D) ? xr0[c] : 0.f;
+      const float v1 = (ok && two && c < D) ? xr1[c] : 0.f;
+      ds_fma(d0h, d0l, v0, ph[j], pl[j]);
+      ds_fma(d1h, d1l, v1, ph[j], pl[j]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      float oh = __shfl_xor_sync(0xffffffffu, d0h, o), ol = __shfl_xor_sync(0xffffffffu, d0l, o);
+      ds_add(d0h, d0l, oh, ol);
+      oh = __shfl_xor_sync(0xffffffffu, d1h, o);
+      ol = __shfl_xor_sync(0xffffffffu, d1l, o);
+      ds_add(d1h, d1l, oh, ol);
+    }
+    if (lane == 0) {
+      part[s0 * 8 + warp] = make_float2(d0h, d0l);
+      part[s1 * 8 + warp] = make_float2(d1h, d1l);
+    }
+    int any_fail;
+    asm volatile(
+        "{\n .reg .pred pf, pr;\n setp.eq.u32 pf, %1, 0;\n bar.red.or.pred pr, 1, %2, pf;\n selp.u32 %0, 1, 0, pr;\n}\n"
+        : "=r"(any_fail)
+        : "r"((unsigned)ok), "n"(kWConsumers));
+    if (any_fail) {
+      if (tid == 0) atomicExch(err, 1);
+      break;
+    }
+    float a0h = 0.f, a0l = 0.f, a1h = 0.f, a1l = 0.f;
+#pragma unroll
+    for (int w8 = 0; w8 < 8; ++w8) {
+      const float2 p0 = part[s0 * 8 + w8], p1 = part[s1 * 8 + w8];
+      ds_add(a0h, a0l, p0.x, p0.y);
+      ds_add(a1h, a1l, p1.x, p1.y);
+    }
+    // s_r = w_r * (x_r . p) for both rows
+    float t0h, t0l, t1h, t1l;
+    {
+      const float sp = a0h * wv0.x, se = fmaf(a0h, wv0.y, fmaf(a0l, wv0.x, fmaf(a0h, wv0.x, -sp)));
+      t0h = sp + se;
+      t0l = se - (t0h - sp);
+    }
+    {
+      const float sp = a1h * wv1.x, se = fmaf(a1h, wv1.y, fmaf(a1l, wv1.x, fmaf(a1h, wv1.x, -sp)));
+      t1h = sp + se;
+      t1l = se - (t1h - sp);
+    }
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) {
+      const int c = tid + kWConsumers * j;
+      const float v0 = c < D ? xr0[c] : 0.f;
+      const float v1 = (two && c < D) ? xr1[c] : 0.f;
+      ds_fma(ah[j], al[j], v0, t0h, t0l);
+      ds_fma(ah[j], al[j], v1, t1h, t1l);
+    }
+    // both stages are read: release them to the producer
+    __syncwarp();
+    if (lane == 0) {
+      ptx::mbar_arrive(&empty[s0]);
+      if (two) ptx::mbar_arrive(&empty[s1]);
+    }
+    if (((k >> 1) & 31) == 31) {
+#pragma unroll
+      for (int j = 0; j < CPT; ++j) ds_norm(ah[j], al[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < CPT; ++j) {
+    const int c = tid + kWConsumers * j;
+    const double v = (double)ah[j] + (double)al[j];
+    if (c < D && v != 0.0) atomicAdd(&q[c], v);
+  }
+}
+
 namespace {
 // design-row chunk per CTA so that about 8 CTAs per SM run over all column blocks
 long long rows_per_cta(long long M, int ncb, int nsm) {
@@ -400,32 +549,85 @@ cudaError_t launch_rhs(const T* X, int ldx, const double* w, const double* y, lo
   return cudaGetLastError();
 }
 
+// out = sum_r w[r] y[r]^2 (out is zeroed here)
+__global__ void __launch_bounds__(256) k_weighted_sumsq(const double* __restrict__ w, const double* __restrict__ y,
+                                                        long long M, double* __restrict__ out) {
+  __shared__ double red[8];
+  double a = 0.0;
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < M; r += (long long)gridDim.x * blockDim.x)
+    a = fma(w[r] * y[r], y[r], a);
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < 8; ++k) t += red[k];
+    atomicAdd(out, t);
+  }
+}
+
+cudaError_t launch_weighted_sumsq(const double* w, const double* y, long long M, double* out, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), st);
+  if (e != cudaSuccess || M == 0) return e;
+  const unsigned blocks = (unsigned)std::min<long long>((M + 255) / 256, 1024);
+  k_weighted_sumsq<<<blocks, 256, 0, st>>>(w, y, M, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_split_weights(const double* w, long long M, float2* wds, cudaStream_t st) {
   if (M > 0) k_w_ds<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(w, M, wds);
   return cudaGetLastError();
 }
 
-// q = X^T W X p (+ lambda p) for an FP32 X in double-FP32 arithmetic: one fused pass for
-// D <= 256 (weights as pairs in sv, from launch_split_weights), else sv = W X p then X^T sv
-// (sv: M float2 of scratch).  *launches: kernels issued.
-cudaError_t launch_normal_matvec(const float* X, int ldx, int D, const double* w, const double* p, long long M,
-                                 double lambda, float2* sv, double* q, int nsm, cudaStream_t st, int* launches) {
+// q = X^T W X p (+ lambda p) over columns [c0, c0 + D) of an FP32 X in double-FP32 arithmetic:
+// one fused pass (D <= 256: rows in registers; wider: rows streamed through shared memory) with
+// the weights as pairs in wds (launch_split_weights); when a wide row does not fit the shared
+// memory ring, sv = W X p then X^T sv (sv: M float2 of scratch, overwriting wds).
+// *launches: kernels issued; *err: set by a wait that expired.
+cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const double* w, const double* p, long long M,
+                                 double lambda, float2* sv, double* q, int nsm, cudaStream_t st, int* launches,
+                                 int* err) {
   cudaError_t e = cudaMemsetAsync(q, 0, sizeof(double) * (size_t)D, st);
   if (e != cudaSuccess) return e;
   *launches = 0;
+  const float* Xc = X + c0;
+  // shared memory of the wide fused kernel: the row ring and the per-warp partials
+  const int a0 = c0 & ~3;
+  const int rowf = ((c0 + D + 3) & ~3) - a0;
+  static int optin = 0;
+  if (!optin) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  }
+  const size_t per_stage = sizeof(float) * rowf + 8 * sizeof(float2) + 2 * sizeof(uint64_t);
+  const int stages = (int)std::min<size_t>(6, ((size_t)optin - 256) / per_stage);
+  const int cpt = (D + kWConsumers - 1) / kWConsumers;
   if (M > 0 && D <= 256) {
     const long long rpb = rows_per_cta(M, 1, nsm);
     const unsigned nrb = (unsigned)((M + rpb - 1) / rpb);
     switch ((D + 31) / 32) {
-      case 1: k_normal_matvec_narrow<1><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
-      case 2: k_normal_matvec_narrow<2><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
-      case 3: k_normal_matvec_narrow<3><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
-      case 4: k_normal_matvec_narrow<4><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
-      case 5: k_normal_matvec_narrow<5><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
-      case 6: k_normal_matvec_narrow<6><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
-      case 7: k_normal_matvec_narrow<7><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
-      default: k_normal_matvec_narrow<8><<<nrb, 256, 0, st>>>(X, ldx, D, sv, p, M, rpb, q); break;
+      case 1: k_normal_matvec_narrow<1><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
+      case 2: k_normal_matvec_narrow<2><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
+      case 3: k_normal_matvec_narrow<3><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
+      case 4: k_normal_matvec_narrow<4><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
+      case 5: k_normal_matvec_narrow<5><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
+      case 6: k_normal_matvec_narrow<6><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
+      case 7: k_normal_matvec_narrow<7><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
+      default: k_normal_matvec_narrow<8><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
     }
+    *launches = 1;
+  } else if (M > 0 && stages >= 2 && (ldx % 4) == 0 && cpt <= 32) {
+    const size_t smem = 256 + (size_t)stages * per_stage;
+    const long long rpb = (M + nsm - 1) / nsm;
+    const unsigned grid = (unsigned)((M + rpb - 1) / rpb);
+    auto kern = cpt <= 4 ? k_normal_matvec_wide<4>
+              : cpt <= 8 ? k_normal_matvec_wide<8>
+              : cpt <= 16 ? k_normal_matvec_wide<16>
+              : cpt <= 24 ? k_normal_matvec_wide<24> : k_normal_matvec_wide<32>;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, kWThreads, smem, st>>>(X, ldx, c0, D, sv, p, M, rpb, rowf, stages, q, err);
     *launches = 1;
   } else if (M > 0) {
     const size_t smem = sizeof(float) * 2 * (size_t)D;
@@ -433,11 +635,11 @@ cudaError_t launch_normal_matvec(const float* X, int ldx, int D, const double* w
       e = cudaFuncSetAttribute(k_xp_ds, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }
-    k_xp_ds<<<(unsigned)(nsm * 8), 256, smem, st>>>(X, ldx, D, w, p, M, sv);
+    k_xp_ds<<<(unsigned)(nsm * 8), 256, smem, st>>>(Xc, ldx, D, w, p, M, sv);
     const int ncb = (D + 255) / 256;
     const long long rpb = rows_per_cta(M, ncb, nsm);
     const long long nrb = (M + rpb - 1) / rpb;
-    k_xtv_ds<<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(X, ldx, D, sv, M, rpb, q);
+    k_xtv_ds<<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(Xc, ldx, D, sv, M, rpb, q);
     *launches = 2;
   }
   if (lambda > 0) {

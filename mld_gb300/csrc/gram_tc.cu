@@ -24,6 +24,7 @@
 #include <algorithm>
 
 #include "mld_internal.h"
+#include "ptx.cuh"
 
 namespace mld {
 
@@ -34,48 +35,16 @@ constexpr int kTK = 64;                        // design rows per stage: 128 byt
 constexpr int kStages = 3;
 constexpr int kTileBytes = kTM * kTK * 2;      // 16 KB per operand tile
 constexpr int kStageBytes = 4 * kTileBytes;    // A_hi, A_lo, B_hi, B_lo
-constexpr int kFlush = 2;                      // K slices per TMEM accumulation (128 design rows)
+constexpr int kFlush = 1;                      // K slices per TMEM accumulation (64 design rows)
 constexpr int kEpiWarps = 16;                  // four per TMEM lane quarter, 32 columns each
 constexpr int kGramThreads = 32 * (2 + kEpiWarps);
 constexpr size_t kGramSmem = (size_t)kStages * kStageBytes + 1024 + 256;
-constexpr long long kWaitLimit = 2000000000LL;  // SM clocks (about one second)
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait for the phase of the given parity; false on expiry
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitLimit) return false;
-  }
-  return true;
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          smem_u32(dst)),
-      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
+using ptx::mbar_expect_tx;
+using ptx::mbar_init;
+using ptx::mbar_wait;
+using ptx::smem_u32;
+using ptx::tma_load_2d;
 
 // Shared-memory matrix descriptor of a K-major tile written by TMA with 128-byte swizzle:
 // rows of 128 bytes, 8-row core groups 1024 bytes apart (stride byte offset), version 1.
@@ -145,7 +114,7 @@ __global__ void __launch_bounds__(256) k_split_bf16(const T* __restrict__ X, int
 // blockIdx.x = tile + ntile * split; tile enumerates the upper-triangle pairs ti <= tj.
 // Row split s covers K slices [s * kps, min(nk, (s + 1) * kps)) of 64 design rows.
 //
-// The FP32 accumulator lives in TMEM for `flush` K slices only (kFlush = 2: 128 design rows), because
+// The FP32 accumulator lives in TMEM for `flush` K slices only (kFlush = 1: 64 design rows), because
 // the tensor core rounds its FP32 accumulation toward zero (a bias that grows with the chain): the MMA issuer
 // alternates between two 128-column TMEM buffers, and the epilogue warps drain the idle buffer
 // into compensated (Kahan) FP32 register sums, so the error of the whole split stays at the
@@ -183,7 +152,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
       mbar_init(&tfull[b], 1);
       mbar_init(&tempty[b], kEpiWarps);
     }
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    ptx::mbar_init_fence();
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -281,7 +250,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncwarp();
-      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+      if (lane == 0) ptx::mbar_arrive(&tempty[b]);
     }
     if (got) {
       const int i = ti * kTM + q * 32 + lane;

@@ -189,9 +189,13 @@ cudaError_t launch_neighbours(const DevBatch& b, double rcut, int* counts, int* 
                               int pass /*0 count, 1 fill*/);
 cudaError_t launch_scan(const int* in, int* out, int n, int* d_tmp, cudaStream_t st);
 
+// Y scratch the descriptor kernel needs in global memory for up to max_ctas CTAs (0 when Y fits
+// in shared memory); pass it to launch_bso4_rows, which then runs that many persistent CTAs.
+size_t bso4_y_scratch_bytes(const DevTables& tb, int nch, int eb, int max_ctas);
 template <typename T>
 cudaError_t launch_bso4_rows(const DevTables& tb, const DevBatch& b, const DevRows& rows, const BsoParams& p,
-                             T* X, T* Bout, T* dBout, int want_rows, cudaStream_t st);
+                             T* X, T* Bout, T* dBout, int want_rows, cudaStream_t st, void* yscratch = nullptr,
+                             size_t yscratch_bytes = 0);
 
 template <typename T>
 cudaError_t launch_gram(const T* X, int ldx, const double* w, const double* y, long long M, int D, double* G,
@@ -202,9 +206,11 @@ template <typename T>
 cudaError_t launch_rhs(const T* X, int ldx, const double* w, const double* y, long long M, int D, double* h,
                        int nsm, cudaStream_t st, float2* sv);
 cudaError_t launch_symmetrize(double* G, int D, cudaStream_t st);
+cudaError_t launch_weighted_sumsq(const double* w, const double* y, long long M, double* out, cudaStream_t st);
 cudaError_t launch_split_weights(const double* w, long long M, float2* wds, cudaStream_t st);
-cudaError_t launch_normal_matvec(const float* X, int ldx, int D, const double* w, const double* p, long long M,
-                                 double lambda, float2* sv, double* q, int nsm, cudaStream_t st, int* launches);
+cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const double* w, const double* p, long long M,
+                                 double lambda, float2* sv, double* q, int nsm, cudaStream_t st, int* launches,
+                                 int* err);
 template <typename T>
 cudaError_t launch_predict_sq(const T* X, int ldx, const double* w, long long M, int D, double* pred, const double* y,
                               const int* kind, double* sq, cudaStream_t st);
@@ -223,6 +229,9 @@ cudaError_t launch_chol_solve(const double* L, int D, const double* b, double* x
 cudaError_t launch_chol_solve_blocked(const double* L, int D, const double* b, double* x, double* tmp,
                                       cudaStream_t st);
 inline int chol_solve_launches(int D) { return 2 * ((D + 63) / 64); }
+cudaError_t launch_cholesky_inverse(const double* L, int D, double* R, double* Rt, cudaStream_t st, int* launches);
+cudaError_t launch_precond_apply(const double* R, const double* Rt, int D, const double* r, double* z, double* tmp,
+                                 cudaStream_t st);
 inline int cholesky_launches(int D) { return 3 * ((D + 31) / 32) - 2; }
 cudaError_t launch_residual(const double* G, int D, double lambda, const double* w, const double* h, double* r,
                             cudaStream_t st);

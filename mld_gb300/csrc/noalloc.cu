@@ -261,6 +261,10 @@ extern "C" int mld_gpu_descriptors_noalloc(const mld_gpu_config* cfg, int nat, c
   int* scan_tmp = reinterpret_cast<int*>(take(sizeof(int) * ((nat + 1023) / 1024 + 2)));
   int* dmax = reinterpret_cast<int*>(take(sizeof(int) * 2));
   float* bstage = mixed ? reinterpret_cast<float*>(take(sizeof(float) * (size_t)nat * KK)) : nullptr;
+  // global Y slices of the descriptor kernel when they do not fit in shared memory (FP64 with
+  // several channels); at most 64 persistent CTAs
+  const size_t ysb = bso4_y_scratch_bytes(dt, nch, mixed ? 4 : 8, 64);
+  void* yscr = ysb ? take(ysb) : nullptr;
   const size_t fixed = (size_t)(p - S->base);
   if (fixed > kScratchBytes) {
     set_err(err, err_len, "descriptor staging exceeds the scratch array");
@@ -327,12 +331,12 @@ extern "C" int mld_gpu_descriptors_noalloc(const mld_gpu_config* cfg, int nat, c
   rows.D = 1 + KK;
   rows.ldx = round_up4(rows.D);
   if (mixed) {
-    CKN(launch_bso4_rows<float>(dt, b, rows, prm, (float*)nullptr, bstage, (float*)nullptr, 0, st));
+    CKN(launch_bso4_rows<float>(dt, b, rows, prm, (float*)nullptr, bstage, (float*)nullptr, 0, st, yscr, ysb));
     const size_t n = (size_t)nat * KK;
     k_widen<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(bstage, B, n);
     CKN(cudaGetLastError());
   } else {
-    CKN(launch_bso4_rows<double>(dt, b, rows, prm, (double*)nullptr, B, (double*)nullptr, 0, st));
+    CKN(launch_bso4_rows<double>(dt, b, rows, prm, (double*)nullptr, B, (double*)nullptr, 0, st, yscr, ysb));
   }
 #undef CKN
   return MLD_OK;

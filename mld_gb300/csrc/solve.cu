@@ -247,7 +247,8 @@ __global__ void k_shift_diag_rel(double* A, int D, double lambda, double rel) {
 
 // ------------------------------------------------------------------------------------
 // Preconditioned conjugate gradients on the normal equations, vector updates in one CTA.
-// scal[0] = r.z of the current iterate, scal[1] = r.z of the first iterate, scal[2] = alpha.
+// scal[0] = r.z of the current iterate, scal[1] = r.z of the first iterate, scal[2] = alpha,
+// scal[3] = alpha * r.z, the decrease of sum_r w_r (y_r - x_r.w)^2 + lambda |w|^2 in the step.
 // ------------------------------------------------------------------------------------
 __device__ double block_sum(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -272,7 +273,10 @@ __global__ void __launch_bounds__(1024) k_pcg_alpha(int D, const double* __restr
     x[i] = fma(alpha, p[i], x[i]);
     r[i] = fma(-alpha, q[i], r[i]);
   }
-  if (threadIdx.x == 0) scal[2] = alpha;
+  if (threadIdx.x == 0) {
+    scal[2] = alpha;
+    scal[3] = alpha * scal[0];  // decrease of the least-squares objective in this step
+  }
 }
 
 // p = z + beta p with beta = (r.z)_new / (r.z)_old; first: p = z
@@ -327,6 +331,127 @@ cudaError_t launch_chol_solve_blocked(const double* L, int D, const double* b, d
     const int grid = max(1, min((k0 + 255) / 256, 296));
     k_trsv_bwd<<<grid, 256, 0, st>>>(L, D, k0, nb, y, x);
   }
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------
+// Explicit inverse R = L^-1 of the Cholesky factor (lower, row-major D x D), so that the
+// preconditioner of the conjugate-gradient solve is two dense triangular matvecs instead of
+// two chains of block substitutions.  Blocked by kCB: the diagonal blocks are inverted
+// independently, then block row i of R follows from the rows above it:
+//   R_ij = -R_ii * sum_{k=j}^{i-1} L_ik R_kj   (j < i).
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kCB) k_trinv_diag(const double* __restrict__ L, int D, double* __restrict__ R) {
+  __shared__ double Ld[kCB][kCB + 1], X[kCB][kCB + 1];
+  const int k0 = blockIdx.x * kCB, nb = min(kCB, D - k0), t = threadIdx.x;
+  for (int e = t; e < nb * nb; e += blockDim.x) {
+    const int i = e / nb, j = e % nb;
+    Ld[i][j] = (j <= i) ? L[(size_t)(k0 + i) * D + k0 + j] : 0.0;
+  }
+  __syncthreads();
+  if (t < nb) {
+    // column t of the inverse by forward substitution (rows below t)
+    for (int i = 0; i < nb; ++i) {
+      double v = (i == t) ? 1.0 : 0.0;
+      for (int c = t; c < i; ++c) v -= Ld[i][c] * X[c][t];
+      X[i][t] = (i < t) ? 0.0 : v / Ld[i][i];
+    }
+  }
+  __syncthreads();
+  for (int e = t; e < nb * nb; e += blockDim.x) {
+    const int i = e / nb, j = e % nb;
+    R[(size_t)(k0 + i) * D + k0 + j] = (j <= i) ? X[i][j] : 0.0;
+  }
+}
+
+// block row bi of R, block column j = blockIdx.x < bi (16 x 16 threads, 2 x 2 outputs each)
+__global__ void __launch_bounds__(256) k_trinv_row(const double* __restrict__ L, int D, int bi, double* __restrict__ R) {
+  __shared__ double A[kCB][kCB + 1], B[kCB][kCB + 1];
+  const int i0 = bi * kCB, ni = min(kCB, D - i0);
+  const int bj = blockIdx.x, j0 = bj * kCB;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[2][2] = {{0, 0}, {0, 0}};
+  for (int bk = bj; bk < bi; ++bk) {
+    const int k0 = bk * kCB;
+    for (int e = threadIdx.x; e < kCB * kCB; e += 256) {
+      const int r = e / kCB, c = e % kCB;
+      A[r][c] = (r < ni) ? L[(size_t)(i0 + r) * D + k0 + c] : 0.0;         // L_ik (k block full)
+      B[r][c] = R[(size_t)(k0 + r) * D + j0 + c];                          // R_kj
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int c = 0; c < kCB; ++c) {
+      const double a0 = A[ty][c], a1 = A[ty + 16][c], b0 = B[c][tx], b1 = B[c][tx + 16];
+      acc[0][0] = fma(a0, b0, acc[0][0]);
+      acc[0][1] = fma(a0, b1, acc[0][1]);
+      acc[1][0] = fma(a1, b0, acc[1][0]);
+      acc[1][1] = fma(a1, b1, acc[1][1]);
+    }
+    __syncthreads();
+  }
+  // T in B, R_ii in A; R_ij = -R_ii T
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) B[ty + 16 * a][tx + 16 * b] = acc[a][b];
+  for (int e = threadIdx.x; e < kCB * kCB; e += 256) {
+    const int r = e / kCB, c = e % kCB;
+    A[r][c] = (r < ni && c < ni) ? R[(size_t)(i0 + r) * D + i0 + c] : 0.0;
+  }
+  __syncthreads();
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) {
+      const int r = ty + 16 * a, c = tx + 16 * b;
+      double v = 0.0;
+      for (int k = 0; k <= r; ++k) v = fma(A[r][k], B[k][c], v);
+      if (r < ni) R[(size_t)(i0 + r) * D + j0 + c] = -v;
+    }
+}
+
+// Rt = R^T (upper part of Rt = lower part of R; the rest zero)
+__global__ void k_transpose_lower(const double* __restrict__ R, int D, double* __restrict__ Rt) {
+  __shared__ double tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;  // source block (rows by, cols bx)
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int r = by + y, c = bx + threadIdx.x;
+    tile[y][threadIdx.x] = (r < D && c < D && c <= r) ? R[(size_t)r * D + c] : 0.0;
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int r = bx + y, c = by + threadIdx.x;  // Rt[r][c] = R[c][r]
+    if (r < D && c < D) Rt[(size_t)r * D + c] = tile[threadIdx.x][y];
+  }
+}
+
+// y = T x for a triangular T stored densely (zeros outside the triangle): warp per row,
+// columns [lo, hi) of row i with lo = upper ? i : 0, hi = upper ? D : i + 1
+__global__ void __launch_bounds__(256) k_trmv(const double* __restrict__ T, int D, int upper,
+                                             const double* __restrict__ x, double* __restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= D) return;
+  const int lo = upper ? i : 0, hi = upper ? D : i + 1;
+  double a = 0.0;
+  for (int c = lo + lane; c < hi; c += 32) a = fma(T[(size_t)i * D + c], x[c], a);
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if (lane == 0) y[i] = a;
+}
+
+// R = L^-1 and Rt = R^T (D x D each); returns the launches issued through *launches
+cudaError_t launch_cholesky_inverse(const double* L, int D, double* R, double* Rt, cudaStream_t st, int* launches) {
+  const int nb = (D + kCB - 1) / kCB;
+  k_trinv_diag<<<nb, kCB, 0, st>>>(L, D, R);
+  for (int bi = 1; bi < nb; ++bi) k_trinv_row<<<bi, 256, 0, st>>>(L, D, bi, R);
+  dim3 g((D + 31) / 32, (D + 31) / 32);
+  k_transpose_lower<<<g, dim3(32, 8), 0, st>>>(R, D, Rt);
+  *launches = nb + 1;
+  return cudaGetLastError();
+}
+
+// z = (L L^T)^-1 r = Rt (R r); tmp holds D doubles
+cudaError_t launch_precond_apply(const double* R, const double* Rt, int D, const double* r, double* z, double* tmp,
+                                 cudaStream_t st) {
+  const unsigned blocks = (unsigned)(((long long)D * 32 + 255) / 256);
+  k_trmv<<<blocks, 256, 0, st>>>(R, D, 0, r, tmp);
+  k_trmv<<<blocks, 256, 0, st>>>(Rt, D, 1, tmp, z);
   return cudaGetLastError();
 }
 

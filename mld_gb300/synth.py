@@ -185,3 +185,54 @@ def fe_bcc_batched(n_struct: int = 2000, nmin: int = 16, nmax: int = 1024, sigma
     else:
         out = [_batched_one(j) for j in jobs]
     return Dataset(out, rcut, f"fe_bcc_batched_{n_struct}")
+
+
+# ---------------------------------------------------------------------------------------------
+# 5-element equiatomic bcc alloy (quadratic-fit workload)
+# ---------------------------------------------------------------------------------------------
+HEA_ELEMENTS = ["Mo", "Nb", "Ta", "V", "Cr"]
+HEA_A = 3.2
+# weight_per_element of the weighted (two-channel) bispectrum: Z / 100
+HEA_WEIGHTS = (0.42, 0.41, 0.73, 0.23, 0.24)
+
+
+def hea_morse_table(seed: int = 20240603, r0: float = 2.75) -> np.ndarray:
+    """Seeded symmetric element-pair Morse table (5 x 5 x (D, alpha, r0)): D in [0.3, 0.6] eV,
+    alpha in [1.2, 1.6] 1/A, r0 at the bcc nearest-neighbour distance of a = 3.2 A."""
+    rng = np.random.default_rng(seed)
+    n = len(HEA_ELEMENTS)
+    t = np.zeros((n, n, 3))
+    for i in range(n):
+        for j in range(i, n):
+            t[i, j] = t[j, i] = (rng.uniform(0.3, 0.6), rng.uniform(1.2, 1.6), r0)
+    return t
+
+
+def _hea_one(args):
+    s, seed, reps, sigma, rcut, table = args
+    rng = np.random.default_rng(np.random.SeedSequence([seed, s]))
+    pos, cell = bcc(reps, reps, reps, HEA_A)
+    n = pos.shape[0]
+    ne = len(HEA_ELEMENTS)
+    types = rng.permutation(np.arange(n) % ne).astype(np.int32)   # equiatomic random occupation
+    pos = pos + rng.normal(0.0, sigma, size=pos.shape)
+    E, F, S = morse_labels(pos, cell, types, rcut, table=table)
+    return Structure(cell=cell, positions=pos, types=types, elements=list(HEA_ELEMENTS),
+                     energies=np.array([E, E, E]), forces=F, stress=S, name=f"hea_{s:05d}")
+
+
+def hea_bcc_batched(n_struct: int = 4000, reps: int = 5, sigma: float = 0.1, rcut: float = 5.0,
+                    seed: int = 20240604, workers: int = 0) -> Dataset:
+    """(Mo, Nb, Ta, V, Cr) bcc a = 3.2 A, reps^3 cubic cells (250 atoms for reps = 5) with random
+    equiatomic occupation, Gaussian noise sigma, labels from the seeded element-pair Morse table.
+    Structure s draws from its own seeded stream (independent of ``workers``)."""
+    table = hea_morse_table()
+    jobs = [(s, seed, reps, sigma, rcut, table) for s in range(n_struct)]
+    if workers and workers > 1 and n_struct > 8:
+        import concurrent.futures as cf
+        import multiprocessing as mp
+        with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            out = list(ex.map(_hea_one, jobs, chunksize=max(1, n_struct // (4 * workers))))
+    else:
+        out = [_hea_one(j) for j in jobs]
+    return Dataset(out, rcut, f"hea_bcc_{n_struct}")

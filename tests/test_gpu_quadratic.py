@@ -113,3 +113,27 @@ def test_large_dense_solve_cholesky(lib):
         w, _ = h.solve(G, h_)
     w_ref = np.linalg.solve(G + 1e-3 * np.eye(D), h_)
     assert _rel(w, w_ref) < 1e-10
+
+
+def test_weighted_descriptors_fp64_two_and_three_channels(lib):
+    """Two- and three-channel FP64 descriptors at j_max = 4 keep their Z blocks in global scratch
+    (they exceed shared memory); the descriptors must still match the oracle."""
+    from mld_gb300 import _lib, synth
+    ds = synth.hea_bcc_batched(n_struct=2, reps=3, seed=5)
+    s = ds.structures[0]
+    for three in (0, 1):
+        chw = np.array([list(synth.HEA_WEIGHTS)] * (2 + three))
+        chw[0] = 1.0
+        if three:
+            chw[2] = np.array(synth.HEA_WEIGHTS) ** 2
+        c = _lib.default_config()
+        c.j_max, c.r_cut, c.weighted, c.weighted_3ch = 4.0, 5.0, 1, three
+        c.n_elements = 5
+        for i, wv in enumerate(synth.HEA_WEIGHTS):
+            c.weight_per_element[i] = wv
+            c.weight_per_element_3ch[i] = wv ** 2
+        with _lib.Handle(c) as h:
+            h.set_structures(np.array([s.nat], np.int32), s.positions, s.cell[None], s.types)
+            B, _ = h.descriptors()
+        ref = oracle.bispectrum(s.positions, s.cell, s.types, 5.0, 4.0, channel_weights=chw, want_deriv=False)
+        assert _rel(B, ref["B"]) < 1e-10
