@@ -64,14 +64,22 @@ typedef struct mld_gpu_config {
   double r_cut_pair_in[MLD_MAX_ELEMENTS * MLD_MAX_ELEMENTS];  /* inner cutoff per element pair, 0 = off */
   double r_cut_width_in;    /* default 0.4 */
   int desc_forces;          /* 1: force and stress design rows */
-  int ml_type;              /* 0 (linear / quadratic models) */
-  int mld_order;            /* 1 linear (this build) */
-  double lambda_krr;        /* ridge added to the diagonal of the normal matrix; < 0 -> 0; default -1 */
+  int ml_type;              /* 0 linear / quadratic models, 1 kernel ridge regression (KRR) */
+  int mld_order;            /* ml_type 0: 1 linear, 2 quadratic (QNML two-stage) */
+  double lambda_krr;        /* ridge: lambda added to the normal-matrix diagonal (ml_type 0) or
+                               lambda^2 (ml_type 1, [sqrt(W) A; lambda I] least squares); < 0 -> 0;
+                               default -1 */
   double svd_rcond;         /* singular-value cut of the min-norm solve; < 0 -> machine precision; default -1 */
   double sign_stress;       /* default 1 */
   double sign_stress_big_box; /* default 1 */
   int imm_neigh;            /* neighbour cap per atom; default 300 */
   int precision;            /* MLD_PRECISION_PLAIN_FP64 or MLD_PRECISION_MIXED */
+  /* kernel ridge regression (ml_type 1): &input_ml kernel_type, kernel_power, length_kernel,
+     sigma_kernel (read_ml_file.F90:338-347); only kernel_type 4 (normalised polynomial) */
+  int kernel_type;          /* default 4 */
+  double kernel_power;      /* default 2 */
+  double length_kernel;     /* default sqrt(1/2) */
+  double sigma_kernel;      /* default 0 */
 } mld_gpu_config;
 
 typedef struct mld_gpu_handle mld_gpu_handle;
@@ -168,6 +176,13 @@ int mld_gpu_work_counts(const mld_gpu_handle* h, long long* out);
  * (FP64 for MLD_PRECISION_PLAIN_FP64, FP32 for MLD_PRECISION_MIXED): the roofline denominator
  * of the descriptor kernel. */
 int mld_gpu_peak_flops(mld_gpu_handle* h, int precision, double* tflops);
+
+/* Reference points of the kernel model (ml_type 1): nk raw descriptors of selected atoms
+ * (nk x dim_desc, row-major), the rows of kernel_matrix.dat (compute_kernel.F90:1058-1256).
+ * They are standardised per component over the set, z = (z_raw - mean) / std (population
+ * std); a component with zero spread is rejected (MLD_ERR_INVALID).  Sets dim_design_line to
+ * 1 + dim_desc + nk. */
+int mld_gpu_set_kernel_points(mld_gpu_handle* h, int nk, const double* z_raw);
 
 /* Solver record of the last mixed-method fit: conjugate-gradient iterations, final relative
  * preconditioned residual and the relative diagonal shift of the Cholesky preconditioner, per

@@ -27,7 +27,8 @@ EXPORTED = ["mld_gpu_config_defaults", "mld_gpu_create", "mld_gpu_destroy", "mld
             "mld_gpu_descriptor_derivatives", "mld_gpu_num_rows", "mld_gpu_design_matrix", "mld_gpu_gram",
             "mld_gpu_solve", "mld_gpu_fit", "mld_gpu_predict", "mld_gpu_synchronize", "mld_gpu_set_profiling",
             "mld_gpu_profile", "mld_gpu_timer_start", "mld_gpu_timer_stop", "mld_gpu_work_counts",
-            "mld_gpu_peak_flops", "mld_gpu_descriptors_noalloc", "mld_gpu_solve_info", "mld_gpu_gram_rows"]
+            "mld_gpu_peak_flops", "mld_gpu_descriptors_noalloc", "mld_gpu_solve_info", "mld_gpu_gram_rows",
+            "mld_gpu_set_kernel_points"]
 NPHASE = 6
 PHASES = ["neighbours", "rows", "descriptors", "gram", "solve", "predict"]
 
@@ -54,6 +55,10 @@ class MldGpuConfig(ctypes.Structure):
         ("sign_stress_big_box", ctypes.c_double),
         ("imm_neigh", ctypes.c_int),
         ("precision", ctypes.c_int),
+        ("kernel_type", ctypes.c_int),
+        ("kernel_power", ctypes.c_double),
+        ("length_kernel", ctypes.c_double),
+        ("sigma_kernel", ctypes.c_double),
     ]
 
 
@@ -128,10 +133,13 @@ class Handle:
         if rc != MLD_OK:
             raise MldError(rc, "mld_gpu_create failed")
         self.cfg = cfg
+        self.nat = np.zeros(0, np.int32)
+        self._dims()
+
+    def _dims(self):
         K, dd, D = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         self._L.mld_gpu_dims(self._h, ctypes.byref(K), ctypes.byref(dd), ctypes.byref(D))
         self.K, self.dim_desc, self.dim_design_line = K.value, dd.value, D.value
-        self.nat = np.zeros(0, np.int32)
 
     def close(self):
         if self._h:
@@ -262,6 +270,11 @@ class Handle:
         keys = ["NU", "u_one_term", "u_two_term", "cg_terms", "z_row_extents", "z_outputs", "y_slots",
                 "y_slots_za", "K", "nch", "pairs", "atoms"]
         return dict(zip(keys, (int(v) for v in out)))
+
+    def set_kernel_points(self, z_raw: np.ndarray) -> None:
+        Z = np.ascontiguousarray(z_raw, dtype=np.float64)
+        self._check(self._L.mld_gpu_set_kernel_points(self._h, int(Z.shape[0]), _p(Z)))
+        self._dims()
 
     def solve_info(self):
         it = np.zeros(2, np.int32)

@@ -40,6 +40,10 @@ struct mld_gpu_handle {
   // quadratic model (mld_order = 2): linear block DL = 1 + KK, upper-triangle quadratic block DQ
   bool quad = false;
   int DL = 0, DQ = 0, Dfull = 0;
+  // kernel ridge regression (ml_type 1): nk standardised reference points, columns DL .. DL+nk
+  bool krr = false;
+  int nk = 0;
+  double lam_eff = 0.0;  // ridge added to the normal-matrix diagonal (lambda, or lambda^2 for KRR)
   bool mixed = false;
 
   // staged batch
@@ -79,7 +83,7 @@ struct mld_gpu_handle {
   int chol_retries = 0;
 
   std::vector<void*> owned;  // table allocations
-  Buf bufs[48];
+  Buf bufs[64];
   enum {
     B_ATOM_START, B_ATOM_STRUCT, B_TYPES, B_POS, B_CELL, B_RECIP, B_SMALL, B_NSIZE, B_VOL,
     B_NN, B_NBR_OFF, B_NBR_IDX, B_NBR_U, B_SCAN_TMP, B_MAXNN,
@@ -87,10 +91,10 @@ struct mld_gpu_handle {
     B_ROWE, B_ROWF, B_ROWS, B_X, B_Y, B_WROW, B_KIND,
     B_G, B_H, B_W, B_EVALS, B_INFO, B_SQ, B_PRED, B_BOUT, B_DBOUT,
     B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
-    B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV,
+    B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV, B_KZD, B_KZF, B_KWS,
     B_COUNT
   };
-  static_assert(B_COUNT <= 48, "buffer table too small");
+  static_assert(B_COUNT <= 64, "buffer table too small");
 };
 
 namespace {
@@ -237,6 +241,7 @@ int build_neighbours(mld_gpu_handle* h) {
                 "an atom has " + std::to_string(hv[1]) + " neighbours within r_cut, more than imm_neigh=" +
                     std::to_string(h->cfg.imm_neigh));
   h->max_nn = hv[1];
+  b.maxnn = hv[1];
   b.P = hv[0];
   CK(ensure(h, mld_gpu_handle::B_NBR_IDX, sizeof(int) * std::max<long long>(b.P, 1)));
   CK(ensure(h, mld_gpu_handle::B_NBR_U, sizeof(double) * 3 * std::max<long long>(b.P, 1)));
@@ -262,6 +267,7 @@ int y_scratch(mld_gpu_handle* h, void** p, size_t* bytes) {
 
 template <typename T>
 int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) {
+  if (h->krr && h->nk == 0) return fail(h, MLD_ERR_STATE, "kernel model without reference points");
   DevRows rows;
   rows.M = L.M;
   rows.D = h->D;
@@ -303,7 +309,7 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
   nl(h, 1);
   mark(h, MLD_PHASE_ROWS, 1);
   mark(h, MLD_PHASE_DESCRIPTORS, 0);
-  if (!h->quad) {
+  if (!h->quad && !h->krr) {
     void* ys = nullptr;
     size_t ysb = 0;
     int rcy = y_scratch<T>(h, &ys, &ysb);
@@ -316,7 +322,7 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
     CK(ensure(h, mld_gpu_handle::B_BOUT, sizeof(T) * nB));
     CK(ensure(h, mld_gpu_handle::B_DBOUT, sizeof(T) * nd));
     CK(ensure(h, mld_gpu_handle::B_REV, sizeof(int) * (size_t)std::max<long long>(1, h->b.P)));
-    CK(ensure(h, mld_gpu_handle::B_HQ, sizeof(T) * (size_t)std::max(1, h->A) * 6 * h->KK));
+    if (h->quad) CK(ensure(h, mld_gpu_handle::B_HQ, sizeof(T) * (size_t)std::max(1, h->A) * 6 * h->KK));
     T* Bq = bp_<T>(h, mld_gpu_handle::B_BOUT);
     T* dBq = bp_<T>(h, mld_gpu_handle::B_DBOUT);
     void* ys = nullptr;
@@ -325,9 +331,21 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
     if (rcy) return rcy;
     CK(launch_bso4_rows<T>(h->dt, h->b, rows, h->bp, X, Bq, dBq, 1, h->st, ys, ysb));
     CK(launch_reverse_pairs(h->b, bp_<int>(h, mld_gpu_handle::B_REV), h->st));
-    CK(launch_quad_rows<T>(h->b, rows, h->bp, h->KK, bp_<int>(h, mld_gpu_handle::B_REV), Bq, dBq,
-                           bp_<T>(h, mld_gpu_handle::B_HQ), X, h->DL, h->st));
-    nl(h, 4);
+    if (h->quad) {
+      CK(launch_quad_rows<T>(h->b, rows, h->bp, h->KK, bp_<int>(h, mld_gpu_handle::B_REV), Bq, dBq,
+                             bp_<T>(h, mld_gpu_handle::B_HQ), X, h->DL, h->st));
+      nl(h, 4);
+    } else {
+      // kernel columns (compute_kernel.F90, mld_energy/forces/stress kernel packing)
+      const size_t wse = krr_workspace_elems(h->A, h->nk, h->KK);
+      CK(ensure(h, mld_gpu_handle::B_KWS, sizeof(T) * wse));
+      const T* Zp = bp_<T>(h, sizeof(T) == 8 ? mld_gpu_handle::B_KZD : mld_gpu_handle::B_KZF);
+      int nkl = 0;
+      CK(launch_krr_rows<T>(h->b, rows, bp_<int>(h, mld_gpu_handle::B_REV), Bq, dBq, Zp, h->nk, h->KK,
+                            h->cfg.kernel_power, h->cfg.length_kernel, h->cfg.sigma_kernel, h->cfg.sign_stress,
+                            h->cfg.sign_stress_big_box, bp_<T>(h, mld_gpu_handle::B_KWS), X, h->DL, h->st, &nkl));
+      nl(h, 2 + nkl);
+    }
   }
   mark(h, MLD_PHASE_DESCRIPTORS, 1);
   *Xout = X;
@@ -339,7 +357,7 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
 // lambda, or a 1e-12 relative jitter when lambda <= 0).  G is left intact.
 int solve_any(mld_gpu_handle* h, double* G, const double* rhs, int D, double* w) {
   if (D <= 112) {
-    CK(launch_solve_sym(G, rhs, D, h->cfg.lambda_krr, h->cfg.svd_rcond, w, bp_<double>(h, mld_gpu_handle::B_EVALS),
+    CK(launch_solve_sym(G, rhs, D, h->lam_eff, h->cfg.svd_rcond, w, bp_<double>(h, mld_gpu_handle::B_EVALS),
                         bp_<int>(h, mld_gpu_handle::B_INFO), h->st));
     nl(h, 1);
     return MLD_OK;
@@ -352,7 +370,7 @@ int solve_any(mld_gpu_handle* h, double* G, const double* rhs, int D, double* w)
   double* r = bp_<double>(h, mld_gpu_handle::B_RES);
   double* dw = bp_<double>(h, mld_gpu_handle::B_DW);
   double* tmp = dw + D;
-  double shift = h->cfg.lambda_krr > 0 ? h->cfg.lambda_krr : 0.0;
+  double shift = h->lam_eff > 0 ? h->lam_eff : 0.0;
   if (shift <= 0) {
     std::vector<double> diag(D);
     CK(cudaMemcpy2DAsync(diag.data(), sizeof(double), G, sizeof(double) * (D + 1), sizeof(double), D,
@@ -404,6 +422,10 @@ void full_to_dedup(const mld_gpu_handle* h, const double* wf, double* wd) {
 // a working-layout design row -> the reference's row (full K*K quadratic block)
 void export_row(const mld_gpu_handle* h, const double* xd, double* xf) {
   const int KK = h->KK, DL = h->DL;
+  if (h->krr) {
+    for (int c = 0; c < h->D; ++c) xf[c] = xd[c];
+    return;
+  }
   for (int c = 0; c < DL; ++c) xf[c] = xd[c];
   if (!h->quad) return;
   const double r2 = std::sqrt(2.0);
@@ -474,7 +496,7 @@ int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const dou
   double* G = bp_<double>(h, mld_gpu_handle::B_G);
   double* hv = bp_<double>(h, mld_gpu_handle::B_H);
   const double* wrow = bp_<double>(h, mld_gpu_handle::B_WROW);
-  const double lam = h->cfg.lambda_krr > 0 ? h->cfg.lambda_krr : 0.0;
+  const double lam = h->lam_eff > 0 ? h->lam_eff : 0.0;
   mark(h, MLD_PHASE_GRAM, 0);
   const size_t need = (size_t)4 * Db * (size_t)((std::max<long long>(M, 1) + 63) / 64 * 64) + 256;
   const size_t wsb = std::max(gram_tc_min_workspace(Db), std::min(need, kGramWorkspaceCap));
@@ -609,8 +631,15 @@ int fit_block<float>(mld_gpu_handle* h, const float* X, int c0, int Db, const do
   return fit_block_mixed(h, X, c0, Db, y, M, w, stage);
 }
 
+void set_lam_eff(mld_gpu_handle* h) {
+  const double l = h->cfg.lambda_krr > 0 ? h->cfg.lambda_krr : 0.0;
+  h->lam_eff = h->krr ? l * l : l;  // parameters.F90:1018-1099 (lambda) / :1217-1395 (lambda^2)
+}
+
 template <typename T>
 int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
+  if (h->krr && h->nk == 0) return fail(h, MLD_ERR_STATE, "kernel model without reference points");
+  set_lam_eff(h);
   h->pending.clear();
   h->pcg_iters[0] = h->pcg_iters[1] = 0;
   h->chol_retries = 0;
@@ -623,7 +652,7 @@ int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
   if (rc) return rc;
   const long long M = h->fit_rows.M;
   const int D = h->D;
-  const size_t gdim = (size_t)std::max(h->DL, h->DQ);
+  const size_t gdim = (size_t)std::max(h->krr ? h->D : h->DL, h->DQ);
   CK(ensure(h, mld_gpu_handle::B_G, sizeof(double) * gdim * gdim));
   CK(ensure(h, mld_gpu_handle::B_H, sizeof(double) * gdim));
   CK(ensure(h, mld_gpu_handle::B_W, sizeof(double) * D));
@@ -632,8 +661,9 @@ int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
   CK(ensure(h, mld_gpu_handle::B_SQ, sizeof(double) * 6));
   double* w = bp_<double>(h, mld_gpu_handle::B_W);
   double* y = bp_<double>(h, mld_gpu_handle::B_Y);
-  // linear block (QNML stage 1, or the whole linear model): parameters.F90:1018-1099
-  rc = fit_block<T>(h, X, 0, h->DL, y, M, w, 0);
+  // linear block (QNML stage 1, or the whole linear model): parameters.F90:1018-1099; the
+  // kernel model is one block of all its columns (parameters.F90:1217-1395)
+  rc = fit_block<T>(h, X, 0, h->krr ? h->D : h->DL, y, M, w, 0);
   if (rc) return rc;
   if (h->quad) {
     // QNML stage 2 (parameters.F90:404-421, 476-1015): the quadratic block is fitted to the
@@ -701,6 +731,10 @@ void mld_gpu_config_defaults(mld_gpu_config* c) {
   c->sign_stress_big_box = 1.0;
   c->imm_neigh = 300;
   c->precision = MLD_PRECISION_PLAIN_FP64;
+  c->kernel_type = 4;
+  c->kernel_power = 2.0;
+  c->length_kernel = std::sqrt(0.5);
+  c->sigma_kernel = 0.0;
 }
 
 const char* mld_gpu_last_error(const mld_gpu_handle* h) { return h ? h->err.c_str() : "null handle"; }
@@ -709,7 +743,10 @@ int mld_gpu_create(const mld_gpu_config* cfg, mld_gpu_handle** out) {
   if (!cfg || !out) return MLD_ERR_INVALID;
   *out = nullptr;
   if (cfg->descriptor_type != 9) return MLD_ERR_UNSUPPORTED;
-  if (cfg->ml_type != 0 || (cfg->mld_order != 1 && cfg->mld_order != 2)) return MLD_ERR_UNSUPPORTED;
+  if (cfg->ml_type != 0 && cfg->ml_type != 1) return MLD_ERR_UNSUPPORTED;
+  if (cfg->ml_type == 0 && cfg->mld_order != 1 && cfg->mld_order != 2) return MLD_ERR_UNSUPPORTED;
+  if (cfg->ml_type == 1 && cfg->kernel_type != 4) return MLD_ERR_UNSUPPORTED;  // polynomial kernel only
+  if (cfg->ml_type == 1 && !(cfg->length_kernel > 0)) return MLD_ERR_INVALID;
   if (!(cfg->inv_r0_input > 0.0 && cfg->inv_r0_input < 1.0)) return MLD_ERR_INVALID;  // test_parameters_bso4
   if (cfg->j_max < 0 || !(cfg->r_cut > 0)) return MLD_ERR_INVALID;
   if (cfg->n_elements < 1 || cfg->n_elements > MLD_MAX_ELEMENTS) return MLD_ERR_INVALID;
@@ -735,7 +772,9 @@ int mld_gpu_create(const mld_gpu_config* cfg, mld_gpu_handle** out) {
   h->K = t.K;
   h->KK = h->nch * t.K;
   h->DL = 1 + h->KK;
-  h->quad = cfg->mld_order == 2;
+  h->krr = cfg->ml_type == 1;
+  h->quad = !h->krr && cfg->mld_order == 2;
+  set_lam_eff(h);
   h->DQ = h->quad ? h->KK * (h->KK + 1) / 2 : 0;
   h->D = h->DL + h->DQ;                                       // working (deduplicated) row width
   h->Dfull = h->DL + (h->quad ? h->KK * h->KK : 0);           // reference layout (dim_design_line)
@@ -1265,6 +1304,40 @@ extern "C" int mld_gpu_peak_flops(mld_gpu_handle* h, int precision, double* tflo
   cudaError_t e = precision == MLD_PRECISION_MIXED ? mld::measure_fma_peak<float>(h->st, tflops)
                                                    : mld::measure_fma_peak<double>(h->st, tflops);
   return e == cudaSuccess ? MLD_OK : cuda_fail(h, e, "mld_gpu_peak_flops");
+}
+
+extern "C" int mld_gpu_set_kernel_points(mld_gpu_handle* h, int nk, const double* z_raw) {
+  if (!h) return MLD_ERR_INVALID;
+  if (!h->krr) return fail(h, MLD_ERR_STATE, "reference points need ml_type = 1");
+  if (nk < 1 || !z_raw) return fail(h, MLD_ERR_INVALID, "need at least one reference point");
+  const int KK = h->KK;
+  // standardisation over the reference set (compute_kernel.F90:1058-1256, init_kernel)
+  std::vector<double> mean(KK, 0.0), sd(KK, 0.0), zd((size_t)nk * KK);
+  for (int k = 0; k < nk; ++k)
+    for (int c = 0; c < KK; ++c) mean[c] += z_raw[(size_t)k * KK + c];
+  for (int c = 0; c < KK; ++c) mean[c] /= nk;
+  for (int k = 0; k < nk; ++k)
+    for (int c = 0; c < KK; ++c) {
+      const double d = z_raw[(size_t)k * KK + c] - mean[c];
+      sd[c] += d * d;
+    }
+  for (int c = 0; c < KK; ++c) {
+    sd[c] = std::sqrt(sd[c] / nk);
+    if (!(sd[c] > 0.0))
+      return fail(h, MLD_ERR_INVALID, "kernel reference points: descriptor component " + std::to_string(c) +
+                                          " has zero spread over the set");
+  }
+  for (int k = 0; k < nk; ++k)
+    for (int c = 0; c < KK; ++c) zd[(size_t)k * KK + c] = (z_raw[(size_t)k * KK + c] - mean[c]) / sd[c];
+  std::vector<float> zf(zd.begin(), zd.end());
+  CK(upload(h, mld_gpu_handle::B_KZD, zd.data(), zd.size()));
+  CK(upload(h, mld_gpu_handle::B_KZF, zf.data(), zf.size()));
+  CK(cudaStreamSynchronize(h->st));
+  h->nk = nk;
+  h->D = h->DL + nk;
+  h->Dfull = h->D;
+  h->ldx = round_up4(h->D);
+  return MLD_OK;
 }
 
 extern "C" int mld_gpu_solve_info(const mld_gpu_handle* h, int* pcg_iterations, double* pcg_residual,

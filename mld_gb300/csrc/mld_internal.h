@@ -160,6 +160,7 @@ struct DevBatch {
   int* nbr_idx = nullptr;    // P
   double* nbr_u = nullptr;   // 3P  (x_neighbour - x_centre, FP64)
   long long P = 0;
+  int maxnn = 0;             // largest neighbour count (after the counting pass)
 };
 
 // Design-row placement of each structure (-1 when a block is absent).
@@ -241,6 +242,14 @@ cudaError_t launch_pcg_alpha(int D, const double* p, const double* q, double* x,
                              cudaStream_t st);
 cudaError_t launch_pcg_beta(int D, const double* z, const double* r, double* p, double* scal, int first,
                             cudaStream_t st);
+
+// kernel ridge regression rows (kernel_rows.cu)
+size_t krr_workspace_elems(int A, int nk, int KK);
+template <typename T>
+cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* rev, const T* Bq, const T* dBq,
+                            const T* Z, int nk, int KK, double power, double length, double sigma,
+                            double sign_stress, double sign_big, T* ws, T* X, int c0, cudaStream_t st,
+                            int* launches);
 
 // tensor-core Gram in BF16 split precision (gram_tc.cu)
 size_t gram_tc_min_workspace(int D);

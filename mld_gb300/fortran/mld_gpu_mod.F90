@@ -35,11 +35,16 @@ module mld_gpu_mod
     real(c_double) :: sign_stress_big_box
     integer(c_int) :: imm_neigh
     integer(c_int) :: precision
+    integer(c_int) :: kernel_type
+    real(c_double) :: kernel_power
+    real(c_double) :: length_kernel
+    real(c_double) :: sigma_kernel
   end type mld_gpu_config
 
   public :: mld_gpu_config_defaults, mld_gpu_create, mld_gpu_destroy, mld_gpu_dims, &
             mld_gpu_set_structures, mld_gpu_set_labels, mld_gpu_descriptors, mld_gpu_num_rows, &
             mld_gpu_design_matrix, mld_gpu_gram, mld_gpu_solve, mld_gpu_fit, mld_gpu_predict, &
+            mld_gpu_set_kernel_points, &
             mld_gpu_synchronize
 
   interface
@@ -114,6 +119,12 @@ module mld_gpu_mod
     integer(c_int) function mld_gpu_predict(h, w_params, e, f, s) bind(C, name="mld_gpu_predict")
       import :: c_int, c_ptr
       type(c_ptr), value :: h, w_params, e, f, s
+    end function
+
+    integer(c_int) function mld_gpu_set_kernel_points(h, nk, z_raw) bind(C, name="mld_gpu_set_kernel_points")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, z_raw
+      integer(c_int), value :: nk
     end function
 
     integer(c_int) function mld_gpu_synchronize(h) bind(C, name="mld_gpu_synchronize")

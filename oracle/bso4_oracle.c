@@ -638,3 +638,91 @@ int orc_rows_quadratic(int nat, int KK, const double *B, const double *dB, const
     }
     return 0;
 }
+
+/* Kernel ridge design rows (ml_type = 1, polynomial kernel kernel_type = 4) of one structure,
+ * D = 1 + KK + nk: columns [const, linear descriptor part, kernel part]
+ * (mld_energy.F90:122-144, mld_forces.F90:268-320, mld_stress.F90:246-250,456,577).
+ * Per atom x = B_i (raw) and reference point z_k (standardised, init_kernel in
+ * compute_kernel.F90:1058-1256), inner_kernel_po (compute_kernel.F90:91-150):
+ *   f(x,z) = (sigma2 + x.z/l2)^p, k = f / sqrt(f(x,x) f(z,z)), l2 = 2 length^2;
+ *   per neighbour n and direction a, with g = force(:, i, n, a):
+ *   dk = (p (sigma2 + x.z/l2)^(p-1)/l2 (g.z) - f * (g.x) * dker_xx / (2 f(x,x))) / sqrt(f(x,x) f(z,z)),
+ *   dker_xx = 2 p (sigma2 + x.x/l2)^(p-1)/l2; force_kernel(k, i, 0) = -sum_n dk.
+ * An atom without neighbours contributes zero kernel energy (compute_kernel.F90:747-749).
+ * Packing follows the linear rows: row(i) += sum_n dk, row(nbr) -= dk; stress rows from the
+ * per-pair dk with uu/r as in orc_rows_linear. */
+int orc_rows_kernel(int nat, int KK, const double *B, const double *dB, const int *nn, const int *nbr,
+                    const double *u, int cap, int is_small, double sign_stress, double sign_big, double volume,
+                    int nk, const double *Z, double power, double length, double sigma,
+                    double *rowE, double *rowF, double *rowS) {
+    const int D = 1 + KK + nk, c0 = 1 + KK;
+    static const int sa[6] = {0, 1, 2, 1, 0, 0}, sb[6] = {0, 1, 2, 2, 2, 1};
+    const double l2 = 2.0 * length * length, s2 = sigma * sigma;
+    /* linear part first (also zeroes the rows) */
+    double *tE = rowE ? malloc(sizeof(double) * (1 + KK)) : NULL;
+    double *tF = rowF ? malloc(sizeof(double) * (size_t)3 * nat * (1 + KK)) : NULL;
+    double *tS = rowS ? malloc(sizeof(double) * 6 * (1 + KK)) : NULL;
+    orc_rows_linear(nat, KK, B, dB, nn, nbr, u, cap, is_small, sign_stress, sign_big, volume, tE, tF, tS);
+    if (rowE) { memset(rowE, 0, sizeof(double) * D); memcpy(rowE, tE, sizeof(double) * (1 + KK)); }
+    if (rowF) {
+        memset(rowF, 0, sizeof(double) * (size_t)3 * nat * D);
+        for (long r = 0; r < 3L * nat; r++) memcpy(rowF + r * D, tF + r * (1 + KK), sizeof(double) * (1 + KK));
+    }
+    if (rowS) {
+        memset(rowS, 0, sizeof(double) * 6 * D);
+        for (int r = 0; r < 6; r++) memcpy(rowS + r * D, tS + r * (1 + KK), sizeof(double) * (1 + KK));
+    }
+    free(tE); free(tF); free(tS);
+    double *zz = malloc(sizeof(double) * nk);
+    for (int k = 0; k < nk; k++) {
+        double s = 0.0;
+        for (int c = 0; c < KK; c++) s += Z[(size_t)k * KK + c] * Z[(size_t)k * KK + c];
+        zz[k] = pow(s2 + s / l2, power);  /* f(z,z) */
+    }
+    double *gx = malloc(sizeof(double) * 3), *Sk = calloc((size_t)6 * nk, sizeof(double));
+    for (int i = 0; i < nat; i++) {
+        if (nn[i] == 0) continue;
+        const double *x = B + (size_t)i * KK;
+        double xx = 0.0;
+        for (int c = 0; c < KK; c++) xx += x[c] * x[c];
+        const double kxx = pow(s2 + xx / l2, power), skxx = sqrt(kxx);
+        const double dkxx = 2.0 * power * pow(s2 + xx / l2, power - 1.0) / l2;
+        for (int k = 0; k < nk; k++) {
+            const double *z = Z + (size_t)k * KK;
+            double xz = 0.0;
+            for (int c = 0; c < KK; c++) xz += x[c] * z[c];
+            const double base = s2 + xz / l2;
+            const double kt = pow(base, power);
+            const double aaa = sqrt(zz[k]) * skxx, bbb = 2.0 * kxx;
+            if (rowE) rowE[c0 + k] += kt / aaa;
+            const double tf1 = power * pow(base, power - 1.0) / l2;
+            for (int n = 0; n < nn[i]; n++) {
+                const int ia = nbr[i * cap + n];
+                const double *xn = u + ((size_t)i * cap + n) * 3;
+                const double r = sqrt(xn[0] * xn[0] + xn[1] * xn[1] + xn[2] * xn[2]);
+                double dk[3];
+                for (int a = 0; a < 3; a++) {
+                    const double *g = dB + (((size_t)i * cap + n) * 3 + a) * KK;
+                    double gz = 0.0, gxv = 0.0;
+                    for (int c = 0; c < KK; c++) { gz += g[c] * z[c]; gxv += g[c] * x[c]; }
+                    dk[a] = (tf1 * gz - kt * gxv * dkxx / bbb) / aaa;
+                    if (rowF) {
+                        rowF[((size_t)i * 3 + a) * D + c0 + k] += dk[a];
+                        rowF[((size_t)ia * 3 + a) * D + c0 + k] -= dk[a];
+                    }
+                }
+                if (rowS) {
+                    double uu[3];
+                    for (int c = 0; c < 3; c++) uu[c] = is_small ? xn[c] : -sign_big * xn[c];
+                    for (int s = 0; s < 6; s++) Sk[(size_t)s * nk + k] += dk[sa[s]] * uu[sb[s]] / r;
+                }
+            }
+        }
+    }
+    if (rowS) {
+        const double sc = sign_stress * 3.0 / volume;
+        for (int s = 0; s < 6; s++) for (int k = 0; k < nk; k++) rowS[s * D + c0 + k] = sc * Sk[(size_t)s * nk + k];
+    }
+    free(zz); free(gx); free(Sk);
+    return 0;
+}

@@ -188,3 +188,41 @@ def fit_qnml(A: np.ndarray, y: np.ndarray, wts: np.ndarray, lam: float, n_linear
     res = y - AL @ wL
     wQ = fit_linear(AQ, res, wts, lam, rcond)
     return np.concatenate([wL, wQ])
+
+
+def kernel_points(B_ref: np.ndarray):
+    """Standardised reference points of the kernel (compute_kernel.F90:1058-1256, init_kernel):
+    z = (z_raw - mean) / std over the reference set (std = population standard deviation)."""
+    Br = np.asarray(B_ref, dtype=np.float64)
+    mean = Br.mean(axis=0)
+    std = np.sqrt(((Br - mean) ** 2).sum(axis=0) / Br.shape[0])
+    return (Br - mean) / std, mean, std
+
+
+def kernel_rows(desc: Dict[str, np.ndarray], cell: np.ndarray, Z: np.ndarray, *, power: float = 2.0,
+                length: float = np.sqrt(0.5), sigma: float = 0.0, sign_stress: float = 1.0, sign_big: float = 1.0):
+    """Kernel ridge design rows (polynomial kernel) in the reference layout 1 + KK + nk."""
+    L = lib()
+    d, i, p = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+    L.orc_rows_kernel.argtypes = [i, i, p, p, p, p, p, i, i, d, d, d, i, p, d, d, d, p, p, p]
+    B, dB = desc["B"], desc["dB"]
+    nat, KK = B.shape
+    Zc = np.ascontiguousarray(Z, dtype=np.float64)
+    nk = Zc.shape[0]
+    D = 1 + KK + nk
+    rowE = np.zeros(D)
+    rowF = np.zeros((3 * nat, D))
+    rowS = np.zeros((6, D))
+    vol = L.orc_volume(_ptr(np.ascontiguousarray(cell, dtype=np.float64)))
+    L.orc_rows_kernel(nat, KK, _ptr(B), _ptr(dB), _ptr(desc["nn"]), _ptr(desc["nbr"]), _ptr(desc["u"]),
+                      desc["cap"], int(desc["small"]), float(sign_stress), float(sign_big), float(vol), nk, _ptr(Zc),
+                      float(power), float(length), float(sigma), _ptr(rowE), _ptr(rowF), _ptr(rowS))
+    return rowE, rowF, rowS
+
+
+def fit_kernel(A: np.ndarray, y: np.ndarray, wts: np.ndarray, lam: float, rcond: float = -1.0) -> np.ndarray:
+    """Kernel ridge solve (parameters.F90:1217-1395): [sqrt(W) A; lambda I] w ~ [sqrt(W) y; 0], i.e.
+    the normal equations with a lambda^2 penalty (lambda < 0 -> 0)."""
+    lam = 0.0 if lam < 0 else lam
+    phi, rhs = normal_equations(A, y, wts, lam * lam)
+    return solve_gelsd(phi, rhs, rcond)

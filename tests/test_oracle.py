@@ -83,3 +83,24 @@ def test_gelsd_min_norm_on_rank_deficient():
     y = rng.normal(size=50)
     w = oracle.fit_linear(A, y, np.ones(50), -1.0)
     assert abs(w[4] - w[5]) < 1e-10       # minimum norm splits the duplicate evenly
+
+
+def test_kernel_rows_are_gradients_of_the_energy_row():
+    """Kernel force rows equal minus the position gradient of the kernel energy row, the
+    convention of the linear rows (compute_kernel.F90:91-150 with the mld_forces packing)."""
+    from mld_gb300 import synth
+    ds = synth.fe_bcc_batched(n_struct=1, nmin=16, nmax=40, seed=4)
+    s = ds.structures[0]
+    d = oracle.bispectrum(s.positions, s.cell, s.types, 4.7, 1.5)
+    Z, _, _ = oracle.kernel_points(d["B"][:6])
+    E, F, S = oracle.kernel_rows(d, s.cell, Z, power=2.0, length=0.8, sigma=0.3)
+    h = 1e-5
+    for atom, comp in ((0, 0), (3, 2)):
+        rows = []
+        for sgn in (1, -1):
+            p = s.positions.copy()
+            p[atom, comp] += sgn * h
+            dd = oracle.bispectrum(p, s.cell, s.types, 4.7, 1.5)
+            rows.append(oracle.kernel_rows(dd, s.cell, Z, power=2.0, length=0.8, sigma=0.3)[0])
+        fd = (rows[0] - rows[1]) / (2 * h)
+        assert np.abs(fd + F[3 * atom + comp]).max() <= 1e-6 * max(1.0, np.abs(fd).max())
