@@ -47,9 +47,11 @@ def _args():
     p.add_argument("--plain-steps", type=int, default=2)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--workload", choices=["fe_linear", "hea_qnml"], default="fe_linear",
+    p.add_argument("--workload", choices=["fe_linear", "hea_qnml", "hea_krr"], default="fe_linear",
                    help="fe_linear: batched linear Fe fit (default); hea_qnml: quadratic QNML fit of the "
-                        "5-element alloy (4,000 x 250 atoms, weighted two-channel bispectrum)")
+                        "5-element alloy (4,000 x 250 atoms, weighted two-channel bispectrum); hea_krr: kernel "
+                        "ridge regression of the same structures with 4,000 leverage-selected reference atoms")
+    p.add_argument("--ref-points", type=int, default=4000, help="hea_krr: kernel reference points")
     p.add_argument("--plain-structures", type=int, default=200,
                    help="hea_qnml: structures of the sample on which mixed and plain FP64 are compared")
     return p.parse_args()
@@ -297,6 +299,87 @@ def run_hea(a):
     print(json.dumps(line))
 
 
+def run_hea_krr(a):
+    """Kernel ridge regression (ml_type 1, polynomial kernel p = 2, length sqrt(1/2), sigma 0,
+    lambda = 1e-6 with the lambda^2 penalty) of the 5-element alloy set: reference atoms chosen
+    by seeded leverage-score selection over all atoms' descriptors.  One step = one full mixed
+    fit (descriptors, kernel features and derivatives, design rows, tensor-core Gram, CG); the
+    plain FP64 method is compared on the first --plain-structures structures with the same
+    reference points."""
+    from mld_gb300 import _lib, kernel_select, synth
+    n_struct = a.structures if a.structures != N_STRUCT else 4000
+    ds = synth.hea_bcc_batched(n_struct=n_struct, workers=min(16, os.cpu_count() or 1))
+    lam = 1e-6
+
+    def handle(precision, idx=None):
+        c = _lib.default_config()
+        c.j_max, c.r_cut, c.lambda_krr, c.precision, c.ml_type = 4.0, 5.0, lam, precision, 1
+        c.weighted = 1
+        c.n_elements = len(synth.HEA_ELEMENTS)
+        for i, wv in enumerate(synth.HEA_WEIGHTS):
+            c.weight_per_element[i] = wv
+        h = _lib.Handle(c)
+        sub = ds if idx is None else synth.Dataset([ds.structures[i] for i in idx], ds.rcut, ds.name)
+        nat, pos, cell, types = sub.arrays()
+        E, F, S, has = sub.labels()
+        h.set_structures(nat, pos, cell, types)
+        h.set_labels(E, F, S, has, np.ones((len(nat), 3)))
+        return h, int(nat.sum())
+
+    h, A = handle(_lib.MIXED)
+    B, _ = h.descriptors()
+    ref = kernel_select.select(B, a.ref_points)
+    Zraw = B[ref].copy()
+    del B
+    h.set_kernel_points(Zraw)
+    M = h.num_rows()
+    for _ in range(a.warmup):
+        h.fit()
+    h.set_profiling(True)
+    h.profile(reset=True)
+    with Clocks() as clk:
+        h.timer_start()
+        for _ in range(a.steps):
+            w, rmse = h.fit()
+        ms = h.timer_stop() / a.steps
+    prof = h.profile(reset=True)
+    out = dict(ms=ms, rmse=rmse.tolist(), prof={k: v[0] / a.steps for k, v in prof.items()},
+               launches=int(sum(v[1] for v in prof.values())), solve=h.solve_info(), clocks=clk.summary(),
+               D=h.dim_design_line)
+    h.close()
+    sample = {}
+    if a.plain_structures > 0:
+        idx = list(range(min(a.plain_structures, n_struct)))
+        for name, prec in (("mixed", _lib.MIXED), ("plain_fp64", _lib.PLAIN_FP64)):
+            hs, As = handle(prec, idx)
+            hs.set_kernel_points(Zraw)
+            Ms = hs.num_rows()
+            hs.fit()
+            hs.timer_start()
+            ws, rs = hs.fit()
+            t = hs.timer_stop()
+            sample[name] = {"ms_per_fit": t, "design_rows": Ms, "rows_per_s": Ms / (t * 1e-3), "rmse_efs": rs.tolist()}
+            hs.close()
+        mx, pl = sample["mixed"], sample["plain_fp64"]
+        sample["force_rmse_rel_diff"] = abs(mx["rmse_efs"][1] - pl["rmse_efs"][1]) / pl["rmse_efs"][1]
+        sample["speedup_rows_per_s_vs_plain_fp64"] = (M / (ms * 1e-3)) / pl["rows_per_s"]
+    line = {
+        "metric": "design rows/s (kernel ridge regression, polynomial kernel, 5-element bcc alloy)",
+        "value": M / (ms * 1e-3), "unit": "design rows/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 descriptors/kernel rows + bf16x3 tensor-core Gram (fp32 acc) + fp64 Cholesky / double-fp32 CG",
+        "data": "synthetic",
+        "config": {"workload": "hea_bcc_MoNbTaVCr_4000x250_krr_poly2_weighted_jmax4", "structures": n_struct,
+                   "atoms": A, "design_rows": M, "reference_points": int(a.ref_points),
+                   "dim_design_line": out["D"], "r_cut": 5.0, "lambda_krr": lam, "penalty": "lambda^2",
+                   "l2": "working set above L2 every step", "parallelism": "single"},
+        "atom_evals_per_s": A / (ms * 1e-3), "rmse_efs": out["rmse"], "phase_ms": out["prof"],
+        "mixed_solve": out["solve"], "gpu_launches": out["launches"], "clocks": out["clocks"],
+        "sample_comparison": sample or None,
+    }
+    print(json.dumps(line))
+
+
 def cpu_sample(ds, target_s=15.0, threads=None):
     """Time the oracle (CPU restatement of the reference) on a bounded sample of the same set:
     neighbours + descriptors + rows in C (OpenMP over structures), Gram + gelsd in NumPy/LAPACK."""
@@ -371,9 +454,9 @@ def main():
         print(json.dumps(line))
         return
 
-    if a.workload == "hea_qnml":
+    if a.workload in ("hea_qnml", "hea_krr"):
         if rank == 0:
-            run_hea(a)
+            run_hea(a) if a.workload == "hea_qnml" else run_hea_krr(a)
         return
     if world > 1:
         import torch.distributed as dist

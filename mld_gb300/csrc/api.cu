@@ -370,29 +370,35 @@ int solve_any(mld_gpu_handle* h, double* G, const double* rhs, int D, double* w)
   double* r = bp_<double>(h, mld_gpu_handle::B_RES);
   double* dw = bp_<double>(h, mld_gpu_handle::B_DW);
   double* tmp = dw + D;
-  double shift = h->lam_eff > 0 ? h->lam_eff : 0.0;
-  if (shift <= 0) {
-    std::vector<double> diag(D);
-    CK(cudaMemcpy2DAsync(diag.data(), sizeof(double), G, sizeof(double) * (D + 1), sizeof(double), D,
-                         cudaMemcpyDeviceToHost, h->st));
-    CK(cudaStreamSynchronize(h->st));
-    double mx = 0;
-    for (double v : diag) mx = std::max(mx, std::fabs(v));
-    shift = 1e-12 * (mx > 0 ? mx : 1.0);
-  }
-  CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)D * D, cudaMemcpyDeviceToDevice, h->st));
-  int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
-  CK(launch_cholesky(Lf, D, shift, info, h->st));
-  CK(launch_chol_solve_blocked(Lf, D, rhs, w, tmp, h->st));
-  for (int it = 0; it < 2; ++it) {
-    CK(launch_residual(G, D, shift, w, rhs, r, h->st));
-    CK(launch_chol_solve_blocked(Lf, D, r, dw, tmp, h->st));
-    CK(launch_axpy(D, 1.0, dw, w, h->st));
-  }
-  nl(h, cholesky_launches(D) + 3 * chol_solve_launches(D) + 4);
-  int hinfo = 0;
-  CK(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  // diagonal shift: lambda, but at least 1e-12 of the largest diagonal entry (a rank-deficient
+  // normal matrix: the min-norm solution of dgelsd differs only in the near-null space); x10 on
+  // a failed factorisation
+  std::vector<double> diag(D);
+  CK(cudaMemcpy2DAsync(diag.data(), sizeof(double), G, sizeof(double) * (D + 1), sizeof(double), D,
+                       cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
+  double mx = 0;
+  for (double v : diag) mx = std::max(mx, std::fabs(v));
+  double jitter = 1e-12 * (mx > 0 ? mx : 1.0);
+  int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
+  int hinfo = 0;
+  for (int attempt = 0; attempt < 5; ++attempt, jitter *= 10.0) {
+    const double shift = std::max(h->lam_eff > 0 ? h->lam_eff : 0.0, jitter);
+    CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)D * D, cudaMemcpyDeviceToDevice, h->st));
+    CK(launch_cholesky(Lf, D, shift, info, h->st));
+    CK(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    nl(h, cholesky_launches(D));
+    if (hinfo != 0) continue;
+    CK(launch_chol_solve_blocked(Lf, D, rhs, w, tmp, h->st));
+    for (int it = 0; it < 2; ++it) {
+      CK(launch_residual(G, D, shift, w, rhs, r, h->st));
+      CK(launch_chol_solve_blocked(Lf, D, r, dw, tmp, h->st));
+      CK(launch_axpy(D, 1.0, dw, w, h->st));
+    }
+    nl(h, 3 * chol_solve_launches(D) + 4);
+    break;
+  }
   if (hinfo != 0)
     return fail(h, MLD_ERR_SOLVE, "normal matrix not positive definite at column " + std::to_string(hinfo));
   return MLD_OK;

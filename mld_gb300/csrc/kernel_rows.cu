@@ -94,15 +94,26 @@ __global__ void __launch_bounds__(256) k_krr_xz(int A, int nk, int KK, const T* 
     }
 }
 
+// base^p for the kernel power: repeated products for small integer powers, pow otherwise
+__device__ __forceinline__ double kpow(double base, double p) {
+  const int ip = (int)p;
+  if ((double)ip == p && ip >= 0 && ip <= 8) {
+    double r = 1.0;
+    for (int i = 0; i < ip; ++i) r *= base;
+    return r;
+  }
+  return pow(base, p);
+}
+
 // kernel value and the two derivative coefficients of centre atom a and reference point k
 template <typename T>
 __device__ __forceinline__ void krr_coef(T xz, const T* at, T szz, double s2, double l2, double p, T& kv, T& c1,
                                          T& c2) {
   const double base = s2 + (double)xz / l2;
-  const double kt = pow(base, p);
+  const double kt = kpow(base, p);
   const double aaa = (double)szz * (double)at[1];
   kv = (T)(kt / aaa);
-  c1 = (T)(p * pow(base, p - 1.0) / l2 / aaa);
+  c1 = (T)(p * kpow(base, p - 1.0) / l2 / aaa);
   c2 = (T)(kt * (double)at[2] / (2.0 * (double)at[0]) / aaa);
 }
 
@@ -125,112 +136,193 @@ __global__ void __launch_bounds__(kKT) k_krr_energy(int nk, const int* __restric
   X[rowE[s] * ldx + c0 + k] = (T)acc;
 }
 
-// Derivative vectors of target atom a (staged by k_krr_force): vector 0 is the sum of a's own
-// pair derivatives (self term, centre a, sign +1); vectors 1..n are the derivatives of the
-// reversed pairs (j -> a) (centre j, sign -1).  Per vector and direction also g . x_centre.
-// One CTA per atom; threads over reference points.
+// Force rows as a register-tiled product: CTA = (tile of NZ reference points, range of target
+// atoms).  The tile of standardised reference points Zs[c][k] stays in shared memory; for each
+// target atom a its derivative vectors are staged as rows r = 3 v + alpha (vector 0: sum of a's
+// own pair derivatives, centre a, sign +1; vectors 1..n: the reversed pairs (j -> a), centre j,
+// sign -1), the dots (row . z_k) are formed in 6 x (NZ/16) register tiles, and the epilogue
+// forms sign * (c1(centre, k) dot - c2(centre, k) (row . x_centre)) and sums the rows of each
+// alpha into the atom's three force rows.
+template <int NZ_>
+struct KrrTile {
+  static constexpr int NZ = NZ_;      // reference points per tile
+  static constexpr int CJ = NZ / 16;  // columns per thread
+  static constexpr int RI = 6;        // rows per thread per pass (96 rows per pass)
+};
+
+// kernel coefficients of centre atom (its [f(x,x), sqrt f(x,x), dker_xx, has neighbours]) and
+// a reference point, in the kernel's precision: (c1, c2); zero for an atom without neighbours
 template <typename T>
-__global__ void __launch_bounds__(kKT) k_krr_force(
-    int KK, int nk, const int* __restrict__ atom_struct, const int* __restrict__ atom_start,
-    const long long* __restrict__ rowF, const int* __restrict__ nbr_off, const int* __restrict__ nbr_idx,
-    const int* __restrict__ rev, const T* __restrict__ B, const T* __restrict__ dB, const T* __restrict__ Zt,
-    const T* __restrict__ F, const T* __restrict__ at, const T* __restrict__ szz, double s2, double l2, double p,
-    int c0, int ldx, T* __restrict__ X) {
+__device__ __forceinline__ void krr_c12(T xz, const T* atc, T szz, T s2, T l2, T p, T& c1, T& c2) {
+  if (atc[3] == T(0)) {
+    c1 = c2 = T(0);
+    return;
+  }
+  const T base = s2 + xz / l2;
+  T bp1 = T(1);  // base^(p-1)
+  const int ip = (int)p;
+  if ((T)ip == p && ip >= 1 && ip <= 8) {
+    for (int i = 1; i < ip; ++i) bp1 *= base;
+  } else {
+    bp1 = (T)pow((double)base, (double)p - 1.0);
+  }
+  const T kt = bp1 * base;
+  const T inv_aaa = T(1) / (szz * atc[1]);
+  c1 = p * bp1 / l2 * inv_aaa;
+  c2 = kt * atc[2] / (T(2) * atc[0]) * inv_aaa;
+}
+
+template <typename T, int NZ_>
+__global__ void __launch_bounds__(256) k_krr_force_tiled(
+    int KK, int nk, int A, int atoms_per_cta, int maxnv, const int* __restrict__ atom_struct,
+    const int* __restrict__ atom_start, const long long* __restrict__ rowF, const int* __restrict__ nbr_off,
+    const int* __restrict__ nbr_idx, const int* __restrict__ rev, const T* __restrict__ B, const T* __restrict__ dB,
+    const T* __restrict__ Z, const T* __restrict__ F, const T* __restrict__ at, const T* __restrict__ szz, double s2,
+    double l2, double p, int c0, int ldx, T* __restrict__ X) {
+  using Tl = KrrTile<NZ_>;
+  constexpr int NZ = Tl::NZ, CJ = Tl::CJ, RI = Tl::RI;
   extern __shared__ __align__(16) unsigned char ksm[];
-  const int a = blockIdx.x;
-  const int s = atom_struct[a];
-  if (rowF[s] < 0) return;
-  const int p0 = nbr_off[a], nn = nbr_off[a + 1] - p0;
-  const int nv = nn + 1;
-  T* V = reinterpret_cast<T*>(ksm);                 // nv * 3 * KK
-  T* gx = V + (size_t)nv * 3 * KK;                   // nv * 3
-  int* cen = reinterpret_cast<int*>(gx + nv * 3);    // nv
-  const int tid = threadIdx.x;
-  // stage the vectors
-  for (int e = tid; e < 3 * KK; e += kKT) {
-    T acc = T(0);
-    for (int q = 0; q < nn; ++q) acc += dB[(size_t)(p0 + q) * 3 * KK + e];
-    V[e] = acc;
+  T* Zs = reinterpret_cast<T*>(ksm);                   // KK * NZ   [c][k]
+  T* Vt = Zs + (size_t)KK * NZ;                        // KK * (3 maxnv)  [c][r]
+  T* gx = Vt + (size_t)KK * 3 * maxnv;                 // 3 maxnv
+  T* red = gx + 3 * maxnv;                             // 3 * NZ
+  T* cf = red + 3 * NZ;                                // maxnv * NZ * 2 (c1, c2 per centre)
+  int* cen = reinterpret_cast<int*>(cf + (size_t)2 * maxnv * NZ);  // maxnv
+  const T s2t = (T)s2, l2t = (T)l2, pt = (T)p;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int k0 = blockIdx.x * NZ;
+  const int nkt = min(NZ, nk - k0);
+  for (int e = tid; e < KK * NZ; e += 256) {
+    const int c = e / NZ, k = e - c * NZ;
+    Zs[e] = (k < nkt) ? Z[(size_t)(k0 + k) * KK + c] : T(0);
   }
-  for (int e = tid; e < nn * 3 * KK; e += kKT) {
-    const int q = e / (3 * KK), r = e - q * 3 * KK;
-    V[(size_t)(q + 1) * 3 * KK + r] = dB[(size_t)rev[p0 + q] * 3 * KK + r];
-  }
-  for (int v = tid; v < nv; v += kKT) cen[v] = v == 0 ? a : nbr_idx[p0 + v - 1];
-  __syncthreads();
-  for (int e = tid; e < nv * 3; e += kKT) {
-    const int v = e / 3;
-    const T* x = B + (size_t)cen[v] * KK;
-    const T* g = V + (size_t)e * KK;
-    T d = T(0);
-    for (int c = 0; c < KK; ++c) d = fma(g[c], x[c], d);
-    gx[e] = d;
-  }
-  __syncthreads();
-  const long long row = rowF[s] + 3LL * (a - atom_start[s]);
-  for (int k = tid; k < nk; k += kKT) {
-    T out[3] = {T(0), T(0), T(0)};
-    const T sz = szz[k];
-    for (int v0 = 0; v0 < nv; v0 += kVC) {
-      const int vn = min(kVC, nv - v0);
-      T dot[kVC][3];
-#pragma unroll
-      for (int v = 0; v < kVC; ++v) dot[v][0] = dot[v][1] = dot[v][2] = T(0);
-      for (int c = 0; c < KK; ++c) {
-        const T zc = Zt[(size_t)c * nk + k];
-#pragma unroll
-        for (int v = 0; v < kVC; ++v) {
-          if (v < vn) {
-            const T* g = V + (size_t)(v0 + v) * 3 * KK + c;
-            dot[v][0] = fma(g[0], zc, dot[v][0]);
-            dot[v][1] = fma(g[KK], zc, dot[v][1]);
-            dot[v][2] = fma(g[2 * KK], zc, dot[v][2]);
-          }
-        }
+  const int a_begin = blockIdx.y * atoms_per_cta, a_end = min(A, a_begin + atoms_per_cta);
+  for (int a = a_begin; a < a_end; ++a) {
+    const int s = atom_struct[a];
+    if (rowF[s] < 0) continue;  // uniform over the CTA
+    const int p0 = nbr_off[a], nn = nbr_off[a + 1] - p0;
+    const int nv = nn + 1, R = 3 * nv;
+    __syncthreads();  // previous atom's epilogue is done with Vt / red
+    // stage the rows: Vt[c][3 v + alpha]
+    for (int e = tid; e < 3 * KK; e += 256) {
+      const int al = e / KK, c = e - al * KK;
+      T acc = T(0);
+      for (int q = 0; q < nn; ++q) acc += dB[((size_t)(p0 + q) * 3 + al) * KK + c];
+      Vt[(size_t)c * R + al] = acc;
+    }
+    for (int e = tid; e < nn * 3 * KK; e += 256) {
+      const int q = e / (3 * KK), r = e - q * 3 * KK, al = r / KK, c = r - al * KK;
+      Vt[(size_t)c * R + 3 * (q + 1) + al] = dB[(size_t)rev[p0 + q] * 3 * KK + r];
+    }
+    for (int v = tid; v < nv; v += 256) cen[v] = v == 0 ? a : nbr_idx[p0 + v - 1];
+    for (int e = tid; e < 3 * NZ; e += 256) red[e] = T(0);
+    __syncthreads();
+    for (int r = tid; r < R; r += 256) {
+      const T* x = B + (size_t)cen[r / 3] * KK;
+      T d = T(0);
+      for (int c = 0; c < KK; ++c) d = fma(Vt[(size_t)c * R + r], x[c], d);
+      gx[r] = d;
+    }
+    // coefficient table of the centres for this tile of reference points
+    for (int e = tid; e < nv * NZ; e += 256) {
+      const int v = e / NZ, k = e - v * NZ;
+      T c1 = T(0), c2 = T(0);
+      if (k < nkt) {
+        const int ce = cen[v];
+        krr_c12<T>(F[(size_t)ce * nk + k0 + k], at + 4 * (size_t)ce, szz[k0 + k], s2t, l2t, pt, c1, c2);
       }
+      cf[2 * (size_t)e] = c1;
+      cf[2 * (size_t)e + 1] = c2;
+    }
+    __syncthreads();
+    T part[3][CJ];
 #pragma unroll
-      for (int v = 0; v < kVC; ++v) {
-        if (v < vn) {
-          const int vv = v0 + v, ce = cen[vv];
-          const T* atc = at + 4 * (size_t)ce;
-          if (atc[3] == T(0)) continue;  // a centre without neighbours has no kernel derivative
-          T kv, c1, c2;
-          krr_coef<T>(F[(size_t)ce * nk + k], atc, sz, s2, l2, p, kv, c1, c2);
-          const T sg = vv == 0 ? T(1) : T(-1);
+    for (int al = 0; al < 3; ++al)
 #pragma unroll
-          for (int al = 0; al < 3; ++al) out[al] += sg * (c1 * dot[v][al] - c2 * gx[vv * 3 + al]);
+      for (int j = 0; j < CJ; ++j) part[al][j] = T(0);
+    for (int rb = 0; rb < R; rb += 16 * RI) {
+      T acc[RI][CJ];
+#pragma unroll
+      for (int i = 0; i < RI; ++i)
+#pragma unroll
+        for (int j = 0; j < CJ; ++j) acc[i][j] = T(0);
+      for (int c = 0; c < KK; ++c) {
+        T vr[RI], zc[CJ];
+#pragma unroll
+        for (int i = 0; i < RI; ++i) {
+          const int r = rb + ty + 16 * i;
+          vr[i] = r < R ? Vt[(size_t)c * R + r] : T(0);
+        }
+#pragma unroll
+        for (int j = 0; j < CJ; ++j) zc[j] = Zs[(size_t)c * NZ + tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < RI; ++i)
+#pragma unroll
+          for (int j = 0; j < CJ; ++j) acc[i][j] = fma(vr[i], zc[j], acc[i][j]);
+      }
+      // epilogue of this row block
+#pragma unroll
+      for (int i = 0; i < RI; ++i) {
+        const int r = rb + ty + 16 * i;
+        if (r >= R) continue;
+        const int v = r / 3, al = r - 3 * v;
+        const T sg = v == 0 ? T(1) : T(-1);
+        const T g = gx[r];
+        const T* cv = cf + (size_t)2 * v * NZ;
+#pragma unroll
+        for (int j = 0; j < CJ; ++j) {
+          const int k = tx + 16 * j;
+          const T val = sg * (cv[2 * k] * acc[i][j] - cv[2 * k + 1] * g);
+          if (al == 0) part[0][j] += val;
+          else if (al == 1) part[1][j] += val;
+          else part[2][j] += val;
         }
       }
     }
 #pragma unroll
-    for (int al = 0; al < 3; ++al) X[(row + al) * ldx + c0 + k] = out[al];
+    for (int al = 0; al < 3; ++al)
+#pragma unroll
+      for (int j = 0; j < CJ; ++j)
+        if (part[al][j] != T(0)) atomicAdd(&red[al * NZ + tx + 16 * j], part[al][j]);
+    __syncthreads();
+    const long long row = rowF[s] + 3LL * (a - atom_start[s]);
+    for (int e = tid; e < 3 * nkt; e += 256) {
+      const int al = e / nkt, k = e - al * nkt;
+      X[(row + al) * ldx + c0 + k0 + k] = red[al * NZ + k];
+    }
   }
 }
 
-// per atom: T_s = sum_n g_{n, sa(s)} uu_{sb(s)} / r (6 x KK) and T_s . x (6)
+// per atom: T_s = sum_n g_{n, sa(s)} uu_{sb(s)} / r (6 x KK) and T_s . x (6); the pair factors
+// uu_b / r are formed once per pair
 template <typename T>
-__global__ void __launch_bounds__(128) k_krr_stress_atom(int KK, const int* __restrict__ atom_struct,
+__global__ void __launch_bounds__(128) k_krr_stress_atom(int KK, int maxnn, const int* __restrict__ atom_struct,
                                                          const int* __restrict__ small,
                                                          const int* __restrict__ nbr_off,
                                                          const double* __restrict__ nbr_u, const T* __restrict__ B,
                                                          const T* __restrict__ dB, double sign_big,
                                                          T* __restrict__ Ts, T* __restrict__ tx) {
+  extern __shared__ __align__(16) unsigned char ssm[];
+  T* fac = reinterpret_cast<T*>(ssm);  // maxnn * 3: uu_b / r
+  __shared__ double red[6][4];
   const int a = blockIdx.x;
   const int p0 = nbr_off[a], nn = nbr_off[a + 1] - p0;
   const bool sm = small[atom_struct[a]] != 0;
-  __shared__ double red[6][4];
+  for (int q = threadIdx.x; q < nn; q += blockDim.x) {
+    const double* u = nbr_u + 3 * (size_t)(p0 + q);
+    const double r = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    const double sg = sm ? 1.0 : -sign_big;
+    for (int b = 0; b < 3; ++b) fac[3 * q + b] = (T)(sg * u[b] / r);
+  }
+  __syncthreads();
   double part[6] = {0, 0, 0, 0, 0, 0};
   for (int e = threadIdx.x; e < 6 * KK; e += blockDim.x) {
     const int sidx = e / KK, c = e - sidx * KK;
-    double acc = 0.0;
-    for (int q = 0; q < nn; ++q) {
-      const double* u = nbr_u + 3 * (size_t)(p0 + q);
-      const double r = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
-      const double uu = sm ? u[c_sb[sidx]] : -sign_big * u[c_sb[sidx]];
-      acc += (double)dB[((size_t)(p0 + q) * 3 + c_sa[sidx]) * KK + c] * uu / r;
-    }
-    Ts[((size_t)a * 6 + sidx) * KK + c] = (T)acc;
-    part[sidx] += acc * (double)B[(size_t)a * KK + c];
+    const int sa = c_sa[sidx], sb = c_sb[sidx];
+    T acc = T(0);
+    for (int q = 0; q < nn; ++q) acc = fma(dB[((size_t)(p0 + q) * 3 + sa) * KK + c], fac[3 * q + sb], acc);
+    Ts[((size_t)a * 6 + sidx) * KK + c] = acc;
+    part[sidx] += (double)acc * (double)B[(size_t)a * KK + c];
   }
   for (int sidx = 0; sidx < 6; ++sidx) {
     double v = part[sidx];
@@ -245,53 +337,115 @@ __global__ void __launch_bounds__(128) k_krr_stress_atom(int KK, const int* __re
   }
 }
 
-// stress rows: grid (S, ceil(nk / kKT)); scale sign_stress * 3 / V
-template <typename T>
-__global__ void __launch_bounds__(kKT) k_krr_stress(int KK, int nk, const int* __restrict__ atom_start,
-                                                    const long long* __restrict__ rowS,
-                                                    const double* __restrict__ volume, double sign_stress,
-                                                    const T* __restrict__ Ts, const T* __restrict__ tx,
-                                                    const T* __restrict__ Zt, const T* __restrict__ F,
-                                                    const T* __restrict__ at, const T* __restrict__ szz, double s2,
-                                                    double l2, double p, int c0, int ldx, T* __restrict__ X) {
-  const int s = blockIdx.x;
-  const int k = blockIdx.y * kKT + threadIdx.x;
-  if (rowS[s] < 0 || k >= nk) return;
-  double acc[6] = {0, 0, 0, 0, 0, 0};
-  const T sz = szz[k];
-  for (int a = atom_start[s]; a < atom_start[s + 1]; ++a) {
-    const T* atc = at + 4 * (size_t)a;
-    if (atc[3] == T(0)) continue;
-    T kv, c1, c2;
-    krr_coef<T>(F[(size_t)a * nk + k], atc, sz, s2, l2, p, kv, c1, c2);
-    const T* Ta = Ts + (size_t)a * 6 * KK;
-    T d[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-    for (int c = 0; c < KK; ++c) {
-      const T zc = Zt[(size_t)c * nk + k];
+// Stress rows as a register-tiled product: CTA = (tile of NZ reference points, range of
+// structures); per structure its atoms' stress vectors T_{a,s} (6 per atom, centre a) are
+// staged 16 atoms (96 rows) at a time, dotted with the tile, turned into
+// c1(a, k) dot - c2(a, k) (T_{a,s} . x_a) and summed into the six stress rows.
+template <typename T, int NZ_>
+__global__ void __launch_bounds__(256) k_krr_stress_tiled(
+    int KK, int nk, int S, int structs_per_cta, const int* __restrict__ atom_start,
+    const long long* __restrict__ rowS, const double* __restrict__ volume, double sign_stress,
+    const T* __restrict__ Ts, const T* __restrict__ tx, const T* __restrict__ Z, const T* __restrict__ F,
+    const T* __restrict__ at, const T* __restrict__ szz, double s2, double l2, double p, int c0, int ldx,
+    T* __restrict__ X) {
+  using Tl = KrrTile<NZ_>;
+  constexpr int NZ = Tl::NZ, CJ = Tl::CJ, RI = Tl::RI;
+  constexpr int RB = 16 * RI;  // 96 rows = 16 atoms
+  extern __shared__ __align__(16) unsigned char ksm[];
+  T* Zs = reinterpret_cast<T*>(ksm);  // KK * NZ
+  T* Vt = Zs + (size_t)KK * NZ;       // KK * RB  [c][r]
+  T* red = Vt + (size_t)KK * RB;      // 6 * NZ
+  T* cf = red + 6 * NZ;               // 16 atoms * NZ * 2
+  const T s2t = (T)s2, l2t = (T)l2, pt = (T)p;
+  const int tid = threadIdx.x, txi = tid & 15, ty = tid >> 4;
+  const int k0 = blockIdx.x * NZ;
+  const int nkt = min(NZ, nk - k0);
+  for (int e = tid; e < KK * NZ; e += 256) {
+    const int c = e / NZ, k = e - c * NZ;
+    Zs[e] = (k < nkt) ? Z[(size_t)(k0 + k) * KK + c] : T(0);
+  }
+  const int s_begin = blockIdx.y * structs_per_cta, s_end = min(S, s_begin + structs_per_cta);
+  for (int s = s_begin; s < s_end; ++s) {
+    if (rowS[s] < 0) continue;
+    const int a0 = atom_start[s], na = atom_start[s + 1] - a0;
+    __syncthreads();
+    for (int e = tid; e < 6 * NZ; e += 256) red[e] = T(0);
+    T part[6][CJ];
 #pragma unroll
-      for (int sidx = 0; sidx < 6; ++sidx) d[sidx] = fma(Ta[sidx * KK + c], zc, d[sidx]);
+    for (int q = 0; q < 6; ++q)
+#pragma unroll
+      for (int j = 0; j < CJ; ++j) part[q][j] = T(0);
+    for (int ab = 0; ab < na; ab += 16) {
+      const int nrow = 6 * min(16, na - ab);
+      __syncthreads();
+      for (int e = tid; e < nrow * KK; e += 256) {
+        const int r = e / KK, c = e - r * KK;
+        Vt[(size_t)c * RB + r] = Ts[(size_t)(a0 + ab) * 6 * KK + e];
+      }
+      for (int e = tid; e < (nrow / 6) * NZ; e += 256) {
+        const int ai = e / NZ, k = e - ai * NZ;
+        T c1 = T(0), c2 = T(0);
+        if (k < nkt) {
+          const int a = a0 + ab + ai;
+          krr_c12<T>(F[(size_t)a * nk + k0 + k], at + 4 * (size_t)a, szz[k0 + k], s2t, l2t, pt, c1, c2);
+        }
+        cf[2 * (size_t)e] = c1;
+        cf[2 * (size_t)e + 1] = c2;
+      }
+      __syncthreads();
+      T acc[RI][CJ];
+#pragma unroll
+      for (int i = 0; i < RI; ++i)
+#pragma unroll
+        for (int j = 0; j < CJ; ++j) acc[i][j] = T(0);
+      for (int c = 0; c < KK; ++c) {
+        T vr[RI], zc[CJ];
+#pragma unroll
+        for (int i = 0; i < RI; ++i) {
+          const int r = ty + 16 * i;
+          vr[i] = r < nrow ? Vt[(size_t)c * RB + r] : T(0);
+        }
+#pragma unroll
+        for (int j = 0; j < CJ; ++j) zc[j] = Zs[(size_t)c * NZ + txi + 16 * j];
+#pragma unroll
+        for (int i = 0; i < RI; ++i)
+#pragma unroll
+          for (int j = 0; j < CJ; ++j) acc[i][j] = fma(vr[i], zc[j], acc[i][j]);
+      }
+#pragma unroll
+      for (int i = 0; i < RI; ++i) {
+        const int r = ty + 16 * i;
+        if (r >= nrow) continue;
+        const int ai = r / 6, a = a0 + ab + ai, sidx = r % 6;
+        const T tv = tx[6 * (size_t)a + sidx];
+        const T* cv = cf + (size_t)2 * ai * NZ;
+#pragma unroll
+        for (int j = 0; j < CJ; ++j) {
+          const int k = txi + 16 * j;
+          const T val = cv[2 * k] * acc[i][j] - cv[2 * k + 1] * tv;
+#pragma unroll
+          for (int q = 0; q < 6; ++q)
+            if (q == sidx) part[q][j] += val;
+        }
+      }
     }
 #pragma unroll
-    for (int sidx = 0; sidx < 6; ++sidx)
-      acc[sidx] += (double)c1 * (double)d[sidx] - (double)c2 * (double)tx[6 * (size_t)a + sidx];
-  }
-  const double sc = sign_stress * 3.0 / volume[s];
+    for (int q = 0; q < 6; ++q)
 #pragma unroll
-  for (int sidx = 0; sidx < 6; ++sidx) X[(rowS[s] + sidx) * ldx + c0 + k] = (T)(sc * acc[sidx]);
-}
-
-// Zt[c][k] = Z[k][c]
-template <typename T>
-__global__ void k_krr_transpose(int nk, int KK, const T* __restrict__ Z, T* __restrict__ Zt) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nk * KK) return;
-  const int k = e / KK, c = e - k * KK;
-  Zt[(size_t)c * nk + k] = Z[e];
+      for (int j = 0; j < CJ; ++j)
+        if (part[q][j] != T(0)) atomicAdd(&red[q * NZ + txi + 16 * j], part[q][j]);
+    __syncthreads();
+    const double sc = sign_stress * 3.0 / volume[s];
+    for (int e = tid; e < 6 * nkt; e += 256) {
+      const int q = e / nkt, k = e - q * nkt;
+      X[(rowS[s] + q) * ldx + c0 + k0 + k] = (T)(sc * (double)red[q * NZ + k]);
+    }
+  }
 }
 
 size_t krr_workspace_elems(int A, int nk, int KK) {
-  // at (4A), szz (nk), Zt (nk KK), F (A nk), Ts (6 A KK), tx (6A)
-  return 4 * (size_t)A + nk + (size_t)nk * KK + (size_t)A * nk + 6 * (size_t)A * KK + 6 * (size_t)A + 64;
+  // at (4A), szz (nk), F (A nk), Ts (6 A KK), tx (6A)
+  return 4 * (size_t)A + nk + (size_t)A * nk + 6 * (size_t)A * KK + 6 * (size_t)A + 64;
 }
 
 template <typename T>
@@ -303,29 +457,94 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
   const double l2 = 2.0 * length * length, s2 = sigma * sigma;
   T* at = ws;
   T* szz = at + 4 * (size_t)b.A;
-  T* Zt = szz + nk;
-  T* F = Zt + (size_t)nk * KK;
+  T* F = szz + nk;
   T* Ts = F + (size_t)b.A * nk;
   T* tx = Ts + 6 * (size_t)b.A * KK;
   k_krr_atom<T><<<(b.A + 255) / 256, 256, 0, st>>>(b.A, KK, Bq, b.nbr_off, s2, l2, power, at);
   k_krr_points<T><<<(nk + 255) / 256, 256, 0, st>>>(nk, KK, Z, s2, l2, power, szz);
-  k_krr_transpose<T><<<(nk * KK + 255) / 256, 256, 0, st>>>(nk, KK, Z, Zt);
   dim3 gx((nk + 63) / 64, (b.A + 63) / 64);
   k_krr_xz<T><<<gx, 256, 0, st>>>(b.A, nk, KK, Bq, Z, F);
   dim3 gs(b.S, (nk + kKT - 1) / kKT);
   k_krr_energy<T><<<gs, kKT, 0, st>>>(nk, b.atom_start, rows.rowE, F, at, szz, s2, l2, power, c0, rows.ldx, X);
-  // force rows: shared memory for the largest neighbour count
-  const int maxnn = b.maxnn;
-  const size_t smem = sizeof(T) * ((size_t)(maxnn + 1) * 3 * KK + 3 * (size_t)(maxnn + 1)) + sizeof(int) * (maxnn + 1) + 16;
-  cudaError_t e = cudaFuncSetAttribute(k_krr_force<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  k_krr_force<T><<<b.A, kKT, smem, st>>>(KK, nk, b.atom_struct, b.atom_start, rows.rowF, b.nbr_off, b.nbr_idx, rev,
-                                         Bq, dBq, Zt, F, at, szz, s2, l2, power, c0, rows.ldx, X);
-  k_krr_stress_atom<T><<<b.A, 128, 0, st>>>(KK, b.atom_struct, b.small, b.nbr_off, b.nbr_u, Bq, dBq, sign_big, Ts,
-                                            tx);
-  k_krr_stress<T><<<gs, kKT, 0, st>>>(KK, nk, b.atom_start, rows.rowS, b.volume, sign_stress, Ts, tx, Zt, F, at,
-                                      szz, s2, l2, power, c0, rows.ldx, X);
-  *launches = 8;
+  // force rows: register-tiled, reference-point tiles of NZ in shared memory (the widest tile
+  // whose working set fits)
+  {
+    static int optin = 0;
+    if (!optin) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    }
+    const int maxnv = b.maxnn + 1;
+    auto smem_for = [&](int nz) {
+      return sizeof(T) * ((size_t)KK * nz + (size_t)KK * 3 * maxnv + 3 * (size_t)maxnv + 3 * (size_t)nz +
+                          (size_t)2 * maxnv * nz) +
+             sizeof(int) * maxnv + 16;
+    };
+    // FP32 tiles up to 256 reference points, FP64 up to 64 (register budget of the 6 x NZ/16 tile)
+    int nz = 0;
+    for (int cand : {256, 128, 64, 32})
+      if ((sizeof(T) == 4 || cand <= 64) && smem_for(cand) <= (size_t)optin) {
+        nz = cand;
+        break;
+      }
+    if (!nz) return cudaErrorInvalidConfiguration;  // neighbour count too large for the tile
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int ntiles = (nk + nz - 1) / nz;
+    const int ranges = std::max(1, std::min(b.A, (2 * nsm + ntiles - 1) / ntiles * 4));
+    const int apc = (b.A + ranges - 1) / ranges;
+    dim3 g(ntiles, (b.A + apc - 1) / apc);
+    const size_t smem = smem_for(nz);
+    auto kern = nz == 64 ? k_krr_force_tiled<T, 64> : k_krr_force_tiled<T, 32>;
+    if constexpr (sizeof(T) == 4) {
+      if (nz == 256) kern = k_krr_force_tiled<T, 256>;
+      if (nz == 128) kern = k_krr_force_tiled<T, 128>;
+    }
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<g, 256, smem, st>>>(KK, nk, b.A, apc, maxnv, b.atom_struct, b.atom_start, rows.rowF, b.nbr_off,
+                               b.nbr_idx, rev, Bq, dBq, Z, F, at, szz, s2, l2, power, c0, rows.ldx, X);
+  }
+  k_krr_stress_atom<T><<<b.A, 128, sizeof(T) * 3 * (size_t)std::max(1, b.maxnn), st>>>(
+      KK, b.maxnn, b.atom_struct, b.small, b.nbr_off, b.nbr_u, Bq, dBq, sign_big, Ts, tx);
+  {
+    static int optin2 = 0;
+    if (!optin2) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&optin2, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    }
+    auto smem_for = [&](int nz) {
+      return sizeof(T) * ((size_t)KK * nz + (size_t)KK * 96 + 6 * (size_t)nz + (size_t)2 * 16 * nz) + 16;
+    };
+    int nz = 0;
+    for (int cand : {256, 128, 64, 32})
+      if ((sizeof(T) == 4 || cand <= 64) && smem_for(cand) <= (size_t)optin2) {
+        nz = cand;
+        break;
+      }
+    if (!nz) return cudaErrorInvalidConfiguration;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int ntiles = (nk + nz - 1) / nz;
+    const int ranges = std::max(1, std::min(b.S, (2 * nsm + ntiles - 1) / ntiles * 4));
+    const int spc = (b.S + ranges - 1) / ranges;
+    dim3 g(ntiles, (b.S + spc - 1) / spc);
+    const size_t smem = smem_for(nz);
+    auto kern = nz == 64 ? k_krr_stress_tiled<T, 64> : k_krr_stress_tiled<T, 32>;
+    if constexpr (sizeof(T) == 4) {
+      if (nz == 256) kern = k_krr_stress_tiled<T, 256>;
+      if (nz == 128) kern = k_krr_stress_tiled<T, 128>;
+    }
+    cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e2 != cudaSuccess) return e2;
+    kern<<<g, 256, smem, st>>>(KK, nk, b.S, spc, b.atom_start, rows.rowS, b.volume, sign_stress, Ts, tx, Z, F, at,
+                               szz, s2, l2, power, c0, rows.ldx, X);
+  }
+  *launches = 6;
   return cudaGetLastError();
 }
 

@@ -80,3 +80,16 @@ def test_batched_set_is_deterministic():
     b = synth.fe_bcc_batched(n_struct=5, seed=3)
     assert all(np.array_equal(x.positions, y.positions) for x, y in zip(a.structures, b.structures))
     assert all(16 <= x.nat <= 1024 for x in a.structures)
+
+
+def test_kernel_reference_selection_is_seeded_and_prefers_leverage():
+    from mld_gb300 import kernel_select
+    rng = np.random.default_rng(0)
+    B = rng.normal(size=(2000, 6))
+    B[:10] *= 50.0  # ten high-leverage atoms
+    a = kernel_select.select(B, 100, seed=7)
+    b = kernel_select.select(B, 100, seed=7)
+    assert np.array_equal(a, b) and len(a) == 100 and len(set(a.tolist())) == 100
+    lev, k = kernel_select.leverage_scores(B)
+    assert k == 6 and abs(lev.sum() - 1.0) < 1e-9
+    assert len(set(range(10)) & set(a.tolist())) >= 9
