@@ -47,11 +47,13 @@ def _args():
     p.add_argument("--plain-steps", type=int, default=2)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--workload", choices=["fe_linear", "hea_qnml", "hea_krr"], default="fe_linear",
+    p.add_argument("--workload", choices=["fe_linear", "hea_qnml", "hea_krr", "serve"], default="fe_linear",
                    help="fe_linear: batched linear Fe fit (default); hea_qnml: quadratic QNML fit of the "
                         "5-element alloy (4,000 x 250 atoms, weighted two-channel bispectrum); hea_krr: kernel "
                         "ridge regression of the same structures with 4,000 leverage-selected reference atoms")
     p.add_argument("--ref-points", type=int, default=4000, help="hea_krr: kernel reference points")
+    p.add_argument("--requests", type=int, default=300, help="serve: number of requests")
+    p.add_argument("--rate", type=float, default=100.0, help="serve: Poisson arrival rate [requests/s]")
     p.add_argument("--plain-structures", type=int, default=200,
                    help="hea_qnml: structures of the sample on which mixed and plain FP64 are compared")
     return p.parse_args()
@@ -380,6 +382,87 @@ def run_hea_krr(a):
     print(json.dumps(line))
 
 
+def run_serve(a):
+    """Serving loop with the fitted quadratic alloy potential: requests are random 5-element bcc
+    structures with atom counts log-uniform in 8..20,000 (sigma 0.1 A) arriving as a Poisson
+    stream at --rate; the server admits them into free evaluation slots by HBM budget
+    (continuous batching) and evaluates energy, forces and stress.  Reports p50/p99 latency
+    (submit to result) and atoms/s for the mixed and the plain FP64 method on the same request
+    stream, and the relative force difference between the two."""
+    from mld_gb300 import _lib, synth
+    rng = np.random.default_rng(20240607)
+    # the potential: QNML fit on a training set of the alloy (mixed method)
+    train = synth.hea_bcc_batched(n_struct=240, workers=min(16, os.cpu_count() or 1), seed=20240608)
+    c = _lib.default_config()
+    c.j_max, c.r_cut, c.lambda_krr, c.precision, c.mld_order = 4.0, 5.0, 1e-8, _lib.MIXED, 2
+    c.weighted, c.n_elements = 1, len(synth.HEA_ELEMENTS)
+    for i, wv in enumerate(synth.HEA_WEIGHTS):
+        c.weight_per_element[i] = wv
+    with _lib.Handle(c) as h:
+        nat, pos, cell, types = train.arrays()
+        E, F, S, has = train.labels()
+        h.set_structures(nat, pos, cell, types)
+        h.set_labels(E, F, S, has, np.ones((len(nat), 3)))
+        w, _ = h.fit()
+    n = a.requests
+    sizes = np.exp(rng.uniform(np.log(8), np.log(20000), size=n)).round().astype(int)
+    reqs = [synth.hea_request(rng, int(k)) for k in sizes]
+    arrivals = np.cumsum(rng.exponential(1.0 / a.rate, size=n))
+    total_atoms = int(sizes.sum())
+    out = {}
+    forces = {}
+    for name, prec in (("mixed", _lib.MIXED), ("plain_fp64", _lib.PLAIN_FP64)):
+        c.precision = prec
+        srv = _lib.Server(c, w, n_slots=3, max_batch_atoms=150000, hbm_fraction=0.5)
+        # warm-up: one request of each size class through every slot
+        for k in (16, 2000, 20000):
+            srv.wait(srv.submit(*(lambda r: (r.positions, r.cell, r.types))(synth.hea_request(rng, k))))
+        lat = np.zeros(n)
+        res = [None] * n
+        pending = {}
+        t0 = time.perf_counter()
+        i = done = 0
+        with Clocks() as clk:
+            while done < n:
+                now = time.perf_counter() - t0
+                while i < n and arrivals[i] <= now:
+                    r = reqs[i]
+                    pending[srv.submit(r.positions, r.cell, r.types)] = i
+                    i += 1
+                srv.progress()
+                for t in list(pending):
+                    got = srv.result(t)
+                    if got is not None:
+                        j = pending.pop(t)
+                        res[j] = got[1]
+                        lat[j] = got[3]
+                        done += 1
+                if not pending and i < n:
+                    time.sleep(max(0.0, min(0.002, arrivals[i] - (time.perf_counter() - t0))))
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        forces[name] = res
+        out[name] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                     "mean_ms": float(lat.mean()), "atoms_per_s": total_atoms / wall, "wall_s": wall,
+                     "batches": st["batches"], "clocks": clk.summary()}
+    ferr = max(float(np.abs(fm - fp).max() / max(np.abs(fp).max(), 1e-300))
+               for fm, fp in zip(forces["mixed"], forces["plain_fp64"]))
+    mx = out["mixed"]
+    line = {
+        "metric": "serving atoms/s and p99 latency (continuous batching, fitted QNML alloy potential)",
+        "value": mx["atoms_per_s"], "unit": "atoms/s", "n_gpus": 1, "steps": n, "warmup": 3,
+        "ms_per_step": mx["mean_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 descriptors/rows (mixed) vs fp64 (plain)", "data": "synthetic",
+        "config": {"workload": "hea_serve_poisson_8to20000_atoms_qnml_weighted_jmax4", "requests": n,
+                   "rate_per_s": a.rate, "atoms": total_atoms, "slots": 3, "max_batch_atoms": 150000,
+                   "hbm_fraction": 0.5, "parallelism": "single"},
+        "p50_ms": mx["p50_ms"], "p99_ms": mx["p99_ms"], "mixed": mx, "plain_fp64": out["plain_fp64"],
+        "force_rel_diff_mixed_vs_plain": ferr,
+    }
+    print(json.dumps(line))
+
+
 def cpu_sample(ds, target_s=15.0, threads=None):
     """Time the oracle (CPU restatement of the reference) on a bounded sample of the same set:
     neighbours + descriptors + rows in C (OpenMP over structures), Gram + gelsd in NumPy/LAPACK."""
@@ -454,9 +537,9 @@ def main():
         print(json.dumps(line))
         return
 
-    if a.workload in ("hea_qnml", "hea_krr"):
+    if a.workload in ("hea_qnml", "hea_krr", "serve"):
         if rank == 0:
-            run_hea(a) if a.workload == "hea_qnml" else run_hea_krr(a)
+            {"hea_qnml": run_hea, "hea_krr": run_hea_krr, "serve": run_serve}[a.workload](a)
         return
     if world > 1:
         import torch.distributed as dist

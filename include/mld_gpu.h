@@ -192,6 +192,33 @@ int mld_gpu_set_kernel_points(mld_gpu_handle* h, int nk, const double* z_raw);
 int mld_gpu_solve_info(const mld_gpu_handle* h, int* pcg_iterations /*[2]*/, double* pcg_residual /*[2]*/,
                        double* precond_shift /*[2]*/, int* chol_retries);
 
+/* ---------------------------------------------------------------------------------------
+ * Serving loop (evaluation with a fitted potential under continuous batching; the evaluation
+ * side of mld.F90:1579-1867 as driven by mld_md_driver.F90:324-375,579-651).
+ * A server holds n_slots evaluation slots (one stream and one set of device buffers each).
+ * Requests (one structure each) are queued by submit and evaluated by progress(), which
+ * retires finished batches and fills idle slots with queued requests in arrival order while a
+ * batch stays within its share of hbm_fraction * (free HBM at creation) and max_batch_atoms.
+ * w_params: fitted weights in the reference's full layout (dim_design_line of cfg). */
+typedef struct mld_gpu_server mld_gpu_server;
+int mld_gpu_server_create(const mld_gpu_config* cfg, const double* w_params, int n_slots, long long max_batch_atoms,
+                          double hbm_fraction, mld_gpu_server** out);
+void mld_gpu_server_destroy(mld_gpu_server* s);
+const char* mld_gpu_server_last_error(const mld_gpu_server* s);
+/* copies the structure (positions 3*nat, cell 3x3 rows = lattice vectors, types) */
+int mld_gpu_server_submit(mld_gpu_server* s, int nat, const double* pos, const double* cell, const int* types,
+                          long long* ticket);
+/* non-blocking: retire finished batches, launch queued requests into idle slots */
+int mld_gpu_server_progress(mld_gpu_server* s, int* n_busy_slots, int* n_queued);
+/* *ready = 1 and the results (E, F[3*nat], S[6], latency from submit to completion) once the
+ * request is done; the ticket is then released.  A failed request returns its error code. */
+int mld_gpu_server_result(mld_gpu_server* s, long long ticket, double* E, double* F, double* S, double* latency_ms,
+                          int* ready);
+/* progress() until the request is done or timeout_ms (> 0) passes (MLD_ERR_TIMEOUT) */
+int mld_gpu_server_wait(mld_gpu_server* s, long long ticket, double* E, double* F, double* S, double* latency_ms,
+                        double timeout_ms);
+int mld_gpu_server_stats(const mld_gpu_server* s, long long* batches, long long* atoms_done, double* budget_bytes);
+
 /* Weighted Gram matrix and right-hand side of caller-owned DEVICE rows, the per-block
  * accumulation of the online fit (gram%accumulate, module_online_fit.F90:49-53,138-265):
  *   G   (D x D, row-major FP64, device)   = sum_r w[r] x_r x_r^T

@@ -28,7 +28,9 @@ EXPORTED = ["mld_gpu_config_defaults", "mld_gpu_create", "mld_gpu_destroy", "mld
             "mld_gpu_solve", "mld_gpu_fit", "mld_gpu_predict", "mld_gpu_synchronize", "mld_gpu_set_profiling",
             "mld_gpu_profile", "mld_gpu_timer_start", "mld_gpu_timer_stop", "mld_gpu_work_counts",
             "mld_gpu_peak_flops", "mld_gpu_descriptors_noalloc", "mld_gpu_solve_info", "mld_gpu_gram_rows",
-            "mld_gpu_set_kernel_points"]
+            "mld_gpu_set_kernel_points", "mld_gpu_server_create", "mld_gpu_server_destroy",
+            "mld_gpu_server_last_error", "mld_gpu_server_submit", "mld_gpu_server_progress",
+            "mld_gpu_server_result", "mld_gpu_server_wait", "mld_gpu_server_stats"]
 NPHASE = 6
 PHASES = ["neighbours", "rows", "descriptors", "gram", "solve", "predict"]
 
@@ -297,3 +299,88 @@ def gram_rows(method: int, X_ptr: int, x_is_fp32: bool, M: int, D: int, ldx: int
                              512)
     if rc != 0:
         raise MldError(rc, err.value.decode(errors="replace"))
+
+
+class Server:
+    """Serving loop over the C ABI: submit structures, progress(), collect results."""
+
+    def __init__(self, cfg: MldGpuConfig, w_params: np.ndarray, n_slots: int = 2, max_batch_atoms: int = 200000,
+                 hbm_fraction: float = 0.5):
+        L = load()
+        L.mld_gpu_server_last_error.restype = ctypes.c_char_p
+        L.mld_gpu_server_last_error.argtypes = [ctypes.c_void_p]
+        L.mld_gpu_server_destroy.restype = None
+        L.mld_gpu_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double]
+        L.mld_gpu_server_result.argtypes = [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.mld_gpu_server_create.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong,
+                                            ctypes.c_double, ctypes.c_void_p]
+        self._L = L
+        self._s = ctypes.c_void_p()
+        w = np.ascontiguousarray(w_params, dtype=np.float64)
+        rc = L.mld_gpu_server_create(ctypes.byref(cfg), _p(w), int(n_slots), int(max_batch_atoms), float(hbm_fraction),
+                                     ctypes.byref(self._s))
+        if rc != MLD_OK:
+            raise MldError(rc, "mld_gpu_server_create failed")
+        self._nat = {}
+
+    def _check(self, rc):
+        if rc != MLD_OK:
+            raise MldError(rc, (self._L.mld_gpu_server_last_error(self._s) or b"").decode())
+
+    def submit(self, pos, cell, types) -> int:
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        cell = np.ascontiguousarray(cell, dtype=np.float64).reshape(-1)
+        types = np.ascontiguousarray(types, dtype=np.int32).reshape(-1)
+        t = ctypes.c_longlong()
+        self._check(self._L.mld_gpu_server_submit(self._s, int(types.shape[0]), _p(pos), _p(cell), _p(types),
+                                                  ctypes.byref(t)))
+        self._nat[t.value] = int(types.shape[0])
+        return t.value
+
+    def progress(self):
+        b, q = ctypes.c_int(), ctypes.c_int()
+        self._check(self._L.mld_gpu_server_progress(self._s, ctypes.byref(b), ctypes.byref(q)))
+        return b.value, q.value
+
+    def result(self, ticket: int):
+        nat = self._nat[ticket]
+        E, F, S = ctypes.c_double(), np.zeros((nat, 3)), np.zeros(6)
+        lat, ready = ctypes.c_double(), ctypes.c_int()
+        self._check(self._L.mld_gpu_server_result(self._s, ctypes.c_longlong(ticket), ctypes.byref(E), _p(F), _p(S),
+                                                  ctypes.byref(lat), ctypes.byref(ready)))
+        if not ready.value:
+            return None
+        del self._nat[ticket]
+        return E.value, F, S, lat.value
+
+    def wait(self, ticket: int, timeout_ms: float = 600000.0):
+        nat = self._nat[ticket]
+        E, F, S, lat = ctypes.c_double(), np.zeros((nat, 3)), np.zeros(6), ctypes.c_double()
+        self._check(self._L.mld_gpu_server_wait(self._s, ctypes.c_longlong(ticket), ctypes.byref(E), _p(F), _p(S),
+                                                ctypes.byref(lat), float(timeout_ms)))
+        del self._nat[ticket]
+        return E.value, F, S, lat.value
+
+    def stats(self):
+        b, a, bud = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_double()
+        self._check(self._L.mld_gpu_server_stats(self._s, ctypes.byref(b), ctypes.byref(a), ctypes.byref(bud)))
+        return {"batches": b.value, "atoms_done": a.value, "budget_bytes": bud.value}
+
+    def close(self):
+        if self._s:
+            self._L.mld_gpu_server_destroy(self._s)
+            self._s = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

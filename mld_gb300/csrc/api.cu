@@ -75,6 +75,11 @@ struct mld_gpu_handle {
   long long launches[MLD_NPHASE] = {0};
   long long calls[MLD_NPHASE] = {0};
 
+  // serving: row layout of the last launched batch and its pinned prediction buffer
+  RowLayout serve_rows;
+  double* pinned = nullptr;
+  size_t pinned_cap = 0;
+
   // device properties and the last mixed-method solve
   int nsm = 0;
   int pcg_iters[2] = {0, 0};
@@ -91,7 +96,7 @@ struct mld_gpu_handle {
     B_ROWE, B_ROWF, B_ROWS, B_X, B_Y, B_WROW, B_KIND,
     B_G, B_H, B_W, B_EVALS, B_INFO, B_SQ, B_PRED, B_BOUT, B_DBOUT,
     B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
-    B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV, B_KZD, B_KZF, B_KWS,
+    B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV, B_KZD, B_KZF, B_KWS, B_WSERVE,
     B_COUNT
   };
   static_assert(B_COUNT <= 64, "buffer table too small");
@@ -868,6 +873,7 @@ void mld_gpu_destroy(mld_gpu_handle* h) {
   for (auto& bf : h->bufs)
     if (bf.p) cudaFree(bf.p);
   for (void* p : h->owned) cudaFree(p);
+  if (h->pinned) cudaFreeHost(h->pinned);
   for (auto& e : h->evpool)
     if (e) cudaEventDestroy(e);
   for (auto& e : h->tev)
@@ -1227,6 +1233,85 @@ int mld_gpu_predict(mld_gpu_handle* h, const double* w_params, double* E, double
   }
   return MLD_OK;
 }
+
+}  // extern "C"
+
+namespace mld {
+
+// Asynchronous halves of mld_gpu_predict for the serving loop: predict_launch stages nothing on
+// the host side but the neighbour counts (one stream synchronisation), queues the descriptor,
+// design-row and prediction kernels and the copy of the predictions into a pinned host buffer
+// on the handle's stream, and records `done`; predict_collect scatters the predictions of
+// structure s into its energy / forces / stress once `done` has completed.
+int predict_launch(mld_gpu_handle* h, const double* w_dev, cudaEvent_t done, double** pinned_out) {
+  int rc = build_neighbours(h);
+  if (rc) return rc;
+  std::vector<int> all(3 * (size_t)h->S, 1);
+  h->serve_rows = make_layout(h, all, true);
+  const RowLayout& L = h->serve_rows;
+  CK(ensure(h, mld_gpu_handle::B_PRED, sizeof(double) * std::max<long long>(L.M, 1)));
+  double* pred = bp_<double>(h, mld_gpu_handle::B_PRED);
+  if (h->mixed) {
+    float* X = nullptr;
+    rc = run_rows<float>(h, L, false, &X);
+    if (rc) return rc;
+    CK(launch_predict_sq<float>(X, h->ldx, w_dev, L.M, h->D, pred, nullptr, nullptr, nullptr, h->st));
+  } else {
+    double* X = nullptr;
+    rc = run_rows<double>(h, L, false, &X);
+    if (rc) return rc;
+    CK(launch_predict_sq<double>(X, h->ldx, w_dev, L.M, h->D, pred, nullptr, nullptr, nullptr, h->st));
+  }
+  if ((size_t)L.M > h->pinned_cap) {
+    if (h->pinned) cudaFreeHost(h->pinned);
+    h->pinned = nullptr;
+    h->pinned_cap = 0;
+    CK(cudaMallocHost(&h->pinned, sizeof(double) * (size_t)std::max<long long>(L.M, 1)));
+    h->pinned_cap = (size_t)std::max<long long>(L.M, 1);
+  }
+  CK(cudaMemcpyAsync(h->pinned, pred, sizeof(double) * L.M, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaEventRecord(done, h->st));
+  *pinned_out = h->pinned;
+  return MLD_OK;
+}
+
+void predict_collect(const mld_gpu_handle* h, int s, double* E, double* F, double* Sout) {
+  const RowLayout& L = h->serve_rows;
+  const double* hp = h->pinned;
+  const int a0 = h->h_atom_start[s], nat = h->h_atom_start[s + 1] - a0;
+  (void)a0;
+  if (E) *E = hp[L.rowE[s]];
+  if (F && L.rowF[s] >= 0)
+    for (int i = 0; i < 3 * nat; ++i) F[i] = hp[L.rowF[s] + i];
+  if (Sout && L.rowS[s] >= 0)
+    for (int k = 0; k < 6; ++k) Sout[k] = hp[L.rowS[s] + k];
+}
+
+// device copy of fitted weights (reference full layout) in the handle's working layout
+int upload_weights(mld_gpu_handle* h, const double* w_full, double** w_dev) {
+  std::vector<double> wd(h->D);
+  if (h->quad) full_to_dedup(h, w_full, wd.data());
+  else std::copy(w_full, w_full + h->D, wd.begin());
+  CK(ensure(h, mld_gpu_handle::B_WSERVE, sizeof(double) * h->D));
+  CK(cudaMemcpyAsync(bp_<double>(h, mld_gpu_handle::B_WSERVE), wd.data(), sizeof(double) * h->D,
+                     cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  *w_dev = bp_<double>(h, mld_gpu_handle::B_WSERVE);
+  return MLD_OK;
+}
+
+cudaStream_t handle_stream(const mld_gpu_handle* h) { return h->st; }
+int handle_dims(const mld_gpu_handle* h, int* D, int* ldx, int* KK, int* nch) {
+  *D = h->D;
+  *ldx = h->ldx;
+  *KK = h->KK;
+  *nch = h->nch;
+  return MLD_OK;
+}
+
+}  // namespace mld
+
+extern "C" {
 
 int mld_gpu_set_profiling(mld_gpu_handle* h, int on) {
   if (!h) return MLD_ERR_INVALID;

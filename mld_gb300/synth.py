@@ -236,3 +236,15 @@ def hea_bcc_batched(n_struct: int = 4000, reps: int = 5, sigma: float = 0.1, rcu
     else:
         out = [_hea_one(j) for j in jobs]
     return Dataset(out, rcut, f"hea_bcc_{n_struct}")
+
+
+def hea_request(rng: np.random.Generator, n_atoms: int, sigma: float = 0.1) -> Structure:
+    """One serving request: a random 5-element bcc alloy cell of n_atoms atoms (a near-cubic
+    supercell trimmed to size), Gaussian noise sigma; no labels."""
+    n, m, k = _dims_for(n_atoms)
+    pos, cell = bcc(n, m, k, HEA_A)
+    keep = np.sort(rng.choice(pos.shape[0], size=n_atoms, replace=False))
+    pos = pos[keep] + rng.normal(0.0, sigma, size=(n_atoms, 3))
+    types = rng.integers(0, len(HEA_ELEMENTS), size=n_atoms).astype(np.int32)
+    return Structure(cell=cell, positions=pos, types=types, elements=list(HEA_ELEMENTS),
+                     energies=np.zeros(3), forces=np.zeros((n_atoms, 3)), stress=np.zeros(6), name="req")
