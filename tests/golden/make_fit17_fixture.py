@@ -3,7 +3,7 @@
 fit17 (tests/train_tests/fit17 in the MILADY project) computes bispectrum-SO(4) descriptors
 (descriptor_type=9, j_max=4, r_cut=4.7, unweighted, tungsten) for 20 POSCAR files selected by
 its db_model.in and writes the reference's per-atom B to REF/descDB/<name>.eml (column 1 = the
-species tag, columns 2..56 = B_1..B_55, format es30.18e3).  This script packs, per structure,
+1-based atom index, columns 2..56 = B_1..B_55, format es30.18e3).  This script packs, per structure,
 the cell, positions, types and the reference's B into one compressed fixture so the tests can
 run where the MILADY sources are absent.
 
