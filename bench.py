@@ -569,7 +569,7 @@ def main():
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "fp32 descriptors/rows + fp64 gram/solve",
+        "dtype": "fp32 descriptors/rows + bf16x3 tensor-core Gram (fp32 acc) + fp64 Cholesky / double-fp32 CG",
         "data": "synthetic",
         "config": {"workload": "fe_bcc_2000_struct_16to1024_atoms_linear_jmax4", "structures": len(res["ds"].structures),
                    "atoms": A, "design_rows": M, "dim_design_line": 56, "r_cut": RCUT, "lambda_krr": LAMBDA,

@@ -15,7 +15,7 @@ from typing import Dict, List, Optional
 
 import numpy as np
 
-from . import _lib, db_model, namelist, poscar
+from . import _lib, db_model, elements, namelist, poscar
 
 
 @dataclasses.dataclass
@@ -43,12 +43,8 @@ def _config(nl: dict, precision: int) -> _lib.MldGpuConfig:
     c.n_elements = len(els)
     w1 = namelist.element_weights(nl, "weight_per_element")
     w2 = namelist.element_weights(nl, "weight_per_element_3ch")
-    if nl.get("weighted_auto"):
-        # fix_poscar_weights (build_subdata.F90:2953-2999): channel weights renormalised
-        r1 = float(np.sqrt(np.mean(np.square(w1)))) if w1 else 1.0
-        r2 = float(np.mean(w2)) if w2 else 1.0
-        w1 = [x / r1 for x in w1]
-        w2 = [x / r2 for x in w2]
+    if nl.get("weighted_auto") and c.weighted:
+        w1, w2 = (list(x) for x in elements.auto_channel_weights(els))
     for i, x in enumerate(w1[: _lib.MAX_ELEMENTS]):
         c.weight_per_element[i] = x
     for i, x in enumerate(w2[: _lib.MAX_ELEMENTS]):

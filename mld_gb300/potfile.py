@@ -23,12 +23,8 @@ from typing import Dict, Optional, Sequence, Tuple
 
 import numpy as np
 
-# atomic weights as the reference's periodic table holds them (ml_in_ndm_module.F90:1675-2343)
-ATOMIC_MASS = {
-    "H": 1.008, "Li": 6.941, "C": 12.011, "Al": 26.982, "Si": 28.086, "Ti": 47.867, "V": 50.942,
-    "Cr": 51.996, "Mn": 54.938, "Fe": 55.845, "Co": 58.933, "Ni": 58.693, "Cu": 63.546, "Zr": 91.224,
-    "Nb": 92.906, "Mo": 95.940, "Hf": 178.490, "Ta": 180.948, "W": 183.840, "Re": 186.207,
-}
+from . import elements as elements_table
+
 
 
 def _es(v: float, width: int, digits: int, expd: int = 3) -> str:
@@ -105,7 +101,7 @@ def write_lammps_pot(path: str, w: Sequence[float], elements: Sequence[str], *, 
     wt = list(weights) if weights is not None else [1.0] * ne
     w3 = list(weights_3ch) if weights_3ch is not None else [1.0] * ne
     er = list(ref_energy) if ref_energy is not None else [0.0] * ne
-    ms = list(masses) if masses is not None else [ATOMIC_MASS[e] for e in elements]
+    ms = list(masses) if masses is not None else [elements_table.mass(e) for e in elements]
     with open(path, "w") as f:
         for c in _LAMMPS_COMMENTS:
             f.write(c + "\n")

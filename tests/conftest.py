@@ -19,6 +19,12 @@ def fit17():
 
 
 @pytest.fixture(scope="session")
+def fit19():
+    import numpy as np
+    return np.load(os.path.join(ROOT, "tests", "golden", "fit19_bso4_3ch.npz"))
+
+
+@pytest.fixture(scope="session")
 def lib():
     from mld_gb300 import build, _lib
     build.build()

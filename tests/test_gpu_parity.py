@@ -56,6 +56,30 @@ def test_fit17_descriptors(lib, fit17, precision, tol):
     h.close()
 
 
+@pytest.mark.parametrize("precision,tol", [(0, TOL64), (1, TOL32)])
+def test_fit19_three_channel_descriptors(lib, fit19, precision, tol):
+    """Weighted 3-channel descriptors (weighted_auto channel weights) against fit19's golden B."""
+    from mld_gb300 import _lib, elements
+    els = [str(e) for e in fit19["elements"]]
+    w2, w3 = elements.auto_channel_weights(els)
+    c = _lib.default_config()
+    c.j_max, c.r_cut, c.precision, c.n_elements = 4.0, 4.7, precision, len(els)
+    c.weighted, c.weighted_3ch = 1, 1
+    for i in range(len(els)):
+        c.weight_per_element[i] = w2[i]
+        c.weight_per_element_3ch[i] = w3[i]
+    idx = range(len(fit19["names"]))
+    nat = [fit19[f"pos_{i}"].shape[0] for i in idx]
+    with _lib.Handle(c) as h:
+        h.set_structures(nat, np.concatenate([fit19[f"pos_{i}"] for i in idx]),
+                         np.stack([fit19[f"cell_{i}"] for i in idx]),
+                         np.concatenate([fit19[f"types_{i}"] for i in idx]))
+        B, _ = h.descriptors()
+    ref = np.concatenate([fit19[f"B_{i}"] for i in idx])
+    assert B.shape == ref.shape == (sum(nat), 165)
+    assert _rel(B, ref) < tol
+
+
 def _small_dataset(seed=5):
     from mld_gb300 import synth
     rng = np.random.default_rng(seed)

@@ -44,6 +44,27 @@ def _energy_row_sum(pos, cell, types):
     return oracle.bispectrum(pos, cell, types, 4.7, 4.0, want_deriv=False)["B"].sum(0)
 
 
+def test_fit19_golden_three_channel_descriptors(fit19):
+    """The oracle reproduces MILADY's fit19 REF/descDB (Ta-Ti-V-W, weighted + weighted_3ch with
+    weighted_auto): channel 2 weights Z / rms(Z), channel 3 (m^2 + r_cov^2) / mean, masses at the
+    reference's single precision."""
+    from mld_gb300 import elements
+    els = [str(e) for e in fit19["elements"]]
+    w2, w3 = elements.auto_channel_weights(els)
+    chw = np.stack([np.ones(len(els)), w2, w3])
+    for i in range(len(fit19["names"])):
+        d = oracle.bispectrum(fit19[f"pos_{i}"], fit19[f"cell_{i}"], fit19[f"types_{i}"], 4.7, 4.0,
+                              channel_weights=chw, want_deriv=False)
+        ref = fit19[f"B_{i}"]
+        assert d["B"].shape == ref.shape
+        assert np.abs(d["B"] - ref).max() / np.abs(ref).max() < 1e-13
+    # with the masses in double precision channel 3 misses by ~1e-8: the binary32 rounding is real
+    m64 = np.array([elements.TABLE[e][1] for e in els])
+    rc = np.array([elements.covalent_radius(e) for e in els])
+    w3_64 = (m64 ** 2 + rc ** 2) / np.mean(m64 ** 2 + rc ** 2)
+    assert 1e-9 < np.abs(w3_64 - w3).max() < 1e-6
+
+
 @pytest.mark.parametrize("idx", [2, 9])
 def test_force_rows_are_negative_gradient(fit17, idx):
     pos = fit17[f"pos_{idx}"].copy()
