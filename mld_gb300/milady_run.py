@@ -2,10 +2,19 @@
 
 Mirrors the documented surface ``milady_run(input, db_model, DB, workdir, output, check)`` of the
 reference's Python wrapper (README of the MILADY project): it reads the ``&input_ml`` namelist,
-``db_model.in`` and the POSCAR database, fits with ``mld_gpu_fit`` and writes the predictions of
-the training and test configurations in the reference's ``train_*.out`` / ``test_*.out`` layout
-(``es20.10`` predicted and reference values, class and file name; mld.F90:944-1020).
-Only descriptor_type = 9 with ml_type = 0 and mld_order = 1 is supported by this build.
+``db_model.in`` and the POSCAR database, then for descriptor_type = 9
+
+* ml_type = -1 writes the descriptors of every selected configuration to
+  ``desc<db_path><class>_<klm>_<n>.eml`` (read_write_descriptors.F90:120-200);
+* ml_type = 0 (mld_order 1 linear, 2 quadratic QNML) or 1 (kernel ridge, polynomial kernel) fits
+  with ``mld_gpu_fit``, writes ``<desc>_<model>_params.pot`` and ``lammps_<...>`` (module_write_
+  parameters.F90:762-1530) and the predictions of the training and test configurations in the
+  reference's ``train_*.out`` / ``test_*.out`` layout (``es20.10`` predicted and reference values,
+  class and file name; mld.F90:944-1020).
+
+The kernel model reads its reference points from ``kernel_matrix.dat`` in ``workdir`` when the
+file exists (compute_kernel.F90:1106-1160); otherwise it selects ``np_kernel_ref +
+np_kernel_full`` training atoms by leverage score (mld_gb300.kernel_select) and writes the file.
 """
 from __future__ import annotations
 
@@ -15,13 +24,13 @@ from typing import Dict, List, Optional
 
 import numpy as np
 
-from . import _lib, db_model, elements, namelist, poscar
+from . import _lib, db_model, elements, kernel_select, namelist, poscar, potfile
 
 
 @dataclasses.dataclass
 class FitResult:
-    w: np.ndarray
-    rmse_train: np.ndarray
+    w: Optional[np.ndarray]
+    rmse_train: Optional[np.ndarray]
     rmse_test: Optional[np.ndarray]
     n_train: int
     n_test: int
@@ -31,14 +40,19 @@ class FitResult:
 def _config(nl: dict, precision: int) -> _lib.MldGpuConfig:
     if int(nl["descriptor_type"]) != 9:
         raise ValueError("this build implements descriptor_type = 9 (bispectrum SO(4)) only")
-    if int(nl["ml_type"]) != 0 or int(nl["mld_order"]) != 1:
-        raise ValueError("this build implements ml_type = 0 with mld_order = 1")
+    ml_type, order = int(nl["ml_type"]), int(nl["mld_order"])
+    if ml_type not in (-1, 0, 1) or (ml_type == 0 and order not in (1, 2)):
+        raise ValueError("this build implements ml_type -1, 0 (mld_order 1 or 2) and 1 (kernel ridge)")
+    if ml_type == 1 and int(nl["kernel_type"]) != potfile.KERNEL_PO:
+        raise ValueError("the kernel model implements kernel_type = 4 (polynomial) only")
     c = _lib.default_config()
+    c.ml_type = max(ml_type, 0)
+    c.mld_order = order if ml_type == 0 else 1
     c.j_max = float(nl["j_max"])
     c.r_cut = float(nl["r_cut"])
     c.inv_r0_input = float(nl["inv_r0_input"])
     c.weighted = int(bool(nl["weighted"]))
-    c.weighted_3ch = int(bool(nl["weighted_3ch"]))
+    c.weighted_3ch = int(bool(nl["weighted_3ch"])) if c.weighted else 0
     els = namelist.elements(nl) or ["X"]
     c.n_elements = len(els)
     w1 = namelist.element_weights(nl, "weight_per_element")
@@ -49,11 +63,15 @@ def _config(nl: dict, precision: int) -> _lib.MldGpuConfig:
         c.weight_per_element[i] = x
     for i, x in enumerate(w2[: _lib.MAX_ELEMENTS]):
         c.weight_per_element_3ch[i] = x
-    c.desc_forces = int(bool(nl["desc_forces"]))
+    c.desc_forces = int(bool(nl["desc_forces"])) or int(ml_type >= 0)
     c.lambda_krr = float(nl["lambda_krr"])
     c.svd_rcond = float(nl["svd_rcond"])
     c.sign_stress = float(nl["sign_stress"])
     c.sign_stress_big_box = float(nl["sign_stress_big_box"])
+    c.kernel_type = int(nl["kernel_type"])
+    c.kernel_power = float(nl["kernel_power"])
+    c.length_kernel = float(nl["length_kernel"])
+    c.sigma_kernel = float(nl["sigma_kernel"])
     c.precision = precision
     return c
 
@@ -85,6 +103,31 @@ def _write(path: str, rows: List[tuple]):
             fh.write("%20.10E%20.10E %s %s\n" % (pred, ref, cls, name))
 
 
+def _stem(c: db_model.Config) -> str:
+    return os.path.splitext(os.path.basename(c.filename))[0]
+
+
+def _kernel_points(h: _lib.Handle, nl: dict, train: List[db_model.Config], nat: np.ndarray, workdir: str,
+                   files: Dict[str, str]) -> np.ndarray:
+    path = os.path.join(workdir, "kernel_matrix.dat")
+    if os.path.exists(path):
+        return potfile.read_kernel_matrix(path)
+    B, _ = h.descriptors()
+    nk = min(int(nl.get("np_kernel_ref", 200)) + int(nl.get("np_kernel_full", 800)), B.shape[0])
+    idx = kernel_select.select(B, nk, seed=int(nl["seed"]))
+    starts = np.concatenate([[0], np.cumsum(nat)])
+    conf = np.searchsorted(starts, idx, side="right") - 1
+    potfile.write_kernel_matrix(path, B[idx], conf + 1, idx - starts[conf] + 1, [_stem(train[i]) for i in conf])
+    files["kernel_matrix"] = path
+    return potfile.read_kernel_matrix(path)  # the fit uses the points as written (10 digits), as the reference does
+
+
+def _standardise(z: np.ndarray) -> np.ndarray:
+    """(z - mean) / population std per component (compute_kernel.F90:1170-1199)."""
+    d = z - z.mean(axis=0)
+    return d / np.sqrt((d * d).mean(axis=0))
+
+
 def milady_run(input: str, db_model_file: str = "db_model.in", DB: str = "DB/", workdir: str = ".",
                output: str = "out", check: bool = False, precision: int = _lib.MIXED) -> FitResult:
     nl = namelist.read_input_ml(input)
@@ -93,15 +136,50 @@ def milady_run(input: str, db_model_file: str = "db_model.in", DB: str = "DB/", 
                            factors=(float(nl["factor_energy_error"]), float(nl["factor_force_error"]),
                                     float(nl["factor_stress_error"])))
     els = namelist.elements(nl)
+    ml_type = int(nl["ml_type"])
+    files: Dict[str, str] = {}
+    cfg = _config(nl, precision)
+
+    if ml_type == -1:
+        out_dir = os.path.join(workdir, "desc" + str(nl["db_path"]).strip())
+        os.makedirs(out_dir, exist_ok=True)
+        with _lib.Handle(cfg) as h:
+            ss, nat, pos, cell, types, *_ = _load(cfgs, DB, els, int(nl["iread_energy"]), False)
+            h.set_structures(nat, pos, cell, types)
+            B, _ = h.descriptors()
+        a0 = 0
+        for c, n in zip(cfgs, nat):
+            p = os.path.join(out_dir, _stem(c) + ".eml")
+            potfile.write_eml(p, B[a0:a0 + n])
+            files[_stem(c)] = p
+            a0 += int(n)
+        return FitResult(None, None, None, 0, len(cfgs), files)
+
     train = [c for c in cfgs if c.train]
     test = [c for c in cfgs if not c.train]
     os.makedirs(os.path.join(workdir, output), exist_ok=True)
-    files: Dict[str, str] = {}
-    with _lib.Handle(_config(nl, precision)) as h:
+    with _lib.Handle(cfg) as h:
         ss, nat, pos, cell, types, E, F, S, has, w = _load(train, DB, els, int(nl["iread_energy"]), True)
         h.set_structures(nat, pos, cell, types)
+        Z = None
+        if ml_type == 1:
+            Z = _kernel_points(h, nl, train, nat, workdir, files)
+            h.set_kernel_points(Z)
         h.set_labels(E, F, S, has, w)
         coef, rmse = h.fit()
+
+        order = potfile.MLD_KERNEL if ml_type == 1 else int(nl["mld_order"])
+        extra = {}
+        if ml_type == 1:
+            extra = dict(kernel_points=_standardise(Z), kernel_type=cfg.kernel_type, sigma_kernel=cfg.sigma_kernel,
+                         length_kernel=cfg.length_kernel, kernel_power=cfg.kernel_power)
+        nch = 3 if cfg.weighted_3ch else (2 if cfg.weighted else 1)
+        p_mld, p_lmp = potfile.write_potential(
+            workdir, coef, els or ["X"], j_max=cfg.j_max, r_cut=cfg.r_cut, mld_order=order, nchannels=nch,
+            weights=list(cfg.weight_per_element)[:len(els)] if cfg.weighted else None,
+            weights_3ch=list(cfg.weight_per_element_3ch)[:len(els)] if cfg.weighted_3ch else None, **extra)
+        files["pot"], files["lammps_pot"] = p_mld, p_lmp
+
         rmse_test = None
         for tag, group in (("train", train), ("test", test)):
             if not group or (tag == "test" and nl.get("train_only")):

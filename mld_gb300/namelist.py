@@ -25,6 +25,8 @@ DEFAULTS: Dict[str, Any] = {
     "kernel_power": 2.0,
     "length_kernel": math.sqrt(0.5),
     "sigma_kernel": 0.0,
+    "np_kernel_ref": 200,
+    "np_kernel_full": 800,
     "seed": 14792435,
     "selection_type": 3,
     "iread_energy": 2,

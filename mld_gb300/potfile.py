@@ -185,3 +185,29 @@ def read_eml(path: str):
     """(atom indices, descriptors) of a descriptor dump."""
     data = np.loadtxt(path, ndmin=2)
     return data[:, 0].astype(np.int64), data[:, 1:]
+
+
+def write_kernel_matrix(path: str, points: np.ndarray, iconf: Sequence[int], iatom: Sequence[int],
+                        names: Sequence[str]) -> None:
+    """``kernel_matrix.dat``: the raw descriptors of the kernel's reference atoms
+    (module_write_parameters.F90:1585-1600): a ``(2I9)`` header (count, dim + 4), then per point
+    ``(I6, n E20.10, I6, I6, A15)`` = index, descriptor, configuration, atom, ``"  <class>_<klm>_<n>"``."""
+    P = np.asarray(points, dtype=np.float64)
+    with open(path, "w") as f:
+        f.write(f"{P.shape[0]:9d}{P.shape[1] + 4:9d}\n")
+        for k, row in enumerate(P):
+            tag = ("  " + names[k])[:15].ljust(15)
+            f.write(f"{k + 1:6d}" + "".join(_e(v, 20, 10) for v in row) + f"{iconf[k]:6d}{iatom[k]:6d}" + tag + "\n")
+
+
+def read_kernel_matrix(path: str) -> np.ndarray:
+    """Points of ``kernel_matrix.dat`` (compute_kernel.F90:1106-1160), ordered by their index."""
+    with open(path) as f:
+        nk, dim4 = (int(t) for t in f.readline().split()[:2])
+        dim = dim4 - 4
+        P = np.zeros((nk, dim))
+        for _ in range(nk):
+            line = f.readline()
+            k = int(line[:6])
+            P[k - 1] = [float(line[6 + 20 * i:26 + 20 * i]) for i in range(dim)]
+    return P

@@ -25,6 +25,20 @@ def fit19():
 
 
 @pytest.fixture(scope="session")
+def predictions():
+    import numpy as np
+    return np.load(os.path.join(ROOT, "tests", "golden", "predictions_fit03_fit08.npz"))
+
+
+def channel_weights_for(elements):
+    """(channels x elements) weights of the fit08 setup: unweighted, then the weighted_auto pair."""
+    import numpy as np
+    from mld_gb300 import elements as el
+    w2, w3 = el.auto_channel_weights(list(elements))
+    return np.stack([np.ones(len(elements)), w2, w3])
+
+
+@pytest.fixture(scope="session")
 def lib():
     from mld_gb300 import build, _lib
     build.build()

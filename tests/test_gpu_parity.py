@@ -80,6 +80,43 @@ def test_fit19_three_channel_descriptors(lib, fit19, precision, tol):
     assert _rel(B, ref) < tol
 
 
+@pytest.mark.parametrize("fit", ["fit03", "fit08"])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_reference_run_predictions(lib, predictions, fit, precision):
+    """mld_gpu_predict with a reference run's .pot weights reproduces that run's train_*.out."""
+    from mld_gb300 import _lib
+    from conftest import channel_weights_for
+    d = predictions
+    j_max, r_cut, order = d[f"{fit}_params"]
+    els = [str(e) for e in d[f"{fit}_elements"]]
+    c = _lib.default_config()
+    c.j_max, c.r_cut, c.mld_order, c.precision, c.n_elements = float(j_max), float(r_cut), int(order), precision, len(els)
+    if len(els) > 1:
+        chw = channel_weights_for(els)
+        c.weighted, c.weighted_3ch = 1, 1
+        for k in range(len(els)):
+            c.weight_per_element[k], c.weight_per_element_3ch[k] = chw[1, k], chw[2, k]
+    n = len(d[f"{fit}_names"])
+    nat = [d[f"{fit}_pos_{i}"].shape[0] for i in range(n)]
+    with _lib.Handle(c) as h:
+        h.set_structures(nat, np.concatenate([d[f"{fit}_pos_{i}"] for i in range(n)]),
+                         np.stack([d[f"{fit}_cell_{i}"] for i in range(n)]),
+                         np.concatenate([d[f"{fit}_types_{i}"] for i in range(n)]))
+        E, F, S = h.predict(d[f"{fit}_w"])
+    # plain: the printed precision of es20.10; mixed: FP32 descriptors and rows
+    tol = 1e-9 if precision == 0 else 2e-4
+    scaleE = max(np.abs([d[f"{fit}_E_{i}"][0] for i in range(n)]).max(), 1.0)
+    a0 = 0
+    for i in range(n):
+        Er, Fr, Sr = d[f"{fit}_E_{i}"], d[f"{fit}_F_{i}"], d[f"{fit}_S_{i}"]
+        assert abs(E[i] - Er[0]) <= tol * scaleE, (i, E[i], Er[0])
+        if Fr.size:
+            assert np.abs(F[a0:a0 + nat[i]].reshape(-1) - Fr).max() <= tol * max(np.abs(Fr).max(), 1.0)
+        if Sr.size:
+            assert np.abs(S[i] - Sr).max() <= tol * max(np.abs(Sr).max(), 0.1)
+        a0 += nat[i]
+
+
 def _small_dataset(seed=5):
     from mld_gb300 import synth
     rng = np.random.default_rng(seed)

@@ -65,6 +65,30 @@ def test_fit19_golden_three_channel_descriptors(fit19):
     assert 1e-9 < np.abs(w3_64 - w3).max() < 1e-6
 
 
+@pytest.mark.parametrize("fit", ["fit03", "fit08"])
+def test_reference_run_predictions(predictions, fit):
+    """Design rows x the .pot weights of a reference run reproduce that run's train_*.out
+    predictions (es20.10): fit03 quadratic QNML incl. 1-atom small-box stresses, fit08 3-channel
+    weighted linear."""
+    from conftest import channel_weights_for
+    d = predictions
+    j_max, r_cut, order = d[f"{fit}_params"]
+    els = [str(e) for e in d[f"{fit}_elements"]]
+    chw = channel_weights_for(els) if len(els) > 1 else None
+    rows = oracle.quadratic_rows if int(order) == 2 else oracle.linear_rows
+    w = d[f"{fit}_w"]
+    for i in range(len(d[f"{fit}_names"])):
+        desc = oracle.bispectrum(d[f"{fit}_pos_{i}"], d[f"{fit}_cell_{i}"], d[f"{fit}_types_{i}"], float(r_cut),
+                                 float(j_max), channel_weights=chw)
+        e, f, st = rows(desc, d[f"{fit}_cell_{i}"])
+        E, F, S = d[f"{fit}_E_{i}"], d[f"{fit}_F_{i}"], d[f"{fit}_S_{i}"]
+        assert abs(e @ w - E[0]) <= 1e-9 * max(abs(E[0]), 1.0)
+        if F.size:
+            assert np.abs(f @ w - F).max() <= 1e-9 * max(np.abs(F).max(), 1.0)
+        if S.size:
+            assert np.abs(st @ w - S).max() <= 1e-10 * max(np.abs(S).max(), 1.0)
+
+
 @pytest.mark.parametrize("idx", [2, 9])
 def test_force_rows_are_negative_gradient(fit17, idx):
     pos = fit17[f"pos_{idx}"].copy()
