@@ -44,7 +44,12 @@ module mld_gpu_mod
   public :: mld_gpu_config_defaults, mld_gpu_create, mld_gpu_destroy, mld_gpu_dims, &
             mld_gpu_set_structures, mld_gpu_set_labels, mld_gpu_descriptors, mld_gpu_num_rows, &
             mld_gpu_design_matrix, mld_gpu_gram, mld_gpu_solve, mld_gpu_fit, mld_gpu_predict, &
-            mld_gpu_set_kernel_points, &
+            mld_gpu_set_kernel_points, mld_gpu_solve_info, mld_gpu_gram_rows, &
+            mld_gpu_server_create, mld_gpu_server_destroy, mld_gpu_server_submit, &
+            mld_gpu_server_progress, mld_gpu_server_result, mld_gpu_server_wait, mld_gpu_server_stats, &
+            mld_gpu_descriptor_derivatives, mld_gpu_last_error, mld_gpu_server_last_error, &
+            mld_gpu_set_profiling, mld_gpu_profile, mld_gpu_timer_start, mld_gpu_timer_stop, &
+            mld_gpu_work_counts, mld_gpu_peak_flops, mld_gpu_descriptors_noalloc, &
             mld_gpu_synchronize
 
   interface
@@ -130,6 +135,135 @@ module mld_gpu_mod
     integer(c_int) function mld_gpu_synchronize(h) bind(C, name="mld_gpu_synchronize")
       import :: c_int, c_ptr
       type(c_ptr), value :: h
+    end function
+
+    integer(c_int) function mld_gpu_solve_info(h, pcg_iterations, pcg_residual, precond_shift, chol_retries) &
+        bind(C, name="mld_gpu_solve_info")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, pcg_iterations, pcg_residual, precond_shift, chol_retries
+    end function
+
+    integer(c_int) function mld_gpu_gram_rows(method, x, x_is_fp32, m, d, ldx, w, y, g, rhs, stream, err, err_len) &
+        bind(C, name="mld_gpu_gram_rows")
+      import :: c_int, c_long_long, c_ptr
+      integer(c_int), value :: method, x_is_fp32, d, ldx, err_len
+      integer(c_long_long), value :: m
+      type(c_ptr), value :: x, w, y, g, rhs, stream, err
+    end function
+
+    ! returns a NUL-terminated C string owned by the handle (c_f_pointer to read it)
+    type(c_ptr) function mld_gpu_last_error(h) bind(C, name="mld_gpu_last_error")
+      import :: c_ptr
+      type(c_ptr), value :: h
+    end function
+
+    type(c_ptr) function mld_gpu_server_last_error(srv) bind(C, name="mld_gpu_server_last_error")
+      import :: c_ptr
+      type(c_ptr), value :: srv
+    end function
+
+    integer(c_int) function mld_gpu_descriptor_derivatives(h, p_inout, nbr_out, u_out, db_out) &
+        bind(C, name="mld_gpu_descriptor_derivatives")
+      import :: c_int, c_ptr, c_long_long
+      type(c_ptr), value :: h, nbr_out, u_out, db_out
+      integer(c_long_long), intent(inout) :: p_inout
+    end function
+
+    integer(c_int) function mld_gpu_set_profiling(h, on) bind(C, name="mld_gpu_set_profiling")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+      integer(c_int), value :: on
+    end function
+
+    integer(c_int) function mld_gpu_profile(h, ms, launches, calls, reset) bind(C, name="mld_gpu_profile")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, ms, launches, calls
+      integer(c_int), value :: reset
+    end function
+
+    integer(c_int) function mld_gpu_timer_start(h) bind(C, name="mld_gpu_timer_start")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+
+    integer(c_int) function mld_gpu_timer_stop(h, ms) bind(C, name="mld_gpu_timer_stop")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(out) :: ms
+    end function
+
+    integer(c_int) function mld_gpu_work_counts(h, counts) bind(C, name="mld_gpu_work_counts")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, counts
+    end function
+
+    integer(c_int) function mld_gpu_peak_flops(h, precision, tflops) bind(C, name="mld_gpu_peak_flops")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      integer(c_int), value :: precision
+      real(c_double), intent(out) :: tflops
+    end function
+
+    integer(c_int) function mld_gpu_descriptors_noalloc(cfg, nat, pos, cell, types, b, stream, err, err_len) &
+        bind(C, name="mld_gpu_descriptors_noalloc")
+      import :: c_int, c_ptr, mld_gpu_config
+      type(mld_gpu_config), intent(in) :: cfg
+      integer(c_int), value :: nat, err_len
+      type(c_ptr), value :: pos, cell, types, b, stream, err
+    end function
+
+    ! serving loop: one server per GPU, continuous batching over n_slots evaluation slots
+    integer(c_int) function mld_gpu_server_create(cfg, w_params, n_slots, max_batch_atoms, hbm_fraction, srv) &
+        bind(C, name="mld_gpu_server_create")
+      import :: c_int, c_long_long, c_double, c_ptr, mld_gpu_config
+      type(mld_gpu_config), intent(in) :: cfg
+      type(c_ptr), value :: w_params
+      integer(c_int), value :: n_slots
+      integer(c_long_long), value :: max_batch_atoms
+      real(c_double), value :: hbm_fraction
+      type(c_ptr), intent(out) :: srv
+    end function
+
+    subroutine mld_gpu_server_destroy(srv) bind(C, name="mld_gpu_server_destroy")
+      import :: c_ptr
+      type(c_ptr), value :: srv
+    end subroutine
+
+    integer(c_int) function mld_gpu_server_submit(srv, nat, pos, cell, types, ticket) bind(C, name="mld_gpu_server_submit")
+      import :: c_int, c_ptr, c_long_long
+      type(c_ptr), value :: srv, pos, cell, types
+      integer(c_int), value :: nat
+      integer(c_long_long), intent(out) :: ticket
+    end function
+
+    integer(c_int) function mld_gpu_server_progress(srv, n_busy, n_queued) bind(C, name="mld_gpu_server_progress")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: srv
+      integer(c_int), intent(out) :: n_busy, n_queued
+    end function
+
+    integer(c_int) function mld_gpu_server_result(srv, ticket, e, f, s, latency_ms, ready) &
+        bind(C, name="mld_gpu_server_result")
+      import :: c_int, c_ptr, c_long_long
+      type(c_ptr), value :: srv, e, f, s, latency_ms
+      integer(c_long_long), value :: ticket
+      integer(c_int), intent(out) :: ready
+    end function
+
+    integer(c_int) function mld_gpu_server_wait(srv, ticket, e, f, s, latency_ms, timeout_ms) &
+        bind(C, name="mld_gpu_server_wait")
+      import :: c_int, c_ptr, c_long_long, c_double
+      type(c_ptr), value :: srv, e, f, s, latency_ms
+      integer(c_long_long), value :: ticket
+      real(c_double), value :: timeout_ms
+    end function
+
+    integer(c_int) function mld_gpu_server_stats(srv, batches, atoms_done, budget_bytes) &
+        bind(C, name="mld_gpu_server_stats")
+      import :: c_int, c_ptr, c_long_long, c_double
+      type(c_ptr), value :: srv
+      integer(c_long_long), intent(out) :: batches, atoms_done
+      real(c_double), intent(out) :: budget_bytes
     end function
   end interface
 end module mld_gpu_mod

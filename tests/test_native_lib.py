@@ -29,6 +29,18 @@ def test_python_binding_lists_all(lib):
     assert set(declared_symbols()) <= set(_lib.EXPORTED)
 
 
+def test_fortran_module_binds_every_entry_point():
+    """The ISO_C_BINDING module declares every C entry point, and its mld_gpu_config type has
+    the C struct's fields in the same order (no Fortran compiler here: checked as text)."""
+    from mld_gb300 import _lib
+    src = open(os.path.join(ROOT, "mld_gb300", "fortran", "mld_gpu_mod.F90")).read()
+    bound = set(re.findall(r'name="(mld_gpu_\w+)"', src))
+    assert set(declared_symbols()) <= bound, sorted(set(declared_symbols()) - bound)
+    body = re.search(r"type, bind\(C\), public :: mld_gpu_config(.*?)end type", src, flags=re.S).group(1)
+    fields = re.findall(r"::\s*(\w+)", body)
+    assert fields == [f[0] for f in _lib.MldGpuConfig._fields_]
+
+
 def test_config_defaults_match_namelist():
     from mld_gb300 import _lib
     c = _lib.default_config()
