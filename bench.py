@@ -35,6 +35,10 @@ N_STRUCT = 2000
 RCUT = 4.7
 J_MAX = 4.0
 LAMBDA = 1e-8
+# DRAM bytes (read + write) of one k_bso4<float> launch per atom: 78.05 MB over 45,702 atoms in
+# the ncu capture of the 200-structure Fe case (profiles/k_bso4_f32_fe200.md); the traffic is
+# per-atom neighbour data and rows, so it is scaled by the atoms of the launch
+BSO4_DRAM_BYTES_PER_ATOM = 78.05e6 / 45702
 
 
 def _args():
@@ -446,8 +450,13 @@ def run_serve(a):
         out[name] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                      "mean_ms": float(lat.mean()), "atoms_per_s": total_atoms / wall, "wall_s": wall,
                      "batches": st["batches"], "clocks": clk.summary()}
+    # per request: max |F_mixed - F_plain| / max |F_plain|; worst request reported
     ferr = max(float(np.abs(fm - fp).max() / max(np.abs(fp).max(), 1e-300))
                for fm, fp in zip(forces["mixed"], forces["plain_fp64"]))
+    # over all atoms of all requests: ||F_mixed - F_plain|| / ||F_plain||
+    fm_all = np.concatenate([np.asarray(f).reshape(-1) for f in forces["mixed"]])
+    fp_all = np.concatenate([np.asarray(f).reshape(-1) for f in forces["plain_fp64"]])
+    ferr_rms = float(np.linalg.norm(fm_all - fp_all) / max(np.linalg.norm(fp_all), 1e-300))
     mx = out["mixed"]
     line = {
         "metric": "serving atoms/s and p99 latency (continuous batching, fitted QNML alloy potential)",
@@ -459,6 +468,7 @@ def run_serve(a):
                    "hbm_fraction": 0.5, "parallelism": "single"},
         "p50_ms": mx["p50_ms"], "p99_ms": mx["p99_ms"], "mixed": mx, "plain_fp64": out["plain_fp64"],
         "force_rel_diff_mixed_vs_plain": ferr,
+        "force_rel_diff_mixed_vs_plain_rms": ferr_rms,
     }
     print(json.dumps(line))
 
@@ -588,7 +598,10 @@ def main():
                      "achieved": achieved, "peak": res["peak32"], "unit": "TFLOP/s", "frac": achieved / res["peak32"],
                      "peak_source": "measured in this run (FP32 FMA probe; not in MEASURED_PEAKS.json)",
                      "flops_per_launch": res["flops"], "flops_per_pair": res["per_pair"],
-                     "flops_per_atom": res["per_atom"], "traffic": None},
+                     "flops_per_atom": res["per_atom"], "traffic": BSO4_DRAM_BYTES_PER_ATOM * A,
+                     "traffic_unit": "bytes per launch",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the "
+                                       "200-structure case, scaled by atoms"},
         "gpu_launches": res["launches"],
         "clocks": res["clocks"],
     }

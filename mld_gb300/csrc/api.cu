@@ -96,7 +96,7 @@ struct mld_gpu_handle {
     B_ROWE, B_ROWF, B_ROWS, B_X, B_Y, B_WROW, B_KIND,
     B_G, B_H, B_W, B_EVALS, B_INFO, B_SQ, B_PRED, B_BOUT, B_DBOUT,
     B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
-    B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV, B_KZD, B_KZF, B_KWS, B_WSERVE,
+    B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV, B_KZD, B_KZF, B_KWS, B_WSERVE, B_P32,
     B_COUNT
   };
   static_assert(B_COUNT <= 64, "buffer table too small");
@@ -492,6 +492,9 @@ constexpr double kPrecondShiftMin = 1e-6;
 constexpr double kPrecondShiftPerColumn = 2e-7;
 constexpr double kPcgTol2 = 1e-22;   // (preconditioned residual / initial)^2 that ends the iteration
 constexpr double kPcgFloor2 = 1e-14; // below this, stagnation also ends it
+constexpr int kPrecond32MinD = 768;  // blocks this wide get the FP32 preconditioner (precond32.cu)
+// its first shift per column: a retry costs one FP32 factorisation, so it starts lower
+constexpr double kPrecond32ShiftPerColumn = 5e-8;
 
 // Mixed method, one block of columns [c0, c0 + Db) of the FP32 design matrix.
 //  * normal matrix G~ = X^T W X on the tensor cores in BF16 split precision (gram_tc.cu) and
@@ -548,13 +551,27 @@ int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const dou
   int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
   // the error of the BF16x3 Gram is coherent across the matrix (the tensor core truncates its
   // FP32 sums), so the shift that keeps G~ positive definite grows with D
-  double rel = std::max(kPrecondShiftMin, kPrecondShiftPerColumn * Db);
+  const bool p32 = Db >= kPrecond32MinD;
+  double rel = std::max(kPrecondShiftMin, (p32 ? kPrecond32ShiftPerColumn : kPrecondShiftPerColumn) * Db);
   int retries = 0;
+  // wide blocks: Jacobi-scaled FP32 factor and inverse (the FP64 pipe is 1/64 of FP32 here);
+  // narrow blocks: FP64, where the small shift of a short block needs the precision
+  void* pws = nullptr;
+  if (p32) {
+    CK(ensure(h, mld_gpu_handle::B_P32, precond32_workspace_bytes(Db)));
+    pws = bp_<void>(h, mld_gpu_handle::B_P32);
+  }
   for (;; ++retries) {
-    CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)Db * Db, cudaMemcpyDeviceToDevice, h->st));
-    CK(launch_shift_diag_rel(Lf, Db, lam, rel, h->st));
-    CK(launch_cholesky(Lf, Db, 0.0, info, h->st));
-    nl(h, 1 + cholesky_launches(Db));
+    if (p32) {
+      int nb = 0;
+      CK(launch_precond32_build(G, Db, lam, rel, pws, info, h->st, &nb));
+      nl(h, nb);
+    } else {
+      CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)Db * Db, cudaMemcpyDeviceToDevice, h->st));
+      CK(launch_shift_diag_rel(Lf, Db, lam, rel, h->st));
+      CK(launch_cholesky(Lf, Db, 0.0, info, h->st));
+      nl(h, 1 + cholesky_launches(Db));
+    }
     int hinfo = 0;
     CK(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
@@ -566,21 +583,27 @@ int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const dou
   h->precond_shift[stage] = rel;
   h->chol_retries += retries;
   // explicit inverse of the factor: each preconditioner application is two dense matvecs
-  CK(ensure(h, mld_gpu_handle::B_RINV, sizeof(double) * 2 * (size_t)Db * Db));
-  double* Rinv = bp_<double>(h, mld_gpu_handle::B_RINV);
-  double* Rinvt = Rinv + (size_t)Db * Db;
-  {
+  double* Rinv = nullptr;
+  double* Rinvt = nullptr;
+  if (!p32) {
+    CK(ensure(h, mld_gpu_handle::B_RINV, sizeof(double) * 2 * (size_t)Db * Db));
+    Rinv = bp_<double>(h, mld_gpu_handle::B_RINV);
+    Rinvt = Rinv + (size_t)Db * Db;
     int ninv = 0;
     CK(launch_cholesky_inverse(Lf, Db, Rinv, Rinvt, h->st, &ninv));
     nl(h, ninv);
   }
+  auto precond = [&](const double* rr, double* zz) {
+    return p32 ? launch_precond32_apply(pws, Db, rr, zz, tmp, h->st)
+               : launch_precond_apply(Rinv, Rinvt, Db, rr, zz, tmp, h->st);
+  };
   // objective sum_r w_r y_r^2 at w = 0, for the stopping test on its decrease
   CK(launch_weighted_sumsq(wrow, y, M, scal + 4, h->st));
   nl(h, 1);
   // x0 = 0, r0 = rhs
   CK(cudaMemsetAsync(w, 0, sizeof(double) * Db, h->st));
   CK(cudaMemcpyAsync(r, hv, sizeof(double) * Db, cudaMemcpyDeviceToDevice, h->st));
-  CK(launch_precond_apply(Rinv, Rinvt, Db, r, z, tmp, h->st));
+  CK(precond(r, z));
   CK(launch_pcg_beta(Db, z, r, p, scal, 1, h->st));
   nl(h, 3);
   CK(launch_split_weights(wrow, M, sv, h->st));  // the fused matvecs read w as pairs
@@ -593,7 +616,7 @@ int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const dou
     int nmv = 0;
     CK(launch_normal_matvec(X, h->ldx, c0, Db, wrow, p, M, lam, sv, q, h->nsm, h->st, &nmv, terr));
     CK(launch_pcg_alpha(Db, p, q, w, r, scal, h->st));
-    CK(launch_precond_apply(Rinv, Rinvt, Db, r, z, tmp, h->st));
+    CK(precond(r, z));
     CK(launch_pcg_beta(Db, z, r, p, scal, 0, h->st));
     nl(h, nmv + 4);
     CK(cudaMemcpyAsync(hs, scal, sizeof(double) * 5, cudaMemcpyDeviceToHost, h->st));

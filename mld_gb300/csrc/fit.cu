@@ -373,25 +373,35 @@ __global__ void __launch_bounds__(256) k_xtv_ds(const float* __restrict__ X, int
 
 // ------------------------------------------------------------------------------------
 // Normal-equation matvec of a wide block (D > 256) in one pass over X.  Design rows stream
-// through a ring of shared-memory stages by 1-D bulk copies issued from one producer thread;
-// eight consumer warps form the dot x_r . p over column slices (double-FP32), combine the
-// slices, and add w_r (x_r . p) x_r into per-column double-FP32 sums held in shared memory.
+// through a ring of shared-memory stages by 1-D bulk copies issued from one producer thread.
+// Eight consumer warps own the columns c = tid + 256 j (j < CPT).  Per step of kWRows rows:
+//   * each thread forms FP32 partial dots of its columns with p (rounded to FP32);
+//   * warps reduce them, one warp per row sums the eight warp partials in FP64 and scales by
+//     w_r, giving t_r = w_r (x_r . p);
+//   * each thread adds x_rc t_r to FP32 column sums, which are moved into FP64 sums every
+//     kWFlushSteps steps.
+// FP32 arithmetic on chunks (24 columns of a dot, 8 rows of a column sum) with FP64 between
+// chunks keeps the relative error near 1e-7 at about three FP32 operations per element, so
+// the pass runs at HBM speed.  The blocks that take this path (quadratic and kernel columns)
+// are so ill-conditioned that the iteration stops at relative residuals far above 1e-7; the
+// narrow linear blocks keep double-FP32 (k_normal_matvec_narrow).
 // Every wait is bounded: on expiry the CTA sets *err and leaves the loop uniformly.
 // ------------------------------------------------------------------------------------
 constexpr int kWConsumers = 256;
+constexpr int kWRows = 4;        // design rows per consumer step
+constexpr int kWFlushSteps = 2;  // steps between FP32 -> FP64 moves of the column sums
 constexpr int kWThreads = kWConsumers + 32;
 
-// CPT columns per consumer thread (c = tid + 256 k): p as pairs and the column sums live in
-// registers; the row ring and the per-warp dot partials are in shared memory.
 template <int CPT>
 __global__ void __launch_bounds__(kWThreads, 1)
     k_normal_matvec_wide(const float* __restrict__ X, long long ldx, int c0, int D, const float2* __restrict__ wds,
                          const double* __restrict__ p, long long M, long long rpb, int rowf, int stages,
                          double* __restrict__ q, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char wsm[];
-  float* rows = reinterpret_cast<float*>(wsm);                             // stages * rowf
-  float2* part = reinterpret_cast<float2*>(rows + (size_t)stages * rowf);  // stages * 8
-  uint64_t* full = reinterpret_cast<uint64_t*>(part + stages * 8);
+  float* rows = reinterpret_cast<float*>(wsm);                              // stages * rowf
+  double* part = reinterpret_cast<double*>(rows + (size_t)stages * rowf);   // stages * 8
+  double* tv = part + stages * 8;                                           // stages
+  uint64_t* full = reinterpret_cast<uint64_t*>(tv + stages);
   uint64_t* empty = full + stages;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int a0 = c0 & ~3, off = c0 - a0;
@@ -427,42 +437,47 @@ __global__ void __launch_bounds__(kWThreads, 1)
     return;
   }
   // consumers
-  float ph[CPT], pl[CPT], ah[CPT], al[CPT];
+  float pf[CPT], acc[CPT];
+  double acc64[CPT];
 #pragma unroll
   for (int k = 0; k < CPT; ++k) {
     const int c = tid + kWConsumers * k;
-    ds_split(c < D ? p[c] : 0.0, ph[k], pl[k]);
-    ah[k] = al[k] = 0.f;
+    pf[k] = c < D ? (float)p[c] : 0.f;
+    acc[k] = 0.f;
+    acc64[k] = 0.0;
   }
-  // two design rows per step: independent dot chains and one pass over the sums for both
-  for (long long k = 0; k < nr; k += 2) {
-    const bool two = k + 1 < nr;
-    const int s0 = (int)(k % stages), s1 = (int)((k + 1) % stages);
-    const float2 wv0 = wds[r0 + k];
-    const float2 wv1 = two ? wds[r0 + k + 1] : make_float2(0.f, 0.f);
-    bool ok = ptx::mbar_wait(&full[s0], (uint32_t)((k / stages) & 1));
-    if (two) ok = ok && ptx::mbar_wait(&full[s1], (uint32_t)(((k + 1) / stages) & 1));
-    const float* xr0 = rows + (size_t)s0 * rowf + off;
-    const float* xr1 = rows + (size_t)s1 * rowf + off;
-    float d0h = 0.f, d0l = 0.f, d1h = 0.f, d1l = 0.f;
+  long long step = 0;
+  for (long long k = 0; k < nr; k += kWRows, ++step) {
+    const int nv = (int)min((long long)kWRows, nr - k);
+    int sr[kWRows];
+    bool ok = true;
 #pragma unroll
-    for (int j = 0; j < CPT; ++j) {
-      const int c = tid + kWConsumers * j;
-      const float v0 = (ok && c < D) ? xr0[c] : 0.f;
-      const float v1 = (ok && two && c < D) ? xr1[c] : 0.f;
-      ds_fma(d0h, d0l, v0, ph[j], pl[j]);
-      ds_fma(d1h, d1l, v1, ph[j], pl[j]);
+    for (int r = 0; r < kWRows; ++r) {
+      sr[r] = (int)((k + r) % stages);
+      if (r < nv) ok = ok && ptx::mbar_wait(&full[sr[r]], (uint32_t)(((k + r) / stages) & 1));
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      float oh = __shfl_xor_sync(0xffffffffu, d0h, o), ol = __shfl_xor_sync(0xffffffffu, d0l, o);
-      ds_add(d0h, d0l, oh, ol);
-      oh = __shfl_xor_sync(0xffffffffu, d1h, o);
-      ol = __shfl_xor_sync(0xffffffffu, d1l, o);
-      ds_add(d1h, d1l, oh, ol);
+    float d[kWRows];
+#pragma unroll
+    for (int r = 0; r < kWRows; ++r) d[r] = 0.f;
+    if (ok) {
+#pragma unroll
+      for (int j = 0; j < CPT; ++j) {
+        const int c = tid + kWConsumers * j;
+        if (c < D) {
+#pragma unroll
+          for (int r = 0; r < kWRows; ++r) {
+            const float v = r < nv ? rows[(size_t)sr[r] * rowf + off + c] : 0.f;
+            d[r] = fmaf(v, pf[j], d[r]);
+          }
+        }
+      }
     }
+#pragma unroll
+    for (int r = 0; r < kWRows; ++r)
+      for (int o = 16; o > 0; o >>= 1) d[r] += __shfl_xor_sync(0xffffffffu, d[r], o);
     if (lane == 0) {
-      part[s0 * 8 + warp] = make_float2(d0h, d0l);
-      part[s1 * 8 + warp] = make_float2(d1h, d1l);
+#pragma unroll
+      for (int r = 0; r < kWRows; ++r) part[sr[r] * 8 + warp] = (double)d[r];
     }
     int any_fail;
     asm volatile(
@@ -473,48 +488,50 @@ __global__ void __launch_bounds__(kWThreads, 1)
       if (tid == 0) atomicExch(err, 1);
       break;
     }
-    float a0h = 0.f, a0l = 0.f, a1h = 0.f, a1l = 0.f;
+    // warp r sums the eight slices of row r in FP64 and scales by w_r
+    if (warp < nv) {
+      const int sw = (int)((k + warp) % stages);
+      double v = lane < 8 ? part[sw * 8 + lane] : 0.0;
+      for (int o = 4; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) {
+        const float2 wv = wds[r0 + k + warp];
+        tv[sw] = v * ((double)wv.x + (double)wv.y);
+      }
+    }
+    asm volatile("bar.sync 2, %0;\n" ::"n"(kWConsumers));
+    float th[kWRows];
 #pragma unroll
-    for (int w8 = 0; w8 < 8; ++w8) {
-      const float2 p0 = part[s0 * 8 + w8], p1 = part[s1 * 8 + w8];
-      ds_add(a0h, a0l, p0.x, p0.y);
-      ds_add(a1h, a1l, p1.x, p1.y);
-    }
-    // s_r = w_r * (x_r . p) for both rows
-    float t0h, t0l, t1h, t1l;
-    {
-      const float sp = a0h * wv0.x, se = fmaf(a0h, wv0.y, fmaf(a0l, wv0.x, fmaf(a0h, wv0.x, -sp)));
-      t0h = sp + se;
-      t0l = se - (t0h - sp);
-    }
-    {
-      const float sp = a1h * wv1.x, se = fmaf(a1h, wv1.y, fmaf(a1l, wv1.x, fmaf(a1h, wv1.x, -sp)));
-      t1h = sp + se;
-      t1l = se - (t1h - sp);
-    }
+    for (int r = 0; r < kWRows; ++r) th[r] = r < nv ? (float)tv[sr[r]] : 0.f;
 #pragma unroll
     for (int j = 0; j < CPT; ++j) {
       const int c = tid + kWConsumers * j;
-      const float v0 = c < D ? xr0[c] : 0.f;
-      const float v1 = (two && c < D) ? xr1[c] : 0.f;
-      ds_fma(ah[j], al[j], v0, t0h, t0l);
-      ds_fma(ah[j], al[j], v1, t1h, t1l);
+      if (c < D) {
+#pragma unroll
+        for (int r = 0; r < kWRows; ++r) {
+          const float v = r < nv ? rows[(size_t)sr[r] * rowf + off + c] : 0.f;
+          acc[j] = fmaf(v, th[r], acc[j]);
+        }
+      }
     }
-    // both stages are read: release them to the producer
+    // every stage of this step is read: release them to the producer
     __syncwarp();
     if (lane == 0) {
-      ptx::mbar_arrive(&empty[s0]);
-      if (two) ptx::mbar_arrive(&empty[s1]);
-    }
-    if (((k >> 1) & 31) == 31) {
 #pragma unroll
-      for (int j = 0; j < CPT; ++j) ds_norm(ah[j], al[j]);
+      for (int r = 0; r < kWRows; ++r)
+        if (r < nv) ptx::mbar_arrive(&empty[sr[r]]);
+    }
+    if ((step % kWFlushSteps) == kWFlushSteps - 1) {
+#pragma unroll
+      for (int j = 0; j < CPT; ++j) {
+        acc64[j] += (double)acc[j];
+        acc[j] = 0.f;
+      }
     }
   }
 #pragma unroll
   for (int j = 0; j < CPT; ++j) {
     const int c = tid + kWConsumers * j;
-    const double v = (double)ah[j] + (double)al[j];
+    const double v = acc64[j] + (double)acc[j];
     if (c < D && v != 0.0) atomicAdd(&q[c], v);
   }
 }
@@ -600,8 +617,8 @@ cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const d
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   }
-  const size_t per_stage = sizeof(float) * rowf + 8 * sizeof(float2) + 2 * sizeof(uint64_t);
-  const int stages = (int)std::min<size_t>(6, ((size_t)optin - 256) / per_stage);
+  const size_t per_stage = sizeof(float) * rowf + 9 * sizeof(double) + 2 * sizeof(uint64_t);
+  const int stages = (int)std::min<size_t>(8, ((size_t)optin - 256) / per_stage);
   const int cpt = (D + kWConsumers - 1) / kWConsumers;
   if (M > 0 && D <= 256) {
     const long long rpb = rows_per_cta(M, 1, nsm);
@@ -617,7 +634,7 @@ cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const d
       default: k_normal_matvec_narrow<8><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
     }
     *launches = 1;
-  } else if (M > 0 && stages >= 2 && (ldx % 4) == 0 && cpt <= 32) {
+  } else if (M > 0 && stages >= kWRows && (ldx % 4) == 0 && cpt <= 32) {
     const size_t smem = 256 + (size_t)stages * per_stage;
     const long long rpb = (M + nsm - 1) / nsm;
     const unsigned grid = (unsigned)((M + rpb - 1) / rpb);

@@ -234,6 +234,12 @@ cudaError_t launch_cholesky_inverse(const double* L, int D, double* R, double* R
 cudaError_t launch_precond_apply(const double* R, const double* Rt, int D, const double* r, double* z, double* tmp,
                                  cudaStream_t st);
 inline int cholesky_launches(int D) { return 3 * ((D + 31) / 32) - 2; }
+
+// FP32 Cholesky preconditioner of large blocks (precond32.cu)
+size_t precond32_workspace_bytes(int D);
+cudaError_t launch_precond32_build(const double* G, int D, double lam, double rel, void* ws, int* info,
+                                   cudaStream_t st, int* launches);
+cudaError_t launch_precond32_apply(const void* ws, int D, const double* r, double* z, double* tmp, cudaStream_t st);
 cudaError_t launch_residual(const double* G, int D, double lambda, const double* w, const double* h, double* r,
                             cudaStream_t st);
 cudaError_t launch_axpy(int n, double a, const double* x, double* y, cudaStream_t st);
