@@ -146,6 +146,13 @@ int mld_gpu_fit(mld_gpu_handle* h, double* w_params, double* rmse_efs);
 /* Predictions of the staged batch with coefficients w_params (md_mld_compute_energy/force/stress):
  * E[S] (w . energy row, excluding reference energies), F[3*sum(nat)], S[6*S]; any may be NULL. */
 int mld_gpu_predict(mld_gpu_handle* h, const double* w_params, double* E, double* F, double* S);
+/* The same energies, forces and stress as mld_gpu_predict (ml_type 0), evaluated without design
+ * rows: the descriptor derivatives are contracted with the per-atom effective weights
+ * beta_a = dE/dB_a (w_lin; w_lin + (W + W^T) B_a for the quadratic model, the neighbour's beta in
+ * the stress as the reference's quadratic stress rows use the neighbour's B) and summed in FP64.
+ * This is how the reference's MD evaluation (md_mld_compute_energy/force/stress, mld.F90:1579-1867)
+ * can be computed when only E/F/S are wanted; the serving loop uses it. */
+int mld_gpu_evaluate(mld_gpu_handle* h, const double* w_params, double* E, double* F, double* S);
 
 /* Block until the handle's stream has finished. */
 int mld_gpu_synchronize(mld_gpu_handle* h);

@@ -25,7 +25,7 @@ MAX_ELEMENTS = 8
 EXPORTED = ["mld_gpu_config_defaults", "mld_gpu_create", "mld_gpu_destroy", "mld_gpu_last_error", "mld_gpu_dims",
             "mld_gpu_set_structures", "mld_gpu_set_labels", "mld_gpu_descriptors",
             "mld_gpu_descriptor_derivatives", "mld_gpu_num_rows", "mld_gpu_design_matrix", "mld_gpu_gram",
-            "mld_gpu_solve", "mld_gpu_fit", "mld_gpu_predict", "mld_gpu_synchronize", "mld_gpu_set_profiling",
+            "mld_gpu_solve", "mld_gpu_fit", "mld_gpu_predict", "mld_gpu_evaluate", "mld_gpu_synchronize", "mld_gpu_set_profiling",
             "mld_gpu_profile", "mld_gpu_timer_start", "mld_gpu_timer_stop", "mld_gpu_work_counts",
             "mld_gpu_peak_flops", "mld_gpu_descriptors_noalloc", "mld_gpu_solve_info", "mld_gpu_gram_rows",
             "mld_gpu_set_kernel_points", "mld_gpu_server_create", "mld_gpu_server_destroy",
@@ -100,6 +100,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.mld_gpu_solve.argtypes = [P, P, P, I, P, ctypes.POINTER(I)]
     L.mld_gpu_fit.argtypes = [P, P, P]
     L.mld_gpu_predict.argtypes = [P, P, P, P, P]
+    L.mld_gpu_evaluate.argtypes = [P, P, P, P, P]
     L.mld_gpu_synchronize.argtypes = [P]
     L.mld_gpu_set_profiling.argtypes = [P, I]
     L.mld_gpu_profile.argtypes = [P, P, P, P, I]
@@ -238,6 +239,17 @@ class Handle:
         St = np.zeros((S, 6))
         w = np.ascontiguousarray(w, dtype=np.float64)
         self._check(self._L.mld_gpu_predict(self._h, _p(w), _p(E), _p(F), _p(St)))
+        return E, F, St
+
+    def evaluate(self, w: np.ndarray):
+        """E, F, S as predict() gives them, computed without design rows (mld_gpu_evaluate)."""
+        A = int(self.nat.sum())
+        S = len(self.nat)
+        E = np.zeros(S)
+        F = np.zeros((A, 3))
+        St = np.zeros((S, 6))
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        self._check(self._L.mld_gpu_evaluate(self._h, _p(w), _p(E), _p(F), _p(St)))
         return E, F, St
 
     def synchronize(self):

@@ -84,6 +84,8 @@ struct mld_gpu_handle {
   int nsm = 0;
   int pcg_iters[2] = {0, 0};
   double precond_shift[2] = {0, 0};
+  double ew0 = 0.0;        // constant weight of the evaluation weights (B_EW)
+  bool ew_ready = false;
   double pcg_rel[2] = {0, 0};
   int chol_retries = 0;
 
@@ -97,6 +99,7 @@ struct mld_gpu_handle {
     B_G, B_H, B_W, B_EVALS, B_INFO, B_SQ, B_PRED, B_BOUT, B_DBOUT,
     B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
     B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV, B_KZD, B_KZF, B_KWS, B_WSERVE, B_P32,
+    B_EW, B_EBETA, B_EB, B_EOUT,
     B_COUNT
   };
   static_assert(B_COUNT <= 64, "buffer table too small");
@@ -739,6 +742,11 @@ int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
 
 }  // namespace
 
+namespace mld {
+int eval_weights_upload(mld_gpu_handle* h, const double* w_full);
+int eval_launch(mld_gpu_handle* h, cudaEvent_t done, double** pinned_out);
+}  // namespace mld
+
 extern "C" {
 
 void mld_gpu_config_defaults(mld_gpu_config* c) {
@@ -1217,6 +1225,22 @@ int mld_gpu_fit(mld_gpu_handle* h, double* w_params, double* rmse_efs) {
   return h->mixed ? fit_impl<float>(h, w_params, rmse_efs) : fit_impl<double>(h, w_params, rmse_efs);
 }
 
+int mld_gpu_evaluate(mld_gpu_handle* h, const double* w_params, double* E, double* F, double* Sout) {
+  if (!h || !w_params) return MLD_ERR_INVALID;
+  int rc = mld::eval_weights_upload(h, w_params);
+  if (rc) return rc;
+  rc = mld::eval_launch(h, nullptr, nullptr);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->st));
+  const double* out = bp_<double>(h, mld_gpu_handle::B_EOUT);
+  std::vector<double> ho((size_t)h->S + 3 * (size_t)h->A + 6 * (size_t)h->S);
+  CK(cudaMemcpy(ho.data(), out, sizeof(double) * ho.size(), cudaMemcpyDeviceToHost));
+  if (E) std::copy(ho.begin(), ho.begin() + h->S, E);
+  if (F) std::copy(ho.begin() + h->S, ho.begin() + h->S + 3 * (size_t)h->A, F);
+  if (Sout) std::copy(ho.begin() + h->S + 3 * (size_t)h->A, ho.end(), Sout);
+  return MLD_OK;
+}
+
 int mld_gpu_predict(mld_gpu_handle* h, const double* w_params, double* E, double* F, double* Sout) {
   if (!h || !w_params) return MLD_ERR_INVALID;
   int rc = build_neighbours(h);
@@ -1321,6 +1345,117 @@ int upload_weights(mld_gpu_handle* h, const double* w_full, double** w_dev) {
   CK(cudaStreamSynchronize(h->st));
   *w_dev = bp_<double>(h, mld_gpu_handle::B_WSERVE);
   return MLD_OK;
+}
+
+// ---- evaluation with fitted weights, without design rows (bispectrum.cu eval mode, eval.cu) ----
+// Weights of the reference's full layout [w0, w_lin (KK), W (KK x KK, quadratic)] are kept on
+// the device as w_lin (FP64), w_lin in the descriptor precision, and Wsym = W + W^T (FP64).
+int eval_weights_upload(mld_gpu_handle* h, const double* w_full) {
+  if (h->krr) return fail(h, MLD_ERR_UNSUPPORTED, "evaluation without design rows covers ml_type 0 only");
+  const int KK = h->KK;
+  const size_t n2 = h->quad ? (size_t)KK * KK : 0;
+  std::vector<double> hw((size_t)KK + n2);
+  std::copy(w_full + 1, w_full + 1 + KK, hw.begin());
+  if (h->quad) {
+    const double* W = w_full + 1 + KK;
+    for (int i = 0; i < KK; ++i)
+      for (int j = 0; j < KK; ++j) hw[KK + (size_t)i * KK + j] = W[(size_t)i * KK + j] + W[(size_t)j * KK + i];
+  }
+  const size_t eb = h->mixed ? sizeof(float) : sizeof(double);
+  CK(ensure(h, mld_gpu_handle::B_EW, sizeof(double) * hw.size() + eb * KK + 256));
+  double* dw = bp_<double>(h, mld_gpu_handle::B_EW);
+  CK(cudaMemcpyAsync(dw, hw.data(), sizeof(double) * hw.size(), cudaMemcpyHostToDevice, h->st));
+  void* wt = dw + hw.size();
+  if (h->mixed) {
+    std::vector<float> f(w_full + 1, w_full + 1 + KK);
+    CK(cudaMemcpyAsync(wt, f.data(), sizeof(float) * KK, cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  } else {
+    CK(cudaMemcpyAsync(wt, w_full + 1, sizeof(double) * KK, cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  h->ew0 = w_full[0];
+  h->ew_ready = true;
+  return MLD_OK;
+}
+
+template <typename T>
+static int eval_run(mld_gpu_handle* h, double* out) {
+  const int KK = h->KK;
+  double* E = out;
+  double* F = out + h->S;
+  double* S = F + 3 * (size_t)h->A;
+  const double* wlin = bp_<double>(h, mld_gpu_handle::B_EW);
+  const double* wsym = wlin + KK;
+  const T* wlinT = reinterpret_cast<const T*>(wlin + KK + (h->quad ? (size_t)KK * KK : 0));
+  size_t ysb = 0;
+  void* ys = nullptr;
+  int rc = y_scratch<T>(h, &ys, &ysb);
+  if (rc) return rc;
+  DevRows none{};
+  DevEval<T> ev;
+  ev.F = F;
+  ev.S = S;
+  ev.w0 = h->ew0;
+  if (h->quad) {
+    // pass 1: B of every atom; beta_a and the energies; pass 2: forces and stress
+    CK(ensure(h, mld_gpu_handle::B_EB, sizeof(T) * std::max<size_t>(1, (size_t)h->A * KK)));
+    CK(ensure(h, mld_gpu_handle::B_EBETA, sizeof(T) * std::max<size_t>(1, (size_t)h->A * KK)));
+    T* B = bp_<T>(h, mld_gpu_handle::B_EB);
+    T* beta = bp_<T>(h, mld_gpu_handle::B_EBETA);
+    CK(launch_bso4_rows<T>(h->dt, h->b, none, h->bp, (T*)nullptr, B, (T*)nullptr, 0, h->st, ys, ysb));
+    CK(launch_eval_beta<T>(B, h->A, KK, wlin, wsym, h->ew0, h->b.atom_struct, beta, E, h->st));
+    ev.beta = beta;
+    ev.beta_per_atom = 1;
+    CK(launch_bso4_rows<T>(h->dt, h->b, none, h->bp, (T*)nullptr, (T*)nullptr, (T*)nullptr, 0, h->st, ys, ysb, &ev));
+    nl(h, 3);
+  } else {
+    ev.beta = wlinT;
+    ev.beta_per_atom = 0;
+    ev.wlin = wlin;
+    ev.E = E;
+    CK(launch_bso4_rows<T>(h->dt, h->b, none, h->bp, (T*)nullptr, (T*)nullptr, (T*)nullptr, 0, h->st, ys, ysb, &ev));
+    nl(h, 1);
+  }
+  return MLD_OK;
+}
+
+// Queue the evaluation of the staged batch on the handle's stream: outputs [E (S) | F (3A) |
+// S (6S)] in FP64 in B_EOUT and, when `pinned_out` is given, copied into a pinned host buffer;
+// `done` (optional) is recorded after the copy.
+int eval_launch(mld_gpu_handle* h, cudaEvent_t done, double** pinned_out) {
+  if (!h->ew_ready) return fail(h, MLD_ERR_STATE, "evaluation weights not uploaded");
+  int rc = build_neighbours(h);
+  if (rc) return rc;
+  const size_t nout = (size_t)h->S + 3 * (size_t)h->A + 6 * (size_t)h->S;
+  CK(ensure(h, mld_gpu_handle::B_EOUT, sizeof(double) * std::max<size_t>(nout, 1)));
+  double* out = bp_<double>(h, mld_gpu_handle::B_EOUT);
+  CK(cudaMemsetAsync(out, 0, sizeof(double) * nout, h->st));
+  rc = h->mixed ? eval_run<float>(h, out) : eval_run<double>(h, out);
+  if (rc) return rc;
+  if (pinned_out) {
+    if (nout > h->pinned_cap) {
+      if (h->pinned) cudaFreeHost(h->pinned);
+      h->pinned = nullptr;
+      h->pinned_cap = 0;
+      CK(cudaMallocHost(&h->pinned, sizeof(double) * std::max<size_t>(nout, 1)));
+      h->pinned_cap = std::max<size_t>(nout, 1);
+    }
+    CK(cudaMemcpyAsync(h->pinned, out, sizeof(double) * nout, cudaMemcpyDeviceToHost, h->st));
+    *pinned_out = h->pinned;
+  }
+  if (done) CK(cudaEventRecord(done, h->st));
+  return MLD_OK;
+}
+
+void eval_collect(const mld_gpu_handle* h, int s, double* E, double* F, double* Sout) {
+  const double* hp = h->pinned;
+  const int a0 = h->h_atom_start[s], nat = h->h_atom_start[s + 1] - a0;
+  if (E) *E = hp[s];
+  if (F)
+    for (int i = 0; i < 3 * nat; ++i) F[i] = hp[h->S + 3 * (size_t)a0 + i];
+  if (Sout)
+    for (int k = 0; k < 6; ++k) Sout[k] = hp[h->S + 3 * (size_t)h->A + 6 * (size_t)s + k];
 }
 
 cudaStream_t handle_stream(const mld_gpu_handle* h) { return h->st; }

@@ -261,6 +261,8 @@ struct KernelArgs {
   // Y (the contracted Z blocks, nch * NYP complex per atom) in global memory, one slice per CTA,
   // when it does not fit in shared memory next to the rest (FP64 with several channels)
   void* yglobal;
+  // evaluation with fitted weights (eF != nullptr): no design rows
+  DevEval<T> ev;
 };
 
 constexpr int kNW = 8;           // warps per CTA (kNW*32 == kZThreads)
@@ -308,7 +310,8 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
     const long long rE = args.want_rows ? args.rowE[s] : -1;
     const long long rF = args.want_rows ? args.rowF[s] : -1;
     const long long rS = args.want_rows ? args.rowS[s] : -1;
-    const bool need_d = (dBout != nullptr) || rF >= 0 || rS >= 0;
+    const bool eval = args.ev.F != nullptr;
+    const bool need_d = (dBout != nullptr) || rF >= 0 || rS >= 0 || eval;
     const int a0 = args.atom_start[s];
     const int ldx = args.ldx;
 
@@ -410,6 +413,14 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
       if (Bout) Bout[(size_t)atom * nch * K + e] = b;
       if (rE >= 0) atomicAdd(&X[rE * ldx + 1 + e], b);
     }
+    if (args.ev.E && args.ev.wlin && warp == 0) {
+      // linear model: E_s += w0 + w_lin . B_a (FP64)
+      double e = 0.0;
+      if (nn > 0)
+        for (int k = lane; k < nch * K; k += 32) e += args.ev.wlin[k] * (double)Bk[k];
+      for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+      if (lane == 0) atomicAdd(&args.ev.E[s], e + args.ev.w0);
+    }
     if (!need_d || nn == 0) {
       __syncthreads();
       continue;
@@ -461,11 +472,12 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
           const int j = tile >> 8, rt = tile & 255;
           const int Mp = tb.Mp[j], H = tb.hoff[j + 1] - tb.hoff[j];
           const cx<T>* Yp = Yc + tb.yoff[j] + rt * kRowTile;
-          const int c0 = ct * kColTile;
+          // columns ct, ct + ncolt, ...: lanes of a warp read consecutive columns of V, whose odd
+          // stride HU spreads them over distinct shared-memory banks
           const cx<T>* Vp[kColTile];
 #pragma unroll
           for (int c = 0; c < kColTile; ++c) {
-            const int col = min(c0 + c, ncols - 1);
+            const int col = min(ct + c * ncolt, ncols - 1);
             Vp[c] = V + (size_t)col * HU + tb.hoff[j];  // col = n*3 + a -> V[n][a][.]
           }
           T acc[kRowTile][kColTile];
@@ -491,10 +503,49 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
             if (k < 0) continue;
 #pragma unroll
             for (int c = 0; c < kColTile; ++c)
-              if (c0 + c < ncols) atomicAdd(&dBs[(c0 + c) * K + k], acc[r][c]);
+              if (ct + c * ncolt < ncols) atomicAdd(&dBs[(ct + c * ncolt) * K + k], acc[r][c]);
           }
         }
         __syncthreads();
+        if (eval) {
+          // forces and stress with the effective weights: the centre's for the forces, the
+          // neighbour's for the stress (the neighbour's B in the quadratic stress rows,
+          // mld_stress.F90:580-603); sums per (neighbour, component) in T, totals in FP64
+          double* acc = reinterpret_cast<double*>(stacc);  // [0..2] self force, [3..8] stress
+          const T* bc = args.ev.beta + (args.ev.beta_per_atom ? (size_t)atom * nch * K : 0) + ch * K;
+          for (int it = tid; it < 3 * nb_here; it += nth) {
+            const int n = it / 3, a = it - 3 * n;
+            const T* d = dBs + (size_t)(n * 3 + a) * K;
+            T f = T(0);
+            for (int k = 0; k < K; ++k) f = fma(d[k], bc[k], f);
+            const T wn = nwt[ch * NB + n];
+            const double fv = (double)(f * wn);
+            atomicAdd(&args.ev.F[3 * (size_t)nidx[n] + a], -fv);
+            atomicAdd(&acc[a], fv);
+            if (args.ev.S) {
+              T g = f;
+              if (args.ev.beta_per_atom) {
+                const T* bn = args.ev.beta + (size_t)nidx[n] * nch * K + ch * K;
+                g = T(0);
+                for (int k = 0; k < K; ++k) g = fma(d[k], bn[k], g);
+              }
+              const double gv = (double)(g * wn) * (double)nuu[n * 4 + 3];
+              const double ux = nuu[n * 4 + 0], uy = nuu[n * 4 + 1], uz = nuu[n * 4 + 2];
+              if (a == 0) {  // xx, xz, xy
+                atomicAdd(&acc[3], gv * ux);
+                atomicAdd(&acc[7], gv * uz);
+                atomicAdd(&acc[8], gv * uy);
+              } else if (a == 1) {  // yy, yz
+                atomicAdd(&acc[4], gv * uy);
+                atomicAdd(&acc[6], gv * uz);
+              } else {  // zz
+                atomicAdd(&acc[5], gv * uz);
+              }
+            }
+          }
+          __syncthreads();
+          continue;
+        }
         // scatter: neighbour force rows (atomic), self force and stress accumulators
         for (int it = tid; it < 3 * K; it += nth) {
           const int a = it / K, k = it - a * K;
@@ -523,6 +574,16 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
         }
         __syncthreads();
       }
+    }
+    if (eval) {
+      const double* acc = reinterpret_cast<const double*>(stacc);
+      if (tid < 3) atomicAdd(&args.ev.F[3 * (size_t)atom + tid], acc[tid]);
+      if (args.ev.S && tid >= 32 && tid < 38) {
+        const double sc = args.p.sign_stress * 3.0 / args.volume[s];
+        atomicAdd(&args.ev.S[6 * (size_t)s + tid - 32], sc * acc[3 + tid - 32]);
+      }
+      __syncthreads();
+      continue;
     }
     // flush self force row and stress rows
     for (int ch = 0; ch < nch; ++ch) {
@@ -574,7 +635,8 @@ size_t bso4_y_scratch_bytes(const DevTables& tb, int nch, int eb, int max_ctas) 
 
 template <typename T>
 cudaError_t launch_bso4_rows(const DevTables& tb, const DevBatch& b, const DevRows& rows, const BsoParams& p, T* X,
-                             T* Bout, T* dBout, int want_rows, cudaStream_t st, void* yscratch, size_t yscratch_bytes) {
+                             T* Bout, T* dBout, int want_rows, cudaStream_t st, void* yscratch, size_t yscratch_bytes,
+                             const DevEval<T>* ev) {
   const int NB = kNW * (32 / kG3);
   if (b.A == 0) return cudaSuccess;
   KernelArgs<T> a{};
@@ -602,6 +664,7 @@ cudaError_t launch_bso4_rows(const DevTables& tb, const DevBatch& b, const DevRo
   a.want_rows = want_rows;
   a.NB = NB;
   a.p = p;
+  if (ev) a.ev = *ev;
   const bool y_in_smem = smem_bytes(tb, p.nch, sizeof(T), NB, true) <= (size_t)max_optin_smem();
   size_t smem = smem_bytes(tb, p.nch, sizeof(T), NB, y_in_smem);
   a.yglobal = nullptr;
@@ -628,8 +691,10 @@ cudaError_t launch_bso4_rows(const DevTables& tb, const DevBatch& b, const DevRo
 }
 
 template cudaError_t launch_bso4_rows<double>(const DevTables&, const DevBatch&, const DevRows&, const BsoParams&,
-                                              double*, double*, double*, int, cudaStream_t, void*, size_t);
+                                              double*, double*, double*, int, cudaStream_t, void*, size_t,
+                                              const DevEval<double>*);
 template cudaError_t launch_bso4_rows<float>(const DevTables&, const DevBatch&, const DevRows&, const BsoParams&,
-                                             float*, float*, float*, int, cudaStream_t, void*, size_t);
+                                             float*, float*, float*, int, cudaStream_t, void*, size_t,
+                                             const DevEval<float>*);
 
 }  // namespace mld

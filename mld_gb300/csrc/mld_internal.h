@@ -193,10 +193,28 @@ cudaError_t launch_scan(const int* in, int* out, int n, int* d_tmp, cudaStream_t
 // Y scratch the descriptor kernel needs in global memory for up to max_ctas CTAs (0 when Y fits
 // in shared memory); pass it to launch_bso4_rows, which then runs that many persistent CTAs.
 size_t bso4_y_scratch_bytes(const DevTables& tb, int nch, int eb, int max_ctas);
+// Evaluation with fitted weights instead of design rows: the energy, forces and stress that
+// the rows times the weights would give, formed from the per-atom effective weights
+// beta_a = dE/dB_a (w_lin for the linear model; w_lin + (W + W^T) B_a for the quadratic one).
+template <typename T>
+struct DevEval {
+  const T* beta = nullptr;       // one vector (nch*K) or one per atom (A x nch*K)
+  int beta_per_atom = 0;
+  const double* wlin = nullptr;  // linear weights: the kernel adds w0 + w_lin . B_a to E (linear model)
+  double w0 = 0.0;
+  double* F = nullptr;           // 3A forces, accumulated (zeroed by the caller)
+  double* S = nullptr;           // 6S stress rows' predictions, accumulated
+  double* E = nullptr;           // S energies, accumulated
+};
+
 template <typename T>
 cudaError_t launch_bso4_rows(const DevTables& tb, const DevBatch& b, const DevRows& rows, const BsoParams& p,
                              T* X, T* Bout, T* dBout, int want_rows, cudaStream_t st, void* yscratch = nullptr,
-                             size_t yscratch_bytes = 0);
+                             size_t yscratch_bytes = 0, const DevEval<T>* ev = nullptr);
+// beta_a = w_lin + Wsym B_a and E_s += sum_a (w0 + B_a . (beta_a + w_lin) / 2)   (eval.cu)
+template <typename T>
+cudaError_t launch_eval_beta(const T* B, int A, int nchK, const double* wlin, const double* wsym, double w0,
+                             const int* atom_struct, T* beta, double* E, cudaStream_t st);
 
 template <typename T>
 cudaError_t launch_gram(const T* X, int ldx, const double* w, const double* y, long long M, int D, double* G,

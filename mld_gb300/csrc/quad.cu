@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(256) k_quad_force(
     const int* __restrict__ nbr_off, const int* __restrict__ nbr_idx, const double* __restrict__ nbr_u,
     const int* __restrict__ rev, const int* __restrict__ small, double sign_big, const T* __restrict__ B,
     const T* __restrict__ dB, const long long* __restrict__ rowF, T* __restrict__ X, int ldx, int qoff,
-    T* __restrict__ H) {
+    T* __restrict__ H, int maxnn) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int a = blockIdx.x;
   if (a >= A) return;
@@ -70,22 +70,35 @@ __global__ void __launch_bounds__(256) k_quad_force(
   const int KP = (KK + kQT - 1) / kQT * kQT;
   T* G = reinterpret_cast<T*>(smem_raw);        // kQC * 3 * KP
   T* Bc = G + kQC * 3 * KP;                      // kQC * KP
+  T* fac = Bc + kQC * KP;                        // maxnn * 3: lever-arm factors of the reverse pairs
+  int* qrev = reinterpret_cast<int*>(fac + 3 * (size_t)maxnn);  // maxnn
   const int tid = threadIdx.x, nth = blockDim.x;
 
-  // stress partials of atom a (as the neighbour of its neighbours' pairs)
+  // stress partials of atom a (as the neighbour of its neighbours' pairs); the FP64 geometry of
+  // each reverse pair is reduced to three factors once
   if (H) {
     const double sg = small[s] ? 1.0 : -sign_big;
+    for (int n = tid; n < nn; n += nth) {
+      const int q = rev[p0 + n];
+      qrev[n] = q;
+      if (q >= 0) {
+        const double* u = nbr_u + 3 * (size_t)q;
+        const double f = sg / sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+        fac[3 * n + 0] = (T)(f * u[0]);
+        fac[3 * n + 1] = (T)(f * u[1]);
+        fac[3 * n + 2] = (T)(f * u[2]);
+      }
+    }
+    __syncthreads();
     for (int e = tid; e < 6 * KK; e += nth) {
       const int sidx = e / KK, k = e - sidx * KK;
       const int aa = sidx < 3 ? sidx : (sidx == 3 ? 1 : 0);
       const int bb = sidx < 3 ? sidx : (sidx == 5 ? 1 : 2);
       T acc = T(0);
       for (int n = 0; n < nn; ++n) {
-        const int q = rev[p0 + n];
+        const int q = qrev[n];
         if (q < 0) continue;
-        const double* u = nbr_u + 3 * (size_t)q;
-        const double r = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
-        acc += dB[((size_t)q * 3 + aa) * KK + k] * (T)(sg * u[bb] / r);
+        acc = fma(dB[((size_t)q * 3 + aa) * KK + k], fac[3 * n + bb], acc);
       }
       H[((size_t)a * 6 + sidx) * KK + k] = acc;
     }
@@ -275,11 +288,12 @@ cudaError_t launch_quad_rows(const DevBatch& b, const DevRows& rows, const BsoPa
                              const T* B, const T* dB, T* H, T* X, int qoff, cudaStream_t st) {
   if (b.A == 0) return cudaSuccess;
   const int KP = (KK + kQT - 1) / kQT * kQT;
-  size_t sm1 = sizeof(T) * (size_t)kQC * 4 * KP;
+  const int mnn = std::max(1, b.maxnn);
+  size_t sm1 = sizeof(T) * ((size_t)kQC * 4 * KP + 3 * (size_t)mnn) + sizeof(int) * (size_t)mnn + 16;
   cudaError_t e = cudaFuncSetAttribute(k_quad_force<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
   if (e != cudaSuccess) return e;
   k_quad_force<T><<<b.A, 256, sm1, st>>>(b.A, KK, b.atom_struct, b.atom_start, b.nbr_off, b.nbr_idx, b.nbr_u, rev,
-                                         b.small, p.sign_big, B, dB, rows.rowF, X, rows.ldx, qoff, H);
+                                         b.small, p.sign_big, B, dB, rows.rowF, X, rows.ldx, qoff, H, mnn);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   size_t sm2 = sizeof(T) * (size_t)2 * 32 * KP;

@@ -26,9 +26,9 @@
 #include "mld_internal.h"
 
 namespace mld {
-int predict_launch(mld_gpu_handle* h, const double* w_dev, cudaEvent_t done, double** pinned_out);
-void predict_collect(const mld_gpu_handle* h, int s, double* E, double* F, double* Sout);
-int upload_weights(mld_gpu_handle* h, const double* w_full, double** w_dev);
+int eval_launch(mld_gpu_handle* h, cudaEvent_t done, double** pinned_out);
+void eval_collect(const mld_gpu_handle* h, int s, double* E, double* F, double* Sout);
+int eval_weights_upload(mld_gpu_handle* h, const double* w_full);
 int handle_dims(const mld_gpu_handle* h, int* D, int* ldx, int* KK, int* nch);
 }  // namespace mld
 
@@ -54,7 +54,6 @@ struct Request {
 
 struct Slot {
   mld_gpu_handle* h = nullptr;
-  double* w_dev = nullptr;
   cudaEvent_t done = nullptr;
   std::vector<long long> batch;
   bool busy = false;
@@ -82,8 +81,9 @@ int sfail(mld_gpu_server* s, int code, const std::string& msg) {
   return code;
 }
 
-// device bytes of one structure's batch buffers: design rows, descriptor derivatives and
-// neighbour pairs (expected neighbours from the number density within r_cut, 1.5x margin)
+// device bytes of one structure's batch buffers: neighbour pairs (expected neighbours from the
+// number density within r_cut, 1.5x margin), per-atom descriptors and effective weights, the
+// FP64 outputs (evaluation without design rows)
 double request_bytes(const mld_gpu_server* s, int nat, const double* cell) {
   const double* c = cell;
   const double vol = std::fabs(c[0] * (c[4] * c[8] - c[5] * c[7]) - c[1] * (c[3] * c[8] - c[5] * c[6]) +
@@ -91,9 +91,8 @@ double request_bytes(const mld_gpu_server* s, int nat, const double* cell) {
   const double rc = s->cfg.r_cut;
   const double nn = std::min<double>(s->cfg.imm_neigh, 1.5 * nat / std::max(vol, 1e-9) * 4.18879 * rc * rc * rc + 8);
   const double eb = s->cfg.precision == MLD_PRECISION_MIXED ? 4.0 : 8.0;
-  const double rows = 1.0 + 3.0 * nat + 6.0;
   const double pairs = nat * nn;
-  return rows * s->ldx * eb + pairs * (3.0 * s->KK * eb + 36.0) + nat * (s->KK * eb + 64.0) + rows * 32.0;
+  return pairs * 36.0 + nat * (2.0 * s->KK * eb + 24.0 + 64.0) + 128.0;
 }
 
 void retire(mld_gpu_server* s, Slot& sl) {
@@ -104,7 +103,7 @@ void retire(mld_gpu_server* s, Slot& sl) {
     Request& r = s->reqs[sl.batch[i]];
     if (q == cudaSuccess) {
       r.F.assign(3 * (size_t)r.nat, 0.0);
-      mld::predict_collect(sl.h, (int)i, &r.E, r.F.data(), r.S);
+      mld::eval_collect(sl.h, (int)i, &r.E, r.F.data(), r.S);
       r.state = 2;
       s->atoms_done += r.nat;
     } else {
@@ -158,7 +157,7 @@ int launch(mld_gpu_server* s, Slot& sl) {
   }
   int rc = mld_gpu_set_structures(sl.h, (int)batch.size(), nat.data(), pos.data(), cell.data(), types.data());
   double* pinned = nullptr;
-  if (rc == MLD_OK) rc = mld::predict_launch(sl.h, sl.w_dev, sl.done, &pinned);
+  if (rc == MLD_OK) rc = mld::eval_launch(sl.h, sl.done, &pinned);
   if (rc != MLD_OK) {
     s->err = mld_gpu_last_error(sl.h);
     const double t = now_ms();
@@ -201,7 +200,7 @@ int mld_gpu_server_create(const mld_gpu_config* cfg, const double* w_params, int
       mld_gpu_server_destroy(s);
       return MLD_ERR_CUDA;
     }
-    rc = mld::upload_weights(sl.h, w_params, &sl.w_dev);
+    rc = mld::eval_weights_upload(sl.h, w_params);
     s->slots.push_back(sl);
     if (rc != MLD_OK) {
       mld_gpu_server_destroy(s);

@@ -43,7 +43,7 @@ module mld_gpu_mod
 
   public :: mld_gpu_config_defaults, mld_gpu_create, mld_gpu_destroy, mld_gpu_dims, &
             mld_gpu_set_structures, mld_gpu_set_labels, mld_gpu_descriptors, mld_gpu_num_rows, &
-            mld_gpu_design_matrix, mld_gpu_gram, mld_gpu_solve, mld_gpu_fit, mld_gpu_predict, &
+            mld_gpu_design_matrix, mld_gpu_gram, mld_gpu_solve, mld_gpu_fit, mld_gpu_predict, mld_gpu_evaluate, &
             mld_gpu_set_kernel_points, mld_gpu_solve_info, mld_gpu_gram_rows, &
             mld_gpu_server_create, mld_gpu_server_destroy, mld_gpu_server_submit, &
             mld_gpu_server_progress, mld_gpu_server_result, mld_gpu_server_wait, mld_gpu_server_stats, &
@@ -122,6 +122,11 @@ module mld_gpu_mod
     end function
 
     integer(c_int) function mld_gpu_predict(h, w_params, e, f, s) bind(C, name="mld_gpu_predict")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h, w_params, e, f, s
+    end function
+
+    integer(c_int) function mld_gpu_evaluate(h, w_params, e, f, s) bind(C, name="mld_gpu_evaluate")
       import :: c_int, c_ptr
       type(c_ptr), value :: h, w_params, e, f, s
     end function

@@ -82,8 +82,10 @@ def test_fit19_three_channel_descriptors(lib, fit19, precision, tol):
 
 @pytest.mark.parametrize("fit", ["fit03", "fit08"])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_reference_run_predictions(lib, predictions, fit, precision):
-    """mld_gpu_predict with a reference run's .pot weights reproduces that run's train_*.out."""
+@pytest.mark.parametrize("evaluate", [False, True])
+def test_reference_run_predictions(lib, predictions, fit, precision, evaluate):
+    """mld_gpu_predict (design rows x weights) and mld_gpu_evaluate (no rows) with a reference
+    run's .pot weights reproduce that run's train_*.out."""
     from mld_gb300 import _lib
     from conftest import channel_weights_for
     d = predictions
@@ -102,7 +104,7 @@ def test_reference_run_predictions(lib, predictions, fit, precision):
         h.set_structures(nat, np.concatenate([d[f"{fit}_pos_{i}"] for i in range(n)]),
                          np.stack([d[f"{fit}_cell_{i}"] for i in range(n)]),
                          np.concatenate([d[f"{fit}_types_{i}"] for i in range(n)]))
-        E, F, S = h.predict(d[f"{fit}_w"])
+        E, F, S = h.evaluate(d[f"{fit}_w"]) if evaluate else h.predict(d[f"{fit}_w"])
     # plain: the printed precision of es20.10; mixed: FP32 descriptors and rows
     tol = 1e-9 if precision == 0 else 2e-4
     scaleE = max(np.abs([d[f"{fit}_E_{i}"][0] for i in range(n)]).max(), 1.0)
@@ -250,3 +252,33 @@ def test_neighbour_cap_is_reported(lib):
     # the handle stays usable after the error
     c2 = _lib.default_config()
     h.close()
+
+
+@pytest.mark.parametrize("order,j_max", [(1, 4.0), (2, 2.0), (2, 4.0)])
+@pytest.mark.parametrize("precision,tol", [(0, 1e-10), (1, 2e-5)])
+def test_evaluate_matches_predict(lib, order, j_max, precision, tol):
+    """Evaluation without design rows equals rows x weights (both box branches, two channels)."""
+    from mld_gb300 import _lib, synth
+    ds = synth.hea_bcc_batched(n_struct=5, reps=3, seed=31)
+    structs = list(ds.structures) + list(synth.fe_bcc_batched(n_struct=3, nmin=2, nmax=40, seed=3).structures)
+    c = _lib.default_config()
+    c.j_max, c.r_cut, c.precision, c.mld_order, c.lambda_krr = j_max, 4.7, precision, order, 1e-6
+    c.weighted, c.n_elements = 1, len(synth.HEA_ELEMENTS)
+    for i, wv in enumerate(synth.HEA_WEIGHTS):
+        c.weight_per_element[i] = wv
+    sub = synth.Dataset(structs, 4.7, "mix")
+    nat, pos, cell, types = sub.arrays()
+    with _lib.Handle(c) as h:
+        h.set_structures(nat, pos, cell, types)
+        rng = np.random.default_rng(7)
+        w = rng.standard_normal(h.dim_design_line) * 1e-3
+        if order == 2:
+            # full layout 1 + KK + KK^2: a symmetric quadratic block as a fit produces
+            KK = int(round((-1 + np.sqrt(1 + 4 * (h.dim_design_line - 1))) / 2))
+            Wq = rng.standard_normal((KK, KK)) * 1e-5
+            w = np.concatenate([rng.standard_normal(1 + KK) * 1e-3, ((Wq + Wq.T) / 2).reshape(-1)])
+        E0, F0, S0 = h.predict(w)
+        E1, F1, S1 = h.evaluate(w)
+    assert _rel(E1, E0) < tol
+    assert _rel(F1, F0) < tol
+    assert _rel(S1, S0) < tol
