@@ -374,33 +374,38 @@ __global__ void __launch_bounds__(256) k_xtv_ds(const float* __restrict__ X, int
 // ------------------------------------------------------------------------------------
 // Normal-equation matvec of a wide block (D > 256) in one pass over X.  Design rows stream
 // through a ring of shared-memory stages by 1-D bulk copies issued from one producer thread.
-// Eight consumer warps own the columns c = tid + 256 j (j < CPT).  Per step of kWRows rows:
+// Sixteen consumer warps own the columns c = tid + 512 j (j < CPT).  Per step of kWRows rows:
 //   * each thread forms FP32 partial dots of its columns with p (rounded to FP32);
-//   * warps reduce them, one warp per row sums the eight warp partials in FP64 and scales by
+//   * warps reduce them, one warp per row sums the sixteen warp partials in FP64 and scales by
 //     w_r, giving t_r = w_r (x_r . p);
 //   * each thread adds x_rc t_r to FP32 column sums, which are moved into FP64 sums every
 //     kWFlushSteps steps.
-// FP32 arithmetic on chunks (24 columns of a dot, 8 rows of a column sum) with FP64 between
-// chunks keeps the relative error near 1e-7 at about three FP32 operations per element, so
-// the pass runs at HBM speed.  The blocks that take this path (quadratic and kernel columns)
-// are so ill-conditioned that the iteration stops at relative residuals far above 1e-7; the
-// narrow linear blocks keep double-FP32 (k_normal_matvec_narrow).
+// FP32 arithmetic on chunks (12 columns of a dot, 8 rows of a column sum) with FP64 between
+// chunks keeps the relative error near 1e-7 at about three FP32 operations per element.  The
+// blocks that take this path (quadratic and kernel columns) are so ill-conditioned that the
+// iteration stops at relative residuals far above 1e-7; the narrow linear blocks keep
+// double-FP32 (k_normal_matvec_narrow).  A stage is `stride` floats, at least 512 * CPT past
+// the row's first column: the tail beyond the copied row stays zero, so the inner loops carry
+// no bounds tests (p is zero there and those column sums are dropped).
 // Every wait is bounded: on expiry the CTA sets *err and leaves the loop uniformly.
 // ------------------------------------------------------------------------------------
-constexpr int kWConsumers = 256;
+constexpr int kWConsumers = 512;
+constexpr int kWWarps = kWConsumers / 32;
 constexpr int kWRows = 4;        // design rows per consumer step
 constexpr int kWFlushSteps = 2;  // steps between FP32 -> FP64 moves of the column sums
+constexpr int kWMaxStages = 16;
+constexpr int kWChunks = 8;      // bulk copies per design row
 constexpr int kWThreads = kWConsumers + 32;
 
 template <int CPT>
 __global__ void __launch_bounds__(kWThreads, 1)
     k_normal_matvec_wide(const float* __restrict__ X, long long ldx, int c0, int D, const float2* __restrict__ wds,
-                         const double* __restrict__ p, long long M, long long rpb, int rowf, int stages,
+                         const double* __restrict__ p, long long M, long long rpb, int rowf, int stride, int stages,
                          double* __restrict__ q, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char wsm[];
-  float* rows = reinterpret_cast<float*>(wsm);                              // stages * rowf
-  double* part = reinterpret_cast<double*>(rows + (size_t)stages * rowf);   // stages * 8
-  double* tv = part + stages * 8;                                           // stages
+  float* rows = reinterpret_cast<float*>(wsm);                                 // stages * stride
+  double* part = reinterpret_cast<double*>(rows + (size_t)stages * stride);    // stages * kWWarps
+  double* tv = part + stages * kWWarps;                                        // stages
   uint64_t* full = reinterpret_cast<uint64_t*>(tv + stages);
   uint64_t* empty = full + stages;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -409,75 +414,82 @@ __global__ void __launch_bounds__(kWThreads, 1)
   const long long r0 = (long long)blockIdx.x * rpb;
   const long long nr = min(M, r0 + rpb) - r0;
   if (nr <= 0) return;
+  for (int e = tid; e < stages * stride; e += blockDim.x) rows[e] = 0.f;
   if (tid == 0) {
     for (int s = 0; s < stages; ++s) {
       ptx::mbar_init(&full[s], 1);
-      ptx::mbar_init(&empty[s], kWConsumers / 32);
+      ptx::mbar_init(&empty[s], kWWarps);
     }
     ptx::mbar_init_fence();
   }
+  // the zero tails must be visible to the async proxy before the first bulk copy lands
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   __syncthreads();
-  if (warp == kWConsumers / 32) {
-    // producer
-    if (lane == 0) {
-      long long issued = 0;
-      for (long long k = 0; k < nr; ++k) {
-        const int s = (int)(k % stages);
-        if (k >= stages && !ptx::mbar_wait(&empty[s], (uint32_t)(((k / stages) - 1) & 1))) {
-          atomicExch(err, 1);
-          break;
-        }
-        ptx::mbar_expect_tx(&full[s], bytes);
-        ptx::bulk_load(rows + (size_t)s * rowf, X + (r0 + k) * ldx + a0, bytes, &full[s]);
-        issued = k + 1;
+  if (warp == kWWarps) {
+    // producer warp: each row goes in kWChunks bulk copies issued by as many lanes, so that
+    // several copies per row are in flight at once
+    const uint32_t cb = ((bytes / kWChunks) + 15u) & ~15u;
+    long long issued = 0;
+    for (long long k = 0; k < nr; ++k) {
+      const int s = (int)(k % stages);
+      int okw = 1;
+      if (k >= stages && lane == 0) okw = ptx::mbar_wait(&empty[s], (uint32_t)(((k / stages) - 1) & 1)) ? 1 : 0;
+      okw = __shfl_sync(0xffffffffu, okw, 0);
+      if (!okw) {
+        if (lane == 0) atomicExch(err, 1);
+        break;
       }
+      if (lane == 0) ptx::mbar_expect_tx(&full[s], bytes);
+      __syncwarp();
+      const uint32_t o = (uint32_t)lane * cb;
+      if (lane < kWChunks && o < bytes)
+        ptx::bulk_load(reinterpret_cast<char*>(rows + (size_t)s * stride) + o,
+                       reinterpret_cast<const char*>(X + (r0 + k) * ldx + a0) + o, min(cb, bytes - o), &full[s]);
+      issued = k + 1;
+    }
+    if (lane == 0)
       for (long long k = max(0LL, issued - stages); k < issued; ++k)
         ptx::mbar_wait(&full[k % stages], (uint32_t)((k / stages) & 1));
-    }
     return;
   }
   // consumers
   float pf[CPT], acc[CPT];
   double acc64[CPT];
 #pragma unroll
-  for (int k = 0; k < CPT; ++k) {
-    const int c = tid + kWConsumers * k;
-    pf[k] = c < D ? (float)p[c] : 0.f;
-    acc[k] = 0.f;
-    acc64[k] = 0.0;
+  for (int j = 0; j < CPT; ++j) {
+    const int c = tid + kWConsumers * j;
+    pf[j] = c < D ? (float)p[c] : 0.f;
+    acc[j] = 0.f;
+    acc64[j] = 0.0;
   }
   long long step = 0;
   for (long long k = 0; k < nr; k += kWRows, ++step) {
     const int nv = (int)min((long long)kWRows, nr - k);
-    int sr[kWRows];
+    // the row weight this warp needs after the barrier, loaded before the dots
+    const float2 wv = warp < nv ? wds[r0 + k + warp] : make_float2(0.f, 0.f);
+    const float* rp[kWRows];
     bool ok = true;
 #pragma unroll
     for (int r = 0; r < kWRows; ++r) {
-      sr[r] = (int)((k + r) % stages);
-      if (r < nv) ok = ok && ptx::mbar_wait(&full[sr[r]], (uint32_t)(((k + r) / stages) & 1));
+      const int s = (int)((k + r) % stages);
+      rp[r] = rows + s * stride + off + tid;
+      if (r < nv) ok = ok && ptx::mbar_wait(&full[s], (uint32_t)(((k + r) / stages) & 1));
     }
     float d[kWRows];
 #pragma unroll
     for (int r = 0; r < kWRows; ++r) d[r] = 0.f;
     if (ok) {
 #pragma unroll
-      for (int j = 0; j < CPT; ++j) {
-        const int c = tid + kWConsumers * j;
-        if (c < D) {
+      for (int j = 0; j < CPT; ++j)
 #pragma unroll
-          for (int r = 0; r < kWRows; ++r) {
-            const float v = r < nv ? rows[(size_t)sr[r] * rowf + off + c] : 0.f;
-            d[r] = fmaf(v, pf[j], d[r]);
-          }
-        }
-      }
+        for (int r = 0; r < kWRows; ++r) d[r] = fmaf(rp[r][kWConsumers * j], pf[j], d[r]);
     }
 #pragma unroll
     for (int r = 0; r < kWRows; ++r)
       for (int o = 16; o > 0; o >>= 1) d[r] += __shfl_xor_sync(0xffffffffu, d[r], o);
     if (lane == 0) {
 #pragma unroll
-      for (int r = 0; r < kWRows; ++r) part[sr[r] * 8 + warp] = (double)d[r];
+      for (int r = 0; r < kWRows; ++r) part[(int)((k + r) % stages) * kWWarps + warp] = (double)d[r];
     }
     int any_fail;
     asm volatile(
@@ -488,37 +500,27 @@ __global__ void __launch_bounds__(kWThreads, 1)
       if (tid == 0) atomicExch(err, 1);
       break;
     }
-    // warp r sums the eight slices of row r in FP64 and scales by w_r
-    if (warp < nv) {
+    // warp r sums the sixteen slices of row r in FP64 and scales by w_r
+    if (warp < kWRows) {
       const int sw = (int)((k + warp) % stages);
-      double v = lane < 8 ? part[sw * 8 + lane] : 0.0;
-      for (int o = 4; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) {
-        const float2 wv = wds[r0 + k + warp];
-        tv[sw] = v * ((double)wv.x + (double)wv.y);
-      }
+      double v = (lane < kWWarps && warp < nv) ? part[sw * kWWarps + lane] : 0.0;
+      for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) tv[sw] = v * ((double)wv.x + (double)wv.y);
     }
     asm volatile("bar.sync 2, %0;\n" ::"n"(kWConsumers));
     float th[kWRows];
 #pragma unroll
-    for (int r = 0; r < kWRows; ++r) th[r] = r < nv ? (float)tv[sr[r]] : 0.f;
+    for (int r = 0; r < kWRows; ++r) th[r] = (float)tv[(int)((k + r) % stages)];
 #pragma unroll
-    for (int j = 0; j < CPT; ++j) {
-      const int c = tid + kWConsumers * j;
-      if (c < D) {
+    for (int j = 0; j < CPT; ++j)
 #pragma unroll
-        for (int r = 0; r < kWRows; ++r) {
-          const float v = r < nv ? rows[(size_t)sr[r] * rowf + off + c] : 0.f;
-          acc[j] = fmaf(v, th[r], acc[j]);
-        }
-      }
-    }
+      for (int r = 0; r < kWRows; ++r) acc[j] = fmaf(rp[r][kWConsumers * j], th[r], acc[j]);
     // every stage of this step is read: release them to the producer
     __syncwarp();
     if (lane == 0) {
 #pragma unroll
       for (int r = 0; r < kWRows; ++r)
-        if (r < nv) ptx::mbar_arrive(&empty[sr[r]]);
+        if (r < nv) ptx::mbar_arrive(&empty[(int)((k + r) % stages)]);
     }
     if ((step % kWFlushSteps) == kWFlushSteps - 1) {
 #pragma unroll
@@ -617,9 +619,13 @@ cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const d
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   }
-  const size_t per_stage = sizeof(float) * rowf + 9 * sizeof(double) + 2 * sizeof(uint64_t);
-  const int stages = (int)std::min<size_t>(8, ((size_t)optin - 256) / per_stage);
+  // columns per consumer thread of the wide kernel (instances 1, 2, 4, 8, 12, 16) and its stage
+  // stride: the copied row plus a zero tail up to the last column a thread reads
   const int cpt = (D + kWConsumers - 1) / kWConsumers;
+  const int cpti = cpt <= 1 ? 1 : cpt <= 2 ? 2 : cpt <= 4 ? 4 : cpt <= 8 ? 8 : cpt <= 12 ? 12 : 16;
+  const int stride = (std::max(rowf, (c0 - a0) + kWConsumers * cpti) + 3) & ~3;
+  const size_t per_stage = sizeof(float) * stride + (kWWarps + 1) * sizeof(double) + 2 * sizeof(uint64_t);
+  const int stages = (int)std::min<size_t>(kWMaxStages, ((size_t)optin - 256) / per_stage);
   if (M > 0 && D <= 256) {
     const long long rpb = rows_per_cta(M, 1, nsm);
     const unsigned nrb = (unsigned)((M + rpb - 1) / rpb);
@@ -634,17 +640,18 @@ cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const d
       default: k_normal_matvec_narrow<8><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
     }
     *launches = 1;
-  } else if (M > 0 && stages >= kWRows && (ldx % 4) == 0 && cpt <= 32) {
+  } else if (M > 0 && stages >= kWRows && (ldx % 4) == 0 && cpt <= 16) {
     const size_t smem = 256 + (size_t)stages * per_stage;
     const long long rpb = (M + nsm - 1) / nsm;
     const unsigned grid = (unsigned)((M + rpb - 1) / rpb);
-    auto kern = cpt <= 4 ? k_normal_matvec_wide<4>
-              : cpt <= 8 ? k_normal_matvec_wide<8>
-              : cpt <= 16 ? k_normal_matvec_wide<16>
-              : cpt <= 24 ? k_normal_matvec_wide<24> : k_normal_matvec_wide<32>;
+    auto kern = cpti == 1 ? k_normal_matvec_wide<1>
+              : cpti == 2 ? k_normal_matvec_wide<2>
+              : cpti == 4 ? k_normal_matvec_wide<4>
+              : cpti == 8 ? k_normal_matvec_wide<8>
+              : cpti == 12 ? k_normal_matvec_wide<12> : k_normal_matvec_wide<16>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<grid, kWThreads, smem, st>>>(X, ldx, c0, D, sv, p, M, rpb, rowf, stages, q, err);
+    kern<<<grid, kWThreads, smem, st>>>(X, ldx, c0, D, sv, p, M, rpb, rowf, stride, stages, q, err);
     *launches = 1;
   } else if (M > 0) {
     const size_t smem = sizeof(float) * 2 * (size_t)D;
