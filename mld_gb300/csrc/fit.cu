@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <type_traits>
 
+#include "ds.cuh"
 #include "mld_internal.h"
 #include "ptx.cuh"
 
@@ -178,45 +179,6 @@ __global__ void __launch_bounds__(256) k_xtv(const T* __restrict__ X, int ldx, i
   if (cb + threadIdx.x < D && sum != 0.0) atomicAdd(&q[cb + threadIdx.x], sum);
 }
 
-// ------------------------------------------------------------------------------------
-// Double-FP32 ("double-single") arithmetic for the refinement matvecs of the mixed method.
-// GB300 issues FP64 at 1/64 of its FP32 rate, so the FP64-accumulated products of the
-// refinement are formed from FP32 error-free transformations instead: TwoSum (Knuth) and
-// TwoProd via fmaf give sums and products as unevaluated pairs hi + lo, about 2^-44 relative
-// to the sum of the magnitudes.  X is FP32, so x * (p_hi + p_lo) is formed exactly up to the
-// x * p_lo term.
-// ------------------------------------------------------------------------------------
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-// (sh, sl) += x * (ph + pl)
-__device__ __forceinline__ void ds_fma(float& sh, float& sl, float x, float ph, float pl) {
-  const float p = x * ph;
-  const float pe = fmaf(x, pl, fmaf(x, ph, -p));
-  float t, e;
-  two_sum(sh, p, t, e);
-  sh = t;
-  sl += e + pe;
-}
-// (sh, sl) += (oh, ol)
-__device__ __forceinline__ void ds_add(float& sh, float& sl, float oh, float ol) {
-  float t, e;
-  two_sum(sh, oh, t, e);
-  sh = t;
-  sl += e + ol;
-}
-__device__ __forceinline__ void ds_norm(float& sh, float& sl) {
-  const float t = sh + sl;
-  sl = sl - (t - sh);
-  sh = t;
-}
-__device__ __forceinline__ void ds_split(double v, float& h, float& l) {
-  h = (float)v;
-  l = (float)(v - (double)h);
-}
-
 // Normal-equation matvec of a narrow block (D <= 32*NK <= 256) in one pass over X:
 // q = sum_r w[r] (x_r . p) x_r, the row held in registers between the dot and the update.
 template <int NK>
@@ -376,12 +338,13 @@ __global__ void __launch_bounds__(256) k_xtv_ds(const float* __restrict__ X, int
 // through a ring of shared-memory stages by 1-D bulk copies issued from one producer thread.
 // Sixteen consumer warps own the columns c = tid + 512 j (j < CPT).  Per step of kWRows rows:
 //   * each thread forms FP32 partial dots of its columns with p (rounded to FP32);
-//   * warps reduce them, one warp per row sums the sixteen warp partials in FP64 and scales by
-//     w_r, giving t_r = w_r (x_r . p);
-//   * each thread adds x_rc t_r to FP32 column sums, which are moved into FP64 sums every
-//     kWFlushSteps steps.
-// FP32 arithmetic on chunks (12 columns of a dot, 8 rows of a column sum) with FP64 between
-// chunks keeps the relative error near 1e-7 at about three FP32 operations per element.  The
+//   * warps reduce them, one warp per row sums the sixteen warp partials and scales by w_r,
+//     giving t_r = w_r (x_r . p);
+//   * each thread adds x_rc t_r to FP32 column sums, which are moved into double-FP32 sums
+//     (TwoSum) every kWFlushSteps steps.
+// FP32 arithmetic on chunks (12 columns of a dot, 8 rows of a column sum) with double-FP32
+// between chunks keeps the relative error near 1e-7 at about three FP32 operations per element
+// and leaves the FP64 pipe, 1/64 of the FP32 rate on this GPU, out of the loop.  The
 // blocks that take this path (quadratic and kernel columns) are so ill-conditioned that the
 // iteration stops at relative residuals far above 1e-7; the narrow linear blocks keep
 // double-FP32 (k_normal_matvec_narrow).  A stage is `stride` floats, at least 512 * CPT past
@@ -404,9 +367,9 @@ __global__ void __launch_bounds__(kWThreads, 1)
                          double* __restrict__ q, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char wsm[];
   float* rows = reinterpret_cast<float*>(wsm);                                 // stages * stride
-  double* part = reinterpret_cast<double*>(rows + (size_t)stages * stride);    // stages * kWWarps
-  double* tv = part + stages * kWWarps;                                        // stages
-  uint64_t* full = reinterpret_cast<uint64_t*>(tv + stages);
+  float* part = rows + (size_t)stages * stride;                                // stages * kWWarps
+  float* tv = part + stages * kWWarps;                                         // stages
+  uint64_t* full = reinterpret_cast<uint64_t*>(tv + stages + (stages & 1));
   uint64_t* empty = full + stages;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int a0 = c0 & ~3, off = c0 - a0;
@@ -453,14 +416,12 @@ __global__ void __launch_bounds__(kWThreads, 1)
     return;
   }
   // consumers
-  float pf[CPT], acc[CPT];
-  double acc64[CPT];
+  float pf[CPT], acc[CPT], sh[CPT], sl[CPT];
 #pragma unroll
   for (int j = 0; j < CPT; ++j) {
     const int c = tid + kWConsumers * j;
     pf[j] = c < D ? (float)p[c] : 0.f;
-    acc[j] = 0.f;
-    acc64[j] = 0.0;
+    acc[j] = sh[j] = sl[j] = 0.f;
   }
   long long step = 0;
   for (long long k = 0; k < nr; k += kWRows, ++step) {
@@ -489,7 +450,7 @@ __global__ void __launch_bounds__(kWThreads, 1)
       for (int o = 16; o > 0; o >>= 1) d[r] += __shfl_xor_sync(0xffffffffu, d[r], o);
     if (lane == 0) {
 #pragma unroll
-      for (int r = 0; r < kWRows; ++r) part[(int)((k + r) % stages) * kWWarps + warp] = (double)d[r];
+      for (int r = 0; r < kWRows; ++r) part[(int)((k + r) % stages) * kWWarps + warp] = d[r];
     }
     int any_fail;
     asm volatile(
@@ -500,17 +461,17 @@ __global__ void __launch_bounds__(kWThreads, 1)
       if (tid == 0) atomicExch(err, 1);
       break;
     }
-    // warp r sums the sixteen slices of row r in FP64 and scales by w_r
+    // warp r sums the sixteen slices of row r and scales by w_r
     if (warp < kWRows) {
       const int sw = (int)((k + warp) % stages);
-      double v = (lane < kWWarps && warp < nv) ? part[sw * kWWarps + lane] : 0.0;
+      float v = (lane < kWWarps && warp < nv) ? part[sw * kWWarps + lane] : 0.f;
       for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) tv[sw] = v * ((double)wv.x + (double)wv.y);
+      if (lane == 0) tv[sw] = v * wv.x + v * wv.y;
     }
     asm volatile("bar.sync 2, %0;\n" ::"n"(kWConsumers));
     float th[kWRows];
 #pragma unroll
-    for (int r = 0; r < kWRows; ++r) th[r] = (float)tv[(int)((k + r) % stages)];
+    for (int r = 0; r < kWRows; ++r) th[r] = tv[(int)((k + r) % stages)];
 #pragma unroll
     for (int j = 0; j < CPT; ++j)
 #pragma unroll
@@ -523,9 +484,13 @@ __global__ void __launch_bounds__(kWThreads, 1)
         if (r < nv) ptx::mbar_arrive(&empty[(int)((k + r) % stages)]);
     }
     if ((step % kWFlushSteps) == kWFlushSteps - 1) {
+      // chunk sums into double-FP32 column sums (TwoSum on the FP32 pipe)
 #pragma unroll
       for (int j = 0; j < CPT; ++j) {
-        acc64[j] += (double)acc[j];
+        float t, e;
+        two_sum(sh[j], acc[j], t, e);
+        sh[j] = t;
+        sl[j] += e;
         acc[j] = 0.f;
       }
     }
@@ -533,7 +498,7 @@ __global__ void __launch_bounds__(kWThreads, 1)
 #pragma unroll
   for (int j = 0; j < CPT; ++j) {
     const int c = tid + kWConsumers * j;
-    const double v = acc64[j] + (double)acc[j];
+    const double v = (double)sh[j] + (double)sl[j] + (double)acc[j];
     if (c < D && v != 0.0) atomicAdd(&q[c], v);
   }
 }
@@ -624,7 +589,7 @@ cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const d
   const int cpt = (D + kWConsumers - 1) / kWConsumers;
   const int cpti = cpt <= 1 ? 1 : cpt <= 2 ? 2 : cpt <= 4 ? 4 : cpt <= 8 ? 8 : cpt <= 12 ? 12 : 16;
   const int stride = (std::max(rowf, (c0 - a0) + kWConsumers * cpti) + 3) & ~3;
-  const size_t per_stage = sizeof(float) * stride + (kWWarps + 1) * sizeof(double) + 2 * sizeof(uint64_t);
+  const size_t per_stage = sizeof(float) * stride + (kWWarps + 2) * sizeof(float) + 2 * sizeof(uint64_t);
   const int stages = (int)std::min<size_t>(kWMaxStages, ((size_t)optin - 256) / per_stage);
   if (M > 0 && D <= 256) {
     const long long rpb = rows_per_cta(M, 1, nsm);

@@ -10,12 +10,13 @@
 //   A   = L L^T                       blocked right-looking Cholesky, 64-column panels
 //   R   = L^-1                        diagonal 64-blocks, then recursive doubling with GEMMs:
 //                                     R21 = -R22 (L21 R11)
-//   M^-1 r = S R^T R S r              two dense triangular matvecs, FP64 accumulation
+//   M^-1 r = S R^T R S r              two dense triangular matvecs, double-FP32 arithmetic
 // M^-1 is a fixed symmetric positive-definite operator (R and R^T hold the same FP32 numbers),
 // so the standard conjugate-gradient recurrences stay valid.
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "ds.cuh"
 #include "mld_internal.h"
 
 namespace mld {
@@ -227,30 +228,45 @@ __global__ void k_p32_transpose(const float* __restrict__ R, int D, float* __res
   }
 }
 
-// y_i = so_i * sum_c T[i][c] * si_c * x_c over the triangle of row i (FP32 matrix, FP64
-// arithmetic); si / so may be null (unit).  Warp per row.
+// x2 = (si * x) as double-FP32 pairs (si may be null: unit)
+__global__ void k_p32_split(const double* __restrict__ si, const double* __restrict__ x, int D,
+                            float2* __restrict__ x2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= D) return;
+  float h, l;
+  ds_split(si ? si[i] * x[i] : x[i], h, l);
+  x2[i] = make_float2(h, l);
+}
+
+// y_i = so_i * sum_c T[i][c] * x2_c over the triangle of row i (FP32 matrix, double-FP32
+// arithmetic on the FP32 pipe); so may be null (unit).  Warp per row.
 __global__ void __launch_bounds__(256) k_p32_trmv(const float* __restrict__ T, int D, int upper,
-                                                 const double* __restrict__ si, const double* __restrict__ x,
-                                                 const double* __restrict__ so, double* __restrict__ y) {
+                                                 const float2* __restrict__ x2, const double* __restrict__ so,
+                                                 double* __restrict__ y) {
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= D) return;
   const int lo = upper ? i : 0, hi = upper ? D : i + 1;
   const float* row = T + (size_t)i * D;
-  double a = 0.0;
-  if (si) {
-    for (int c = lo + lane; c < hi; c += 32) a = fma((double)row[c], si[c] * x[c], a);
-  } else {
-    for (int c = lo + lane; c < hi; c += 32) a = fma((double)row[c], x[c], a);
+  float sh = 0.f, sl = 0.f;
+  for (int c = lo + lane; c < hi; c += 32) {
+    const float2 v = x2[c];
+    ds_fma(sh, sl, row[c], v.x, v.y);
   }
-  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-  if (lane == 0) y[i] = so ? so[i] * a : a;
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, sh, o), ol = __shfl_xor_sync(0xffffffffu, sl, o);
+    ds_add(sh, sl, oh, ol);
+  }
+  if (lane == 0) {
+    const double a = (double)sh + (double)sl;
+    y[i] = so ? so[i] * a : a;
+  }
 }
 
 size_t precond32_workspace_bytes(int D) {
   const size_t d2 = (size_t)D * D;
   const size_t h = (size_t)(D + 1) / 2;
-  return sizeof(float) * (3 * d2 + h * h) + sizeof(double) * (size_t)D + 256;
+  return sizeof(float) * (3 * d2 + h * h) + sizeof(double) * (size_t)D + 256 + sizeof(float2) * (size_t)D + 256;
 }
 
 // Factorise: on return *info (device) is 0 on success, or the first failing column + 1.
@@ -314,9 +330,13 @@ cudaError_t launch_precond32_apply(const void* ws, int D, const double* r, doubl
   const size_t d2 = (size_t)D * D;
   const float* R = L + d2;
   const float* Rt = R + d2;
+  const size_t h = (size_t)(D + 1) / 2;
+  float2* x2 = (float2*)((char*)(Rt + d2 + h * h) + (256 - ((uintptr_t)(Rt + d2 + h * h) & 255)) % 256);
   const unsigned blocks = (unsigned)(((long long)D * 32 + 255) / 256);
-  k_p32_trmv<<<blocks, 256, 0, st>>>(R, D, 0, s, r, nullptr, tmp);
-  k_p32_trmv<<<blocks, 256, 0, st>>>(Rt, D, 1, nullptr, tmp, s, z);
+  k_p32_split<<<(D + 255) / 256, 256, 0, st>>>(s, r, D, x2);
+  k_p32_trmv<<<blocks, 256, 0, st>>>(R, D, 0, x2, nullptr, tmp);
+  k_p32_split<<<(D + 255) / 256, 256, 0, st>>>(nullptr, tmp, D, x2);
+  k_p32_trmv<<<blocks, 256, 0, st>>>(Rt, D, 1, x2, s, z);
   return cudaGetLastError();
 }
 
