@@ -830,6 +830,7 @@ int mld_gpu_create(const mld_gpu_config* cfg, mld_gpu_handle** out) {
   d.NS = (int)t.yslots.size();
   d.NYP = t.NYP;
   d.NTILE = (int)t.tiles.size();
+  d.NCG = (int)t.cg.size();
   for (int j = 0; j <= t.J + 1; ++j) {
     d.hoff[j] = t.hoff[j];
     d.rowk_off[j] = t.rowk_off[j];

@@ -289,7 +289,8 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
   cx<T>* Y = kYShared ? cfull + nch * NU
                       : reinterpret_cast<cx<T>*>(args.yglobal) + (size_t)blockIdx.x * nch * NYP;  // nch*NYP
   cx<T>* V = kYShared ? Y + (size_t)nch * NYP : cfull + nch * NU;  // max(NB*3, kNW*nch)*HU
-  const size_t vblock = (size_t)max(NB * 3, kNW * nch) * HU;
+  // V also holds the CG table during phase 2
+  const size_t vblock = max((size_t)max(NB * 3, kNW * nch) * HU, (size_t)(tb.NCG + 1) / 2);
   cx<T>* ubuf = V + vblock;                                         // (32/kG1)*kNW*2*LH
   T* dBs = reinterpret_cast<T*>(ubuf + (size_t)(32 / kG1) * kNW * 2 * LH);  // 3*NB*K  [col][k]
   T* Bk = dBs + (size_t)3 * NB * K;                                 // nch*K
@@ -364,7 +365,12 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
     __syncthreads();
 
     // ---------------- phase 2: folded Z -> Y, B on the balanced schedule ---------------
-    // a thread owns whole slots (their terms are consecutive items), so Y is stored once
+    // a thread owns whole slots (their terms are consecutive items), so Y is stored once.
+    // The CG coefficients (a few thousand) are staged in V, free until phase 3, so that the
+    // per-term coefficient loads of the per-thread schedules come from shared memory.
+    T* cgs = reinterpret_cast<T*>(V);
+    for (int e = tid; e < tb.NCG; e += nth) cgs[e] = args.cg[e];
+    __syncthreads();
     {
       const int i0 = tb.zitem_off[tid], i1 = tb.zitem_off[tid + 1];
       for (int ch = 0; ch < nch; ++ch) {
@@ -380,14 +386,14 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
           const ZTerm z = tb.zterms[zi.zt];
           cx<T> zs = {T(0), T(0)};
           int i1a = z.i1, i2a = z.i2;
-          const T* cg2 = args.cg + z.cg2;
+          const T* cg2 = cgs + z.cg2;
           for (int a = 0; a < z.na; ++a) {
-            const T c1 = __ldg(args.cg + z.cg1 + a);
+            const T c1 = cgs[z.cg1 + a];
             cx<T> part = {T(0), T(0)};
 #pragma unroll 3
             for (int b = 0; b < z.nb; ++b) {
               const cx<T> pr = cmul(cc[i1a + b], cc[i2a - b]);
-              const T c2 = __ldg(cg2 + b);
+              const T c2 = cg2[b];
               part.x = fma(c2, pr.x, part.x);
               part.y = fma(c2, pr.y, part.y);
             }
@@ -609,7 +615,7 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
 static size_t smem_bytes(const DevTables& tb, int nch, int eb, int NB, bool y_in_smem) {
   const size_t LH = tb.hoff[tb.J + 1] - tb.hoff[tb.J];
   const size_t cxb = 2 * (size_t)eb;
-  const size_t vblock = (size_t)std::max(NB * 3, kNW * nch) * tb.HU;
+  const size_t vblock = std::max((size_t)std::max(NB * 3, kNW * nch) * tb.HU, (size_t)(tb.NCG + 1) / 2);
   size_t b = cxb * ((size_t)nch * tb.NU + (y_in_smem ? (size_t)nch * tb.NYP : 0) + vblock +
                     (size_t)(32 / kG1) * kNW * 2 * LH);
   b += (size_t)eb * ((size_t)3 * NB * tb.K + (size_t)nch * 10 * tb.K + (size_t)nch * NB + (size_t)NB * 4);

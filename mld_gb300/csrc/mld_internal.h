@@ -102,6 +102,7 @@ double cg_coefficient(int j1, int m1, int j2, int m2, int j, int m);  // doubled
 // Device copies of the tables.
 struct DevTables {
   int J = 0, NU = 0, HU = 0, K = 0, NS = 0, NYP = 0, NTILE = 0;
+  int NCG = 0;  // entries of the 1-D CG coefficient table
   int hoff[kMaxJ + 2] = {0};
   int Mp[kMaxJ + 1] = {0};
   int yoff[kMaxJ + 1] = {0};

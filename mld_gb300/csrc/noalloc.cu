@@ -94,6 +94,7 @@ int noalloc_setup(int dev, double j_max, DeviceState** out, std::string* msg) {
     d.NS = (int)t.yslots.size();
     d.NYP = t.NYP;
     d.NTILE = (int)t.tiles.size();
+    d.NCG = (int)t.cg.size();
     for (int j = 0; j <= t.J + 1; ++j) {
       d.hoff[j] = t.hoff[j];
       d.rowk_off[j] = t.rowk_off[j];
