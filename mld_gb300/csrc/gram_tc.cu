@@ -85,17 +85,18 @@ __global__ void __launch_bounds__(256) k_split_bf16(const T* __restrict__ X, int
                                                     long long Mp, __nv_bfloat16* __restrict__ hi,
                                                     __nv_bfloat16* __restrict__ lo) {
   __shared__ float tile[32][33];
-  __shared__ double sw[32];
+  __shared__ float sw[32];
   const long long rb = (long long)blockIdx.x * 32;
   const int cb = blockIdx.y * 32;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  if (tid < 32) sw[tid] = (rb + tid < rows) ? sqrt(w[r0 + rb + tid]) : 0.0;
+  // sqrt(w) and x' in FP32: the split keeps about 17 bits of x', and FP64 runs at 1/64 rate
+  if (tid < 32) sw[tid] = (rb + tid < rows) ? (float)sqrt(w[r0 + rb + tid]) : 0.f;
   __syncthreads();
   for (int y = threadIdx.y; y < 32; y += blockDim.y) {
     const long long r = rb + y;
     const int c = cb + threadIdx.x;
     float v = 0.f;
-    if (r < rows && c < D) v = (float)((double)X[(r0 + r) * ldx + c0 + c] * sw[y]);
+    if (r < rows && c < D) v = (float)X[(r0 + r) * ldx + c0 + c] * sw[y];
     tile[y][threadIdx.x] = v;
   }
   __syncthreads();

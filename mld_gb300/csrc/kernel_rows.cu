@@ -16,13 +16,13 @@
 
 #include <algorithm>
 
+#include "ds.cuh"
 #include "mld_internal.h"
 
 namespace mld {
 
 namespace {
 constexpr int kKT = 256;   // threads per CTA (one reference point each per pass)
-constexpr int kVC = 8;     // derivative vectors per register pass
 __constant__ int c_sa[6] = {0, 1, 2, 1, 0, 0};
 __constant__ int c_sb[6] = {0, 1, 2, 2, 2, 1};
 }  // namespace
@@ -94,28 +94,6 @@ __global__ void __launch_bounds__(256) k_krr_xz(int A, int nk, int KK, const T* 
     }
 }
 
-// base^p for the kernel power: repeated products for small integer powers, pow otherwise
-__device__ __forceinline__ double kpow(double base, double p) {
-  const int ip = (int)p;
-  if ((double)ip == p && ip >= 0 && ip <= 8) {
-    double r = 1.0;
-    for (int i = 0; i < ip; ++i) r *= base;
-    return r;
-  }
-  return pow(base, p);
-}
-
-// kernel value and the two derivative coefficients of centre atom a and reference point k
-template <typename T>
-__device__ __forceinline__ void krr_coef(T xz, const T* at, T szz, double s2, double l2, double p, T& kv, T& c1,
-                                         T& c2) {
-  const double base = s2 + (double)xz / l2;
-  const double kt = kpow(base, p);
-  const double aaa = (double)szz * (double)at[1];
-  kv = (T)(kt / aaa);
-  c1 = (T)(p * kpow(base, p - 1.0) / l2 / aaa);
-  c2 = (T)(kt * (double)at[2] / (2.0 * (double)at[0]) / aaa);
-}
 
 // energy rows: grid (S, ceil(nk / kKT))
 template <typename T>
@@ -126,14 +104,33 @@ __global__ void __launch_bounds__(kKT) k_krr_energy(int nk, const int* __restric
   const int s = blockIdx.x;
   const int k = blockIdx.y * kKT + threadIdx.x;
   if (rowE[s] < 0 || k >= nk) return;
-  double acc = 0.0;
+  // kernel values in the kernel's precision (FP64 runs at 1/64 rate), summed in double-FP32
+  const T s2t = (T)s2, l2t = (T)l2, pt = (T)p;
+  const int ip = (int)p;
+  const bool ipow = (double)ip == p && ip >= 0 && ip <= 8;
+  float sh = 0.f, sl = 0.f;
+  double acc = 0.0;  // FP64 method
   for (int a = atom_start[s]; a < atom_start[s + 1]; ++a) {
-    if (at[4 * (size_t)a + 3] == T(0)) continue;  // atoms without neighbours contribute zero
-    T kv, c1, c2;
-    krr_coef<T>(F[(size_t)a * nk + k], at + 4 * (size_t)a, szz[k], s2, l2, p, kv, c1, c2);
-    acc += (double)kv;
+    const T* ata = at + 4 * (size_t)a;
+    if (ata[3] == T(0)) continue;  // atoms without neighbours contribute zero
+    const T base = s2t + F[(size_t)a * nk + k] / l2t;
+    T kt = T(1);
+    if (ipow) {
+      for (int i = 0; i < ip; ++i) kt *= base;
+    } else {
+      kt = (T)pow((double)base, (double)pt);
+    }
+    const T kv = kt / (szz[k] * ata[1]);
+    if constexpr (sizeof(T) == 8) {
+      acc += kv;
+    } else {
+      float t, e;
+      two_sum(sh, kv, t, e);
+      sh = t;
+      sl += e;
+    }
   }
-  X[rowE[s] * ldx + c0 + k] = (T)acc;
+  X[rowE[s] * ldx + c0 + k] = sizeof(T) == 8 ? (T)acc : (T)((double)sh + (double)sl);
 }
 
 // Force rows as a register-tiled product: CTA = (tile of NZ reference points, range of target
