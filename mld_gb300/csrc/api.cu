@@ -99,7 +99,7 @@ struct mld_gpu_handle {
     B_G, B_H, B_W, B_EVALS, B_INFO, B_SQ, B_PRED, B_BOUT, B_DBOUT,
     B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
     B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV, B_KZD, B_KZF, B_KWS, B_WSERVE, B_P32,
-    B_EW, B_EBETA, B_EB, B_EOUT,
+    B_EW, B_EBETA, B_EB, B_EOUT, B_KTC,
     B_COUNT
   };
   static_assert(B_COUNT <= 64, "buffer table too small");
@@ -261,6 +261,9 @@ int build_neighbours(mld_gpu_handle* h) {
   return MLD_OK;
 }
 
+// workspace of the tensor-core kernel-row product (derivative-vector planes of one atom chunk)
+constexpr size_t kKrrTcWorkspaceCap = size_t(6) << 30;
+
 // global Y scratch of the descriptor kernel when its per-atom Y does not fit in shared memory
 template <typename T>
 int y_scratch(mld_gpu_handle* h, void** p, size_t* bytes) {
@@ -349,10 +352,35 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
       CK(ensure(h, mld_gpu_handle::B_KWS, sizeof(T) * wse));
       const T* Zp = bp_<T>(h, sizeof(T) == 8 ? mld_gpu_handle::B_KZD : mld_gpu_handle::B_KZF);
       int nkl = 0;
+      // FP32 rows: force rows on the tensor cores, in atom chunks that fit a bounded workspace
+      void* tcws = nullptr;
+      size_t tcb = 0;
+      int* terr = nullptr;
+      if (sizeof(T) == 4 && krr_force_tc_available()) {
+        const size_t KP = (size_t)(h->KK + 63) / 64 * 64;
+        const size_t nvp = (size_t)(h->b.maxnn + 1 + 31) / 32 * 32;
+        const size_t tiles = (size_t)h->A * ((3 * nvp + 127) / 128);
+        const size_t per_tile = 128 * (4 * KP + 12) + 20;
+        const size_t zb = 2 * ((size_t)h->nk * KP * 2 + 256);
+        tcb = std::min(kKrrTcWorkspaceCap, zb + tiles * per_tile + 16 * per_tile + 4096);
+        tcb = std::max(tcb, zb + 16 * per_tile + 4096);
+        CK(ensure(h, mld_gpu_handle::B_KTC, tcb));
+        CK(ensure(h, mld_gpu_handle::B_TERR, sizeof(int)));
+        tcws = bp_<void>(h, mld_gpu_handle::B_KTC);
+        terr = bp_<int>(h, mld_gpu_handle::B_TERR);
+        CK(cudaMemsetAsync(terr, 0, sizeof(int), h->st));
+      }
       CK(launch_krr_rows<T>(h->b, rows, bp_<int>(h, mld_gpu_handle::B_REV), Bq, dBq, Zp, h->nk, h->KK,
                             h->cfg.kernel_power, h->cfg.length_kernel, h->cfg.sigma_kernel, h->cfg.sign_stress,
-                            h->cfg.sign_stress_big_box, bp_<T>(h, mld_gpu_handle::B_KWS), X, h->DL, h->st, &nkl));
+                            h->cfg.sign_stress_big_box, bp_<T>(h, mld_gpu_handle::B_KWS), X, h->DL, h->st, &nkl, tcws,
+                            tcb, terr, h->nsm));
       nl(h, 2 + nkl);
+      if (terr) {
+        int herr = 0;
+        CK(cudaMemcpyAsync(&herr, terr, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        if (herr) return fail(h, MLD_ERR_TIMEOUT, "tensor-core kernel rows: a pipeline wait timed out");
+      }
     }
   }
   mark(h, MLD_PHASE_DESCRIPTORS, 1);

@@ -25,15 +25,16 @@
 
 #include "mld_internal.h"
 #include "ptx.cuh"
+#include "tc.cuh"
 
 namespace mld {
 
 namespace {
 
-constexpr int kTM = 128;                       // tile rows (i) = tile columns (j)
-constexpr int kTK = 64;                        // design rows per stage: 128 bytes of bf16, one swizzle row
+using tc::kTK;
+using tc::kTM;
+using tc::kTileBytes;
 constexpr int kStages = 3;
-constexpr int kTileBytes = kTM * kTK * 2;      // 16 KB per operand tile
 constexpr int kStageBytes = 4 * kTileBytes;    // A_hi, A_lo, B_hi, B_lo
 constexpr int kFlush = 1;                      // K slices per TMEM accumulation (64 design rows)
 constexpr int kEpiWarps = 16;                  // four per TMEM lane quarter, 32 columns each
@@ -45,34 +46,9 @@ using ptx::mbar_init;
 using ptx::mbar_wait;
 using ptx::smem_u32;
 using ptx::tma_load_2d;
-
-// Shared-memory matrix descriptor of a K-major tile written by TMA with 128-byte swizzle:
-// rows of 128 bytes, 8-row core groups 1024 bytes apart (stride byte offset), version 1.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);  // start address, bits 0-13
-  d |= (uint64_t)1 << 16;                    // leading byte offset (not used by swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset, bits 32-45
-  d |= (uint64_t)1 << 46;                    // descriptor version
-  d |= (uint64_t)2 << 61;                    // 128-byte swizzle
-  return d;
-}
-
-// kind::f16 instruction descriptor: D FP32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1),
-// both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28; M = N = 128.
-constexpr uint32_t kIdesc =
-    (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTM >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
-}
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
+using tc::mma_bf16;
+using tc::mma_commit;
+using tc::sw128_desc;
 
 }  // namespace
 
@@ -276,39 +252,9 @@ __global__ void __launch_bounds__(kGramThreads, 1)
 }
 
 // ---------------------------------------------------------------------------------------
-namespace {
-using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-  }
-  return fn;
-}
-// plane of D feature rows x Mp design rows (bf16, row stride Mp * 2 bytes); box 64 x 128
-bool make_plane_map(CUtensorMap* m, void* base, long long Mp, int D) {
-  EncodeTiledFn fn = encode_fn();
-  if (!fn) return false;
-  cuuint64_t dims[2] = {(cuuint64_t)Mp, (cuuint64_t)D};
-  cuuint64_t strides[1] = {(cuuint64_t)Mp * 2};
-  cuuint32_t box[2] = {(cuuint32_t)kTK, (cuuint32_t)kTM};
-  cuuint32_t estr[2] = {1, 1};
-  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-}  // namespace
-
 size_t gram_tc_min_workspace(int D) { return (size_t)4 * D * kTK + 256; }
 
-bool gram_tc_available() { return encode_fn() != nullptr; }
+bool gram_tc_available() { return tc::encode_fn() != nullptr; }
 
 // G (FP64, D x D, upper triangle) += sum over rows r of w_r x_r x_r^T for columns [c0, c0 + D)
 // of X (M rows, stride ldx).  `ws` holds ws_bytes >= gram_tc_min_workspace(D) bytes; the rows
@@ -339,7 +285,7 @@ cudaError_t launch_gram_tc(const T* X, int ldx, int c0, int D, const double* w, 
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     CUtensorMap mh, ml;
-    if (!make_plane_map(&mh, hi, Mp, D) || !make_plane_map(&ml, lo, Mp, D)) return cudaErrorInvalidValue;
+    if (!tc::make_plane_map(&mh, hi, Mp, D, Mp) || !tc::make_plane_map(&ml, lo, Mp, D, Mp)) return cudaErrorInvalidValue;
     const int nk = (int)((rows + kTK - 1) / kTK);
     // row splits: at least two waves of CTAs where the tile count alone does not give them
     int nsplit = std::max(1, std::min(nk, (2 * nsm + ntile - 1) / ntile));

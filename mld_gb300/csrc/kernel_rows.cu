@@ -17,6 +17,7 @@
 #include <algorithm>
 
 #include "ds.cuh"
+#include "krr.cuh"
 #include "mld_internal.h"
 
 namespace mld {
@@ -146,28 +147,6 @@ struct KrrTile {
   static constexpr int CJ = NZ / 16;  // columns per thread
   static constexpr int RI = 6;        // rows per thread per pass (96 rows per pass)
 };
-
-// kernel coefficients of centre atom (its [f(x,x), sqrt f(x,x), dker_xx, has neighbours]) and
-// a reference point, in the kernel's precision: (c1, c2); zero for an atom without neighbours
-template <typename T>
-__device__ __forceinline__ void krr_c12(T xz, const T* atc, T szz, T s2, T l2, T p, T& c1, T& c2) {
-  if (atc[3] == T(0)) {
-    c1 = c2 = T(0);
-    return;
-  }
-  const T base = s2 + xz / l2;
-  T bp1 = T(1);  // base^(p-1)
-  const int ip = (int)p;
-  if ((T)ip == p && ip >= 1 && ip <= 8) {
-    for (int i = 1; i < ip; ++i) bp1 *= base;
-  } else {
-    bp1 = (T)pow((double)base, (double)p - 1.0);
-  }
-  const T kt = bp1 * base;
-  const T inv_aaa = T(1) / (szz * atc[1]);
-  c1 = p * bp1 / l2 * inv_aaa;
-  c2 = kt * atc[2] / (T(2) * atc[0]) * inv_aaa;
-}
 
 template <typename T, int NZ_>
 __global__ void __launch_bounds__(256) k_krr_force_tiled(
@@ -449,8 +428,9 @@ template <typename T>
 cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* rev, const T* Bq, const T* dBq,
                             const T* Z, int nk, int KK, double power, double length, double sigma,
                             double sign_stress, double sign_big, T* ws, T* X, int c0, cudaStream_t st,
-                            int* launches) {
+                            int* launches, void* tcws, size_t tcws_bytes, int* err, int nsm) {
   if (b.A == 0 || nk == 0) return cudaSuccess;
+  *launches = 4;
   const double l2 = 2.0 * length * length, s2 = sigma * sigma;
   T* at = ws;
   T* szz = at + 4 * (size_t)b.A;
@@ -463,9 +443,21 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
   k_krr_xz<T><<<gx, 256, 0, st>>>(b.A, nk, KK, Bq, Z, F);
   dim3 gs(b.S, (nk + kKT - 1) / kKT);
   k_krr_energy<T><<<gs, kKT, 0, st>>>(nk, b.atom_start, rows.rowE, F, at, szz, s2, l2, power, c0, rows.ldx, X);
-  // force rows: register-tiled, reference-point tiles of NZ in shared memory (the widest tile
+  // force rows: on the tensor cores for FP32 rows (krr_tc.cu) when a workspace is given;
+  // otherwise register-tiled, reference-point tiles of NZ in shared memory (the widest tile
   // whose working set fits)
-  {
+  bool force_done = false;
+  if constexpr (sizeof(T) == 4) {
+    if (tcws && krr_force_tc_available()) {
+      int nl = 0;
+      cudaError_t e = launch_krr_force_tc(b, rows, rev, Bq, dBq, Z, F, at, szz, nk, KK, power, length, sigma, tcws,
+                                          tcws_bytes, X, c0, err, nsm, st, &nl);
+      if (e != cudaSuccess) return e;
+      *launches += nl;
+      force_done = true;
+    }
+  }
+  if (!force_done) {
     static int optin = 0;
     if (!optin) {
       int dev = 0;
@@ -503,6 +495,7 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
     if (e != cudaSuccess) return e;
     kern<<<g, 256, smem, st>>>(KK, nk, b.A, apc, maxnv, b.atom_struct, b.atom_start, rows.rowF, b.nbr_off,
                                b.nbr_idx, rev, Bq, dBq, Z, F, at, szz, s2, l2, power, c0, rows.ldx, X);
+    *launches += 1;
   }
   k_krr_stress_atom<T><<<b.A, 128, sizeof(T) * 3 * (size_t)std::max(1, b.maxnn), st>>>(
       KK, b.maxnn, b.atom_struct, b.small, b.nbr_off, b.nbr_u, Bq, dBq, sign_big, Ts, tx);
@@ -541,15 +534,16 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
     kern<<<g, 256, smem, st>>>(KK, nk, b.S, spc, b.atom_start, rows.rowS, b.volume, sign_stress, Ts, tx, Z, F, at,
                                szz, s2, l2, power, c0, rows.ldx, X);
   }
-  *launches = 6;
+  *launches += 2;  // stress partials and stress rows
   return cudaGetLastError();
 }
 
 template cudaError_t launch_krr_rows<float>(const DevBatch&, const DevRows&, const int*, const float*, const float*,
                                             const float*, int, int, double, double, double, double, double, float*,
-                                            float*, int, cudaStream_t, int*);
+                                            float*, int, cudaStream_t, int*, void*, size_t, int*, int);
 template cudaError_t launch_krr_rows<double>(const DevBatch&, const DevRows&, const int*, const double*,
                                              const double*, const double*, int, int, double, double, double, double,
-                                             double, double*, double*, int, cudaStream_t, int*);
+                                             double, double*, double*, int, cudaStream_t, int*, void*, size_t, int*,
+                                             int);
 
 }  // namespace mld

@@ -274,7 +274,14 @@ template <typename T>
 cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* rev, const T* Bq, const T* dBq,
                             const T* Z, int nk, int KK, double power, double length, double sigma,
                             double sign_stress, double sign_big, T* ws, T* X, int c0, cudaStream_t st,
-                            int* launches);
+                            int* launches, void* tcws = nullptr, size_t tcws_bytes = 0, int* err = nullptr,
+                            int nsm = 0);
+// kernel-block force rows on the tensor cores (krr_tc.cu)
+bool krr_force_tc_available();
+cudaError_t launch_krr_force_tc(const DevBatch& b, const DevRows& rows, const int* rev, const float* Bq,
+                                const float* dBq, const float* Z, const float* F, const float* at, const float* szz,
+                                int nk, int KK, double power, double length, double sigma, void* ws, size_t ws_bytes,
+                                float* X, int c0, int* err, int nsm, cudaStream_t st, int* launches);
 
 // tensor-core Gram in BF16 split precision (gram_tc.cu)
 size_t gram_tc_min_workspace(int D);
