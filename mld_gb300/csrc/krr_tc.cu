@@ -127,7 +127,9 @@ __global__ void __launch_bounds__(kKThreads, 1)
   const uint32_t opb = (uint32_t)nkb * 2 * kTileBytes;  // bytes of one operand tile set (hi and lo blocks)
   unsigned char* atile = btile + opb;
   float2* tab = reinterpret_cast<float2*>(atile + (size_t)stages * opb);  // kTM x (tabv + 1)
-  uint64_t* bfull = reinterpret_cast<uint64_t*>(tab + (size_t)kTM * (tabv + 1));
+  float* iszz = reinterpret_cast<float*>(tab + (size_t)kTM * (tabv + 1));  // kTM: 1 / szz of the CTA's points
+  float2* fac = reinterpret_cast<float2*>(iszz + kTM);                      // tabv: per-vector centre factors
+  uint64_t* bfull = reinterpret_cast<uint64_t*>(fac + tabv + (tabv & 1));
   uint64_t* full = bfull + 1;
   uint64_t* empty = full + stages;
   uint64_t* tfull = empty + stages;  // [2] accumulator ready
@@ -225,6 +227,10 @@ __global__ void __launch_bounds__(kKThreads, 1)
     // epilogue: lane quarter q (32 rows of one atom and one alpha), 32 reference points
     const int q = warp & 3, cq = (warp - 2) >> 2;
     const int etid = threadIdx.x - 64;  // 0 .. 511 over the epilogue warps
+    const float il2 = 1.f / l2;
+    const int ipw = (int)pw;
+    const bool int_pow = (float)ipw == pw && ipw >= 1 && ipw <= 8;
+    if (etid < kTM) iszz[etid] = (n0 + etid < nk) ? 1.f / szz[n0 + etid] : 0.f;
     bool got = true;
     for (int i = 0; i < nmine; ++i) {
       const int b = i & 1;
@@ -234,32 +240,41 @@ __global__ void __launch_bounds__(kKThreads, 1)
       // coefficient table of the tile's atom (the previous tile's reads are done at the barrier)
       asm volatile("bar.sync 1, %0;" ::"n"(kKEpiWarps * 32));
       if (use_tab) {
+        // per vector: the centre's factors 1 / sqrt f(x,x) and dker_xx / (2 f(x,x) sqrt f(x,x)), zero
+        // for a centre without neighbours (krr_c12 with the divisions taken out of the entries)
+        const long long r0 = (long long)(t - tm.ti) * kTM;  // the atom's alpha = 0 rows: vector v = row
+        if (etid < tm.nv) {
+          const float4 a4 = *reinterpret_cast<const float4*>(at + 4 * (size_t)rce[r0 + etid]);
+          const float f1 = a4.w == 0.f ? 0.f : 1.f / a4.y;
+          fac[etid] = make_float2(f1, a4.z / (2.f * a4.x) * f1);
+        }
+        asm volatile("bar.sync 3, %0;" ::"n"(kKEpiWarps * 32));
         // four entries per thread and pass, their loads issued together (the kernel features of
         // the neighbour centres are scattered rows of F)
-        const long long r0 = (long long)(t - tm.ti) * kTM;  // the atom's alpha = 0 rows: vector v = row
         const int nvk = tm.nv * kTM;
         constexpr int kU = 4, kStep = kKEpiWarps * 32;
         for (int e0 = etid; e0 < nvk; e0 += kU * kStep) {
-          float xf[kU], zz[kU];
-          float4 a4[kU];
+          float xf[kU];
 #pragma unroll
           for (int u = 0; u < kU; ++u) {
-            const int e = e0 + u * kStep, v = e >> 7, k = n0 + (e & (kTM - 1));
-            const bool live = e < nvk && k < nk;
-            const int ce = live ? rce[r0 + v] : 0;
-            xf[u] = live ? F[(size_t)ce * nk + k] : 0.f;
-            zz[u] = live ? szz[k] : 1.f;
-            a4[u] = live ? *reinterpret_cast<const float4*>(at + 4 * (size_t)ce) : make_float4(1.f, 1.f, 0.f, 0.f);
+            const int e = e0 + u * kStep, k = n0 + (e & (kTM - 1));
+            xf[u] = (e < nvk && k < nk) ? F[(size_t)rce[r0 + (e >> 7)] * nk + k] : 0.f;
           }
 #pragma unroll
           for (int u = 0; u < kU; ++u) {
             const int e = e0 + u * kStep;
             if (e >= nvk) break;
-            const float atc[4] = {a4[u].x, a4[u].y, a4[u].z, a4[u].w};
-            float c1, c2;
-            krr_c12<float>(xf[u], atc, zz[u], s2, l2, pw, c1, c2);
-            if (n0 + (e & (kTM - 1)) >= nk) c1 = c2 = 0.f;
-            tab[(size_t)(e & (kTM - 1)) * (tabv + 1) + (e >> 7)] = make_float2(c1, c2);
+            const int kl = e & (kTM - 1), v = e >> 7;
+            const float base = s2 + xf[u] * il2;
+            float bp1 = 1.f;  // base^(p - 1)
+            if (int_pow) {
+              for (int j = 1; j < ipw; ++j) bp1 *= base;
+            } else {
+              bp1 = powf(base, pw - 1.f);
+            }
+            const float2 f = fac[v];
+            const float sc = iszz[kl];  // zero past nk
+            tab[(size_t)kl * (tabv + 1) + v] = make_float2(pw * bp1 * il2 * sc * f.x, bp1 * base * sc * f.y);
           }
         }
       }
@@ -356,7 +371,7 @@ cudaError_t launch_krr_force_tc(const DevBatch& b, const DevRows& rows, const in
   const int stages = 1;
   const size_t opb = (size_t)nkb * 2 * kTileBytes;
   const size_t kSmemMax = 227 * 1024;
-  const size_t fixed = 1024 + (1 + (size_t)stages) * opb + 8 * (3 + 2 * (size_t)stages + 4) + 16;
+  const size_t fixed = 1024 + (1 + (size_t)stages) * opb + 8 * (3 + 2 * (size_t)stages + 4) + 16 + 4 * kTM + 8 * 66;
   if (fixed + (size_t)kTM * 8 * 2 > kSmemMax) return cudaErrorInvalidValue;
   const int tabv = (int)std::min<size_t>(64, (kSmemMax - fixed) / ((size_t)kTM * 8) - 1);
   const size_t smem = fixed + (size_t)kTM * 8 * (tabv + 1);
