@@ -356,14 +356,11 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
       void* tcws = nullptr;
       size_t tcb = 0;
       int* terr = nullptr;
-      if (sizeof(T) == 4 && krr_force_tc_available()) {
-        const size_t KP = (size_t)(h->KK + 63) / 64 * 64;
-        const size_t nvp = (size_t)(h->b.maxnn + 1 + 31) / 32 * 32;
-        const size_t tiles = (size_t)h->A * ((3 * nvp + 127) / 128);
-        const size_t per_tile = 128 * (4 * KP + 12) + 20;
-        const size_t zb = 2 * ((size_t)h->nk * KP * 2 + 256);
-        tcb = std::min(kKrrTcWorkspaceCap, zb + tiles * per_tile + 16 * per_tile + 4096);
-        tcb = std::max(tcb, zb + 16 * per_tile + 4096);
+      if (sizeof(T) == 4 && krr_force_tc_available() && h->KK <= kKrrTcMaxK) {
+        // all atoms at once when that fits the cap, else chunks of at least 64 atoms
+        const int maxnv = h->b.maxnn + 1;
+        tcb = std::min(kKrrTcWorkspaceCap, krr_force_tc_workspace_bytes(h->A, maxnv, (int)h->nk, h->KK));
+        tcb = std::max(tcb, krr_force_tc_workspace_bytes(std::min<long long>(h->A, 64), maxnv, (int)h->nk, h->KK));
         CK(ensure(h, mld_gpu_handle::B_KTC, tcb));
         CK(ensure(h, mld_gpu_handle::B_TERR, sizeof(int)));
         tcws = bp_<void>(h, mld_gpu_handle::B_KTC);

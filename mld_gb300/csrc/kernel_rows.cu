@@ -150,7 +150,7 @@ struct KrrTile {
 
 template <typename T, int NZ_>
 __global__ void __launch_bounds__(256) k_krr_force_tiled(
-    int KK, int nk, int A, int atoms_per_cta, int maxnv, const int* __restrict__ atom_struct,
+    int KK, int nk, int A, int atoms_per_cta, int vc, const int* __restrict__ atom_struct,
     const int* __restrict__ atom_start, const long long* __restrict__ rowF, const int* __restrict__ nbr_off,
     const int* __restrict__ nbr_idx, const int* __restrict__ rev, const T* __restrict__ B, const T* __restrict__ dB,
     const T* __restrict__ Z, const T* __restrict__ F, const T* __restrict__ at, const T* __restrict__ szz, double s2,
@@ -159,11 +159,11 @@ __global__ void __launch_bounds__(256) k_krr_force_tiled(
   constexpr int NZ = Tl::NZ, CJ = Tl::CJ, RI = Tl::RI;
   extern __shared__ __align__(16) unsigned char ksm[];
   T* Zs = reinterpret_cast<T*>(ksm);                   // KK * NZ   [c][k]
-  T* Vt = Zs + (size_t)KK * NZ;                        // KK * (3 maxnv)  [c][r]
-  T* gx = Vt + (size_t)KK * 3 * maxnv;                 // 3 maxnv
-  T* red = gx + 3 * maxnv;                             // 3 * NZ
-  T* cf = red + 3 * NZ;                                // maxnv * NZ * 2 (c1, c2 per centre)
-  int* cen = reinterpret_cast<int*>(cf + (size_t)2 * maxnv * NZ);  // maxnv
+  T* Vt = Zs + (size_t)KK * NZ;                        // KK * (3 vc)  [c][r]
+  T* gx = Vt + (size_t)KK * 3 * vc;                    // 3 vc
+  T* red = gx + 3 * vc;                                // 3 * NZ
+  T* cf = red + 3 * NZ;                                // vc * NZ * 2 (c1, c2 per centre)
+  int* cen = reinterpret_cast<int*>(cf + (size_t)2 * vc * NZ);  // vc
   const T s2t = (T)s2, l2t = (T)l2, pt = (T)p;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int k0 = blockIdx.x * NZ;
@@ -177,21 +177,34 @@ __global__ void __launch_bounds__(256) k_krr_force_tiled(
     const int s = atom_struct[a];
     if (rowF[s] < 0) continue;  // uniform over the CTA
     const int p0 = nbr_off[a], nn = nbr_off[a + 1] - p0;
-    const int nv = nn + 1, R = 3 * nv;
-    __syncthreads();  // previous atom's epilogue is done with Vt / red
-    // stage the rows: Vt[c][3 v + alpha]
-    for (int e = tid; e < 3 * KK; e += 256) {
-      const int al = e / KK, c = e - al * KK;
-      T acc = T(0);
-      for (int q = 0; q < nn; ++q) acc += dB[((size_t)(p0 + q) * 3 + al) * KK + c];
-      Vt[(size_t)c * R + al] = acc;
+    const int nv = nn + 1;
+    T part[3][CJ];
+#pragma unroll
+    for (int al = 0; al < 3; ++al)
+#pragma unroll
+      for (int j = 0; j < CJ; ++j) part[al][j] = T(0);
+    // derivative vectors in chunks of vc (the atom's neighbour count may exceed what shared
+    // memory holds next to the reference-point tile)
+    for (int vb = 0; vb < nv; vb += vc) {
+    const int nvc = min(vc, nv - vb), R = 3 * nvc;
+    __syncthreads();  // previous chunk's (or atom's) epilogue is done with Vt / cf / red
+    // stage the rows: Vt[c][3 v + alpha] for the chunk's vectors v = vb + (0 .. nvc - 1)
+    if (vb == 0)
+      for (int e = tid; e < 3 * KK; e += 256) {
+        const int al = e / KK, c = e - al * KK;
+        T acc = T(0);
+        for (int q = 0; q < nn; ++q) acc += dB[((size_t)(p0 + q) * 3 + al) * KK + c];
+        Vt[(size_t)c * R + al] = acc;
+      }
+    const int q0 = vb == 0 ? 0 : vb - 1, nq = vb + nvc - 1 - q0;  // pairs of the chunk
+    for (int e = tid; e < nq * 3 * KK; e += 256) {
+      const int qq = e / (3 * KK), r = e - qq * 3 * KK, al = r / KK, c = r - al * KK;
+      const int q = q0 + qq, rq = rev[p0 + q];
+      Vt[(size_t)c * R + 3 * (q + 1 - vb) + al] = rq >= 0 ? dB[(size_t)rq * 3 * KK + r] : T(0);
     }
-    for (int e = tid; e < nn * 3 * KK; e += 256) {
-      const int q = e / (3 * KK), r = e - q * 3 * KK, al = r / KK, c = r - al * KK;
-      Vt[(size_t)c * R + 3 * (q + 1) + al] = dB[(size_t)rev[p0 + q] * 3 * KK + r];
-    }
-    for (int v = tid; v < nv; v += 256) cen[v] = v == 0 ? a : nbr_idx[p0 + v - 1];
-    for (int e = tid; e < 3 * NZ; e += 256) red[e] = T(0);
+    for (int v = tid; v < nvc; v += 256) cen[v] = vb + v == 0 ? a : nbr_idx[p0 + vb + v - 1];
+    if (vb == 0)
+      for (int e = tid; e < 3 * NZ; e += 256) red[e] = T(0);
     __syncthreads();
     for (int r = tid; r < R; r += 256) {
       const T* x = B + (size_t)cen[r / 3] * KK;
@@ -200,7 +213,7 @@ __global__ void __launch_bounds__(256) k_krr_force_tiled(
       gx[r] = d;
     }
     // coefficient table of the centres for this tile of reference points
-    for (int e = tid; e < nv * NZ; e += 256) {
+    for (int e = tid; e < nvc * NZ; e += 256) {
       const int v = e / NZ, k = e - v * NZ;
       T c1 = T(0), c2 = T(0);
       if (k < nkt) {
@@ -211,11 +224,6 @@ __global__ void __launch_bounds__(256) k_krr_force_tiled(
       cf[2 * (size_t)e + 1] = c2;
     }
     __syncthreads();
-    T part[3][CJ];
-#pragma unroll
-    for (int al = 0; al < 3; ++al)
-#pragma unroll
-      for (int j = 0; j < CJ; ++j) part[al][j] = T(0);
     for (int rb = 0; rb < R; rb += 16 * RI) {
       T acc[RI][CJ];
 #pragma unroll
@@ -242,7 +250,7 @@ __global__ void __launch_bounds__(256) k_krr_force_tiled(
         const int r = rb + ty + 16 * i;
         if (r >= R) continue;
         const int v = r / 3, al = r - 3 * v;
-        const T sg = v == 0 ? T(1) : T(-1);
+        const T sg = vb + v == 0 ? T(1) : T(-1);
         const T g = gx[r];
         const T* cv = cf + (size_t)2 * v * NZ;
 #pragma unroll
@@ -255,6 +263,7 @@ __global__ void __launch_bounds__(256) k_krr_force_tiled(
         }
       }
     }
+    }  // vector chunks
 #pragma unroll
     for (int al = 0; al < 3; ++al)
 #pragma unroll
@@ -448,7 +457,7 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
   // whose working set fits)
   bool force_done = false;
   if constexpr (sizeof(T) == 4) {
-    if (tcws && krr_force_tc_available()) {
+    if (tcws && krr_force_tc_available() && KK <= kKrrTcMaxK) {
       int nl = 0;
       cudaError_t e = launch_krr_force_tc(b, rows, rev, Bq, dBq, Z, F, at, szz, nk, KK, power, length, sigma, tcws,
                                           tcws_bytes, X, c0, err, nsm, st, &nl);
@@ -465,19 +474,24 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     }
     const int maxnv = b.maxnn + 1;
-    auto smem_for = [&](int nz) {
-      return sizeof(T) * ((size_t)KK * nz + (size_t)KK * 3 * maxnv + 3 * (size_t)maxnv + 3 * (size_t)nz +
-                          (size_t)2 * maxnv * nz) +
-             sizeof(int) * maxnv + 16;
+    auto smem_for = [&](int nz, int vc) {
+      return sizeof(T) * ((size_t)KK * nz + (size_t)KK * 3 * vc + 3 * (size_t)vc + 3 * (size_t)nz +
+                          (size_t)2 * vc * nz) +
+             sizeof(int) * vc + 16;
     };
-    // FP32 tiles up to 256 reference points, FP64 up to 64 (register budget of the 6 x NZ/16 tile)
-    int nz = 0;
+    // FP32 tiles up to 256 reference points, FP64 up to 64 (register budget of the 6 x NZ/16 tile),
+    // all of an atom's derivative vectors at once where they fit, else in chunks of vc
+    int nz = 0, vc = maxnv;
     for (int cand : {256, 128, 64, 32})
-      if ((sizeof(T) == 4 || cand <= 64) && smem_for(cand) <= (size_t)optin) {
+      if ((sizeof(T) == 4 || cand <= 64) && smem_for(cand, maxnv) <= (size_t)optin) {
         nz = cand;
         break;
       }
-    if (!nz) return cudaErrorInvalidConfiguration;  // neighbour count too large for the tile
+    if (!nz) {
+      nz = 32;
+      while (vc > 1 && smem_for(nz, vc) > (size_t)optin) vc = (vc + 1) / 2;
+      if (smem_for(nz, vc) > (size_t)optin) return cudaErrorInvalidConfiguration;  // K too large for the tile
+    }
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -485,7 +499,7 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
     const int ranges = std::max(1, std::min(b.A, (2 * nsm + ntiles - 1) / ntiles * 4));
     const int apc = (b.A + ranges - 1) / ranges;
     dim3 g(ntiles, (b.A + apc - 1) / apc);
-    const size_t smem = smem_for(nz);
+    const size_t smem = smem_for(nz, vc);
     auto kern = nz == 64 ? k_krr_force_tiled<T, 64> : k_krr_force_tiled<T, 32>;
     if constexpr (sizeof(T) == 4) {
       if (nz == 256) kern = k_krr_force_tiled<T, 256>;
@@ -493,7 +507,7 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
     }
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<g, 256, smem, st>>>(KK, nk, b.A, apc, maxnv, b.atom_struct, b.atom_start, rows.rowF, b.nbr_off,
+    kern<<<g, 256, smem, st>>>(KK, nk, b.A, apc, vc, b.atom_struct, b.atom_start, rows.rowF, b.nbr_off,
                                b.nbr_idx, rev, Bq, dBq, Z, F, at, szz, s2, l2, power, c0, rows.ldx, X);
     *launches += 1;
   }

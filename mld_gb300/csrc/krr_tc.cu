@@ -4,17 +4,23 @@
 // 268-320) is a sum over the derivative vectors of a: its own pair sum (v = 0, centre a, sign +1)
 // and the reversed pairs j -> a (v >= 1, centre j, sign -1):
 //   row(a, alpha, k) = sum_v sign_v (c1(ce_v, k) (V_{v,alpha} . z_k) - c2(ce_v, k) (V_{v,alpha} . x_{ce_v}))
-// The products V . z_k over all rows and reference points are one large GEMM, V (rows x KK) times
-// Z^T (KK x nk), which this file runs on the 5th-generation tensor cores in BF16 split precision
-// (v = hi + lo; hi hi + hi lo + lo hi, three MMAs per K step, FP32 accumulation of KK <= 192
+// The products z_k . V over all reference points and rows are one large GEMM, Z (nk x KK) times
+// V^T (KK x rows), which this file runs on the 5th-generation tensor cores in BF16 split precision
+// (v = hi + lo; hi hi + lo hi + hi lo, three MMAs per K step, FP32 accumulation of KK <= 192
 // products in TMEM), with the coefficient transform and the sum over v in the epilogue:
-//   * operands: V and Z as K-major bf16 hi/lo planes, K padded to a multiple of 64;
-//   * rows of an atom are laid out alpha-major, each alpha padded to a multiple of 32 rows, and
-//     every atom starts on a 128-row tile: a 32-row TMEM lane quarter then holds one atom and
-//     one alpha, and a warp's 32 x 32 block reduces over its rows with a shuffle butterfly;
-//   * CTA = one 128-point tile of Z (resident in shared memory) and a strided set of row tiles,
-//     with the Gram kernel's roles: TMA producer warp, MMA warp (two TMEM accumulators), sixteen
-//     epilogue warps; the per-quarter sums are added to the force rows with FP32 atomics.
+//   * operands: Z and V as K-major bf16 hi/lo planes, K padded to a multiple of 64;
+//   * the 128 reference points of a CTA are the MMA's M side (TMEM lanes) and the rows of one
+//     atom tile its N side (TMEM columns): the tile's vectors alpha-major, nvp (a multiple of 8)
+//     rows per alpha, N = 3 nvp rounded up to 16 <= 256; an atom with more vectors than a tile
+//     holds is split over several tiles;
+//   * an epilogue thread owns one reference point (a TMEM lane), so its coefficients come from
+//     coalesced rows of the kernel features, the sum over v stays in registers, and the three
+//     alpha columns of a vector share one coefficient pair;
+//   * CTA = one 128-point tile of Z (resident in shared memory) and a strided set of atom tiles,
+//     with a TMA producer warp, an MMA warp (two TMEM accumulators of 256 columns) and sixteen
+//     epilogue warps (four per lane quarter, splitting the vectors in chunks of eight); the
+//     quarter's partial sums meet in shared memory and are added to the force rows with FP32
+//     atomics (an atom split over tiles sums there too).
 // Every mbarrier wait is bounded: on expiry the CTA sets *err, waits (bounded) for its copies in
 // flight and frees its TMEM.
 #include <cuda.h>
@@ -24,7 +30,6 @@
 #include <algorithm>
 #include <vector>
 
-#include "krr.cuh"
 #include "mld_internal.h"
 #include "ptx.cuh"
 #include "tc.cuh"
@@ -37,13 +42,28 @@ using tc::kTM;
 using tc::kTileBytes;
 constexpr int kKEpiWarps = 16;
 constexpr int kKThreads = 32 * (2 + kKEpiWarps);
+constexpr int kBoxRows = 32;                   // rows per TMA box of a V tile
+constexpr int kBoxBytes = kBoxRows * kTK * 2;  // 4 KB
+constexpr int kChunks = 3;                      // vector chunks per epilogue warp and tile
+constexpr int kTmemCols = 512;                 // two accumulators of up to 256 columns
+
+// rows of a V tile: up to 256 for K <= 128 (two K blocks), 128 for three K blocks (shared memory)
+__host__ __device__ constexpr int max_tile_rows(int nkb) { return nkb <= 2 ? 256 : 128; }
+// vectors of a tile: 3 nvp <= rows, nvp a multiple of 8
+__host__ __device__ constexpr int max_tile_vectors(int nkb) { return max_tile_rows(nkb) / 3 / 8 * 8; }
+static_assert(max_tile_vectors(1) / 8 <= 4 * kChunks, "chunks per epilogue warp");
 
 struct TileMeta {
   int atom;  // target atom (batch index)
-  int ti;    // tile index within the atom
-  int nvp;   // rows per alpha of the atom (multiple of 32)
-  int nv;    // derivative vectors of the atom (its neighbours + 1)
+  int row0;  // first plane row of the tile within the chunk
+  int N;     // plane rows of the tile (MMA N): 3 nvp rounded up to 16
+  int nvp;   // rows per alpha (a multiple of 8)
+  int vr0;   // first vector record of the tile within the chunk (nvp records)
+  int v0;    // first derivative vector of the atom in this tile
+  int nvt;   // derivative vectors in this tile
+  int pad;
 };
+static_assert(sizeof(TileMeta) == 32, "tile records are 32 bytes");
 }  // namespace
 
 // Z (nk x KK, row-major) -> bf16 hi/lo planes (nk x KP), zero past KK.
@@ -58,25 +78,26 @@ __global__ void k_ktc_zplanes(const float* __restrict__ Z, int nk, int KK, int K
   lo[e] = __float2bfloat16_rn(v - __bfloat162float(h));
 }
 
-// Derivative vectors of atoms [a0, a1) as bf16 hi/lo planes (KP per row) plus per-row
-// centre, sign and g = V . x_centre.  One CTA (4 warps) per atom; warp w builds rows w, w + 4, ...
-// of the atom's tiles.  tile0[a - a0] is the atom's first tile within the chunk.
-__global__ void __launch_bounds__(128) k_ktc_vplanes(int a0, int a1, int KK, int KP, const int* __restrict__ nbr_off,
-                                                     const int* __restrict__ nbr_idx, const int* __restrict__ rev,
-                                                     const float* __restrict__ B, const float* __restrict__ dB,
-                                                     const int* __restrict__ tile0, __nv_bfloat16* __restrict__ hi,
-                                                     __nv_bfloat16* __restrict__ lo, int* __restrict__ rce,
-                                                     float* __restrict__ rsg, float* __restrict__ rg) {
-  const int a = a0 + blockIdx.x;
-  if (a >= a1) return;
+// The derivative vectors of a chunk's atom tiles as bf16 hi/lo planes (KP per row; rows past
+// 3 nvp of a tile are zero) and one 32-byte record per vector: {centre (int bits), sign / sqrt
+// f(x,x), sign dker_xx / (2 f(x,x) sqrt f(x,x)), 0} and {g_x, g_y, g_z, 0} with g = V . x_centre.
+// A padding vector has centre = the atom and zero factors; a centre without neighbours has zero
+// factors (krr_c12 of kernel_rows with the point terms left out).  One CTA (4 warps) per tile;
+// warp w builds rows w, w + 4, ... of the tile.
+__global__ void __launch_bounds__(128) k_ktc_vplanes(const TileMeta* __restrict__ tmeta, int KK, int KP,
+                                                     const int* __restrict__ nbr_off, const int* __restrict__ nbr_idx,
+                                                     const int* __restrict__ rev, const float* __restrict__ B,
+                                                     const float* __restrict__ dB, const float* __restrict__ at,
+                                                     __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                                                     float* __restrict__ vrec) {
+  const TileMeta m = tmeta[blockIdx.x];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int p0 = nbr_off[a], nn = nbr_off[a + 1] - p0, nv = nn + 1;
-  const int nvp = (nv + 31) / 32 * 32;
-  const int t0 = tile0[a - a0], nt = tile0[a - a0 + 1] - t0;
-  for (int lr = warp; lr < nt * kTM; lr += 4) {
-    const long long row = (long long)t0 * kTM + lr;
-    const int al = lr / nvp, v = lr - al * nvp;
-    const bool valid = al < 3 && v < nv;
+  const int a = m.atom;
+  const int p0 = nbr_off[a], nn = nbr_off[a + 1] - p0;
+  for (int lr = warp; lr < m.N; lr += 4) {
+    const long long row = (long long)m.row0 + lr;
+    const int al = lr / m.nvp, vl = lr - al * m.nvp, v = m.v0 + vl;
+    const bool valid = al < 3 && vl < m.nvt;
     int ce = a;
     const float* src = nullptr;  // pair row (v >= 1) or null for the self sum
     if (valid && v > 0) {
@@ -100,41 +121,76 @@ __global__ void __launch_bounds__(128) k_ktc_vplanes(int a0, int a1, int KK, int
       lo[row * KP + c] = __float2bfloat16_rn(x - __bfloat162float(h));
     }
     for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
-    if (lane == 0) {
-      rce[row] = ce;
-      rsg[row] = valid ? (v == 0 ? 1.f : -1.f) : 0.f;
-      rg[row] = g;
+    if (lane == 0 && al < 3) {
+      float* r = vrec + 8 * ((size_t)m.vr0 + vl);
+      r[4 + al] = g;
+      if (al == 0) {
+        float f1 = 0.f, f2 = 0.f;
+        if (valid) {
+          const float4 a4 = *reinterpret_cast<const float4*>(at + 4 * (size_t)ce);
+          const float sg = v == 0 ? 1.f : -1.f;
+          if (a4.w != 0.f) {
+            f1 = sg / a4.y;
+            f2 = a4.z / (2.f * a4.x) * f1;
+          }
+        }
+        r[0] = __int_as_float(ce);
+        r[1] = f1;
+        r[2] = f2;
+        r[3] = 0.f;
+        r[7] = 0.f;
+      }
     }
   }
 }
 
-// CTA (blockIdx.x = 128-point tile of Z, blockIdx.y = g): row tiles t = g, g + G, ... of the
-// chunk.  Shared memory: the Z tile (nkb K blocks x hi, lo), `stages` row-tile stages, and the
-// coefficient table of the current tile's atom: (c1, c2) per (reference point, derivative
-// vector), tab[k * (tabv + 1) + v], filled with coalesced loads of the kernel features while the
-// MMAs of the tile run (an atom with more than tabv vectors reads them per element instead).
+namespace {
+// 3 x 8 consecutive TMEM columns (at taddr, taddr + stride, taddr + 2 stride) of the warp's 32
+// lanes into registers, waited for inside the same statement
+__device__ __forceinline__ void tmem_ld3x8(uint32_t taddr, uint32_t stride, float* out) {
+  uint32_t v[24];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%24];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%25];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16,%17,%18,%19,%20,%21,%22,%23}, [%26];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+        "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23])
+      : "r"(taddr), "r"(taddr + stride), "r"(taddr + 2 * stride)
+      : "memory");
+#pragma unroll
+  for (int c = 0; c < 24; ++c) out[c] = __uint_as_float(v[c]);
+}
+}  // namespace
+
+// CTA (blockIdx.x = 128-point tile of Z, blockIdx.y = g): atom tiles t = g, g + G, ... of the
+// chunk.  Shared memory: the Z tile (nkb K blocks x hi, lo), one V tile stage (nkb x hi, lo blocks
+// of max_tile_rows rows), the vector records of three tiles (the current one, the next one whose
+// kernel features are being fetched, and the one after, being staged), and the quarters' partial
+// sums of two tiles.  The epilogue fetches the kernel features of tile i + 1 into registers
+// before it waits for the accumulator of tile i + 1.
 __global__ void __launch_bounds__(kKThreads, 1)
     k_krr_force_tc(const __grid_constant__ CUtensorMap vhi, const __grid_constant__ CUtensorMap vlo,
                    const __grid_constant__ CUtensorMap zhi, const __grid_constant__ CUtensorMap zlo, int ntiles,
-                   int nkb, int stages, int nk, const TileMeta* __restrict__ tmeta, const int* __restrict__ rce,
-                   const float* __restrict__ rsg, const float* __restrict__ rg, const float* __restrict__ F,
-                   const float* __restrict__ at, const float* __restrict__ szz, float s2, float l2, float pw,
+                   int nkb, int nk, const TileMeta* __restrict__ tmeta, const float4* __restrict__ vrec,
+                   const float* __restrict__ F, const float* __restrict__ szz, float s2, float l2, float pw,
                    const int* __restrict__ atom_struct, const int* __restrict__ atom_start,
-                   const long long* __restrict__ rowF, int c0, int ldx, float* __restrict__ X, int tabv,
-                   int* __restrict__ err) {
+                   const long long* __restrict__ rowF, int c0, int ldx, float* __restrict__ X, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  unsigned char* btile = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  const uint32_t opb = (uint32_t)nkb * 2 * kTileBytes;  // bytes of one operand tile set (hi and lo blocks)
-  unsigned char* atile = btile + opb;
-  float2* tab = reinterpret_cast<float2*>(atile + (size_t)stages * opb);  // kTM x (tabv + 1)
-  float* iszz = reinterpret_cast<float*>(tab + (size_t)kTM * (tabv + 1));  // kTM: 1 / szz of the CTA's points
-  float2* fac = reinterpret_cast<float2*>(iszz + kTM);                      // tabv: per-vector centre factors
-  uint64_t* bfull = reinterpret_cast<uint64_t*>(fac + tabv + (tabv & 1));
+  unsigned char* ztile = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const uint32_t zbytes = (uint32_t)nkb * 2 * kTileBytes;
+  const uint32_t vblk = (uint32_t)max_tile_rows(nkb) * kTK * 2;  // one K block of one plane
+  const int nvmax = max_tile_vectors(nkb);
+  unsigned char* vtile = ztile + zbytes;
+  float4* srec = reinterpret_cast<float4*>(vtile + (size_t)nkb * 2 * vblk);  // [3][2 nvmax]
+  float* red = reinterpret_cast<float*>(srec + 3 * 2 * nvmax);               // [2][4][3][4][32]
+  uint64_t* bfull = reinterpret_cast<uint64_t*>(red + 2 * 4 * 3 * 4 * 32);
   uint64_t* full = bfull + 1;
-  uint64_t* empty = full + stages;
-  uint64_t* tfull = empty + stages;  // [2] accumulator ready
-  uint64_t* tempty = tfull + 2;      // [2] accumulator drained
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
+  uint64_t* empty = bfull + 2;
+  uint64_t* tfull = bfull + 3;   // [2] accumulator ready
+  uint64_t* tempty = bfull + 5;  // [2] accumulator drained
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bfull + 7);
 
   const int n0 = blockIdx.x * kTM;
   const int g = blockIdx.y, G = gridDim.y;
@@ -143,10 +199,8 @@ __global__ void __launch_bounds__(kKThreads, 1)
 
   if (threadIdx.x == 0) {
     ptx::mbar_init(bfull, 1);
-    for (int s = 0; s < stages; ++s) {
-      ptx::mbar_init(&full[s], 1);
-      ptx::mbar_init(&empty[s], 1);
-    }
+    ptx::mbar_init(full, 1);
+    ptx::mbar_init(empty, 1);
     for (int b = 0; b < 2; ++b) {
       ptx::mbar_init(&tfull[b], 1);
       ptx::mbar_init(&tempty[b], kKEpiWarps);
@@ -155,7 +209,7 @@ __global__ void __launch_bounds__(kKThreads, 1)
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(ptx::smem_u32(tmem_slot)),
-                 "r"(2 * kTM));
+                 "n"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -165,121 +219,112 @@ __global__ void __launch_bounds__(kKThreads, 1)
   bool ok = true;
 
   if (warp == 0 && lane == 0) {
-    // producer: the Z tile once, then the row tiles
-    ptx::mbar_expect_tx(bfull, opb);
+    // producer: the Z tile once, then the atom tiles in 32-row boxes (the rows past a tile's N
+    // belong to the next tile or to the chunk's spare rows and feed unused accumulator columns)
+    ptx::mbar_expect_tx(bfull, zbytes);
     for (int kb = 0; kb < nkb; ++kb) {
-      ptx::tma_load_2d(btile + (2 * kb) * kTileBytes, &zhi, kb * kTK, n0, bfull);
-      ptx::tma_load_2d(btile + (2 * kb + 1) * kTileBytes, &zlo, kb * kTK, n0, bfull);
+      ptx::tma_load_2d(ztile + (2 * kb) * kTileBytes, &zhi, kb * kTK, n0, bfull);
+      ptx::tma_load_2d(ztile + (2 * kb + 1) * kTileBytes, &zlo, kb * kTK, n0, bfull);
     }
     int issued = 0;
     for (int i = 0; i < nmine; ++i) {
-      const int s = i % stages;
-      if (i >= stages && !ptx::mbar_wait(&empty[s], ((i / stages) - 1) & 1)) {
+      if (i >= 1 && !ptx::mbar_wait(empty, (i - 1) & 1)) {
         ok = false;
         break;
       }
-      const int t = g + i * G;
-      unsigned char* st = atile + (size_t)s * opb;
-      ptx::mbar_expect_tx(&full[s], opb);
-      for (int kb = 0; kb < nkb; ++kb) {
-        ptx::tma_load_2d(st + (2 * kb) * kTileBytes, &vhi, kb * kTK, t * kTM, &full[s]);
-        ptx::tma_load_2d(st + (2 * kb + 1) * kTileBytes, &vlo, kb * kTK, t * kTM, &full[s]);
-      }
+      const TileMeta m = tmeta[g + i * G];
+      const int nbox = (m.N + kBoxRows - 1) / kBoxRows;
+      ptx::mbar_expect_tx(full, (uint32_t)(nkb * 2 * nbox * kBoxBytes));
+      for (int kb = 0; kb < nkb; ++kb)
+        for (int j = 0; j < nbox; ++j) {
+          ptx::tma_load_2d(vtile + (2 * kb) * vblk + j * kBoxBytes, &vhi, kb * kTK, m.row0 + j * kBoxRows, full);
+          ptx::tma_load_2d(vtile + (2 * kb + 1) * vblk + j * kBoxBytes, &vlo, kb * kTK, m.row0 + j * kBoxRows,
+                           full);
+        }
       issued = i + 1;
     }
     // copies still in flight are waited for (bounded) before leaving
-    for (int i = max(0, issued - stages); i < issued; ++i) ptx::mbar_wait(&full[i % stages], (i / stages) & 1);
+    if (issued > 0) ptx::mbar_wait(full, (issued - 1) & 1);
     ptx::mbar_wait(bfull, 0);
   } else if (warp == 1 && lane == 0) {
-    // MMA issuer: row tile i into TMEM buffer i & 1
+    // MMA issuer: atom tile i into TMEM buffer i & 1 (columns 256 (i & 1) + [0, N))
     if (nmine > 0 && !ptx::mbar_wait(bfull, 0)) ok = false;
-    const uint32_t sb = ptx::smem_u32(btile);
+    const uint32_t sz = ptx::smem_u32(ztile), sv = ptx::smem_u32(vtile);
     for (int i = 0; i < nmine && ok; ++i) {
-      const int b = i & 1, s = i % stages;
+      const int b = i & 1;
       if (i >= 2 && !ptx::mbar_wait(&tempty[b], ((i >> 1) - 1) & 1)) {
         ok = false;
         break;
       }
-      if (!ptx::mbar_wait(&full[s], (i / stages) & 1)) {
+      if (!ptx::mbar_wait(full, i & 1)) {
         ok = false;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t acc = tmem + (uint32_t)(b * kTM);
-      const uint32_t sa = ptx::smem_u32(atile + (size_t)s * opb);
+      const uint32_t idesc = tc::idesc_m128(tmeta[g + i * G].N);
+      const uint32_t acc = tmem + (uint32_t)(b * (kTmemCols / 2));
       for (int kb = 0; kb < nkb; ++kb) {
 #pragma unroll
         for (int kk = 0; kk < kTK / 16; ++kk) {
           const uint32_t off = kk * 32;  // 16 bf16 along K inside the 128-byte swizzle row
-          const uint64_t ahi = tc::sw128_desc(sa + (2 * kb) * kTileBytes + off);
-          const uint64_t alo = tc::sw128_desc(sa + (2 * kb + 1) * kTileBytes + off);
-          const uint64_t bhi = tc::sw128_desc(sb + (2 * kb) * kTileBytes + off);
-          const uint64_t blo = tc::sw128_desc(sb + (2 * kb + 1) * kTileBytes + off);
-          tc::mma_bf16(acc, ahi, bhi, (kb > 0 || kk > 0) ? 1u : 0u);
-          tc::mma_bf16(acc, ahi, blo, 1u);
-          tc::mma_bf16(acc, alo, bhi, 1u);
+          const uint64_t zh = tc::sw128_desc(sz + (2 * kb) * kTileBytes + off);
+          const uint64_t zl = tc::sw128_desc(sz + (2 * kb + 1) * kTileBytes + off);
+          const uint64_t vh = tc::sw128_desc(sv + (2 * kb) * vblk + off);
+          const uint64_t vl = tc::sw128_desc(sv + (2 * kb + 1) * vblk + off);
+          tc::mma_bf16_id(acc, zh, vh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+          tc::mma_bf16_id(acc, zl, vh, idesc, 1u);
+          tc::mma_bf16_id(acc, zh, vl, idesc, 1u);
         }
       }
-      tc::mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
+      tc::mma_commit(empty);  // frees the stage once these MMAs have read it
       tc::mma_commit(&tfull[b]);
     }
   } else if (warp >= 2) {
-    // epilogue: lane quarter q (32 rows of one atom and one alpha), 32 reference points
-    const int q = warp & 3, cq = (warp - 2) >> 2;
+    // epilogue: lane quarter q (reference points n0 + 32 q + lane), vector chunks sub, sub + 4, ...
+    const int q = warp & 3, sub = (warp - 2) >> 2;
     const int etid = threadIdx.x - 64;  // 0 .. 511 over the epilogue warps
+    const int k = n0 + q * 32 + lane;
+    const bool kv = k < nk;
     const float il2 = 1.f / l2;
+    const float izk = kv ? 1.f / szz[k] : 0.f;  // zero past nk: every coefficient vanishes
+    const float k1 = pw * il2 * izk;
     const int ipw = (int)pw;
     const bool int_pow = (float)ipw == pw && ipw >= 1 && ipw <= 8;
-    if (etid < kTM) iszz[etid] = (n0 + etid < nk) ? 1.f / szz[n0 + etid] : 0.f;
+    // the records of tile j into buffer j % 3 (two float4 per vector)
+    auto stage = [&](int j) {
+      if (j >= nmine) return;
+      const TileMeta m = tmeta[g + j * G];
+      float4* d = srec + (j % 3) * 2 * nvmax;
+      const float4* s = vrec + 2 * (size_t)m.vr0;
+      for (int e = etid; e < 2 * m.nvp; e += kKEpiWarps * 32) d[e] = s[e];
+    };
+    // the kernel features F[centre of v, k] of the warp's vectors of tile j (coalesced rows)
+    float xf[kChunks][8];
+    auto fetch = [&](int j) {
+      if (j >= nmine) return;
+      const int nch = tmeta[g + j * G].nvp >> 3;
+      const float4* s = srec + (j % 3) * 2 * nvmax;
+#pragma unroll
+      for (int cc = 0; cc < kChunks; ++cc) {
+        const int c = sub + 4 * cc;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          float x = 0.f;
+          if (c < nch && kv) x = __ldg(F + (size_t)__float_as_int(s[2 * (c * 8 + u)].x) * nk + k);
+          xf[cc][u] = x;
+        }
+      }
+    };
+    stage(0);
+    stage(1);
+    asm volatile("bar.sync 1, %0;" ::"n"(kKEpiWarps * 32));
+    fetch(0);
     bool got = true;
     for (int i = 0; i < nmine; ++i) {
       const int b = i & 1;
-      const int t = g + i * G;
-      const TileMeta tm = tmeta[t];
-      const bool use_tab = tm.nv <= tabv;
-      // coefficient table of the tile's atom (the previous tile's reads are done at the barrier)
-      asm volatile("bar.sync 1, %0;" ::"n"(kKEpiWarps * 32));
-      if (use_tab) {
-        // per vector: the centre's factors 1 / sqrt f(x,x) and dker_xx / (2 f(x,x) sqrt f(x,x)), zero
-        // for a centre without neighbours (krr_c12 with the divisions taken out of the entries)
-        const long long r0 = (long long)(t - tm.ti) * kTM;  // the atom's alpha = 0 rows: vector v = row
-        if (etid < tm.nv) {
-          const float4 a4 = *reinterpret_cast<const float4*>(at + 4 * (size_t)rce[r0 + etid]);
-          const float f1 = a4.w == 0.f ? 0.f : 1.f / a4.y;
-          fac[etid] = make_float2(f1, a4.z / (2.f * a4.x) * f1);
-        }
-        asm volatile("bar.sync 3, %0;" ::"n"(kKEpiWarps * 32));
-        // four entries per thread and pass, their loads issued together (the kernel features of
-        // the neighbour centres are scattered rows of F)
-        const int nvk = tm.nv * kTM;
-        constexpr int kU = 4, kStep = kKEpiWarps * 32;
-        for (int e0 = etid; e0 < nvk; e0 += kU * kStep) {
-          float xf[kU];
-#pragma unroll
-          for (int u = 0; u < kU; ++u) {
-            const int e = e0 + u * kStep, k = n0 + (e & (kTM - 1));
-            xf[u] = (e < nvk && k < nk) ? F[(size_t)rce[r0 + (e >> 7)] * nk + k] : 0.f;
-          }
-#pragma unroll
-          for (int u = 0; u < kU; ++u) {
-            const int e = e0 + u * kStep;
-            if (e >= nvk) break;
-            const int kl = e & (kTM - 1), v = e >> 7;
-            const float base = s2 + xf[u] * il2;
-            float bp1 = 1.f;  // base^(p - 1)
-            if (int_pow) {
-              for (int j = 1; j < ipw; ++j) bp1 *= base;
-            } else {
-              bp1 = powf(base, pw - 1.f);
-            }
-            const float2 f = fac[v];
-            const float sc = iszz[kl];  // zero past nk
-            tab[(size_t)kl * (tabv + 1) + v] = make_float2(pw * bp1 * il2 * sc * f.x, bp1 * base * sc * f.y);
-          }
-        }
-      }
-      // the accumulator; the barrier also publishes the table, and a timed-out wait in any
-      // epilogue warp ends the loop for all of them together
+      const TileMeta m = tmeta[g + i * G];
+      // the accumulator; the barrier also publishes the records staged one tile earlier, and a
+      // timed-out wait in any epilogue warp ends the loop for all of them together
       const bool ready = ptx::mbar_wait(&tfull[b], (i >> 1) & 1);
       int any_fail;
       asm volatile(
@@ -291,53 +336,52 @@ __global__ void __launch_bounds__(kKThreads, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-      float v[32];
+      const float4* s = srec + (i % 3) * 2 * nvmax;
+      const int nch = m.nvp >> 3;
+      const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * (kTmemCols / 2));
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f;
 #pragma unroll
-      for (int h = 0; h < 4; ++h)
-        tc::tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kTM + cq * 32 + h * 8), v + h * 8);
+      for (int cc = 0; cc < kChunks; ++cc) {
+        const int c = sub + 4 * cc;
+        if (c < nch) {
+          float d[24];
+          tmem_ld3x8(tq + (uint32_t)(c * 8), (uint32_t)m.nvp, d);
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const float4 r = s[2 * (c * 8 + u)], gg = s[2 * (c * 8 + u) + 1];
+            const float base = fmaf(xf[cc][u], il2, s2);
+            float bp1 = 1.f;  // base^(p - 1)
+            if (int_pow) {
+              for (int j = 1; j < ipw; ++j) bp1 *= base;
+            } else {
+              bp1 = powf(base, pw - 1.f);
+            }
+            const float c1 = k1 * r.y * bp1, c2 = izk * base * bp1 * r.z;
+            a0 = fmaf(c1, d[u], fmaf(-c2, gg.x, a0));
+            a1 = fmaf(c1, d[8 + u], fmaf(-c2, gg.y, a1));
+            a2 = fmaf(c1, d[16 + u], fmaf(-c2, gg.z, a2));
+          }
+        }
+      }
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(&tempty[b]);
-      const int lr0 = tm.ti * kTM + q * 32;
-      const int al = lr0 / tm.nvp;  // the same for the whole quarter
-      if (al >= 3) continue;        // padding quarter
-      const long long row = (long long)t * kTM + q * 32 + lane;
-      const int vi = lr0 + lane - al * tm.nvp;  // derivative vector of this row
-      const float sg = rsg[row], gv = rg[row];
-      const int ce = rce[row];
-#pragma unroll
-      for (int c = 0; c < 32; ++c) {
-        const int kl = cq * 32 + c, k = n0 + kl;
-        float val = 0.f;
-        if (sg != 0.f && k < nk) {
-          float c1, c2;
-          if (use_tab) {
-            const float2 cc = tab[(size_t)kl * (tabv + 1) + vi];
-            c1 = cc.x;
-            c2 = cc.y;
-          } else {
-            krr_c12<float>(F[(size_t)ce * nk + k], at + 4 * (size_t)ce, szz[k], s2, l2, pw, c1, c2);
-          }
-          val = sg * (c1 * v[c] - c2 * gv);
-        }
-        v[c] = val;
+      // the quarter's four partial sums per alpha, added in a fixed order
+      float* rq = red + (size_t)((i & 1) * 4 + q) * 3 * 4 * 32;  // [alpha][sub][lane]
+      rq[(0 * 4 + sub) * 32 + lane] = a0;
+      rq[(1 * 4 + sub) * 32 + lane] = a1;
+      rq[(2 * 4 + sub) * 32 + lane] = a2;
+      asm volatile("bar.sync %0, %1;" ::"r"(4 + q), "n"(128));
+      if (sub < 3) {
+        const float* ra = rq + sub * 4 * 32 + lane;
+        const float sum = ((ra[0] + ra[32]) + ra[64]) + ra[96];
+        const int a = m.atom, sidx = atom_struct[a];
+        const long long rf = rowF[sidx];
+        if (kv && rf >= 0 && sum != 0.f)
+          atomicAdd(&X[(rf + 3LL * (a - atom_start[sidx]) + sub) * ldx + c0 + k], sum);
       }
-      // sum over the quarter's 32 rows: transposing butterfly, lane c ends with column c
-#pragma unroll
-      for (int sh = 16; sh >= 1; sh >>= 1) {
-#pragma unroll
-        for (int j = 0; j < sh; ++j) {
-          const bool up = (lane & sh) != 0;
-          const float send = up ? v[j] : v[j + sh];
-          const float keep = up ? v[j + sh] : v[j];
-          v[j] = keep + __shfl_xor_sync(0xffffffffu, send, sh);
-        }
-      }
-      const int k = n0 + cq * 32 + lane;
-      const int a = tm.atom, sidx = atom_struct[a];
-      const long long rf = rowF[sidx];
-      if (k < nk && rf >= 0 && v[0] != 0.f)
-        atomicAdd(&X[(rf + 3LL * (a - atom_start[sidx]) + al) * ldx + c0 + k], v[0]);
+      stage(i + 2);
+      fetch(i + 1);
     }
     if (!got && lane == 0) atomicExch(err, 1);
   }
@@ -346,15 +390,36 @@ __global__ void __launch_bounds__(kKThreads, 1)
   __syncthreads();
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kTM));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(kTmemCols));
   }
 }
 
 bool krr_force_tc_available() { return tc::encode_fn() != nullptr; }
 
+namespace {
+size_t al256(size_t x) { return (x + 255) / 256 * 256; }
+// split of an atom with nv derivative vectors into tiles: count, and vectors of tile j
+int tiles_of(int nv, int nvmax) { return (nv + nvmax - 1) / nvmax; }
+int tile_vectors(int nv, int ns, int j) { return nv / ns + (j < nv % ns ? 1 : 0); }
+int rows_of(int nvp) { return (3 * nvp + 15) / 16 * 16; }
+// workspace of a chunk: planes (with a spare box of rows), vector records, tile records
+size_t chunk_bytes(size_t rows, size_t vecs, size_t tiles, int KP) {
+  return 2 * al256((rows + kBoxRows) * (size_t)KP * 2) + al256(vecs * 32) + al256(tiles * sizeof(TileMeta));
+}
+}  // namespace
+
+size_t krr_force_tc_workspace_bytes(long long atoms, int maxnv, int nk, int KK) {
+  const int nkb = (KK + kTK - 1) / kTK, KP = nkb * kTK;
+  const int nvmax = max_tile_vectors(std::min(nkb, 3));
+  const int ns = tiles_of(std::max(maxnv, 1), nvmax);
+  const int nvp = (tile_vectors(std::max(maxnv, 1), ns, 0) + 7) / 8 * 8;
+  const size_t tiles = (size_t)atoms * ns;
+  return 2 * al256((size_t)nk * KP * 2) + 8 * 256 + chunk_bytes(tiles * rows_of(nvp), tiles * nvp, tiles, KP);
+}
+
 // Force rows of the kernel block (columns [c0, c0 + nk) of X) for every atom with force rows,
 // replacing k_krr_force_tiled for the FP32 rows.  ws (ws_bytes) holds the Z planes and, per
-// chunk of atoms, the derivative-vector planes and their row and tile records; chunks are as
+// chunk of atoms, the derivative-vector planes and their vector and tile records; chunks are as
 // large as ws allows.  F, at, szz: the kernel features, atom terms and point norms of
 // launch_krr_rows.  X must hold zeros in these columns (the sums are added atomically).
 cudaError_t launch_krr_force_tc(const DevBatch& b, const DevRows& rows, const int* rev, const float* Bq,
@@ -365,46 +430,32 @@ cudaError_t launch_krr_force_tc(const DevBatch& b, const DevRows& rows, const in
   if (b.A == 0 || nk == 0) return cudaSuccess;
   const int nkb = (KK + kTK - 1) / kTK;
   const int KP = nkb * kTK;
-  if (nkb > 3) return cudaErrorInvalidValue;  // K blocks beyond the shared-memory budget
-  // one row-tile stage: the epilogue (coefficients, reduction) bounds the tile rate, and the rest
-  // of shared memory holds the coefficient table of up to tabv derivative vectors
-  const int stages = 1;
-  const size_t opb = (size_t)nkb * 2 * kTileBytes;
+  if (KK > kKrrTcMaxK) return cudaErrorInvalidValue;  // K blocks beyond the shared-memory budget
+  const int nvmax = max_tile_vectors(nkb);
+  const size_t vblk = (size_t)max_tile_rows(nkb) * kTK * 2;
+  const size_t smem = 1024 + (size_t)nkb * 2 * kTileBytes + (size_t)nkb * 2 * vblk + 3 * 2 * (size_t)nvmax * 16 +
+                      2 * 4 * 3 * 4 * 32 * 4 + 8 * 7 + 8;
   const size_t kSmemMax = 227 * 1024;
-  const size_t fixed = 1024 + (1 + (size_t)stages) * opb + 8 * (3 + 2 * (size_t)stages + 4) + 16 + 4 * kTM + 8 * 66;
-  if (fixed + (size_t)kTM * 8 * 2 > kSmemMax) return cudaErrorInvalidValue;
-  const int tabv = (int)std::min<size_t>(64, (kSmemMax - fixed) / ((size_t)kTM * 8) - 1);
-  const size_t smem = fixed + (size_t)kTM * 8 * (tabv + 1);
+  if (smem > kSmemMax) return cudaErrorInvalidValue;
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_krr_force_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(k_krr_force_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  if (smem > kSmemMax) return cudaErrorInvalidValue;
-  // per-atom tiles from the neighbour counts
+  // atom tiles from the neighbour counts
   std::vector<int> off(b.A + 1);
   cudaError_t e = cudaMemcpyAsync(off.data(), b.nbr_off, sizeof(int) * (b.A + 1), cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return e;
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return e;
-  std::vector<int> ntile(b.A), nvp(b.A);
-  for (int a = 0; a < b.A; ++a) {
-    const int nv = off[a + 1] - off[a] + 1;
-    nvp[a] = (nv + 31) / 32 * 32;
-    ntile[a] = (3 * nvp[a] + kTM - 1) / kTM;
-  }
-  // workspace: Z planes, then the chunk's planes (4 KP bytes per row), row records (12 bytes per
-  // row), tile records and the atoms' first tiles
-  auto al256 = [](size_t x) { return (x + 255) / 256 * 256; };
+  // workspace: Z planes, then the chunk's planes, vector records and tile records
   unsigned char* w = static_cast<unsigned char*>(ws);
   const size_t zb = al256((size_t)nk * KP * 2);
   __nv_bfloat16* zhi = reinterpret_cast<__nv_bfloat16*>(w);
   __nv_bfloat16* zlo = reinterpret_cast<__nv_bfloat16*>(w + zb);
-  const size_t per_tile = (size_t)kTM * (4 * (size_t)KP + 12) + sizeof(TileMeta) + 4;
-  if (ws_bytes < 2 * zb + 8 * 256 + per_tile * 16 + 8) return cudaErrorInvalidValue;
+  if (ws_bytes < 2 * zb + 8 * 256) return cudaErrorInvalidValue;
   const size_t room = ws_bytes - 2 * zb - 8 * 256;
-  const long long max_tiles = (long long)(room / per_tile) - 1;
   {
     const long long n = (long long)nk * KP;
     k_ktc_zplanes<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(Z, nk, KK, KP, zhi, zlo);
@@ -415,53 +466,57 @@ cudaError_t launch_krr_force_tc(const DevBatch& b, const DevRows& rows, const in
     return cudaErrorInvalidValue;
   const float s2 = (float)(sigma * sigma), l2 = (float)(2.0 * length * length), pw = (float)power;
   const int NT = (nk + kTM - 1) / kTM;
-  std::vector<int> tile0;
   std::vector<TileMeta> meta;
   for (int a0 = 0; a0 < b.A;) {
     // the largest run of atoms whose tiles fit the workspace
-    long long nt = 0;
-    int a1 = a0;
-    while (a1 < b.A && nt + ntile[a1] <= max_tiles) nt += ntile[a1++];
-    if (a1 == a0) return cudaErrorInvalidValue;  // one atom alone exceeds the workspace
-    tile0.assign(a1 - a0 + 1, 0);
     meta.clear();
-    for (int a = a0; a < a1; ++a) {
-      tile0[a - a0 + 1] = tile0[a - a0] + ntile[a];
-      for (int ti = 0; ti < ntile[a]; ++ti) meta.push_back(TileMeta{a, ti, nvp[a], off[a + 1] - off[a] + 1});
+    size_t nrows = 0, nvecs = 0;
+    int a1 = a0;
+    while (a1 < b.A) {
+      const int nv = off[a1 + 1] - off[a1] + 1, ns = tiles_of(nv, nvmax);
+      size_t r = 0, v = 0;
+      for (int j = 0; j < ns; ++j) {
+        const int nvp = (tile_vectors(nv, ns, j) + 7) / 8 * 8;
+        r += rows_of(nvp);
+        v += nvp;
+      }
+      if (chunk_bytes(nrows + r, nvecs + v, meta.size() + ns, KP) > room) break;
+      for (int j = 0, v0 = 0; j < ns; ++j) {
+        const int nvt = tile_vectors(nv, ns, j), nvp = (nvt + 7) / 8 * 8;
+        meta.push_back(TileMeta{a1, (int)nrows, rows_of(nvp), nvp, (int)nvecs, v0, nvt, 0});
+        nrows += rows_of(nvp);
+        nvecs += nvp;
+        v0 += nvt;
+      }
+      ++a1;
     }
-    const size_t rows_c = (size_t)nt * kTM;
+    if (a1 == a0) return cudaErrorInvalidValue;  // one atom alone exceeds the workspace
+    const size_t nt = meta.size();
     unsigned char* p = w + 2 * zb;
     __nv_bfloat16* vhi = reinterpret_cast<__nv_bfloat16*>(p);
-    p += al256(rows_c * KP * 2);
+    p += al256((nrows + kBoxRows) * KP * 2);
     __nv_bfloat16* vlo = reinterpret_cast<__nv_bfloat16*>(p);
-    p += al256(rows_c * KP * 2);
-    int* rce = reinterpret_cast<int*>(p);
-    p += al256(rows_c * 4);
-    float* rsg = reinterpret_cast<float*>(p);
-    p += al256(rows_c * 4);
-    float* rg = reinterpret_cast<float*>(p);
-    p += al256(rows_c * 4);
+    p += al256((nrows + kBoxRows) * KP * 2);
+    float* vrec = reinterpret_cast<float*>(p);
+    p += al256(nvecs * 32);
     TileMeta* dmeta = reinterpret_cast<TileMeta*>(p);
-    p += al256(sizeof(TileMeta) * meta.size());
-    int* dtile0 = reinterpret_cast<int*>(p);
-    e = cudaMemcpyAsync(dmeta, meta.data(), sizeof(TileMeta) * meta.size(), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(dtile0, tile0.data(), sizeof(int) * tile0.size(), cudaMemcpyHostToDevice, st);
+    e = cudaMemcpyAsync(dmeta, meta.data(), sizeof(TileMeta) * nt, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
-    k_ktc_vplanes<<<(unsigned)(a1 - a0), 128, 0, st>>>(a0, a1, KK, KP, b.nbr_off, b.nbr_idx, rev, Bq, dBq, dtile0,
-                                                      vhi, vlo, rce, rsg, rg);
+    k_ktc_vplanes<<<(unsigned)nt, 128, 0, st>>>(dmeta, KK, KP, b.nbr_off, b.nbr_idx, rev, Bq, dBq, at, vhi, vlo,
+                                                vrec);
     CUtensorMap mvh, mvl;
-    if (!tc::make_plane_map(&mvh, vhi, KP, (long long)rows_c, KP) ||
-        !tc::make_plane_map(&mvl, vlo, KP, (long long)rows_c, KP))
+    if (!tc::make_plane_map(&mvh, vhi, KP, (long long)(nrows + kBoxRows), KP, kBoxRows) ||
+        !tc::make_plane_map(&mvl, vlo, KP, (long long)(nrows + kBoxRows), KP, kBoxRows))
       return cudaErrorInvalidValue;
-    const int G = std::max(1, std::min<int>((int)nt, (2 * nsm + NT - 1) / NT));
+    // one CTA per SM: the column tiles times G row groups in a single wave
+    const int G = std::max(1, std::min<int>((int)nt, NT >= nsm ? 1 : nsm / NT));
     k_krr_force_tc<<<dim3((unsigned)NT, (unsigned)G), kKThreads, smem, st>>>(
-        mvh, mvl, mzh, mzl, (int)nt, nkb, stages, nk, dmeta, rce, rsg, rg, F, at, szz, s2, l2, pw, b.atom_struct,
-        b.atom_start, rows.rowF, c0, rows.ldx, X, tabv, err);
+        mvh, mvl, mzh, mzl, (int)nt, nkb, nk, dmeta, reinterpret_cast<const float4*>(vrec), F, szz, s2, l2, pw,
+        b.atom_struct, b.atom_start, rows.rowF, c0, rows.ldx, X, err);
     *launches += 2;
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    // the host records of the next chunk overwrite dmeta / dtile0 only after this chunk's kernels
+    // the host records of the next chunk overwrite dmeta only after this chunk's kernels
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;
     a0 = a1;

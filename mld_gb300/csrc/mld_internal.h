@@ -276,8 +276,11 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
                             double sign_stress, double sign_big, T* ws, T* X, int c0, cudaStream_t st,
                             int* launches, void* tcws = nullptr, size_t tcws_bytes = 0, int* err = nullptr,
                             int nsm = 0);
-// kernel-block force rows on the tensor cores (krr_tc.cu)
+// kernel-block force rows on the tensor cores (krr_tc.cu); the workspace that holds all `atoms`
+// (maxnv derivative vectors at most) in one chunk
+constexpr int kKrrTcMaxK = 192;  // three K blocks of 64 in shared memory
 bool krr_force_tc_available();
+size_t krr_force_tc_workspace_bytes(long long atoms, int maxnv, int nk, int KK);
 cudaError_t launch_krr_force_tc(const DevBatch& b, const DevRows& rows, const int* rev, const float* Bq,
                                 const float* dBq, const float* Z, const float* F, const float* at, const float* szz,
                                 int nk, int KK, double power, double length, double sigma, void* ws, size_t ws_bytes,

@@ -29,14 +29,21 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
 
 // kind::f16 instruction descriptor: D FP32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1),
 // both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28; M = N = 128.
-constexpr uint32_t kIdesc =
-    (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTM >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
+__host__ __device__ constexpr uint32_t idesc_m128(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
+}
+constexpr uint32_t kIdesc = idesc_m128(kTM);
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+// D (TMEM) += A B^T with the given instruction descriptor (M = 128, N a multiple of 16, <= 256)
+__device__ __forceinline__ void mma_bf16_id(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                            uint32_t accumulate) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  mma_bf16_id(tmem_d, a, b, kIdesc, accumulate);
 }
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -70,13 +77,14 @@ inline EncodeTiledFn encode_fn() {
   return fn;
 }
 // bf16 plane of `outer` rows x `inner` K elements (row stride row_elems * 2 bytes, a multiple of
-// 16 bytes); box 64 (K) x 128 (rows), 128-byte swizzle; rows past `outer` read as zero
-inline bool make_plane_map(CUtensorMap* m, void* base, long long inner, long long outer, long long row_elems) {
+// 16 bytes); box 64 (K) x box_rows, 128-byte swizzle; rows past `outer` read as zero
+inline bool make_plane_map(CUtensorMap* m, void* base, long long inner, long long outer, long long row_elems,
+                           int box_rows = kTM) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
   cuuint64_t strides[1] = {(cuuint64_t)row_elems * 2};
-  cuuint32_t box[2] = {(cuuint32_t)kTK, (cuuint32_t)kTM};
+  cuuint32_t box[2] = {(cuuint32_t)kTK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,

@@ -107,3 +107,64 @@ def test_kernel_points_validation(lib):
         with pytest.raises(_lib.MldError) as ei:
             h.design_matrix()  # no reference points yet
         assert ei.value.code == 6
+
+
+@pytest.mark.parametrize("j_max,r_cut,channels,system", [
+    (4.0, 4.7, 2, "hea"),   # K = 110: two K blocks of the tensor-core tiles
+    (4.0, 4.7, 3, "hea"),   # K = 165: three K blocks, at most 40 vectors per tile
+    (4.0, 6.0, 3, "hea"),   # about 65 vectors per atom: atoms split over two tiles
+    (2.0, 6.6, 1, "fe"),    # 89 vectors per atom: split with one K block
+])
+def test_kernel_force_rows_mixed_vs_plain(lib, j_max, r_cut, channels, system):
+    """FP32 kernel rows (force rows on the tensor cores) against the FP64 rows of the same
+    handle setup, over K-block counts and atoms split over several tiles."""
+    from mld_gb300 import _lib, synth
+    if system == "fe":
+        ds = synth.fe_bcc_batched(n_struct=3, nmin=16, nmax=60, seed=5)
+        els, w2, w3 = ["Fe"], [1.0], [1.0]
+    else:
+        ds = synth.hea_bcc_batched(n_struct=3, reps=2, seed=11)
+        els = list(synth.HEA_ELEMENTS)
+        from mld_gb300 import elements as el
+        w2, w3 = el.auto_channel_weights(els)
+    nat, pos, cell, types = ds.arrays()
+
+    def cfg(precision):
+        c = _lib.default_config()
+        c.j_max, c.r_cut, c.precision, c.ml_type, c.lambda_krr = j_max, r_cut, precision, 1, 1e-6
+        c.kernel_power, c.length_kernel, c.sigma_kernel = 2.0, 1.3, 0.2
+        c.n_elements = len(els)
+        c.weighted, c.weighted_3ch = int(channels >= 2), int(channels >= 3)
+        for i in range(len(els)):
+            c.weight_per_element[i], c.weight_per_element_3ch[i] = w2[i], w3[i]
+        return c
+
+    c0 = cfg(0)
+    c0.ml_type = 0
+    with _lib.Handle(c0) as h:
+        h.set_structures(nat, pos, cell, types)
+        B, nn = h.descriptors()
+    assert B.shape[1] == channels * {4.0: 55, 2.0: 14}[j_max]
+    idx = np.random.default_rng(2).choice(B.shape[0], size=150, replace=B.shape[0] < 150)
+    Zraw = B[idx]
+    E, F, S, has = ds.labels()
+    out = []
+    for precision in (0, 1):
+        with _lib.Handle(cfg(precision)) as h:
+            h.set_structures(nat, pos, cell, types)
+            h.set_labels(E, F, S, has, np.ones((len(nat), 3)))
+            h.set_kernel_points(Zraw)
+            A, _, _ = h.design_matrix()
+        out.append(np.asarray(A, dtype=np.float64))
+    KK = B.shape[1]
+    kb0, kb1 = out[0][:, 1 + KK:], out[1][:, 1 + KK:]
+    assert kb0.shape[1] == 150
+    rows_E = np.cumsum([0] + [1 + 3 * n + 6 for n in nat])[:-1]
+    fmask = np.ones(kb0.shape[0], bool)
+    for r, n in zip(rows_E, nat):
+        fmask[r] = False
+        fmask[r + 1 + 3 * n: r + 1 + 3 * n + 6] = False
+    assert nn.max() + 1 > (40 if channels == 3 else 80) or r_cut < 5
+    ef, ea = _rel(kb1[fmask], kb0[fmask]), _rel(kb1, kb0)
+    assert ef < 5e-5, (ef, ea)
+    assert ea < 2e-4, (ef, ea)
