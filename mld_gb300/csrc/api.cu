@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -99,7 +100,7 @@ struct mld_gpu_handle {
     B_G, B_H, B_W, B_EVALS, B_INFO, B_SQ, B_PRED, B_BOUT, B_DBOUT,
     B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
     B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV, B_KZD, B_KZF, B_KWS, B_WSERVE, B_P32,
-    B_EW, B_EBETA, B_EB, B_EOUT, B_KTC,
+    B_EW, B_EBETA, B_EB, B_EOUT, B_KTC, B_SKW,
     B_COUNT
   };
   static_assert(B_COUNT <= 64, "buffer table too small");
@@ -521,6 +522,8 @@ constexpr double kPrecondShiftPerColumn = 2e-7;
 constexpr double kPcgTol2 = 1e-22;   // (preconditioned residual / initial)^2 that ends the iteration
 constexpr double kPcgFloor2 = 1e-14; // below this, stagnation also ends it
 constexpr int kPrecond32MinD = 768;  // blocks this wide get the FP32 preconditioner (precond32.cu)
+constexpr int kSketchMinD = 768;     // blocks this wide get the sketched preconditioner (sketch.cu)
+constexpr uint64_t kSketchSeed = 0x5EED5EED12345ull;
 // its first shift per column: a retry costs one FP32 factorisation, so it starts lower
 constexpr double kPrecond32ShiftPerColumn = 5e-8;
 
@@ -533,8 +536,75 @@ constexpr double kPrecond32ShiftPerColumn = 5e-8;
 //  * conjugate gradients on (X^T W X + lambda I) w = X^T W y with FP64-accumulated matvecs
 //    over X itself, so the converged coefficients are those of the FP64 normal equations of
 //    this X, whatever the precision of G~.
+int pcg_solve(mld_gpu_handle* h, const float* X, int c0, int Db, const double* y, long long M, double lam,
+              double* w, int stage, const std::function<cudaError_t(const double*, double*)>& precond);
+
+// Mixed method, wide block (Db >= kSketchMinD): the preconditioner is the FP64 Cholesky factor
+// of Y^T Y + mu I for the sketch Y = S W^1/2 X (sketch.cu), whose error grows with the condition
+// number of X rather than of X^T X, and CG runs on (X^T W X + mu I) w = X^T W y with
+// mu = max(lambda, 1e-12 max_i G_ii), the diagonal shift of the plain solver (solve_any).
+int fit_block_sketch(mld_gpu_handle* h, const float* X, int c0, int Db, const double* y, long long M, double* w,
+                     int stage) {
+  double* G = bp_<double>(h, mld_gpu_handle::B_G);
+  double* hv = bp_<double>(h, mld_gpu_handle::B_H);
+  const double* wrow = bp_<double>(h, mld_gpu_handle::B_WROW);
+  mark(h, MLD_PHASE_GRAM, 0);
+  CK(ensure(h, mld_gpu_handle::B_TERR, sizeof(int)));
+  CK(ensure(h, mld_gpu_handle::B_PRED, sizeof(double) * (size_t)std::max<long long>(M, 1)));
+  CK(launch_rhs<float>(X + c0, h->ldx, wrow, y, M, Db, hv, h->nsm, h->st, bp_<float2>(h, mld_gpu_handle::B_PRED)));
+  nl(h, 2);
+  if (M >= (1LL << 31)) return fail(h, MLD_ERR_INVALID, "sketch: more than 2^31 design rows");
+  const SketchParams P = sketch_params(M, Db, kSketchSeed + (uint64_t)stage);
+  CK(ensure(h, mld_gpu_handle::B_SKW, sketch_workspace_bytes(M, Db)));
+  int nsk = 0;
+  CK(launch_sketch_gram(X, h->ldx, c0, Db, wrow, M, P, bp_<void>(h, mld_gpu_handle::B_SKW), G, h->st, &nsk));
+  nl(h, nsk + 1);
+  mark(h, MLD_PHASE_GRAM, 1);
+
+  mark(h, MLD_PHASE_SOLVE, 0);
+  CK(ensure(h, mld_gpu_handle::B_GF, sizeof(double) * (size_t)Db * Db));
+  CK(ensure(h, mld_gpu_handle::B_PCG, sizeof(double) * (7 * (size_t)Db + 8)));
+  CK(ensure(h, mld_gpu_handle::B_INFO, sizeof(int) * 4));
+  CK(ensure(h, mld_gpu_handle::B_RINV, sizeof(double) * 2 * (size_t)Db * Db));
+  double* Lf = bp_<double>(h, mld_gpu_handle::B_GF);
+  double* tmp = bp_<double>(h, mld_gpu_handle::B_PCG) + 4 * (size_t)Db;  // 2 Db
+  int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
+  std::vector<double> diag(Db);
+  CK(cudaMemcpy2DAsync(diag.data(), sizeof(double), G, sizeof(double) * (Db + 1), sizeof(double), Db,
+                       cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  double mx = 0;
+  for (double v : diag) mx = std::max(mx, std::fabs(v));
+  const double lam = h->lam_eff > 0 ? h->lam_eff : 0.0;
+  double jitter = 1e-12 * (mx > 0 ? mx : 1.0);
+  const double mu = std::max(lam, jitter);
+  int retries = 0, hinfo = 0;
+  for (double shift = mu;; shift = std::max(mu, jitter *= 10.0), ++retries) {
+    CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)Db * Db, cudaMemcpyDeviceToDevice, h->st));
+    CK(launch_cholesky(Lf, Db, shift, info, h->st));
+    nl(h, cholesky_launches(Db));
+    CK(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (hinfo == 0) {
+      h->precond_shift[stage] = shift / (mx > 0 ? mx : 1.0);
+      break;
+    }
+    if (retries >= 5)
+      return fail(h, MLD_ERR_SOLVE, "sketched preconditioner not positive definite at column " + std::to_string(hinfo));
+  }
+  h->chol_retries += retries;
+  double* Rinv = bp_<double>(h, mld_gpu_handle::B_RINV);
+  double* Rinvt = Rinv + (size_t)Db * Db;
+  int ninv = 0;
+  CK(launch_cholesky_inverse(Lf, Db, Rinv, Rinvt, h->st, &ninv));
+  nl(h, ninv);
+  auto precond = [&](const double* rr, double* zz) { return launch_precond_apply(Rinv, Rinvt, Db, rr, zz, tmp, h->st); };
+  return pcg_solve(h, X, c0, Db, y, M, mu, w, stage, precond);
+}
+
 int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const double* y, long long M, double* w,
                     int stage) {
+  if (Db >= kSketchMinD) return fit_block_sketch(h, X, c0, Db, y, M, w, stage);
   double* G = bp_<double>(h, mld_gpu_handle::B_G);
   double* hv = bp_<double>(h, mld_gpu_handle::B_H);
   const double* wrow = bp_<double>(h, mld_gpu_handle::B_WROW);
@@ -569,13 +639,7 @@ int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const dou
   CK(ensure(h, mld_gpu_handle::B_INFO, sizeof(int) * 4));
   CK(ensure(h, mld_gpu_handle::B_PRED, sizeof(double) * (size_t)std::max<long long>(M, 1)));
   double* Lf = bp_<double>(h, mld_gpu_handle::B_GF);
-  double* r = bp_<double>(h, mld_gpu_handle::B_PCG);
-  double* z = r + Db;
-  double* p = z + Db;
-  double* q = p + Db;
-  double* tmp = q + Db;  // 2 Db
-  double* scal = tmp + 2 * (size_t)Db;  // [0..3] CG scalars, [4] objective at w = 0
-  float2* sv = bp_<float2>(h, mld_gpu_handle::B_PRED);  // per-row double-FP32 scratch
+  double* tmp = bp_<double>(h, mld_gpu_handle::B_PCG) + 4 * (size_t)Db;  // 2 Db
   int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
   // the error of the BF16x3 Gram is coherent across the matrix (the tensor core truncates its
   // FP32 sums), so the shift that keeps G~ positive definite grows with D
@@ -625,6 +689,24 @@ int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const dou
     return p32 ? launch_precond32_apply(pws, Db, rr, zz, tmp, h->st)
                : launch_precond_apply(Rinv, Rinvt, Db, rr, zz, tmp, h->st);
   };
+  return pcg_solve(h, X, c0, Db, y, M, lam, w, stage, precond);
+}
+
+// Conjugate gradients on (X^T W X + lam I) w = X^T W y (the right-hand side in B_H) from w = 0,
+// with FP64-accumulated matvecs over the FP32 rows of X and the given preconditioner; stops on
+// the preconditioned residual, on the objective's decrease or on stagnation.
+int pcg_solve(mld_gpu_handle* h, const float* X, int c0, int Db, const double* y, long long M, double lam,
+              double* w, int stage, const std::function<cudaError_t(const double*, double*)>& precond) {
+  const double* hv = bp_<double>(h, mld_gpu_handle::B_H);
+  const double* wrow = bp_<double>(h, mld_gpu_handle::B_WROW);
+  int* terr = bp_<int>(h, mld_gpu_handle::B_TERR);
+  double* r = bp_<double>(h, mld_gpu_handle::B_PCG);
+  double* z = r + Db;
+  double* p = z + Db;
+  double* q = p + Db;
+  double* scal = q + 3 * (size_t)Db;  // [0..3] CG scalars, [4] objective at w = 0
+  float2* sv = bp_<float2>(h, mld_gpu_handle::B_PRED);  // per-row double-FP32 scratch
+  int herr = 0;
   // objective sum_r w_r y_r^2 at w = 0, for the stopping test on its decrease
   CK(launch_weighted_sumsq(wrow, y, M, scal + 4, h->st));
   nl(h, 1);

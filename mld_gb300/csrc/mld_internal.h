@@ -278,6 +278,20 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
                             int nsm = 0);
 // kernel-block force rows on the tensor cores (krr_tc.cu); the workspace that holds all `atoms`
 // (maxnv derivative vectors at most) in one chunk
+// sketched preconditioner of wide mixed blocks (sketch.cu)
+constexpr int kSketchZeta = 8;
+struct SketchParams {
+  int zeta;        // signed copies of each row of X
+  int s;           // sketch rows
+  long long M;     // rows of X
+  uint64_t seed;   // signs
+  long long a[kSketchZeta], ainv[kSketchZeta], b[kSketchZeta];  // affine permutations of the rows
+};
+SketchParams sketch_params(long long M, int D, uint64_t seed);
+size_t sketch_workspace_bytes(long long M, int D);
+// G (D x D, FP64, full) = Y^T Y of the sketch Y = S W^1/2 X[:, c0 : c0 + D]
+cudaError_t launch_sketch_gram(const float* X, int ldx, int c0, int D, const double* w, long long M,
+                               const SketchParams& P, void* ws, double* G, cudaStream_t st, int* launches);
 constexpr int kKrrTcMaxK = 192;  // three K blocks of 64 in shared memory
 bool krr_force_tc_available();
 size_t krr_force_tc_workspace_bytes(long long atoms, int maxnv, int nk, int KK);
