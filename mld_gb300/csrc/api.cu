@@ -521,13 +521,11 @@ constexpr double kPrecondShiftMin = 1e-6;
 constexpr double kPrecondShiftPerColumn = 2e-7;
 constexpr double kPcgTol2 = 1e-22;   // (preconditioned residual / initial)^2 that ends the iteration
 constexpr double kPcgFloor2 = 1e-14; // below this, stagnation also ends it
-constexpr int kPrecond32MinD = 768;  // blocks this wide get the FP32 preconditioner (precond32.cu)
 constexpr int kSketchMinD = 768;     // blocks this wide get the sketched preconditioner (sketch.cu)
 constexpr uint64_t kSketchSeed = 0x5EED5EED12345ull;
-// its first shift per column: a retry costs one FP32 factorisation, so it starts lower
-constexpr double kPrecond32ShiftPerColumn = 5e-8;
 
-// Mixed method, one block of columns [c0, c0 + Db) of the FP32 design matrix.
+// Mixed method, one block of columns [c0, c0 + Db) of the FP32 design matrix; blocks of
+// kSketchMinD columns or more take fit_block_sketch instead.
 //  * normal matrix G~ = X^T W X on the tensor cores in BF16 split precision (gram_tc.cu) and
 //    rhs = X^T W y with FP64 accumulation;
 //  * preconditioner: FP64 Cholesky of G~ + diag(max(lambda, rel * G~_ii)), rel = max(1e-6,
@@ -565,7 +563,7 @@ int fit_block_sketch(mld_gpu_handle* h, const float* X, int c0, int Db, const do
   CK(ensure(h, mld_gpu_handle::B_GF, sizeof(double) * (size_t)Db * Db));
   CK(ensure(h, mld_gpu_handle::B_PCG, sizeof(double) * (7 * (size_t)Db + 8)));
   CK(ensure(h, mld_gpu_handle::B_INFO, sizeof(int) * 4));
-  CK(ensure(h, mld_gpu_handle::B_RINV, sizeof(double) * 2 * (size_t)Db * Db));
+  CK(ensure(h, mld_gpu_handle::B_P32, precond32_workspace_bytes(Db)));
   double* Lf = bp_<double>(h, mld_gpu_handle::B_GF);
   double* tmp = bp_<double>(h, mld_gpu_handle::B_PCG) + 4 * (size_t)Db;  // 2 Db
   int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
@@ -581,7 +579,7 @@ int fit_block_sketch(mld_gpu_handle* h, const float* X, int c0, int Db, const do
   int retries = 0, hinfo = 0;
   for (double shift = mu;; shift = std::max(mu, jitter *= 10.0), ++retries) {
     CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)Db * Db, cudaMemcpyDeviceToDevice, h->st));
-    CK(launch_cholesky(Lf, Db, shift, info, h->st));
+    CK(launch_cholesky(Lf, Db, shift, info, h->st, true));
     nl(h, cholesky_launches(Db));
     CK(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
@@ -593,12 +591,11 @@ int fit_block_sketch(mld_gpu_handle* h, const float* X, int c0, int Db, const do
       return fail(h, MLD_ERR_SOLVE, "sketched preconditioner not positive definite at column " + std::to_string(hinfo));
   }
   h->chol_retries += retries;
-  double* Rinv = bp_<double>(h, mld_gpu_handle::B_RINV);
-  double* Rinvt = Rinv + (size_t)Db * Db;
+  void* pws = bp_<void>(h, mld_gpu_handle::B_P32);
   int ninv = 0;
-  CK(launch_cholesky_inverse(Lf, Db, Rinv, Rinvt, h->st, &ninv));
+  CK(launch_precond32_from_factor(Lf, Db, pws, h->st, &ninv));
   nl(h, ninv);
-  auto precond = [&](const double* rr, double* zz) { return launch_precond_apply(Rinv, Rinvt, Db, rr, zz, tmp, h->st); };
+  auto precond = [&](const double* rr, double* zz) { return launch_precond32_apply(pws, Db, rr, zz, tmp, h->st); };
   return pcg_solve(h, X, c0, Db, y, M, mu, w, stage, precond);
 }
 
@@ -643,27 +640,13 @@ int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const dou
   int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
   // the error of the BF16x3 Gram is coherent across the matrix (the tensor core truncates its
   // FP32 sums), so the shift that keeps G~ positive definite grows with D
-  const bool p32 = Db >= kPrecond32MinD;
-  double rel = std::max(kPrecondShiftMin, (p32 ? kPrecond32ShiftPerColumn : kPrecondShiftPerColumn) * Db);
+  double rel = std::max(kPrecondShiftMin, kPrecondShiftPerColumn * Db);
   int retries = 0;
-  // wide blocks: Jacobi-scaled FP32 factor and inverse (the FP64 pipe is 1/64 of FP32 here);
-  // narrow blocks: FP64, where the small shift of a short block needs the precision
-  void* pws = nullptr;
-  if (p32) {
-    CK(ensure(h, mld_gpu_handle::B_P32, precond32_workspace_bytes(Db)));
-    pws = bp_<void>(h, mld_gpu_handle::B_P32);
-  }
   for (;; ++retries) {
-    if (p32) {
-      int nb = 0;
-      CK(launch_precond32_build(G, Db, lam, rel, pws, info, h->st, &nb));
-      nl(h, nb);
-    } else {
-      CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)Db * Db, cudaMemcpyDeviceToDevice, h->st));
-      CK(launch_shift_diag_rel(Lf, Db, lam, rel, h->st));
-      CK(launch_cholesky(Lf, Db, 0.0, info, h->st));
-      nl(h, 1 + cholesky_launches(Db));
-    }
+    CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)Db * Db, cudaMemcpyDeviceToDevice, h->st));
+    CK(launch_shift_diag_rel(Lf, Db, lam, rel, h->st));
+    CK(launch_cholesky(Lf, Db, 0.0, info, h->st));
+    nl(h, 1 + cholesky_launches(Db));
     int hinfo = 0;
     CK(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
@@ -675,20 +658,13 @@ int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const dou
   h->precond_shift[stage] = rel;
   h->chol_retries += retries;
   // explicit inverse of the factor: each preconditioner application is two dense matvecs
-  double* Rinv = nullptr;
-  double* Rinvt = nullptr;
-  if (!p32) {
-    CK(ensure(h, mld_gpu_handle::B_RINV, sizeof(double) * 2 * (size_t)Db * Db));
-    Rinv = bp_<double>(h, mld_gpu_handle::B_RINV);
-    Rinvt = Rinv + (size_t)Db * Db;
-    int ninv = 0;
-    CK(launch_cholesky_inverse(Lf, Db, Rinv, Rinvt, h->st, &ninv));
-    nl(h, ninv);
-  }
-  auto precond = [&](const double* rr, double* zz) {
-    return p32 ? launch_precond32_apply(pws, Db, rr, zz, tmp, h->st)
-               : launch_precond_apply(Rinv, Rinvt, Db, rr, zz, tmp, h->st);
-  };
+  CK(ensure(h, mld_gpu_handle::B_RINV, sizeof(double) * 2 * (size_t)Db * Db));
+  double* Rinv = bp_<double>(h, mld_gpu_handle::B_RINV);
+  double* Rinvt = Rinv + (size_t)Db * Db;
+  int ninv = 0;
+  CK(launch_cholesky_inverse(Lf, Db, Rinv, Rinvt, h->st, &ninv));
+  nl(h, ninv);
+  auto precond = [&](const double* rr, double* zz) { return launch_precond_apply(Rinv, Rinvt, Db, rr, zz, tmp, h->st); };
   return pcg_solve(h, X, c0, Db, y, M, lam, w, stage, precond);
 }
 

@@ -244,7 +244,8 @@ cudaError_t launch_quad_rows(const DevBatch& b, const DevRows& rows, const BsoPa
 cudaError_t launch_reverse_pairs(const DevBatch& b, int* rev, cudaStream_t st);
 
 // dense FP64 factorisation / solves (solve.cu)
-cudaError_t launch_cholesky(double* A, int D, double shift, int* info, cudaStream_t st);
+// ds_update: trailing updates in double-FP32 on the FP32 pipe (preconditioner factors)
+cudaError_t launch_cholesky(double* A, int D, double shift, int* info, cudaStream_t st, bool ds_update = false);
 cudaError_t launch_chol_solve(const double* L, int D, const double* b, double* x, cudaStream_t st);
 cudaError_t launch_chol_solve_blocked(const double* L, int D, const double* b, double* x, double* tmp,
                                       cudaStream_t st);
@@ -254,10 +255,9 @@ cudaError_t launch_precond_apply(const double* R, const double* Rt, int D, const
                                  cudaStream_t st);
 inline int cholesky_launches(int D) { return 3 * ((D + 31) / 32) - 2; }
 
-// FP32 Cholesky preconditioner of large blocks (precond32.cu)
+// FP32 inverse of a wide block's preconditioner factor (precond32.cu)
 size_t precond32_workspace_bytes(int D);
-cudaError_t launch_precond32_build(const double* G, int D, double lam, double rel, void* ws, int* info,
-                                   cudaStream_t st, int* launches);
+cudaError_t launch_precond32_from_factor(const double* Lf, int D, void* ws, cudaStream_t st, int* launches);
 cudaError_t launch_precond32_apply(const void* ws, int D, const double* r, double* z, double* tmp, cudaStream_t st);
 cudaError_t launch_residual(const double* G, int D, double lambda, const double* w, const double* h, double* r,
                             cudaStream_t st);

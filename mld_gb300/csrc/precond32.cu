@@ -1,15 +1,16 @@
-// FP32 Cholesky preconditioner of a large normal matrix for the conjugate-gradient solve of the
-// mixed method (the quadratic block of the QNML fit, the kernel block of KRR).
+// FP32 inverse of a preconditioner factor for the conjugate-gradient solve of the mixed method
+// (the wide blocks: the quadratic block of the QNML fit, the kernel block of KRR).
 //
-// The preconditioner only steers the conjugate-gradient iteration: the iterates solve the FP64
-// normal equations whatever its accuracy, and the diagonal shift it carries (relative 1e-3 at
-// D ~ 6000) is far above FP32 rounding.  So it is factorised in FP32 on the CUDA cores, which
-// run FP32 at 64x the FP64 rate of this GPU:
-//   s_i = 1 / sqrt(d_i),  d_i = G_ii + max(lambda, rel G_ii)            (Jacobi scaling)
-//   A   = S (G + diag(d - G_ii)) S, unit diagonal                          (FP32)
-//   A   = L L^T                       blocked right-looking Cholesky, 64-column panels
-//   R   = L^-1                        diagonal 64-blocks, then recursive doubling with GEMMs:
-//                                     R21 = -R22 (L21 R11)
+// The factor L (FP64, lower) comes from the Cholesky factorisation of the sketched normal matrix
+// (sketch.cu).  Its inverse only steers the iteration: the iterates solve the FP64 normal
+// equations whatever its accuracy, and an FP32 inverse of a triangular factor has a relative
+// error of about 2^-24 times its condition number (the square root of the normal matrix's), well
+// inside what CG absorbs.  So it is inverted in FP32 on the CUDA cores, which run FP32 at 64x the
+// FP64 rate of this GPU:
+//   s_i = 1 / |L_i,:|                 (Jacobi scaling: (L L^T)_ii = |L_i,:|^2)
+//   A   = S L                         FP32, unit-norm rows
+//   R   = A^-1                        diagonal 64-blocks, then recursive doubling with GEMMs:
+//                                     R21 = -R22 (A21 R11)
 //   M^-1 r = S R^T R S r              two dense triangular matvecs, double-FP32 arithmetic
 // M^-1 is a fixed symmetric positive-definite operator (R and R^T hold the same FP32 numbers),
 // so the standard conjugate-gradient recurrences stay valid.
@@ -23,130 +24,22 @@ namespace mld {
 
 constexpr int kNB = 64;  // panel width of the FP32 factorisation and size of the base inverse blocks
 
-// s_i and the scaled, shifted matrix (full square; only the lower triangle is used later).
-// A column whose shifted diagonal is not positive (an all-zero feature without ridge) gets
-// s_i = 0 and a unit diagonal: the preconditioner then leaves that direction untouched.
-__global__ void k_p32_scale_diag(const double* __restrict__ G, int D, double lam, double rel, double* __restrict__ s) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// s_i = 1 / |L_i,:| and A = S L in FP32 (lower triangle, zero above); warp per row.  A zero row
+// (an all-zero feature) gets s_i = 0 and a unit diagonal.
+__global__ void __launch_bounds__(256) k_p32_from_factor(const double* __restrict__ Lf, int D,
+                                                         double* __restrict__ s, float* __restrict__ A) {
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= D) return;
-  const double g = G[(size_t)i * D + i];
-  const double d = g + fmax(lam, rel * g);
-  s[i] = d > 0.0 ? 1.0 / sqrt(d) : 0.0;
-}
-
-__global__ void k_p32_scale(const double* __restrict__ G, int D, const double* __restrict__ s, float* __restrict__ A) {
-  const int j = blockIdx.x * 32 + threadIdx.x;
-  for (int i = blockIdx.y * 32 + threadIdx.y; i < min(D, blockIdx.y * 32 + 32); i += blockDim.y) {
-    if (j >= D) continue;
-    const double v = (i == j) ? 1.0 : G[(size_t)i * D + j] * s[i] * s[j];
-    A[(size_t)i * D + j] = (float)v;
-  }
-}
-
-// Factor the diagonal block [k0, k0 + nb) in place (one CTA); info = first failing column + 1.
-__global__ void __launch_bounds__(256) k_p32_potrf_diag(float* A, int D, int k0, int nb, int* info) {
-  __shared__ float L[kNB][kNB + 1];
-  const int tid = threadIdx.x;
-  for (int e = tid; e < nb * nb; e += blockDim.x) {
-    const int i = e / nb, j = e % nb;
-    L[i][j] = A[(size_t)(k0 + i) * D + (k0 + j)];
-  }
-  __syncthreads();
-  for (int j = 0; j < nb; ++j) {
-    if (tid == 0) {
-      float d = L[j][j];
-      if (!(d > 0.0f)) {
-        if (info[0] == 0) info[0] = k0 + j + 1;
-        d = 1.0f;
-      }
-      L[j][j] = sqrtf(d);
-    }
-    __syncthreads();
-    const float djj = L[j][j];
-    for (int i = j + 1 + tid; i < nb; i += blockDim.x) L[i][j] /= djj;
-    __syncthreads();
-    const int m = nb - j - 1;
-    for (int e = tid; e < m * m; e += blockDim.x) {
-      const int i = j + 1 + e / m, c = j + 1 + e % m;
-      if (c <= i) L[i][c] -= L[i][j] * L[c][j];
-    }
-    __syncthreads();
-  }
-  for (int e = tid; e < nb * nb; e += blockDim.x) {
-    const int i = e / nb, j = e % nb;
-    if (j <= i) A[(size_t)(k0 + i) * D + (k0 + j)] = L[i][j];
-  }
-}
-
-// Panel below the diagonal block: rows r >= k0 + kNB, A[r][k0..k0+kNB) <- A[r][..] L11^-T.
-// One thread per row; the block is full width here (nb == kNB: only the last panel is ragged
-// and it has no rows below it).
-__global__ void __launch_bounds__(128) k_p32_trsm(float* A, int D, int k0) {
-  __shared__ float L[kNB][kNB + 1];
-  for (int e = threadIdx.x; e < kNB * kNB; e += blockDim.x) {
-    const int i = e / kNB, j = e % kNB;
-    L[i][j] = (j <= i) ? A[(size_t)(k0 + i) * D + (k0 + j)] : 0.0f;
-  }
-  __syncthreads();
-  const int r = k0 + kNB + blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= D) return;
-  float x[kNB];
-  float* row = A + (size_t)r * D + k0;
-#pragma unroll
-  for (int j = 0; j < kNB; ++j) x[j] = row[j];
-#pragma unroll
-  for (int j = 0; j < kNB; ++j) {
-    float v = x[j];
-#pragma unroll
-    for (int c = 0; c < j; ++c) v = fmaf(-x[c], L[j][c], v);
-    x[j] = v / L[j][j];
-  }
-#pragma unroll
-  for (int j = 0; j < kNB; ++j) row[j] = x[j];
-}
-
-// Trailing update of the lower triangle: A[i][j] -= sum_c P[i][c] P[j][c] over the panel
-// columns c in [k0, k0 + kNB), for i, j >= k1 = k0 + kNB, j <= i.  64 x 64 tiles over the
-// lower-triangular tile pairs, 16 x 16 threads with 4 x 4 outputs each.
-__global__ void __launch_bounds__(256) k_p32_syrk(float* A, int D, int k0) {
-  const int k1 = k0 + kNB;
-  int t = blockIdx.x, ti = 0;
-  while (t >= ti + 1) {
-    t -= ti + 1;
-    ++ti;
-  }
-  const int tj = t;
-  const int i0 = k1 + ti * 64, j0 = k1 + tj * 64;
-  if (i0 >= D) return;
-  __shared__ float Pi[64][kNB + 1], Pj[64][kNB + 1];
-  for (int e = threadIdx.x; e < 64 * kNB; e += blockDim.x) {
-    const int r = e / kNB, c = e % kNB;
-    Pi[r][c] = (i0 + r < D) ? A[(size_t)(i0 + r) * D + k0 + c] : 0.0f;
-    Pj[r][c] = (j0 + r < D) ? A[(size_t)(j0 + r) * D + k0 + c] : 0.0f;
-  }
-  __syncthreads();
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  float acc[4][4] = {};
-#pragma unroll 4
-  for (int c = 0; c < kNB; ++c) {
-    float a[4], b[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      a[u] = Pi[ty + 16 * u][c];
-      b[u] = Pj[tx + 16 * u][c];
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-#pragma unroll
-      for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], b[v], acc[u][v]);
-  }
-#pragma unroll
-  for (int u = 0; u < 4; ++u)
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const int i = i0 + ty + 16 * u, j = j0 + tx + 16 * v;
-      if (i < D && j <= i) A[(size_t)i * D + j] -= acc[u][v];
-    }
+  const double* row = Lf + (size_t)i * D;
+  double n2 = 0.0;
+  for (int c = lane; c <= i; c += 32) n2 = fma(row[c], row[c], n2);
+  for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
+  const double si = n2 > 0.0 ? 1.0 / sqrt(n2) : 0.0;
+  float* out = A + (size_t)i * D;
+  for (int c = lane; c < D; c += 32)
+    out[c] = c > i ? 0.0f : (si > 0.0 ? (float)(row[c] * si) : (c == i ? 1.0f : 0.0f));
+  if (lane == 0) s[i] = si;
 }
 
 // Inverse of each diagonal 64-block of L (one CTA per block, one thread per column).
@@ -269,10 +162,9 @@ size_t precond32_workspace_bytes(int D) {
   return sizeof(float) * (3 * d2 + h * h) + sizeof(double) * (size_t)D + 256 + sizeof(float2) * (size_t)D + 256;
 }
 
-// Factorise: on return *info (device) is 0 on success, or the first failing column + 1.
-// ws: precond32_workspace_bytes(D) bytes; layout [s (D doubles) | L | R | Rt | T].
-cudaError_t launch_precond32_build(const double* G, int D, double lam, double rel, void* ws, int* info,
-                                   cudaStream_t st, int* launches) {
+// From the FP64 factor Lf (lower triangle read): S, A = S L and R = A^-1, R^T.
+// ws: precond32_workspace_bytes(D) bytes; layout [s (D doubles) | A | R | Rt | T].
+cudaError_t launch_precond32_from_factor(const double* Lf, int D, void* ws, cudaStream_t st, int* launches) {
   double* s = (double*)ws;
   float* L = (float*)((char*)ws + ((sizeof(double) * (size_t)D + 255) / 256) * 256);
   const size_t d2 = (size_t)D * D;
@@ -280,26 +172,11 @@ cudaError_t launch_precond32_build(const double* G, int D, double lam, double re
   float* Rt = R + d2;
   float* T = Rt + d2;
   int n = 0;
-  cudaError_t e = cudaMemsetAsync(info, 0, sizeof(int), st);
-  if (e != cudaSuccess) return e;
-  k_p32_scale_diag<<<(D + 255) / 256, 256, 0, st>>>(G, D, lam, rel, s);
+  k_p32_from_factor<<<(unsigned)(((long long)D * 32 + 255) / 256), 256, 0, st>>>(Lf, D, s, L);
+  ++n;
   dim3 g32((D + 31) / 32, (D + 31) / 32);
-  k_p32_scale<<<g32, dim3(32, 8), 0, st>>>(G, D, s, L);
-  n += 2;
-  for (int k0 = 0; k0 < D; k0 += kNB) {
-    const int nb = min(kNB, D - k0);
-    k_p32_potrf_diag<<<1, 256, 0, st>>>(L, D, k0, nb, info);
-    ++n;
-    const int rows = D - k0 - nb;
-    if (rows > 0) {
-      k_p32_trsm<<<(rows + 127) / 128, 128, 0, st>>>(L, D, k0);
-      const int nt = (rows + 63) / 64;
-      k_p32_syrk<<<nt * (nt + 1) / 2, 256, 0, st>>>(L, D, k0);
-      n += 2;
-    }
-  }
   // R = L^-1: zero, invert the diagonal blocks, then merge pairs of blocks of doubling size
-  e = cudaMemsetAsync(R, 0, sizeof(float) * d2, st);
+  cudaError_t e = cudaMemsetAsync(R, 0, sizeof(float) * d2, st);
   if (e != cudaSuccess) return e;
   k_p32_trinv_diag<<<(D + kNB - 1) / kNB, kNB, 0, st>>>(L, D, R);
   ++n;

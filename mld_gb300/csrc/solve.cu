@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "ds.cuh"
 #include "mld_internal.h"
 
 namespace mld {
@@ -109,6 +110,55 @@ __global__ void __launch_bounds__(256) k_syrk_update(double* A, int lda, int D, 
     for (int b = 0; b < 2; ++b) {
       const int i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
       if (i < D && j < D && j <= i) A[(size_t)i * lda + j] -= acc[a][b];
+    }
+}
+
+// k_syrk_update in double-FP32 arithmetic on the FP32 pipe (GB300 issues FP64 at 1/64 of its FP32
+// rate): the panel entries as FP32 pairs hi + lo, each product formed as the exact hi hi (fmaf)
+// plus hi lo + lo hi, the sum over the panel as an unevaluated pair, one FP64 subtraction per
+// element and panel.  About 2^-44 relative to the magnitudes of the products: used for the
+// preconditioner factor of the mixed method, not for the plain solve.
+__global__ void __launch_bounds__(256) k_syrk_update_ds(double* A, int lda, int D, int k0, int nb, int k1) {
+  const int ntile = (D - k1 + 31) / 32;
+  int t = blockIdx.x, ti = 0;
+  while (t >= ti + 1) {
+    t -= ti + 1;
+    ++ti;
+  }
+  const int tj = t;
+  if (ti >= ntile) return;
+  const int i0 = k1 + ti * 32, j0 = k1 + tj * 32;
+  __shared__ float2 Li[kCB][33], Lj[kCB][33];  // [c][row]
+  for (int e = threadIdx.x; e < 32 * nb; e += blockDim.x) {
+    const int r = e / nb, c = e % nb;
+    float h, l;
+    ds_split((i0 + r < D) ? A[(size_t)(i0 + r) * lda + k0 + c] : 0.0, h, l);
+    Li[c][r] = make_float2(h, l);
+    ds_split((j0 + r < D) ? A[(size_t)(j0 + r) * lda + k0 + c] : 0.0, h, l);
+    Lj[c][r] = make_float2(h, l);
+  }
+  __syncthreads();
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float sh[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, sl[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+  for (int c = 0; c < nb; ++c) {
+    const float2 a[2] = {Li[c][ty], Li[c][ty + 16]};
+    const float2 b[2] = {Lj[c][tx], Lj[c][tx + 16]};
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const float pr = a[p].x * b[q].x;
+        const float pe = fmaf(a[p].x, b[q].y, fmaf(a[p].y, b[q].x, fmaf(a[p].x, b[q].x, -pr)));
+        float su, er;
+        two_sum(sh[p][q], pr, su, er);
+        sh[p][q] = su;
+        sl[p][q] += er + pe;
+      }
+  }
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) {
+      const int i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
+      if (i < D && j < D && j <= i) A[(size_t)i * lda + j] -= (double)sh[a][b] + (double)sl[a][b];
     }
 }
 
@@ -455,7 +505,7 @@ cudaError_t launch_precond_apply(const double* R, const double* Rt, int D, const
   return cudaGetLastError();
 }
 
-cudaError_t launch_cholesky(double* A, int D, double shift, int* info, cudaStream_t st) {
+cudaError_t launch_cholesky(double* A, int D, double shift, int* info, cudaStream_t st, bool ds_update) {
   cudaError_t e = cudaMemsetAsync(info, 0, sizeof(int), st);
   if (e != cudaSuccess) return e;
   for (int k0 = 0; k0 < D; k0 += kCB) {
@@ -466,7 +516,10 @@ cudaError_t launch_cholesky(double* A, int D, double shift, int* info, cudaStrea
       const int rows = D - k1;
       k_trsm_panel<<<(rows + 127) / 128, 128, 0, st>>>(A, D, D, k0, nb);
       const int nt = (rows + 31) / 32;
-      k_syrk_update<<<nt * (nt + 1) / 2, 256, 0, st>>>(A, D, D, k0, nb, k1);
+      if (ds_update)
+        k_syrk_update_ds<<<nt * (nt + 1) / 2, 256, 0, st>>>(A, D, D, k0, nb, k1);
+      else
+        k_syrk_update<<<nt * (nt + 1) / 2, 256, 0, st>>>(A, D, D, k0, nb, k1);
     }
     // the shift applies to the diagonal blocks only once: later blocks still hold raw values
   }
