@@ -293,7 +293,8 @@ def run_hea(a):
         "metric": "design rows/s (QNML quadratic fit, 5-element bcc alloy, weighted bispectrum j_max=4)",
         "value": M / (ms * 1e-3), "unit": "design rows/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32 descriptors/rows + bf16x3 tensor-core Gram (fp32 acc) + fp64 Cholesky / double-fp32 CG",
+        "dtype": "fp32 descriptors/rows; linear block: bf16x3 tensor-core Gram (fp32 acc) + fp64 Cholesky; "
+                 "quadratic block: sparse-sign sketch + double-fp32 Gram/Cholesky + fp32 inverse; double-fp32 CG",
         "data": "synthetic",
         "config": {"workload": "hea_bcc_MoNbTaVCr_4000x250_qnml_weighted_jmax4", "structures": n_struct,
                    "atoms": A, "design_rows": M, "dim_design_line_full": out["D"], "r_cut": 5.0, "lambda_krr": lam,
@@ -373,7 +374,8 @@ def run_hea_krr(a):
         "metric": "design rows/s (kernel ridge regression, polynomial kernel, 5-element bcc alloy)",
         "value": M / (ms * 1e-3), "unit": "design rows/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32 descriptors/kernel rows + bf16x3 tensor-core Gram (fp32 acc) + fp64 Cholesky / double-fp32 CG",
+        "dtype": "fp32 descriptors, kernel rows (force rows: bf16x3 tensor cores, fp32 acc); sparse-sign sketch + "
+                 "double-fp32 Gram/Cholesky + fp32 inverse as preconditioner; double-fp32 CG",
         "data": "synthetic",
         "config": {"workload": "hea_bcc_MoNbTaVCr_4000x250_krr_poly2_weighted_jmax4", "structures": n_struct,
                    "atoms": A, "design_rows": M, "reference_points": int(a.ref_points),
