@@ -265,7 +265,7 @@ struct KernelArgs {
   DevEval<T> ev;
 };
 
-constexpr int kNW = 8;           // warps per CTA (kNW*32 == kZThreads)
+constexpr int kNW = 8;           // warps per CTA (== kZWarps)
 constexpr int kG1 = 8;           // lanes per neighbour in phase 1
 constexpr int kG3 = 16;          // lanes per neighbour in phase 3
 
@@ -364,25 +364,21 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
     }
     __syncthreads();
 
-    // ---------------- phase 2: folded Z -> Y, B on the balanced schedule ---------------
-    // a thread owns whole slots (their terms are consecutive items), so Y is stored once.
+    // ---------------- phase 2: folded Z -> Y, B in rounds of equal-shape terms ---------------
+    // lane l of a round computes one Z term; the 32 terms of a round share their loop extents,
+    // so the warp runs without divergence.  Terms add into Y (zeroed above) and B atomically.
     // The CG coefficients (a few thousand) are staged in V, free until phase 3, so that the
-    // per-term coefficient loads of the per-thread schedules come from shared memory.
+    // per-term coefficient loads come from shared memory.
     T* cgs = reinterpret_cast<T*>(V);
     for (int e = tid; e < tb.NCG; e += nth) cgs[e] = args.cg[e];
     __syncthreads();
     {
-      const int i0 = tb.zitem_off[tid], i1 = tb.zitem_off[tid + 1];
+      const int r0 = tb.zitem_off[warp], r1 = tb.zitem_off[warp + 1];
       for (int ch = 0; ch < nch; ++ch) {
         const cx<T>* cc = cfull + ch * NU;
-        cx<T> acc = {T(0), T(0)};
-        int left = 0;
-        for (int it = i0; it < i1; ++it) {
-          const ZItem zi = tb.zitems[it];
-          if (zi.pad) {
-            left = (int)zi.pad;
-            acc = {T(0), T(0)};
-          }
+        cx<T>* Yc = Y + (size_t)ch * NYP;
+        for (int r = r0; r < r1; ++r) {
+          const ZItem zi = tb.zitems[(size_t)r * 32 + lane];
           const ZTerm z = tb.zterms[zi.zt];
           cx<T> zs = {T(0), T(0)};
           int i1a = z.i1, i2a = z.i2;
@@ -406,10 +402,11 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
             const cx<T> cv = cc[zi.ufull];
             atomicAdd(&Bk[ch * K + zi.k], (T)zi.wgt * (cv.x * zs.x + cv.y * zs.y));  // w * Re(conj(c) ZA)
           }
-          const T sc = (T)zi.snum / (T)zi.sden * (T)zi.wgt;
-          acc.x = fma(sc, zs.x, acc.x);
-          acc.y = fma(sc, zs.y, acc.y);
-          if (--left == 0) Y[(size_t)ch * NYP + zi.ypos] = acc;
+          if (zi.wgt) {
+            const T sc = (T)zi.snum / (T)zi.sden * (T)zi.wgt;
+            atomicAdd(&Yc[zi.ypos].x, sc * zs.x);
+            atomicAdd(&Yc[zi.ypos].y, sc * zs.y);
+          }
         }
       }
     }

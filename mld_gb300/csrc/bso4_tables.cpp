@@ -255,28 +255,13 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
   for (int j = J; j >= 0; --j)
     for (int rt = 0; rt < t->Mp[j] / kRowTile; ++rt) t->tiles.push_back((j << 8) | rt);
 
-  // phase-2 schedule: one item per slot (all of its terms, so Y is written once without
-  // atomics); longest-processing-time-first assignment of slots to kZThreads threads, so that
-  // each thread's total CG work is nearly equal.  Items of a slot are consecutive: the first
-  // carries the slot's term count in `pad`.
+  // phase-2 schedule: every Z term of every slot is one work entry.  Entries of equal loop shape
+  // (na, nb) form rounds of 32, one per lane, padded with zero-weight copies, so that the lanes
+  // of a warp run identical loops; rounds go to the kZWarps warps longest-first (LPT) by their
+  // na * nb cost.  A term adds its scaled Z into its slot of Y (and, for ZA, into B) atomically.
   {
-    struct It { int slot; long long cost; };
-    std::vector<It> items;
-    for (size_t si = 0; si < t->yslots.size(); ++si) {
-      const YSlot& s = t->yslots[si];
-      long long c = 4;
-      for (int tt = 0; tt < s.nterm; ++tt) c += (long long)t->zterms[s.term[tt]].na * t->zterms[s.term[tt]].nb;
-      items.push_back({(int)si, c});
-    }
-    std::stable_sort(items.begin(), items.end(), [](const It& a, const It& b) { return a.cost > b.cost; });
-    std::vector<long long> load(kZThreads, 0);
-    std::vector<std::vector<ZItem>> per(kZThreads);
-    for (const It& it : items) {
-      int best = 0;
-      for (int th = 1; th < kZThreads; ++th)
-        if (load[th] < load[best]) best = th;
-      load[best] += it.cost;
-      const YSlot& s = t->yslots[it.slot];
+    std::map<std::pair<int, int>, std::vector<ZItem>> byshape;
+    for (const YSlot& s : t->yslots) {
       for (int tt = 0; tt < s.nterm; ++tt) {
         const ZTerm& z = t->zterms[s.term[tt]];
         ZItem zi{};
@@ -288,16 +273,41 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
         zi.sden = z.sden;
         zi.wgt = s.wgt;
         zi.is_a = (tt == 0 && s.is_a) ? 1 : 0;
-        zi.pad = (tt == 0) ? (uint32_t)s.nterm : 0u;
-        per[best].push_back(zi);
+        byshape[{z.na, z.nb}].push_back(zi);
       }
     }
-    t->zitem_off.assign(kZThreads + 1, 0);
-    for (int th = 0; th < kZThreads; ++th) {
-      t->zitem_off[th] = (int)t->zitems.size();
-      t->zitems.insert(t->zitems.end(), per[th].begin(), per[th].end());
+    struct Round { long long cost; std::vector<ZItem> lanes; };
+    std::vector<Round> rounds;
+    for (auto& kv : byshape) {
+      const std::vector<ZItem>& v = kv.second;
+      for (size_t i = 0; i < v.size(); i += 32) {
+        Round r{(long long)kv.first.first * kv.first.second, {}};
+        for (size_t l = i; l < std::min(v.size(), i + 32); ++l) r.lanes.push_back(v[l]);
+        while (r.lanes.size() < 32) {
+          ZItem pad = v[i];
+          pad.wgt = 0;
+          pad.is_a = 0;
+          r.lanes.push_back(pad);
+        }
+        rounds.push_back(std::move(r));
+      }
     }
-    t->zitem_off[kZThreads] = (int)t->zitems.size();
+    std::stable_sort(rounds.begin(), rounds.end(), [](const Round& x, const Round& y) { return x.cost > y.cost; });
+    std::vector<long long> load(kZWarps, 0);
+    std::vector<std::vector<const Round*>> per(kZWarps);
+    for (const Round& r : rounds) {
+      int best = 0;
+      for (int w = 1; w < kZWarps; ++w)
+        if (load[w] < load[best]) best = w;
+      load[best] += r.cost;
+      per[best].push_back(&r);
+    }
+    t->zitem_off.assign(kZWarps + 1, 0);
+    for (int w = 0; w < kZWarps; ++w) {
+      t->zitem_off[w] = (int)(t->zitems.size() / 32);
+      for (const Round* r : per[w]) t->zitems.insert(t->zitems.end(), r->lanes.begin(), r->lanes.end());
+    }
+    t->zitem_off[kZWarps] = (int)(t->zitems.size() / 32);
   }
   return true;
 }

@@ -43,7 +43,8 @@ struct YSlot {
   uint8_t pad;
 };
 
-// One Z-term work item of the balanced phase-2 schedule: term `zt` of the slot at `ypos`.
+// One Z-term work entry of the phase-2 schedule (one lane of a round): term `zt` of the slot at
+// `ypos`; wgt = 0 marks a padding lane.
 struct ZItem {
   uint16_t zt;             // ZTerm index
   uint16_t ypos;           // Y position of its slot
@@ -66,12 +67,12 @@ struct RecEntry64 {
   int64_t pad;
 };
 
-constexpr int kZThreads = 256;  // threads of the phase-2 schedule (= CTA size of k_bso4)
+constexpr int kZWarps = 8;  // warps of the phase-2 schedule (= warps of a k_bso4 CTA)
 
 // Host-built constant tables of the SO(4) bispectrum for a given j_max.
 struct Bso4Tables {
-  std::vector<ZItem> zitems;    // phase-2 work, grouped per thread (LPT-balanced)
-  std::vector<int> zitem_off;   // kZThreads + 1 offsets into zitems
+  std::vector<ZItem> zitems;    // phase-2 rounds of 32 equal-shape terms, grouped per warp (LPT)
+  std::vector<int> zitem_off;   // kZWarps + 1 round offsets (a round is 32 consecutive zitems)
   int J = 0, NU = 0, HU = 0, K = 0, NYP = 0;
   int off[kMaxJ + 2] = {0};     // full-layer offsets
   int hoff[kMaxJ + 2] = {0};    // half-layer offsets
@@ -126,7 +127,7 @@ struct DevTables {
   RecEntry32* rec32 = nullptr;  // packed recursion records (FP32 method)
   RecEntry64* rec64 = nullptr;  // packed recursion records (FP64 method)
   ZItem* zitems = nullptr;
-  int* zitem_off = nullptr;     // kZThreads + 1
+  int* zitem_off = nullptr;     // kZWarps + 1
 };
 
 // Packed recursion records from the table vectors.
