@@ -46,6 +46,7 @@ constexpr int kBoxRows = 32;                   // rows per TMA box of a V tile
 constexpr int kBoxBytes = kBoxRows * kTK * 2;  // 4 KB
 constexpr int kChunks = 3;                      // vector chunks per epilogue warp and tile
 constexpr int kTmemCols = 512;                 // two accumulators of up to 256 columns
+constexpr int kMaxStages = 4;                  // V tile stages
 
 // rows of a V tile: up to 256 for K <= 128 (two K blocks), 128 for three K blocks (shared memory)
 __host__ __device__ constexpr int max_tile_rows(int nkb) { return nkb <= 2 ? 256 : 128; }
@@ -79,7 +80,8 @@ __global__ void k_ktc_zplanes(const float* __restrict__ Z, int nk, int KK, int K
 }
 
 // The derivative vectors of a chunk's atom tiles as bf16 hi/lo planes (KP per row; rows past
-// 3 nvp of a tile are zero) and one 32-byte record per vector: {centre (int bits), sign / sqrt
+// 3 nvp of a tile are zero), the first force row of each tile (trow), and one 32-byte record per
+// vector: {centre (int bits), sign / sqrt
 // f(x,x), sign dker_xx / (2 f(x,x) sqrt f(x,x)), 0} and {g_x, g_y, g_z, 0} with g = V . x_centre.
 // A padding vector has centre = the atom and zero factors; a centre without neighbours has zero
 // factors (krr_c12 of kernel_rows with the point terms left out).  One CTA (4 warps) per tile;
@@ -89,8 +91,16 @@ __global__ void __launch_bounds__(128) k_ktc_vplanes(const TileMeta* __restrict_
                                                      const int* __restrict__ rev, const float* __restrict__ B,
                                                      const float* __restrict__ dB, const float* __restrict__ at,
                                                      __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
-                                                     float* __restrict__ vrec) {
+                                                     float* __restrict__ vrec, const int* __restrict__ atom_struct,
+                                                     const int* __restrict__ atom_start,
+                                                     const long long* __restrict__ rowF, long long* __restrict__ trow) {
   const TileMeta m = tmeta[blockIdx.x];
+  if (threadIdx.x == 0) {
+    // the tile's first force row (alpha = 0), -1 for a structure without force rows
+    const int sidx = atom_struct[m.atom];
+    const long long rf = rowF[sidx];
+    trow[blockIdx.x] = rf >= 0 ? rf + 3LL * (m.atom - atom_start[sidx]) : -1;
+  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int a = m.atom;
   const int p0 = nbr_off[a], nn = nbr_off[a + 1] - p0;
@@ -165,32 +175,38 @@ __device__ __forceinline__ void tmem_ld3x8(uint32_t taddr, uint32_t stride, floa
 }  // namespace
 
 // CTA (blockIdx.x = 128-point tile of Z, blockIdx.y = g): atom tiles t = g, g + G, ... of the
-// chunk.  Shared memory: the Z tile (nkb K blocks x hi, lo), one V tile stage (nkb x hi, lo blocks
-// of max_tile_rows rows), the vector records of three tiles (the current one, the next one whose
+// chunk.  Shared memory: the Z tile (nkb K blocks x hi, lo), `stages` V tile stages (nkb x hi, lo
+// blocks of vrows rows, vrows >= the largest N of the chunk; the loads of the next tiles overlap
+// the MMAs of the current one), the vector records of three tiles (the current one, the next one whose
 // kernel features are being fetched, and the one after, being staged), and the quarters' partial
 // sums of two tiles.  The epilogue fetches the kernel features of tile i + 1 into registers
-// before it waits for the accumulator of tile i + 1.
+// before it waits for the accumulator of tile i + 1.  P: the kernel power when it is a small
+// integer (1-4), 0 for any other power (powf).
+template <int P>
 __global__ void __launch_bounds__(kKThreads, 1)
     k_krr_force_tc(const __grid_constant__ CUtensorMap vhi, const __grid_constant__ CUtensorMap vlo,
                    const __grid_constant__ CUtensorMap zhi, const __grid_constant__ CUtensorMap zlo, int ntiles,
-                   int nkb, int nk, const TileMeta* __restrict__ tmeta, const float4* __restrict__ vrec,
+                   int nkb, int stages, int vrows, int nvr, int nk, const TileMeta* __restrict__ tmeta,
+                   const float4* __restrict__ vrec,
                    const float* __restrict__ F, const float* __restrict__ szz, float s2, float l2, float pw,
-                   const int* __restrict__ atom_struct, const int* __restrict__ atom_start,
-                   const long long* __restrict__ rowF, int c0, int ldx, float* __restrict__ X, int* __restrict__ err) {
+                   const long long* __restrict__ trow, int c0, int ldx, float* __restrict__ X,
+                   int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* ztile = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const uint32_t zbytes = (uint32_t)nkb * 2 * kTileBytes;
-  const uint32_t vblk = (uint32_t)max_tile_rows(nkb) * kTK * 2;  // one K block of one plane
-  const int nvmax = max_tile_vectors(nkb);
+  const uint32_t vblk = (uint32_t)vrows * kTK * 2;  // one K block of one plane
+  const uint32_t sbytes = (uint32_t)nkb * 2 * vblk;  // one stage
+  const int nvmax = nvr;  // record rows per buffer: the chunk's largest nvp
   unsigned char* vtile = ztile + zbytes;
-  float4* srec = reinterpret_cast<float4*>(vtile + (size_t)nkb * 2 * vblk);  // [3][2 nvmax]
+  float4* srec = reinterpret_cast<float4*>(vtile + (size_t)stages * sbytes);  // [3][2 nvmax]
   float* red = reinterpret_cast<float*>(srec + 3 * 2 * nvmax);               // [2][4][3][4][32]
-  uint64_t* bfull = reinterpret_cast<uint64_t*>(red + 2 * 4 * 3 * 4 * 32);
-  uint64_t* full = bfull + 1;
-  uint64_t* empty = bfull + 2;
-  uint64_t* tfull = bfull + 3;   // [2] accumulator ready
-  uint64_t* tempty = bfull + 5;  // [2] accumulator drained
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bfull + 7);
+  int* sce = reinterpret_cast<int*>(red + 2 * 4 * 3 * 4 * 32);               // [3][nvmax] centres
+  uint64_t* bfull = reinterpret_cast<uint64_t*>(sce + 3 * nvmax);
+  uint64_t* full = bfull + 1;                 // [kMaxStages]
+  uint64_t* empty = full + kMaxStages;        // [kMaxStages]
+  uint64_t* tfull = empty + kMaxStages;       // [2] accumulator ready
+  uint64_t* tempty = tfull + 2;               // [2] accumulator drained
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
 
   const int n0 = blockIdx.x * kTM;
   const int g = blockIdx.y, G = gridDim.y;
@@ -199,8 +215,10 @@ __global__ void __launch_bounds__(kKThreads, 1)
 
   if (threadIdx.x == 0) {
     ptx::mbar_init(bfull, 1);
-    ptx::mbar_init(full, 1);
-    ptx::mbar_init(empty, 1);
+    for (int st = 0; st < stages; ++st) {
+      ptx::mbar_init(&full[st], 1);
+      ptx::mbar_init(&empty[st], 1);
+    }
     for (int b = 0; b < 2; ++b) {
       ptx::mbar_init(&tfull[b], 1);
       ptx::mbar_init(&tempty[b], kKEpiWarps);
@@ -228,23 +246,25 @@ __global__ void __launch_bounds__(kKThreads, 1)
     }
     int issued = 0;
     for (int i = 0; i < nmine; ++i) {
-      if (i >= 1 && !ptx::mbar_wait(empty, (i - 1) & 1)) {
+      const int st = i % stages;
+      if (i >= stages && !ptx::mbar_wait(&empty[st], ((i / stages) - 1) & 1)) {
         ok = false;
         break;
       }
       const TileMeta m = tmeta[g + i * G];
       const int nbox = (m.N + kBoxRows - 1) / kBoxRows;
-      ptx::mbar_expect_tx(full, (uint32_t)(nkb * 2 * nbox * kBoxBytes));
+      unsigned char* vs = vtile + (size_t)st * sbytes;
+      ptx::mbar_expect_tx(&full[st], (uint32_t)(nkb * 2 * nbox * kBoxBytes));
       for (int kb = 0; kb < nkb; ++kb)
         for (int j = 0; j < nbox; ++j) {
-          ptx::tma_load_2d(vtile + (2 * kb) * vblk + j * kBoxBytes, &vhi, kb * kTK, m.row0 + j * kBoxRows, full);
-          ptx::tma_load_2d(vtile + (2 * kb + 1) * vblk + j * kBoxBytes, &vlo, kb * kTK, m.row0 + j * kBoxRows,
-                           full);
+          ptx::tma_load_2d(vs + (2 * kb) * vblk + j * kBoxBytes, &vhi, kb * kTK, m.row0 + j * kBoxRows, &full[st]);
+          ptx::tma_load_2d(vs + (2 * kb + 1) * vblk + j * kBoxBytes, &vlo, kb * kTK, m.row0 + j * kBoxRows,
+                           &full[st]);
         }
       issued = i + 1;
     }
     // copies still in flight are waited for (bounded) before leaving
-    if (issued > 0) ptx::mbar_wait(full, (issued - 1) & 1);
+    for (int i = max(0, issued - stages); i < issued; ++i) ptx::mbar_wait(&full[i % stages], (i / stages) & 1);
     ptx::mbar_wait(bfull, 0);
   } else if (warp == 1 && lane == 0) {
     // MMA issuer: atom tile i into TMEM buffer i & 1 (columns 256 (i & 1) + [0, N))
@@ -256,27 +276,29 @@ __global__ void __launch_bounds__(kKThreads, 1)
         ok = false;
         break;
       }
-      if (!ptx::mbar_wait(full, i & 1)) {
+      const int st = i % stages;
+      if (!ptx::mbar_wait(&full[st], (i / stages) & 1)) {
         ok = false;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
       const uint32_t idesc = tc::idesc_m128(tmeta[g + i * G].N);
       const uint32_t acc = tmem + (uint32_t)(b * (kTmemCols / 2));
+      const uint32_t svs = sv + (uint32_t)st * sbytes;
       for (int kb = 0; kb < nkb; ++kb) {
 #pragma unroll
         for (int kk = 0; kk < kTK / 16; ++kk) {
           const uint32_t off = kk * 32;  // 16 bf16 along K inside the 128-byte swizzle row
           const uint64_t zh = tc::sw128_desc(sz + (2 * kb) * kTileBytes + off);
           const uint64_t zl = tc::sw128_desc(sz + (2 * kb + 1) * kTileBytes + off);
-          const uint64_t vh = tc::sw128_desc(sv + (2 * kb) * vblk + off);
-          const uint64_t vl = tc::sw128_desc(sv + (2 * kb + 1) * vblk + off);
+          const uint64_t vh = tc::sw128_desc(svs + (2 * kb) * vblk + off);
+          const uint64_t vl = tc::sw128_desc(svs + (2 * kb + 1) * vblk + off);
           tc::mma_bf16_id(acc, zh, vh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
           tc::mma_bf16_id(acc, zl, vh, idesc, 1u);
           tc::mma_bf16_id(acc, zh, vl, idesc, 1u);
         }
       }
-      tc::mma_commit(empty);  // frees the stage once these MMAs have read it
+      tc::mma_commit(&empty[st]);  // frees the stage once these MMAs have read it
       tc::mma_commit(&tfull[b]);
     }
   } else if (warp >= 2) {
@@ -287,42 +309,58 @@ __global__ void __launch_bounds__(kKThreads, 1)
     const bool kv = k < nk;
     const float il2 = 1.f / l2;
     const float izk = kv ? 1.f / szz[k] : 0.f;  // zero past nk: every coefficient vanishes
+    // per vector v: c1 = k1 f1_v b^(p-1), c2 = izk f2_v b^p with b = s2 + F[centre, k] / l2; the
+    // sums over v keep the per-point factors k1, izk outside
     const float k1 = pw * il2 * izk;
-    const int ipw = (int)pw;
-    const bool int_pow = (float)ipw == pw && ipw >= 1 && ipw <= 8;
-    // the records of tile j into buffer j % 3 (two float4 per vector)
-    auto stage = [&](int j) {
+    // the records of tile j into buffer j % 3 (two float4 per vector) and its centres: a tile
+    // has at most 2 nvmax <= 160 float4, one per epilogue thread, loaded into registers a whole
+    // iteration before they are stored
+    static_assert(2 * max_tile_vectors(1) <= kKEpiWarps * 32, "one record float4 per epilogue thread");
+    float4 rv = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto stage_load = [&](int j) {
       if (j >= nmine) return;
       const TileMeta m = tmeta[g + j * G];
-      float4* d = srec + (j % 3) * 2 * nvmax;
-      const float4* s = vrec + 2 * (size_t)m.vr0;
-      for (int e = etid; e < 2 * m.nvp; e += kKEpiWarps * 32) d[e] = s[e];
+      if (etid < 2 * m.nvp) rv = vrec[2 * (size_t)m.vr0 + etid];
+    };
+    auto stage_store = [&](int j) {
+      if (j >= nmine) return;
+      if (etid < 2 * tmeta[g + j * G].nvp) {
+        srec[(j % 3) * 2 * nvmax + etid] = rv;
+        if (!(etid & 1)) sce[(j % 3) * nvmax + (etid >> 1)] = __float_as_int(rv.x);
+      }
     };
     // the kernel features F[centre of v, k] of the warp's vectors of tile j (coalesced rows)
     float xf[kChunks][8];
     auto fetch = [&](int j) {
       if (j >= nmine) return;
       const int nch = tmeta[g + j * G].nvp >> 3;
-      const float4* s = srec + (j % 3) * 2 * nvmax;
+      const int* ce = sce + (j % 3) * nvmax;
 #pragma unroll
       for (int cc = 0; cc < kChunks; ++cc) {
         const int c = sub + 4 * cc;
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          float x = 0.f;
-          if (c < nch && kv) x = __ldg(F + (size_t)__float_as_int(s[2 * (c * 8 + u)].x) * nk + k);
-          xf[cc][u] = x;
+        int cv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (c < nch) {
+          const int4 lo = *reinterpret_cast<const int4*>(ce + c * 8);
+          const int4 hi = *reinterpret_cast<const int4*>(ce + c * 8 + 4);
+          cv[0] = lo.x, cv[1] = lo.y, cv[2] = lo.z, cv[3] = lo.w;
+          cv[4] = hi.x, cv[5] = hi.y, cv[6] = hi.z, cv[7] = hi.w;
         }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) xf[cc][u] = (c < nch && kv) ? __ldg(F + (size_t)cv[u] * nk + k) : 0.f;
       }
     };
-    stage(0);
-    stage(1);
+    stage_load(0);
+    stage_store(0);
+    stage_load(1);
+    stage_store(1);
     asm volatile("bar.sync 1, %0;" ::"n"(kKEpiWarps * 32));
     fetch(0);
     bool got = true;
     for (int i = 0; i < nmine; ++i) {
       const int b = i & 1;
       const TileMeta m = tmeta[g + i * G];
+      const long long xr = trow[g + i * G];
+      stage_load(i + 2);
       // the accumulator; the barrier also publishes the records staged one tile earlier, and a
       // timed-out wait in any epilogue warp ends the loop for all of them together
       const bool ready = ptx::mbar_wait(&tfull[b], (i >> 1) & 1);
@@ -339,7 +377,8 @@ __global__ void __launch_bounds__(kKThreads, 1)
       const float4* s = srec + (i % 3) * 2 * nvmax;
       const int nch = m.nvp >> 3;
       const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * (kTmemCols / 2));
-      float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+      // sum_v f1 b^(p-1) (V.z) and sum_v f2 b^p (V.x_centre) per alpha
+      float s0 = 0.f, s1 = 0.f, s2a = 0.f, t0 = 0.f, t1 = 0.f, t2 = 0.f;
 #pragma unroll
       for (int cc = 0; cc < kChunks; ++cc) {
         const int c = sub + 4 * cc;
@@ -350,19 +389,25 @@ __global__ void __launch_bounds__(kKThreads, 1)
           for (int u = 0; u < 8; ++u) {
             const float4 r = s[2 * (c * 8 + u)], gg = s[2 * (c * 8 + u) + 1];
             const float base = fmaf(xf[cc][u], il2, s2);
-            float bp1 = 1.f;  // base^(p - 1)
-            if (int_pow) {
-              for (int j = 1; j < ipw; ++j) bp1 *= base;
-            } else {
+            float bp1;  // base^(p - 1)
+            if constexpr (P == 0) {
               bp1 = powf(base, pw - 1.f);
+            } else {
+              bp1 = 1.f;
+#pragma unroll
+              for (int j = 1; j < P; ++j) bp1 *= base;
             }
-            const float c1 = k1 * r.y * bp1, c2 = izk * base * bp1 * r.z;
-            a0 = fmaf(c1, d[u], fmaf(-c2, gg.x, a0));
-            a1 = fmaf(c1, d[8 + u], fmaf(-c2, gg.y, a1));
-            a2 = fmaf(c1, d[16 + u], fmaf(-c2, gg.z, a2));
+            const float e1 = r.y * bp1, e2 = r.z * (bp1 * base);
+            s0 = fmaf(e1, d[u], s0);
+            s1 = fmaf(e1, d[8 + u], s1);
+            s2a = fmaf(e1, d[16 + u], s2a);
+            t0 = fmaf(e2, gg.x, t0);
+            t1 = fmaf(e2, gg.y, t1);
+            t2 = fmaf(e2, gg.z, t2);
           }
         }
       }
+      const float a0 = fmaf(k1, s0, -izk * t0), a1 = fmaf(k1, s1, -izk * t1), a2 = fmaf(k1, s2a, -izk * t2);
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(&tempty[b]);
@@ -375,12 +420,9 @@ __global__ void __launch_bounds__(kKThreads, 1)
       if (sub < 3) {
         const float* ra = rq + sub * 4 * 32 + lane;
         const float sum = ((ra[0] + ra[32]) + ra[64]) + ra[96];
-        const int a = m.atom, sidx = atom_struct[a];
-        const long long rf = rowF[sidx];
-        if (kv && rf >= 0 && sum != 0.f)
-          atomicAdd(&X[(rf + 3LL * (a - atom_start[sidx]) + sub) * ldx + c0 + k], sum);
+        if (kv && xr >= 0 && sum != 0.f) atomicAdd(&X[(xr + sub) * ldx + c0 + k], sum);
       }
-      stage(i + 2);
+      stage_store(i + 2);
       fetch(i + 1);
     }
     if (!got && lane == 0) atomicExch(err, 1);
@@ -404,7 +446,8 @@ int tile_vectors(int nv, int ns, int j) { return nv / ns + (j < nv % ns ? 1 : 0)
 int rows_of(int nvp) { return (3 * nvp + 15) / 16 * 16; }
 // workspace of a chunk: planes (with a spare box of rows), vector records, tile records
 size_t chunk_bytes(size_t rows, size_t vecs, size_t tiles, int KP) {
-  return 2 * al256((rows + kBoxRows) * (size_t)KP * 2) + al256(vecs * 32) + al256(tiles * sizeof(TileMeta));
+  return 2 * al256((rows + kBoxRows) * (size_t)KP * 2) + al256(vecs * 32) + al256(tiles * sizeof(TileMeta)) +
+         al256(tiles * sizeof(long long));
 }
 }  // namespace
 
@@ -432,16 +475,24 @@ cudaError_t launch_krr_force_tc(const DevBatch& b, const DevRows& rows, const in
   const int KP = nkb * kTK;
   if (KK > kKrrTcMaxK) return cudaErrorInvalidValue;  // K blocks beyond the shared-memory budget
   const int nvmax = max_tile_vectors(nkb);
-  const size_t vblk = (size_t)max_tile_rows(nkb) * kTK * 2;
-  const size_t smem = 1024 + (size_t)nkb * 2 * kTileBytes + (size_t)nkb * 2 * vblk + 3 * 2 * (size_t)nvmax * 16 +
-                      2 * 4 * 3 * 4 * 32 * 4 + 8 * 7 + 8;
+  // shared memory: everything but the V stages, then as many stages of the chunk's largest tile
+  // as fit (at least one stage of max_tile_rows rows does)
+  auto fixed_for = [&](int nvr) {
+    return 1024 + (size_t)nkb * 2 * kTileBytes + 3 * 2 * (size_t)nvr * 16 + 2 * 4 * 3 * 4 * 32 * 4 +
+           3 * (size_t)nvr * 4 + 8 * (1 + 2 * kMaxStages + 4) + 8;
+  };
   const size_t kSmemMax = 227 * 1024;
-  if (smem > kSmemMax) return cudaErrorInvalidValue;
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_krr_force_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax);
+  if (fixed_for(nvmax) + (size_t)nkb * 2 * max_tile_rows(nkb) * kTK * 2 > kSmemMax) return cudaErrorInvalidValue;
+  // the instance for the kernel power
+  const int ip = (int)power;
+  const int P = ((double)ip == power && ip >= 1 && ip <= 4) ? ip : 0;
+  auto kern = P == 1 ? k_krr_force_tc<1> : P == 2 ? k_krr_force_tc<2> : P == 3 ? k_krr_force_tc<3>
+            : P == 4 ? k_krr_force_tc<4> : k_krr_force_tc<0>;
+  static bool attr[5] = {false, false, false, false, false};
+  if (!attr[P]) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax);
     if (e != cudaSuccess) return e;
-    attr = true;
+    attr[P] = true;
   }
   // atom tiles from the neighbour counts
   std::vector<int> off(b.A + 1);
@@ -492,6 +543,16 @@ cudaError_t launch_krr_force_tc(const DevBatch& b, const DevRows& rows, const in
     }
     if (a1 == a0) return cudaErrorInvalidValue;  // one atom alone exceeds the workspace
     const size_t nt = meta.size();
+    int maxN = 0, nvr = 8;
+    for (const TileMeta& m : meta) {
+      maxN = std::max(maxN, m.N);
+      nvr = std::max(nvr, m.nvp);
+    }
+    const int vrows = (maxN + kBoxRows - 1) / kBoxRows * kBoxRows;
+    const size_t sbytes = (size_t)nkb * 2 * vrows * kTK * 2;
+    const size_t fixed = fixed_for(nvr);
+    const int stages = (int)std::min<size_t>(kMaxStages, (kSmemMax - fixed) / sbytes);
+    const size_t smem = fixed + (size_t)stages * sbytes;
     unsigned char* p = w + 2 * zb;
     __nv_bfloat16* vhi = reinterpret_cast<__nv_bfloat16*>(p);
     p += al256((nrows + kBoxRows) * KP * 2);
@@ -500,19 +561,21 @@ cudaError_t launch_krr_force_tc(const DevBatch& b, const DevRows& rows, const in
     float* vrec = reinterpret_cast<float*>(p);
     p += al256(nvecs * 32);
     TileMeta* dmeta = reinterpret_cast<TileMeta*>(p);
+    p += al256(sizeof(TileMeta) * nt);
+    long long* trow = reinterpret_cast<long long*>(p);
     e = cudaMemcpyAsync(dmeta, meta.data(), sizeof(TileMeta) * nt, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
     k_ktc_vplanes<<<(unsigned)nt, 128, 0, st>>>(dmeta, KK, KP, b.nbr_off, b.nbr_idx, rev, Bq, dBq, at, vhi, vlo,
-                                                vrec);
+                                                vrec, b.atom_struct, b.atom_start, rows.rowF, trow);
     CUtensorMap mvh, mvl;
     if (!tc::make_plane_map(&mvh, vhi, KP, (long long)(nrows + kBoxRows), KP, kBoxRows) ||
         !tc::make_plane_map(&mvl, vlo, KP, (long long)(nrows + kBoxRows), KP, kBoxRows))
       return cudaErrorInvalidValue;
     // one CTA per SM: the column tiles times G row groups in a single wave
     const int G = std::max(1, std::min<int>((int)nt, NT >= nsm ? 1 : nsm / NT));
-    k_krr_force_tc<<<dim3((unsigned)NT, (unsigned)G), kKThreads, smem, st>>>(
-        mvh, mvl, mzh, mzl, (int)nt, nkb, nk, dmeta, reinterpret_cast<const float4*>(vrec), F, szz, s2, l2, pw,
-        b.atom_struct, b.atom_start, rows.rowF, c0, rows.ldx, X, err);
+    kern<<<dim3((unsigned)NT, (unsigned)G), kKThreads, smem, st>>>(
+        mvh, mvl, mzh, mzl, (int)nt, nkb, stages, vrows, nvr, nk, dmeta, reinterpret_cast<const float4*>(vrec), F, szz, s2, l2, pw,
+        trow, c0, rows.ldx, X, err);
     *launches += 2;
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
