@@ -452,17 +452,20 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
   k_krr_xz<T><<<gx, 256, 0, st>>>(b.A, nk, KK, Bq, Z, F);
   dim3 gs(b.S, (nk + kKT - 1) / kKT);
   k_krr_energy<T><<<gs, kKT, 0, st>>>(nk, b.atom_start, rows.rowE, F, at, szz, s2, l2, power, c0, rows.ldx, X);
-  // force rows: on the tensor cores for FP32 rows (krr_tc.cu) when a workspace is given;
-  // otherwise register-tiled, reference-point tiles of NZ in shared memory (the widest tile
-  // whose working set fits)
+  // stress partials T_s, T_s . x per atom (both paths)
+  k_krr_stress_atom<T><<<b.A, 128, sizeof(T) * 3 * (size_t)std::max(1, b.maxnn), st>>>(
+      KK, b.maxnn, b.atom_struct, b.small, b.nbr_off, b.nbr_u, Bq, dBq, sign_big, Ts, tx);
+  // force and stress rows: on the tensor cores for FP32 rows (krr_tc.cu) when a workspace is
+  // given; otherwise register-tiled, reference-point tiles of NZ in shared memory (the widest
+  // tile whose working set fits)
   bool force_done = false;
   if constexpr (sizeof(T) == 4) {
     if (tcws && krr_force_tc_available() && KK <= kKrrTcMaxK) {
       int nl = 0;
-      cudaError_t e = launch_krr_force_tc(b, rows, rev, Bq, dBq, Z, F, at, szz, nk, KK, power, length, sigma, tcws,
-                                          tcws_bytes, X, c0, err, nsm, st, &nl);
+      cudaError_t e = launch_krr_force_tc(b, rows, rev, Bq, dBq, Z, F, at, szz, Ts, tx, sign_stress, nk, KK, power,
+                                          length, sigma, tcws, tcws_bytes, X, c0, err, nsm, st, &nl);
       if (e != cudaSuccess) return e;
-      *launches += nl;
+      *launches += nl + 1;
       force_done = true;
     }
   }
@@ -511,8 +514,7 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
                                b.nbr_idx, rev, Bq, dBq, Z, F, at, szz, s2, l2, power, c0, rows.ldx, X);
     *launches += 1;
   }
-  k_krr_stress_atom<T><<<b.A, 128, sizeof(T) * 3 * (size_t)std::max(1, b.maxnn), st>>>(
-      KK, b.maxnn, b.atom_struct, b.small, b.nbr_off, b.nbr_u, Bq, dBq, sign_big, Ts, tx);
+  if (force_done) return cudaGetLastError();
   {
     static int optin2 = 0;
     if (!optin2) {

@@ -50,9 +50,12 @@ constexpr int kMaxStages = 4;                  // V tile stages
 
 // rows of a V tile: up to 256 for K <= 128 (two K blocks), 128 for three K blocks (shared memory)
 __host__ __device__ constexpr int max_tile_rows(int nkb) { return nkb <= 2 ? 256 : 128; }
-// vectors of a tile: 3 nvp <= rows, nvp a multiple of 8
-__host__ __device__ constexpr int max_tile_vectors(int nkb) { return max_tile_rows(nkb) / 3 / 8 * 8; }
+// vectors of a tile with R components per vector (3 force directions, 6 stress components):
+// R nvp <= rows, nvp a multiple of 8
+__host__ __device__ constexpr int max_tile_vectors(int nkb, int R = 3) { return max_tile_rows(nkb) / R / 8 * 8; }
 static_assert(max_tile_vectors(1) / 8 <= 4 * kChunks, "chunks per epilogue warp");
+// float4 records per vector: {centre, f1, f2, 0} and the R values g, four per float4
+__host__ __device__ constexpr int recs_of(int R) { return 1 + (R + 3) / 4; }
 
 struct TileMeta {
   int atom;  // target atom (batch index)
@@ -155,6 +158,17 @@ __global__ void __launch_bounds__(128) k_ktc_vplanes(const TileMeta* __restrict_
 }
 
 namespace {
+// the R values g of a vector record
+template <int R>
+__device__ __forceinline__ void load_g(const float4* p, float* g) {
+  static_assert(R == 3 || R == 6, "force (3) or stress (6) components");
+  const float4 a = p[0];
+  g[0] = a.x, g[1] = a.y, g[2] = a.z;
+  if constexpr (R == 6) {
+    const float4 b = p[1];
+    g[3] = a.w, g[4] = b.x, g[5] = b.y;
+  }
+}
 // 3 x 8 consecutive TMEM columns (at taddr, taddr + stride, taddr + 2 stride) of the warp's 32
 // lanes into registers, waited for inside the same statement
 __device__ __forceinline__ void tmem_ld3x8(uint32_t taddr, uint32_t stride, float* out) {
@@ -182,7 +196,7 @@ __device__ __forceinline__ void tmem_ld3x8(uint32_t taddr, uint32_t stride, floa
 // sums of two tiles.  The epilogue fetches the kernel features of tile i + 1 into registers
 // before it waits for the accumulator of tile i + 1.  P: the kernel power when it is a small
 // integer (1-4), 0 for any other power (powf).
-template <int P>
+template <int P, int R>
 __global__ void __launch_bounds__(kKThreads, 1)
     k_krr_force_tc(const __grid_constant__ CUtensorMap vhi, const __grid_constant__ CUtensorMap vlo,
                    const __grid_constant__ CUtensorMap zhi, const __grid_constant__ CUtensorMap zlo, int ntiles,
@@ -198,9 +212,11 @@ __global__ void __launch_bounds__(kKThreads, 1)
   const uint32_t sbytes = (uint32_t)nkb * 2 * vblk;  // one stage
   const int nvmax = nvr;  // record rows per buffer: the chunk's largest nvp
   unsigned char* vtile = ztile + zbytes;
-  float4* srec = reinterpret_cast<float4*>(vtile + (size_t)stages * sbytes);  // [3][2 nvmax]
-  float* red = reinterpret_cast<float*>(srec + 3 * 2 * nvmax);               // [2][4][3][4][32]
-  int* sce = reinterpret_cast<int*>(red + 2 * 4 * 3 * 4 * 32);               // [3][nvmax] centres
+  constexpr int RECS = recs_of(R);
+  constexpr int NCH = (max_tile_vectors(1, R) / 8 + 3) / 4;  // vector chunks per epilogue warp and tile
+  float4* srec = reinterpret_cast<float4*>(vtile + (size_t)stages * sbytes);  // [3][RECS nvmax]
+  float* red = reinterpret_cast<float*>(srec + 3 * RECS * nvmax);            // [2][4][R][4][32]
+  int* sce = reinterpret_cast<int*>(red + 2 * 4 * R * 4 * 32);               // [3][nvmax] centres
   uint64_t* bfull = reinterpret_cast<uint64_t*>(sce + 3 * nvmax);
   uint64_t* full = bfull + 1;                 // [kMaxStages]
   uint64_t* empty = full + kMaxStages;        // [kMaxStages]
@@ -315,28 +331,28 @@ __global__ void __launch_bounds__(kKThreads, 1)
     // the records of tile j into buffer j % 3 (two float4 per vector) and its centres: a tile
     // has at most 2 nvmax <= 160 float4, one per epilogue thread, loaded into registers a whole
     // iteration before they are stored
-    static_assert(2 * max_tile_vectors(1) <= kKEpiWarps * 32, "one record float4 per epilogue thread");
+    static_assert(RECS * max_tile_vectors(1, R) <= kKEpiWarps * 32, "one record float4 per epilogue thread");
     float4 rv = make_float4(0.f, 0.f, 0.f, 0.f);
     auto stage_load = [&](int j) {
       if (j >= nmine) return;
       const TileMeta m = tmeta[g + j * G];
-      if (etid < 2 * m.nvp) rv = vrec[2 * (size_t)m.vr0 + etid];
+      if (etid < RECS * m.nvp) rv = vrec[RECS * (size_t)m.vr0 + etid];
     };
     auto stage_store = [&](int j) {
       if (j >= nmine) return;
-      if (etid < 2 * tmeta[g + j * G].nvp) {
-        srec[(j % 3) * 2 * nvmax + etid] = rv;
-        if (!(etid & 1)) sce[(j % 3) * nvmax + (etid >> 1)] = __float_as_int(rv.x);
+      if (etid < RECS * tmeta[g + j * G].nvp) {
+        srec[(j % 3) * RECS * nvmax + etid] = rv;
+        if (etid % RECS == 0) sce[(j % 3) * nvmax + etid / RECS] = __float_as_int(rv.x);
       }
     };
     // the kernel features F[centre of v, k] of the warp's vectors of tile j (coalesced rows)
-    float xf[kChunks][8];
+    float xf[NCH][8];
     auto fetch = [&](int j) {
       if (j >= nmine) return;
       const int nch = tmeta[g + j * G].nvp >> 3;
       const int* ce = sce + (j % 3) * nvmax;
 #pragma unroll
-      for (int cc = 0; cc < kChunks; ++cc) {
+      for (int cc = 0; cc < NCH; ++cc) {
         const int c = sub + 4 * cc;
         int cv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         if (c < nch) {
@@ -374,20 +390,28 @@ __global__ void __launch_bounds__(kKThreads, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const float4* s = srec + (i % 3) * 2 * nvmax;
+      const float4* s = srec + (i % 3) * RECS * nvmax;
       const int nch = m.nvp >> 3;
       const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * (kTmemCols / 2));
       // sum_v f1 b^(p-1) (V.z) and sum_v f2 b^p (V.x_centre) per alpha
-      float s0 = 0.f, s1 = 0.f, s2a = 0.f, t0 = 0.f, t1 = 0.f, t2 = 0.f;
+      float sq[R], tq2[R];
 #pragma unroll
-      for (int cc = 0; cc < kChunks; ++cc) {
+      for (int c = 0; c < R; ++c) sq[c] = tq2[c] = 0.f;
+#pragma unroll
+      for (int cc = 0; cc < NCH; ++cc) {
         const int c = sub + 4 * cc;
         if (c < nch) {
-          float d[24];
-          tmem_ld3x8(tq + (uint32_t)(c * 8), (uint32_t)m.nvp, d);
+          // three components: the accumulator columns first, so that their load overlaps the
+          // coefficients; six: coefficients first, then three columns at a time (registers)
+          float d0[24];
+          if constexpr (R == 3) tmem_ld3x8(tq + (uint32_t)(c * 8), (uint32_t)m.nvp, d0);
+          // per vector: e1 = f1 b^(p-1), e2 = f2 b^p; the g sums need no accumulator values
+          float e1[8];
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
-            const float4 r = s[2 * (c * 8 + u)], gg = s[2 * (c * 8 + u) + 1];
+            const float4 r = s[RECS * (c * 8 + u)];
+            float gv[R];
+            load_g<R>(s + RECS * (c * 8 + u) + 1, gv);
             const float base = fmaf(xf[cc][u], il2, s2);
             float bp1;  // base^(p - 1)
             if constexpr (P == 0) {
@@ -397,30 +421,43 @@ __global__ void __launch_bounds__(kKThreads, 1)
 #pragma unroll
               for (int j = 1; j < P; ++j) bp1 *= base;
             }
-            const float e1 = r.y * bp1, e2 = r.z * (bp1 * base);
-            s0 = fmaf(e1, d[u], s0);
-            s1 = fmaf(e1, d[8 + u], s1);
-            s2a = fmaf(e1, d[16 + u], s2a);
-            t0 = fmaf(e2, gg.x, t0);
-            t1 = fmaf(e2, gg.y, t1);
-            t2 = fmaf(e2, gg.z, t2);
+            e1[u] = r.y * bp1;
+            const float e2 = r.z * (bp1 * base);
+#pragma unroll
+            for (int q2 = 0; q2 < R; ++q2) tq2[q2] = fmaf(e2, gv[q2], tq2[q2]);
+          }
+          // the accumulator columns, three components at a time
+#pragma unroll
+          for (int h = 0; h < R / 3; ++h) {
+            float d[24];
+            if constexpr (R == 3) {
+#pragma unroll
+              for (int x = 0; x < 24; ++x) d[x] = d0[x];
+            } else {
+              tmem_ld3x8(tq + (uint32_t)(c * 8 + 3 * h * m.nvp), (uint32_t)m.nvp, d);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+#pragma unroll
+              for (int q2 = 0; q2 < 3; ++q2) sq[3 * h + q2] = fmaf(e1[u], d[8 * q2 + u], sq[3 * h + q2]);
           }
         }
       }
-      const float a0 = fmaf(k1, s0, -izk * t0), a1 = fmaf(k1, s1, -izk * t1), a2 = fmaf(k1, s2a, -izk * t2);
+      float av[R];
+#pragma unroll
+      for (int q2 = 0; q2 < R; ++q2) av[q2] = fmaf(k1, sq[q2], -izk * tq2[q2]);
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(&tempty[b]);
       // the quarter's four partial sums per alpha, added in a fixed order
-      float* rq = red + (size_t)((i & 1) * 4 + q) * 3 * 4 * 32;  // [alpha][sub][lane]
-      rq[(0 * 4 + sub) * 32 + lane] = a0;
-      rq[(1 * 4 + sub) * 32 + lane] = a1;
-      rq[(2 * 4 + sub) * 32 + lane] = a2;
+      float* rq = red + (size_t)((i & 1) * 4 + q) * R * 4 * 32;  // [component][sub][lane]
+#pragma unroll
+      for (int q2 = 0; q2 < R; ++q2) rq[(q2 * 4 + sub) * 32 + lane] = av[q2];
       asm volatile("bar.sync %0, %1;" ::"r"(4 + q), "n"(128));
-      if (sub < 3) {
-        const float* ra = rq + sub * 4 * 32 + lane;
+      for (int q2 = sub; q2 < R; q2 += 4) {
+        const float* ra = rq + q2 * 4 * 32 + lane;
         const float sum = ((ra[0] + ra[32]) + ra[64]) + ra[96];
-        if (kv && xr >= 0 && sum != 0.f) atomicAdd(&X[(xr + sub) * ldx + c0 + k], sum);
+        if (kv && xr >= 0 && sum != 0.f) atomicAdd(&X[(xr + q2) * ldx + c0 + k], sum);
       }
       stage_store(i + 2);
       fetch(i + 1);
@@ -438,16 +475,178 @@ __global__ void __launch_bounds__(kKThreads, 1)
 
 bool krr_force_tc_available() { return tc::encode_fn() != nullptr; }
 
+// Stress tiles: tile = a run of <= max_tile_vectors(nkb, 6) atoms of one structure (TileMeta.atom
+// holds the structure, v0 its first atom within the structure).  Rows: Ts[a][sigma] (the stress
+// partials of k_krr_stress_atom, sigma-major, nvp rows per component); records {atom, sc / sqrt
+// f(x,x), sc dker_xx / (2 f(x,x) sqrt f(x,x)), 0}, {tx[a][0..3]}, {tx[a][4..5], 0, 0} with
+// sc = sign_stress * 3 / volume (the normalisation of k_krr_stress_tiled).
+__global__ void __launch_bounds__(128) k_ktc_splanes(const TileMeta* __restrict__ tmeta, int KK, int KP,
+                                                     const int* __restrict__ atom_start, const float* __restrict__ Ts,
+                                                     const float* __restrict__ tx, const float* __restrict__ at,
+                                                     const double* __restrict__ volume, double sign_stress,
+                                                     const long long* __restrict__ rowS,
+                                                     __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                                                     float* __restrict__ vrec, long long* __restrict__ trow) {
+  const TileMeta m = tmeta[blockIdx.x];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sidx = m.atom, a0 = atom_start[sidx] + m.v0;
+  if (threadIdx.x == 0) trow[blockIdx.x] = rowS[sidx];
+  const float sc = (float)(sign_stress * 3.0 / volume[sidx]);
+  for (int lr = warp; lr < m.N; lr += 4) {
+    const long long row = (long long)m.row0 + lr;
+    const int q = lr / m.nvp, vl = lr - q * m.nvp;
+    const bool valid = q < 6 && vl < m.nvt;
+    const int a = valid ? a0 + vl : a0;
+    for (int c = lane; c < KP; c += 32) {
+      const float x = (valid && c < KK) ? Ts[((size_t)a * 6 + q) * KK + c] : 0.f;
+      const __nv_bfloat16 h = __float2bfloat16_rn(x);
+      hi[row * KP + c] = h;
+      lo[row * KP + c] = __float2bfloat16_rn(x - __bfloat162float(h));
+    }
+    if (lane == 0 && q < 6) {
+      float* r = vrec + 12 * ((size_t)m.vr0 + vl);
+      r[4 + q] = valid ? tx[6 * (size_t)a + q] : 0.f;
+      if (q == 0) {
+        float f1 = 0.f, f2 = 0.f;
+        if (valid) {
+          const float4 a4 = *reinterpret_cast<const float4*>(at + 4 * (size_t)a);
+          if (a4.w != 0.f) {
+            f1 = sc / a4.y;
+            f2 = a4.z / (2.f * a4.x) * f1;
+          }
+        }
+        r[0] = __int_as_float(a);
+        r[1] = f1;
+        r[2] = f2;
+        r[3] = 0.f;
+        r[10] = 0.f;
+        r[11] = 0.f;
+      }
+    }
+  }
+}
+
 namespace {
 size_t al256(size_t x) { return (x + 255) / 256 * 256; }
-// split of an atom with nv derivative vectors into tiles: count, and vectors of tile j
+// split of a group of nv vectors into tiles: count, and vectors of tile j
 int tiles_of(int nv, int nvmax) { return (nv + nvmax - 1) / nvmax; }
 int tile_vectors(int nv, int ns, int j) { return nv / ns + (j < nv % ns ? 1 : 0); }
-int rows_of(int nvp) { return (3 * nvp + 15) / 16 * 16; }
-// workspace of a chunk: planes (with a spare box of rows), vector records, tile records
-size_t chunk_bytes(size_t rows, size_t vecs, size_t tiles, int KP) {
-  return 2 * al256((rows + kBoxRows) * (size_t)KP * 2) + al256(vecs * 32) + al256(tiles * sizeof(TileMeta)) +
-         al256(tiles * sizeof(long long));
+int rows_of(int nvp, int R) { return (R * nvp + 15) / 16 * 16; }
+// workspace of a chunk: planes (with a spare box of rows), vector records, tile records and rows
+size_t chunk_bytes(size_t rows, size_t vecs, size_t tiles, int KP, int R) {
+  return 2 * al256((rows + kBoxRows) * (size_t)KP * 2) + al256(vecs * 16 * recs_of(R)) +
+         al256(tiles * sizeof(TileMeta)) + al256(tiles * sizeof(long long));
+}
+// the tiles of a group of nv vectors owned by `owner` (row0 and vr0 are set per chunk)
+void push_tiles(std::vector<TileMeta>& tiles, int owner, int nv, int nvmax, int R) {
+  const int ns = tiles_of(nv, nvmax);
+  for (int j = 0, v0 = 0; j < ns; ++j) {
+    const int nvt = tile_vectors(nv, ns, j), nvp = (nvt + 7) / 8 * 8;
+    tiles.push_back(TileMeta{owner, 0, rows_of(nvp, R), nvp, 0, v0, nvt, 0});
+    v0 += nvt;
+  }
+}
+size_t fixed_smem(int nkb, int nvr, int R) {
+  return 1024 + (size_t)nkb * 2 * kTileBytes + 3 * (size_t)recs_of(R) * nvr * 16 + 2 * 4 * (size_t)R * 4 * 32 * 4 +
+         3 * (size_t)nvr * 4 + 8 * (1 + 2 * kMaxStages + 4) + 8;
+}
+constexpr size_t kSmemMax = 227 * 1024;
+
+using ForceKernel = void (*)(CUtensorMap, CUtensorMap, CUtensorMap, CUtensorMap, int, int, int, int, int, int,
+                             const TileMeta*, const float4*, const float*, const float*, float, float, float,
+                             const long long*, int, int, float*, int*);
+template <int R>
+ForceKernel kernel_for(int P) {
+  return P == 1 ? k_krr_force_tc<1, R> : P == 2 ? k_krr_force_tc<2, R> : P == 3 ? k_krr_force_tc<3, R>
+       : P == 4 ? k_krr_force_tc<4, R> : k_krr_force_tc<0, R>;
+}
+
+// shared state of the force and stress passes
+struct PassCtx {
+  int nkb, KP, nk, NT, nsm;
+  CUtensorMap mzh, mzl;
+  unsigned char* chunk_ws;  // after the Z planes
+  size_t room;
+  const float* F;
+  const float* szz;
+  float s2, l2, pw;
+  int P, c0, ldx;
+  float* X;
+  int* err;
+  cudaStream_t st;
+};
+
+// Runs `tiles` in chunks that fit the workspace: `build` writes a chunk's planes, records and
+// tile rows, then the tensor-core kernel adds the chunk's rows into X.
+template <int R, typename Build>
+cudaError_t run_tiles(const std::vector<TileMeta>& tiles, const PassCtx& c, Build build, int* launches) {
+  ForceKernel kern = kernel_for<R>(c.P);
+  static bool attr[5] = {false, false, false, false, false};
+  if (!attr[c.P]) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax);
+    if (e != cudaSuccess) return e;
+    attr[c.P] = true;
+  }
+  std::vector<TileMeta> meta;
+  for (size_t i0 = 0; i0 < tiles.size();) {
+    meta.clear();
+    size_t nrows = 0, nvecs = 0, i1 = i0;
+    while (i1 < tiles.size()) {
+      TileMeta m = tiles[i1];
+      if (chunk_bytes(nrows + m.N, nvecs + m.nvp, meta.size() + 1, c.KP, R) > c.room) break;
+      m.row0 = (int)nrows;
+      m.vr0 = (int)nvecs;
+      meta.push_back(m);
+      nrows += m.N;
+      nvecs += m.nvp;
+      ++i1;
+    }
+    if (i1 == i0) return cudaErrorInvalidValue;  // one tile alone exceeds the workspace
+    const size_t nt = meta.size();
+    // shared memory: everything but the V stages, then as many stages of the chunk's largest
+    // tile as fit (at least one stage of max_tile_rows rows does)
+    int maxN = 0, nvr = 8;
+    for (const TileMeta& m : meta) {
+      maxN = std::max(maxN, m.N);
+      nvr = std::max(nvr, m.nvp);
+    }
+    const int vrows = (maxN + kBoxRows - 1) / kBoxRows * kBoxRows;
+    const size_t sbytes = (size_t)c.nkb * 2 * vrows * kTK * 2;
+    const size_t fixed = fixed_smem(c.nkb, nvr, R);
+    const int stages = (int)std::min<size_t>(kMaxStages, (kSmemMax - fixed) / sbytes);
+    if (stages < 1) return cudaErrorInvalidValue;
+    const size_t smem = fixed + (size_t)stages * sbytes;
+    unsigned char* p = c.chunk_ws;
+    __nv_bfloat16* vhi = reinterpret_cast<__nv_bfloat16*>(p);
+    p += al256((nrows + kBoxRows) * c.KP * 2);
+    __nv_bfloat16* vlo = reinterpret_cast<__nv_bfloat16*>(p);
+    p += al256((nrows + kBoxRows) * c.KP * 2);
+    float* vrec = reinterpret_cast<float*>(p);
+    p += al256(nvecs * 16 * recs_of(R));
+    TileMeta* dmeta = reinterpret_cast<TileMeta*>(p);
+    p += al256(sizeof(TileMeta) * nt);
+    long long* trow = reinterpret_cast<long long*>(p);
+    cudaError_t e = cudaMemcpyAsync(dmeta, meta.data(), sizeof(TileMeta) * nt, cudaMemcpyHostToDevice, c.st);
+    if (e != cudaSuccess) return e;
+    build(dmeta, (int)nt, vhi, vlo, vrec, trow);
+    CUtensorMap mvh, mvl;
+    if (!tc::make_plane_map(&mvh, vhi, c.KP, (long long)(nrows + kBoxRows), c.KP, kBoxRows) ||
+        !tc::make_plane_map(&mvl, vlo, c.KP, (long long)(nrows + kBoxRows), c.KP, kBoxRows))
+      return cudaErrorInvalidValue;
+    // one CTA per SM: the column tiles times G row groups in a single wave
+    const int G = std::max(1, std::min<int>((int)nt, c.NT >= c.nsm ? 1 : c.nsm / c.NT));
+    kern<<<dim3((unsigned)c.NT, (unsigned)G), kKThreads, smem, c.st>>>(
+        mvh, mvl, c.mzh, c.mzl, (int)nt, c.nkb, stages, vrows, nvr, c.nk, dmeta,
+        reinterpret_cast<const float4*>(vrec), c.F, c.szz, c.s2, c.l2, c.pw, trow, c.c0, c.ldx, c.X, c.err);
+    *launches += 2;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // the host records of the next chunk overwrite dmeta only after this chunk's kernels
+    e = cudaStreamSynchronize(c.st);
+    if (e != cudaSuccess) return e;
+    i0 = i1;
+  }
+  return cudaSuccess;
 }
 }  // namespace
 
@@ -457,134 +656,96 @@ size_t krr_force_tc_workspace_bytes(long long atoms, int maxnv, int nk, int KK) 
   const int ns = tiles_of(std::max(maxnv, 1), nvmax);
   const int nvp = (tile_vectors(std::max(maxnv, 1), ns, 0) + 7) / 8 * 8;
   const size_t tiles = (size_t)atoms * ns;
-  return 2 * al256((size_t)nk * KP * 2) + 8 * 256 + chunk_bytes(tiles * rows_of(nvp), tiles * nvp, tiles, KP);
+  return 2 * al256((size_t)nk * KP * 2) + 8 * 256 +
+         chunk_bytes(tiles * rows_of(nvp, 3), tiles * nvp, tiles, KP, 3);
 }
 
-// Force rows of the kernel block (columns [c0, c0 + nk) of X) for every atom with force rows,
-// replacing k_krr_force_tiled for the FP32 rows.  ws (ws_bytes) holds the Z planes and, per
-// chunk of atoms, the derivative-vector planes and their vector and tile records; chunks are as
-// large as ws allows.  F, at, szz: the kernel features, atom terms and point norms of
-// launch_krr_rows.  X must hold zeros in these columns (the sums are added atomically).
+// Force and stress rows of the kernel block (columns [c0, c0 + nk) of X), replacing
+// k_krr_force_tiled and k_krr_stress_tiled for the FP32 rows.  ws (ws_bytes) holds the Z planes
+// and, per chunk of tiles, the row planes and their vector and tile records; chunks are as large
+// as ws allows.  F, at, szz: the kernel features, atom terms and point norms of launch_krr_rows;
+// Ts, tx: the stress partials of k_krr_stress_atom.  X must hold zeros in these columns (the sums
+// are added atomically).
 cudaError_t launch_krr_force_tc(const DevBatch& b, const DevRows& rows, const int* rev, const float* Bq,
                                 const float* dBq, const float* Z, const float* F, const float* at, const float* szz,
-                                int nk, int KK, double power, double length, double sigma, void* ws, size_t ws_bytes,
-                                float* X, int c0, int* err, int nsm, cudaStream_t st, int* launches) {
+                                const float* Ts, const float* tx, double sign_stress, int nk, int KK, double power,
+                                double length, double sigma, void* ws, size_t ws_bytes, float* X, int c0, int* err,
+                                int nsm, cudaStream_t st, int* launches) {
   *launches = 0;
   if (b.A == 0 || nk == 0) return cudaSuccess;
   const int nkb = (KK + kTK - 1) / kTK;
   const int KP = nkb * kTK;
   if (KK > kKrrTcMaxK) return cudaErrorInvalidValue;  // K blocks beyond the shared-memory budget
-  const int nvmax = max_tile_vectors(nkb);
-  // shared memory: everything but the V stages, then as many stages of the chunk's largest tile
-  // as fit (at least one stage of max_tile_rows rows does)
-  auto fixed_for = [&](int nvr) {
-    return 1024 + (size_t)nkb * 2 * kTileBytes + 3 * 2 * (size_t)nvr * 16 + 2 * 4 * 3 * 4 * 32 * 4 +
-           3 * (size_t)nvr * 4 + 8 * (1 + 2 * kMaxStages + 4) + 8;
-  };
-  const size_t kSmemMax = 227 * 1024;
-  if (fixed_for(nvmax) + (size_t)nkb * 2 * max_tile_rows(nkb) * kTK * 2 > kSmemMax) return cudaErrorInvalidValue;
-  // the instance for the kernel power
-  const int ip = (int)power;
-  const int P = ((double)ip == power && ip >= 1 && ip <= 4) ? ip : 0;
-  auto kern = P == 1 ? k_krr_force_tc<1> : P == 2 ? k_krr_force_tc<2> : P == 3 ? k_krr_force_tc<3>
-            : P == 4 ? k_krr_force_tc<4> : k_krr_force_tc<0>;
-  static bool attr[5] = {false, false, false, false, false};
-  if (!attr[P]) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax);
-    if (e != cudaSuccess) return e;
-    attr[P] = true;
-  }
-  // atom tiles from the neighbour counts
-  std::vector<int> off(b.A + 1);
+  const int nvmax3 = max_tile_vectors(nkb, 3), nvmax6 = max_tile_vectors(nkb, 6);
+  if (fixed_smem(nkb, nvmax3, 3) + (size_t)nkb * 2 * max_tile_rows(nkb) * kTK * 2 > kSmemMax ||
+      fixed_smem(nkb, nvmax6, 6) + (size_t)nkb * 2 * max_tile_rows(nkb) * kTK * 2 > kSmemMax)
+    return cudaErrorInvalidValue;
+  // tiles: per atom its derivative vectors (force), per structure its atoms (stress)
+  std::vector<int> off(b.A + 1), ast(b.S + 1);
   cudaError_t e = cudaMemcpyAsync(off.data(), b.nbr_off, sizeof(int) * (b.A + 1), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ast.data(), b.atom_start, sizeof(int) * (b.S + 1), cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return e;
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return e;
-  // workspace: Z planes, then the chunk's planes, vector records and tile records
+  std::vector<TileMeta> ftiles, stiles;
+  for (int a = 0; a < b.A; ++a) push_tiles(ftiles, a, off[a + 1] - off[a] + 1, nvmax3, 3);
+  for (int s = 0; s < b.S; ++s)
+    if (ast[s + 1] > ast[s]) push_tiles(stiles, s, ast[s + 1] - ast[s], nvmax6, 6);
+  // workspace: Z planes, then the chunks
+  PassCtx c{};
   unsigned char* w = static_cast<unsigned char*>(ws);
   const size_t zb = al256((size_t)nk * KP * 2);
   __nv_bfloat16* zhi = reinterpret_cast<__nv_bfloat16*>(w);
   __nv_bfloat16* zlo = reinterpret_cast<__nv_bfloat16*>(w + zb);
   if (ws_bytes < 2 * zb + 8 * 256) return cudaErrorInvalidValue;
-  const size_t room = ws_bytes - 2 * zb - 8 * 256;
+  c.chunk_ws = w + 2 * zb;
+  c.room = ws_bytes - 2 * zb - 8 * 256;
   {
     const long long n = (long long)nk * KP;
     k_ktc_zplanes<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(Z, nk, KK, KP, zhi, zlo);
     ++*launches;
   }
-  CUtensorMap mzh, mzl;
-  if (!tc::make_plane_map(&mzh, zhi, KP, nk, KP) || !tc::make_plane_map(&mzl, zlo, KP, nk, KP))
+  if (!tc::make_plane_map(&c.mzh, zhi, KP, nk, KP) || !tc::make_plane_map(&c.mzl, zlo, KP, nk, KP))
     return cudaErrorInvalidValue;
-  const float s2 = (float)(sigma * sigma), l2 = (float)(2.0 * length * length), pw = (float)power;
-  const int NT = (nk + kTM - 1) / kTM;
-  std::vector<TileMeta> meta;
-  for (int a0 = 0; a0 < b.A;) {
-    // the largest run of atoms whose tiles fit the workspace
-    meta.clear();
-    size_t nrows = 0, nvecs = 0;
-    int a1 = a0;
-    while (a1 < b.A) {
-      const int nv = off[a1 + 1] - off[a1] + 1, ns = tiles_of(nv, nvmax);
-      size_t r = 0, v = 0;
-      for (int j = 0; j < ns; ++j) {
-        const int nvp = (tile_vectors(nv, ns, j) + 7) / 8 * 8;
-        r += rows_of(nvp);
-        v += nvp;
-      }
-      if (chunk_bytes(nrows + r, nvecs + v, meta.size() + ns, KP) > room) break;
-      for (int j = 0, v0 = 0; j < ns; ++j) {
-        const int nvt = tile_vectors(nv, ns, j), nvp = (nvt + 7) / 8 * 8;
-        meta.push_back(TileMeta{a1, (int)nrows, rows_of(nvp), nvp, (int)nvecs, v0, nvt, 0});
-        nrows += rows_of(nvp);
-        nvecs += nvp;
-        v0 += nvt;
-      }
-      ++a1;
-    }
-    if (a1 == a0) return cudaErrorInvalidValue;  // one atom alone exceeds the workspace
-    const size_t nt = meta.size();
-    int maxN = 0, nvr = 8;
-    for (const TileMeta& m : meta) {
-      maxN = std::max(maxN, m.N);
-      nvr = std::max(nvr, m.nvp);
-    }
-    const int vrows = (maxN + kBoxRows - 1) / kBoxRows * kBoxRows;
-    const size_t sbytes = (size_t)nkb * 2 * vrows * kTK * 2;
-    const size_t fixed = fixed_for(nvr);
-    const int stages = (int)std::min<size_t>(kMaxStages, (kSmemMax - fixed) / sbytes);
-    const size_t smem = fixed + (size_t)stages * sbytes;
-    unsigned char* p = w + 2 * zb;
-    __nv_bfloat16* vhi = reinterpret_cast<__nv_bfloat16*>(p);
-    p += al256((nrows + kBoxRows) * KP * 2);
-    __nv_bfloat16* vlo = reinterpret_cast<__nv_bfloat16*>(p);
-    p += al256((nrows + kBoxRows) * KP * 2);
-    float* vrec = reinterpret_cast<float*>(p);
-    p += al256(nvecs * 32);
-    TileMeta* dmeta = reinterpret_cast<TileMeta*>(p);
-    p += al256(sizeof(TileMeta) * nt);
-    long long* trow = reinterpret_cast<long long*>(p);
-    e = cudaMemcpyAsync(dmeta, meta.data(), sizeof(TileMeta) * nt, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return e;
-    k_ktc_vplanes<<<(unsigned)nt, 128, 0, st>>>(dmeta, KK, KP, b.nbr_off, b.nbr_idx, rev, Bq, dBq, at, vhi, vlo,
-                                                vrec, b.atom_struct, b.atom_start, rows.rowF, trow);
-    CUtensorMap mvh, mvl;
-    if (!tc::make_plane_map(&mvh, vhi, KP, (long long)(nrows + kBoxRows), KP, kBoxRows) ||
-        !tc::make_plane_map(&mvl, vlo, KP, (long long)(nrows + kBoxRows), KP, kBoxRows))
-      return cudaErrorInvalidValue;
-    // one CTA per SM: the column tiles times G row groups in a single wave
-    const int G = std::max(1, std::min<int>((int)nt, NT >= nsm ? 1 : nsm / NT));
-    kern<<<dim3((unsigned)NT, (unsigned)G), kKThreads, smem, st>>>(
-        mvh, mvl, mzh, mzl, (int)nt, nkb, stages, vrows, nvr, nk, dmeta, reinterpret_cast<const float4*>(vrec), F, szz, s2, l2, pw,
-        trow, c0, rows.ldx, X, err);
-    *launches += 2;
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    // the host records of the next chunk overwrite dmeta only after this chunk's kernels
-    e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return e;
-    a0 = a1;
-  }
-  return cudaSuccess;
+  c.nkb = nkb;
+  c.KP = KP;
+  c.nk = nk;
+  c.NT = (nk + kTM - 1) / kTM;
+  c.nsm = nsm;
+  c.F = F;
+  c.szz = szz;
+  c.s2 = (float)(sigma * sigma);
+  c.l2 = (float)(2.0 * length * length);
+  c.pw = (float)power;
+  const int ip = (int)power;
+  c.P = ((double)ip == power && ip >= 1 && ip <= 4) ? ip : 0;
+  c.c0 = c0;
+  c.ldx = rows.ldx;
+  c.X = X;
+  c.err = err;
+  c.st = st;
+  int nl = 0;
+  e = run_tiles<3>(ftiles, c,
+                   [&](const TileMeta* dm, int nt, __nv_bfloat16* vhi, __nv_bfloat16* vlo, float* vrec,
+                       long long* trow) {
+                     k_ktc_vplanes<<<(unsigned)nt, 128, 0, st>>>(dm, KK, KP, b.nbr_off, b.nbr_idx, rev, Bq, dBq, at,
+                                                                 vhi, vlo, vrec, b.atom_struct, b.atom_start,
+                                                                 rows.rowF, trow);
+                   },
+                   &nl);
+  *launches += nl;
+  if (e != cudaSuccess) return e;
+  nl = 0;
+  e = run_tiles<6>(stiles, c,
+                   [&](const TileMeta* dm, int nt, __nv_bfloat16* vhi, __nv_bfloat16* vlo, float* vrec,
+                       long long* trow) {
+                     k_ktc_splanes<<<(unsigned)nt, 128, 0, st>>>(dm, KK, KP, b.atom_start, Ts, tx, at, b.volume,
+                                                                 sign_stress, rows.rowS, vhi, vlo, vrec, trow);
+                   },
+                   &nl);
+  *launches += nl;
+  return e;
 }
 
 }  // namespace mld

@@ -298,8 +298,9 @@ bool krr_force_tc_available();
 size_t krr_force_tc_workspace_bytes(long long atoms, int maxnv, int nk, int KK);
 cudaError_t launch_krr_force_tc(const DevBatch& b, const DevRows& rows, const int* rev, const float* Bq,
                                 const float* dBq, const float* Z, const float* F, const float* at, const float* szz,
-                                int nk, int KK, double power, double length, double sigma, void* ws, size_t ws_bytes,
-                                float* X, int c0, int* err, int nsm, cudaStream_t st, int* launches);
+                                const float* Ts, const float* tx, double sign_stress, int nk, int KK, double power,
+                                double length, double sigma, void* ws, size_t ws_bytes, float* X, int c0, int* err,
+                                int nsm, cudaStream_t st, int* launches);
 
 // tensor-core Gram in BF16 split precision (gram_tc.cu)
 size_t gram_tc_min_workspace(int D);
