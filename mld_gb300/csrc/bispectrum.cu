@@ -377,17 +377,20 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
       for (int ch = 0; ch < nch; ++ch) {
         const cx<T>* cc = cfull + ch * NU;
         cx<T>* Yc = Y + (size_t)ch * NYP;
+        // each lane's entry of the next round is loaded while the current one is computed
+        ZItem nx{};
+        if (r0 < r1) nx = tb.zitems[(size_t)r0 * 32 + lane];
         for (int r = r0; r < r1; ++r) {
-          const ZItem zi = tb.zitems[(size_t)r * 32 + lane];
-          const ZTerm z = tb.zterms[zi.zt];
+          const ZItem zi = nx;
+          if (r + 1 < r1) nx = tb.zitems[(size_t)(r + 1) * 32 + lane];
           cx<T> zs = {T(0), T(0)};
-          int i1a = z.i1, i2a = z.i2;
-          const T* cg2 = cgs + z.cg2;
-          for (int a = 0; a < z.na; ++a) {
-            const T c1 = cgs[z.cg1 + a];
+          int i1a = zi.i1, i2a = zi.i2;
+          const T* cg2 = cgs + zi.cg2;
+          for (int a = 0; a < zi.na; ++a) {
+            const T c1 = cgs[zi.cg1 + a];
             cx<T> part = {T(0), T(0)};
 #pragma unroll 3
-            for (int b = 0; b < z.nb; ++b) {
+            for (int b = 0; b < zi.nb; ++b) {
               const cx<T> pr = cmul(cc[i1a + b], cc[i2a - b]);
               const T c2 = cg2[b];
               part.x = fma(c2, pr.x, part.x);
@@ -395,8 +398,8 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
             }
             zs.x = fma(c1, part.x, zs.x);
             zs.y = fma(c1, part.y, zs.y);
-            i1a += z.s1;
-            i2a -= z.s2;
+            i1a += zi.s1;
+            i2a -= zi.s2;
           }
           if (zi.is_a) {
             const cx<T> cv = cc[zi.ufull];

@@ -265,14 +265,21 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
       for (int tt = 0; tt < s.nterm; ++tt) {
         const ZTerm& z = t->zterms[s.term[tt]];
         ZItem zi{};
-        zi.zt = s.term[tt];
+        zi.i1 = z.i1;
+        zi.i2 = z.i2;
+        zi.cg1 = z.cg1;
+        zi.cg2 = z.cg2;
+        zi.na = z.na;
+        zi.nb = z.nb;
+        zi.s1 = z.s1;
+        zi.s2 = z.s2;
         zi.ypos = s.ypos;
         zi.ufull = s.ufull;
         zi.k = s.k;
-        zi.snum = z.snum;
-        zi.sden = z.sden;
         zi.wgt = s.wgt;
         zi.is_a = (tt == 0 && s.is_a) ? 1 : 0;
+        zi.snum = z.snum;
+        zi.sden = z.sden;
         byshape[{z.na, z.nb}].push_back(zi);
       }
     }

@@ -43,16 +43,19 @@ struct YSlot {
   uint8_t pad;
 };
 
-// One Z-term work entry of the phase-2 schedule (one lane of a round): term `zt` of the slot at
-// `ypos`; wgt = 0 marks a padding lane.
-struct ZItem {
-  uint16_t zt;             // ZTerm index
-  uint16_t ypos;           // Y position of its slot
-  uint16_t ufull;          // c index of the slot's (j,p,q) (for B)
-  uint16_t k;              // triple
-  uint8_t snum, sden, wgt, is_a;  // scale, fold weight, ZA flag
-  uint32_t pad;
+// One lane of a phase-2 round, self-contained so that a lane fetches its work with one 32-byte
+// load: the Z term (c indices of its first product, CG offsets, loop extents and strides) and
+// its slot (Y position, c index of the slot's (j,p,q) for B, triple, scale); wgt = 0 marks a
+// padding lane.
+struct alignas(16) ZItem {
+  uint16_t i1, i2, cg1, cg2;  // first (ma,mb) c index / matching second factor, CG offsets
+  uint8_t na, nb, s1, s2;     // loop extents and layer strides (j+1)
+  uint16_t ypos, ufull, k;    // slot: Y position, c index of its (j,p,q), triple
+  uint8_t wgt, is_a;          // fold weight, ZA flag
+  uint8_t snum, sden;         // scale snum / sden (formed in the kernel's precision)
+  uint8_t pad[10];
 };
+static_assert(sizeof(ZItem) == 32, "phase-2 entries are 32 bytes");
 
 // Packed per-entry recursion record of the half layers (one 16-byte load per entry).
 struct RecEntry32 {
