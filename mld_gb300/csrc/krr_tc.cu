@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kKThreads, 1)
     int issued = 0;
     for (int i = 0; i < nmine; ++i) {
       const int st = i % stages;
-      if (i >= stages && !ptx::mbar_wait(&empty[st], ((i / stages) - 1) & 1)) {
+      if (i >= stages && !ptx::mbar_wait_sleep(&empty[st], ((i / stages) - 1) & 1)) {
         ok = false;
         break;
       }
@@ -288,12 +288,12 @@ __global__ void __launch_bounds__(kKThreads, 1)
     const uint32_t sz = ptx::smem_u32(ztile), sv = ptx::smem_u32(vtile);
     for (int i = 0; i < nmine && ok; ++i) {
       const int b = i & 1;
-      if (i >= 2 && !ptx::mbar_wait(&tempty[b], ((i >> 1) - 1) & 1)) {
+      if (i >= 2 && !ptx::mbar_wait_sleep(&tempty[b], ((i >> 1) - 1) & 1)) {
         ok = false;
         break;
       }
       const int st = i % stages;
-      if (!ptx::mbar_wait(&full[st], (i / stages) & 1)) {
+      if (!ptx::mbar_wait_sleep(&full[st], (i / stages) & 1)) {
         ok = false;
         break;
       }

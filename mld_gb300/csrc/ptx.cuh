@@ -33,6 +33,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// try_wait that lets the hardware suspend the thread for up to `ns` nanoseconds before it
+// reports an incomplete phase (a waiting warp then stops taking issue slots)
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait (about one second) with suspension between polls; false on expiry
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait_sleep(bar, parity, 2000u)) {
+    if (clock64() - t0 > kWaitLimit) return false;
+  }
+  return true;
+}
 // bounded wait for the phase of the given parity; false on expiry
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   const long long t0 = clock64();
