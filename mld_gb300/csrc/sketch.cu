@@ -13,9 +13,9 @@
 //   * the embedding: copy j of row r goes to sketch row (pi_j(r) mod s) with a hashed sign,
 //     pi_j(r) = (a_j r + b_j) mod M an affine permutation; sketch row i therefore gathers rows
 //     r = a_j^-1 (t - b_j) mod M for t = i, i + s, ... < M, in a fixed order (deterministic sums);
-//   * k_sketch_gather: one CTA per sketch row, double-FP32 sums of the signed, weighted rows, the
-//     result rounded to FP32 (a relative perturbation of 2^-24, far inside the preconditioner's
-//     tolerance);
+//   * k_sketch_gather: one CTA per (sketch row, 2048-column block), two rows in flight,
+//     double-FP32 sums of the signed, weighted rows, the result rounded to FP32 (a relative
+//     perturbation of 2^-24, far inside the preconditioner's tolerance);
 //   * k_ds_gram: upper 64 x 64 tiles of Y^T Y with exact FP32 products (fmaf) and double-FP32
 //     sums, written as FP64.
 // With M <= s the "sketch" is W^1/2 X itself (zeta = 1, identity permutation, sign +1).
@@ -71,12 +71,14 @@ __global__ void k_sketch_scale(const double* __restrict__ w, long long M, double
   if (r < M) sw[r] = (float)sqrt(w[r] * inv_zeta);
 }
 
-// Y[i, :] = sum over the rows r of sketch row i of sign(r, j) sw[r] X[r, c0 : c0 + D]
+// Y[i, cb : cb + 256 CPT] = sum over the rows r of sketch row i of sign(r, j) sw[r] X[r, c0 + cb ...],
+// cb = 256 CPT blockIdx.y: a CTA per (sketch row, column block)
 template <int CPT>
 __global__ void __launch_bounds__(256) k_sketch_gather(const float* __restrict__ X, int ldx, int c0, int D,
                                                        const float* __restrict__ sw, SketchParams P,
                                                        float* __restrict__ Y) {
   const int i = blockIdx.x;
+  const int cb = blockIdx.y * 256 * CPT;
   const int lane = threadIdx.x & 31;
   float sh[CPT], sl[CPT];
 #pragma unroll
@@ -97,26 +99,38 @@ __global__ void __launch_bounds__(256) k_sketch_gather(const float* __restrict__
         sc = (P.zeta == 1 || (h & 1u)) ? sw[r] : -sw[r];
       }
       const int ne = (int)min(32LL, cnt - k0);
-      for (int e = 0; e < ne; ++e) {
-        const long long re = __shfl_sync(0xffffffffu, r, e);
-        const float se = __shfl_sync(0xffffffffu, sc, e);
-        const float* xr = X + re * ldx + c0;
+      // two rows per step: both rows' loads are in flight before either is added (an odd last
+      // entry pairs with a zero-scaled copy of itself)
+      for (int e = 0; e < ne; e += 2) {
+        const int e2 = min(e + 1, ne - 1);
+        const long long ra = __shfl_sync(0xffffffffu, r, e), rb = __shfl_sync(0xffffffffu, r, e2);
+        const float sa = __shfl_sync(0xffffffffu, sc, e);
+        const float sb = e + 1 < ne ? __shfl_sync(0xffffffffu, sc, e2) : 0.f;
+        const float* xa = X + ra * ldx + c0;
+        const float* xb = X + rb * ldx + c0;
+        float va[CPT], vb[CPT];
 #pragma unroll
         for (int u = 0; u < CPT; ++u) {
-          const int c = threadIdx.x + 256 * u;
-          if (c < D) {
-            float t, er;
-            two_sum(sh[u], xr[c] * se, t, er);
-            sh[u] = t;
-            sl[u] += er;
-          }
+          const int c = cb + threadIdx.x + 256 * u;
+          va[u] = c < D ? xa[c] : 0.f;
+          vb[u] = c < D ? xb[c] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < CPT; ++u) {
+          float t, er;
+          two_sum(sh[u], va[u] * sa, t, er);
+          sh[u] = t;
+          sl[u] += er;
+          two_sum(sh[u], vb[u] * sb, t, er);
+          sh[u] = t;
+          sl[u] += er;
         }
       }
     }
   }
 #pragma unroll
   for (int u = 0; u < CPT; ++u) {
-    const int c = threadIdx.x + 256 * u;
+    const int c = cb + threadIdx.x + 256 * u;
     if (c < D) Y[(size_t)i * D + c] = sh[u] + sl[u];
   }
 }
@@ -220,16 +234,9 @@ cudaError_t launch_sketch_gram(const float* X, int ldx, int c0, int D, const dou
   float* sw = static_cast<float*>(ws);
   float* Y = sw + ((M + 63) / 64 * 64);
   k_sketch_scale<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(w, M, 1.0 / P.zeta, sw);
-  const int cpt = (D + 255) / 256;
-  if (cpt <= 8) {
-    k_sketch_gather<8><<<P.s, 256, 0, st>>>(X, ldx, c0, D, sw, P, Y);
-  } else if (cpt <= 16) {
-    k_sketch_gather<16><<<P.s, 256, 0, st>>>(X, ldx, c0, D, sw, P, Y);
-  } else if (cpt <= 32) {
-    k_sketch_gather<32><<<P.s, 256, 0, st>>>(X, ldx, c0, D, sw, P, Y);
-  } else {
-    return cudaErrorInvalidValue;  // wider than 8192 columns
-  }
+  constexpr int kCPT = 8;  // columns per thread: 2048 per CTA
+  const dim3 gg((unsigned)P.s, (unsigned)((D + 256 * kCPT - 1) / (256 * kCPT)));
+  k_sketch_gather<kCPT><<<gg, 256, 0, st>>>(X, ldx, c0, D, sw, P, Y);
   const int nt = (D + kGT - 1) / kGT;
   const long long ntile = (long long)nt * (nt + 1) / 2;
   k_ds_gram<<<(unsigned)ntile, 256, 0, st>>>(Y, P.s, D, nt, G);
