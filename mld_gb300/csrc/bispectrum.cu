@@ -42,6 +42,32 @@ __device__ __forceinline__ cx<T> fetch(const cx<T>* base, int code) {
   return {sn * v.x, sn * sy * v.y};
 }
 
+// One Z term: sum_a c1_a sum_b c2_b c[i1 + a s1 + b] c[i2 - a s2 - b] with NB = nb known at compile
+// time, so that the b loop unrolls and the term's NB coefficients c2 stay in registers.
+template <int NB, typename T>
+__device__ __forceinline__ cx<T> zterm(const cx<T>* __restrict__ cc, const T* __restrict__ cgs, const ZItem& zi) {
+  T c2[NB];
+#pragma unroll
+  for (int b = 0; b < NB; ++b) c2[b] = cgs[zi.cg2 + b];
+  cx<T> zs = {T(0), T(0)};
+  int i1a = zi.i1, i2a = zi.i2;
+  for (int a = 0; a < zi.na; ++a) {
+    const T c1 = cgs[zi.cg1 + a];
+    cx<T> part = {T(0), T(0)};
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const cx<T> pr = cmul(cc[i1a + b], cc[i2a - b]);
+      part.x = fma(c2[b], pr.x, part.x);
+      part.y = fma(c2[b], pr.y, part.y);
+    }
+    zs.x = fma(c1, part.x, zs.x);
+    zs.y = fma(c1, part.y, zs.y);
+    i1a += zi.s1;
+    i2a -= zi.s2;
+  }
+  return zs;
+}
+
 template <typename T>
 struct RecEntry;
 template <>
@@ -383,23 +409,19 @@ __global__ void __launch_bounds__(kNW * 32, 2) k_bso4(KernelArgs<T> args, T* __r
         for (int r = r0; r < r1; ++r) {
           const ZItem zi = nx;
           if (r + 1 < r1) nx = tb.zitems[(size_t)(r + 1) * 32 + lane];
-          cx<T> zs = {T(0), T(0)};
-          int i1a = zi.i1, i2a = zi.i2;
-          const T* cg2 = cgs + zi.cg2;
-          for (int a = 0; a < zi.na; ++a) {
-            const T c1 = cgs[zi.cg1 + a];
-            cx<T> part = {T(0), T(0)};
-#pragma unroll 3
-            for (int b = 0; b < zi.nb; ++b) {
-              const cx<T> pr = cmul(cc[i1a + b], cc[i2a - b]);
-              const T c2 = cg2[b];
-              part.x = fma(c2, pr.x, part.x);
-              part.y = fma(c2, pr.y, part.y);
-            }
-            zs.x = fma(c1, part.x, zs.x);
-            zs.y = fma(c1, part.y, zs.y);
-            i1a += zi.s1;
-            i2a -= zi.s2;
+          cx<T> zs;
+          switch (zi.nb) {  // uniform over the round
+            case 1: zs = zterm<1, T>(cc, cgs, zi); break;
+            case 2: zs = zterm<2, T>(cc, cgs, zi); break;
+            case 3: zs = zterm<3, T>(cc, cgs, zi); break;
+            case 4: zs = zterm<4, T>(cc, cgs, zi); break;
+            case 5: zs = zterm<5, T>(cc, cgs, zi); break;
+            case 6: zs = zterm<6, T>(cc, cgs, zi); break;
+            case 7: zs = zterm<7, T>(cc, cgs, zi); break;
+            case 8: zs = zterm<8, T>(cc, cgs, zi); break;
+            case 9: zs = zterm<9, T>(cc, cgs, zi); break;
+            case 10: zs = zterm<10, T>(cc, cgs, zi); break;
+            default: zs = zterm<11, T>(cc, cgs, zi); break;
           }
           if (zi.is_a) {
             const cx<T> cv = cc[zi.ufull];
