@@ -257,7 +257,7 @@ int build_neighbours(mld_gpu_handle* h) {
   b.nbr_idx = bp_<int>(h, mld_gpu_handle::B_NBR_IDX);
   b.nbr_u = bp_<double>(h, mld_gpu_handle::B_NBR_U);
   CK(launch_neighbours(b, h->cfg.r_cut, b.nn, dmax, h->st, 1));
-  nl(h, 1);
+  nl(h, b.P > 0 ? 2 : 1);  // filling pass and pair displacements
   h->nbr_valid = true;
   return MLD_OK;
 }

@@ -28,10 +28,33 @@ __global__ void k_nbr_prep(int A, const int* __restrict__ atom_struct, const dou
                           (float)(x0 * bg[6] + x1 * bg[7] + x2 * bg[8]), 0.f);
 }
 
+// periodic image (n1, n2, n3), |n| < 128, packed in one int
+__device__ __forceinline__ int pack_image(int n1, int n2, int n3) {
+  return ((n1 + 128) << 16) | ((n2 + 128) << 8) | (n3 + 128);
+}
+// large box: u = x_j - x_i through the fractional coordinates, components with |ds| > 0.5
+// wrapped by nint (neighbours.F90:315-324), in FP64
+__device__ __forceinline__ void min_image_u(const double* __restrict__ pos, int j, double xi0, double xi1,
+                                            double xi2, const double* cl, const double* bg, double* u) {
+  const double* xj = pos + 3 * (size_t)j;
+  const double e0 = xj[0] - xi0, e1 = xj[1] - xi1, e2 = xj[2] - xi2;
+  double ds[3];
+  for (int k = 0; k < 3; ++k) {
+    double v = e0 * bg[3 * k] + e1 * bg[3 * k + 1] + e2 * bg[3 * k + 2];
+    if (v > 0.5 || v < -0.5) v -= round(v);
+    ds[k] = v;
+  }
+  u[0] = cl[0] * ds[0] + cl[3] * ds[1] + cl[6] * ds[2];
+  u[1] = cl[1] * ds[0] + cl[4] * ds[1] + cl[7] * ds[2];
+  u[2] = cl[2] * ds[0] + cl[5] * ds[1] + cl[8] * ds[2];
+}
+
 // One warp per centre atom; lanes take candidates (j, image) in order.  Candidates clearly
 // inside or outside r_cut are classified in FP32 from the prepared copies (position error of
-// order 1e-6 A against a band of 1e-3 A); only candidates within r_cut + band take the exact
-// FP64 test of the reference, so the list is the FP64 list.
+// order 1e-6 A against a band of 1e-3 A); only candidates within the band around r_cut (and the
+// zero-distance self image) take the exact FP64 test of the reference, so the list is the FP64
+// list.  GB300 issues FP64 at 1/64 of the FP32 rate: the counting pass does no FP64 work for the
+// clear cases, and the filling pass forms the FP64 displacement only for accepted neighbours.
 __global__ void __launch_bounds__(256) k_neighbours(
     int A, const int* __restrict__ atom_struct, const int* __restrict__ atom_start, const double* __restrict__ pos,
     const float4* __restrict__ pos32, const float4* __restrict__ frac32, const double* __restrict__ cell,
@@ -53,6 +76,8 @@ __global__ void __launch_bounds__(256) k_neighbours(
   const double xi0 = pos[3 * (size_t)g], xi1 = pos[3 * (size_t)g + 1], xi2 = pos[3 * (size_t)g + 2];
   const double rc2 = rcut * rcut;
   const float rcb = (float)rcut + kBand, rcb2 = rcb * rcb;
+  const float rci = (float)rcut - kBand, rci2 = rci > 0.f ? rci * rci : 0.f;
+  constexpr float kSelf2 = 1e-8f;  // FP32 squared distances below this take the exact test (self image)
   const int sm = small[s];
   int n1s = 0, n2s = 0, n3s = 0, nimg = 1;
   if (sm) {
@@ -67,8 +92,7 @@ __global__ void __launch_bounds__(256) k_neighbours(
   for (long long base = 0; base < ncand; base += 32) {
     const long long cidx = base + lane;
     bool ok = false;
-    double u0 = 0, u1 = 0, u2 = 0;
-    int jj = 0;
+    int jj = 0, img = 0;
     if (cidx < ncand) {
       if (sm) {
         jj = (int)(cidx / nimg);
@@ -81,17 +105,18 @@ __global__ void __launch_bounds__(256) k_neighbours(
         const float f0 = (pi.x - pj.x) - (c32[0] * n1 + c32[3] * n2 + c32[6] * n3);
         const float f1 = (pi.y - pj.y) - (c32[1] * n1 + c32[4] * n2 + c32[7] * n3);
         const float f2 = (pi.z - pj.z) - (c32[2] * n1 + c32[5] * n2 + c32[8] * n3);
-        if (f0 * f0 + f1 * f1 + f2 * f2 < rcb2) {
+        const float r2f = f0 * f0 + f1 * f1 + f2 * f2;
+        if (r2f < rci2 && r2f > kSelf2) {
+          ok = true;
+        } else if (r2f < rcb2) {
           const double* xj = pos + 3 * (size_t)(a0 + jj);
           const double t0 = xi0 - (xj[0] + cl[0] * n1 + cl[3] * n2 + cl[6] * n3);
           const double t1 = xi1 - (xj[1] + cl[1] * n1 + cl[4] * n2 + cl[7] * n3);
           const double t2 = xi2 - (xj[2] + cl[2] * n1 + cl[5] * n2 + cl[8] * n3);
           const double r2 = t0 * t0 + t1 * t1 + t2 * t2;
           ok = (r2 >= 1e-15) && (r2 <= rc2) && (sqrt(r2) < rcut);
-          u0 = -t0;
-          u1 = -t1;
-          u2 = -t2;
         }
+        img = pack_image(n1, n2, n3);
       } else {
         jj = (int)cidx;
         if (a0 + jj != g) {
@@ -105,30 +130,25 @@ __global__ void __launch_bounds__(256) k_neighbours(
           const float g2 = c32[2] * d0 + c32[5] * d1 + c32[8] * d2;
           // the FP32 image can differ from the reference's only when a component sits at +-0.5,
           // i.e. at half a cell width (> r_cut for a large box), so its distance is a lower bound
-          if (g0 * g0 + g1 * g1 + g2 * g2 < rcb2) {
-            const double* xj = pos + 3 * (size_t)(a0 + jj);
-            const double e0 = xj[0] - xi0, e1 = xj[1] - xi1, e2 = xj[2] - xi2;
-            double ds[3];
-            for (int k = 0; k < 3; ++k) {
-              double v = e0 * bg[3 * k] + e1 * bg[3 * k + 1] + e2 * bg[3 * k + 2];
-              if (v > 0.5 || v < -0.5) v -= round(v);
-              ds[k] = v;
-            }
-            u0 = cl[0] * ds[0] + cl[3] * ds[1] + cl[6] * ds[2];
-            u1 = cl[1] * ds[0] + cl[4] * ds[1] + cl[7] * ds[2];
-            u2 = cl[2] * ds[0] + cl[5] * ds[1] + cl[8] * ds[2];
-            ok = sqrt(u0 * u0 + u1 * u1 + u2 * u2) < rcut;
+          const float r2f = g0 * g0 + g1 * g1 + g2 * g2;
+          // clearly inside: the FP32 image is the reference's (no component near +-0.5)
+          if (r2f < rci2) {
+            ok = true;
+          } else if (r2f < rcb2) {
+            double u[3];
+            min_image_u(pos, a0 + jj, xi0, xi1, xi2, cl, bg, u);
+            ok = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) < rcut;
           }
         }
       }
     }
     const unsigned m = __ballot_sync(0xffffffffu, ok);
     if (pass == 1 && ok) {
+      // the pair and its image; k_nbr_u forms the FP64 displacement, one thread per pair
       const int slot = wbase + count + __popc(m & ((1u << lane) - 1u));
       nbr_idx[slot] = a0 + jj;
-      nbr_u[3 * (size_t)slot] = u0;
-      nbr_u[3 * (size_t)slot + 1] = u1;
-      nbr_u[3 * (size_t)slot + 2] = u2;
+      nbr_u[3 * (size_t)slot] = (double)g;
+      nbr_u[3 * (size_t)slot + 1] = (double)img;
     }
     count += __popc(m);
   }
@@ -136,6 +156,32 @@ __global__ void __launch_bounds__(256) k_neighbours(
     counts[g] = count;
     atomicMax(maxcount, count);
   }
+}
+
+// FP64 displacement u = x_j + image - x_i of every pair (the reference's arithmetic), from the
+// centre and image recorded by the filling pass; one thread per pair.
+__global__ void k_nbr_u(long long P, const int* __restrict__ atom_struct, const double* __restrict__ pos,
+                        const double* __restrict__ cell, const double* __restrict__ recip,
+                        const int* __restrict__ small, const int* __restrict__ nbr_idx, double* __restrict__ nbr_u) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const int i = (int)nbr_u[3 * p], img = (int)nbr_u[3 * p + 1], j = nbr_idx[p];
+  const int s = atom_struct[i];
+  const double* cl = cell + 9 * (size_t)s;
+  const double xi0 = pos[3 * (size_t)i], xi1 = pos[3 * (size_t)i + 1], xi2 = pos[3 * (size_t)i + 2];
+  double u[3];
+  if (small[s]) {
+    const int n1 = ((img >> 16) & 255) - 128, n2 = ((img >> 8) & 255) - 128, n3 = (img & 255) - 128;
+    const double* xj = pos + 3 * (size_t)j;
+    u[0] = -(xi0 - (xj[0] + cl[0] * n1 + cl[3] * n2 + cl[6] * n3));
+    u[1] = -(xi1 - (xj[1] + cl[1] * n1 + cl[4] * n2 + cl[7] * n3));
+    u[2] = -(xi2 - (xj[2] + cl[2] * n1 + cl[5] * n2 + cl[8] * n3));
+  } else {
+    min_image_u(pos, j, xi0, xi1, xi2, cl, recip + 9 * (size_t)s, u);
+  }
+  nbr_u[3 * p] = u[0];
+  nbr_u[3 * p + 1] = u[1];
+  nbr_u[3 * p + 2] = u[2];
 }
 
 // Three-phase exclusive scan of n ints: out[0..n], out[n] = total.
@@ -208,6 +254,9 @@ cudaError_t launch_neighbours(const DevBatch& b, double rcut, int* counts, int* 
   k_neighbours<<<blocks, threads, 0, st>>>(b.A, b.atom_struct, b.atom_start, b.pos, b.pos32, b.frac32, b.cell,
                                            b.recip, b.small, b.nsize, rcut, pass, counts, maxcount, b.nbr_off,
                                            b.nbr_idx, b.nbr_u);
+  if (pass == 1 && b.P > 0)
+    k_nbr_u<<<(unsigned)((b.P + 255) / 256), 256, 0, st>>>(b.P, b.atom_struct, b.pos, b.cell, b.recip, b.small,
+                                                           b.nbr_idx, b.nbr_u);
   return cudaGetLastError();
 }
 
