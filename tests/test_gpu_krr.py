@@ -168,3 +168,43 @@ def test_kernel_force_rows_mixed_vs_plain(lib, j_max, r_cut, channels, system):
     ef, ea = _rel(kb1[fmask], kb0[fmask]), _rel(kb1, kb0)
     assert ef < 5e-5, (ef, ea)
     assert ea < 2e-4, (ef, ea)
+
+
+@pytest.mark.parametrize("n_struct", [48, 12])
+def test_kernel_fit_sketched_preconditioner(lib, n_struct):
+    """A kernel block of D = 783 columns (768 reference points) takes the sketched preconditioner
+    of the mixed method: a sparse sign sketch when the design rows exceed 3 D (48 structures),
+    the weighted rows themselves otherwise (12 structures).  The mixed fit solves the same
+    normal equations as the FP64 fit, so their training RMSEs and predictions agree."""
+    from mld_gb300 import _lib, synth
+    ds = synth.fe_bcc_batched(n_struct=n_struct, nmin=16, nmax=40, seed=23)
+    nat, pos, cell, types = ds.arrays()
+    E, F, S, has = ds.labels()
+    c0 = _lib.default_config()
+    c0.j_max, c0.r_cut, c0.precision, c0.ml_type = 2.0, 4.7, 0, 0
+    with _lib.Handle(c0) as h:
+        h.set_structures(nat, pos, cell, types)
+        B, _ = h.descriptors()
+    idx = np.random.default_rng(5).choice(B.shape[0], size=768, replace=B.shape[0] < 768)
+    Zraw = B[idx] + np.random.default_rng(6).normal(scale=1e-6, size=(768, B.shape[1]))
+    out = {}
+    for precision in (0, 1):
+        c = _lib.default_config()
+        c.j_max, c.r_cut, c.precision, c.ml_type, c.lambda_krr = 2.0, 4.7, precision, 1, 1e-6
+        with _lib.Handle(c) as h:
+            h.set_structures(nat, pos, cell, types)
+            h.set_labels(E, F, S, has, np.ones((len(nat), 3)))
+            h.set_kernel_points(Zraw)
+            assert h.dim_design_line == 1 + 14 + 768
+            rows = h.num_rows()
+            w, rmse = h.fit()
+            Ep, Fp, Sp = h.predict(w)
+            info = h.solve_info()
+        out[precision] = (rmse, Ep, Fp, info, rows)
+    (r0, E0, F0, _, rows), (r1, E1, F1, info1, _) = out[0], out[1]
+    assert (rows > 3 * 783) == (n_struct == 48)
+    # converged CG (not the iteration cap), RMSE within 1 % of FP64
+    assert info1["pcg_iterations"][0] < 150, info1
+    assert abs(r1[1] - r0[1]) <= 0.01 * r0[1], (r0, r1)
+    assert abs(r1[0] - r0[0]) <= 0.01 * max(r0[0], 1e-3), (r0, r1)
+    assert _rel(F1, F0) < 2e-2
