@@ -38,7 +38,7 @@ LAMBDA = 1e-8
 # DRAM bytes (read + write) of one k_bso4<float> launch per atom: 78.05 MB over 45,702 atoms in
 # the ncu capture of the 200-structure Fe case (profiles/k_bso4_f32_fe200.md); the traffic is
 # per-atom neighbour data and rows, so it is scaled by the atoms of the launch
-BSO4_DRAM_BYTES_PER_ATOM = 78.05e6 / 45702
+BSO4_DRAM_BYTES_PER_ATOM = 78.29e6 / 45702
 
 
 def _args():
