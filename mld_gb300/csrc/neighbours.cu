@@ -95,8 +95,16 @@ __global__ void __launch_bounds__(256) k_neighbours(
     int jj = 0, img = 0;
     if (cidx < ncand) {
       if (sm) {
-        jj = (int)(cidx / nimg);
-        int im = (int)(cidx - (long long)jj * nimg);
+        // 32-bit division when the candidate count fits (the 64-bit one is emulated)
+        int im;
+        if (ncand < 0x7fffffffLL) {
+          const int ci = (int)cidx;
+          jj = ci / nimg;
+          im = ci - jj * nimg;
+        } else {
+          jj = (int)(cidx / nimg);
+          im = (int)(cidx - (long long)jj * nimg);
+        }
         const int n3 = im % (2 * n3s + 1) - n3s;
         im /= (2 * n3s + 1);
         const int n2 = im % (2 * n2s + 1) - n2s;
