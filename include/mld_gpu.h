@@ -46,7 +46,13 @@ extern "C" {
 #define MLD_ERR_TIMEOUT 9        /* a bounded device-side wait expired (kernel returned early) */
 
 #define MLD_PRECISION_PLAIN_FP64 0  /* all-FP64 on the GPU */
-#define MLD_PRECISION_MIXED 1       /* FP32 descriptors/rows, FP64 Gram accumulation and solve */
+#define MLD_PRECISION_MIXED 1       /* FP32 descriptors and rows; normal matrix on the tensor cores in
+                                       BF16 split precision (hi*hi + hi*lo + lo*hi, FP32 accumulation,
+                                       FP64 across row blocks) or, for blocks of 768 columns or more, a
+                                       sparse-sign sketch in double-FP32; FP64 Cholesky of the
+                                       preconditioner; conjugate gradients with double-FP32 matvecs over
+                                       the FP32 rows, so the coefficients solve the FP32 rows' normal
+                                       equations */
 
 #define MLD_MAX_ELEMENTS 8
 
@@ -199,6 +205,14 @@ int mld_gpu_set_kernel_points(mld_gpu_handle* h, int nk, const double* z_raw);
 int mld_gpu_solve_info(const mld_gpu_handle* h, int* pcg_iterations /*[2]*/, double* pcg_residual /*[2]*/,
                        double* precond_shift /*[2]*/, int* chol_retries);
 
+/* Test hook of the device-side timeout path (no reference counterpart).  skip_loads = 1 makes
+ * the producer warp of the tensor-core Gram (the mixed method's narrow-block normal matrix and
+ * mld_gpu_gram_rows) issue no loads, so its consumers' bounded waits expire after
+ * wait_limit_clocks SM clocks (0 = the default of about one second); the kernel then reports the
+ * expiry, frees its tensor memory and returns, and the call fails with MLD_ERR_TIMEOUT while the
+ * handle stays usable.  (0, 0) restores normal operation.  Process-wide; not for production use. */
+int mld_gpu_test_pipeline_timeout(int skip_loads, long long wait_limit_clocks);
+
 /* ---------------------------------------------------------------------------------------
  * Serving loop (evaluation with a fitted potential under continuous batching; the evaluation
  * side of mld.F90:1579-1867 as driven by mld_md_driver.F90:324-375,579-651).
@@ -225,6 +239,12 @@ int mld_gpu_server_result(mld_gpu_server* s, long long ticket, double* E, double
 int mld_gpu_server_wait(mld_gpu_server* s, long long ticket, double* E, double* F, double* S, double* latency_ms,
                         double timeout_ms);
 int mld_gpu_server_stats(const mld_gpu_server* s, long long* batches, long long* atoms_done, double* budget_bytes);
+/* Admission record: the largest sum of estimated device bytes of the batches on the GPU at one
+ * time (never above budget_bytes), the per-slot share of the budget, and the largest estimated
+ * bytes of one batch.  A request above the share waits until every slot is idle and then runs
+ * alone.  (No reference counterpart: the reference evaluates one structure per MD step.) */
+int mld_gpu_server_admission(const mld_gpu_server* s, double* peak_bytes_in_flight, double* share_bytes,
+                             double* largest_batch_bytes);
 
 /* Weighted Gram matrix and right-hand side of caller-owned DEVICE rows, the per-block
  * accumulation of the online fit (gram%accumulate, module_online_fit.F90:49-53,138-265):
@@ -256,11 +276,13 @@ int mld_gpu_gram_rows(int method, const void* X, int x_is_fp32, long long M, int
  * Limits: nat <= MLD_NOALLOC_MAX_ATOMS and at most MLD_NOALLOC_MAX_PAIRS neighbour pairs
  * (fewer when many channels need FP32 staging).  Larger inputs return MLD_ERR_NOALLOC_LIMIT.
  * The first call on a device resolves the array's address (cudaGetSymbolAddress) and uploads
- * the tables; make that first call before any stream capture.  Every call shares the array
- * and it keeps the last call's contents.  Counters that must start at zero are cleared on
- * every call.  Calls that overlap on the GPU (two streams, or two host threads on one device)
- * race on the array: serialise them.  The call synchronises once on `stream` to read the pair
- * count; B is complete when `stream` is next synchronised. */
+ * the tables; make that first call before any stream capture.  A call whose j_max differs from
+ * the previous call's on that device re-uploads the tables, and first waits for the whole device
+ * (cudaDeviceSynchronize), because the previous call may have run on another stream.  Every call
+ * shares the array and it keeps the last call's contents.  Counters that must start at zero are
+ * cleared on every call.  Calls that overlap on the GPU (two streams, or two host threads on one
+ * device) race on the array: serialise them.  The call synchronises once on `stream` to read the
+ * pair count; B is complete when `stream` is next synchronised. */
 #define MLD_NOALLOC_SCRATCH_MIB 48
 #define MLD_NOALLOC_MAX_ATOMS 16384
 #define MLD_NOALLOC_MAX_PAIRS 1048576

@@ -30,7 +30,8 @@ EXPORTED = ["mld_gpu_config_defaults", "mld_gpu_create", "mld_gpu_destroy", "mld
             "mld_gpu_peak_flops", "mld_gpu_descriptors_noalloc", "mld_gpu_solve_info", "mld_gpu_gram_rows",
             "mld_gpu_set_kernel_points", "mld_gpu_server_create", "mld_gpu_server_destroy",
             "mld_gpu_server_last_error", "mld_gpu_server_submit", "mld_gpu_server_progress",
-            "mld_gpu_server_result", "mld_gpu_server_wait", "mld_gpu_server_stats"]
+            "mld_gpu_server_result", "mld_gpu_server_wait", "mld_gpu_server_stats", "mld_gpu_server_admission",
+            "mld_gpu_test_pipeline_timeout"]
 NPHASE = 6
 PHASES = ["neighbours", "rows", "descriptors", "gram", "solve", "predict"]
 
@@ -379,6 +380,12 @@ class Server:
         b, a, bud = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_double()
         self._check(self._L.mld_gpu_server_stats(self._s, ctypes.byref(b), ctypes.byref(a), ctypes.byref(bud)))
         return {"batches": b.value, "atoms_done": a.value, "budget_bytes": bud.value}
+
+    def admission(self):
+        """Admission record: peak estimated bytes on the GPU, per-slot share, largest batch."""
+        pk, sh, lg = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._check(self._L.mld_gpu_server_admission(self._s, ctypes.byref(pk), ctypes.byref(sh), ctypes.byref(lg)))
+        return {"peak_bytes_in_flight": pk.value, "share_bytes": sh.value, "largest_batch_bytes": lg.value}
 
     def close(self):
         if self._s:

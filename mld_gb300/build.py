@@ -11,7 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libmld_gpu.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["api.cu", "bispectrum.cu", "neighbours.cu", "fit.cu", "quad.cu", "solve.cu", "gram_tc.cu", "kernel_rows.cu", "serve.cu", "noalloc.cu", "precond32.cu", "eval.cu", "krr_tc.cu", "sketch.cu",
+SOURCES = ["api.cu", "bispectrum.cu", "neighbours.cu", "fit.cu", "quad.cu", "solve.cu", "gram_tc.cu", "kernel_rows.cu", "serve.cu", "noalloc.cu", "precond32.cu", "eval.cu", "krr_tc.cu", "sketch.cu", "rows.cu",
            "bso4_tables.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",

@@ -89,6 +89,7 @@ struct mld_gpu_handle {
   bool ew_ready = false;
   double pcg_rel[2] = {0, 0};
   int chol_retries = 0;
+  int last_rank = 0;  // rank of the last symmetric solve (eigenvalues kept by the rcond cut)
 
   std::vector<void*> owned;  // table allocations
   Buf bufs[64];
@@ -100,7 +101,7 @@ struct mld_gpu_handle {
     B_G, B_H, B_W, B_EVALS, B_INFO, B_SQ, B_PRED, B_BOUT, B_DBOUT,
     B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
     B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV, B_KZD, B_KZF, B_KWS, B_WSERVE, B_P32,
-    B_EW, B_EBETA, B_EB, B_EOUT, B_KTC, B_SKW,
+    B_EW, B_EBETA, B_EB, B_EOUT, B_KTC, B_SKW, B_ORDER, B_QCNT, B_SP, B_EPAIR, B_EATOM, B_GP,
     B_COUNT
   };
   static_assert(B_COUNT <= 64, "buffer table too small");
@@ -258,9 +259,17 @@ int build_neighbours(mld_gpu_handle* h) {
   b.nbr_u = bp_<double>(h, mld_gpu_handle::B_NBR_U);
   CK(launch_neighbours(b, h->cfg.r_cut, b.nn, dmax, h->st, 1));
   nl(h, b.P > 0 ? 2 : 1);  // filling pass and pair displacements
+  // longest-first order of the descriptor kernel's work queue; one counter int + sort workspace
+  CK(ensure(h, mld_gpu_handle::B_ORDER, sizeof(int) * std::max(1, h->A)));
+  CK(ensure(h, mld_gpu_handle::B_QCNT, sizeof(int) * (4 + atom_order_tmp_ints(h->max_nn))));
+  CK(launch_atom_order(b.nn, h->A, h->max_nn, bp_<int>(h, mld_gpu_handle::B_ORDER),
+                       bp_<int>(h, mld_gpu_handle::B_QCNT) + 4, h->st));
+  nl(h, 3);
   h->nbr_valid = true;
   return MLD_OK;
 }
+
+
 
 // workspace of the tensor-core kernel-row product (derivative-vector planes of one atom chunk)
 constexpr size_t kKrrTcWorkspaceCap = size_t(6) << 30;
@@ -274,6 +283,25 @@ int y_scratch(mld_gpu_handle* h, void** p, size_t* bytes) {
     CK(ensure(h, mld_gpu_handle::B_YSCR, *bytes));
     *p = bp_<void>(h, mld_gpu_handle::B_YSCR);
   }
+  return MLD_OK;
+}
+
+// B and w_ch * dB of the staged batch into B_BOUT / B_DBOUT (dB optional) through the
+// descriptor kernel's queue
+template <typename T>
+int run_descriptors(mld_gpu_handle* h, bool want_dB, const DevEval<T>* ev, T* Bout) {
+  void* ys = nullptr;
+  size_t ysb = 0;
+  int rcy = y_scratch<T>(h, &ys, &ysb);
+  if (rcy) return rcy;
+  T* dB = nullptr;
+  if (want_dB) {
+    CK(ensure(h, mld_gpu_handle::B_DBOUT, sizeof(T) * std::max<size_t>((size_t)h->b.P * 3 * h->KK, 1)));
+    dB = bp_<T>(h, mld_gpu_handle::B_DBOUT);
+  }
+  CK(launch_bso4<T>(h->dt, h->b, h->bp, Bout, dB, ev, bp_<int>(h, mld_gpu_handle::B_ORDER),
+                    bp_<int>(h, mld_gpu_handle::B_QCNT), h->st, ys, ysb));
+  nl(h, 1);
   return MLD_OK;
 }
 
@@ -321,33 +349,27 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
   nl(h, 1);
   mark(h, MLD_PHASE_ROWS, 1);
   mark(h, MLD_PHASE_DESCRIPTORS, 0);
-  if (!h->quad && !h->krr) {
-    void* ys = nullptr;
-    size_t ysb = 0;
-    int rcy = y_scratch<T>(h, &ys, &ysb);
-    if (rcy) return rcy;
-    CK(launch_bso4_rows<T>(h->dt, h->b, rows, h->bp, X, (T*)nullptr, (T*)nullptr, 1, h->st, ys, ysb));
-    nl(h, 1);
-  } else {
-    // quadratic rows need every atom's B and every pair's dB (mld_forces.F90:410-500)
-    const size_t nB = (size_t)std::max(1, h->A) * h->KK, nd = (size_t)std::max<long long>(1, h->b.P) * 3 * h->KK;
+  {
+    // B of every atom and w_ch * dB of every pair, then the rows gathered through the reverse
+    // pairs in a fixed order (rows.cu); the quadratic and kernel columns use the same B and dB
+    const size_t nB = (size_t)std::max(1, h->A) * h->KK;
     CK(ensure(h, mld_gpu_handle::B_BOUT, sizeof(T) * nB));
-    CK(ensure(h, mld_gpu_handle::B_DBOUT, sizeof(T) * nd));
     CK(ensure(h, mld_gpu_handle::B_REV, sizeof(int) * (size_t)std::max<long long>(1, h->b.P)));
+    CK(ensure(h, mld_gpu_handle::B_SP, sizeof(T) * nB * 6));
     if (h->quad) CK(ensure(h, mld_gpu_handle::B_HQ, sizeof(T) * (size_t)std::max(1, h->A) * 6 * h->KK));
     T* Bq = bp_<T>(h, mld_gpu_handle::B_BOUT);
+    int rcd = run_descriptors<T>(h, true, nullptr, Bq);
+    if (rcd) return rcd;
     T* dBq = bp_<T>(h, mld_gpu_handle::B_DBOUT);
-    void* ys = nullptr;
-    size_t ysb = 0;
-    int rcy = y_scratch<T>(h, &ys, &ysb);
-    if (rcy) return rcy;
-    CK(launch_bso4_rows<T>(h->dt, h->b, rows, h->bp, X, Bq, dBq, 1, h->st, ys, ysb));
     CK(launch_reverse_pairs(h->b, bp_<int>(h, mld_gpu_handle::B_REV), h->st));
+    CK(launch_lin_rows<T>(h->b, rows, h->bp, h->KK, bp_<int>(h, mld_gpu_handle::B_REV), Bq, dBq,
+                          bp_<T>(h, mld_gpu_handle::B_SP), X, h->st));
+    nl(h, 3);
     if (h->quad) {
       CK(launch_quad_rows<T>(h->b, rows, h->bp, h->KK, bp_<int>(h, mld_gpu_handle::B_REV), Bq, dBq,
                              bp_<T>(h, mld_gpu_handle::B_HQ), X, h->DL, h->st));
-      nl(h, 4);
-    } else {
+      nl(h, 2);
+    } else if (h->krr) {
       // kernel columns (compute_kernel.F90, mld_energy/forces/stress kernel packing)
       const size_t wse = krr_workspace_elems(h->A, h->nk, h->KK);
       CK(ensure(h, mld_gpu_handle::B_KWS, sizeof(T) * wse));
@@ -372,7 +394,7 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
                             h->cfg.kernel_power, h->cfg.length_kernel, h->cfg.sigma_kernel, h->cfg.sign_stress,
                             h->cfg.sign_stress_big_box, bp_<T>(h, mld_gpu_handle::B_KWS), X, h->DL, h->st, &nkl, tcws,
                             tcb, terr, h->nsm));
-      nl(h, 2 + nkl);
+      nl(h, nkl);
       if (terr) {
         int herr = 0;
         CK(cudaMemcpyAsync(&herr, terr, sizeof(int), cudaMemcpyDeviceToHost, h->st));
@@ -386,16 +408,22 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
   return MLD_OK;
 }
 
-// Symmetric solve of (G + lambda I) w = rhs: min-norm Jacobi (gelsd semantics) up to
-// kJacobiMax, blocked Cholesky with two FP64 refinement steps above (diagonal shift
-// lambda, or a 1e-12 relative jitter when lambda <= 0).  G is left intact.
-int solve_any(mld_gpu_handle* h, double* G, const double* rhs, int D, double* w) {
-  if (D <= 112) {
-    CK(launch_solve_sym(G, rhs, D, h->lam_eff, h->cfg.svd_rcond, w, bp_<double>(h, mld_gpu_handle::B_EVALS),
-                        bp_<int>(h, mld_gpu_handle::B_INFO), h->st));
-    nl(h, 1);
-    return MLD_OK;
-  }
+// workspace of the fixed-order Gram / rhs reductions over M rows of D columns
+double* gram_ws(mld_gpu_handle* h, long long M, int D) {
+  if (ensure(h, mld_gpu_handle::B_GP, sizeof(double) * gram_workspace_doubles(M, D)) != cudaSuccess) return nullptr;
+  return bp_<double>(h, mld_gpu_handle::B_GP);
+}
+
+// Symmetric solve of (G + lambda I) w = rhs with the reference's dgelsd semantics
+// (stats_tools.F90:1153-1213: minimum-norm solution, singular values below rcond * s_max cut).
+//  * D <= 112: one-CTA Jacobi eigen-solve.  When it cuts no eigenvalue (full rank), the same
+//    solution is recomputed from the Cholesky factor with two FP64 refinement steps, which is
+//    more accurate than the eigen-solve on an ill-conditioned matrix; a cut keeps the
+//    minimum-norm eigen-solution.
+//  * above: blocked Cholesky with two refinement steps (diagonal shift lambda, or a 1e-12
+//    relative jitter when lambda <= 0 or the factorisation fails).
+// G is left intact.
+int chol_refined(mld_gpu_handle* h, const double* G, const double* rhs, int D, double shift, double* w, int* hinfo) {
   CK(ensure(h, mld_gpu_handle::B_GF, sizeof(double) * (size_t)D * D));
   CK(ensure(h, mld_gpu_handle::B_RES, sizeof(double) * D));
   CK(ensure(h, mld_gpu_handle::B_DW, sizeof(double) * 3 * (size_t)D));
@@ -404,6 +432,38 @@ int solve_any(mld_gpu_handle* h, double* G, const double* rhs, int D, double* w)
   double* r = bp_<double>(h, mld_gpu_handle::B_RES);
   double* dw = bp_<double>(h, mld_gpu_handle::B_DW);
   double* tmp = dw + D;
+  int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
+  CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)D * D, cudaMemcpyDeviceToDevice, h->st));
+  CK(launch_cholesky(Lf, D, shift, info, h->st));
+  CK(cudaMemcpyAsync(hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  nl(h, cholesky_launches(D));
+  if (*hinfo != 0) return MLD_OK;
+  CK(launch_chol_solve_blocked(Lf, D, rhs, w, tmp, h->st));
+  for (int it = 0; it < 2; ++it) {
+    CK(launch_residual(G, D, shift, w, rhs, r, h->st));
+    CK(launch_chol_solve_blocked(Lf, D, r, dw, tmp, h->st));
+    CK(launch_axpy(D, 1.0, dw, w, h->st));
+  }
+  nl(h, 3 * chol_solve_launches(D) + 4);
+  return MLD_OK;
+}
+
+int solve_any(mld_gpu_handle* h, double* G, const double* rhs, int D, double* w) {
+  if (D <= 112) {
+    CK(ensure(h, mld_gpu_handle::B_INFO, sizeof(int) * 4));
+    int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
+    CK(launch_solve_sym(G, rhs, D, h->lam_eff, h->cfg.svd_rcond, w, bp_<double>(h, mld_gpu_handle::B_EVALS), info,
+                        h->st));
+    nl(h, 1);
+    int hv[2] = {0, 0};
+    CK(cudaMemcpyAsync(hv, info, sizeof(int) * 2, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->last_rank = hv[1];
+    if (hv[1] < D) return MLD_OK;  // eigenvalues cut: the minimum-norm solution stands
+    int hinfo = 0;
+    return chol_refined(h, G, rhs, D, h->lam_eff > 0 ? h->lam_eff : 0.0, w, &hinfo);  // on failure w is kept
+  }
   // diagonal shift: lambda, but at least 1e-12 of the largest diagonal entry (a rank-deficient
   // normal matrix: the min-norm solution of dgelsd differs only in the near-null space); x10 on
   // a failed factorisation
@@ -414,24 +474,13 @@ int solve_any(mld_gpu_handle* h, double* G, const double* rhs, int D, double* w)
   double mx = 0;
   for (double v : diag) mx = std::max(mx, std::fabs(v));
   double jitter = 1e-12 * (mx > 0 ? mx : 1.0);
-  int* info = bp_<int>(h, mld_gpu_handle::B_INFO);
   int hinfo = 0;
+  h->last_rank = D;
   for (int attempt = 0; attempt < 5; ++attempt, jitter *= 10.0) {
     const double shift = std::max(h->lam_eff > 0 ? h->lam_eff : 0.0, jitter);
-    CK(cudaMemcpyAsync(Lf, G, sizeof(double) * (size_t)D * D, cudaMemcpyDeviceToDevice, h->st));
-    CK(launch_cholesky(Lf, D, shift, info, h->st));
-    CK(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
-    CK(cudaStreamSynchronize(h->st));
-    nl(h, cholesky_launches(D));
-    if (hinfo != 0) continue;
-    CK(launch_chol_solve_blocked(Lf, D, rhs, w, tmp, h->st));
-    for (int it = 0; it < 2; ++it) {
-      CK(launch_residual(G, D, shift, w, rhs, r, h->st));
-      CK(launch_chol_solve_blocked(Lf, D, r, dw, tmp, h->st));
-      CK(launch_axpy(D, 1.0, dw, w, h->st));
-    }
-    nl(h, 3 * chol_solve_launches(D) + 4);
-    break;
+    int rc = chol_refined(h, G, rhs, D, shift, w, &hinfo);
+    if (rc) return rc;
+    if (hinfo == 0) break;
   }
   if (hinfo != 0)
     return fail(h, MLD_ERR_SOLVE, "normal matrix not positive definite at column " + std::to_string(hinfo));
@@ -503,8 +552,10 @@ int fit_block_plain(mld_gpu_handle* h, const double* X, int c0, int Db, const do
   double* G = bp_<double>(h, mld_gpu_handle::B_G);
   double* hv = bp_<double>(h, mld_gpu_handle::B_H);
   mark(h, MLD_PHASE_GRAM, 0);
-  CK(launch_gram<double>(X + c0, h->ldx, bp_<double>(h, mld_gpu_handle::B_WROW), y, M, Db, G, hv, h->st));
-  nl(h, 3);
+  double* gws = gram_ws(h, M, Db);
+  if (!gws) return fail(h, MLD_ERR_OOM, "Gram workspace");
+  CK(launch_gram<double>(X + c0, h->ldx, bp_<double>(h, mld_gpu_handle::B_WROW), y, M, Db, G, hv, h->st, gws));
+  nl(h, 5);  // tiles, tile reduction, rhs partials, rhs reduction, symmetrise
   mark(h, MLD_PHASE_GRAM, 1);
   mark(h, MLD_PHASE_SOLVE, 0);
   int rc = solve_any(h, G, hv, Db, w);
@@ -549,8 +600,10 @@ int fit_block_sketch(mld_gpu_handle* h, const float* X, int c0, int Db, const do
   mark(h, MLD_PHASE_GRAM, 0);
   CK(ensure(h, mld_gpu_handle::B_TERR, sizeof(int)));
   CK(ensure(h, mld_gpu_handle::B_PRED, sizeof(double) * (size_t)std::max<long long>(M, 1)));
-  CK(launch_rhs<float>(X + c0, h->ldx, wrow, y, M, Db, hv, h->nsm, h->st, bp_<float2>(h, mld_gpu_handle::B_PRED)));
-  nl(h, 2);
+  double* rws = gram_ws(h, M, Db);
+  if (!rws) return fail(h, MLD_ERR_OOM, "rhs workspace");
+  CK(launch_rhs<float>(X + c0, h->ldx, wrow, y, M, Db, hv, h->nsm, h->st, bp_<float2>(h, mld_gpu_handle::B_PRED), rws));
+  nl(h, 3);
   if (M >= (1LL << 31)) return fail(h, MLD_ERR_INVALID, "sketch: more than 2^31 design rows");
   const SketchParams P = sketch_params(M, Db, kSketchSeed + (uint64_t)stage);
   CK(ensure(h, mld_gpu_handle::B_SKW, sketch_workspace_bytes(M, Db)));
@@ -621,9 +674,11 @@ int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const dou
   nl(h, 2 * ((M + chunk - 1) / chunk));
   CK(launch_symmetrize(G, Db, h->st));
   CK(ensure(h, mld_gpu_handle::B_PRED, sizeof(double) * (size_t)std::max<long long>(M, 1)));
-  CK(launch_rhs<float>(X + c0, h->ldx, wrow, y, M, Db, hv, h->nsm, h->st,
-                       bp_<float2>(h, mld_gpu_handle::B_PRED)));
-  nl(h, 2);
+  double* rws = gram_ws(h, M, Db);
+  if (!rws) return fail(h, MLD_ERR_OOM, "rhs workspace");
+  CK(launch_rhs<float>(X + c0, h->ldx, wrow, y, M, Db, hv, h->nsm, h->st, bp_<float2>(h, mld_gpu_handle::B_PRED),
+                       rws));
+  nl(h, 3);
   mark(h, MLD_PHASE_GRAM, 1);
   int herr = 0;
   CK(cudaMemcpyAsync(&herr, terr, sizeof(int), cudaMemcpyDeviceToHost, h->st));
@@ -778,7 +833,7 @@ int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
   CK(ensure(h, mld_gpu_handle::B_W, sizeof(double) * D));
   CK(ensure(h, mld_gpu_handle::B_EVALS, sizeof(double) * gdim));
   CK(ensure(h, mld_gpu_handle::B_INFO, sizeof(int) * 4));
-  CK(ensure(h, mld_gpu_handle::B_SQ, sizeof(double) * 6));
+  CK(ensure(h, mld_gpu_handle::B_SQ, sizeof(double) * predict_sq_doubles()));
   double* w = bp_<double>(h, mld_gpu_handle::B_W);
   double* y = bp_<double>(h, mld_gpu_handle::B_Y);
   // linear block (QNML stage 1, or the whole linear model): parameters.F90:1018-1099; the
@@ -806,7 +861,7 @@ int fit_impl(mld_gpu_handle* h, double* w_params, double* rmse) {
   CK(cudaMemsetAsync(sq, 0, sizeof(double) * 6, h->st));
   CK(launch_predict_sq<T>(X, h->ldx, w, M, D, nullptr, bp_<double>(h, mld_gpu_handle::B_Y), bp_<int>(h, mld_gpu_handle::B_KIND),
                           sq, h->st));
-  nl(h, 1);
+  nl(h, 2);
   mark(h, MLD_PHASE_PREDICT, 1);
   double hsq[6];
   std::vector<double> wd(D);
@@ -905,52 +960,7 @@ int mld_gpu_create(const mld_gpu_config* cfg, mld_gpu_handle** out) {
   h->Dfull = h->DL + (h->quad ? h->KK * h->KK : 0);           // reference layout (dim_design_line)
   h->ldx = round_up4(h->D);
   // device tables
-  DevTables& d = h->dt;
-  d.J = t.J;
-  d.NU = t.NU;
-  d.HU = t.HU;
-  d.K = t.K;
-  d.NS = (int)t.yslots.size();
-  d.NYP = t.NYP;
-  d.NTILE = (int)t.tiles.size();
-  d.NCG = (int)t.cg.size();
-  for (int j = 0; j <= t.J + 1; ++j) {
-    d.hoff[j] = t.hoff[j];
-    d.rowk_off[j] = t.rowk_off[j];
-  }
-  for (int j = 0; j <= t.J; ++j) {
-    d.Mp[j] = t.Mp[j];
-    d.yoff[j] = t.yoff[j];
-  }
-  std::vector<float> cg32(t.cg.begin(), t.cg.end());
-  std::vector<float> tz32(t.rec_tz.begin(), t.rec_tz.end()), tx32(t.rec_tx.begin(), t.rec_tx.end());
-  e = cudaSuccess;
-#define UP(dst, vec) \
-  if (e == cudaSuccess) e = dev_alloc_copy(h, &dst, vec.data(), vec.size())
-  UP(d.zterms, t.zterms);
-  UP(d.yslots, t.yslots);
-  UP(d.yorder, t.yorder);
-  UP(d.rowk, t.rowk);
-  UP(d.tiles, t.tiles);
-  UP(d.cg64, t.cg);
-  UP(d.cg32, cg32);
-  UP(d.rec_tz64, t.rec_tz);
-  UP(d.rec_tx64, t.rec_tx);
-  UP(d.rec_tz32, tz32);
-  UP(d.rec_tx32, tx32);
-  UP(d.rec_sz, t.rec_sz);
-  UP(d.rec_sx, t.rec_sx);
-  UP(d.rec_qneg, t.rec_qneg);
-  UP(d.expand, t.expand);
-  UP(d.half_diag, t.half_diag);
-  std::vector<RecEntry32> r32;
-  std::vector<RecEntry64> r64;
-  pack_recursion(t, &r32, &r64);
-  UP(d.rec32, r32);
-  UP(d.rec64, r64);
-  UP(d.zitems, t.zitems);
-  UP(d.zitem_off, t.zitem_off);
-#undef UP
+  e = fill_dev_tables(t, &h->dt, [h](const auto& vec, auto** dst) { return dev_alloc_copy(h, dst, vec.data(), vec.size()); });
   if (e != cudaSuccess) {
     int code = cuda_fail(h, e, "table upload");
     mld_gpu_destroy(h);
@@ -1040,6 +1050,10 @@ int mld_gpu_set_structures(mld_gpu_handle* h, int nstruct, const int* nat, const
       int nc = (int)(2.0 * h->cfg.r_cut / bval) + 1;
       if (nc > 1) sm = 1;
       nsize[3 * s + i] = nc / 2 + 1;
+      // the neighbour search packs each periodic image index in 8 bits
+      if (nsize[3 * s + i] > 127)
+        return fail(h, MLD_ERR_INVALID, "structure " + std::to_string(s) +
+                                            ": cell too thin for r_cut (more than 127 periodic images along a lattice vector)");
     }
     small[s] = sm;
   }
@@ -1112,29 +1126,11 @@ int mld_gpu_descriptors(mld_gpu_handle* h, double* B_out, int* n_neigh_out) {
   if (!h) return MLD_ERR_INVALID;
   int rc = build_neighbours(h);
   if (rc) return rc;
-  RowLayout none;
-  none.rowE.assign(h->S, -1);
-  none.rowF.assign(h->S, -1);
-  none.rowS.assign(h->S, -1);
-  DevRows rows;
-  rows.D = h->D;
-  CK(upload(h, mld_gpu_handle::B_ROWE, none.rowE.data(), h->S));
-  CK(upload(h, mld_gpu_handle::B_ROWF, none.rowF.data(), h->S));
-  CK(upload(h, mld_gpu_handle::B_ROWS, none.rowS.data(), h->S));
-  rows.rowE = bp_<long long>(h, mld_gpu_handle::B_ROWE);
-  rows.rowF = bp_<long long>(h, mld_gpu_handle::B_ROWF);
-  rows.rowS = bp_<long long>(h, mld_gpu_handle::B_ROWS);
   const size_t nB = (size_t)h->A * h->KK;
-  const size_t nd = (size_t)h->b.P * 3 * h->KK;
   if (h->mixed) {
     CK(ensure(h, mld_gpu_handle::B_BOUT, sizeof(float) * std::max<size_t>(nB, 1)));
-    CK(ensure(h, mld_gpu_handle::B_DBOUT, sizeof(float) * std::max<size_t>(nd, 1)));
-    void* ys = nullptr;
-    size_t ysb = 0;
-    int rcy = y_scratch<float>(h, &ys, &ysb);
-    if (rcy) return rcy;
-    CK(launch_bso4_rows<float>(h->dt, h->b, rows, h->bp, (float*)nullptr, bp_<float>(h, mld_gpu_handle::B_BOUT),
-                               bp_<float>(h, mld_gpu_handle::B_DBOUT), 0, h->st, ys, ysb));
+    rc = run_descriptors<float>(h, true, nullptr, bp_<float>(h, mld_gpu_handle::B_BOUT));
+    if (rc) return rc;
     if (B_out) {
       std::vector<float> tmp(nB);
       CK(cudaMemcpyAsync(tmp.data(), bp_<float>(h, mld_gpu_handle::B_BOUT), sizeof(float) * nB,
@@ -1144,13 +1140,8 @@ int mld_gpu_descriptors(mld_gpu_handle* h, double* B_out, int* n_neigh_out) {
     }
   } else {
     CK(ensure(h, mld_gpu_handle::B_BOUT, sizeof(double) * std::max<size_t>(nB, 1)));
-    CK(ensure(h, mld_gpu_handle::B_DBOUT, sizeof(double) * std::max<size_t>(nd, 1)));
-    void* ys = nullptr;
-    size_t ysb = 0;
-    int rcy = y_scratch<double>(h, &ys, &ysb);
-    if (rcy) return rcy;
-    CK(launch_bso4_rows<double>(h->dt, h->b, rows, h->bp, (double*)nullptr, bp_<double>(h, mld_gpu_handle::B_BOUT),
-                                bp_<double>(h, mld_gpu_handle::B_DBOUT), 0, h->st, ys, ysb));
+    rc = run_descriptors<double>(h, true, nullptr, bp_<double>(h, mld_gpu_handle::B_BOUT));
+    if (rc) return rc;
     if (B_out)
       CK(cudaMemcpyAsync(B_out, bp_<double>(h, mld_gpu_handle::B_BOUT), sizeof(double) * nB, cudaMemcpyDeviceToHost,
                          h->st));
@@ -1262,8 +1253,11 @@ int mld_gpu_gram(mld_gpu_handle* h, double* G, double* rhs) {
                              bp_<void>(h, mld_gpu_handle::B_GWS), wsb, terr, h->nsm, h->st));
     CK(launch_symmetrize(dG, D, h->st));
     CK(ensure(h, mld_gpu_handle::B_PRED, sizeof(double) * (size_t)std::max<long long>(M, 1)));
+    double* rws = gram_ws(h, M, D);
+    if (!rws) return fail(h, MLD_ERR_OOM, "rhs workspace");
     CK(launch_rhs<float>(X, h->ldx, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D,
-                         bp_<double>(h, mld_gpu_handle::B_H), h->nsm, h->st, bp_<float2>(h, mld_gpu_handle::B_PRED)));
+                         bp_<double>(h, mld_gpu_handle::B_H), h->nsm, h->st, bp_<float2>(h, mld_gpu_handle::B_PRED),
+                         rws));
     int herr = 0;
     CK(cudaMemcpyAsync(&herr, terr, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
@@ -1272,8 +1266,10 @@ int mld_gpu_gram(mld_gpu_handle* h, double* G, double* rhs) {
     double* X = nullptr;
     rc = run_rows<double>(h, h->fit_rows, true, &X);
     if (rc) return rc;
+    double* gws = gram_ws(h, M, D);
+    if (!gws) return fail(h, MLD_ERR_OOM, "Gram workspace");
     CK(launch_gram<double>(X, h->ldx, bp_<double>(h, mld_gpu_handle::B_WROW), bp_<double>(h, mld_gpu_handle::B_Y), M, D,
-                           bp_<double>(h, mld_gpu_handle::B_G), bp_<double>(h, mld_gpu_handle::B_H), h->st));
+                           bp_<double>(h, mld_gpu_handle::B_G), bp_<double>(h, mld_gpu_handle::B_H), h->st, gws));
   }
   if (G) CK(cudaMemcpyAsync(G, bp_<double>(h, mld_gpu_handle::B_G), sizeof(double) * D * D, cudaMemcpyDeviceToHost, h->st));
   if (rhs) CK(cudaMemcpyAsync(rhs, bp_<double>(h, mld_gpu_handle::B_H), sizeof(double) * D, cudaMemcpyDeviceToHost, h->st));
@@ -1295,11 +1291,9 @@ int mld_gpu_solve(mld_gpu_handle* h, const double* G, const double* rhs, int D, 
   CK(cudaMemcpyAsync(dh, rhs, sizeof(double) * D, cudaMemcpyHostToDevice, h->st));
   int rc = solve_any(h, dG, dh, D, dw);
   if (rc) return rc;
-  int info[2] = {0, D};
   CK(cudaMemcpyAsync(w, dw, sizeof(double) * D, cudaMemcpyDeviceToHost, h->st));
-  if (D <= 112) CK(cudaMemcpyAsync(info, bp_<int>(h, mld_gpu_handle::B_INFO), sizeof(int) * 2, cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
-  if (rank_out) *rank_out = info[1];
+  if (rank_out) *rank_out = h->last_rank;
   return MLD_OK;
 }
 
@@ -1472,35 +1466,38 @@ static int eval_run(mld_gpu_handle* h, double* out) {
   const double* wlin = bp_<double>(h, mld_gpu_handle::B_EW);
   const double* wsym = wlin + KK;
   const T* wlinT = reinterpret_cast<const T*>(wlin + KK + (h->quad ? (size_t)KK * KK : 0));
-  size_t ysb = 0;
-  void* ys = nullptr;
-  int rc = y_scratch<T>(h, &ys, &ysb);
-  if (rc) return rc;
-  DevRows none{};
+  CK(ensure(h, mld_gpu_handle::B_EPAIR, sizeof(double) * 9 * (size_t)std::max<long long>(1, h->b.P)));
+  CK(ensure(h, mld_gpu_handle::B_EATOM, sizeof(double) * (size_t)std::max(1, h->A)));
+  CK(ensure(h, mld_gpu_handle::B_REV, sizeof(int) * (size_t)std::max<long long>(1, h->b.P)));
+  double* Eatom = bp_<double>(h, mld_gpu_handle::B_EATOM);
   DevEval<T> ev;
-  ev.F = F;
-  ev.S = S;
+  ev.pair = bp_<double>(h, mld_gpu_handle::B_EPAIR);
   ev.w0 = h->ew0;
   if (h->quad) {
-    // pass 1: B of every atom; beta_a and the energies; pass 2: forces and stress
+    // pass 1: B of every atom; beta_a and the atom energies; pass 2: per-pair forces and stress
     CK(ensure(h, mld_gpu_handle::B_EB, sizeof(T) * std::max<size_t>(1, (size_t)h->A * KK)));
     CK(ensure(h, mld_gpu_handle::B_EBETA, sizeof(T) * std::max<size_t>(1, (size_t)h->A * KK)));
     T* B = bp_<T>(h, mld_gpu_handle::B_EB);
     T* beta = bp_<T>(h, mld_gpu_handle::B_EBETA);
-    CK(launch_bso4_rows<T>(h->dt, h->b, none, h->bp, (T*)nullptr, B, (T*)nullptr, 0, h->st, ys, ysb));
-    CK(launch_eval_beta<T>(B, h->A, KK, wlin, wsym, h->ew0, h->b.atom_struct, beta, E, h->st));
+    int rc = run_descriptors<T>(h, false, nullptr, B);
+    if (rc) return rc;
+    CK(launch_eval_beta<T>(B, h->A, KK, wlin, wsym, h->ew0, beta, Eatom, h->st));
     ev.beta = beta;
     ev.beta_per_atom = 1;
-    CK(launch_bso4_rows<T>(h->dt, h->b, none, h->bp, (T*)nullptr, (T*)nullptr, (T*)nullptr, 0, h->st, ys, ysb, &ev));
-    nl(h, 3);
+    rc = run_descriptors<T>(h, false, &ev, (T*)nullptr);
+    if (rc) return rc;
+    nl(h, 1);
   } else {
     ev.beta = wlinT;
     ev.beta_per_atom = 0;
     ev.wlin = wlin;
-    ev.E = E;
-    CK(launch_bso4_rows<T>(h->dt, h->b, none, h->bp, (T*)nullptr, (T*)nullptr, (T*)nullptr, 0, h->st, ys, ysb, &ev));
-    nl(h, 1);
+    ev.Eatom = Eatom;
+    int rc = run_descriptors<T>(h, false, &ev, (T*)nullptr);
+    if (rc) return rc;
   }
+  CK(launch_reverse_pairs(h->b, bp_<int>(h, mld_gpu_handle::B_REV), h->st));
+  CK(launch_eval_gather(h->b, h->bp, bp_<int>(h, mld_gpu_handle::B_REV), ev.pair, Eatom, E, F, S, h->st));
+  nl(h, 3);
   return MLD_OK;
 }
 
@@ -1549,6 +1546,21 @@ int handle_dims(const mld_gpu_handle* h, int* D, int* ldx, int* KK, int* nch) {
   *KK = h->KK;
   *nch = h->nch;
   return MLD_OK;
+}
+
+// Free every per-batch device buffer of an idle handle (the evaluation weights stay); the next
+// batch allocates what it needs again.
+void handle_release_buffers(mld_gpu_handle* h) {
+  cudaStreamSynchronize(h->st);
+  for (int id = 0; id < mld_gpu_handle::B_COUNT; ++id) {
+    if (id == mld_gpu_handle::B_EW) continue;
+    Buf& bf = h->bufs[id];
+    if (bf.p) cudaFree(bf.p);
+    bf.p = nullptr;
+    bf.cap = 0;
+  }
+  h->has_batch = false;
+  h->nbr_valid = false;
 }
 
 }  // namespace mld
@@ -1673,6 +1685,12 @@ extern "C" int mld_gpu_set_kernel_points(mld_gpu_handle* h, int nk, const double
   return MLD_OK;
 }
 
+extern "C" int mld_gpu_test_pipeline_timeout(int skip_loads, long long wait_limit_clocks) {
+  if (skip_loads < 0 || wait_limit_clocks < 0) return MLD_ERR_INVALID;
+  mld::gram_tc_test_timeout(skip_loads, wait_limit_clocks);
+  return MLD_OK;
+}
+
 extern "C" int mld_gpu_solve_info(const mld_gpu_handle* h, int* pcg_iterations, double* pcg_residual,
                                   double* precond_shift, int* chol_retries) {
   if (!h) return MLD_ERR_INVALID;
@@ -1732,8 +1750,11 @@ extern "C" int mld_gpu_gram_rows(int method, const void* X, int x_is_fp32, long 
       if (e != cudaSuccess) return cuda_err(e, "cudaMemsetAsync");
       yy = yz;
     }
-    e = x_is_fp32 ? launch_gram<float>(static_cast<const float*>(X), ldx, w, yy, M, D, G, hv, st)
-                  : launch_gram<double>(static_cast<const double*>(X), ldx, w, yy, M, D, G, hv, st);
+    e = cudaMalloc(&ws, sizeof(double) * gram_workspace_doubles(M, D));
+    if (e != cudaSuccess) return cuda_err(e, "workspace");
+    double* gws = static_cast<double*>(ws);
+    e = x_is_fp32 ? launch_gram<float>(static_cast<const float*>(X), ldx, w, yy, M, D, G, hv, st, gws)
+                  : launch_gram<double>(static_cast<const double*>(X), ldx, w, yy, M, D, G, hv, st, gws);
     if (e != cudaSuccess) return cuda_err(e, "launch_gram");
   } else {
     if (!gram_tc_available())

@@ -195,23 +195,46 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
     return false;
   }
 
-  // layer-blocked Y: rows of layer j are the triples using layer j (any of l, l1, l2)
-  std::vector<std::vector<int>> rows(J + 1);
-  for (int k = 0; k < t->K; ++k) {
-    int js[3] = {t->l[k], t->l1[k], t->l2[k]};
-    for (int b = 0; b < 3; ++b) {
-      bool seen = false;
-      for (int c = 0; c < b; ++c) seen |= js[c] == js[b];
-      if (!seen) rows[js[b]].push_back(k);
+  // layer-blocked Y: rows of layer j are the triples using layer j (any of l, l1, l2).  A
+  // triple's distinct layers in ascending order have ranks 0, 1, 2; within a layer the rows are
+  // grouped by rank (each group padded to whole row tiles), so the dB contraction can run in
+  // kRounds rounds in which every triple receives at most one row's contribution (no atomics,
+  // a fixed summation order).
+  std::vector<std::vector<int>> rows(J + 1);  // row position -> triple (-1 padding)
+  std::vector<std::map<int, int>> rowpos(J + 1);  // triple -> row position
+  std::vector<std::vector<int>> round_tiles(kRounds);
+  {
+    std::vector<std::vector<std::vector<int>>> byrank(J + 1, std::vector<std::vector<int>>(kRounds));
+    for (int k = 0; k < t->K; ++k) {
+      int js[3] = {t->l[k], t->l1[k], t->l2[k]};
+      std::sort(js, js + 3);
+      int rank = 0;
+      for (int b = 0; b < 3; ++b) {
+        if (b > 0 && js[b] == js[b - 1]) continue;
+        byrank[js[b]][rank++].push_back(k);
+      }
     }
+    for (int j = 0; j <= J; ++j)
+      for (int r = 0; r < kRounds; ++r) {
+        const std::vector<int>& v = byrank[j][r];
+        if (v.empty()) continue;
+        const int first = (int)rows[j].size();
+        for (int k : v) {
+          rowpos[j][k] = (int)rows[j].size();
+          rows[j].push_back(k);
+        }
+        while (rows[j].size() % kRowTile) rows[j].push_back(-1);
+        for (int rt = first / kRowTile; rt < (int)rows[j].size() / kRowTile; ++rt)
+          round_tiles[r].push_back((j << 8) | rt);
+      }
   }
   int ypos = 0, rk = 0;
   for (int j = 0; j <= J; ++j) {
-    t->Mp[j] = ((int)rows[j].size() + kRowTile - 1) / kRowTile * kRowTile;
+    t->Mp[j] = (int)rows[j].size();
     t->yoff[j] = ypos;
     ypos += t->Mp[j] * H(j);
     t->rowk_off[j] = rk;
-    for (int r = 0; r < t->Mp[j]; ++r) t->rowk.push_back(r < (int)rows[j].size() ? (int16_t)rows[j][r] : -1);
+    for (int r = 0; r < t->Mp[j]; ++r) t->rowk.push_back((int16_t)rows[j][r]);
     rk += t->Mp[j];
   }
   t->rowk_off[J + 1] = rk;
@@ -220,68 +243,74 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
     *err = "Y table exceeds 16-bit offsets";
     return false;
   }
+  // row tiles of the dB contraction by round, heaviest layers first within a round
+  for (int r = 0; r < kRounds; ++r) {
+    std::vector<int>& v = round_tiles[r];
+    std::stable_sort(v.begin(), v.end(), [](int x, int y) { return (x >> 8) > (y >> 8); });
+    t->tile_off[r] = (int)t->tiles.size();
+    t->tiles.insert(t->tiles.end(), v.begin(), v.end());
+  }
+  t->tile_off[kRounds] = (int)t->tiles.size();
 
-  // folded slots
-  std::vector<long long> cost;
+  // folded slots; the kernel's slot entries; the ZA entries of every triple for B
+  std::vector<std::vector<BkItem>> bk(t->K);
   for (int j = 0; j <= J; ++j) {
-    for (int r = 0; r < (int)rows[j].size(); ++r) {
-      const int k = rows[j][r];
+    for (const auto& kr : rowpos[j]) {
+      const int k = kr.first, r = kr.second;
       const auto& bl = kblocks[k];
       for (int e = 0; e < H(j); ++e) {
         int p = -j + 2 * (e / (j + 1)), q = -j + 2 * (e % (j + 1));
         YSlot s{};
-        long long c = 0;
+        SlotEntry se{};
         for (int b = 0; b < 3; ++b) {
           if (bl[b].jO != j) continue;
           if (b == 0) s.is_a = 1;
           int zi = bl[b].first + e;  // half outputs are stored in row-major order of the layer
+          se.snum[s.nterm] = (uint8_t)t->zterms[zi].snum;
+          se.sden[s.nterm] = (uint8_t)t->zterms[zi].sden;
+          se.term[s.nterm] = (uint16_t)zi;
           s.term[s.nterm++] = (uint16_t)zi;
-          c += (long long)t->zterms[zi].na * t->zterms[zi].nb;
         }
         s.ufull = (uint16_t)uidx(j, p, q);
         s.k = (uint16_t)k;
         s.ypos = (uint16_t)(t->yoff[j] + e * t->Mp[j] + r);
         s.wgt = (uint8_t)((p == 0 && q == 0) ? 1 : 2);
+        se.ypos = s.ypos;
+        se.nterm = s.nterm;
+        se.wgt = s.wgt;
         t->yslots.push_back(s);
-        cost.push_back(c);
+        t->slots.push_back(se);
+        if (s.is_a) bk[k].push_back(BkItem{s.term[0], s.ufull, s.wgt, {0, 0, 0}});
       }
     }
   }
-  t->yorder.resize(t->yslots.size());
-  for (size_t i = 0; i < t->yorder.size(); ++i) t->yorder[i] = (int)i;
-  std::stable_sort(t->yorder.begin(), t->yorder.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  t->bk_off.assign(t->K + 1, 0);
+  for (int k = 0; k < t->K; ++k) {
+    t->bk_off[k] = (int)t->bk_items.size();
+    t->bk_items.insert(t->bk_items.end(), bk[k].begin(), bk[k].end());
+  }
+  t->bk_off[t->K] = (int)t->bk_items.size();
 
-  // row tiles of the dB contraction, heaviest layers first
-  for (int j = J; j >= 0; --j)
-    for (int rt = 0; rt < t->Mp[j] / kRowTile; ++rt) t->tiles.push_back((j << 8) | rt);
-
-  // phase-2 schedule: every Z term of every slot is one work entry.  Entries of equal loop shape
-  // (na, nb) form rounds of 32, one per lane, padded with zero-weight copies, so that the lanes
+  // phase-2 schedule: every Z term is one work entry.  Entries of equal loop shape (na, nb)
+  // form rounds of 32, one per lane, padded with entries that write nothing, so that the lanes
   // of a warp run identical loops; rounds go to the kZWarps warps longest-first (LPT) by their
-  // na * nb cost.  A term adds its scaled Z into its slot of Y (and, for ZA, into B) atomically.
+  // na * nb cost.  A term stores its Z value at its own index of the term buffer; the slots and
+  // B are summed from there in a fixed order.
   {
     std::map<std::pair<int, int>, std::vector<ZItem>> byshape;
-    for (const YSlot& s : t->yslots) {
-      for (int tt = 0; tt < s.nterm; ++tt) {
-        const ZTerm& z = t->zterms[s.term[tt]];
-        ZItem zi{};
-        zi.i1 = z.i1;
-        zi.i2 = z.i2;
-        zi.cg1 = z.cg1;
-        zi.cg2 = z.cg2;
-        zi.na = z.na;
-        zi.nb = z.nb;
-        zi.s1 = z.s1;
-        zi.s2 = z.s2;
-        zi.ypos = s.ypos;
-        zi.ufull = s.ufull;
-        zi.k = s.k;
-        zi.wgt = s.wgt;
-        zi.is_a = (tt == 0 && s.is_a) ? 1 : 0;
-        zi.snum = z.snum;
-        zi.sden = z.sden;
-        byshape[{z.na, z.nb}].push_back(zi);
-      }
+    for (size_t zi = 0; zi < t->zterms.size(); ++zi) {
+      const ZTerm& z = t->zterms[zi];
+      ZItem it{};
+      it.i1 = z.i1;
+      it.i2 = z.i2;
+      it.cg1 = z.cg1;
+      it.cg2 = z.cg2;
+      it.na = z.na;
+      it.nb = z.nb;
+      it.s1 = z.s1;
+      it.s2 = z.s2;
+      it.term = (uint16_t)zi;
+      byshape[{z.na, z.nb}].push_back(it);
     }
     struct Round { long long cost; std::vector<ZItem> lanes; };
     std::vector<Round> rounds;
@@ -292,8 +321,7 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
         for (size_t l = i; l < std::min(v.size(), i + 32); ++l) r.lanes.push_back(v[l]);
         while (r.lanes.size() < 32) {
           ZItem pad = v[i];
-          pad.wgt = 0;
-          pad.is_a = 0;
+          pad.term = kNoTerm;
           r.lanes.push_back(pad);
         }
         rounds.push_back(std::move(r));

@@ -12,12 +12,11 @@
 namespace mld {
 
 // One CTA per atom: beta[k] = w_lin[k] + sum_j Wsym[j][k] B[j] (Wsym symmetric, read by rows j
-// so that consecutive threads read consecutive k) and E_s += w0 + B . (beta + w_lin) / 2.
+// so that consecutive threads read consecutive k) and the atom's energy w0 + B . (beta + w_lin) / 2.
 template <typename T>
 __global__ void __launch_bounds__(128) k_eval_beta(const T* __restrict__ B, int nchK, const double* __restrict__ wlin,
-                                                  const double* __restrict__ wsym, double w0,
-                                                  const int* __restrict__ atom_struct, T* __restrict__ beta,
-                                                  double* __restrict__ E) {
+                                                  const double* __restrict__ wsym, double w0, T* __restrict__ beta,
+                                                  double* __restrict__ Eatom) {
   extern __shared__ double bsh[];  // nchK
   __shared__ double red[4];
   const int a = blockIdx.x, tid = threadIdx.x;
@@ -33,20 +32,20 @@ __global__ void __launch_bounds__(128) k_eval_beta(const T* __restrict__ B, int 
   for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
   if ((tid & 31) == 0) red[tid >> 5] = e;
   __syncthreads();
-  if (tid == 0) atomicAdd(&E[atom_struct[a]], w0 + red[0] + red[1] + red[2] + red[3]);
+  if (tid == 0) Eatom[a] = w0 + red[0] + red[1] + red[2] + red[3];
 }
 
 template <typename T>
-cudaError_t launch_eval_beta(const T* B, int A, int nchK, const double* wlin, const double* wsym, double w0,
-                             const int* atom_struct, T* beta, double* E, cudaStream_t st) {
+cudaError_t launch_eval_beta(const T* B, int A, int nchK, const double* wlin, const double* wsym, double w0, T* beta,
+                             double* Eatom, cudaStream_t st) {
   if (A <= 0) return cudaSuccess;
-  k_eval_beta<T><<<A, 128, sizeof(double) * nchK, st>>>(B, nchK, wlin, wsym, w0, atom_struct, beta, E);
+  k_eval_beta<T><<<A, 128, sizeof(double) * nchK, st>>>(B, nchK, wlin, wsym, w0, beta, Eatom);
   return cudaGetLastError();
 }
 
-template cudaError_t launch_eval_beta<double>(const double*, int, int, const double*, const double*, double, const int*,
-                                              double*, double*, cudaStream_t);
-template cudaError_t launch_eval_beta<float>(const float*, int, int, const double*, const double*, double, const int*,
-                                             float*, double*, cudaStream_t);
+template cudaError_t launch_eval_beta<double>(const double*, int, int, const double*, const double*, double, double*,
+                                              double*, cudaStream_t);
+template cudaError_t launch_eval_beta<float>(const float*, int, int, const double*, const double*, double, float*,
+                                             double*, cudaStream_t);
 
 }  // namespace mld

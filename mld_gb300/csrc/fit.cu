@@ -61,9 +61,12 @@ __global__ void k_rows_prep(int S, const int* __restrict__ atom_start, const lon
 constexpr int GT = 32;   // tile edge
 constexpr int GR = 32;   // rows per smem stage
 
+// part != nullptr: each CTA stores its 32 x 32 partial tile at part[(blockIdx.y * npairs +
+// blockIdx.x) * 1024] for k_gram_reduce (fixed summation order); else atomics into G.
 template <typename T>
 __global__ void __launch_bounds__(256) k_gram(const T* __restrict__ X, int ldx, const double* __restrict__ w,
-                                              long long M, int D, long long rows_per_block, double* __restrict__ G) {
+                                              long long M, int D, long long rows_per_block, double* __restrict__ G,
+                                              double* __restrict__ part) {
   const int nt = (D + GT - 1) / GT;
   // decode upper-triangular tile pair from blockIdx.x
   int t = blockIdx.x, ti = 0;
@@ -104,11 +107,44 @@ __global__ void __launch_bounds__(256) k_gram(const T* __restrict__ X, int ldx, 
     }
     __syncthreads();
   }
+  if (part) {
+    double* pt = part + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * (GT * GT);
+    for (int a = 0; a < 2; ++a)
+      for (int b = 0; b < 2; ++b) pt[(ty + 16 * a) * GT + tx + 16 * b] = acc[a][b];
+    return;
+  }
   for (int a = 0; a < 2; ++a)
     for (int b = 0; b < 2; ++b) {
       const int i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
       if (i < D && j < D && (ti != tj || i <= j)) atomicAdd(&G[(size_t)i * D + j], acc[a][b]);
     }
+}
+
+// G (upper triangle of each tile pair) = sum over the row chunks of the partial tiles, in chunk
+// order; one CTA per tile pair, one thread per element.
+__global__ void __launch_bounds__(GT * GT) k_gram_reduce(const double* __restrict__ part, int npairs, int chunks, int D,
+                                                         double* __restrict__ G) {
+  const int nt = (D + GT - 1) / GT;
+  int t = blockIdx.x, ti = 0;
+  while (t >= nt - ti) {
+    t -= nt - ti;
+    ++ti;
+  }
+  const int tj = ti + t;
+  const int e = threadIdx.x, i = ti * GT + e / GT, j = tj * GT + e % GT;
+  if (i >= D || j >= D || (ti == tj && i > j)) return;
+  double sum = 0.0;
+  for (int c = 0; c < chunks; ++c) sum += part[((size_t)c * npairs + blockIdx.x) * (GT * GT) + e];
+  G[(size_t)i * D + j] = sum;
+}
+
+// q[c] = sum over the row blocks of part[b * D + c], in block order.
+__global__ void k_colsum_reduce(const double* __restrict__ part, long long nrb, int D, double* __restrict__ q) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= D) return;
+  double sum = 0.0;
+  for (long long b = 0; b < nrb; ++b) sum += part[(size_t)b * D + c];
+  q[c] = sum;
 }
 
 __global__ void k_symmetrize(double* G, int D) {
@@ -117,31 +153,57 @@ __global__ void k_symmetrize(double* G, int D) {
     if (jj < i) G[(size_t)i * D + jj] = G[(size_t)jj * D + i];
 }
 
+namespace {
+long long rows_per_cta(long long M, int ncb, int nsm);
+// row chunks of the FP64 Gram: enough CTAs to fill the machine (~8 per SM overall)
+void gram_chunks(long long M, int D, int nsm, int* npairs, long long* chunks, long long* rpb) {
+  const int nt = (D + GT - 1) / GT;
+  *npairs = nt * (nt + 1) / 2;
+  long long c = (long long)nsm * 8 / *npairs;
+  if (c < 1) c = 1;
+  long long r = (std::max<long long>(M, 1) + c - 1) / c;
+  r = ((r + GR - 1) / GR) * GR;
+  c = (std::max<long long>(M, 1) + r - 1) / r;
+  if (c > 65535) {
+    c = 65535;
+    r = (M + c - 1) / c;
+  }
+  *chunks = c;
+  *rpb = r;
+}
+int device_sms() {
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return nsm;
+}
+}  // namespace
+
+size_t gram_workspace_doubles(long long M, int D) {
+  const int nsm = device_sms();
+  int npairs = 0;
+  long long chunks = 0, rpb = 0;
+  gram_chunks(M, D, nsm, &npairs, &chunks, &rpb);
+  const int ncb = (D + 255) / 256;
+  const long long nrb = (std::max<long long>(M, 1) + rows_per_cta(M, ncb, nsm) - 1) / rows_per_cta(M, ncb, nsm);
+  return std::max<size_t>((size_t)chunks * npairs * GT * GT, (size_t)nrb * D);
+}
+
 template <typename T>
 cudaError_t launch_gram(const T* X, int ldx, const double* w, const double* y, long long M, int D, double* G,
-                        double* h, cudaStream_t st) {
+                        double* h, cudaStream_t st, double* ws) {
   cudaError_t e = cudaMemsetAsync(G, 0, sizeof(double) * (size_t)D * D, st);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(h, 0, sizeof(double) * (size_t)D, st);
   if (e != cudaSuccess) return e;
   if (M == 0) return cudaSuccess;
-  const int nt = (D + GT - 1) / GT;
-  const int npairs = nt * (nt + 1) / 2;
-  // enough row chunks to fill the machine (~8 CTAs per SM overall)
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  long long chunks = (long long)nsm * 8 / npairs;
-  if (chunks < 1) chunks = 1;
-  long long rpb = (M + chunks - 1) / chunks;
-  rpb = ((rpb + GR - 1) / GR) * GR;
-  chunks = (M + rpb - 1) / rpb;
-  if (chunks > 65535) {
-    chunks = 65535;
-    rpb = (M + chunks - 1) / chunks;
-  }
-  k_gram<T><<<dim3(npairs, (unsigned)chunks), 256, 0, st>>>(X, ldx, w, M, D, rpb, G);
-  e = launch_rhs<T>(X, ldx, w, y, M, D, h, nsm, st, nullptr);
+  const int nsm = device_sms();
+  int npairs = 0;
+  long long chunks = 0, rpb = 0;
+  gram_chunks(M, D, nsm, &npairs, &chunks, &rpb);
+  k_gram<T><<<dim3(npairs, (unsigned)chunks), 256, 0, st>>>(X, ldx, w, M, D, rpb, G, ws);
+  if (ws) k_gram_reduce<<<npairs, GT * GT, 0, st>>>(ws, npairs, (int)chunks, D, G);
+  e = launch_rhs<T>(X, ldx, w, y, M, D, h, nsm, st, nullptr, ws);
   if (e != cudaSuccess) return e;
   k_symmetrize<<<D, 128, 0, st>>>(G, D);
   return cudaGetLastError();
@@ -153,7 +215,7 @@ cudaError_t launch_gram(const T* X, int ldx, const double* w, const double* y, l
 template <typename T>
 __global__ void __launch_bounds__(256) k_xtv(const T* __restrict__ X, int ldx, int D, const double* __restrict__ w,
                                              const double* __restrict__ v, long long M, long long rpb,
-                                             double* __restrict__ q) {
+                                             double* __restrict__ q, double* __restrict__ part) {
   __shared__ double red[8][256];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int cb = blockIdx.y * 256;
@@ -176,7 +238,10 @@ __global__ void __launch_bounds__(256) k_xtv(const T* __restrict__ X, int ldx, i
   double sum = 0.0;
 #pragma unroll
   for (int w8 = 0; w8 < 8; ++w8) sum += red[w8][threadIdx.x];
-  if (cb + threadIdx.x < D && sum != 0.0) atomicAdd(&q[cb + threadIdx.x], sum);
+  if (cb + threadIdx.x < D) {
+    if (part) part[(size_t)blockIdx.x * D + cb + threadIdx.x] = sum;
+    else if (sum != 0.0) atomicAdd(&q[cb + threadIdx.x], sum);
+  }
 }
 
 // Normal-equation matvec of a narrow block (D <= 32*NK <= 256) in one pass over X:
@@ -303,7 +368,7 @@ __global__ void k_wy_ds(const double* __restrict__ w, const double* __restrict__
 // (blockIdx.y), design rows in chunks (blockIdx.x) walked by the 8 warps.
 __global__ void __launch_bounds__(256) k_xtv_ds(const float* __restrict__ X, int ldx, int D,
                                                 const float2* __restrict__ sv, long long M, long long rpb,
-                                                double* __restrict__ q) {
+                                                double* __restrict__ q, double* __restrict__ part) {
   __shared__ double red[8][256];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int cb = blockIdx.y * 256;
@@ -330,7 +395,10 @@ __global__ void __launch_bounds__(256) k_xtv_ds(const float* __restrict__ X, int
   double sum = 0.0;
 #pragma unroll
   for (int w8 = 0; w8 < 8; ++w8) sum += red[w8][threadIdx.x];
-  if (cb + threadIdx.x < D && sum != 0.0) atomicAdd(&q[cb + threadIdx.x], sum);
+  if (cb + threadIdx.x < D) {
+    if (part) part[(size_t)blockIdx.x * D + cb + threadIdx.x] = sum;
+    else if (sum != 0.0) atomicAdd(&q[cb + threadIdx.x], sum);
+  }
 }
 
 // ------------------------------------------------------------------------------------
@@ -516,20 +584,22 @@ long long rows_per_cta(long long M, int ncb, int nsm) {
 // given, FP64 accumulation otherwise
 template <typename T>
 cudaError_t launch_rhs(const T* X, int ldx, const double* w, const double* y, long long M, int D, double* h,
-                       int nsm, cudaStream_t st, float2* sv) {
+                       int nsm, cudaStream_t st, float2* sv, double* ws) {
   cudaError_t e = cudaMemsetAsync(h, 0, sizeof(double) * (size_t)D, st);
   if (e != cudaSuccess || M == 0) return e;
   const int ncb = (D + 255) / 256;
   const long long rpb = rows_per_cta(M, ncb, nsm);
   const long long nrb = (M + rpb - 1) / rpb;
+  bool done = false;
   if constexpr (std::is_same<T, float>::value) {
     if (sv) {
       k_wy_ds<<<(unsigned)((M + 255) / 256), 256, 0, st>>>(w, y, M, sv);
-      k_xtv_ds<<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(X, ldx, D, sv, M, rpb, h);
-      return cudaGetLastError();
+      k_xtv_ds<<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(X, ldx, D, sv, M, rpb, h, ws);
+      done = true;
     }
   }
-  k_xtv<T><<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(X, ldx, D, w, y, M, rpb, h);
+  if (!done) k_xtv<T><<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(X, ldx, D, w, y, M, rpb, h, ws);
+  if (ws) k_colsum_reduce<<<(D + 255) / 256, 256, 0, st>>>(ws, nrb, D, h);
   return cudaGetLastError();
 }
 
@@ -628,7 +698,7 @@ cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const d
     const int ncb = (D + 255) / 256;
     const long long rpb = rows_per_cta(M, ncb, nsm);
     const long long nrb = (M + rpb - 1) / rpb;
-    k_xtv_ds<<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(Xc, ldx, D, sv, M, rpb, q);
+    k_xtv_ds<<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(Xc, ldx, D, sv, M, rpb, q, nullptr);
     *launches = 2;
   }
   if (lambda > 0) {
@@ -640,9 +710,9 @@ cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const d
 }
 
 template cudaError_t launch_rhs<double>(const double*, int, const double*, const double*, long long, int, double*, int,
-                                        cudaStream_t, float2*);
+                                        cudaStream_t, float2*, double*);
 template cudaError_t launch_rhs<float>(const float*, int, const double*, const double*, long long, int, double*, int,
-                                       cudaStream_t, float2*);
+                                       cudaStream_t, float2*, double*);
 
 // lower triangle <- upper triangle
 cudaError_t launch_symmetrize(double* G, int D, cudaStream_t st) {
@@ -807,11 +877,13 @@ cudaError_t launch_solve_sym(double* G, const double* h, int D, double lambda, d
 // Predictions X w (warp per design row, grid-stride) and per-kind squared errors: FP64 dot for
 // an FP64 X, double-FP32 dot for an FP32 X (w split into FP32 pairs in shared memory).  The
 // squared errors are reduced per block before six FP64 atomics.
+constexpr int kSqPartials = 8;  // offset of the per-CTA partials in the squared-error buffer
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_predict(const T* __restrict__ X, int ldx, const double* __restrict__ w,
                                                  long long M, int D, double* __restrict__ pred,
                                                  const double* __restrict__ y, const int* __restrict__ kind,
-                                                 double* __restrict__ sq /*3 sums + 3 counts*/) {
+                                                 double* __restrict__ sq /*3 sums + 3 counts, then per-CTA partials*/) {
   extern __shared__ float wsp[];  // [2][D] for FP32 X
   __shared__ double red[8][6];
   constexpr bool kDs = std::is_same<T, float>::value;
@@ -856,8 +928,17 @@ __global__ void __launch_bounds__(256) k_predict(const T* __restrict__ X, int ld
   if (threadIdx.x < 6) {
     double t = 0.0;
     for (int w8 = 0; w8 < 8; ++w8) t += red[w8][threadIdx.x];
-    if (t != 0.0) atomicAdd(&sq[threadIdx.x], t);
+    sq[kSqPartials + 6 * (size_t)blockIdx.x + threadIdx.x] = t;
   }
+}
+
+// sq[0..5] = the per-CTA partials summed in CTA order
+__global__ void k_sq_reduce(double* __restrict__ sq, int blocks) {
+  const int k = threadIdx.x;
+  if (k >= 6) return;
+  double t = 0.0;
+  for (int b = 0; b < blocks; ++b) t += sq[kSqPartials + 6 * (size_t)b + k];
+  sq[k] = t;
 }
 
 template <typename T>
@@ -878,7 +959,15 @@ cudaError_t launch_predict_sq(const T* X, int ldx, const double* w, long long M,
     }
   }
   k_predict<T><<<blocks, 256, smem, st>>>(X, ldx, w, M, D, pred, y, kind, sq);
+  if (sq) k_sq_reduce<<<1, 32, 0, st>>>(sq, (int)blocks);
   return cudaGetLastError();
+}
+
+size_t predict_sq_doubles() {
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return kSqPartials + 6 * (size_t)nsm * 8;
 }
 
 template <typename T>
@@ -892,9 +981,9 @@ cudaError_t launch_rows_prep(int S, const int* atom_start, const DevRows& rows, 
 }
 
 template cudaError_t launch_gram<double>(const double*, int, const double*, const double*, long long, int, double*,
-                                         double*, cudaStream_t);
+                                         double*, cudaStream_t, double*);
 template cudaError_t launch_gram<float>(const float*, int, const double*, const double*, long long, int, double*,
-                                        double*, cudaStream_t);
+                                        double*, cudaStream_t, double*);
 template cudaError_t launch_predict_sq<double>(const double*, int, const double*, long long, int, double*,
                                                const double*, const int*, double*, cudaStream_t);
 template cudaError_t launch_predict_sq<float>(const float*, int, const double*, long long, int, double*, const double*,

@@ -99,7 +99,8 @@ __global__ void __launch_bounds__(256) k_split_bf16(const T* __restrict__ X, int
 // quarter (32 columns) of the tile.
 __global__ void __launch_bounds__(kGramThreads, 1)
     k_gram_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo, int nt,
-              int ntile, int nk, int kps, int flush, int D, double* __restrict__ G, int* __restrict__ err) {
+              int ntile, int nk, int kps, int flush, int D, double* __restrict__ G, int* __restrict__ err,
+              int skip_loads, long long wait_limit) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* tiles = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = reinterpret_cast<uint64_t*>(tiles + kStages * kStageBytes);
@@ -145,9 +146,9 @@ __global__ void __launch_bounds__(kGramThreads, 1)
   if (warp == 0 && lane == 0) {
     // producer: A = features of tile ti, B = features of tile tj
     int issued = 0;
-    for (int k = 0; k < nkl; ++k) {
+    for (int k = 0; k < (skip_loads ? 0 : nkl); ++k) {
       const int s = k % kStages;
-      if (k >= kStages && !mbar_wait(&empty[s], ((k / kStages) - 1) & 1)) {
+      if (k >= kStages && !mbar_wait(&empty[s], ((k / kStages) - 1) & 1, wait_limit)) {
         ok = false;
         break;
       }
@@ -161,12 +162,12 @@ __global__ void __launch_bounds__(kGramThreads, 1)
       issued = k + 1;
     }
     // the copies issued last may still be in flight: wait for them (bounded) before leaving
-    for (int k = max(0, issued - kStages); k < issued; ++k) mbar_wait(&full[k % kStages], (k / kStages) & 1);
+    for (int k = max(0, issued - kStages); k < issued; ++k) mbar_wait(&full[k % kStages], (k / kStages) & 1, wait_limit);
   } else if (warp == 1 && lane == 0) {
     // MMA issuer: K-slice group g accumulates into TMEM buffer g & 1
     for (int g = 0; g < ngrp && ok; ++g) {
       const int b = g & 1;
-      if (g >= 2 && !mbar_wait(&tempty[b], ((g >> 1) - 1) & 1)) {
+      if (g >= 2 && !mbar_wait(&tempty[b], ((g >> 1) - 1) & 1, wait_limit)) {
         ok = false;
         break;
       }
@@ -175,7 +176,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
       const int k1 = min(nkl, (g + 1) * flush);
       for (int k = g * flush; k < k1; ++k) {
         const int s = k % kStages;
-        if (!mbar_wait(&full[s], (k / kStages) & 1)) {
+        if (!mbar_wait(&full[s], (k / kStages) & 1, wait_limit)) {
           ok = false;
           break;
         }
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
     bool got = true;
     for (int g = 0; g < ngrp; ++g) {
       const int b = g & 1;
-      if (!mbar_wait(&tfull[b], (g >> 1) & 1)) {
+      if (!mbar_wait(&tfull[b], (g >> 1) & 1, wait_limit)) {
         got = false;
         break;
       }
@@ -252,6 +253,18 @@ __global__ void __launch_bounds__(kGramThreads, 1)
 }
 
 // ---------------------------------------------------------------------------------------
+// Test hook of the timeout path: with skip_loads the producer issues no TMA loads, so the MMA
+// and epilogue warps' bounded waits expire (after wait_limit clocks), the CTA reports *err = 1
+// and frees its TMEM.  (0, 0) restores normal operation.
+namespace {
+int g_skip_loads = 0;
+long long g_wait_limit = ptx::kWaitLimit;
+}  // namespace
+void gram_tc_test_timeout(int skip_loads, long long wait_limit) {
+  g_skip_loads = skip_loads ? 1 : 0;
+  g_wait_limit = wait_limit > 0 ? wait_limit : ptx::kWaitLimit;
+}
+
 size_t gram_tc_min_workspace(int D) { return (size_t)4 * D * kTK + 256; }
 
 bool gram_tc_available() { return tc::encode_fn() != nullptr; }
@@ -292,7 +305,7 @@ cudaError_t launch_gram_tc(const T* X, int ldx, int c0, int D, const double* w, 
     const int kps = (nk + nsplit - 1) / nsplit;
     nsplit = (nk + kps - 1) / kps;  // every split non-empty
     k_gram_tc<<<(unsigned)(ntile * nsplit), kGramThreads, kGramSmem, st>>>(mh, ml, nt, ntile, nk, kps, kFlush, D, G,
-                                                                           err);
+                                                                           err, g_skip_loads, g_wait_limit);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

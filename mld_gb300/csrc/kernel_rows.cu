@@ -148,6 +148,29 @@ struct KrrTile {
   static constexpr int RI = 6;        // rows per thread per pass (96 rows per pass)
 };
 
+// Sum the per-thread partials part[q][j] (column tx + 16 j of output row q) of the 16 thread rows
+// ty of a 256-thread CTA into red[q * NZ + k] in a fixed order: the two rows of a warp through a
+// shuffle (a + b is exact-symmetric), then the 8 warps in warp order through red8 (8 * Q * NZ).
+template <typename T, int Q, int CJ, int NZ>
+__device__ __forceinline__ void reduce_rows16(T (&part)[Q][CJ], T* red8, T* red) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, tx = tid & 15;
+#pragma unroll
+  for (int q = 0; q < Q; ++q)
+#pragma unroll
+    for (int j = 0; j < CJ; ++j) part[q][j] += __shfl_xor_sync(0xffffffffu, part[q][j], 16);
+  if (lane < 16)
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+#pragma unroll
+      for (int j = 0; j < CJ; ++j) red8[((size_t)warp * Q + q) * NZ + tx + 16 * j] = part[q][j];
+  __syncthreads();
+  for (int e = tid; e < Q * NZ; e += 256) {
+    T sum = T(0);
+    for (int w = 0; w < 8; ++w) sum += red8[(size_t)w * Q * NZ + e];
+    red[e] = sum;
+  }
+}
+
 template <typename T, int NZ_>
 __global__ void __launch_bounds__(256) k_krr_force_tiled(
     int KK, int nk, int A, int atoms_per_cta, int vc, const int* __restrict__ atom_struct,
@@ -163,7 +186,8 @@ __global__ void __launch_bounds__(256) k_krr_force_tiled(
   T* gx = Vt + (size_t)KK * 3 * vc;                    // 3 vc
   T* red = gx + 3 * vc;                                // 3 * NZ
   T* cf = red + 3 * NZ;                                // vc * NZ * 2 (c1, c2 per centre)
-  int* cen = reinterpret_cast<int*>(cf + (size_t)2 * vc * NZ);  // vc
+  T* red8 = cf + (size_t)2 * vc * NZ;                  // 8 * 3 * NZ (fixed-order reduction)
+  int* cen = reinterpret_cast<int*>(red8 + (size_t)8 * 3 * NZ);  // vc
   const T s2t = (T)s2, l2t = (T)l2, pt = (T)p;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int k0 = blockIdx.x * NZ;
@@ -264,11 +288,7 @@ __global__ void __launch_bounds__(256) k_krr_force_tiled(
       }
     }
     }  // vector chunks
-#pragma unroll
-    for (int al = 0; al < 3; ++al)
-#pragma unroll
-      for (int j = 0; j < CJ; ++j)
-        if (part[al][j] != T(0)) atomicAdd(&red[al * NZ + tx + 16 * j], part[al][j]);
+    reduce_rows16<T, 3, CJ, NZ>(part, red8, red);
     __syncthreads();
     const long long row = rowF[s] + 3LL * (a - atom_start[s]);
     for (int e = tid; e < 3 * nkt; e += 256) {
@@ -341,6 +361,7 @@ __global__ void __launch_bounds__(256) k_krr_stress_tiled(
   T* Vt = Zs + (size_t)KK * NZ;       // KK * RB  [c][r]
   T* red = Vt + (size_t)KK * RB;      // 6 * NZ
   T* cf = red + 6 * NZ;               // 16 atoms * NZ * 2
+  T* red8 = cf + (size_t)2 * 16 * NZ; // 8 * 6 * NZ (fixed-order reduction)
   const T s2t = (T)s2, l2t = (T)l2, pt = (T)p;
   const int tid = threadIdx.x, txi = tid & 15, ty = tid >> 4;
   const int k0 = blockIdx.x * NZ;
@@ -414,11 +435,7 @@ __global__ void __launch_bounds__(256) k_krr_stress_tiled(
         }
       }
     }
-#pragma unroll
-    for (int q = 0; q < 6; ++q)
-#pragma unroll
-      for (int j = 0; j < CJ; ++j)
-        if (part[q][j] != T(0)) atomicAdd(&red[q * NZ + txi + 16 * j], part[q][j]);
+    reduce_rows16<T, 6, CJ, NZ>(part, red8, red);
     __syncthreads();
     const double sc = sign_stress * 3.0 / volume[s];
     for (int e = tid; e < 6 * nkt; e += 256) {
@@ -479,7 +496,7 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
     const int maxnv = b.maxnn + 1;
     auto smem_for = [&](int nz, int vc) {
       return sizeof(T) * ((size_t)KK * nz + (size_t)KK * 3 * vc + 3 * (size_t)vc + 3 * (size_t)nz +
-                          (size_t)2 * vc * nz) +
+                          (size_t)2 * vc * nz + (size_t)8 * 3 * nz) +
              sizeof(int) * vc + 16;
     };
     // FP32 tiles up to 256 reference points, FP64 up to 64 (register budget of the 6 x NZ/16 tile),
@@ -523,7 +540,8 @@ cudaError_t launch_krr_rows(const DevBatch& b, const DevRows& rows, const int* r
       cudaDeviceGetAttribute(&optin2, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     }
     auto smem_for = [&](int nz) {
-      return sizeof(T) * ((size_t)KK * nz + (size_t)KK * 96 + 6 * (size_t)nz + (size_t)2 * 16 * nz) + 16;
+      return sizeof(T) * ((size_t)KK * nz + (size_t)KK * 96 + 6 * (size_t)nz + (size_t)2 * 16 * nz + (size_t)8 * 6 * nz) +
+             16;
     };
     int nz = 0;
     for (int cand : {256, 128, 64, 32})

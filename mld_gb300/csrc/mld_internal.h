@@ -43,19 +43,33 @@ struct YSlot {
   uint8_t pad;
 };
 
-// One lane of a phase-2 round, self-contained so that a lane fetches its work with one 32-byte
-// load: the Z term (c indices of its first product, CG offsets, loop extents and strides) and
-// its slot (Y position, c index of the slot's (j,p,q) for B, triple, scale); wgt = 0 marks a
-// padding lane.
+// One lane of a phase-2 round (16 bytes): the Z term's c indices of its first product, CG
+// offsets, loop extents and strides, and the term's index in the per-atom term buffer
+// (kNoTerm marks a padding lane).
 struct alignas(16) ZItem {
   uint16_t i1, i2, cg1, cg2;  // first (ma,mb) c index / matching second factor, CG offsets
   uint8_t na, nb, s1, s2;     // loop extents and layer strides (j+1)
-  uint16_t ypos, ufull, k;    // slot: Y position, c index of its (j,p,q), triple
-  uint8_t wgt, is_a;          // fold weight, ZA flag
-  uint8_t snum, sden;         // scale snum / sden (formed in the kernel's precision)
-  uint8_t pad[10];
+  uint16_t term;              // index of the term (its Z value) in the term buffer
+  uint16_t pad;
 };
-static_assert(sizeof(ZItem) == 32, "phase-2 entries are 32 bytes");
+static_assert(sizeof(ZItem) == 16, "phase-2 entries are 16 bytes");
+constexpr uint16_t kNoTerm = 0xFFFF;
+
+// One folded Y slot for the kernel (16 bytes): Y[ypos] = wgt * sum_t (snum_t / sden_t) Z[term_t].
+struct SlotEntry {
+  uint16_t term[3];
+  uint16_t ypos;
+  uint8_t nterm, wgt;
+  uint8_t snum[3], sden[3];
+};
+static_assert(sizeof(SlotEntry) == 16, "slot entries are 16 bytes");
+
+// One ZA half entry of a triple: B_k = sum over its entries of wgt * Re(conj(c[ufull]) Z[term]).
+struct BkItem {
+  uint16_t term, ufull;
+  uint8_t wgt, pad[3];
+};
+static_assert(sizeof(BkItem) == 8, "B items are 8 bytes");
 
 // Packed per-entry recursion record of the half layers (one 16-byte load per entry).
 struct RecEntry32 {
@@ -70,7 +84,8 @@ struct RecEntry64 {
   int64_t pad;
 };
 
-constexpr int kZWarps = 8;  // warps of the phase-2 schedule (= warps of a k_bso4 CTA)
+constexpr int kZWarps = 8;   // warps of the phase-2 schedule (= warps of a k_bso4 CTA)
+constexpr int kRounds = 3;   // contraction rounds: a triple has at most one Y row per round
 
 // Host-built constant tables of the SO(4) bispectrum for a given j_max.
 struct Bso4Tables {
@@ -79,16 +94,19 @@ struct Bso4Tables {
   int J = 0, NU = 0, HU = 0, K = 0, NYP = 0;
   int off[kMaxJ + 2] = {0};     // full-layer offsets
   int hoff[kMaxJ + 2] = {0};    // half-layer offsets
-  int Mp[kMaxJ + 1] = {0};      // padded row count per layer (multiple of kRowTile)
+  int Mp[kMaxJ + 1] = {0};      // padded row count per layer (multiple of kRowTile per round group)
   int yoff[kMaxJ + 1] = {0};    // Y offset of each layer block (complex elements)
   std::vector<int> l1, l2, l;   // triples (reference order)
   std::vector<double> cg;       // 1-D CG coefficient lists
   std::vector<ZTerm> zterms;    // ZA/ZB/ZC outputs on half layers
   std::vector<YSlot> yslots;    // folded slots
-  std::vector<int> yorder;      // slot evaluation order (cost-descending)
+  std::vector<SlotEntry> slots; // the same slots in the kernel's form
+  std::vector<int> bk_off;      // K + 1 offsets into bk_items
+  std::vector<BkItem> bk_items; // ZA entries of each triple
   std::vector<int16_t> rowk;    // per layer-block row: triple index or -1 (padding)
   int rowk_off[kMaxJ + 2] = {0};  // offset of each layer's rows in rowk
-  std::vector<int> tiles;       // row tiles (j << 8 | rt), cost-descending
+  std::vector<int> tiles;       // row tiles (j << 8 | rt), by round, heaviest layers first
+  int tile_off[kRounds + 1] = {0};  // tiles of round r: [tile_off[r], tile_off[r + 1])
   // recursion on half layers: U = tz*Zsel*U[src_z] + tx*(-i)*Xsel*U[src_x]
   std::vector<double> rec_tz, rec_tx;
   std::vector<int16_t> rec_sz, rec_sx;
@@ -105,32 +123,26 @@ double cg_coefficient(int j1, int m1, int j2, int m2, int j, int m);  // doubled
 
 // Device copies of the tables.
 struct DevTables {
-  int J = 0, NU = 0, HU = 0, K = 0, NS = 0, NYP = 0, NTILE = 0;
+  int J = 0, NU = 0, HU = 0, K = 0, NS = 0, NYP = 0, NTILE = 0, NZT = 0, NROWS = 0;
   int NCG = 0;  // entries of the 1-D CG coefficient table
   int hoff[kMaxJ + 2] = {0};
   int Mp[kMaxJ + 1] = {0};
   int yoff[kMaxJ + 1] = {0};
   int rowk_off[kMaxJ + 2] = {0};
-  ZTerm* zterms = nullptr;
-  YSlot* yslots = nullptr;
-  int* yorder = nullptr;
+  int tile_off[kRounds + 1] = {0};
   int16_t* rowk = nullptr;
   int* tiles = nullptr;
   double* cg64 = nullptr;
   float* cg32 = nullptr;
-  double* rec_tz64 = nullptr;
-  double* rec_tx64 = nullptr;
-  float* rec_tz32 = nullptr;
-  float* rec_tx32 = nullptr;
-  int16_t* rec_sz = nullptr;
-  int16_t* rec_sx = nullptr;
-  int8_t* rec_qneg = nullptr;
   int16_t* expand = nullptr;
   int8_t* half_diag = nullptr;
   RecEntry32* rec32 = nullptr;  // packed recursion records (FP32 method)
   RecEntry64* rec64 = nullptr;  // packed recursion records (FP64 method)
   ZItem* zitems = nullptr;
   int* zitem_off = nullptr;     // kZWarps + 1
+  SlotEntry* slots = nullptr;   // NS
+  int* bk_off = nullptr;        // K + 1
+  BkItem* bk_items = nullptr;
 };
 
 // Packed recursion records from the table vectors.
@@ -141,6 +153,51 @@ inline void pack_recursion(const Bso4Tables& t, std::vector<RecEntry32>* r32, st
     (*r32)[h] = RecEntry32{(float)t.rec_tz[h], (float)t.rec_tx[h], t.rec_sz[h], t.rec_sx[h], (int32_t)t.rec_qneg[h]};
     (*r64)[h] = RecEntry64{t.rec_tz[h], t.rec_tx[h], t.rec_sz[h], t.rec_sx[h], (int32_t)t.rec_qneg[h], 0};
   }
+}
+
+// Fill the scalar part of *d from t and place every device table through put(vector, &ptr),
+// which allocates (or carves) device memory of the vector's size and copies it there.
+template <class Put>
+cudaError_t fill_dev_tables(const Bso4Tables& t, DevTables* d, Put put) {
+  *d = DevTables();
+  d->J = t.J;
+  d->NU = t.NU;
+  d->HU = t.HU;
+  d->K = t.K;
+  d->NS = (int)t.slots.size();
+  d->NYP = t.NYP;
+  d->NTILE = (int)t.tiles.size();
+  d->NZT = (int)t.zterms.size();
+  d->NROWS = (int)t.rowk.size();
+  d->NCG = (int)t.cg.size();
+  for (int j = 0; j <= t.J + 1; ++j) {
+    d->hoff[j] = t.hoff[j];
+    d->rowk_off[j] = t.rowk_off[j];
+  }
+  for (int j = 0; j <= t.J; ++j) {
+    d->Mp[j] = t.Mp[j];
+    d->yoff[j] = t.yoff[j];
+  }
+  for (int r = 0; r <= kRounds; ++r) d->tile_off[r] = t.tile_off[r];
+  std::vector<float> cg32(t.cg.begin(), t.cg.end());
+  std::vector<RecEntry32> r32;
+  std::vector<RecEntry64> r64;
+  pack_recursion(t, &r32, &r64);
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = put(t.rowk, &d->rowk);
+  if (e == cudaSuccess) e = put(t.tiles, &d->tiles);
+  if (e == cudaSuccess) e = put(t.cg, &d->cg64);
+  if (e == cudaSuccess) e = put(cg32, &d->cg32);
+  if (e == cudaSuccess) e = put(t.expand, &d->expand);
+  if (e == cudaSuccess) e = put(t.half_diag, &d->half_diag);
+  if (e == cudaSuccess) e = put(r32, &d->rec32);
+  if (e == cudaSuccess) e = put(r64, &d->rec64);
+  if (e == cudaSuccess) e = put(t.zitems, &d->zitems);
+  if (e == cudaSuccess) e = put(t.zitem_off, &d->zitem_off);
+  if (e == cudaSuccess) e = put(t.slots, &d->slots);
+  if (e == cudaSuccess) e = put(t.bk_off, &d->bk_off);
+  if (e == cudaSuccess) e = put(t.bk_items, &d->bk_items);
+  return e;
 }
 
 // Per-batch structure description on the device.
@@ -196,45 +253,65 @@ cudaError_t launch_neighbours(const DevBatch& b, double rcut, int* counts, int* 
 cudaError_t launch_scan(const int* in, int* out, int n, int* d_tmp, cudaStream_t st);
 
 // Y scratch the descriptor kernel needs in global memory for up to max_ctas CTAs (0 when Y fits
-// in shared memory); pass it to launch_bso4_rows, which then runs that many persistent CTAs.
+// in shared memory); pass it to launch_bso4, which then runs at most that many persistent CTAs.
 size_t bso4_y_scratch_bytes(const DevTables& tb, int nch, int eb, int max_ctas);
-// Evaluation with fitted weights instead of design rows: the energy, forces and stress that
-// the rows times the weights would give, formed from the per-atom effective weights
-// beta_a = dE/dB_a (w_lin for the linear model; w_lin + (W + W^T) B_a for the quadratic one).
+// Evaluation with fitted weights instead of design rows: per-pair force and stress
+// contributions of dE/dB_a (beta_a = w_lin for the linear model; w_lin + (W + W^T) B_a for the
+// quadratic one), gathered into E/F/S by launch_eval_gather.
 template <typename T>
 struct DevEval {
   const T* beta = nullptr;       // one vector (nch*K) or one per atom (A x nch*K)
   int beta_per_atom = 0;
-  const double* wlin = nullptr;  // linear weights: the kernel adds w0 + w_lin . B_a to E (linear model)
+  const double* wlin = nullptr;  // linear weights: the kernel writes Eatom = w0 + w_lin . B_a (linear model)
   double w0 = 0.0;
-  double* F = nullptr;           // 3A forces, accumulated (zeroed by the caller)
-  double* S = nullptr;           // 6S stress rows' predictions, accumulated
-  double* E = nullptr;           // S energies, accumulated
+  double* pair = nullptr;        // P x 9: force contribution f_q (3), stress contribution (6: xx yy zz yz xz xy)
+  double* Eatom = nullptr;       // A: energy of each atom (linear model; may be null)
 };
 
+// Descriptor kernel (bispectrum.cu): B (A x nch*K) and w_ch * dB (P x 3 x nch*K) of the batch,
+// either may be null; or evaluation (ev->pair set, dBout null).  Atoms are taken in `order`
+// (null: index order) through `counter` (one int of device memory, reset by the launch).
 template <typename T>
-cudaError_t launch_bso4_rows(const DevTables& tb, const DevBatch& b, const DevRows& rows, const BsoParams& p,
-                             T* X, T* Bout, T* dBout, int want_rows, cudaStream_t st, void* yscratch = nullptr,
-                             size_t yscratch_bytes = 0, const DevEval<T>* ev = nullptr);
-// beta_a = w_lin + Wsym B_a and E_s += sum_a (w0 + B_a . (beta_a + w_lin) / 2)   (eval.cu)
+cudaError_t launch_bso4(const DevTables& tb, const DevBatch& b, const BsoParams& p, T* Bout, T* dBout,
+                        const DevEval<T>* ev, const int* order, int* counter, cudaStream_t st,
+                        void* yscratch = nullptr, size_t yscratch_bytes = 0);
+// Linear design rows of the batch from B, w_ch * dB and the reverse pairs (rows.cu); Sp is a
+// workspace of A x 6 x KK stress partials.  Columns [1, 1 + KK) of the energy, force and stress
+// rows are written.
 template <typename T>
-cudaError_t launch_eval_beta(const T* B, int A, int nchK, const double* wlin, const double* wsym, double w0,
-                             const int* atom_struct, T* beta, double* E, cudaStream_t st);
+cudaError_t launch_lin_rows(const DevBatch& b, const DevRows& rows, const BsoParams& p, int KK, const int* rev,
+                            const T* B, const T* dB, T* Sp, T* X, cudaStream_t st);
+// E (S; from Eatom when given), F (3A) and S (6S) from the per-pair contributions of evaluation.
+cudaError_t launch_eval_gather(const DevBatch& b, const BsoParams& p, const int* rev, const double* pair,
+                               const double* Eatom, double* E, double* F, double* S, cudaStream_t st);
+// Atoms ordered by descending neighbour count (the descriptor kernel's queue); tmp holds
+// atom_order_tmp_ints(maxnn) ints.
+size_t atom_order_tmp_ints(int maxnn);
+cudaError_t launch_atom_order(const int* nn, int A, int maxnn, int* order, int* tmp, cudaStream_t st);
+// beta_a = w_lin + Wsym B_a and Eatom_a = w0 + B_a . (beta_a + w_lin) / 2   (eval.cu)
+template <typename T>
+cudaError_t launch_eval_beta(const T* B, int A, int nchK, const double* wlin, const double* wsym, double w0, T* beta,
+                             double* Eatom, cudaStream_t st);
 
+// FP64 Gram and rhs on the CUDA cores; with ws (gram_workspace_doubles(M, D) doubles) the
+// row-chunk partials are summed in a fixed order (bitwise reproducible), else with atomics
+size_t gram_workspace_doubles(long long M, int D);
 template <typename T>
 cudaError_t launch_gram(const T* X, int ldx, const double* w, const double* y, long long M, int D, double* G,
-                        double* h, cudaStream_t st);
+                        double* h, cudaStream_t st, double* ws = nullptr);
 cudaError_t launch_solve_sym(double* G, const double* h, int D, double lambda, double rcond, double* wout,
                              double* evals, int* info, cudaStream_t st);
 template <typename T>
 cudaError_t launch_rhs(const T* X, int ldx, const double* w, const double* y, long long M, int D, double* h,
-                       int nsm, cudaStream_t st, float2* sv);
+                       int nsm, cudaStream_t st, float2* sv, double* ws = nullptr);
 cudaError_t launch_symmetrize(double* G, int D, cudaStream_t st);
 cudaError_t launch_weighted_sumsq(const double* w, const double* y, long long M, double* out, cudaStream_t st);
 cudaError_t launch_split_weights(const double* w, long long M, float2* wds, cudaStream_t st);
 cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const double* w, const double* p, long long M,
                                  double lambda, float2* sv, double* q, int nsm, cudaStream_t st, int* launches,
                                  int* err);
+// doubles of the squared-error buffer of launch_predict_sq (3 sums, 3 counts, per-CTA partials)
+size_t predict_sq_doubles();
 template <typename T>
 cudaError_t launch_predict_sq(const T* X, int ldx, const double* w, long long M, int D, double* pred, const double* y,
                               const int* kind, double* sq, cudaStream_t st);
@@ -307,6 +384,7 @@ cudaError_t launch_krr_force_tc(const DevBatch& b, const DevRows& rows, const in
 
 // tensor-core Gram in BF16 split precision (gram_tc.cu)
 size_t gram_tc_min_workspace(int D);
+void gram_tc_test_timeout(int skip_loads, long long wait_limit);
 bool gram_tc_available();
 template <typename T>
 cudaError_t launch_gram_tc(const T* X, int ldx, int c0, int D, const double* w, long long M, double* G, void* ws,

@@ -15,17 +15,24 @@
 
 namespace mld {
 
-// FP32 positions and fractional coordinates of every atom for the pre-filter.
-__global__ void k_nbr_prep(int A, const int* __restrict__ atom_struct, const double* __restrict__ pos,
-                           const double* __restrict__ recip, float4* __restrict__ pos32,
-                           float4* __restrict__ frac32) {
+// FP32 positions and fractional coordinates of every atom for the pre-filter.  Positions are
+// taken relative to the structure's first atom and fractional coordinates are wrapped into [0, 1)
+// in FP64 before the FP32 rounding, so that their FP32 error stays of order 1e-7 of the cell
+// size even for unwrapped coordinates far from the origin (the pre-filter's band is 1e-3 A).
+__global__ void k_nbr_prep(int A, const int* __restrict__ atom_struct, const int* __restrict__ atom_start,
+                           const double* __restrict__ pos, const double* __restrict__ recip,
+                           float4* __restrict__ pos32, float4* __restrict__ frac32) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= A) return;
-  const double* bg = recip + 9 * (size_t)atom_struct[i];
+  const int s = atom_struct[i];
+  const double* bg = recip + 9 * (size_t)s;
+  const double* o = pos + 3 * (size_t)atom_start[s];
   const double x0 = pos[3 * (size_t)i], x1 = pos[3 * (size_t)i + 1], x2 = pos[3 * (size_t)i + 2];
-  pos32[i] = make_float4((float)x0, (float)x1, (float)x2, 0.f);
-  frac32[i] = make_float4((float)(x0 * bg[0] + x1 * bg[1] + x2 * bg[2]), (float)(x0 * bg[3] + x1 * bg[4] + x2 * bg[5]),
-                          (float)(x0 * bg[6] + x1 * bg[7] + x2 * bg[8]), 0.f);
+  pos32[i] = make_float4((float)(x0 - o[0]), (float)(x1 - o[1]), (float)(x2 - o[2]), 0.f);
+  const double f0 = x0 * bg[0] + x1 * bg[1] + x2 * bg[2];
+  const double f1 = x0 * bg[3] + x1 * bg[4] + x2 * bg[5];
+  const double f2 = x0 * bg[6] + x1 * bg[7] + x2 * bg[8];
+  frac32[i] = make_float4((float)(f0 - floor(f0)), (float)(f1 - floor(f1)), (float)(f2 - floor(f2)), 0.f);
 }
 
 // periodic image (n1, n2, n3), |n| < 128, packed in one int
@@ -258,7 +265,8 @@ cudaError_t launch_neighbours(const DevBatch& b, double rcut, int* counts, int* 
   const long long warps = b.A;
   const int blocks = (int)((warps * 32 + threads - 1) / threads);
   if (!b.pos32 || !b.frac32) return cudaErrorInvalidValue;
-  if (pass == 0) k_nbr_prep<<<(b.A + 255) / 256, 256, 0, st>>>(b.A, b.atom_struct, b.pos, b.recip, b.pos32, b.frac32);
+  if (pass == 0)
+    k_nbr_prep<<<(b.A + 255) / 256, 256, 0, st>>>(b.A, b.atom_struct, b.atom_start, b.pos, b.recip, b.pos32, b.frac32);
   k_neighbours<<<blocks, threads, 0, st>>>(b.A, b.atom_struct, b.atom_start, b.pos, b.pos32, b.frac32, b.cell,
                                            b.recip, b.small, b.nsize, rcut, pass, counts, maxcount, b.nbr_off,
                                            b.nbr_idx, b.nbr_u);

@@ -60,6 +60,7 @@ void set_err(char* err, int len, const std::string& msg) {
 
 template <typename V>
 cudaError_t put(unsigned char* base, size_t* off, const std::vector<V>& v, V** dst) {
+  // synchronous copy into the static array; callers have waited for earlier calls' kernels
   *off = align256(*off);
   *dst = reinterpret_cast<V*>(base + *off);
   const size_t bytes = sizeof(V) * v.size();
@@ -85,54 +86,19 @@ int noalloc_setup(int dev, double j_max, DeviceState** out, std::string* msg) {
   if (S.j_max != j_max) {
     Bso4Tables t;
     if (!build_bso4_tables(j_max, &t, msg)) return MLD_ERR_INVALID;
-    DevTables& d = S.dt;
-    d = DevTables();
-    d.J = t.J;
-    d.NU = t.NU;
-    d.HU = t.HU;
-    d.K = t.K;
-    d.NS = (int)t.yslots.size();
-    d.NYP = t.NYP;
-    d.NTILE = (int)t.tiles.size();
-    d.NCG = (int)t.cg.size();
-    for (int j = 0; j <= t.J + 1; ++j) {
-      d.hoff[j] = t.hoff[j];
-      d.rowk_off[j] = t.rowk_off[j];
+    if (S.j_max >= 0.0) {
+      // A previous call's kernels may still read the old tables (and the per-call region behind
+      // them) on whatever stream that call was given; the synchronous copies below run on the
+      // legacy default stream, which does not wait for non-blocking streams.  Wait for the
+      // whole device before overwriting.
+      cudaError_t e = cudaDeviceSynchronize();
+      if (e != cudaSuccess) {
+        *msg = std::string("cudaDeviceSynchronize before the table re-upload: ") + cudaGetErrorString(e);
+        return MLD_ERR_CUDA;
+      }
     }
-    for (int j = 0; j <= t.J; ++j) {
-      d.Mp[j] = t.Mp[j];
-      d.yoff[j] = t.yoff[j];
-    }
-    std::vector<float> cg32(t.cg.begin(), t.cg.end());
-    std::vector<float> tz32(t.rec_tz.begin(), t.rec_tz.end()), tx32(t.rec_tx.begin(), t.rec_tx.end());
     size_t off = 0;
-    cudaError_t e = cudaSuccess;
-#define PUT(vec, dst) \
-  if (e == cudaSuccess) e = put(S.base, &off, vec, &dst)
-    PUT(t.zterms, d.zterms);
-    PUT(t.yslots, d.yslots);
-    PUT(t.yorder, d.yorder);
-    PUT(t.rowk, d.rowk);
-    PUT(t.tiles, d.tiles);
-    PUT(t.cg, d.cg64);
-    PUT(cg32, d.cg32);
-    PUT(t.rec_tz, d.rec_tz64);
-    PUT(t.rec_tx, d.rec_tx64);
-    PUT(tz32, d.rec_tz32);
-    PUT(tx32, d.rec_tx32);
-    PUT(t.rec_sz, d.rec_sz);
-    PUT(t.rec_sx, d.rec_sx);
-    PUT(t.rec_qneg, d.rec_qneg);
-    PUT(t.expand, d.expand);
-    PUT(t.half_diag, d.half_diag);
-    std::vector<RecEntry32> r32;
-    std::vector<RecEntry64> r64;
-    pack_recursion(t, &r32, &r64);
-    PUT(r32, d.rec32);
-    PUT(r64, d.rec64);
-    PUT(t.zitems, d.zitems);
-    PUT(t.zitem_off, d.zitem_off);
-#undef PUT
+    cudaError_t e = fill_dev_tables(t, &S.dt, [&](const auto& vec, auto** dst) { return put(S.base, &off, vec, dst); });
     if (e != cudaSuccess) {
       *msg = std::string("table upload into the scratch array: ") + cudaGetErrorString(e);
       S.j_max = -1.0;
@@ -233,6 +199,10 @@ extern "C" int mld_gpu_descriptors_noalloc(const mld_gpu_config* cfg, int nat, c
     const int nc = (int)(2.0 * cfg->r_cut / bval) + 1;
     if (nc > 1) hb.small = 1;
     hb.nsize[i] = nc / 2 + 1;
+    if (hb.nsize[i] > 127) {
+      set_err(err, err_len, "cell too thin for r_cut: more than 127 periodic images along a lattice vector");
+      return MLD_ERR_INVALID;
+    }
   }
 
   // carve the per-call region after the tables
@@ -261,6 +231,7 @@ extern "C" int mld_gpu_descriptors_noalloc(const mld_gpu_config* cfg, int nat, c
   b.frac32 = reinterpret_cast<float4*>(take(sizeof(float4) * nat));
   int* scan_tmp = reinterpret_cast<int*>(take(sizeof(int) * ((nat + 1023) / 1024 + 2)));
   int* dmax = reinterpret_cast<int*>(take(sizeof(int) * 2));
+  int* qcount = reinterpret_cast<int*>(take(sizeof(int)));  // descriptor kernel's queue counter
   float* bstage = mixed ? reinterpret_cast<float*>(take(sizeof(float) * (size_t)nat * KK)) : nullptr;
   // global Y slices of the descriptor kernel when they do not fit in shared memory (FP64 with
   // several channels); at most 64 persistent CTAs
@@ -328,16 +299,13 @@ extern "C" int mld_gpu_descriptors_noalloc(const mld_gpu_config* cfg, int nat, c
   prm.rin_width = cfg->r_cut_width_in;
   prm.sign_stress = cfg->sign_stress;
   prm.sign_big = cfg->sign_stress_big_box;
-  DevRows rows;  // no design rows on this path
-  rows.D = 1 + KK;
-  rows.ldx = round_up4(rows.D);
   if (mixed) {
-    CKN(launch_bso4_rows<float>(dt, b, rows, prm, (float*)nullptr, bstage, (float*)nullptr, 0, st, yscr, ysb));
+    CKN(launch_bso4<float>(dt, b, prm, bstage, (float*)nullptr, nullptr, nullptr, qcount, st, yscr, ysb));
     const size_t n = (size_t)nat * KK;
     k_widen<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(bstage, B, n);
     CKN(cudaGetLastError());
   } else {
-    CKN(launch_bso4_rows<double>(dt, b, rows, prm, (double*)nullptr, B, (double*)nullptr, 0, st, yscr, ysb));
+    CKN(launch_bso4<double>(dt, b, prm, B, (double*)nullptr, nullptr, nullptr, qcount, st, yscr, ysb));
   }
 #undef CKN
   return MLD_OK;

@@ -52,11 +52,11 @@ __device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity) 
   }
   return true;
 }
-// bounded wait for the phase of the given parity; false on expiry
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// bounded wait for the phase of the given parity; false on expiry (after `limit` SM clocks)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = kWaitLimit) {
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitLimit) return false;
+    if (clock64() - t0 > limit) return false;
   }
   return true;
 }

@@ -9,14 +9,16 @@
 // order, admitted while the batch stays within the slot's share of the HBM budget and the atom
 // cap.  Batches in different slots run concurrently on their streams, so requests that arrive
 // while others are on the GPU start as soon as a slot and memory free up.  A request whose own
-// size exceeds the per-slot budget runs alone if it fits the whole budget, else it fails with
-// MLD_ERR_OOM.  Results of a structure do not depend on its batch partners beyond the order of
-// floating-point atomics in the row assembly.
+// size exceeds the per-slot share but fits the whole budget waits at the head of the queue
+// until every slot is idle, then runs alone: nothing else is launched while it is on the GPU,
+// and its slot's buffers are released when it retires, so the bytes on the device never exceed
+// the budget.  A request larger than the whole budget fails with MLD_ERR_OOM.
 #include <cuda_runtime.h>
 
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <algorithm>
 #include <deque>
 #include <string>
 #include <unordered_map>
@@ -30,6 +32,7 @@ int eval_launch(mld_gpu_handle* h, cudaEvent_t done, double** pinned_out);
 void eval_collect(const mld_gpu_handle* h, int s, double* E, double* F, double* Sout);
 int eval_weights_upload(mld_gpu_handle* h, const double* w_full);
 int handle_dims(const mld_gpu_handle* h, int* D, int* ldx, int* KK, int* nch);
+void handle_release_buffers(mld_gpu_handle* h);
 }  // namespace mld
 
 namespace {
@@ -57,6 +60,7 @@ struct Slot {
   cudaEvent_t done = nullptr;
   std::vector<long long> batch;
   bool busy = false;
+  double bytes = 0;  // estimated device bytes of the batch on the GPU
 };
 
 }  // namespace
@@ -72,6 +76,9 @@ struct mld_gpu_server {
   double budget = 0;  // bytes of HBM for the slots' batch buffers
   int D = 0, ldx = 0, KK = 0, nch = 1;
   long long batches = 0, atoms_done = 0;
+  int exclusive_slot = -1;       // slot running a request larger than the per-slot share
+  double peak_in_flight = 0;     // largest sum of the busy slots' estimated bytes
+  double largest_request = 0;    // largest estimated bytes of a request admitted so far
 };
 
 namespace {
@@ -95,7 +102,8 @@ double request_bytes(const mld_gpu_server* s, int nat, const double* cell) {
   return pairs * 36.0 + nat * (2.0 * s->KK * eb + 24.0 + 64.0) + 128.0;
 }
 
-void retire(mld_gpu_server* s, Slot& sl) {
+void retire(mld_gpu_server* s, int idx) {
+  Slot& sl = s->slots[idx];
   const cudaError_t q = cudaEventQuery(sl.done);
   if (q == cudaErrorNotReady) return;
   const double t = now_ms();
@@ -115,10 +123,26 @@ void retire(mld_gpu_server* s, Slot& sl) {
   if (q != cudaSuccess) s->err = std::string("batch failed: ") + cudaGetErrorString(q);
   sl.batch.clear();
   sl.busy = false;
+  sl.bytes = 0;
+  if (s->exclusive_slot == idx) {
+    // the slot grew its buffers past its share: give them back before others are admitted
+    mld::handle_release_buffers(sl.h);
+    s->exclusive_slot = -1;
+  }
 }
 
-int launch(mld_gpu_server* s, Slot& sl) {
+double bytes_in_flight(const mld_gpu_server* s) {
+  double b = 0;
+  for (const Slot& o : s->slots)
+    if (o.busy) b += o.bytes;
+  return b;
+}
+
+int launch(mld_gpu_server* s, int idx) {
+  Slot& sl = s->slots[idx];
+  if (s->exclusive_slot >= 0) return MLD_OK;  // an over-share request is running alone
   const double share = s->budget / std::max<size_t>(1, s->slots.size());
+  bool exclusive = false;
   double used = 0;
   long long atoms = 0;
   std::vector<long long> batch;
@@ -133,6 +157,11 @@ int launch(mld_gpu_server* s, Slot& sl) {
       r.err = MLD_ERR_OOM;
       r.t_done = now_ms();
       continue;
+    }
+    if (first && r.bytes > share) {
+      // runs alone: hold it at the head (and launch nothing else) until every slot is idle
+      if (bytes_in_flight(s) > 0) return MLD_OK;
+      exclusive = true;
     }
     batch.push_back(id);
     used += r.bytes;
@@ -171,6 +200,10 @@ int launch(mld_gpu_server* s, Slot& sl) {
   }
   sl.batch = std::move(batch);
   sl.busy = true;
+  sl.bytes = used;
+  if (exclusive) s->exclusive_slot = idx;
+  s->peak_in_flight = std::max(s->peak_in_flight, bytes_in_flight(s));
+  s->largest_request = std::max(s->largest_request, used);
   ++s->batches;
   return MLD_OK;
 }
@@ -249,11 +282,11 @@ int mld_gpu_server_submit(mld_gpu_server* s, int nat, const double* pos, const d
 
 int mld_gpu_server_progress(mld_gpu_server* s, int* n_busy, int* n_queued) {
   if (!s) return MLD_ERR_INVALID;
-  for (Slot& sl : s->slots)
-    if (sl.busy) retire(s, sl);
-  for (Slot& sl : s->slots)
-    if (!sl.busy && !s->queue.empty()) {
-      const int rc = launch(s, sl);
+  for (size_t i = 0; i < s->slots.size(); ++i)
+    if (s->slots[i].busy) retire(s, (int)i);
+  for (size_t i = 0; i < s->slots.size(); ++i)
+    if (!s->slots[i].busy && !s->queue.empty()) {
+      const int rc = launch(s, (int)i);
       if (rc != MLD_OK) return rc;
     }
   if (n_busy) {
@@ -306,6 +339,15 @@ int mld_gpu_server_stats(const mld_gpu_server* s, long long* batches, long long*
   if (batches) *batches = s->batches;
   if (atoms_done) *atoms_done = s->atoms_done;
   if (budget_bytes) *budget_bytes = s->budget;
+  return MLD_OK;
+}
+
+int mld_gpu_server_admission(const mld_gpu_server* s, double* peak_bytes_in_flight, double* share_bytes,
+                             double* largest_batch_bytes) {
+  if (!s) return MLD_ERR_INVALID;
+  if (peak_bytes_in_flight) *peak_bytes_in_flight = s->peak_in_flight;
+  if (share_bytes) *share_bytes = s->budget / std::max<size_t>(1, s->slots.size());
+  if (largest_batch_bytes) *largest_batch_bytes = s->largest_request;
   return MLD_OK;
 }
 

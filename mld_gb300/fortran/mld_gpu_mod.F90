@@ -1,7 +1,7 @@
 ! ISO_C_BINDING interface to libmld_gpu (include/mld_gpu.h) for the MILADY Fortran host.
 !
-! A MILADY build links this module and libmld_gpu.so; the call sites that replace the
-! reference's own routines are shown in INTEGRATION.md.  Arrays keep the reference's
+! A MILADY build links this module and libmld_gpu.so in place of the reference's own
+! descriptor, row-fill, solve and prediction routines.  Arrays keep the reference's
 ! column-major shapes (pos_cart(3,nat), cell(3,3), force(3,nat), stress(6), energy(dim,nat),
 ! Amat(D,M)) and are passed with c_loc, so no copies are made on the host side.
 module mld_gpu_mod
@@ -47,9 +47,10 @@ module mld_gpu_mod
             mld_gpu_set_kernel_points, mld_gpu_solve_info, mld_gpu_gram_rows, &
             mld_gpu_server_create, mld_gpu_server_destroy, mld_gpu_server_submit, &
             mld_gpu_server_progress, mld_gpu_server_result, mld_gpu_server_wait, mld_gpu_server_stats, &
+            mld_gpu_server_admission, &
             mld_gpu_descriptor_derivatives, mld_gpu_last_error, mld_gpu_server_last_error, &
             mld_gpu_set_profiling, mld_gpu_profile, mld_gpu_timer_start, mld_gpu_timer_stop, &
-            mld_gpu_work_counts, mld_gpu_peak_flops, mld_gpu_descriptors_noalloc, &
+            mld_gpu_work_counts, mld_gpu_peak_flops, mld_gpu_descriptors_noalloc, mld_gpu_test_pipeline_timeout, &
             mld_gpu_synchronize
 
   interface
@@ -269,6 +270,20 @@ module mld_gpu_mod
       type(c_ptr), value :: srv
       integer(c_long_long), intent(out) :: batches, atoms_done
       real(c_double), intent(out) :: budget_bytes
+    end function
+
+    integer(c_int) function mld_gpu_test_pipeline_timeout(skip_loads, wait_limit_clocks) &
+        bind(C, name="mld_gpu_test_pipeline_timeout")
+      import :: c_int, c_long_long
+      integer(c_int), value :: skip_loads
+      integer(c_long_long), value :: wait_limit_clocks
+    end function
+
+    integer(c_int) function mld_gpu_server_admission(srv, peak_bytes_in_flight, share_bytes, largest_batch_bytes) &
+        bind(C, name="mld_gpu_server_admission")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: srv
+      real(c_double), intent(out) :: peak_bytes_in_flight, share_bytes, largest_batch_bytes
     end function
   end interface
 end module mld_gpu_mod

@@ -163,7 +163,7 @@ def test_descriptor_derivatives(lib, precision, tol):
             assert np.allclose(u[p:p + n], d["u"][i, :n], rtol=0, atol=1e-12)
             got = dB[p:p + n]
             want = d["dB"][i, :n]
-            assert _rel(got, want) < tol * 10
+            assert _rel(got, want) < tol
             p += n
         assert _rel(B[a0:a0 + s.nat], d["B"]) < tol
         a0 += s.nat
@@ -181,8 +181,7 @@ def test_design_rows(lib, precision, tol):
     assert np.array_equal(y, y_ref) and np.array_equal(w, w_ref)
     for lo, hi, name in [(0, 1, "E")]:
         assert _rel(A[lo:hi], A_ref[lo:hi]) < tol, name
-    assert _rel(A, A_ref) < tol * 10
-    # stress rows of every structure
+    assert _rel(A, A_ref) < tol
     h.close()
 
 
@@ -200,7 +199,10 @@ def test_gram_and_solve_plain(lib):
     phi = G_ref + 1e-8 * np.eye(G_ref.shape[0])
     w_ref_fit = oracle.solve_gelsd(phi, rhs_ref)
     pred, pred_ref = A_ref @ w, A_ref @ w_ref_fit
-    assert _rel(pred, pred_ref) < 1e-6
+    # predictions within the FP64 bar; coefficients within the rounding of the normal matrix
+    # (eps) times its condition number (about 1e11 here)
+    assert _rel(pred, pred_ref) < TOL64
+    assert _rel(w, w_ref_fit) < 64 * np.finfo(float).eps * np.linalg.cond(phi)
     h.close()
 
 
@@ -212,11 +214,12 @@ def test_fit_end_to_end_plain(lib):
     w, rmse = h.fit()
     w_or = oracle.fit_linear(A_ref, y_ref, w_ref, 1e-8)
     p, p_or = A_ref @ w, A_ref @ w_or
-    assert _rel(p, p_or) < 1e-6
+    assert _rel(p, p_or) < TOL64
     kinds = np.concatenate([[0] + [1] * (3 * s.nat) + [2] * 6 for s in ds.structures])
     for k in range(3):
+        # the RMSE moves by at most the largest prediction difference
         r_or = oracle.rmse(p_or[kinds == k], y_ref[kinds == k])
-        assert abs(rmse[k] - r_or) <= 1e-6 * max(r_or, 1e-12)
+        assert abs(rmse[k] - r_or) <= TOL64 * np.abs(p_or).max()
     # predictions through the serving entry point
     E, F, S = h.predict(w)
     rows_E = np.cumsum([0] + [1 + 3 * s.nat + 6 for s in ds.structures])[:-1]

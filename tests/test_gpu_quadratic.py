@@ -55,7 +55,7 @@ def test_quadratic_rows(lib, precision, tol):
     h.set_labels(E, F, S, has, np.ones((len(nat), 3)))
     A, y, w = h.design_matrix()
     assert A.shape == A_ref.shape
-    assert _rel(A, A_ref) < tol * 10
+    assert _rel(A, A_ref) < tol
     h.close()
 
 
@@ -73,7 +73,7 @@ def test_quadratic_rows_weighted(lib):
     E, F, S, has = ds.labels()
     h.set_labels(E, F, S, has, np.ones((len(nat), 3)))
     A, _, _ = h.design_matrix()
-    assert _rel(A, A_ref) < 1e-9
+    assert _rel(A, A_ref) < 1e-10
     h.close()
 
 
@@ -91,11 +91,11 @@ def test_qnml_fit_predictions(lib):
     assert w.shape[0] == 1 + KK + KK * KK
     w_or = oracle.fit_qnml(A_ref, y_ref, np.ones(len(y_ref)), lam, 1 + KK)
     p, p_or = A_ref @ w, A_ref @ w_or
-    assert _rel(p, p_or) < 1e-6
+    assert _rel(p, p_or) < 1e-10
     # predictions through the serving entry point use the same full-layout weights
     Ep, Fp, Sp = h.predict(w)
     rows_E = np.cumsum([0] + [1 + 3 * s.nat + 6 for s in ds.structures])[:-1]
-    assert _rel(Ep, p[rows_E]) < 1e-9
+    assert _rel(Ep, p[rows_E]) < 1e-10
     h.close()
 
 
