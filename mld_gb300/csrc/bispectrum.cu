@@ -15,11 +15,13 @@
 //
 // Every floating-point sum has a fixed order: lane groups accumulate privately and are reduced
 // in group order, Z terms land in a term buffer from which the Y slots and B are summed, and the
-// dB contraction runs in rounds in which each triple receives at most one layer row.  Results
-// are therefore bitwise reproducible and do not depend on which CTA takes which atom.
+// dB contraction writes each layer row into the buffer of its rank (a triple's distinct layers
+// in ascending order), where every triple has at most one row, so dB = (rank 0 + rank 1) +
+// rank 2.  Results are therefore bitwise reproducible and do not depend on which CTA takes which
+// atom.
 //
-// CTAs are persistent: they stage the recursion records and the CG coefficients in shared memory
-// once, then pull atoms from a queue ordered by descending neighbour count (longest first).
+// CTAs are persistent: they stage the recursion records in shared memory once, then pull atoms
+// from a queue ordered by descending neighbour count (longest first).
 // T = double (plain FP64 method) or float (mixed method: FP32 descriptors).
 #include <cuda_runtime.h>
 
@@ -300,12 +302,15 @@ constexpr int kNB = kNG;                // neighbours per phase-3 chunk (one per
 static_assert(kNW == kZWarps, "phase-2 schedule is built for the CTA's warps");
 
 // Shared-memory carve-up, in order (every region 16-byte aligned):
-//   rec[HU]  cg[NCG]  hoff[kMaxJ+2] rowk[NROWS] tiles[NTILE]  cfull[nch*NU]  Y[nch*NYP] (shared Y)
+//   rec[HU]  hoff[kMaxJ+2]  rowk[NROWS]  tiles[NTILE]  rank_slot[2K]  cfull[nch*NU]
+//   Y[nch*NYP] (shared Y)
 //   V region (phase 1: group partials + recursion buffers; phase 2: term buffer; phase 3: vecall
-//   of a chunk)  W region (phase 3: recursion buffers, then dB of the chunk)  Bk[nch*K]
-//   nwt[nch*NB]  nuu[NB*4]  nidx[NB]  pacc[NB*9] (FP64)  next atom
+//   of a chunk)
+//   W region (phase 2: CG coefficients; phase 3: recursion buffers, then the chunk's dB by rank:
+//   rank 0 [cols][K], rank 1 [cols][nrank1], rank 2 [cols][nrank2])
+//   Bk[nch*K]  nwt[nch*NB]  nuu[NB*4]  nidx[NB]  pacc[NB*9] (FP64)  next atom
 struct SmemPlan {
-  size_t rec, cg, hoff, rowk, tiles, cfull, Y, V, W, Bk, nwt, nuu, nidx, pacc, next, total;
+  size_t rec, hoff, rowk, tiles, rslot, cfull, Y, V, W, Bk, nwt, nuu, nidx, pacc, next, total;
 };
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -318,18 +323,21 @@ __host__ __device__ inline SmemPlan smem_plan(const DevTables& tb, int nch, int 
   const size_t v2 = (size_t)tb.NZT;                                      // phase 2
   const size_t v3 = (size_t)kNB * 3 * tb.HU;                             // phase 3
   const size_t vblock = v1 > v2 ? (v1 > v3 ? v1 : v3) : (v2 > v3 ? v2 : v3);
-  const size_t wrec = (size_t)kNG * 2 * LH * cxb, wdb = (size_t)3 * kNB * tb.K * eb;
+  const size_t wrec = (size_t)kNG * 2 * LH * cxb;
+  const size_t wdb = (size_t)3 * kNB * (tb.nrank[0] + tb.nrank[1] + tb.nrank[2]) * eb;
+  const size_t wcg = (size_t)eb * tb.NCG;
+  const size_t wblock = wrec > wdb ? (wrec > wcg ? wrec : wcg) : (wdb > wcg ? wdb : wcg);
   SmemPlan s;
   size_t o = 0;
   s.rec = o;   o = al16(o + recb * tb.HU);
-  s.cg = o;    o = al16(o + (size_t)eb * tb.NCG);
   s.hoff = o;  o = al16(o + sizeof(int) * (kMaxJ + 2));
   s.rowk = o;  o = al16(o + sizeof(int16_t) * tb.NROWS);
   s.tiles = o; o = al16(o + sizeof(int) * tb.NTILE);
+  s.rslot = o; o = al16(o + sizeof(int16_t) * (kRounds - 1) * tb.K);
   s.cfull = o; o = al16(o + cxb * nch * tb.NU);
   s.Y = o;     o = al16(o + (y_in_smem ? cxb * nch * tb.NYP : 0));
   s.V = o;     o = al16(o + cxb * vblock);
-  s.W = o;     o = al16(o + (wrec > wdb ? wrec : wdb));
+  s.W = o;     o = al16(o + wblock);
   s.Bk = o;    o = al16(o + (size_t)eb * nch * tb.K);
   s.nwt = o;   o = al16(o + (size_t)eb * nch * kNB);
   s.nuu = o;   o = al16(o + (size_t)eb * kNB * 4);
@@ -365,15 +373,16 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
   const SmemPlan sp = smem_plan(tb, nch, (int)sizeof(T), kYShared);
 
   Rec* srec = reinterpret_cast<Rec*>(smem_raw + sp.rec);
-  T* scg = reinterpret_cast<T*>(smem_raw + sp.cg);
   int* shoff = reinterpret_cast<int*>(smem_raw + sp.hoff);
   int16_t* srowk = reinterpret_cast<int16_t*>(smem_raw + sp.rowk);
   int* stile = reinterpret_cast<int*>(smem_raw + sp.tiles);
+  int16_t* srslot = reinterpret_cast<int16_t*>(smem_raw + sp.rslot);
   cx<T>* cfull = reinterpret_cast<cx<T>*>(smem_raw + sp.cfull);
   cx<T>* Y = kYShared ? reinterpret_cast<cx<T>*>(smem_raw + sp.Y)
                       : reinterpret_cast<cx<T>*>(args.yglobal) + (size_t)blockIdx.x * nch * NYP;
   cx<T>* V = reinterpret_cast<cx<T>*>(smem_raw + sp.V);
   unsigned char* W = smem_raw + sp.W;
+  T* scg = reinterpret_cast<T*>(W);  // phase 2 only (restaged per atom)
   T* Bk = reinterpret_cast<T*>(smem_raw + sp.Bk);
   T* nwt = reinterpret_cast<T*>(smem_raw + sp.nwt);
   T* nuu = reinterpret_cast<T*>(smem_raw + sp.nuu);
@@ -383,10 +392,10 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
 
   // tables, once per CTA; Y zeroed once (its padding rows are never written)
   for (int e = tid; e < HU; e += nth) srec[e] = args.rec[e];
-  for (int e = tid; e < tb.NCG; e += nth) scg[e] = args.cg[e];
   for (int e = tid; e < kMaxJ + 2; e += nth) shoff[e] = tb.hoff[e];
   for (int e = tid; e < tb.NROWS; e += nth) srowk[e] = tb.rowk[e];
   for (int e = tid; e < tb.NTILE; e += nth) stile[e] = tb.tiles[e];
+  for (int e = tid; e < (kRounds - 1) * K; e += nth) srslot[e] = tb.rank_slot[e];
   for (int e = tid; e < nch * NYP; e += nth) Y[e] = {T(0), T(0)};
 
   const T rcut = (T)args.p.rcut, inv_r0 = (T)args.p.inv_r0;
@@ -406,6 +415,8 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
     const int nn = args.nbr_off[atom + 1] - p0;
 
     // ---------------- phase 1: c^j on half layers, one lane group per neighbour ------------
+    // (the CG coefficients of phase 2 are loaded into W meanwhile; W held the previous atom's dB)
+    for (int e = tid; e < tb.NCG; e += nth) scg[e] = args.cg[e];
     {
       cx<T>* cpart = V + (size_t)grp * nch * HU;
       cx<T>* ub = V + (size_t)kNG * nch * HU + (size_t)grp * 2 * LH;
@@ -552,59 +563,70 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
       const int ncolt = (ncols + kColTile - 1) / kColTile;
       for (int ch = 0; ch < nch; ++ch) {
         const cx<T>* Yc = Y + (size_t)ch * NYP;
-        // register-tiled contraction in rounds: item = (row tile of layer j, column tile); a
-        // round adds at most one layer row into each triple's column, round 0 stores
-        for (int rd = 0; rd < kRounds; ++rd) {
-          const int t0 = tb.tile_off[rd], ntl = tb.tile_off[rd + 1] - t0;
-          for (int it = tid; it < ntl * ncolt; it += nth) {
-            const int tix = t0 + it / ncolt;
-            const int tile = stile[tix];
-            const int ct = it - (tix - t0) * ncolt;
-            const int j = tile >> 8, rt = tile & 255;
-            const int Mp = tb.Mp[j], H = shoff[j + 1] - shoff[j];
-            const cx<T>* Yp = Yc + tb.yoff[j] + rt * kRowTile;
-            // columns ct, ct + ncolt, ...: lanes of a warp read consecutive columns of V, whose
-            // odd stride HU spreads them over distinct shared-memory banks
-            const cx<T>* Vp[kColTile];
+        // register-tiled contraction, item = (row tile of layer j, column tile), heaviest
+        // layers first; each row's result goes to the buffer of its rank, where it is the
+        // triple's only row, so no two items write the same element
+        T* dB1 = dBs + (size_t)3 * kNB * K;
+        T* dB2 = dB1 + (size_t)3 * kNB * tb.nrank[1];
+        for (int it = tid; it < tb.NTILE * ncolt; it += nth) {
+          const int tix = it / ncolt;
+          const int tile = stile[tix];
+          const int ct = it - tix * ncolt;
+          const int j = tile >> 8, rt = tile & 255;
+          const int Mp = tb.Mp[j], H = shoff[j + 1] - shoff[j];
+          const cx<T>* Yp = Yc + tb.yoff[j] + rt * kRowTile;
+          // columns ct, ct + ncolt, ...: lanes of a warp read consecutive columns of V, whose
+          // odd stride HU spreads them over distinct shared-memory banks
+          const cx<T>* Vp[kColTile];
 #pragma unroll
-            for (int c = 0; c < kColTile; ++c) {
-              const int col = min(ct + c * ncolt, ncols - 1);
-              Vp[c] = V + (size_t)col * HU + shoff[j];  // col = n*3 + a -> V[n][a][.]
-            }
-            T acc[kRowTile][kColTile];
+          for (int c = 0; c < kColTile; ++c) {
+            const int col = min(ct + c * ncolt, ncols - 1);
+            Vp[c] = V + (size_t)col * HU + shoff[j];  // col = n*3 + a -> V[n][a][.]
+          }
+          T acc[kRowTile][kColTile];
+#pragma unroll
+          for (int r = 0; r < kRowTile; ++r)
+#pragma unroll
+            for (int c = 0; c < kColTile; ++c) acc[r][c] = T(0);
+#pragma unroll 2
+          for (int e = 0; e < H; ++e) {
+            cx<T> y[kRowTile], v[kColTile];
+#pragma unroll
+            for (int r = 0; r < kRowTile; ++r) y[r] = Yp[e * Mp + r];
+#pragma unroll
+            for (int c = 0; c < kColTile; ++c) v[c] = Vp[c][e];
 #pragma unroll
             for (int r = 0; r < kRowTile; ++r)
 #pragma unroll
-              for (int c = 0; c < kColTile; ++c) acc[r][c] = T(0);
-#pragma unroll 2
-            for (int e = 0; e < H; ++e) {
-              cx<T> y[kRowTile], v[kColTile];
+              for (int c = 0; c < kColTile; ++c) acc[r][c] = fma(y[r].x, v[c].x, fma(-y[r].y, v[c].y, acc[r][c]));
+          }
 #pragma unroll
-              for (int r = 0; r < kRowTile; ++r) y[r] = Yp[e * Mp + r];
+          for (int r = 0; r < kRowTile; ++r) {
+            const int code = srowk[tb.rowk_off[j] + rt * kRowTile + r];
+            if (code < 0) continue;
+            const int rank = code >> kRankShift, idx = code & ((1 << kRankShift) - 1);
+            T* base = rank == 0 ? dBs : (rank == 1 ? dB1 : dB2);
+            const int ld = tb.nrank[rank];
 #pragma unroll
-              for (int c = 0; c < kColTile; ++c) v[c] = Vp[c][e];
-#pragma unroll
-              for (int r = 0; r < kRowTile; ++r)
-#pragma unroll
-                for (int c = 0; c < kColTile; ++c) acc[r][c] = fma(y[r].x, v[c].x, fma(-y[r].y, v[c].y, acc[r][c]));
-            }
-#pragma unroll
-            for (int r = 0; r < kRowTile; ++r) {
-              const int k = srowk[tb.rowk_off[j] + rt * kRowTile + r];
-              if (k < 0) continue;
-#pragma unroll
-              for (int c = 0; c < kColTile; ++c) {
-                const int col = ct + c * ncolt;
-                if (col < ncols) {
-                  T* d = dBs + (size_t)col * K + k;
-                  *d = (rd == 0) ? acc[r][c] : *d + acc[r][c];
-                }
-              }
+            for (int c = 0; c < kColTile; ++c) {
+              const int col = ct + c * ncolt;
+              if (col < ncols) base[(size_t)col * ld + idx] = acc[r][c];
             }
           }
-          __syncthreads();
         }
+        __syncthreads();
+        // dB = (rank 0 + rank 1) + rank 2 of element e = col * K + k
+        auto dB_of = [&](int e) {
+          const int col = e / K, k = e - col * K;
+          const int s1 = srslot[k * (kRounds - 1)], s2 = srslot[k * (kRounds - 1) + 1];
+          T v = dBs[e];
+          if (s1 >= 0) v += dB1[(size_t)col * tb.nrank[1] + s1];
+          if (s2 >= 0) v += dB2[(size_t)col * tb.nrank[2] + s2];
+          return v;
+        };
         if (eval) {
+          for (int e = tid; e < ncols * K; e += nth) dBs[e] = dB_of(e);  // in place: own element
+          __syncthreads();
           // forces and stress with the effective weights: the centre's for the forces, the
           // neighbour's for the stress (the neighbour's B in the quadratic stress rows,
           // mld_stress.F90:580-603); sums per (neighbour, component) in T, per-pair totals in
@@ -642,7 +664,7 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
           T* out = args.dBout + (size_t)(p0 + base) * 3 * nchK + ch * K;
           for (int e = tid; e < nb_here * 3 * K; e += nth) {
             const int na = e / K, k = e - na * K;  // na = n*3 + a
-            out[(size_t)na * nchK + k] = dBs[e] * nwt[ch * kNB + na / 3];
+            out[(size_t)na * nchK + k] = dB_of(e) * nwt[ch * kNB + na / 3];
           }
         }
         __syncthreads();

@@ -197,12 +197,13 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
 
   // layer-blocked Y: rows of layer j are the triples using layer j (any of l, l1, l2).  A
   // triple's distinct layers in ascending order have ranks 0, 1, 2; within a layer the rows are
-  // grouped by rank (each group padded to whole row tiles), so the dB contraction can run in
-  // kRounds rounds in which every triple receives at most one row's contribution (no atomics,
-  // a fixed summation order).
+  // grouped by rank (each group padded to whole row tiles).  The dB contraction writes a row's
+  // result into the buffer of its rank, where every triple has at most one row, so all tiles run
+  // in one pass without atomics, and dB = (rank 0 + rank 1) + rank 2 in a fixed order.
   std::vector<std::vector<int>> rows(J + 1);  // row position -> triple (-1 padding)
+  std::vector<std::vector<int>> rowrank(J + 1);  // row position -> rank
   std::vector<std::map<int, int>> rowpos(J + 1);  // triple -> row position
-  std::vector<std::vector<int>> round_tiles(kRounds);
+  t->rank_slot.assign((size_t)t->K * (kRounds - 1), -1);
   {
     std::vector<std::vector<std::vector<int>>> byrank(J + 1, std::vector<std::vector<int>>(kRounds));
     for (int k = 0; k < t->K; ++k) {
@@ -218,15 +219,18 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
       for (int r = 0; r < kRounds; ++r) {
         const std::vector<int>& v = byrank[j][r];
         if (v.empty()) continue;
-        const int first = (int)rows[j].size();
         for (int k : v) {
           rowpos[j][k] = (int)rows[j].size();
           rows[j].push_back(k);
+          rowrank[j].push_back(r);
+          if (r > 0) t->rank_slot[(size_t)k * (kRounds - 1) + r - 1] = (int16_t)t->nrank[r]++;
         }
-        while (rows[j].size() % kRowTile) rows[j].push_back(-1);
-        for (int rt = first / kRowTile; rt < (int)rows[j].size() / kRowTile; ++rt)
-          round_tiles[r].push_back((j << 8) | rt);
+        while (rows[j].size() % kRowTile) {
+          rows[j].push_back(-1);
+          rowrank[j].push_back(0);
+        }
       }
+    t->nrank[0] = t->K;
   }
   int ypos = 0, rk = 0;
   for (int j = 0; j <= J; ++j) {
@@ -234,7 +238,12 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
     t->yoff[j] = ypos;
     ypos += t->Mp[j] * H(j);
     t->rowk_off[j] = rk;
-    for (int r = 0; r < t->Mp[j]; ++r) t->rowk.push_back((int16_t)rows[j][r]);
+    for (int r = 0; r < t->Mp[j]; ++r) {
+      const int k = rows[j][r], rank = rowrank[j][r];
+      int16_t code = -1;
+      if (k >= 0) code = (int16_t)((rank << kRankShift) | (rank == 0 ? k : t->rank_slot[(size_t)k * (kRounds - 1) + rank - 1]));
+      t->rowk.push_back(code);
+    }
     rk += t->Mp[j];
   }
   t->rowk_off[J + 1] = rk;
@@ -243,14 +252,13 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
     *err = "Y table exceeds 16-bit offsets";
     return false;
   }
-  // row tiles of the dB contraction by round, heaviest layers first within a round
-  for (int r = 0; r < kRounds; ++r) {
-    std::vector<int>& v = round_tiles[r];
-    std::stable_sort(v.begin(), v.end(), [](int x, int y) { return (x >> 8) > (y >> 8); });
-    t->tile_off[r] = (int)t->tiles.size();
-    t->tiles.insert(t->tiles.end(), v.begin(), v.end());
+  if (t->K >= (1 << kRankShift)) {
+    *err = "too many triples for the row destination code";
+    return false;
   }
-  t->tile_off[kRounds] = (int)t->tiles.size();
+  // row tiles of the dB contraction, heaviest layers first
+  for (int j = J; j >= 0; --j)
+    for (int rt = 0; rt < t->Mp[j] / kRowTile; ++rt) t->tiles.push_back((j << 8) | rt);
 
   // folded slots; the kernel's slot entries; the ZA entries of every triple for B
   std::vector<std::vector<BkItem>> bk(t->K);

@@ -85,7 +85,8 @@ struct RecEntry64 {
 };
 
 constexpr int kZWarps = 8;   // warps of the phase-2 schedule (= warps of a k_bso4 CTA)
-constexpr int kRounds = 3;   // contraction rounds: a triple has at most one Y row per round
+constexpr int kRounds = 3;   // ranks of a triple's layer rows (its distinct layers in ascending order)
+constexpr int kRankShift = 12;  // row destination code: (rank << kRankShift) | index within the rank's buffer
 
 // Host-built constant tables of the SO(4) bispectrum for a given j_max.
 struct Bso4Tables {
@@ -103,10 +104,13 @@ struct Bso4Tables {
   std::vector<SlotEntry> slots; // the same slots in the kernel's form
   std::vector<int> bk_off;      // K + 1 offsets into bk_items
   std::vector<BkItem> bk_items; // ZA entries of each triple
-  std::vector<int16_t> rowk;    // per layer-block row: triple index or -1 (padding)
+  // per layer-block row: destination code (rank << kRankShift) | index, -1 for padding; the
+  // index is the triple for rank 0 and the triple's slot in the rank-1 / rank-2 buffers
+  std::vector<int16_t> rowk;
   int rowk_off[kMaxJ + 2] = {0};  // offset of each layer's rows in rowk
-  std::vector<int> tiles;       // row tiles (j << 8 | rt), by round, heaviest layers first
-  int tile_off[kRounds + 1] = {0};  // tiles of round r: [tile_off[r], tile_off[r + 1])
+  std::vector<int> tiles;       // row tiles (j << 8 | rt), heaviest layers first
+  int nrank[kRounds] = {0};     // triples with a row of rank r (rank 0: all K)
+  std::vector<int16_t> rank_slot;  // K x (kRounds - 1): slot of triple k in the rank-1 / rank-2 buffers, -1 none
   // recursion on half layers: U = tz*Zsel*U[src_z] + tx*(-i)*Xsel*U[src_x]
   std::vector<double> rec_tz, rec_tx;
   std::vector<int16_t> rec_sz, rec_sx;
@@ -129,8 +133,9 @@ struct DevTables {
   int Mp[kMaxJ + 1] = {0};
   int yoff[kMaxJ + 1] = {0};
   int rowk_off[kMaxJ + 2] = {0};
-  int tile_off[kRounds + 1] = {0};
+  int nrank[kRounds] = {0};
   int16_t* rowk = nullptr;
+  int16_t* rank_slot = nullptr;  // K x (kRounds - 1)
   int* tiles = nullptr;
   double* cg64 = nullptr;
   float* cg32 = nullptr;
@@ -178,13 +183,14 @@ cudaError_t fill_dev_tables(const Bso4Tables& t, DevTables* d, Put put) {
     d->Mp[j] = t.Mp[j];
     d->yoff[j] = t.yoff[j];
   }
-  for (int r = 0; r <= kRounds; ++r) d->tile_off[r] = t.tile_off[r];
+  for (int r = 0; r < kRounds; ++r) d->nrank[r] = t.nrank[r];
   std::vector<float> cg32(t.cg.begin(), t.cg.end());
   std::vector<RecEntry32> r32;
   std::vector<RecEntry64> r64;
   pack_recursion(t, &r32, &r64);
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = put(t.rowk, &d->rowk);
+  if (e == cudaSuccess) e = put(t.rank_slot, &d->rank_slot);
   if (e == cudaSuccess) e = put(t.tiles, &d->tiles);
   if (e == cudaSuccess) e = put(t.cg, &d->cg64);
   if (e == cudaSuccess) e = put(cg32, &d->cg32);
