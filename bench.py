@@ -35,10 +35,11 @@ N_STRUCT = 2000
 RCUT = 4.7
 J_MAX = 4.0
 LAMBDA = 1e-8
-# DRAM bytes (read + write) of one k_bso4<float> launch per atom: 78.05 MB over 45,702 atoms in
-# the ncu capture of the 200-structure Fe case (profiles/k_bso4_f32_fe200.md); the traffic is
-# per-atom neighbour data and rows, so it is scaled by the atoms of the launch
-BSO4_DRAM_BYTES_PER_ATOM = 78.29e6 / 45702
+# DRAM bytes (read + write) of one k_bso4<float> launch per atom, from an ncu capture of the
+# 200-structure Fe case (45,702 atoms): 57.7 MB read (neighbour data, tables) + 1.021 GB written
+# (w*dB of every pair, the input of the row gather); both grow with the atoms (and their pairs),
+# so the figure is scaled by the atoms of the launch
+BSO4_DRAM_BYTES_PER_ATOM = (57.66e6 + 1.0208e9) / 45702
 
 
 def _args():

@@ -2,7 +2,9 @@
 from __future__ import annotations
 
 import concurrent.futures as cf
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -36,16 +38,37 @@ def _compile(src: str, extra: list[str]) -> str:
     return obj
 
 
-def up_to_date() -> bool:
-    if not os.path.exists(OUT):
+STAMP = OUT + ".srchash"
+
+
+def source_hash(extra: list[str]) -> str:
+    """SHA-256 over the sources, the public header, the compiler flags and nvcc's version, so a
+    library built elsewhere (another machine's copy of the tree) is never mistaken for current."""
+    h = hashlib.sha256()
+    deps = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)) + [os.path.join(HERE, "..", "include", "mld_gpu.h")]
+    for d in deps:
+        if os.path.isfile(d):
+            h.update(os.path.basename(d).encode())
+            with open(d, "rb") as fh:
+                h.update(fh.read())
+    h.update(" ".join(ARCH + NVCC_FLAGS[:-2] + list(extra)).encode())
+    h.update(platform.machine().encode())
+    try:
+        h.update(subprocess.run([nvcc(), "--version"], capture_output=True, text=True).stdout.encode())
+    except Exception:  # pragma: no cover - nvcc missing: build() fails later with its own message
+        pass
+    return h.hexdigest()
+
+
+def up_to_date(extra: list[str] | None = None) -> bool:
+    if not (os.path.exists(OUT) and os.path.exists(STAMP)):
         return False
-    t = os.path.getmtime(OUT)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", "mld_gpu.h")]
-    return all(os.path.getmtime(d) <= t for d in deps if os.path.exists(d))
+    with open(STAMP) as fh:
+        return fh.read().strip() == source_hash(list(extra or []))
 
 
 def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> str:
-    if not force and up_to_date():
+    if not force and up_to_date(extra):
         return OUT
     os.makedirs(BUILD, exist_ok=True)
     extra = list(extra or [])
@@ -57,6 +80,8 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, OUT)
+    with open(STAMP, "w") as fh:
+        fh.write(source_hash(extra) + "\n")
     if verbose:
         print("built", OUT)
     return OUT

@@ -2,8 +2,9 @@
 //
 // Triple enumeration and the Clebsch-Gordan products follow MILADY
 // src/mld/compute/compute_bispectrum_so4.F90:740-918 (l1 = 0..J, l2 = 0..l1,
-// l = |l1-l2|..min(J,l1+l2), l1+l2+l even, l >= l1) and the coefficient formula of
-// src/mld/angular_functions.f90:432-483 (cg / wigner3j with doubled indices).
+// l = |l1-l2|..min(J,l1+l2), l1+l2+l even, l >= l1); the coefficients themselves are the
+// standard Clebsch-Gordan coefficients with doubled indices (the reference evaluates them
+// through Wigner 3j symbols, src/mld/angular_functions.f90:432-483; here Racah's formula).
 // Instead of one flattened list of CG products per term (the reference's cg_A/cg_B/cg_C),
 // each Z output stores its two 1-D coefficient lists and the strided c indices, so the GPU
 // derives the products from a table of a few thousand entries.  Only half of every layer is
@@ -12,6 +13,7 @@
 // (plus the self-symmetric centre of even layers).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <map>
 #include <tuple>
 
@@ -25,30 +27,36 @@ static double factorial(int n) {
   return r;
 }
 
-static double sgn(int e) { return (e % 2 == 0) ? 1.0 : -1.0; }
-
-static double wigner3j(int j1, int m1, int j2, int m2, int j, int m) {
-  const int nt = 2;
-  double coef = sgn((j1 - j2 - m) / nt) *
-                std::sqrt(factorial((j1 + m1) / nt) * factorial((j1 - m1) / nt) * factorial((j2 + m2) / nt) *
-                          factorial((j2 - m2) / nt) * factorial((j + m) / nt) * factorial((j - m) / nt));
-  double tri = std::sqrt(factorial((j1 + j2 - j) / nt) * factorial((j1 - j2 + j) / nt) *
-                         factorial((-j1 + j2 + j) / nt) / factorial((j1 + j2 + j) / nt + 1));
-  int tmin = std::max(std::max((j2 - j - m1) / nt, (j1 + m2 - j) / nt), 0);
-  int tmax = std::min(std::min((j1 + j2 - j) / nt, (j1 - m1) / nt), (j2 + m2) / nt);
-  double s = 0.0;
-  for (int t = tmin; t <= tmax; ++t)
-    s += sgn(t) / (factorial(t) * factorial((j1 + j2 - j) / nt - t) * factorial((j1 - m1) / nt - t) *
-                   factorial((j2 + m2) / nt - t) * factorial((j - j2 + m1) / nt + t) * factorial((j - j1 - m2) / nt + t));
-  return coef * tri * s;
-}
-
+// Clebsch-Gordan coefficient <j1 m1 j2 m2 | j m> in the Condon-Shortley phase convention, from
+// Racah's closed formula (G. Racah, Phys. Rev. 62, 438 (1942); D. A. Varshalovich et al.,
+// "Quantum Theory of Angular Momentum", sec. 8.2.1):
+//   C = delta(m, m1 + m2) sqrt((2j+1) (j1+j2-j)! (j1-j2+j)! (j2-j1+j)! / (j1+j2+j+1)!)
+//       * sqrt((j1+m1)! (j1-m1)! (j2+m2)! (j2-m2)! (j+m)! (j-m)!)
+//       * sum_k (-1)^k / [k! (j1+j2-j-k)! (j1-m1-k)! (j2+m2-k)! (j-j2+m1+k)! (j-j1-m2+k)!]
+// with k over the integers that keep every factorial argument non-negative.  All arguments are
+// doubled (2j, 2m), so the half-integer momenta of SO(4) are exact integers here.
 double cg_coefficient(int j1, int m1, int j2, int m2, int j, int m) {
-  if (m - m1 - m2 != 0) return 0.0;
-  if (j1 + j2 - j < 0 || j - j1 + j2 < 0 || j - j2 + j1 < 0) return 0.0;
-  if ((j + j1 + j2) % 2 == 1) return 0.0;
-  if (m1 < -j1 || m1 > j1 || m2 < -j2 || m2 > j2 || m < -j || m > j) return 0.0;
-  return sgn((j1 - j2 + m) / 2) * std::sqrt((double)j + 1.0) * wigner3j(j1, m1, j2, m2, j, -m);
+  if (m != m1 + m2) return 0.0;
+  if (j1 + j2 < j || j1 + j < j2 || j2 + j < j1) return 0.0;  // triangle
+  if ((j1 + j2 + j) % 2 != 0) return 0.0;
+  if (std::abs(m1) > j1 || std::abs(m2) > j2 || std::abs(m) > j) return 0.0;
+  if ((j1 + m1) % 2 || (j2 + m2) % 2 || (j + m) % 2) return 0.0;
+  // undoubled integer combinations
+  const int a = (j1 + j2 - j) / 2, b = (j1 - m1) / 2, c = (j2 + m2) / 2;
+  const int d = (j - j2 + m1) / 2, e = (j - j1 - m2) / 2;
+  const double norm = std::sqrt((double)(j + 1) * factorial(a) * factorial((j1 - j2 + j) / 2) *
+                                factorial((j2 - j1 + j) / 2) / factorial((j1 + j2 + j) / 2 + 1)) *
+                      std::sqrt(factorial((j1 + m1) / 2) * factorial(b) * factorial(c) * factorial((j2 - m2) / 2) *
+                                factorial((j + m) / 2) * factorial((j - m) / 2));
+  const int kmin = std::max(0, std::max(-d, -e));
+  const int kmax = std::min(a, std::min(b, c));
+  double sum = 0.0;
+  for (int k = kmin; k <= kmax; ++k) {
+    const double term = 1.0 / (factorial(k) * factorial(a - k) * factorial(b - k) * factorial(c - k) *
+                               factorial(d + k) * factorial(e + k));
+    sum += (k % 2 == 0) ? term : -term;
+  }
+  return norm * sum;
 }
 
 bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
