@@ -59,8 +59,10 @@ def _args():
     p.add_argument("--ref-points", type=int, default=4000, help="hea_krr: kernel reference points")
     p.add_argument("--requests", type=int, default=300, help="serve: number of requests")
     p.add_argument("--rate", type=float, default=100.0, help="serve: Poisson arrival rate [requests/s]")
-    p.add_argument("--plain-structures", type=int, default=200,
-                   help="hea_qnml: structures of the sample on which mixed and plain FP64 are compared")
+    p.add_argument("--plain-structures", type=int, default=100,
+                   help="hea_qnml / hea_krr: structures of the sample on which mixed and plain FP64 are compared")
+    p.add_argument("--no-extra", action="store_true",
+                   help="headline workload only (skip the alloy QNML, KRR and serving records)")
     return p.parse_args()
 
 
@@ -277,7 +279,11 @@ def run_hea(a):
     h.close()
     sample = {}
     if a.plain_structures > 0:
+        # both methods fitted on the same structures: the same-workload speed ratio, and the mixed
+        # fit's error against the FP64 fit per stage (linear block, quadratic block) in the
+        # coefficients and in the energy / force / stress predictions
         idx = list(range(min(a.plain_structures, n_struct)))
+        fits = {}
         for name, prec in (("mixed", _lib.MIXED), ("plain_fp64", _lib.PLAIN_FP64)):
             hs, As = handle(prec, idx)
             Ms = hs.num_rows()
@@ -285,11 +291,22 @@ def run_hea(a):
             hs.timer_start()
             ws, rs = hs.fit()
             t = hs.timer_stop()
+            fits[name] = (ws, hs.predict(ws))
             sample[name] = {"ms_per_fit": t, "design_rows": Ms, "rows_per_s": Ms / (t * 1e-3), "rmse_efs": rs.tolist()}
+            if prec == _lib.MIXED:
+                sample[name]["solve"] = hs.solve_info()
             hs.close()
         mx, pl = sample["mixed"], sample["plain_fp64"]
         sample["force_rmse_rel_diff"] = abs(mx["rmse_efs"][1] - pl["rmse_efs"][1]) / pl["rmse_efs"][1]
-        sample["speedup_rows_per_s_vs_plain_fp64"] = (M / (ms * 1e-3)) / pl["rows_per_s"]
+        sample["speedup_same_structures"] = mx["rows_per_s"] / pl["rows_per_s"]
+        (wm, pm), (wp, pp) = fits["mixed"], fits["plain_fp64"]
+        KK = int(round((-1 + np.sqrt(1 + 4 * (len(wp) - 1))) / 2))
+        rel = lambda x, y: float(np.abs(np.asarray(x) - np.asarray(y)).max() / max(np.abs(y).max(), 1e-300))
+        sample["mixed_vs_fp64"] = {
+            "w_rel_linear_block": rel(wm[:1 + KK], wp[:1 + KK]),
+            "w_rel_quadratic_block": rel(wm[1 + KK:], wp[1 + KK:]),
+            "pred_rel_energy": rel(pm[0], pp[0]), "pred_rel_force": rel(pm[1], pp[1]),
+            "pred_rel_stress": rel(pm[2], pp[2])}
     line = {
         "metric": "design rows/s (QNML quadratic fit, 5-element bcc alloy, weighted bispectrum j_max=4)",
         "value": M / (ms * 1e-3), "unit": "design rows/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
@@ -304,7 +321,7 @@ def run_hea(a):
         "mixed_solve": out["solve"], "gpu_launches": out["launches"], "clocks": out["clocks"],
         "sample_comparison": sample or None,
     }
-    print(json.dumps(line))
+    return line
 
 
 def run_hea_krr(a):
@@ -370,7 +387,7 @@ def run_hea_krr(a):
             hs.close()
         mx, pl = sample["mixed"], sample["plain_fp64"]
         sample["force_rmse_rel_diff"] = abs(mx["rmse_efs"][1] - pl["rmse_efs"][1]) / pl["rmse_efs"][1]
-        sample["speedup_rows_per_s_vs_plain_fp64"] = (M / (ms * 1e-3)) / pl["rows_per_s"]
+        sample["speedup_same_structures"] = mx["rows_per_s"] / pl["rows_per_s"]
     line = {
         "metric": "design rows/s (kernel ridge regression, polynomial kernel, 5-element bcc alloy)",
         "value": M / (ms * 1e-3), "unit": "design rows/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
@@ -386,7 +403,7 @@ def run_hea_krr(a):
         "mixed_solve": out["solve"], "gpu_launches": out["launches"], "clocks": out["clocks"],
         "sample_comparison": sample or None,
     }
-    print(json.dumps(line))
+    return line
 
 
 def run_serve(a):
@@ -473,7 +490,7 @@ def run_serve(a):
         "force_rel_diff_mixed_vs_plain": ferr,
         "force_rel_diff_mixed_vs_plain_rms": ferr_rms,
     }
-    print(json.dumps(line))
+    return line
 
 
 def cpu_sample(ds, target_s=15.0, threads=None):
@@ -552,7 +569,7 @@ def main():
 
     if a.workload in ("hea_qnml", "hea_krr", "serve"):
         if rank == 0:
-            {"hea_qnml": run_hea, "hea_krr": run_hea_krr, "serve": run_serve}[a.workload](a)
+            print(json.dumps({"hea_qnml": run_hea, "hea_krr": run_hea_krr, "serve": run_serve}[a.workload](a)))
         return
     if world > 1:
         import torch.distributed as dist
@@ -614,7 +631,28 @@ def main():
                        "ms_per_step": res["ms_e2e"], "host_wall_ms_per_step": res["wall_e2e"]}
     if cpu:
         line["cpu_baseline"] = cpu
+    if world == 1 and not a.no_extra:
+        line["extra_configs"] = run_extra(a)
     print(json.dumps(line))
+
+
+def run_extra(a):
+    """The alloy workloads of the other configurations at their full size, attached to the
+    headline line (fewer timed steps each): the quadratic QNML fit with the same-structure
+    comparison against the plain FP64 method, the kernel ridge fit, and the serving loop."""
+    import copy
+    out = {}
+    b = copy.copy(a)
+    b.structures, b.steps, b.warmup = N_STRUCT, min(a.steps, 3), 1
+    for name, fn in (("hea_qnml", run_hea), ("hea_krr", run_hea_krr), ("serve", run_serve)):
+        t0 = time.perf_counter()
+        try:
+            r = fn(b)
+            r["wall_s"] = time.perf_counter() - t0
+            out[name] = r
+        except Exception as e:  # report, keep the headline line
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+    return out
 
 
 if __name__ == "__main__":
