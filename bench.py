@@ -177,6 +177,7 @@ def run_ours(a, rank, world):
     peak32 = h.peak_flops(_lib.MIXED)
     launches = int(sum(v[1] for v in prof.values()))
     res["solve_info"] = h.solve_info()
+    res["autotune"] = h.tuning(0)
     res.update(M=M, A=A, ms_step=ms_step, rmse_mixed=rmse_mixed.tolist(), prof=prof, wc=wc, flops=flops,
                t_desc=t_desc, peak32=peak32, launches=launches, clocks=clk.summary(),
                per_pair=per_pair, per_atom=per_atom)
@@ -614,6 +615,7 @@ def main():
         "speedup_vs_plain_fp64": None if res["ms64"] is None else res["ms64"] / ms_step,
         "phase_ms": {k: v[0] / a.steps for k, v in res["prof"].items()},
         "mixed_solve": res["solve_info"],
+        "descriptor_autotune": res["autotune"],
         "roofline": {"kernel": "k_bso4<float> (fused descriptor + design rows)", "bound": "fp32",
                      "achieved": achieved, "peak": res["peak32"], "unit": "TFLOP/s", "frac": achieved / res["peak32"],
                      "peak_source": "measured in this run (FP32 FMA probe; not in MEASURED_PEAKS.json)",

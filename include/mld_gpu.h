@@ -205,6 +205,16 @@ int mld_gpu_set_kernel_points(mld_gpu_handle* h, int nk, const double* z_raw);
 int mld_gpu_solve_info(const mld_gpu_handle* h, int* pcg_iterations /*[2]*/, double* pcg_residual /*[2]*/,
                        double* precond_shift /*[2]*/, int* chol_retries);
 
+/* Launch shape of the descriptor kernel chosen by the handle's autotuner for one output mode
+ * (0: design rows, i.e. B and dB; 1: evaluation with fitted weights; 2: descriptors only).  The
+ * tuner times every candidate once on the first batch with enough atoms and keeps the fastest;
+ * all candidates give bitwise the same results.  shape[4] = {column tile (4 or 2), persistent
+ * CTAs per SM (0 = as many as fit), longest-first queue (1) or index order (0), tuned (1/0)};
+ * *ncand: capacity of ms on input, candidates timed on output; ms[i] the time [ms] of candidate
+ * i in the order (column tile 4, 2) x (CTAs per SM max, 1) x (queue sorted, index).
+ * (No reference counterpart.) */
+int mld_gpu_tuning(const mld_gpu_handle* h, int mode, int* shape, int* ncand, double* ms);
+
 /* Test hook of the device-side timeout path (no reference counterpart).  skip_loads = 1 makes
  * the producer warp of the tensor-core Gram (the mixed method's narrow-block normal matrix and
  * mld_gpu_gram_rows) issue no loads, so its consumers' bounded waits expire after

@@ -31,7 +31,7 @@ EXPORTED = ["mld_gpu_config_defaults", "mld_gpu_create", "mld_gpu_destroy", "mld
             "mld_gpu_set_kernel_points", "mld_gpu_server_create", "mld_gpu_server_destroy",
             "mld_gpu_server_last_error", "mld_gpu_server_submit", "mld_gpu_server_progress",
             "mld_gpu_server_result", "mld_gpu_server_wait", "mld_gpu_server_stats", "mld_gpu_server_admission",
-            "mld_gpu_test_pipeline_timeout"]
+            "mld_gpu_test_pipeline_timeout", "mld_gpu_tuning"]
 NPHASE = 6
 PHASES = ["neighbours", "rows", "descriptors", "gram", "solve", "predict"]
 
@@ -290,6 +290,15 @@ class Handle:
         Z = np.ascontiguousarray(z_raw, dtype=np.float64)
         self._check(self._L.mld_gpu_set_kernel_points(self._h, int(Z.shape[0]), _p(Z)))
         self._dims()
+
+    def tuning(self, mode: int = 0):
+        """Launch shape the autotuner chose for the descriptor kernel and the candidates' times."""
+        shape = np.zeros(4, np.int32)
+        n = ctypes.c_int(16)
+        ms = np.zeros(16)
+        self._check(self._L.mld_gpu_tuning(self._h, int(mode), _p(shape), ctypes.byref(n), _p(ms)))
+        return {"col_tile": int(shape[0]), "ctas_per_sm": int(shape[1]), "sorted_queue": int(shape[2]),
+                "tuned": bool(shape[3]), "candidate_ms": [float(v) for v in ms[:n.value]]}
 
     def solve_info(self):
         it = np.zeros(2, np.int32)

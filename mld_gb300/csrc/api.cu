@@ -91,6 +91,23 @@ struct mld_gpu_handle {
   int chol_retries = 0;
   int last_rank = 0;  // rank of the last symmetric solve (eigenvalues kept by the rcond cut)
 
+  // descriptor-kernel launch shape per output mode (0: B and dB, 1: evaluation, 2: B only),
+  // chosen by timing the candidates once on a batch of at least kTuneMinAtoms per SM
+  struct Tune {
+    bool done = false;
+    Bso4Launch best;
+    std::vector<Bso4Launch> cand;
+    std::vector<float> ms;
+  } tune[3];
+
+  // CUDA graph of the row-assembly stage (descriptor kernel, reverse pairs, row gathers) of the
+  // staged batch, replayed by later fits of the same batch; key = buffer generation and sizes
+  long long buf_gen = 0;  // bumped whenever a device buffer is (re)allocated or freed
+  cudaGraphExec_t rows_graph = nullptr;
+  long long rows_graph_key[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  long long rows_graph_launches = 0;
+  bool rows_graph_off = false;  // a capture failed once: run the stage directly from then on
+
   std::vector<void*> owned;  // table allocations
   Buf bufs[64];
   enum {
@@ -128,6 +145,7 @@ int cuda_fail(mld_gpu_handle* h, cudaError_t e, const char* where) {
 cudaError_t ensure(mld_gpu_handle* h, int id, size_t bytes) {
   Buf& bf = h->bufs[id];
   if (bytes <= bf.cap && bf.p) return cudaSuccess;
+  ++h->buf_gen;
   if (bf.p) cudaFree(bf.p);
   bf.p = nullptr;
   bf.cap = 0;
@@ -286,21 +304,71 @@ int y_scratch(mld_gpu_handle* h, void** p, size_t* bytes) {
   return MLD_OK;
 }
 
+// Autotuner of the descriptor kernel's launch shape: on the first batch large enough (at least
+// kTuneMinAtoms atoms per SM) each candidate shape (column tile 4 or 2, as many persistent CTAs
+// per SM as fit or one, longest-first or index-order queue) runs once on the real batch, timed
+// with CUDA events on the handle's stream, and the fastest is kept for the handle.  Every shape
+// computes bitwise the same outputs, so the last candidate's run is the result.
+constexpr int kTuneMinAtoms = 64;
+
+template <typename T>
+int tuned_launch(mld_gpu_handle* h, int mode, T* Bout, T* dB, const DevEval<T>* ev, void* ys, size_t ysb) {
+  auto& tn = h->tune[mode];
+  const int* order = bp_<int>(h, mld_gpu_handle::B_ORDER);
+  int* counter = bp_<int>(h, mld_gpu_handle::B_QCNT);
+  if (tn.done || h->A < kTuneMinAtoms * std::max(1, h->nsm)) {
+    CK(launch_bso4<T>(h->dt, h->b, h->bp, Bout, dB, ev, order, counter, h->st, ys, ysb, &tn.best));
+    return MLD_OK;
+  }
+  tn.cand.clear();
+  tn.ms.clear();
+  for (int ct : {4, 2})
+    for (int cps : {0, 1})
+      for (int sorted : {1, 0}) tn.cand.push_back(Bso4Launch{ct, cps, sorted});
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  CK(cudaEventCreate(&ev0));
+  CK(cudaEventCreate(&ev1));
+  float best = 0.f;
+  for (const Bso4Launch& c : tn.cand) {
+    CK(cudaEventRecord(ev0, h->st));
+    CK(launch_bso4<T>(h->dt, h->b, h->bp, Bout, dB, ev, order, counter, h->st, ys, ysb, &c));
+    CK(cudaEventRecord(ev1, h->st));
+    CK(cudaEventSynchronize(ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ev0, ev1));
+    tn.ms.push_back(ms);
+    if (tn.ms.size() == 1 || ms < best) {
+      best = ms;
+      tn.best = c;
+    }
+  }
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  nl(h, (long long)tn.cand.size() - 1);
+  tn.done = true;
+  return MLD_OK;
+}
+
+template <typename T>
+int prepare_descriptors(mld_gpu_handle* h, bool want_dB, void** ys, size_t* ysb) {
+  int rcy = y_scratch<T>(h, ys, ysb);
+  if (rcy) return rcy;
+  if (want_dB) CK(ensure(h, mld_gpu_handle::B_DBOUT, sizeof(T) * std::max<size_t>((size_t)h->b.P * 3 * h->KK, 1)));
+  return MLD_OK;
+}
+
 // B and w_ch * dB of the staged batch into B_BOUT / B_DBOUT (dB optional) through the
 // descriptor kernel's queue
 template <typename T>
 int run_descriptors(mld_gpu_handle* h, bool want_dB, const DevEval<T>* ev, T* Bout) {
   void* ys = nullptr;
   size_t ysb = 0;
-  int rcy = y_scratch<T>(h, &ys, &ysb);
+  int rcy = prepare_descriptors<T>(h, want_dB, &ys, &ysb);
   if (rcy) return rcy;
-  T* dB = nullptr;
-  if (want_dB) {
-    CK(ensure(h, mld_gpu_handle::B_DBOUT, sizeof(T) * std::max<size_t>((size_t)h->b.P * 3 * h->KK, 1)));
-    dB = bp_<T>(h, mld_gpu_handle::B_DBOUT);
-  }
-  CK(launch_bso4<T>(h->dt, h->b, h->bp, Bout, dB, ev, bp_<int>(h, mld_gpu_handle::B_ORDER),
-                    bp_<int>(h, mld_gpu_handle::B_QCNT), h->st, ys, ysb));
+  T* dB = want_dB ? bp_<T>(h, mld_gpu_handle::B_DBOUT) : nullptr;
+  const int mode = ev ? 1 : (want_dB ? 0 : 2);
+  int rc = tuned_launch<T>(h, mode, Bout, dB, ev, ys, ysb);
+  if (rc) return rc;
   nl(h, 1);
   return MLD_OK;
 }
@@ -358,18 +426,70 @@ int run_rows(mld_gpu_handle* h, const RowLayout& L, bool with_labels, T** Xout) 
     CK(ensure(h, mld_gpu_handle::B_SP, sizeof(T) * nB * 6));
     if (h->quad) CK(ensure(h, mld_gpu_handle::B_HQ, sizeof(T) * (size_t)std::max(1, h->A) * 6 * h->KK));
     T* Bq = bp_<T>(h, mld_gpu_handle::B_BOUT);
-    int rcd = run_descriptors<T>(h, true, nullptr, Bq);
+    void* ys = nullptr;
+    size_t ysb = 0;
+    int rcd = prepare_descriptors<T>(h, true, &ys, &ysb);
     if (rcd) return rcd;
     T* dBq = bp_<T>(h, mld_gpu_handle::B_DBOUT);
-    CK(launch_reverse_pairs(h->b, bp_<int>(h, mld_gpu_handle::B_REV), h->st));
-    CK(launch_lin_rows<T>(h->b, rows, h->bp, h->KK, bp_<int>(h, mld_gpu_handle::B_REV), Bq, dBq,
-                          bp_<T>(h, mld_gpu_handle::B_SP), X, h->st));
-    nl(h, 3);
-    if (h->quad) {
-      CK(launch_quad_rows<T>(h->b, rows, h->bp, h->KK, bp_<int>(h, mld_gpu_handle::B_REV), Bq, dBq,
-                             bp_<T>(h, mld_gpu_handle::B_HQ), X, h->DL, h->st));
-      nl(h, 2);
-    } else if (h->krr) {
+    // the stage of this batch: descriptor kernel, reverse pairs, linear (and quadratic) rows
+    auto stage = [&]() -> int {
+      int rc = run_descriptors<T>(h, true, nullptr, Bq);
+      if (rc) return rc;
+      CK(launch_reverse_pairs(h->b, bp_<int>(h, mld_gpu_handle::B_REV), h->st));
+      CK(launch_lin_rows<T>(h->b, rows, h->bp, h->KK, bp_<int>(h, mld_gpu_handle::B_REV), Bq, dBq,
+                            bp_<T>(h, mld_gpu_handle::B_SP), X, h->st));
+      nl(h, 3);
+      if (h->quad) {
+        CK(launch_quad_rows<T>(h->b, rows, h->bp, h->KK, bp_<int>(h, mld_gpu_handle::B_REV), Bq, dBq,
+                               bp_<T>(h, mld_gpu_handle::B_HQ), X, h->DL, h->st));
+        nl(h, 2);
+      }
+      return MLD_OK;
+    };
+    if (h->krr || !h->tune[0].done || h->rows_graph_off) {
+      // the kernel model's rows synchronise on a timeout flag, and the autotuner times its
+      // candidates: both run directly
+      int rc = stage();
+      if (rc) return rc;
+    } else {
+      // replayed as a CUDA graph, captured once per batch (and buffer generation)
+      const long long key[8] = {h->buf_gen, h->A, h->b.P, h->S, L.M, h->b.maxnn, h->quad ? 1 : 0,
+                                (long long)(uintptr_t)X};
+      if (!h->rows_graph || !std::equal(key, key + 8, h->rows_graph_key)) {
+        if (h->rows_graph) cudaGraphExecDestroy(h->rows_graph);
+        h->rows_graph = nullptr;
+        const long long l0 = h->cur_launches;
+        CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeRelaxed));
+        const int rc = stage();
+        cudaGraph_t g = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(h->st, &g);
+        if (rc) {
+          if (g) cudaGraphDestroy(g);
+          return rc;
+        }
+        cudaError_t ei = ec;
+        if (ec == cudaSuccess) ei = cudaGraphInstantiate(&h->rows_graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        const long long captured = h->cur_launches - l0;  // kernels of the graph
+        h->cur_launches = l0;
+        if (ei != cudaSuccess) {
+          // the capture did not take: clear the error and run the stage directly from now on
+          (void)cudaGetLastError();
+          h->rows_graph = nullptr;
+          h->rows_graph_off = true;
+          int rc2 = stage();
+          if (rc2) return rc2;
+        } else {
+          std::copy(key, key + 8, h->rows_graph_key);
+          h->rows_graph_launches = captured;
+        }
+      }
+      if (h->rows_graph) {
+        CK(cudaGraphLaunch(h->rows_graph, h->st));
+        nl(h, h->rows_graph_launches);
+      }
+    }
+    if (h->krr) {
       // kernel columns (compute_kernel.F90, mld_energy/forces/stress kernel packing)
       const size_t wse = krr_workspace_elems(h->A, h->nk, h->KK);
       CK(ensure(h, mld_gpu_handle::B_KWS, sizeof(T) * wse));
@@ -995,6 +1115,7 @@ int mld_gpu_create(const mld_gpu_config* cfg, mld_gpu_handle** out) {
 void mld_gpu_destroy(mld_gpu_handle* h) {
   if (!h) return;
   if (h->st) cudaStreamSynchronize(h->st);
+  if (h->rows_graph) cudaGraphExecDestroy(h->rows_graph);
   for (auto& bf : h->bufs)
     if (bf.p) cudaFree(bf.p);
   for (void* p : h->owned) cudaFree(p);
@@ -1552,6 +1673,7 @@ int handle_dims(const mld_gpu_handle* h, int* D, int* ldx, int* KK, int* nch) {
 // batch allocates what it needs again.
 void handle_release_buffers(mld_gpu_handle* h) {
   cudaStreamSynchronize(h->st);
+  ++h->buf_gen;
   for (int id = 0; id < mld_gpu_handle::B_COUNT; ++id) {
     if (id == mld_gpu_handle::B_EW) continue;
     Buf& bf = h->bufs[id];
@@ -1682,6 +1804,21 @@ extern "C" int mld_gpu_set_kernel_points(mld_gpu_handle* h, int nk, const double
   h->D = h->DL + nk;
   h->Dfull = h->D;
   h->ldx = round_up4(h->D);
+  return MLD_OK;
+}
+
+extern "C" int mld_gpu_tuning(const mld_gpu_handle* h, int mode, int* shape, int* ncand, double* ms) {
+  if (!h || mode < 0 || mode > 2 || !shape || !ncand) return MLD_ERR_INVALID;
+  const auto& tn = h->tune[mode];
+  shape[0] = tn.best.col_tile;
+  shape[1] = tn.best.ctas_per_sm;
+  shape[2] = tn.best.sorted_queue;
+  shape[3] = tn.done ? 1 : 0;
+  const int n = std::min<int>(*ncand, (int)tn.ms.size());
+  for (int i = 0; i < n; ++i) {
+    if (ms) ms[i] = tn.ms[i];
+  }
+  *ncand = (int)tn.ms.size();
   return MLD_OK;
 }
 

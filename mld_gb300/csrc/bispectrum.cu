@@ -359,7 +359,8 @@ __device__ __forceinline__ ZItem load_zitem(const ZItem* p) {
 // kYShared: Y lives in shared memory (the common case); otherwise in the per-CTA global slice
 // args.yglobal (FP64 with several channels), a separate instantiation so that the shared-memory
 // variant keeps shared-memory addressing.
-template <typename T, bool kYShared>
+// kCT: columns (neighbour, component) per register tile of the dB contraction (autotuned).
+template <typename T, bool kYShared, int kCT>
 __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(KernelArgs<T> args, int A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using Rec = typename RecEntry<T>::type;
@@ -560,7 +561,7 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
       }
       __syncthreads();  // V of the chunk complete; the recursion buffers become dBs
       const int ncols = 3 * nb_here;
-      const int ncolt = (ncols + kColTile - 1) / kColTile;
+      const int ncolt = (ncols + kCT - 1) / kCT;
       for (int ch = 0; ch < nch; ++ch) {
         const cx<T>* Yc = Y + (size_t)ch * NYP;
         // register-tiled contraction, item = (row tile of layer j, column tile), heaviest
@@ -577,28 +578,28 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
           const cx<T>* Yp = Yc + tb.yoff[j] + rt * kRowTile;
           // columns ct, ct + ncolt, ...: lanes of a warp read consecutive columns of V, whose
           // odd stride HU spreads them over distinct shared-memory banks
-          const cx<T>* Vp[kColTile];
+          const cx<T>* Vp[kCT];
 #pragma unroll
-          for (int c = 0; c < kColTile; ++c) {
+          for (int c = 0; c < kCT; ++c) {
             const int col = min(ct + c * ncolt, ncols - 1);
             Vp[c] = V + (size_t)col * HU + shoff[j];  // col = n*3 + a -> V[n][a][.]
           }
-          T acc[kRowTile][kColTile];
+          T acc[kRowTile][kCT];
 #pragma unroll
           for (int r = 0; r < kRowTile; ++r)
 #pragma unroll
-            for (int c = 0; c < kColTile; ++c) acc[r][c] = T(0);
+            for (int c = 0; c < kCT; ++c) acc[r][c] = T(0);
 #pragma unroll 2
           for (int e = 0; e < H; ++e) {
-            cx<T> y[kRowTile], v[kColTile];
+            cx<T> y[kRowTile], v[kCT];
 #pragma unroll
             for (int r = 0; r < kRowTile; ++r) y[r] = Yp[e * Mp + r];
 #pragma unroll
-            for (int c = 0; c < kColTile; ++c) v[c] = Vp[c][e];
+            for (int c = 0; c < kCT; ++c) v[c] = Vp[c][e];
 #pragma unroll
             for (int r = 0; r < kRowTile; ++r)
 #pragma unroll
-              for (int c = 0; c < kColTile; ++c) acc[r][c] = fma(y[r].x, v[c].x, fma(-y[r].y, v[c].y, acc[r][c]));
+              for (int c = 0; c < kCT; ++c) acc[r][c] = fma(y[r].x, v[c].x, fma(-y[r].y, v[c].y, acc[r][c]));
           }
 #pragma unroll
           for (int r = 0; r < kRowTile; ++r) {
@@ -608,7 +609,7 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
             T* base = rank == 0 ? dBs : (rank == 1 ? dB1 : dB2);
             const int ld = tb.nrank[rank];
 #pragma unroll
-            for (int c = 0; c < kColTile; ++c) {
+            for (int c = 0; c < kCT; ++c) {
               const int col = ct + c * ncolt;
               if (col < ncols) base[(size_t)col * ld + idx] = acc[r][c];
             }
@@ -695,7 +696,8 @@ size_t bso4_y_scratch_bytes(const DevTables& tb, int nch, int eb, int max_ctas) 
 template <typename T>
 cudaError_t launch_bso4(const DevTables& tb, const DevBatch& b, const BsoParams& p, T* Bout, T* dBout,
                         const DevEval<T>* ev, const int* order, int* counter, cudaStream_t st, void* yscratch,
-                        size_t yscratch_bytes) {
+                        size_t yscratch_bytes, const Bso4Launch* shape) {
+  const Bso4Launch sh = shape ? *shape : Bso4Launch{};
   if (b.A == 0) return cudaSuccess;
   if (!counter) return cudaErrorInvalidValue;
   KernelArgs<T> a{};
@@ -713,7 +715,7 @@ cudaError_t launch_bso4(const DevTables& tb, const DevBatch& b, const BsoParams&
   a.nbr_off = b.nbr_off;
   a.nbr_idx = b.nbr_idx;
   a.nbr_u = b.nbr_u;
-  a.order = order;
+  a.order = sh.sorted_queue ? order : nullptr;
   a.counter = counter;
   a.p = p;
   a.Bout = Bout;
@@ -724,13 +726,15 @@ cudaError_t launch_bso4(const DevTables& tb, const DevBatch& b, const BsoParams&
   const size_t smem = smem_plan(tb, p.nch, sizeof(T), y_in_smem).total;
   if (smem > (size_t)max_optin_smem()) return cudaErrorInvalidConfiguration;
   a.yglobal = nullptr;
-  auto kern = y_in_smem ? k_bso4<T, true> : k_bso4<T, false>;
+  auto kern = sh.col_tile == 2 ? (y_in_smem ? k_bso4<T, true, 2> : k_bso4<T, false, 2>)
+                               : (y_in_smem ? k_bso4<T, true, 4> : k_bso4<T, false, 4>);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int occ = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kNW * 32, smem);
   if (e != cudaSuccess) return e;
   if (occ < 1) return cudaErrorInvalidConfiguration;
+  if (sh.ctas_per_sm > 0) occ = std::min(occ, sh.ctas_per_sm);
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -750,8 +754,10 @@ cudaError_t launch_bso4(const DevTables& tb, const DevBatch& b, const BsoParams&
 }
 
 template cudaError_t launch_bso4<double>(const DevTables&, const DevBatch&, const BsoParams&, double*, double*,
-                                         const DevEval<double>*, const int*, int*, cudaStream_t, void*, size_t);
+                                         const DevEval<double>*, const int*, int*, cudaStream_t, void*, size_t,
+                                         const Bso4Launch*);
 template cudaError_t launch_bso4<float>(const DevTables&, const DevBatch&, const BsoParams&, float*, float*,
-                                        const DevEval<float>*, const int*, int*, cudaStream_t, void*, size_t);
+                                        const DevEval<float>*, const int*, int*, cudaStream_t, void*, size_t,
+                                        const Bso4Launch*);
 
 }  // namespace mld

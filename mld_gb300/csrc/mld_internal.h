@@ -12,7 +12,7 @@ constexpr int kMaxJ = 10;          // doubled angular momentum bound (j_max <= 5
 constexpr int kMaxTypes = 8;       // element types per handle
 constexpr int kMaxCh = 3;          // plain, weighted, weighted_3ch
 constexpr int kRowTile = 4;        // rows (triples) per register tile of the dB contraction
-constexpr int kColTile = 4;        // columns (neighbour, component) per register tile
+
 
 // Symmetry used throughout: U^j(-p,-q) = (-1)^((p-q)/2) conj(U^j(p,q)); the same holds for c,
 // the Z blocks and vecall.  Only the "half" of each layer is stored: the first
@@ -274,13 +274,20 @@ struct DevEval {
   double* Eatom = nullptr;       // A: energy of each atom (linear model; may be null)
 };
 
+// Launch shape of the descriptor kernel, chosen per handle by the autotuner (api.cu); every
+// shape gives bitwise the same results.
+struct Bso4Launch {
+  int col_tile = 4;      // columns per register tile of the dB contraction: 2 or 4
+  int ctas_per_sm = 0;   // persistent CTAs per SM (0: as many as fit)
+  int sorted_queue = 1;  // atoms longest first (1) or in index order (0)
+};
 // Descriptor kernel (bispectrum.cu): B (A x nch*K) and w_ch * dB (P x 3 x nch*K) of the batch,
 // either may be null; or evaluation (ev->pair set, dBout null).  Atoms are taken in `order`
 // (null: index order) through `counter` (one int of device memory, reset by the launch).
 template <typename T>
 cudaError_t launch_bso4(const DevTables& tb, const DevBatch& b, const BsoParams& p, T* Bout, T* dBout,
                         const DevEval<T>* ev, const int* order, int* counter, cudaStream_t st,
-                        void* yscratch = nullptr, size_t yscratch_bytes = 0);
+                        void* yscratch = nullptr, size_t yscratch_bytes = 0, const Bso4Launch* shape = nullptr);
 // Linear design rows of the batch from B, w_ch * dB and the reverse pairs (rows.cu); Sp is a
 // workspace of A x 6 x KK stress partials.  Columns [1, 1 + KK) of the energy, force and stress
 // rows are written.

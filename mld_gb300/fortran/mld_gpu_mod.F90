@@ -50,7 +50,7 @@ module mld_gpu_mod
             mld_gpu_server_admission, &
             mld_gpu_descriptor_derivatives, mld_gpu_last_error, mld_gpu_server_last_error, &
             mld_gpu_set_profiling, mld_gpu_profile, mld_gpu_timer_start, mld_gpu_timer_stop, &
-            mld_gpu_work_counts, mld_gpu_peak_flops, mld_gpu_descriptors_noalloc, mld_gpu_test_pipeline_timeout, &
+            mld_gpu_work_counts, mld_gpu_peak_flops, mld_gpu_descriptors_noalloc, mld_gpu_test_pipeline_timeout, mld_gpu_tuning, &
             mld_gpu_synchronize
 
   interface
@@ -270,6 +270,15 @@ module mld_gpu_mod
       type(c_ptr), value :: srv
       integer(c_long_long), intent(out) :: batches, atoms_done
       real(c_double), intent(out) :: budget_bytes
+    end function
+
+    integer(c_int) function mld_gpu_tuning(h, mode, shape, ncand, ms) bind(C, name="mld_gpu_tuning")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      integer(c_int), value :: mode
+      integer(c_int), intent(out) :: shape(4)
+      integer(c_int), intent(inout) :: ncand
+      real(c_double), intent(out) :: ms(*)
     end function
 
     integer(c_int) function mld_gpu_test_pipeline_timeout(skip_loads, wait_limit_clocks) &
