@@ -206,8 +206,10 @@ int mld_gpu_solve_info(const mld_gpu_handle* h, int* pcg_iterations /*[2]*/, dou
                        double* precond_shift /*[2]*/, int* chol_retries);
 
 /* Launch shape of the descriptor kernel chosen by the handle's autotuner for one output mode
- * (0: design rows, i.e. B and dB; 1: evaluation with fitted weights; 2: descriptors only).  The
- * tuner times every candidate once on the first batch with enough atoms and keeps the fastest;
+ * (0: design rows, i.e. B and dB; 1: evaluation with fitted weights; 2: descriptors only).  Only
+ * mode 0 is tuned (modes 1 and 2 run the default shape: column tile 4, as many CTAs per SM as
+ * fit, longest-first queue).  The tuner times every candidate once on the first batch with
+ * enough atoms (64 per SM) and keeps the fastest;
  * all candidates give bitwise the same results.  shape[4] = {column tile (4 or 2), persistent
  * CTAs per SM (0 = as many as fit), longest-first queue (1) or index order (0), tuned (1/0)};
  * *ncand: capacity of ms on input, candidates timed on output; ms[i] the time [ms] of candidate

@@ -109,7 +109,7 @@ struct mld_gpu_handle {
   bool rows_graph_off = false;  // a capture failed once: run the stage directly from then on
 
   std::vector<void*> owned;  // table allocations
-  Buf bufs[64];
+  Buf bufs[80];
   enum {
     B_ATOM_START, B_ATOM_STRUCT, B_TYPES, B_POS, B_CELL, B_RECIP, B_SMALL, B_NSIZE, B_VOL,
     B_NN, B_NBR_OFF, B_NBR_IDX, B_NBR_U, B_SCAN_TMP, B_MAXNN,
@@ -119,9 +119,10 @@ struct mld_gpu_handle {
     B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
     B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV, B_KZD, B_KZF, B_KWS, B_WSERVE, B_P32,
     B_EW, B_EBETA, B_EB, B_EOUT, B_KTC, B_SKW, B_ORDER, B_QCNT, B_SP, B_EPAIR, B_EATOM, B_GP,
+    B_CNC, B_CELLOFF, B_CELLOF, B_CELLSTART, B_CELLATOMS, B_SORTTMP,
     B_COUNT
   };
-  static_assert(B_COUNT <= 64, "buffer table too small");
+  static_assert(B_COUNT <= 80, "buffer table too small");
 };
 
 namespace {
@@ -257,6 +258,11 @@ int build_neighbours(mld_gpu_handle* h) {
   b.nbr_off = bp_<int>(h, mld_gpu_handle::B_NBR_OFF);
   int* dmax = bp_<int>(h, mld_gpu_handle::B_MAXNN);
   CK(cudaMemsetAsync(dmax, 0, sizeof(int), h->st));
+  if (b.ncells > 0) {
+    CK(ensure(h, mld_gpu_handle::B_SCAN_TMP, sizeof(int) * ((std::max(h->A, b.ncells) + 1023) / 1024 + 2)));
+    CK(launch_cells(b, bp_<int>(h, mld_gpu_handle::B_SCAN_TMP), h->st));
+    nl(h, 5);
+  }
   CK(launch_neighbours(b, h->cfg.r_cut, b.nn, dmax, h->st, 0));
   CK(launch_scan(b.nn, b.nbr_off, h->A, bp_<int>(h, mld_gpu_handle::B_SCAN_TMP), h->st));
   nl(h, 5);
@@ -275,6 +281,12 @@ int build_neighbours(mld_gpu_handle* h) {
   CK(ensure(h, mld_gpu_handle::B_NBR_U, sizeof(double) * 3 * std::max<long long>(b.P, 1)));
   b.nbr_idx = bp_<int>(h, mld_gpu_handle::B_NBR_IDX);
   b.nbr_u = bp_<double>(h, mld_gpu_handle::B_NBR_U);
+  if (b.ncells > 0 && b.P > 0) {
+    // workspace of the sort of the celled structures' lists (inside the filling pass)
+    CK(ensure(h, mld_gpu_handle::B_SORTTMP, sizeof(int) * (size_t)b.P));
+    b.sort_tmp = bp_<int>(h, mld_gpu_handle::B_SORTTMP);
+    nl(h, 1);
+  }
   CK(launch_neighbours(b, h->cfg.r_cut, b.nn, dmax, h->st, 1));
   nl(h, b.P > 0 ? 2 : 1);  // filling pass and pair displacements
   // longest-first order of the descriptor kernel's work queue; one counter int + sort workspace
@@ -304,8 +316,8 @@ int y_scratch(mld_gpu_handle* h, void** p, size_t* bytes) {
   return MLD_OK;
 }
 
-// Autotuner of the descriptor kernel's launch shape: on the first batch large enough (at least
-// kTuneMinAtoms atoms per SM) each candidate shape (column tile 4 or 2, as many persistent CTAs
+// Autotuner of the descriptor kernel's launch shape for the design rows of a fit: on the first
+// batch large enough (at least kTuneMinAtoms atoms per SM) each candidate shape (column tile 4 or 2, as many persistent CTAs
 // per SM as fit or one, longest-first or index-order queue) runs once on the real batch, timed
 // with CUDA events on the handle's stream, and the fastest is kept for the handle.  Every shape
 // computes bitwise the same outputs, so the last candidate's run is the result.
@@ -316,7 +328,9 @@ int tuned_launch(mld_gpu_handle* h, int mode, T* Bout, T* dB, const DevEval<T>* 
   auto& tn = h->tune[mode];
   const int* order = bp_<int>(h, mld_gpu_handle::B_ORDER);
   int* counter = bp_<int>(h, mld_gpu_handle::B_QCNT);
-  if (tn.done || h->A < kTuneMinAtoms * std::max(1, h->nsm)) {
+  // only the design-row stage of a fit is tuned: it is repeated on the same batch, while
+  // evaluation batches (serving) and descriptor dumps change from call to call
+  if (tn.done || mode != 0 || h->A < kTuneMinAtoms * std::max(1, h->nsm)) {
     CK(launch_bso4<T>(h->dt, h->b, h->bp, Bout, dB, ev, order, counter, h->st, ys, ysb, &tn.best));
     return MLD_OK;
   }
@@ -1156,6 +1170,10 @@ int mld_gpu_set_structures(mld_gpu_handle* h, int nstruct, const int* nat, const
     if (!std::isfinite(pos[i])) return fail(h, MLD_ERR_INVALID, "non-finite position");
   std::vector<double> rec(9 * (size_t)nstruct), vol(nstruct);
   std::vector<int> small(nstruct), nsize(3 * (size_t)nstruct);
+  // linked cells of large boxes with at least kCellMinAtoms atoms and three cells along some
+  // direction: cells at least r_cut + 1e-3 A wide (perpendicular width / count)
+  constexpr int kCellMinAtoms = 64;
+  std::vector<int> cnc(3 * (size_t)nstruct, 0), cell_off(nstruct + 1, 0);
   for (int s = 0; s < nstruct; ++s) {
     const double* cl = cell + 9 * (size_t)s;
     recips(cl, &rec[9 * (size_t)s]);
@@ -1177,6 +1195,21 @@ int mld_gpu_set_structures(mld_gpu_handle* h, int nstruct, const int* nat, const
                                             ": cell too thin for r_cut (more than 127 periodic images along a lattice vector)");
     }
     small[s] = sm;
+    int ncell = 0;
+    if (!sm && nat[s] >= kCellMinAtoms) {
+      int n[3], mx = 0;
+      for (int i = 0; i < 3; ++i) {
+        const double* bgi = &rec[9 * (size_t)s + 3 * i];
+        const double width = 1.0 / std::sqrt(bgi[0] * bgi[0] + bgi[1] * bgi[1] + bgi[2] * bgi[2]);
+        n[i] = std::max(1, std::min(1024, (int)std::floor(width / (h->cfg.r_cut + 1e-3))));
+        mx = std::max(mx, n[i]);
+      }
+      if (mx >= 3 && (long long)n[0] * n[1] * n[2] <= 4LL * nat[s] + 64) {
+        for (int i = 0; i < 3; ++i) cnc[3 * s + i] = n[i];
+        ncell = n[0] * n[1] * n[2];
+      }
+    }
+    cell_off[s + 1] = cell_off[s] + ncell;
   }
   h->S = nstruct;
   h->A = A;
@@ -1194,7 +1227,21 @@ int mld_gpu_set_structures(mld_gpu_handle* h, int nstruct, const int* nat, const
   if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_SMALL, small.data(), small.size());
   if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_NSIZE, nsize.data(), nsize.size());
   if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_VOL, vol.data(), vol.size());
+  const int ncells = cell_off[nstruct];
+  if (ncells > 0) {
+    if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_CNC, cnc.data(), cnc.size());
+    if (e == cudaSuccess) e = upload(h, mld_gpu_handle::B_CELLOFF, cell_off.data(), cell_off.size());
+    if (e == cudaSuccess) e = ensure(h, mld_gpu_handle::B_CELLOF, sizeof(int) * (size_t)std::max(1, A));
+    if (e == cudaSuccess) e = ensure(h, mld_gpu_handle::B_CELLSTART, sizeof(int) * (2 * (size_t)ncells + 1));
+    if (e == cudaSuccess) e = ensure(h, mld_gpu_handle::B_CELLATOMS, sizeof(int) * (size_t)std::max(1, A));
+  }
   if (e != cudaSuccess) return cuda_fail(h, e, "mld_gpu_set_structures");
+  b.ncells = ncells;
+  b.cnc = ncells ? bp_<int>(h, mld_gpu_handle::B_CNC) : nullptr;
+  b.cell_off = ncells ? bp_<int>(h, mld_gpu_handle::B_CELLOFF) : nullptr;
+  b.cell_of = ncells ? bp_<int>(h, mld_gpu_handle::B_CELLOF) : nullptr;
+  b.cell_start = ncells ? bp_<int>(h, mld_gpu_handle::B_CELLSTART) : nullptr;
+  b.cell_atoms = ncells ? bp_<int>(h, mld_gpu_handle::B_CELLATOMS) : nullptr;
   b.atom_start = bp_<int>(h, mld_gpu_handle::B_ATOM_START);
   b.atom_struct = bp_<int>(h, mld_gpu_handle::B_ATOM_STRUCT);
   b.types = bp_<int>(h, mld_gpu_handle::B_TYPES);

@@ -229,6 +229,14 @@ struct DevBatch {
   double* nbr_u = nullptr;   // 3P  (x_neighbour - x_centre, FP64)
   long long P = 0;
   int maxnn = 0;             // largest neighbour count (after the counting pass)
+  // linked cells of large boxes (null cnc: every structure scans all its atoms)
+  int* cnc = nullptr;        // 3S cells per lattice direction, 0 for a structure without cells
+  int* cell_off = nullptr;   // S+1 first cell of each structure
+  int ncells = 0;
+  int* cell_of = nullptr;    // A cell of each atom (-1 without cells)
+  int* cell_start = nullptr; // ncells+1 first entry of each cell in cell_atoms (then a cursor of ncells)
+  int* cell_atoms = nullptr; // A atoms grouped by cell
+  int* sort_tmp = nullptr;   // P  neighbour indices while the lists of celled structures are sorted
 };
 
 // Design-row placement of each structure (-1 when a block is absent).
@@ -257,6 +265,11 @@ inline int round_up4(int d) { return (d + 3) & ~3; }
 cudaError_t launch_neighbours(const DevBatch& b, double rcut, int* counts, int* maxcount, cudaStream_t st,
                               int pass /*0 count, 1 fill*/);
 cudaError_t launch_scan(const int* in, int* out, int n, int* d_tmp, cudaStream_t st);
+// Bin the atoms of celled structures (b.cnc) into their cells; scan_tmp as for launch_scan over
+// b.ncells entries.  Then launch_neighbours scans the 27 (or fewer, unique) cells around each
+// atom, and launch_sort_lists restores the ascending neighbour order of those atoms' lists.
+cudaError_t launch_cells(const DevBatch& b, int* scan_tmp, cudaStream_t st);
+cudaError_t launch_sort_lists(const DevBatch& b, cudaStream_t st);
 
 // Y scratch the descriptor kernel needs in global memory for up to max_ctas CTAs (0 when Y fits
 // in shared memory); pass it to launch_bso4, which then runs at most that many persistent CTAs.

@@ -1,5 +1,13 @@
 // Neighbour lists within r < r_cut for a batch of periodic structures (one warp per atom).
 //
+// Large boxes with at least three cells of width r_cut along some lattice direction use linked
+// cells: atoms are binned by their fractional coordinates into nc_1 x nc_2 x nc_3 cells (each at
+// least r_cut + 1e-3 A wide, so every neighbour lies in one of the 27 cells around an atom's
+// own, or fewer where a direction has one or two cells), the warp of an atom scans those cells,
+// and each list is then sorted by neighbour index, the order of the all-atom scan.  This is the
+// cell decomposition of the reference's large-box search (neighbours.F90:1091-1139,
+// ondm_caltabt.F90, ondm_caltabi.F90), with the list order of its per-atom tables.
+//
 // Small box (some perpendicular cell width below 2*r_cut): every atom j and periodic image
 // n in [-nsize, nsize]^3 is a candidate, u = x_j + n.cell - x_i, kept when 1e-15 <= |u|^2 and
 // |u| < r_cut -- MILADY src/mld/neighbours.F90:1147-1328 followed by the strict filter of
@@ -67,7 +75,9 @@ __global__ void __launch_bounds__(256) k_neighbours(
     const float4* __restrict__ pos32, const float4* __restrict__ frac32, const double* __restrict__ cell,
     const double* __restrict__ recip, const int* __restrict__ small, const int* __restrict__ nsize, double rcut,
     int pass, int* __restrict__ counts, int* __restrict__ maxcount, const int* __restrict__ offsets,
-    int* __restrict__ nbr_idx, double* __restrict__ nbr_u) {
+    int* __restrict__ nbr_idx, double* __restrict__ nbr_u, const int* __restrict__ cnc,
+    const int* __restrict__ cell_off, const int* __restrict__ cell_of, const int* __restrict__ cell_start,
+    const int* __restrict__ cell_atoms) {
   constexpr float kBand = 1e-3f;
   const int lane = threadIdx.x & 31;
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -93,9 +103,63 @@ __global__ void __launch_bounds__(256) k_neighbours(
     n3s = nsize[3 * s + 2];
     nimg = (2 * n1s + 1) * (2 * n2s + 1) * (2 * n3s + 1);
   }
-  const long long ncand = (long long)nat * nimg;
   int count = 0;
   const int wbase = (pass == 1) ? offsets[g] : 0;
+  if (!sm && cnc && cnc[3 * s] > 0) {
+    // linked cells: the unique cells within one cell of the atom's own, in a fixed order
+    const int n0 = cnc[3 * s], n1 = cnc[3 * s + 1], n2 = cnc[3 * s + 2];
+    const int own = cell_of[g] - cell_off[s];
+    const int c0 = own / (n1 * n2), c1 = (own / n2) % n1, c2 = own % n2;
+    const int lo0 = n0 >= 3 ? -1 : 0, hi0 = n0 >= 3 ? 1 : n0 - 1;
+    const int lo1 = n1 >= 3 ? -1 : 0, hi1 = n1 >= 3 ? 1 : n1 - 1;
+    const int lo2 = n2 >= 3 ? -1 : 0, hi2 = n2 >= 3 ? 1 : n2 - 1;
+    for (int d0 = lo0; d0 <= hi0; ++d0)
+      for (int d1 = lo1; d1 <= hi1; ++d1)
+        for (int d2 = lo2; d2 <= hi2; ++d2) {
+          const int cell = cell_off[s] + (((c0 + d0 + n0) % n0) * n1 + (c1 + d1 + n1) % n1) * n2 + (c2 + d2 + n2) % n2;
+          const int e0 = cell_start[cell], e1 = cell_start[cell + 1];
+          for (int base = e0; base < e1; base += 32) {
+            const int e = base + lane;
+            bool ok = false;
+            int jg = 0;
+            if (e < e1) {
+              jg = cell_atoms[e];
+              if (jg != g) {
+                const float4 fj = frac32[jg];
+                float d0f = fj.x - fi.x, d1f = fj.y - fi.y, d2f = fj.z - fi.z;
+                d0f -= rintf(d0f);
+                d1f -= rintf(d1f);
+                d2f -= rintf(d2f);
+                const float g0 = c32[0] * d0f + c32[3] * d1f + c32[6] * d2f;
+                const float g1 = c32[1] * d0f + c32[4] * d1f + c32[7] * d2f;
+                const float g2 = c32[2] * d0f + c32[5] * d1f + c32[8] * d2f;
+                const float r2f = g0 * g0 + g1 * g1 + g2 * g2;
+                if (r2f < rci2) {
+                  ok = true;
+                } else if (r2f < rcb2) {
+                  double u[3];
+                  min_image_u(pos, jg, xi0, xi1, xi2, cl, bg, u);
+                  ok = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) < rcut;
+                }
+              }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, ok);
+            if (pass == 1 && ok) {
+              const int slot = wbase + count + __popc(m & ((1u << lane) - 1u));
+              nbr_idx[slot] = jg;
+              nbr_u[3 * (size_t)slot] = (double)g;
+              nbr_u[3 * (size_t)slot + 1] = (double)pack_image(0, 0, 0);
+            }
+            count += __popc(m);
+          }
+        }
+    if (pass == 0 && lane == 0) {
+      counts[g] = count;
+      atomicMax(maxcount, count);
+    }
+    return;
+  }
+  const long long ncand = (long long)nat * nimg;
   for (long long base = 0; base < ncand; base += 32) {
     const long long cidx = base + lane;
     bool ok = false;
@@ -259,6 +323,86 @@ cudaError_t launch_scan(const int* in, int* out, int n, int* d_tmp, cudaStream_t
   return cudaGetLastError();
 }
 
+// Cell of every atom of a celled structure from its fractional coordinates wrapped into [0, 1)
+// in FP64; cell_start[cell] counts the cell's atoms (the scan turns the counts into offsets).
+__global__ void k_cell_bin(int A, const int* __restrict__ atom_struct, const double* __restrict__ pos,
+                           const double* __restrict__ recip, const int* __restrict__ cnc,
+                           const int* __restrict__ cell_off, int* __restrict__ cell_of, int* __restrict__ count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A) return;
+  const int s = atom_struct[i];
+  const int n[3] = {cnc[3 * s], cnc[3 * s + 1], cnc[3 * s + 2]};
+  if (n[0] == 0) {
+    cell_of[i] = -1;
+    return;
+  }
+  const double* bg = recip + 9 * (size_t)s;
+  const double x0 = pos[3 * (size_t)i], x1 = pos[3 * (size_t)i + 1], x2 = pos[3 * (size_t)i + 2];
+  int c[3];
+  for (int k = 0; k < 3; ++k) {
+    double f = x0 * bg[3 * k] + x1 * bg[3 * k + 1] + x2 * bg[3 * k + 2];
+    f -= floor(f);
+    c[k] = min(n[k] - 1, max(0, (int)(f * n[k])));
+  }
+  const int cell = cell_off[s] + (c[0] * n[1] + c[1]) * n[2] + c[2];
+  cell_of[i] = cell;
+  atomicAdd(&count[cell], 1);
+}
+
+// atoms into their cells (order within a cell arbitrary: the lists are sorted afterwards)
+__global__ void k_cell_fill(int A, const int* __restrict__ cell_of, const int* __restrict__ cell_start,
+                            int* __restrict__ cursor, int* __restrict__ cell_atoms) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A) return;
+  const int cell = cell_of[i];
+  if (cell < 0) return;
+  cell_atoms[cell_start[cell] + atomicAdd(&cursor[cell], 1)] = i;
+}
+
+// the list of an atom of a celled structure, sorted by neighbour index (ranks of distinct
+// values; one warp per atom); other atoms' lists are copied as they are
+__global__ void k_sort_lists(int A, const int* __restrict__ cell_of, const int* __restrict__ nbr_off,
+                             const int* __restrict__ idx, int* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (g >= A) return;
+  const int p0 = nbr_off[g], n = nbr_off[g + 1] - p0;
+  const bool sort = cell_of[g] >= 0;
+  for (int e = lane; e < n; e += 32) {
+    const int x = idx[p0 + e];
+    int rank = e;
+    if (sort) {
+      rank = 0;
+      for (int f = 0; f < n; ++f) rank += idx[p0 + f] < x;
+    }
+    out[p0 + rank] = x;
+  }
+}
+
+cudaError_t launch_cells(const DevBatch& b, int* scan_tmp, cudaStream_t st) {
+  if (b.A == 0 || b.ncells == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(b.cell_start + b.ncells + 1, 0, sizeof(int) * b.ncells, st);
+  if (e != cudaSuccess) return e;
+  int* count = b.cell_start + b.ncells + 1;  // counts, then the fill cursor
+  k_cell_bin<<<(b.A + 255) / 256, 256, 0, st>>>(b.A, b.atom_struct, b.pos, b.recip, b.cnc, b.cell_off, b.cell_of,
+                                               count);
+  e = launch_scan(count, b.cell_start, b.ncells, scan_tmp, st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(count, 0, sizeof(int) * b.ncells, st);
+  if (e != cudaSuccess) return e;
+  k_cell_fill<<<(b.A + 255) / 256, 256, 0, st>>>(b.A, b.cell_of, b.cell_start, count, b.cell_atoms);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sort_lists(const DevBatch& b, cudaStream_t st) {
+  if (b.A == 0 || b.ncells == 0 || b.P == 0) return cudaSuccess;
+  const long long threads = (long long)b.A * 32;
+  k_sort_lists<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(b.A, b.cell_of, b.nbr_off, b.nbr_idx, b.sort_tmp);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(b.nbr_idx, b.sort_tmp, sizeof(int) * (size_t)b.P, cudaMemcpyDeviceToDevice, st);
+}
+
 cudaError_t launch_neighbours(const DevBatch& b, double rcut, int* counts, int* maxcount, cudaStream_t st, int pass) {
   if (b.A == 0) return cudaSuccess;
   const int threads = 256;
@@ -269,7 +413,14 @@ cudaError_t launch_neighbours(const DevBatch& b, double rcut, int* counts, int* 
     k_nbr_prep<<<(b.A + 255) / 256, 256, 0, st>>>(b.A, b.atom_struct, b.atom_start, b.pos, b.recip, b.pos32, b.frac32);
   k_neighbours<<<blocks, threads, 0, st>>>(b.A, b.atom_struct, b.atom_start, b.pos, b.pos32, b.frac32, b.cell,
                                            b.recip, b.small, b.nsize, rcut, pass, counts, maxcount, b.nbr_off,
-                                           b.nbr_idx, b.nbr_u);
+                                           b.nbr_idx, b.nbr_u, b.ncells > 0 ? b.cnc : nullptr, b.cell_off,
+                                           b.cell_of, b.cell_start, b.cell_atoms);
+  if (pass == 1 && b.P > 0 && b.ncells > 0) {
+    // ascending neighbour order of the celled structures' lists, before their displacements
+    if (!b.sort_tmp) return cudaErrorInvalidValue;
+    cudaError_t e = launch_sort_lists(b, st);
+    if (e != cudaSuccess) return e;
+  }
   if (pass == 1 && b.P > 0)
     k_nbr_u<<<(unsigned)((b.P + 255) / 256), 256, 0, st>>>(b.P, b.atom_struct, b.pos, b.cell, b.recip, b.small,
                                                            b.nbr_idx, b.nbr_u);
