@@ -9,8 +9,8 @@
 // Outputs: B per atom and w_ch * dB per pair (the design rows are gathered from them by
 // rows.cu), or, for evaluation with fitted weights, per-pair force and stress contributions.
 // Only half of every layer is computed (X(-p,-q) = (-1)^((p-q)/2) conj X(p,q) for U, c, Z, V);
-// full-layer sums fold into weighted sums over the half.  Both recursions run on groups of 16
-// lanes per neighbour; phase 2 follows a host-balanced schedule of rounds of 32 equal-shape
+// full-layer sums fold into weighted sums over the half.  The recursions run on groups of 8
+// (phase 1) and 16 (phase 3) lanes per neighbour; phase 2 follows a host-balanced schedule of rounds of 32 equal-shape
 // terms per warp.
 //
 // Every floating-point sum has a fixed order: lane groups accumulate privately and are reduced
@@ -289,6 +289,7 @@ struct KernelArgs {
   // Y (the contracted Z blocks, nch * NYP complex per atom) in global memory, one slice per CTA,
   // when it does not fit in shared memory next to the rest (FP64 with several channels)
   void* yglobal;
+  int g1;  // lanes per neighbour in phase 1 (8 or 16)
   // outputs: B (A x nch*K) and w_ch * dB (P x 3 x nch*K); or evaluation (ev.pair != nullptr)
   T* Bout;
   T* dBout;
@@ -296,9 +297,11 @@ struct KernelArgs {
 };
 
 constexpr int kNW = 8;                  // warps per CTA (== kZWarps)
-constexpr int kG = 16;                  // lanes per neighbour in both recursions
-constexpr int kNG = kNW * 32 / kG;      // lane groups per CTA
+constexpr int kG = 16;                  // lanes per neighbour in the U/dU recursion (phase 3)
+constexpr int kNG = kNW * 32 / kG;      // lane groups per CTA in phase 3
 constexpr int kNB = kNG;                // neighbours per phase-3 chunk (one per group)
+// lanes per neighbour in the U recursion of phase 1: 8 (32 neighbours in flight) where the
+// groups' partial sums fit in shared memory next to the rest, else 16 (KernelArgs::g1)
 static_assert(kNW == kZWarps, "phase-2 schedule is built for the CTA's warps");
 
 // Shared-memory carve-up, in order (every region 16-byte aligned):
@@ -315,11 +318,12 @@ struct SmemPlan {
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-__host__ __device__ inline SmemPlan smem_plan(const DevTables& tb, int nch, int eb, bool y_in_smem) {
+__host__ __device__ inline SmemPlan smem_plan(const DevTables& tb, int nch, int eb, bool y_in_smem, int g1 = 16) {
+  const int ng1 = kNW * 32 / g1;
   const size_t LH = tb.hoff[tb.J + 1] - tb.hoff[tb.J];
   const size_t cxb = 2 * (size_t)eb;
   const size_t recb = eb == 8 ? sizeof(RecEntry64) : sizeof(RecEntry32);
-  const size_t v1 = (size_t)kNG * nch * tb.HU + (size_t)kNG * 2 * LH;  // phase 1
+  const size_t v1 = (size_t)ng1 * nch * tb.HU + (size_t)ng1 * 2 * LH;  // phase 1
   const size_t v2 = (size_t)tb.NZT;                                      // phase 2
   const size_t v3 = (size_t)kNB * 3 * tb.HU;                             // phase 3
   const size_t vblock = v1 > v2 ? (v1 > v3 ? v1 : v3) : (v2 > v3 ? v2 : v3);
@@ -356,6 +360,35 @@ __device__ __forceinline__ ZItem load_zitem(const ZItem* p) {
   return z;
 }
 
+// Phase 1 of one atom: lane groups of G1 lanes take the neighbours in turn and add
+// f_c w_ch U of each to their private partial in V (group g at V + g*nch*HU, recursion buffers
+// behind the partials of all groups).
+template <typename T, int G1>
+__device__ __forceinline__ void phase1_c(const KernelArgs<T>& args, const typename RecEntry<T>::type* srec,
+                                         const int* shoff, cx<T>* V, int nn, int p0, int ti, T rcut, T inv_r0, int J,
+                                         int HU, int LH, int nch, int warp, int lane, int tid) {
+  constexpr int NG1 = kNW * 32 / G1;
+  const int grp1 = tid / G1, sl1 = tid % G1;
+  cx<T>* cpart = V + (size_t)grp1 * nch * HU;
+  cx<T>* ub = V + (size_t)NG1 * nch * HU + (size_t)grp1 * 2 * LH;
+  for (int e = sl1; e < nch * HU; e += G1) cpart[e] = {T(0), T(0)};
+  __syncwarp();
+  for (int nb0 = warp * (32 / G1); nb0 < nn; nb0 += NG1) {
+    const int n = nb0 + (lane / G1);
+    const bool active = n < nn;
+    NbrGeom<T> g;
+    T wch[kMaxCh] = {T(0), T(0), T(0)};
+    if (active) {
+      const int nb = args.nbr_idx[p0 + n];
+      const int tn = args.types[nb];
+      const double rin = args.p.has_rin ? args.p.rin[ti * args.p.ntypes + tn] : 0.0;
+      nbr_geometry<T>(args.nbr_u + 3 * (size_t)(p0 + n), rcut, inv_r0, rin, args.p.rin_width, &g);
+      for (int ch = 0; ch < nch; ++ch) wch[ch] = (T)args.p.chw[ch * args.p.ntypes + tn];
+    }
+    group_recursion<T, G1, false>(g, srec, J, shoff, ub, LH, nullptr, cpart, wch, nch, HU, sl1, active);
+  }
+}
+
 // kYShared: Y lives in shared memory (the common case); otherwise in the per-CTA global slice
 // args.yglobal (FP64 with several channels), a separate instantiation so that the shared-memory
 // variant keeps shared-memory addressing.
@@ -371,7 +404,8 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int nth = kNW * 32;
   const int LH = tb.hoff[J + 1] - tb.hoff[J];  // largest half layer
-  const SmemPlan sp = smem_plan(tb, nch, (int)sizeof(T), kYShared);
+  const SmemPlan sp = smem_plan(tb, nch, (int)sizeof(T), kYShared, args.g1);
+  const int ng1 = kNW * 32 / args.g1;
 
   Rec* srec = reinterpret_cast<Rec*>(smem_raw + sp.rec);
   int* shoff = reinterpret_cast<int*>(smem_raw + sp.hoff);
@@ -418,31 +452,15 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
     // ---------------- phase 1: c^j on half layers, one lane group per neighbour ------------
     // (the CG coefficients of phase 2 are loaded into W meanwhile; W held the previous atom's dB)
     for (int e = tid; e < tb.NCG; e += nth) scg[e] = args.cg[e];
-    {
-      cx<T>* cpart = V + (size_t)grp * nch * HU;
-      cx<T>* ub = V + (size_t)kNG * nch * HU + (size_t)grp * 2 * LH;
-      for (int e = sl; e < nch * HU; e += kG) cpart[e] = {T(0), T(0)};
-      __syncwarp();
-      for (int nb0 = warp * (32 / kG); nb0 < nn; nb0 += kNG) {
-        const int n = nb0 + (lane / kG);
-        const bool active = n < nn;
-        NbrGeom<T> g;
-        T wch[kMaxCh] = {T(0), T(0), T(0)};
-        if (active) {
-          const int nb = args.nbr_idx[p0 + n];
-          const int tn = args.types[nb];
-          const double rin = args.p.has_rin ? args.p.rin[ti * args.p.ntypes + tn] : 0.0;
-          nbr_geometry<T>(args.nbr_u + 3 * (size_t)(p0 + n), rcut, inv_r0, rin, args.p.rin_width, &g);
-          for (int ch = 0; ch < nch; ++ch) wch[ch] = (T)args.p.chw[ch * args.p.ntypes + tn];
-        }
-        group_recursion<T, kG, false>(g, srec, J, shoff, ub, LH, nullptr, cpart, wch, nch, HU, sl, active);
-      }
-    }
+    if (args.g1 == 8)
+      phase1_c<T, 8>(args, srec, shoff, V, nn, p0, ti, rcut, inv_r0, J, HU, LH, nch, warp, lane, tid);
+    else
+      phase1_c<T, 16>(args, srec, shoff, V, nn, p0, ti, rcut, inv_r0, J, HU, LH, nch, warp, lane, tid);
     __syncthreads();
     // group partials summed in group order; the diagonal's +1; expansion to full layers
     for (int e = tid; e < nch * HU; e += nth) {
       cx<T> v = {T(0), T(0)};
-      for (int w = 0; w < kNG; ++w) {
+      for (int w = 0; w < ng1; ++w) {
         const cx<T> q = V[(size_t)w * nch * HU + e];
         v.x += q.x;
         v.y += q.y;
@@ -723,7 +741,12 @@ cudaError_t launch_bso4(const DevTables& tb, const DevBatch& b, const BsoParams&
   if (ev) a.ev = *ev;
   if (a.ev.pair && dBout) return cudaErrorInvalidValue;
   const bool y_in_smem = smem_plan(tb, p.nch, sizeof(T), true).total <= (size_t)max_optin_smem();
-  const size_t smem = smem_plan(tb, p.nch, sizeof(T), y_in_smem).total;
+  // 8-lane phase-1 groups where their partials fit without costing a resident CTA per SM
+  const size_t s16 = smem_plan(tb, p.nch, sizeof(T), y_in_smem, 16).total;
+  const size_t s8 = smem_plan(tb, p.nch, sizeof(T), y_in_smem, 8).total;
+  const size_t per_sm = 228 * 1024;
+  a.g1 = (s8 <= (size_t)max_optin_smem() && per_sm / (s8 + 1024) >= per_sm / (s16 + 1024)) ? 8 : 16;
+  const size_t smem = a.g1 == 8 ? s8 : s16;
   if (smem > (size_t)max_optin_smem()) return cudaErrorInvalidConfiguration;
   a.yglobal = nullptr;
   auto kern = sh.col_tile == 2 ? (y_in_smem ? k_bso4<T, true, 2> : k_bso4<T, false, 2>)

@@ -202,6 +202,27 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
     *err = "contraction tables exceed 16-bit offsets";
     return false;
   }
+  // Z outputs with identical operands (the same c entries, CG lists and extents, e.g. the ZA
+  // block of one triple and the ZB block of another) are one computation: each is evaluated
+  // once, into the term buffer at its computation index, and every slot reads it there with its
+  // own scale
+  std::vector<int> zu(t->zterms.size());
+  std::vector<int> zrep;  // representative output of each computation
+  {
+    std::map<std::tuple<int, int, int, int, int, int, int, int>, int> ids;
+    for (size_t zi = 0; zi < t->zterms.size(); ++zi) {
+      const ZTerm& z = t->zterms[zi];
+      const auto key = std::make_tuple((int)z.i1, (int)z.i2, (int)z.cg1, (int)z.cg2, (int)z.na, (int)z.nb, (int)z.s1,
+                                       (int)z.s2);
+      auto it = ids.find(key);
+      if (it == ids.end()) {
+        it = ids.emplace(key, (int)zrep.size()).first;
+        zrep.push_back((int)zi);
+      }
+      zu[zi] = it->second;
+    }
+    t->nzu = (int)zrep.size();
+  }
 
   // layer-blocked Y: rows of layer j are the triples using layer j (any of l, l1, l2).  A
   // triple's distinct layers in ascending order have ranks 0, 1, 2; within a layer the rows are
@@ -284,7 +305,7 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
           int zi = bl[b].first + e;  // half outputs are stored in row-major order of the layer
           se.snum[s.nterm] = (uint8_t)t->zterms[zi].snum;
           se.sden[s.nterm] = (uint8_t)t->zterms[zi].sden;
-          se.term[s.nterm] = (uint16_t)zi;
+          se.term[s.nterm] = (uint16_t)zu[zi];
           s.term[s.nterm++] = (uint16_t)zi;
         }
         s.ufull = (uint16_t)uidx(j, p, q);
@@ -296,7 +317,7 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
         se.wgt = s.wgt;
         t->yslots.push_back(s);
         t->slots.push_back(se);
-        if (s.is_a) bk[k].push_back(BkItem{s.term[0], s.ufull, s.wgt, {0, 0, 0}});
+        if (s.is_a) bk[k].push_back(BkItem{se.term[0], s.ufull, s.wgt, {0, 0, 0}});
       }
     }
   }
@@ -307,15 +328,15 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
   }
   t->bk_off[t->K] = (int)t->bk_items.size();
 
-  // phase-2 schedule: every Z term is one work entry.  Entries of equal loop shape (na, nb)
+  // phase-2 schedule: every distinct Z computation is one work entry.  Entries of equal loop shape (na, nb)
   // form rounds of 32, one per lane, padded with entries that write nothing, so that the lanes
   // of a warp run identical loops; rounds go to the kZWarps warps longest-first (LPT) by their
   // na * nb cost.  A term stores its Z value at its own index of the term buffer; the slots and
   // B are summed from there in a fixed order.
   {
     std::map<std::pair<int, int>, std::vector<ZItem>> byshape;
-    for (size_t zi = 0; zi < t->zterms.size(); ++zi) {
-      const ZTerm& z = t->zterms[zi];
+    for (size_t u = 0; u < zrep.size(); ++u) {
+      const ZTerm& z = t->zterms[zrep[u]];
       ZItem it{};
       it.i1 = z.i1;
       it.i2 = z.i2;
@@ -325,7 +346,7 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
       it.nb = z.nb;
       it.s1 = z.s1;
       it.s2 = z.s2;
-      it.term = (uint16_t)zi;
+      it.term = (uint16_t)u;
       byshape[{z.na, z.nb}].push_back(it);
     }
     struct Round { long long cost; std::vector<ZItem> lanes; };

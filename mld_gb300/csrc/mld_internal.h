@@ -100,6 +100,7 @@ struct Bso4Tables {
   std::vector<int> l1, l2, l;   // triples (reference order)
   std::vector<double> cg;       // 1-D CG coefficient lists
   std::vector<ZTerm> zterms;    // ZA/ZB/ZC outputs on half layers
+  int nzu = 0;                  // distinct Z computations among them (the term buffer's entries)
   std::vector<YSlot> yslots;    // folded slots
   std::vector<SlotEntry> slots; // the same slots in the kernel's form
   std::vector<int> bk_off;      // K + 1 offsets into bk_items
@@ -172,7 +173,7 @@ cudaError_t fill_dev_tables(const Bso4Tables& t, DevTables* d, Put put) {
   d->NS = (int)t.slots.size();
   d->NYP = t.NYP;
   d->NTILE = (int)t.tiles.size();
-  d->NZT = (int)t.zterms.size();
+  d->NZT = t.nzu;
   d->NROWS = (int)t.rowk.size();
   d->NCG = (int)t.cg.size();
   for (int j = 0; j <= t.J + 1; ++j) {
