@@ -9,9 +9,10 @@
 // Outputs: B per atom and w_ch * dB per pair (the design rows are gathered from them by
 // rows.cu), or, for evaluation with fitted weights, per-pair force and stress contributions.
 // Only half of every layer is computed (X(-p,-q) = (-1)^((p-q)/2) conj X(p,q) for U, c, Z, V);
-// full-layer sums fold into weighted sums over the half.  The recursions run on groups of 8
-// (phase 1) and 16 (phase 3) lanes per neighbour; phase 2 follows a host-balanced schedule of rounds of 32 equal-shape
-// terms per warp.
+// full-layer sums fold into weighted sums over the half.  The recursions run on groups of 8 or
+// 16 lanes per neighbour in phase 1 (8 where the groups' partial sums fit in shared memory without
+// costing a CTA per SM) and 16 in phase 3; phase 2 follows a host-balanced schedule of rounds of
+// 32 equal-shape terms per warp, each distinct Z computation evaluated once.
 //
 // Every floating-point sum has a fixed order: lane groups accumulate privately and are reduced
 // in group order, Z terms land in a term buffer from which the Y slots and B are summed, and the

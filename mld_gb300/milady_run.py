@@ -13,8 +13,10 @@ reference's Python wrapper (README of the MILADY project): it reads the ``&input
   class and file name; mld.F90:944-1020).
 
 The kernel model reads its reference points from ``kernel_matrix.dat`` in ``workdir`` when the
-file exists (compute_kernel.F90:1106-1160); otherwise it selects ``np_kernel_ref +
-np_kernel_full`` training atoms by leverage score (mld_gb300.kernel_select) and writes the file.
+file exists (compute_kernel.F90:1106-1160); otherwise it runs the reference's randomised CUR
+selection (mld_gb300.kernel_select; kernel_dump = 3) over the selected configurations and writes
+the file.  The Mahalanobis-distance selections (kernel_dump 1, 2, 4) need the MCD statistics,
+which this build does not implement, so every kernel_dump value takes the CUR selection.
 """
 from __future__ import annotations
 
@@ -107,17 +109,41 @@ def _stem(c: db_model.Config) -> str:
     return os.path.splitext(os.path.basename(c.filename))[0]
 
 
-def _kernel_points(h: _lib.Handle, nl: dict, train: List[db_model.Config], nat: np.ndarray, workdir: str,
-                   files: Dict[str, str]) -> np.ndarray:
+def _atom_order(classes: List[str], cfg_class: List[str], nat: np.ndarray) -> np.ndarray:
+    """Atoms of the configurations of the given classes, class by class, then in configuration
+    order (the column order of compute_sca_phia, module_Sigma_matrix.F90:458-480)."""
+    starts = np.concatenate([[0], np.cumsum(nat)])
+    out = [np.arange(starts[i], starts[i + 1]) for cl in classes for i, c in enumerate(cfg_class) if c == cl]
+    return np.concatenate(out) if out else np.zeros(0, np.int64)
+
+
+def _kernel_points(cfg: _lib.MldGpuConfig, nl: dict, lines: List[db_model.DbLine], cfgs: List[db_model.Config],
+                   DB: str, els: List[str], workdir: str, files: Dict[str, str]) -> np.ndarray:
+    """Reference points from ``kernel_matrix.dat`` when it exists, else the two CUR picks of the
+    reference's descriptor analysis (kernel_dump = 3): ``np_kernel_ref`` atoms from the classes of
+    ``classes_for_mcd``, ``np_kernel_full`` from every class, over all selected configurations
+    (main_descriptors_analysis.F90:316-372); the file is written and read back."""
     path = os.path.join(workdir, "kernel_matrix.dat")
     if os.path.exists(path):
         return potfile.read_kernel_matrix(path)
-    B, _ = h.descriptors()
-    nk = min(int(nl.get("np_kernel_ref", 200)) + int(nl.get("np_kernel_full", 800)), B.shape[0])
-    idx = kernel_select.select(B, nk, seed=int(nl["seed"]))
+    with _lib.Handle(cfg) as h:
+        _, nat, pos, cell, types, *_ = _load(cfgs, DB, els, int(nl["iread_energy"]), False)
+        h.set_structures(nat, pos, cell, types)
+        B, _ = h.descriptors()
+    cfg_class = [lines[c.line].cls for c in cfgs]
+    full_classes = list(dict.fromkeys(d.cls for d in lines))  # get_distinct_classes, build_subdata.F90:1636-1675
+    inner = _atom_order(str(nl["classes_for_mcd"]).split(), cfg_class, nat)
+    full = _atom_order(full_classes, cfg_class, nat)
+    if inner.size == 0:
+        raise ValueError("no configuration of the classes_for_mcd classes is selected")
+    first, second = kernel_select.cur_kernel_points(
+        B[inner], B[full], int(nl["np_kernel_ref"]), int(nl["np_kernel_full"]), seed=int(nl["seed"]),
+        k=int(nl["cur_kval"]), r=int(nl["cur_rval"]), eps=float(nl["cur_eps"]), svd_rcond=float(nl["svd_rcond"]))
+    idx = np.concatenate([inner[first.selected], full[second.selected]])
     starts = np.concatenate([[0], np.cumsum(nat)])
     conf = np.searchsorted(starts, idx, side="right") - 1
-    potfile.write_kernel_matrix(path, B[idx], conf + 1, idx - starts[conf] + 1, [_stem(train[i]) for i in conf])
+    potfile.write_kernel_matrix(path, B[idx], conf + 1, idx - starts[conf] + 1,
+                                [f"{lines[cfgs[i].line].cls}_{lines[cfgs[i].line].klm}_{_stem(cfgs[i])}" for i in conf])
     files["kernel_matrix"] = path
     return potfile.read_kernel_matrix(path)  # the fit uses the points as written (10 digits), as the reference does
 
@@ -163,7 +189,7 @@ def milady_run(input: str, db_model_file: str = "db_model.in", DB: str = "DB/", 
         h.set_structures(nat, pos, cell, types)
         Z = None
         if ml_type == 1:
-            Z = _kernel_points(h, nl, train, nat, workdir, files)
+            Z = _kernel_points(cfg, nl, lines, cfgs, DB, els, workdir, files)
             h.set_kernel_points(Z)
         h.set_labels(E, F, S, has, w)
         coef, rmse = h.fit()

@@ -27,6 +27,12 @@ DEFAULTS: Dict[str, Any] = {
     "sigma_kernel": 0.0,
     "np_kernel_ref": 200,
     "np_kernel_full": 800,
+    "kernel_dump": 1,
+    "classes_for_mcd": " 01 02",
+    "cur_kval": -1,
+    "cur_rval": -1,
+    "cur_cval": -1,
+    "cur_eps": 1.0,
     "seed": 14792435,
     "selection_type": 3,
     "iread_energy": 2,

@@ -226,3 +226,56 @@ def fit_kernel(A: np.ndarray, y: np.ndarray, wts: np.ndarray, lam: float, rcond:
     lam = 0.0 if lam < 0 else lam
     phi, rhs = normal_equations(A, y, wts, lam * lam)
     return solve_gelsd(phi, rhs, rcond)
+
+
+def _pinv_cut(M: np.ndarray, rcond: float) -> np.ndarray:
+    """Pseudo-inverse keeping singular values s >= max(s) * rcond
+    (scalapack_pseudo_inverse, mld_scalapack.F90:1975-2300)."""
+    U, s, Vt = np.linalg.svd(M, full_matrices=False)
+    keep = s >= s.max() * rcond
+    return (Vt[keep].T / s[keep]) @ U[:, keep].T
+
+
+def cur_decomposition(B: np.ndarray, c: int, ucol: np.ndarray, urow: np.ndarray, k: int = -1, r: int = -1,
+                      eps: float = 1.0, svd_rcond: float = -1.0):
+    """Randomised CUR selection of kernel reference atoms, with explicit matrices (small cases):
+    compute_cur_decomposition, module_Sigma_matrix.F90:865-1052.  ``ucol`` (trials x atoms) and
+    ``urow`` (trials x components) are the uniform draws of the trials, in the reference's order.
+
+    * A = (B - mean)^T, components x atoms (compute_sca_phia :431-490; mean over the same atoms,
+      get_dimension_design_Phi_by_class :162-202);
+    * leverage (compute_leverage_column_score :322-428): rank = #{s >= svd_rcond} (100 eps when
+      negative), k = rank unless cur_kval is set and smaller, p_j = |VT(1:k, j)|^2 / k of A and
+      q_i of A^T; r = int(k ln k / eps^2) when negative;
+    * trial t selects atom j when min(1, c p_j) >= u (perform_cur_selection :515-560), and
+      component i when min(1, r q_i) >= u;
+    * score |A - C U R|_F, C = A(:, 1:n_col) / (c sqrt(p)), R = A(1:n_row, :) / (r sqrt(q)),
+      U = C^+ A R^+ (compute_full_CUR_matrix :622-862);
+    * the winner is minloc of the scores.
+    Returns (selected atoms of every trial, pcol, prow, k, r, scores, winner)."""
+    B = np.asarray(B, dtype=np.float64)
+    A = (B - B.mean(axis=0)).T
+    tol = 100.0 * np.finfo(np.float64).eps if svd_rcond < 0 else svd_rcond
+    _, s, VT = np.linalg.svd(A, full_matrices=False)
+    rank = int(np.sum(np.abs(s) >= tol))
+    if k < 0 or k > rank:
+        k = rank
+    if r < 0:
+        r = int(k * np.log(k) / eps ** 2)
+    nK, nA = A.shape
+    pcol = np.array([np.sum(VT[:k, j] ** 2) / k for j in range(nA)])
+    _, s2, VT2 = np.linalg.svd(A.T, full_matrices=False)
+    prow = np.array([np.sum(VT2[:k, i] ** 2) / k for i in range(nK)])
+    trials = ucol.shape[0]
+    sel, scores = [], []
+    for t in range(trials):
+        selcol = np.array([min(1.0, pcol[j] * c) >= ucol[t, j] for j in range(nA)])
+        selrow = np.array([min(1.0, prow[i] * r) >= urow[t, i] for i in range(nK)])
+        nc, nr = int(selcol.sum()), int(selrow.sum())
+        C = A[:, :nc] / (c * np.sqrt(pcol[:nc]))[None, :]
+        R = A[:nr, :] / (r * np.sqrt(prow[:nr]))[:, None]
+        U = _pinv_cut(C, tol) @ A @ _pinv_cut(R, tol)
+        scores.append(np.linalg.norm(A - C @ U @ R))
+        sel.append(np.flatnonzero(selcol))
+    win = int(np.argmin(scores))
+    return sel, pcol, prow, k, r, np.array(scores), win

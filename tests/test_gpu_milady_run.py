@@ -78,10 +78,13 @@ def test_kernel_fit_selects_and_reuses_points(lib, database):
     r1 = _run(tmp_path, 1)
     assert "kernel_matrix" in r1.files
     Z = potfile.read_kernel_matrix(r1.files["kernel_matrix"])
-    assert Z.shape == (24, 55)
+    # the CUR selection keeps atom j with probability min(1, 24 p_j): about 24 of the 128 atoms of
+    # class 01, none from np_kernel_full = 0
+    nk = Z.shape[0]
+    assert 10 <= nk <= 40 and Z.shape[1] == 55
     L = potfile.read_lammps_pot(r1.files["lammps_pot"])
-    assert L["mld_order"] == potfile.MLD_KERNEL and L["kernel_points"].shape == (24, 55)
-    assert L["w"].shape == (1 + 55 + 24,)
+    assert L["mld_order"] == potfile.MLD_KERNEL and L["kernel_points"].shape == (nk, 55)
+    assert L["w"].shape == (1 + 55 + nk,)
     # a second run reads kernel_matrix.dat instead of selecting again: the same model, bitwise
     # (every sum of the FP64 path has a fixed order)
     r2 = _run(tmp_path, 1)

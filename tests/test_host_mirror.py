@@ -93,3 +93,49 @@ def test_kernel_reference_selection_is_seeded_and_prefers_leverage():
     lev, k = kernel_select.leverage_scores(B)
     assert k == 6 and abs(lev.sum() - 1.0) < 1e-9
     assert len(set(range(10)) & set(a.tolist())) >= 9
+
+
+def _cur_cases():
+    rng = np.random.default_rng(1)
+    L = rng.normal(size=(12, 12)) * np.logspace(0, -3, 12)[None, :]
+    synth_B = rng.normal(size=(300, 12)) @ L.T + 3.0
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "fit17_bso4.npz"))
+    fit17_B = np.concatenate([z[k] for k in sorted(z.files) if k.startswith("B_")])
+    return [(synth_B, 6, 4), (synth_B, 10, -1), (synth_B, 40, 3), (synth_B, 200, -1), (fit17_B, 20, -1),
+            (fit17_B, 60, -1)]
+
+
+@pytest.mark.parametrize("case", range(6))
+def test_cur_selection_matches_oracle(case):
+    """The CUR selection of kernel reference atoms (QR-coordinate products) against the oracle's
+    explicit restatement with full matrices and pseudo-inverses, on the same uniform draws:
+    leverage scores, k and r, every trial's score, the winner and its atoms.  The fit17 cases use
+    MILADY's golden descriptors of 20 W structures (1301 atoms, K = 55)."""
+    import oracle
+    from mld_gb300 import kernel_select
+    B, c, r = _cur_cases()[case]
+    seed = 5 + case
+    res = kernel_select.cur_select(B, c, seed=seed, r=r)
+    g = np.random.default_rng(seed)
+    ucol = g.random((kernel_select.CUR_TRIALS, B.shape[0]))
+    urow = g.random((kernel_select.CUR_TRIALS, B.shape[1]))
+    sels, pcol, prow, k, rr, scores, _ = oracle.cur_decomposition(B, c, ucol, urow, r=r)
+    assert (res.k, res.r) == (k, rr)
+    assert np.abs(res.pcol - pcol).max() <= 1e-10 * pcol.max()
+    assert np.abs(res.prow - prow).max() <= 1e-12
+    assert np.array_equal(res.n_col, [len(s) for s in sels])
+    A = B - B.mean(axis=0)
+    norm_a = np.sqrt((A * A).sum())
+    assert np.abs(res.scores - scores).max() <= 1e-10 * norm_a
+    # the oracle's scores with the same tie rule (rounding-level scores are equal)
+    win = int(np.flatnonzero(scores <= scores.min() + kernel_select.TIE_REL * norm_a)[0])
+    assert res.winner == win and np.array_equal(res.selected, sels[win])
+
+
+def test_cur_kernel_points_carry_k_and_r():
+    from mld_gb300 import kernel_select
+    B = _cur_cases()[4][0]
+    first, second = kernel_select.cur_kernel_points(B[:600], B, 50, 80, seed=3)
+    assert (first.k, first.r) == (second.k, second.r) == (55, int(55 * np.log(55)))
+    assert abs(len(first.selected) - 50) < 25 and abs(len(second.selected) - 80) < 30
+    assert first.selected.max() < 600
