@@ -119,7 +119,7 @@ struct mld_gpu_handle {
     B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
     B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV, B_KZD, B_KZF, B_KWS, B_WSERVE, B_P32,
     B_EW, B_EBETA, B_EB, B_EOUT, B_KTC, B_SKW, B_ORDER, B_QCNT, B_SP, B_EPAIR, B_EATOM, B_GP,
-    B_CNC, B_CELLOFF, B_CELLOF, B_CELLSTART, B_CELLATOMS, B_SORTTMP,
+    B_CNC, B_CELLOFF, B_CELLOF, B_CELLSTART, B_CELLATOMS, B_SORTTMP, B_NBR_U32,
     B_COUNT
   };
   static_assert(B_COUNT <= 80, "buffer table too small");
@@ -281,6 +281,11 @@ int build_neighbours(mld_gpu_handle* h) {
   CK(ensure(h, mld_gpu_handle::B_NBR_U, sizeof(double) * 3 * std::max<long long>(b.P, 1)));
   b.nbr_idx = bp_<int>(h, mld_gpu_handle::B_NBR_IDX);
   b.nbr_u = bp_<double>(h, mld_gpu_handle::B_NBR_U);
+  b.nbr_u32 = nullptr;
+  if (h->mixed) {
+    CK(ensure(h, mld_gpu_handle::B_NBR_U32, sizeof(float4) * std::max<long long>(b.P, 1)));
+    b.nbr_u32 = bp_<float4>(h, mld_gpu_handle::B_NBR_U32);
+  }
   if (b.ncells > 0 && b.P > 0) {
     // workspace of the sort of the celled structures' lists (inside the filling pass)
     CK(ensure(h, mld_gpu_handle::B_SORTTMP, sizeof(int) * (size_t)b.P));

@@ -101,10 +101,8 @@ struct NbrGeom {
 // angular_functions.f90:66-107 (the geometric set-up of spherical_4d) and the cutoff of
 // compute_bispectrum_so4.F90:337-377 (type-2 cosine outer cut times (1 - inner type-3 cut)).
 template <typename T>
-__device__ __forceinline__ void nbr_geometry(const double* u3, T rcut, T inv_r0, double rin, double rin_w,
-                                             NbrGeom<T>* g) {
+__device__ __forceinline__ void nbr_geometry(T x0, T x1, T x2, T rcut, T inv_r0, T rin, T rin_w, NbrGeom<T>* g) {
   const T PI = (T)3.14159265358979323846;
-  T x0 = (T)u3[0], x1 = (T)u3[1], x2 = (T)u3[2];
   T rr = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
   T r0 = rcut / inv_r0;
   T th0 = rr / r0;
@@ -146,8 +144,8 @@ __device__ __forceinline__ void nbr_geometry(const double* u3, T rcut, T inv_r0,
     dfo = -T(0.5) * PI * sp / rcut;
   }
   T fi = 0, dfi = 0;
-  if (rin > 0.0) {
-    T rc2 = (T)(rin + rin_w), w = (T)rin_w;
+  if (rin > T(0)) {
+    T rc2 = rin + rin_w, w = rin_w;
     if (rr <= rc2) {
       if (rr < rc2 - w) {
         fi = 1;
@@ -183,7 +181,9 @@ __device__ __forceinline__ void group_recursion(const NbrGeom<T>& g, const typen
 #pragma unroll
       for (int a = 0; a < 3; ++a) V[a * HU] = {T(0), T(0)};
     } else {
-      for (int ch = 0; ch < nch; ++ch) cpart[ch * HU].x += g.fc * wch[ch];
+#pragma unroll
+      for (int ch = 0; ch < kMaxCh; ++ch)
+        if (ch < nch) cpart[ch * HU].x += g.fc * wch[ch];
     }
   }
   __syncwarp();
@@ -227,7 +227,9 @@ __device__ __forceinline__ void group_recursion(const NbrGeom<T>& g, const typen
         } else {
           if (sz >= 0) u = cmul(A, fetch(prev, sz));
           if (sx >= 0) u = cfma(Bc, fetch(prev, sx), u);
-          for (int ch = 0; ch < nch; ++ch) {
+#pragma unroll
+          for (int ch = 0; ch < kMaxCh; ++ch) {
+            if (ch >= nch) break;
             const T f = g.fc * wch[ch];
             cx<T> v = cpart[ch * HU + idx];
             cpart[ch * HU + idx] = {fma(f, u.x, v.x), fma(f, u.y, v.y)};
@@ -283,6 +285,11 @@ struct KernelArgs {
   const int* nbr_off;
   const int* nbr_idx;
   const double* nbr_u;
+  const float4* u32;  // (u, 1/r) in FP32 for T = float (null: converted from nbr_u)
+  // channel weights and inner cutoffs per type pair in T, converted once at launch
+  T chw[kMaxCh * kMaxTypes];
+  T rin[kMaxTypes * kMaxTypes];
+  T rin_w;
   // work queue: atoms in the order given (nullptr: 0..A-1), taken through a global counter
   const int* order;
   int* counter;
@@ -361,6 +368,24 @@ __device__ __forceinline__ ZItem load_zitem(const ZItem* p) {
   return z;
 }
 
+// Displacement of pair q in T: the FP32 copy for T = float when present, else nbr_u.
+template <typename T>
+__device__ __forceinline__ void pair_u(const KernelArgs<T>& args, size_t q, T* x) {
+  if constexpr (sizeof(T) == 4) {
+    if (args.u32) {
+      const float4 v = args.u32[q];
+      x[0] = v.x;
+      x[1] = v.y;
+      x[2] = v.z;
+      return;
+    }
+  }
+  const double* u3 = args.nbr_u + 3 * q;
+  x[0] = (T)u3[0];
+  x[1] = (T)u3[1];
+  x[2] = (T)u3[2];
+}
+
 // Phase 1 of one atom: lane groups of G1 lanes take the neighbours in turn and add
 // f_c w_ch U of each to their private partial in V (group g at V + g*nch*HU, recursion buffers
 // behind the partials of all groups).
@@ -382,9 +407,13 @@ __device__ __forceinline__ void phase1_c(const KernelArgs<T>& args, const typena
     if (active) {
       const int nb = args.nbr_idx[p0 + n];
       const int tn = args.types[nb];
-      const double rin = args.p.has_rin ? args.p.rin[ti * args.p.ntypes + tn] : 0.0;
-      nbr_geometry<T>(args.nbr_u + 3 * (size_t)(p0 + n), rcut, inv_r0, rin, args.p.rin_width, &g);
-      for (int ch = 0; ch < nch; ++ch) wch[ch] = (T)args.p.chw[ch * args.p.ntypes + tn];
+      const T rin = args.p.has_rin ? args.rin[ti * args.p.ntypes + tn] : T(0);
+      T x[3];
+      pair_u<T>(args, (size_t)(p0 + n), x);
+      nbr_geometry<T>(x[0], x[1], x[2], rcut, inv_r0, rin, args.rin_w, &g);
+#pragma unroll
+      for (int ch = 0; ch < kMaxCh; ++ch)
+        if (ch < nch) wch[ch] = args.chw[ch * args.p.ntypes + tn];
     }
     group_recursion<T, G1, false>(g, srec, J, shoff, ub, LH, nullptr, cpart, wch, nch, HU, sl1, active);
   }
@@ -556,22 +585,34 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
         const int n = grp;  // one neighbour per group
         const bool active = n < nb_here;
         NbrGeom<T> g;
-        const double* u3 = args.nbr_u + 3 * (size_t)(p0 + base + min(n, nb_here - 1));
         if (active) {
-          const int nbi = args.nbr_idx[p0 + base + n];
+          const size_t q = (size_t)(p0 + base + n);
+          const int nbi = args.nbr_idx[q];
           const int tn = args.types[nbi];
-          const double rin = args.p.has_rin ? args.p.rin[ti * args.p.ntypes + tn] : 0.0;
-          nbr_geometry<T>(u3, rcut, inv_r0, rin, args.p.rin_width, &g);
+          const T rin = args.p.has_rin ? args.rin[ti * args.p.ntypes + tn] : T(0);
+          T x[3];
+          pair_u<T>(args, q, x);
+          nbr_geometry<T>(x[0], x[1], x[2], rcut, inv_r0, rin, args.rin_w, &g);
           if (sl == 0) {
-            for (int ch = 0; ch < nch; ++ch) nwt[ch * kNB + n] = (T)args.p.chw[ch * args.p.ntypes + tn];
+            for (int ch = 0; ch < nch; ++ch) nwt[ch * kNB + n] = args.chw[ch * args.p.ntypes + tn];
             nidx[n] = nbi;
-            const double r = sqrt(u3[0] * u3[0] + u3[1] * u3[1] + u3[2] * u3[2]);
             // stress lever arm: x_n - x_i (small box) or sign_big*(x_i - x_n) (large box)
-            const double sgn = args.small[s] ? 1.0 : -args.p.sign_big;
-            nuu[n * 4 + 0] = (T)(sgn * u3[0]);
-            nuu[n * 4 + 1] = (T)(sgn * u3[1]);
-            nuu[n * 4 + 2] = (T)(sgn * u3[2]);
-            nuu[n * 4 + 3] = (T)(1.0 / r);
+            if (sizeof(T) == 4 && args.u32) {
+              const float4 v = args.u32[q];
+              const T sgn = args.small[s] ? T(1) : (T)(-args.p.sign_big);
+              nuu[n * 4 + 0] = sgn * v.x;
+              nuu[n * 4 + 1] = sgn * v.y;
+              nuu[n * 4 + 2] = sgn * v.z;
+              nuu[n * 4 + 3] = v.w;
+            } else {
+              const double* u3 = args.nbr_u + 3 * q;
+              const double r = sqrt(u3[0] * u3[0] + u3[1] * u3[1] + u3[2] * u3[2]);
+              const double sgn = args.small[s] ? 1.0 : -args.p.sign_big;
+              nuu[n * 4 + 0] = (T)(sgn * u3[0]);
+              nuu[n * 4 + 1] = (T)(sgn * u3[1]);
+              nuu[n * 4 + 2] = (T)(sgn * u3[2]);
+              nuu[n * 4 + 3] = (T)(1.0 / r);
+            }
           }
         }
         if (eval && sl < 9) pacc[min(n, kNB - 1) * 9 + sl] = 0.0;
@@ -734,6 +775,10 @@ cudaError_t launch_bso4(const DevTables& tb, const DevBatch& b, const BsoParams&
   a.nbr_off = b.nbr_off;
   a.nbr_idx = b.nbr_idx;
   a.nbr_u = b.nbr_u;
+  a.u32 = sizeof(T) == 4 ? b.nbr_u32 : nullptr;
+  for (int e = 0; e < kMaxCh * kMaxTypes; ++e) a.chw[e] = (T)p.chw[e];
+  for (int e = 0; e < kMaxTypes * kMaxTypes; ++e) a.rin[e] = (T)p.rin[e];
+  a.rin_w = (T)p.rin_width;
   a.order = sh.sorted_queue ? order : nullptr;
   a.counter = counter;
   a.p = p;

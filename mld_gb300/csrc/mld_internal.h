@@ -228,6 +228,8 @@ struct DevBatch {
   int* nbr_off = nullptr;    // A+1
   int* nbr_idx = nullptr;    // P
   double* nbr_u = nullptr;   // 3P  (x_neighbour - x_centre, FP64)
+  float4* nbr_u32 = nullptr; // P (x, y, z, 1/r) rounded from the FP64 values, for the FP32
+                             // descriptor kernel (null: it converts nbr_u itself)
   long long P = 0;
   int maxnn = 0;             // largest neighbour count (after the counting pass)
   // linked cells of large boxes (null cnc: every structure scans all its atoms)

@@ -238,10 +238,12 @@ __global__ void __launch_bounds__(256) k_neighbours(
 }
 
 // FP64 displacement u = x_j + image - x_i of every pair (the reference's arithmetic), from the
-// centre and image recorded by the filling pass; one thread per pair.
+// centre and image recorded by the filling pass; one thread per pair.  u32 (optional) receives
+// (u, 1/|u|) rounded to FP32 for the FP32 descriptor kernel, so that it runs no FP64 arithmetic.
 __global__ void k_nbr_u(long long P, const int* __restrict__ atom_struct, const double* __restrict__ pos,
                         const double* __restrict__ cell, const double* __restrict__ recip,
-                        const int* __restrict__ small, const int* __restrict__ nbr_idx, double* __restrict__ nbr_u) {
+                        const int* __restrict__ small, const int* __restrict__ nbr_idx, double* __restrict__ nbr_u,
+                        float4* __restrict__ u32) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
   const int i = (int)nbr_u[3 * p], img = (int)nbr_u[3 * p + 1], j = nbr_idx[p];
@@ -261,6 +263,9 @@ __global__ void k_nbr_u(long long P, const int* __restrict__ atom_struct, const 
   nbr_u[3 * p] = u[0];
   nbr_u[3 * p + 1] = u[1];
   nbr_u[3 * p + 2] = u[2];
+  if (u32)
+    u32[p] = make_float4((float)u[0], (float)u[1], (float)u[2],
+                         (float)(1.0 / sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2])));
 }
 
 // Three-phase exclusive scan of n ints: out[0..n], out[n] = total.
@@ -423,7 +428,7 @@ cudaError_t launch_neighbours(const DevBatch& b, double rcut, int* counts, int* 
   }
   if (pass == 1 && b.P > 0)
     k_nbr_u<<<(unsigned)((b.P + 255) / 256), 256, 0, st>>>(b.P, b.atom_struct, b.pos, b.cell, b.recip, b.small,
-                                                           b.nbr_idx, b.nbr_u);
+                                                           b.nbr_idx, b.nbr_u, b.nbr_u32);
   return cudaGetLastError();
 }
 
