@@ -51,25 +51,32 @@ __global__ void __launch_bounds__(kRowThreads) k_lin_force_rows(
     fac[3 * n + 2] = (T)(f * u[2]);
   }
   __syncthreads();
-  const int nf = rf >= 0 ? 3 * KK : 0, ns = (rs >= 0 && Sp) ? 6 * KK : 0;
-  for (int c = tid; c < nf + ns; c += kRowThreads) {
-    if (c < nf) {
-      const int a = c / KK, k = c - a * KK;
-      T sum = T(0);
-      for (int n = 0; n < nn; ++n) {
-        const T own = dB[((size_t)(p0 + n) * 3 + a) * KK + k];
-        const int q = qrev[n];
-        const T back = q >= 0 ? dB[((size_t)q * 3 + a) * KK + k] : T(0);
-        sum += own - back;
+  // thread (a, k): the force row entry and the stress partials (aa = a, bb >= a) of column k,
+  // each summed over the neighbours in order from one read of the atom's own derivatives
+  const bool want_f = rf >= 0, want_s = rs >= 0 && Sp;
+  if (!want_f && !want_s) return;
+  for (int c = tid; c < 3 * KK; c += kRowThreads) {
+    const int a = c / KK, k = c - a * KK;
+    T sum = T(0), acc[3] = {T(0), T(0), T(0)};
+#pragma unroll 4
+    for (int n = 0; n < nn; ++n) {
+      const T own = dB[((size_t)(p0 + n) * 3 + a) * KK + k];
+      const int q = qrev[n];
+      const T back = q >= 0 ? dB[((size_t)q * 3 + a) * KK + k] : T(0);
+      sum += own - back;
+#pragma unroll
+      for (int bb = 0; bb < 3; ++bb)
+        if (bb >= a) acc[bb] = fma(own, fac[3 * n + bb], acc[bb]);
+    }
+    if (want_f) X[(rf + 3LL * (i - atom_start[s]) + a) * ldx + 1 + k] = sum;
+    if (want_s) {
+      // (aa, bb) -> stress index: (0,0) xx 0, (1,1) yy 1, (2,2) zz 2, (1,2) yz 3, (0,2) xz 4, (0,1) xy 5
+#pragma unroll
+      for (int bb = 0; bb < 3; ++bb) {
+        if (bb < a) continue;
+        const int sidx = bb == a ? a : (a == 1 ? 3 : (bb == 2 ? 4 : 5));
+        Sp[((size_t)i * 6 + sidx) * KK + k] = acc[bb];
       }
-      X[(rf + 3LL * (i - atom_start[s]) + a) * ldx + 1 + k] = sum;
-    } else {
-      const int e = c - nf, sidx = e / KK, k = e - sidx * KK;
-      const int aa = sidx < 3 ? sidx : (sidx == 3 ? 1 : 0);
-      const int bb = sidx < 3 ? sidx : (sidx == 5 ? 1 : 2);
-      T acc = T(0);
-      for (int n = 0; n < nn; ++n) acc = fma(dB[((size_t)(p0 + n) * 3 + aa) * KK + k], fac[3 * n + bb], acc);
-      Sp[((size_t)i * 6 + sidx) * KK + k] = acc;
     }
   }
 }
