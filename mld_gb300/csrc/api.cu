@@ -119,7 +119,7 @@ struct mld_gpu_handle {
     B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
     B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV, B_KZD, B_KZF, B_KWS, B_WSERVE, B_P32,
     B_EW, B_EBETA, B_EB, B_EOUT, B_KTC, B_SKW, B_ORDER, B_QCNT, B_SP, B_EPAIR, B_EATOM, B_GP,
-    B_CNC, B_CELLOFF, B_CELLOF, B_CELLSTART, B_CELLATOMS, B_SORTTMP, B_NBR_U32,
+    B_CNC, B_CELLOFF, B_CELLOF, B_CELLSTART, B_CELLATOMS, B_SORTTMP, B_NBR_U32, B_MVWS, B_GTCP,
     B_COUNT
   };
   static_assert(B_COUNT <= 80, "buffer table too small");
@@ -807,8 +807,10 @@ int fit_block_mixed(mld_gpu_handle* h, const float* X, int c0, int Db, const dou
   CK(cudaMemsetAsync(G, 0, sizeof(double) * (size_t)Db * Db, h->st));
   CK(cudaMemsetAsync(terr, 0, sizeof(int), h->st));
   if (!gram_tc_available()) return fail(h, MLD_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const size_t npart = gram_tc_part_doubles(Db, h->nsm);
+  CK(ensure(h, mld_gpu_handle::B_GTCP, sizeof(double) * std::max<size_t>(npart, 1)));
   CK(launch_gram_tc<float>(X, h->ldx, c0, Db, wrow, M, G, bp_<void>(h, mld_gpu_handle::B_GWS), wsb, terr, h->nsm,
-                           h->st));
+                           h->st, bp_<double>(h, mld_gpu_handle::B_GTCP), npart));
   const long long chunk = (long long)((wsb - 256) / (4 * (size_t)Db)) / 64 * 64;
   nl(h, 2 * ((M + chunk - 1) / chunk));
   CK(launch_symmetrize(G, Db, h->st));
@@ -876,10 +878,14 @@ int pcg_solve(mld_gpu_handle* h, const float* X, int c0, int Db, const double* y
   double* q = p + Db;
   double* scal = q + 3 * (size_t)Db;  // [0..3] CG scalars, [4] objective at w = 0
   float2* sv = bp_<float2>(h, mld_gpu_handle::B_PRED);  // per-row double-FP32 scratch
+  // per-block partial sums of the matvecs and of the objective, reduced in block order
+  const size_t nmvws = std::max<size_t>(normal_matvec_workspace_doubles(M, Db, h->nsm), kSumsqBlocksMax);
+  CK(ensure(h, mld_gpu_handle::B_MVWS, sizeof(double) * nmvws));
+  double* mvws = bp_<double>(h, mld_gpu_handle::B_MVWS);
   int herr = 0;
   // objective sum_r w_r y_r^2 at w = 0, for the stopping test on its decrease
-  CK(launch_weighted_sumsq(wrow, y, M, scal + 4, h->st));
-  nl(h, 1);
+  CK(launch_weighted_sumsq(wrow, y, M, scal + 4, mvws, h->st));
+  nl(h, 2);
   // x0 = 0, r0 = rhs
   CK(cudaMemsetAsync(w, 0, sizeof(double) * Db, h->st));
   CK(cudaMemcpyAsync(r, hv, sizeof(double) * Db, cudaMemcpyDeviceToDevice, h->st));
@@ -894,7 +900,7 @@ int pcg_solve(mld_gpu_handle* h, const float* X, int c0, int Db, const double* y
   int it = 0, slow = 0;
   for (; it < kPcgMaxIter; ++it) {
     int nmv = 0;
-    CK(launch_normal_matvec(X, h->ldx, c0, Db, wrow, p, M, lam, sv, q, h->nsm, h->st, &nmv, terr));
+    CK(launch_normal_matvec(X, h->ldx, c0, Db, wrow, p, M, lam, sv, q, mvws, h->nsm, h->st, &nmv, terr));
     CK(launch_pcg_alpha(Db, p, q, w, r, scal, h->st));
     CK(precond(r, z));
     CK(launch_pcg_beta(Db, z, r, p, scal, 0, h->st));
@@ -1422,8 +1428,11 @@ int mld_gpu_gram(mld_gpu_handle* h, double* G, double* rhs) {
     CK(cudaMemsetAsync(dG, 0, sizeof(double) * (size_t)D * D, h->st));
     CK(cudaMemsetAsync(terr, 0, sizeof(int), h->st));
     if (!gram_tc_available()) return fail(h, MLD_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    const size_t npart = gram_tc_part_doubles(D, h->nsm);
+    CK(ensure(h, mld_gpu_handle::B_GTCP, sizeof(double) * std::max<size_t>(npart, 1)));
     CK(launch_gram_tc<float>(X, h->ldx, 0, D, bp_<double>(h, mld_gpu_handle::B_WROW), M, dG,
-                             bp_<void>(h, mld_gpu_handle::B_GWS), wsb, terr, h->nsm, h->st));
+                             bp_<void>(h, mld_gpu_handle::B_GWS), wsb, terr, h->nsm, h->st,
+                             bp_<double>(h, mld_gpu_handle::B_GTCP), npart));
     CK(launch_symmetrize(dG, D, h->st));
     CK(ensure(h, mld_gpu_handle::B_PRED, sizeof(double) * (size_t)std::max<long long>(M, 1)));
     double* rws = gram_ws(h, M, D);
@@ -1916,10 +1925,12 @@ extern "C" int mld_gpu_gram_rows(int method, const void* X, int x_is_fp32, long 
   void* ws = nullptr;
   double* hbuf = nullptr;
   int* terr = nullptr;
+  double* part = nullptr;  // tensor-core split partials and right-hand-side partials
   auto cleanup = [&]() {
     if (ws) cudaFree(ws);
     if (hbuf) cudaFree(hbuf);
     if (terr) cudaFree(terr);
+    if (part) cudaFree(part);
   };
   auto cuda_err = [&](cudaError_t ce, const char* where) {
     cleanup();
@@ -1950,20 +1961,27 @@ extern "C" int mld_gpu_gram_rows(int method, const void* X, int x_is_fp32, long 
       return set_err(err, err_len, MLD_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     const size_t need = (size_t)4 * D * (size_t)((std::max<long long>(M, 1) + 63) / 64 * 64) + 256;
     const size_t wsb = std::max(gram_tc_min_workspace(D), std::min(need, kGramWorkspaceCap));
+    const size_t npart = gram_tc_part_doubles(D, nsm);
+    const size_t nrhs = rhs ? gram_workspace_doubles(M, D) : 0;
     e = cudaMalloc(&ws, wsb);
+    if (e == cudaSuccess) e = cudaMalloc(&part, sizeof(double) * std::max<size_t>(std::max(npart, nrhs), 1));
     if (e == cudaSuccess) e = cudaMalloc(&terr, sizeof(int));
     if (e == cudaSuccess) e = cudaMemsetAsync(terr, 0, sizeof(int), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(G, 0, sizeof(double) * (size_t)D * D, st);
     if (e != cudaSuccess) return cuda_err(e, "workspace");
-    e = x_is_fp32 ? launch_gram_tc<float>(static_cast<const float*>(X), ldx, 0, D, w, M, G, ws, wsb, terr, nsm, st)
-                  : launch_gram_tc<double>(static_cast<const double*>(X), ldx, 0, D, w, M, G, ws, wsb, terr, nsm, st);
+    e = x_is_fp32 ? launch_gram_tc<float>(static_cast<const float*>(X), ldx, 0, D, w, M, G, ws, wsb, terr, nsm, st,
+                                          part, npart)
+                  : launch_gram_tc<double>(static_cast<const double*>(X), ldx, 0, D, w, M, G, ws, wsb, terr, nsm, st,
+                                           part, npart);
     if (e == cudaSuccess) e = launch_symmetrize(G, D, st);
     float2* sv = nullptr;
+    // the right-hand side reuses the partial buffer after the Gram (same stream)
     if (e == cudaSuccess && rhs && x_is_fp32) {
       e = cudaMalloc(&sv, sizeof(float2) * (size_t)std::max<long long>(M, 1));
-      if (e == cudaSuccess) e = launch_rhs<float>(static_cast<const float*>(X), ldx, w, y, M, D, rhs, nsm, st, sv);
+      if (e == cudaSuccess)
+        e = launch_rhs<float>(static_cast<const float*>(X), ldx, w, y, M, D, rhs, nsm, st, sv, part);
     } else if (e == cudaSuccess && rhs) {
-      e = launch_rhs<double>(static_cast<const double*>(X), ldx, w, y, M, D, rhs, nsm, st, nullptr);
+      e = launch_rhs<double>(static_cast<const double*>(X), ldx, w, y, M, D, rhs, nsm, st, nullptr, part);
     }
     if (sv) {
       cudaStreamSynchronize(st);

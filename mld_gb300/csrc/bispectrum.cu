@@ -63,6 +63,7 @@ __device__ __forceinline__ cx<T> zterm(const cx<T>* __restrict__ cc, const T* __
   for (int b = 0; b < NB; ++b) c2[b] = cgs[zi.cg2 + b];
   cx<T> zs = {T(0), T(0)};
   int i1a = zi.i1, i2a = zi.i2;
+#pragma unroll (NB <= 2 ? 4 : (NB <= 5 ? 2 : 1))
   for (int a = 0; a < zi.na; ++a) {
     const T c1 = cgs[zi.cg1 + a];
     cx<T> part = {T(0), T(0)};

@@ -138,14 +138,17 @@ __global__ void __launch_bounds__(GT * GT) k_gram_reduce(const double* __restric
   G[(size_t)i * D + j] = sum;
 }
 
-// q[c] = sum over the row blocks of part[b * D + c], in block order.
+// q[c] = sum over the row blocks of part[b * D + c] in a fixed order: one warp per column, lane
+// l adds the blocks l, l + 32, l + 64, ... in turn, then a fixed xor tree over the lanes.
 __global__ void k_colsum_reduce(const double* __restrict__ part, long long nrb, int D, double* __restrict__ q) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= D) return;
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (c >= D) return;  // whole warps leave together
   double sum = 0.0;
-  for (long long b = 0; b < nrb; ++b) sum += part[(size_t)b * D + c];
-  q[c] = sum;
+  for (long long b = lane; b < nrb; b += 32) sum += part[(size_t)b * D + c];
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) q[c] = sum;
 }
+constexpr int kColsumColsPerBlock = 8;  // warps (columns) per block of k_colsum_reduce
 
 __global__ void k_symmetrize(double* G, int D) {
   const int i = blockIdx.x, j = threadIdx.x;
@@ -250,7 +253,7 @@ template <int NK>
 __global__ void __launch_bounds__(256) k_normal_matvec_narrow(const float* __restrict__ X, int ldx, int D,
                                                               const float2* __restrict__ wds,
                                                               const double* __restrict__ p, long long M, long long rpb,
-                                                              double* __restrict__ q) {
+                                                              double* __restrict__ q, double* __restrict__ part) {
   __shared__ double red[8][32 * NK];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float ph[NK], pl[NK], ah[NK], al[NK];
@@ -315,7 +318,10 @@ __global__ void __launch_bounds__(256) k_normal_matvec_narrow(const float* __res
     double sum = 0.0;
 #pragma unroll
     for (int w8 = 0; w8 < 8; ++w8) sum += red[w8][c];
-    if (c < D && sum != 0.0) atomicAdd(&q[c], sum);
+    if (c < D) {
+      if (part) part[(size_t)blockIdx.x * D + c] = sum;  // reduced in block order
+      else if (sum != 0.0) atomicAdd(&q[c], sum);
+    }
   }
 }
 
@@ -432,7 +438,7 @@ template <int CPT>
 __global__ void __launch_bounds__(kWThreads, 1)
     k_normal_matvec_wide(const float* __restrict__ X, long long ldx, int c0, int D, const float2* __restrict__ wds,
                          const double* __restrict__ p, long long M, long long rpb, int rowf, int stride, int stages,
-                         double* __restrict__ q, int* __restrict__ err) {
+                         double* __restrict__ q, double* __restrict__ qpart, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char wsm[];
   float* rows = reinterpret_cast<float*>(wsm);                                 // stages * stride
   float* part = rows + (size_t)stages * stride;                                // stages * kWWarps
@@ -566,8 +572,8 @@ __global__ void __launch_bounds__(kWThreads, 1)
 #pragma unroll
   for (int j = 0; j < CPT; ++j) {
     const int c = tid + kWConsumers * j;
-    const double v = (double)sh[j] + (double)sl[j] + (double)acc[j];
-    if (c < D && v != 0.0) atomicAdd(&q[c], v);
+    // partial column sums of this block, reduced in block order by k_colsum_reduce
+    if (c < D) qpart[(size_t)blockIdx.x * D + c] = (double)sh[j] + (double)sl[j] + (double)acc[j];
   }
 }
 
@@ -599,13 +605,15 @@ cudaError_t launch_rhs(const T* X, int ldx, const double* w, const double* y, lo
     }
   }
   if (!done) k_xtv<T><<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(X, ldx, D, w, y, M, rpb, h, ws);
-  if (ws) k_colsum_reduce<<<(D + 255) / 256, 256, 0, st>>>(ws, nrb, D, h);
+  if (ws)
+    k_colsum_reduce<<<(D + kColsumColsPerBlock - 1) / kColsumColsPerBlock, 32 * kColsumColsPerBlock, 0, st>>>(
+        ws, nrb, D, h);
   return cudaGetLastError();
 }
 
-// out = sum_r w[r] y[r]^2 (out is zeroed here)
+// out = sum_r w[r] y[r]^2: block b writes its partial to part[b]; k_sum_reduce adds them in order
 __global__ void __launch_bounds__(256) k_weighted_sumsq(const double* __restrict__ w, const double* __restrict__ y,
-                                                        long long M, double* __restrict__ out) {
+                                                        long long M, double* __restrict__ part) {
   __shared__ double red[8];
   double a = 0.0;
   for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < M; r += (long long)gridDim.x * blockDim.x)
@@ -616,15 +624,25 @@ __global__ void __launch_bounds__(256) k_weighted_sumsq(const double* __restrict
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int k = 0; k < 8; ++k) t += red[k];
-    atomicAdd(out, t);
+    part[blockIdx.x] = t;
   }
 }
 
-cudaError_t launch_weighted_sumsq(const double* w, const double* y, long long M, double* out, cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), st);
-  if (e != cudaSuccess || M == 0) return e;
-  const unsigned blocks = (unsigned)std::min<long long>((M + 255) / 256, 1024);
-  k_weighted_sumsq<<<blocks, 256, 0, st>>>(w, y, M, out);
+constexpr int kSumsqBlocks = kSumsqBlocksMax;
+
+__global__ void k_sum_reduce(const double* __restrict__ part, int n, double* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double t = 0.0;
+  for (int b = 0; b < n; ++b) t += part[b];
+  *out = t;
+}
+
+cudaError_t launch_weighted_sumsq(const double* w, const double* y, long long M, double* out, double* ws,
+                                  cudaStream_t st) {
+  if (M == 0) return cudaMemsetAsync(out, 0, sizeof(double), st);
+  const unsigned blocks = (unsigned)std::min<long long>((M + 255) / 256, kSumsqBlocks);
+  k_weighted_sumsq<<<blocks, 256, 0, st>>>(w, y, M, ws);
+  k_sum_reduce<<<1, 32, 0, st>>>(ws, (int)blocks, out);
   return cudaGetLastError();
 }
 
@@ -639,11 +657,12 @@ cudaError_t launch_split_weights(const double* w, long long M, float2* wds, cuda
 // memory ring, sv = W X p then X^T sv (sv: M float2 of scratch, overwriting wds).
 // *launches: kernels issued; *err: set by a wait that expired.
 cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const double* w, const double* p, long long M,
-                                 double lambda, float2* sv, double* q, int nsm, cudaStream_t st, int* launches,
-                                 int* err) {
+                                 double lambda, float2* sv, double* q, double* ws, int nsm, cudaStream_t st,
+                                 int* launches, int* err) {
   cudaError_t e = cudaMemsetAsync(q, 0, sizeof(double) * (size_t)D, st);
   if (e != cudaSuccess) return e;
   *launches = 0;
+  long long nparts = 0;  // per-block partial column sums in ws, reduced in block order below
   const float* Xc = X + c0;
   // shared memory of the wide fused kernel: the row ring and the per-warp partials
   const int a0 = c0 & ~3;
@@ -665,17 +684,18 @@ cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const d
     const long long rpb = rows_per_cta(M, 1, nsm);
     const unsigned nrb = (unsigned)((M + rpb - 1) / rpb);
     switch ((D + 31) / 32) {
-      case 1: k_normal_matvec_narrow<1><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
-      case 2: k_normal_matvec_narrow<2><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
-      case 3: k_normal_matvec_narrow<3><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
-      case 4: k_normal_matvec_narrow<4><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
-      case 5: k_normal_matvec_narrow<5><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
-      case 6: k_normal_matvec_narrow<6><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
-      case 7: k_normal_matvec_narrow<7><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
-      default: k_normal_matvec_narrow<8><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q); break;
+      case 1: k_normal_matvec_narrow<1><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q, ws); break;
+      case 2: k_normal_matvec_narrow<2><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q, ws); break;
+      case 3: k_normal_matvec_narrow<3><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q, ws); break;
+      case 4: k_normal_matvec_narrow<4><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q, ws); break;
+      case 5: k_normal_matvec_narrow<5><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q, ws); break;
+      case 6: k_normal_matvec_narrow<6><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q, ws); break;
+      case 7: k_normal_matvec_narrow<7><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q, ws); break;
+      default: k_normal_matvec_narrow<8><<<nrb, 256, 0, st>>>(Xc, ldx, D, sv, p, M, rpb, q, ws); break;
     }
+    nparts = nrb;
     *launches = 1;
-  } else if (M > 0 && stages >= kWRows && (ldx % 4) == 0 && cpt <= 16) {
+  } else if (M > 0 && ws && stages >= kWRows && (ldx % 4) == 0 && cpt <= 16) {
     const size_t smem = 256 + (size_t)stages * per_stage;
     const long long rpb = (M + nsm - 1) / nsm;
     const unsigned grid = (unsigned)((M + rpb - 1) / rpb);
@@ -686,7 +706,8 @@ cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const d
               : cpti == 12 ? k_normal_matvec_wide<12> : k_normal_matvec_wide<16>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<grid, kWThreads, smem, st>>>(X, ldx, c0, D, sv, p, M, rpb, rowf, stride, stages, q, err);
+    kern<<<grid, kWThreads, smem, st>>>(X, ldx, c0, D, sv, p, M, rpb, rowf, stride, stages, q, ws, err);
+    nparts = grid;
     *launches = 1;
   } else if (M > 0) {
     const size_t smem = sizeof(float) * 2 * (size_t)D;
@@ -698,8 +719,14 @@ cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const d
     const int ncb = (D + 255) / 256;
     const long long rpb = rows_per_cta(M, ncb, nsm);
     const long long nrb = (M + rpb - 1) / rpb;
-    k_xtv_ds<<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(Xc, ldx, D, sv, M, rpb, q, nullptr);
+    k_xtv_ds<<<dim3((unsigned)nrb, (unsigned)ncb), 256, 0, st>>>(Xc, ldx, D, sv, M, rpb, q, ws);
+    nparts = nrb;
     *launches = 2;
+  }
+  if (nparts > 0 && ws) {
+    k_colsum_reduce<<<(D + kColsumColsPerBlock - 1) / kColsumColsPerBlock, 32 * kColsumColsPerBlock, 0, st>>>(
+        ws, nparts, D, q);
+    *launches += 1;
   }
   if (lambda > 0) {
     e = launch_axpy(D, lambda, p, q, st);
@@ -707,6 +734,17 @@ cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const d
   }
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
+}
+
+// doubles of the partial column sums launch_normal_matvec needs for M rows of D columns
+size_t normal_matvec_workspace_doubles(long long M, int D, int nsm) {
+  if (M <= 0 || D <= 0) return 1;
+  const long long narrow = (M + rows_per_cta(M, 1, nsm) - 1) / rows_per_cta(M, 1, nsm);
+  const long long wide = (M + (M + nsm - 1) / nsm - 1) / ((M + nsm - 1) / nsm);
+  const int ncb = (D + 255) / 256;
+  const long long rpb = rows_per_cta(M, ncb, nsm);
+  const long long xtv = (M + rpb - 1) / rpb;
+  return (size_t)std::max(narrow, std::max(wide, xtv)) * (size_t)D;
 }
 
 template cudaError_t launch_rhs<double>(const double*, int, const double*, const double*, long long, int, double*, int,
@@ -730,6 +768,7 @@ __global__ void __launch_bounds__(1024) k_jacobi_solve(const double* __restrict_
                                                        int D, double lambda, double rcond, double* __restrict__ wout,
                                                        double* __restrict__ evals, int* __restrict__ info) {
   extern __shared__ double sm[];
+  __shared__ double wred[64];  // per-warp partial sums of the convergence test
   const int n = (D + 1) & ~1;  // even
   double* A = sm;               // n*n
   double* V = A + n * n;        // n*n
@@ -768,9 +807,20 @@ __global__ void __launch_bounds__(1024) k_jacobi_solve(const double* __restrict_
       off += __shfl_xor_sync(0xffffffffu, off, o);
       dia += __shfl_xor_sync(0xffffffffu, dia, o);
     }
+    // warp sums added in warp order (a fixed sweep count for a given matrix)
     if ((tid & 31) == 0) {
-      atomicAdd(&red[0], off);
-      atomicAdd(&red[1], dia);
+      wred[2 * (tid >> 5)] = off;
+      wred[2 * (tid >> 5) + 1] = dia;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double so = 0.0, sd = 0.0;
+      for (int w = 0; w < nth / 32; ++w) {
+        so += wred[2 * w];
+        sd += wred[2 * w + 1];
+      }
+      red[0] = so;
+      red[1] = sd;
     }
     __syncthreads();
     if (red[0] <= 1e-28 * red[1] || red[1] == 0.0) break;

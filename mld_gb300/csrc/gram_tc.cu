@@ -13,8 +13,10 @@
 // Grid: (upper-triangle tile pairs) x (row splits), split-major so that the CTAs resident at one
 // time read the same rows (L2 reuse).  Per CTA: warp 0 issues TMA loads into a 3-stage ring,
 // warp 1 allocates two 128-column TMEM accumulators and issues tcgen05.mma from one thread,
-// warps 2-17 drain the accumulators with tcgen05.ld into compensated FP32 sums and finally add
-// them into the FP64 Gram with atomics (one FP64 add per element and split).  Every mbarrier wait
+// warps 2-17 drain the accumulators with tcgen05.ld into compensated FP32 sums.  With several
+// row splits each split writes its tile to a partial buffer and k_gram_tc_reduce adds the splits
+// into the FP64 Gram in split order (without that buffer: FP64 atomics, order not fixed); with
+// one split the CTA adds its tile directly.  Every mbarrier wait
 // is bounded: on expiry the CTA sets *err, waits (bounded) for its copies in flight and still
 // frees its TMEM.
 #include <cuda.h>
@@ -99,8 +101,8 @@ __global__ void __launch_bounds__(256) k_split_bf16(const T* __restrict__ X, int
 // quarter (32 columns) of the tile.
 __global__ void __launch_bounds__(kGramThreads, 1)
     k_gram_tc(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo, int nt,
-              int ntile, int nk, int kps, int flush, int D, double* __restrict__ G, int* __restrict__ err,
-              int skip_loads, long long wait_limit) {
+              int ntile, int nk, int kps, int flush, int D, double* __restrict__ G, double* __restrict__ part,
+              int* __restrict__ err, int skip_loads, long long wait_limit) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* tiles = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = reinterpret_cast<uint64_t*>(tiles + kStages * kStageBytes);
@@ -230,7 +232,14 @@ __global__ void __launch_bounds__(kGramThreads, 1)
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(&tempty[b]);
     }
-    if (got) {
+    if (got && part) {
+      // this split's tile, added to G in split order by k_gram_tc_reduce
+      double* pt = part + ((size_t)split * ntile + blockIdx.x % ntile) * (kTM * kTM) + (size_t)(q * 32 + lane) * kTM +
+                   cq * 32;
+#pragma unroll
+      for (int c = 0; c < 32; ++c) pt[c] = (double)sum[c] - (double)cmp[c];
+    } else if (got) {
+      // straight into G: with a single split the CTA is the only writer of these elements
       const int i = ti * kTM + q * 32 + lane;
       if (i < D) {
 #pragma unroll
@@ -267,6 +276,41 @@ void gram_tc_test_timeout(int skip_loads, long long wait_limit) {
 
 size_t gram_tc_min_workspace(int D) { return (size_t)4 * D * kTK + 256; }
 
+namespace {
+// row splits of one chunk of nk 64-row slices: at least two waves of CTAs where the tile count
+// alone does not give them, every split non-empty
+int gram_tc_splits(int nk, int ntile, int nsm, int* kps) {
+  const int ns = std::max(1, std::min(nk, (2 * nsm + ntile - 1) / ntile));
+  *kps = (nk + ns - 1) / ns;
+  return (nk + *kps - 1) / *kps;
+}
+
+// G[i][j] += sum over the splits of their tile partials, in split order (upper triangle).
+__global__ void k_gram_tc_reduce(const double* __restrict__ part, int nt, int ntile, int nsplit, int D,
+                                 double* __restrict__ G) {
+  const int tile = blockIdx.y;
+  int t = tile, ti = 0;
+  while (t >= nt - ti) {
+    t -= nt - ti;
+    ++ti;
+  }
+  const int tj = ti + t;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;  // element of the kTM x kTM tile
+  if (e >= kTM * kTM) return;
+  const int i = ti * kTM + e / kTM, j = tj * kTM + e % kTM;
+  if (i >= D || j >= D || j < i) return;
+  double s = 0.0;
+  for (int sp = 0; sp < nsplit; ++sp) s += part[((size_t)sp * ntile + tile) * (kTM * kTM) + e];
+  G[(size_t)i * D + j] += s;
+}
+}  // namespace
+
+size_t gram_tc_part_doubles(int D, int nsm) {
+  const int nt = (D + kTM - 1) / kTM, ntile = nt * (nt + 1) / 2;
+  if (ntile >= 2 * nsm) return 0;  // one split per chunk: no partials
+  return (size_t)(2 * nsm + ntile) * kTM * kTM;
+}
+
 bool gram_tc_available() { return tc::encode_fn() != nullptr; }
 
 // G (FP64, D x D, upper triangle) += sum over rows r of w_r x_r x_r^T for columns [c0, c0 + D)
@@ -274,7 +318,7 @@ bool gram_tc_available() { return tc::encode_fn() != nullptr; }
 // are processed in chunks that fit it.  The caller zeroes G and *err and symmetrises G.
 template <typename T>
 cudaError_t launch_gram_tc(const T* X, int ldx, int c0, int D, const double* w, long long M, double* G, void* ws,
-                           size_t ws_bytes, int* err, int nsm, cudaStream_t st) {
+                           size_t ws_bytes, int* err, int nsm, cudaStream_t st, double* part, size_t part_doubles) {
   if (M <= 0 || D <= 0) return cudaSuccess;
   if (ws_bytes < gram_tc_min_workspace(D) || ((uintptr_t)ws & 15)) return cudaErrorInvalidValue;
   // chunk rows: a multiple of 64 whose two planes fit the workspace
@@ -300,21 +344,28 @@ cudaError_t launch_gram_tc(const T* X, int ldx, int c0, int D, const double* w, 
     CUtensorMap mh, ml;
     if (!tc::make_plane_map(&mh, hi, Mp, D, Mp) || !tc::make_plane_map(&ml, lo, Mp, D, Mp)) return cudaErrorInvalidValue;
     const int nk = (int)((rows + kTK - 1) / kTK);
-    // row splits: at least two waves of CTAs where the tile count alone does not give them
-    int nsplit = std::max(1, std::min(nk, (2 * nsm + ntile - 1) / ntile));
-    const int kps = (nk + nsplit - 1) / nsplit;
-    nsplit = (nk + kps - 1) / kps;  // every split non-empty
+    int kps = 1;
+    const int nsplit = gram_tc_splits(nk, ntile, nsm, &kps);
+    // several splits of a tile: per-split partials reduced in split order when the workspace
+    // holds them (deterministic); otherwise FP64 atomics (order of the splits not fixed)
+    const bool use_part = nsplit > 1 && part && part_doubles >= (size_t)nsplit * ntile * kTM * kTM;
+    double* pt = use_part ? part : nullptr;
     k_gram_tc<<<(unsigned)(ntile * nsplit), kGramThreads, kGramSmem, st>>>(mh, ml, nt, ntile, nk, kps, kFlush, D, G,
-                                                                           err, g_skip_loads, g_wait_limit);
+                                                                           pt, err, g_skip_loads, g_wait_limit);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (use_part) {
+      k_gram_tc_reduce<<<dim3((kTM * kTM + 255) / 256, (unsigned)ntile), 256, 0, st>>>(part, nt, ntile, nsplit, D, G);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
   }
   return cudaSuccess;
 }
 
 template cudaError_t launch_gram_tc<float>(const float*, int, int, int, const double*, long long, double*, void*,
-                                           size_t, int*, int, cudaStream_t);
+                                           size_t, int*, int, cudaStream_t, double*, size_t);
 template cudaError_t launch_gram_tc<double>(const double*, int, int, int, const double*, long long, double*, void*,
-                                            size_t, int*, int, cudaStream_t);
+                                            size_t, int*, int, cudaStream_t, double*, size_t);
 
 }  // namespace mld

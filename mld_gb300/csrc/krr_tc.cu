@@ -203,8 +203,8 @@ __global__ void __launch_bounds__(kKThreads, 1)
                    int nkb, int stages, int vrows, int nvr, int nk, const TileMeta* __restrict__ tmeta,
                    const float4* __restrict__ vrec,
                    const float* __restrict__ F, const float* __restrict__ szz, float s2, float l2, float pw,
-                   const long long* __restrict__ trow, int c0, int ldx, float* __restrict__ X,
-                   int* __restrict__ err) {
+                   const long long* __restrict__ trow, const int* __restrict__ gstart, int c0, int ldx,
+                   float* __restrict__ X, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* ztile = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const uint32_t zbytes = (uint32_t)nkb * 2 * kTileBytes;
@@ -225,8 +225,11 @@ __global__ void __launch_bounds__(kKThreads, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
 
   const int n0 = blockIdx.x * kTM;
-  const int g = blockIdx.y, G = gridDim.y;
-  const int nmine = g < ntiles ? (ntiles - g + G - 1) / G : 0;
+  // the CTA's tiles: the contiguous range [gstart[g], gstart[g + 1]) of the chunk, so that the
+  // tiles of one owner (atom or structure) are added to its rows by one CTA, in order
+  const int g = blockIdx.y;
+  const int t0 = gstart[g];
+  const int nmine = gstart[g + 1] - t0;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
@@ -267,7 +270,7 @@ __global__ void __launch_bounds__(kKThreads, 1)
         ok = false;
         break;
       }
-      const TileMeta m = tmeta[g + i * G];
+      const TileMeta m = tmeta[t0 + i];
       const int nbox = (m.N + kBoxRows - 1) / kBoxRows;
       unsigned char* vs = vtile + (size_t)st * sbytes;
       ptx::mbar_expect_tx(&full[st], (uint32_t)(nkb * 2 * nbox * kBoxBytes));
@@ -298,7 +301,7 @@ __global__ void __launch_bounds__(kKThreads, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t idesc = tc::idesc_m128(tmeta[g + i * G].N);
+      const uint32_t idesc = tc::idesc_m128(tmeta[t0 + i].N);
       const uint32_t acc = tmem + (uint32_t)(b * (kTmemCols / 2));
       const uint32_t svs = sv + (uint32_t)st * sbytes;
       for (int kb = 0; kb < nkb; ++kb) {
@@ -335,12 +338,12 @@ __global__ void __launch_bounds__(kKThreads, 1)
     float4 rv = make_float4(0.f, 0.f, 0.f, 0.f);
     auto stage_load = [&](int j) {
       if (j >= nmine) return;
-      const TileMeta m = tmeta[g + j * G];
+      const TileMeta m = tmeta[t0 + j];
       if (etid < RECS * m.nvp) rv = vrec[RECS * (size_t)m.vr0 + etid];
     };
     auto stage_store = [&](int j) {
       if (j >= nmine) return;
-      if (etid < RECS * tmeta[g + j * G].nvp) {
+      if (etid < RECS * tmeta[t0 + j].nvp) {
         srec[(j % 3) * RECS * nvmax + etid] = rv;
         if (etid % RECS == 0) sce[(j % 3) * nvmax + etid / RECS] = __float_as_int(rv.x);
       }
@@ -349,7 +352,7 @@ __global__ void __launch_bounds__(kKThreads, 1)
     float xf[NCH][8];
     auto fetch = [&](int j) {
       if (j >= nmine) return;
-      const int nch = tmeta[g + j * G].nvp >> 3;
+      const int nch = tmeta[t0 + j].nvp >> 3;
       const int* ce = sce + (j % 3) * nvmax;
 #pragma unroll
       for (int cc = 0; cc < NCH; ++cc) {
@@ -374,8 +377,8 @@ __global__ void __launch_bounds__(kKThreads, 1)
     bool got = true;
     for (int i = 0; i < nmine; ++i) {
       const int b = i & 1;
-      const TileMeta m = tmeta[g + i * G];
-      const long long xr = trow[g + i * G];
+      const TileMeta m = tmeta[t0 + i];
+      const long long xr = trow[t0 + i];
       stage_load(i + 2);
       // the accumulator; the barrier also publishes the records staged one tile earlier, and a
       // timed-out wait in any epilogue warp ends the loop for all of them together
@@ -533,9 +536,10 @@ int tiles_of(int nv, int nvmax) { return (nv + nvmax - 1) / nvmax; }
 int tile_vectors(int nv, int ns, int j) { return nv / ns + (j < nv % ns ? 1 : 0); }
 int rows_of(int nvp, int R) { return (R * nvp + 15) / 16 * 16; }
 // workspace of a chunk: planes (with a spare box of rows), vector records, tile records and rows
+constexpr int kMaxGroups = 1024;  // CTAs per column tile (<= SMs)
 size_t chunk_bytes(size_t rows, size_t vecs, size_t tiles, int KP, int R) {
   return 2 * al256((rows + kBoxRows) * (size_t)KP * 2) + al256(vecs * 16 * recs_of(R)) +
-         al256(tiles * sizeof(TileMeta)) + al256(tiles * sizeof(long long));
+         al256(tiles * sizeof(TileMeta)) + al256(tiles * sizeof(long long)) + al256(sizeof(int) * (kMaxGroups + 1));
 }
 // the tiles of a group of nv vectors owned by `owner` (row0 and vr0 are set per chunk)
 void push_tiles(std::vector<TileMeta>& tiles, int owner, int nv, int nvmax, int R) {
@@ -554,7 +558,7 @@ constexpr size_t kSmemMax = 227 * 1024;
 
 using ForceKernel = void (*)(CUtensorMap, CUtensorMap, CUtensorMap, CUtensorMap, int, int, int, int, int, int,
                              const TileMeta*, const float4*, const float*, const float*, float, float, float,
-                             const long long*, int, int, float*, int*);
+                             const long long*, const int*, int, int, float*, int*);
 template <int R>
 ForceKernel kernel_for(int P) {
   return P == 1 ? k_krr_force_tc<1, R> : P == 2 ? k_krr_force_tc<2, R> : P == 3 ? k_krr_force_tc<3, R>
@@ -626,18 +630,34 @@ cudaError_t run_tiles(const std::vector<TileMeta>& tiles, const PassCtx& c, Buil
     TileMeta* dmeta = reinterpret_cast<TileMeta*>(p);
     p += al256(sizeof(TileMeta) * nt);
     long long* trow = reinterpret_cast<long long*>(p);
+    p += al256(sizeof(long long) * nt);
+    int* dgs = reinterpret_cast<int*>(p);
+    // one CTA per SM: the column tiles times G row groups in a single wave; group g takes the
+    // contiguous tiles [gs[g], gs[g + 1]), about 1/G of the rows each, cut only between owners
+    const int G = std::max(1, std::min<int>({(int)nt, c.NT >= c.nsm ? 1 : c.nsm / c.NT, kMaxGroups}));
+    std::vector<int> gs(G + 1, (int)nt);
+    gs[0] = 0;
+    {
+      size_t acc = 0;
+      int gi = 1;
+      for (size_t t = 0; t < nt && gi < G; ++t) {
+        acc += (size_t)meta[t].N;
+        const bool boundary = t + 1 == nt || meta[t + 1].atom != meta[t].atom;
+        while (gi < G && boundary && acc * (size_t)G >= (size_t)gi * nrows) gs[gi++] = (int)(t + 1);
+      }
+    }
     cudaError_t e = cudaMemcpyAsync(dmeta, meta.data(), sizeof(TileMeta) * nt, cudaMemcpyHostToDevice, c.st);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(dgs, gs.data(), sizeof(int) * (G + 1), cudaMemcpyHostToDevice, c.st);
     if (e != cudaSuccess) return e;
     build(dmeta, (int)nt, vhi, vlo, vrec, trow);
     CUtensorMap mvh, mvl;
     if (!tc::make_plane_map(&mvh, vhi, c.KP, (long long)(nrows + kBoxRows), c.KP, kBoxRows) ||
         !tc::make_plane_map(&mvl, vlo, c.KP, (long long)(nrows + kBoxRows), c.KP, kBoxRows))
       return cudaErrorInvalidValue;
-    // one CTA per SM: the column tiles times G row groups in a single wave
-    const int G = std::max(1, std::min<int>((int)nt, c.NT >= c.nsm ? 1 : c.nsm / c.NT));
     kern<<<dim3((unsigned)c.NT, (unsigned)G), kKThreads, smem, c.st>>>(
         mvh, mvl, c.mzh, c.mzl, (int)nt, c.nkb, stages, vrows, nvr, c.nk, dmeta,
-        reinterpret_cast<const float4*>(vrec), c.F, c.szz, c.s2, c.l2, c.pw, trow, c.c0, c.ldx, c.X, c.err);
+        reinterpret_cast<const float4*>(vrec), c.F, c.szz, c.s2, c.l2, c.pw, trow, dgs, c.c0, c.ldx, c.X, c.err);
     *launches += 2;
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;

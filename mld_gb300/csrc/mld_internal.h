@@ -334,11 +334,17 @@ template <typename T>
 cudaError_t launch_rhs(const T* X, int ldx, const double* w, const double* y, long long M, int D, double* h,
                        int nsm, cudaStream_t st, float2* sv, double* ws = nullptr);
 cudaError_t launch_symmetrize(double* G, int D, cudaStream_t st);
-cudaError_t launch_weighted_sumsq(const double* w, const double* y, long long M, double* out, cudaStream_t st);
+// ws: at least kSumsqBlocks doubles (per-block partials, added in block order)
+constexpr int kSumsqBlocksMax = 1024;
+cudaError_t launch_weighted_sumsq(const double* w, const double* y, long long M, double* out, double* ws,
+                                  cudaStream_t st);
 cudaError_t launch_split_weights(const double* w, long long M, float2* wds, cudaStream_t st);
+// ws: normal_matvec_workspace_doubles(M, D, nsm) doubles for the per-block partial column sums,
+// reduced in block order (null: FP64 atomics, order not fixed)
+size_t normal_matvec_workspace_doubles(long long M, int D, int nsm);
 cudaError_t launch_normal_matvec(const float* X, int ldx, int c0, int D, const double* w, const double* p, long long M,
-                                 double lambda, float2* sv, double* q, int nsm, cudaStream_t st, int* launches,
-                                 int* err);
+                                 double lambda, float2* sv, double* q, double* ws, int nsm, cudaStream_t st,
+                                 int* launches, int* err);
 // doubles of the squared-error buffer of launch_predict_sq (3 sums, 3 counts, per-CTA partials)
 size_t predict_sq_doubles();
 template <typename T>
@@ -413,10 +419,13 @@ cudaError_t launch_krr_force_tc(const DevBatch& b, const DevRows& rows, const in
 
 // tensor-core Gram in BF16 split precision (gram_tc.cu)
 size_t gram_tc_min_workspace(int D);
+// doubles of the per-split partial tiles launch_gram_tc needs for a deterministic sum (0: none)
+size_t gram_tc_part_doubles(int D, int nsm);
 void gram_tc_test_timeout(int skip_loads, long long wait_limit);
 bool gram_tc_available();
 template <typename T>
 cudaError_t launch_gram_tc(const T* X, int ldx, int c0, int D, const double* w, long long M, double* G, void* ws,
-                           size_t ws_bytes, int* err, int nsm, cudaStream_t st);
+                           size_t ws_bytes, int* err, int nsm, cudaStream_t st, double* part = nullptr,
+                           size_t part_doubles = 0);
 
 }  // namespace mld

@@ -11,10 +11,12 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _handle(precision, order=1, lam=1e-8):
+def _handle(precision, order=1, lam=1e-8, j_max=None):
     from mld_gb300 import _lib
     c = _lib.default_config()
     c.j_max, c.r_cut, c.lambda_krr, c.precision, c.mld_order = 4.0 if order == 1 else 2.0, 4.7, lam, precision, order
+    if j_max is not None:
+        c.j_max = j_max
     return _lib.Handle(c)
 
 
@@ -87,4 +89,54 @@ def test_evaluation_is_bitwise_reproducible(lib, precision, order):
         r1 = h.evaluate(w)
         r2 = h.evaluate(w)
     for a, b in zip(r1, r2):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("order,j_max", [(1, 4.0), (2, 4.0)])
+def test_mixed_fit_is_bitwise_reproducible(lib, order, j_max):
+    """The mixed method's fit: tensor-core Gram (split partials added in split order), CG with
+    matvecs whose per-block column sums are added in block order, and for the quadratic model at
+    j_max = 4 (1540 quadratic columns) the sketched preconditioner."""
+    ds = _dataset()
+    res = []
+    for _ in range(2):
+        with _handle(1, order, j_max=j_max) as h:
+            _stage(h, ds)
+            w, rmse = h.fit()
+            res.append((w, rmse, h.solve_info()))
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+    assert repr(res[0][2]) == repr(res[1][2])
+
+
+def test_mixed_kernel_fit_is_bitwise_reproducible(lib):
+    """Mixed kernel ridge regression with the tensor-core force and stress rows: 250-atom
+    structures split into several stress tiles per structure, whose contributions one CTA adds
+    in tile order; the kernel block of 1 + 110 + 800 columns takes the sketched preconditioner."""
+    from mld_gb300 import _lib, synth
+    ds = synth.hea_bcc_batched(n_struct=6, reps=5, seed=41)
+    nat, pos, cell, types = ds.arrays()
+    E, F, S, has = ds.labels()
+
+    def cfg(precision, ml_type):
+        c = _lib.default_config()
+        c.j_max, c.r_cut, c.precision, c.ml_type, c.lambda_krr = 4.0, 5.0, precision, ml_type, 1e-6
+        c.weighted, c.n_elements = 1, len(synth.HEA_ELEMENTS)
+        for i, wv in enumerate(synth.HEA_WEIGHTS):
+            c.weight_per_element[i] = wv
+        return c
+
+    with _lib.Handle(cfg(0, 0)) as h:
+        h.set_structures(nat, pos, cell, types)
+        B, _ = h.descriptors()
+    Zraw = B[np.random.default_rng(8).choice(B.shape[0], size=800, replace=False)]
+    res = []
+    for _ in range(2):
+        with _lib.Handle(cfg(1, 1)) as h:
+            h.set_structures(nat, pos, cell, types)
+            h.set_labels(E, F, S, has, np.ones((len(nat), 3)))
+            h.set_kernel_points(Zraw)
+            A, _, _ = h.design_matrix()
+            w, rmse = h.fit()
+            res.append((A, w, rmse))
+    for a, b in zip(res[0], res[1]):
         assert np.array_equal(a, b)
