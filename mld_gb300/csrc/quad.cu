@@ -35,16 +35,33 @@ __global__ void k_reverse_pairs(int A, const int* __restrict__ nbr_off, const in
   for (int p = nbr_off[a] + lane; p < nbr_off[a + 1]; p += 32) {
     const int b = nbr_idx[p];
     const double u0 = nbr_u[3 * (size_t)p], u1 = nbr_u[3 * (size_t)p + 1], u2 = nbr_u[3 * (size_t)p + 2];
-    int found = -1;
-    for (int q = nbr_off[b]; q < nbr_off[b + 1]; ++q) {
-      if (nbr_idx[q] != a) continue;
+    // the lists are in ascending neighbour order (images of one neighbour adjacent): binary
+    // search for a's first entry in b's list, then its images in order; a full scan only if
+    // that finds nothing, so the result is the first match in list order either way
+    auto matches = [&](int q) {
       const double d = fabs(nbr_u[3 * (size_t)q] + u0) + fabs(nbr_u[3 * (size_t)q + 1] + u1) +
                        fabs(nbr_u[3 * (size_t)q + 2] + u2);
-      if (d < 1e-8) {
+      return d < 1e-8;
+    };
+    const int q0 = nbr_off[b], q1 = nbr_off[b + 1];
+    int lo = q0, hi = q1;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (nbr_idx[mid] < a) lo = mid + 1;
+      else hi = mid;
+    }
+    int found = -1;
+    for (int q = lo; q < q1 && nbr_idx[q] == a; ++q)
+      if (matches(q)) {
         found = q;
         break;
       }
-    }
+    if (found < 0)
+      for (int q = q0; q < q1; ++q)
+        if (nbr_idx[q] == a && matches(q)) {
+          found = q;
+          break;
+        }
     rev[p] = found;
   }
 }
