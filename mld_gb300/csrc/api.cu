@@ -54,6 +54,9 @@ struct mld_gpu_handle {
   bool has_batch = false;
   bool nbr_valid = false;
   int max_nn = 0;
+  // neighbours per atom that the single-pass search reserves: 1.5 x the densest structure's
+  // mean count within r_cut, + 8 (at most imm_neigh); an atom above it reruns the two passes
+  int nn_bound = 0;
 
   // labels
   bool has_labels = false;
@@ -119,7 +122,7 @@ struct mld_gpu_handle {
     B_REV, B_HQ, B_YQ, B_GF, B_RES, B_DW,
     B_GWS, B_TERR, B_PCG, B_POS32, B_YSCR, B_RINV, B_KZD, B_KZF, B_KWS, B_WSERVE, B_P32,
     B_EW, B_EBETA, B_EB, B_EOUT, B_KTC, B_SKW, B_ORDER, B_QCNT, B_SP, B_EPAIR, B_EATOM, B_GP,
-    B_CNC, B_CELLOFF, B_CELLOF, B_CELLSTART, B_CELLATOMS, B_SORTTMP, B_NBR_U32, B_MVWS, B_GTCP,
+    B_CNC, B_CELLOFF, B_CELLOF, B_CELLSTART, B_CELLATOMS, B_SORTTMP, B_NBR_U32, B_MVWS, B_GTCP, B_NBRTMP,
     B_COUNT
   };
   static_assert(B_COUNT <= 80, "buffer table too small");
@@ -263,13 +266,27 @@ int build_neighbours(mld_gpu_handle* h) {
     CK(launch_cells(b, bp_<int>(h, mld_gpu_handle::B_SCAN_TMP), h->st));
     nl(h, 5);
   }
-  CK(launch_neighbours(b, h->cfg.r_cut, b.nn, dmax, h->st, 0));
+  // one scan of the candidates into rows of nn_bound pairs per atom when that workspace can be
+  // had, else (or when an atom has more) a counting scan and a filling scan
+  b.nbr_cap = 0;
+  b.nbr_tmp = nullptr;
+  if (h->nn_bound > 0 && h->A > 0) {
+    const size_t tb = sizeof(int2) * (size_t)h->A * (size_t)h->nn_bound;
+    if (ensure(h, mld_gpu_handle::B_NBRTMP, tb) == cudaSuccess) {
+      b.nbr_cap = h->nn_bound;
+      b.nbr_tmp = bp_<int2>(h, mld_gpu_handle::B_NBRTMP);
+    } else {
+      cudaGetLastError();  // the failed allocation leaves no error for later launches
+    }
+  }
+  CK(launch_neighbours(b, h->cfg.r_cut, b.nn, dmax, h->st, b.nbr_cap > 0 ? 2 : 0));
   CK(launch_scan(b.nn, b.nbr_off, h->A, bp_<int>(h, mld_gpu_handle::B_SCAN_TMP), h->st));
   nl(h, 5);
   int hv[2] = {0, 0};
   CK(cudaMemcpyAsync(&hv[0], b.nbr_off + h->A, sizeof(int), cudaMemcpyDeviceToHost, h->st));
   CK(cudaMemcpyAsync(&hv[1], dmax, sizeof(int), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
+  if (b.nbr_cap > 0 && hv[1] > b.nbr_cap && hv[1] <= h->cfg.imm_neigh) b.nbr_cap = 0;  // the rows overflowed
   if (hv[1] > h->cfg.imm_neigh)
     return fail(h, MLD_ERR_NEIGHBOUR_CAP,
                 "an atom has " + std::to_string(hv[1]) + " neighbours within r_cut, more than imm_neigh=" +
@@ -292,8 +309,8 @@ int build_neighbours(mld_gpu_handle* h) {
     b.sort_tmp = bp_<int>(h, mld_gpu_handle::B_SORTTMP);
     nl(h, 1);
   }
-  CK(launch_neighbours(b, h->cfg.r_cut, b.nn, dmax, h->st, 1));
-  nl(h, b.P > 0 ? 2 : 1);  // filling pass and pair displacements
+  CK(launch_neighbours(b, h->cfg.r_cut, b.nn, dmax, h->st, b.nbr_cap > 0 ? 3 : 1));
+  nl(h, b.P > 0 ? 2 : 1);  // filling pass (or compaction) and pair displacements
   // longest-first order of the descriptor kernel's work queue; one counter int + sort workspace
   CK(ensure(h, mld_gpu_handle::B_ORDER, sizeof(int) * std::max(1, h->A)));
   CK(ensure(h, mld_gpu_handle::B_QCNT, sizeof(int) * (4 + atom_order_tmp_ints(h->max_nn))));
@@ -1221,6 +1238,12 @@ int mld_gpu_set_structures(mld_gpu_handle* h, int nstruct, const int* nat, const
       }
     }
     cell_off[s + 1] = cell_off[s] + ncell;
+  }
+  {
+    const double rc3 = h->cfg.r_cut * h->cfg.r_cut * h->cfg.r_cut;
+    double worst = 0.0;
+    for (int s = 0; s < nstruct; ++s) worst = std::max(worst, nat[s] / vol[s]);
+    h->nn_bound = (int)std::min<double>(h->cfg.imm_neigh, 1.5 * worst * 4.18879 * rc3 + 8.0);
   }
   h->S = nstruct;
   h->A = A;

@@ -650,7 +650,7 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
           for (int r = 0; r < kRowTile; ++r)
 #pragma unroll
             for (int c = 0; c < kCT; ++c) acc[r][c] = T(0);
-#pragma unroll 2
+#pragma unroll 4
           for (int e = 0; e < H; ++e) {
             cx<T> y[kRowTile], v[kCT];
 #pragma unroll

@@ -240,6 +240,9 @@ struct DevBatch {
   int* cell_start = nullptr; // ncells+1 first entry of each cell in cell_atoms (then a cursor of ncells)
   int* cell_atoms = nullptr; // A atoms grouped by cell
   int* sort_tmp = nullptr;   // P  neighbour indices while the lists of celled structures are sorted
+  // single-pass search: each atom's pairs (neighbour, packed image) in a row of nbr_cap entries
+  int2* nbr_tmp = nullptr;   // A * nbr_cap
+  int nbr_cap = 0;
 };
 
 // Design-row placement of each structure (-1 when a block is absent).
@@ -265,8 +268,11 @@ struct BsoParams {
 inline int round_up4(int d) { return (d + 3) & ~3; }
 
 // Kernels / launchers (return cudaError_t of the launch).
+// pass 0 counts and 1 fills the CSR lists (two scans of the candidates); pass 2 counts and
+// writes each atom's pairs into b.nbr_tmp in one scan, pass 3 then compacts them into the CSR.
+// Passes 1 and 3 end with the sorted lists of celled structures and the displacements.
 cudaError_t launch_neighbours(const DevBatch& b, double rcut, int* counts, int* maxcount, cudaStream_t st,
-                              int pass /*0 count, 1 fill*/);
+                              int pass);
 cudaError_t launch_scan(const int* in, int* out, int n, int* d_tmp, cudaStream_t st);
 // Bin the atoms of celled structures (b.cnc) into their cells; scan_tmp as for launch_scan over
 // b.ncells entries.  Then launch_neighbours scans the 27 (or fewer, unique) cells around each

@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(256) k_neighbours(
     int pass, int* __restrict__ counts, int* __restrict__ maxcount, const int* __restrict__ offsets,
     int* __restrict__ nbr_idx, double* __restrict__ nbr_u, const int* __restrict__ cnc,
     const int* __restrict__ cell_off, const int* __restrict__ cell_of, const int* __restrict__ cell_start,
-    const int* __restrict__ cell_atoms) {
+    const int* __restrict__ cell_atoms, int cap, int2* __restrict__ tmp) {
   constexpr float kBand = 1e-3f;
   const int lane = threadIdx.x & 31;
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -149,11 +149,14 @@ __global__ void __launch_bounds__(256) k_neighbours(
               nbr_idx[slot] = jg;
               nbr_u[3 * (size_t)slot] = (double)g;
               nbr_u[3 * (size_t)slot + 1] = (double)pack_image(0, 0, 0);
+            } else if (pass == 2 && ok) {
+              const int k = count + __popc(m & ((1u << lane) - 1u));
+              if (k < cap) tmp[(size_t)g * cap + k] = make_int2(jg, pack_image(0, 0, 0));
             }
             count += __popc(m);
           }
         }
-    if (pass == 0 && lane == 0) {
+    if (pass != 1 && lane == 0) {
       counts[g] = count;
       atomicMax(maxcount, count);
     }
@@ -228,12 +231,32 @@ __global__ void __launch_bounds__(256) k_neighbours(
       nbr_idx[slot] = a0 + jj;
       nbr_u[3 * (size_t)slot] = (double)g;
       nbr_u[3 * (size_t)slot + 1] = (double)img;
+    } else if (pass == 2 && ok) {
+      // single pass: the pair into the atom's fixed-capacity row (compacted after the scan)
+      const int k = count + __popc(m & ((1u << lane) - 1u));
+      if (k < cap) tmp[(size_t)g * cap + k] = make_int2(a0 + jj, img);
     }
     count += __popc(m);
   }
-  if (pass == 0 && lane == 0) {
+  if (pass != 1 && lane == 0) {
     counts[g] = count;
     atomicMax(maxcount, count);
+  }
+}
+
+// Single-pass lists: atom g's pairs from its fixed-capacity row into the CSR (offsets from the
+// scan of the counts), in their order; one warp per atom.
+__global__ void k_nbr_compact(int A, int cap, const int* __restrict__ counts, const int* __restrict__ offsets,
+                              const int2* __restrict__ tmp, int* __restrict__ nbr_idx, double* __restrict__ nbr_u) {
+  const int lane = threadIdx.x & 31;
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (g >= A) return;
+  const int n = min(counts[g], cap), p0 = offsets[g];
+  for (int k = lane; k < n; k += 32) {
+    const int2 t = tmp[(size_t)g * cap + k];
+    nbr_idx[p0 + k] = t.x;
+    nbr_u[3 * (size_t)(p0 + k)] = (double)g;
+    nbr_u[3 * (size_t)(p0 + k) + 1] = (double)t.y;
   }
 }
 
@@ -414,19 +437,24 @@ cudaError_t launch_neighbours(const DevBatch& b, double rcut, int* counts, int* 
   const long long warps = b.A;
   const int blocks = (int)((warps * 32 + threads - 1) / threads);
   if (!b.pos32 || !b.frac32) return cudaErrorInvalidValue;
-  if (pass == 0)
+  if (pass == 0 || pass == 2)
     k_nbr_prep<<<(b.A + 255) / 256, 256, 0, st>>>(b.A, b.atom_struct, b.atom_start, b.pos, b.recip, b.pos32, b.frac32);
-  k_neighbours<<<blocks, threads, 0, st>>>(b.A, b.atom_struct, b.atom_start, b.pos, b.pos32, b.frac32, b.cell,
-                                           b.recip, b.small, b.nsize, rcut, pass, counts, maxcount, b.nbr_off,
-                                           b.nbr_idx, b.nbr_u, b.ncells > 0 ? b.cnc : nullptr, b.cell_off,
-                                           b.cell_of, b.cell_start, b.cell_atoms);
-  if (pass == 1 && b.P > 0 && b.ncells > 0) {
+  if (pass == 2 && (!b.nbr_tmp || b.nbr_cap < 1)) return cudaErrorInvalidValue;
+  if (pass != 3)
+    k_neighbours<<<blocks, threads, 0, st>>>(b.A, b.atom_struct, b.atom_start, b.pos, b.pos32, b.frac32, b.cell,
+                                             b.recip, b.small, b.nsize, rcut, pass, counts, maxcount,
+                                             b.nbr_off, b.nbr_idx, b.nbr_u, b.ncells > 0 ? b.cnc : nullptr,
+                                             b.cell_off, b.cell_of, b.cell_start, b.cell_atoms, b.nbr_cap, b.nbr_tmp);
+  if (pass == 2) return cudaGetLastError();
+  if (pass == 3 && b.P > 0)
+    k_nbr_compact<<<blocks, threads, 0, st>>>(b.A, b.nbr_cap, counts, b.nbr_off, b.nbr_tmp, b.nbr_idx, b.nbr_u);
+  if (pass >= 1 && b.P > 0 && b.ncells > 0) {
     // ascending neighbour order of the celled structures' lists, before their displacements
     if (!b.sort_tmp) return cudaErrorInvalidValue;
     cudaError_t e = launch_sort_lists(b, st);
     if (e != cudaSuccess) return e;
   }
-  if (pass == 1 && b.P > 0)
+  if (pass >= 1 && b.P > 0)
     k_nbr_u<<<(unsigned)((b.P + 255) / 256), 256, 0, st>>>(b.P, b.atom_struct, b.pos, b.cell, b.recip, b.small,
                                                            b.nbr_idx, b.nbr_u, b.nbr_u32);
   return cudaGetLastError();

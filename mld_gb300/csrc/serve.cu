@@ -99,7 +99,8 @@ double request_bytes(const mld_gpu_server* s, int nat, const double* cell) {
   const double nn = std::min<double>(s->cfg.imm_neigh, 1.5 * nat / std::max(vol, 1e-9) * 4.18879 * rc * rc * rc + 8);
   const double eb = s->cfg.precision == MLD_PRECISION_MIXED ? 4.0 : 8.0;
   const double pairs = nat * nn;
-  return pairs * 36.0 + nat * (2.0 * s->KK * eb + 24.0 + 64.0) + 128.0;
+  // per pair: index, FP64 and FP32 displacement, reverse pair, the single-pass search row
+  return pairs * 44.0 + nat * (2.0 * s->KK * eb + 24.0 + 64.0) + 128.0;
 }
 
 void retire(mld_gpu_server* s, int idx) {

@@ -53,3 +53,37 @@ def test_cell_lists_equal_all_atom_search(lib):
         ref = d["B"]
         assert np.abs(B[a0:a0 + pos.shape[0]] - ref).max() <= 1e-10 * np.abs(ref).max()
         a0 += pos.shape[0]
+
+
+def test_single_pass_overflow_falls_back_to_two_passes(lib):
+    """The single-pass search reserves 1.5 x the mean neighbour count of the densest structure
+    (+ 8) per atom.  Compact bcc blocks inside large empty boxes have a mean density far below
+    their local one, so their atoms overflow the reserved rows; the search must then rerun as
+    two scans and still return the oracle's lists."""
+    from mld_gb300 import _lib, synth
+    rng = np.random.default_rng(71)
+    structs = []
+    for reps, edge in ((3, 40.0), (2, 50.0)):
+        blk, _ = synth.bcc(reps, reps, reps, synth.FE_A)
+        structs.append((blk + rng.normal(0.0, 0.05, size=blk.shape) + 10.0, np.eye(3) * edge))
+    c = _lib.default_config()
+    c.j_max, c.r_cut, c.precision = 4.0, 4.7, _lib.PLAIN_FP64
+    with _lib.Handle(c) as h:
+        nat = np.array([p.shape[0] for p, _ in structs], np.int32)
+        h.set_structures(nat, np.concatenate([p for p, _ in structs]), np.stack([cl for _, cl in structs]),
+                         np.zeros(int(nat.sum()), np.int32))
+        B, nn = h.descriptors()
+        nbr, u, _ = h.descriptor_derivatives(int(nn.sum()))
+    a0, p = 0, 0
+    for pos, cell in structs:
+        onn, onbr, ou, _ = oracle.neighbours(pos, cell, 4.7)
+        assert np.array_equal(nn[a0:a0 + pos.shape[0]], onn)
+        for i in range(pos.shape[0]):
+            n = onn[i]
+            assert np.array_equal(nbr[p:p + n] - a0, onbr[i, :n])
+            assert np.abs(u[p:p + n] - ou[i, :n]).max() <= 1e-12
+            p += n
+        a0 += pos.shape[0]
+    # the reserved row length the library derives from the mean densities, exceeded here
+    bound = 1.5 * max(p_.shape[0] / abs(np.linalg.det(cl)) for p_, cl in structs) * 4.18879 * 4.7 ** 3 + 8
+    assert nn.max() > bound
