@@ -36,10 +36,10 @@ RCUT = 4.7
 J_MAX = 4.0
 LAMBDA = 1e-8
 # DRAM bytes (read + write) of one k_bso4<float> launch per atom, from an ncu capture of the
-# 200-structure Fe case (45,702 atoms): 57.7 MB read (neighbour data, tables) + 1.021 GB written
+# 200-structure Fe case (45,702 atoms): 44.3 MB read (neighbour data, tables) + 1.019 GB written
 # (w*dB of every pair, the input of the row gather); both grow with the atoms (and their pairs),
 # so the figure is scaled by the atoms of the launch
-BSO4_DRAM_BYTES_PER_ATOM = (57.66e6 + 1.0208e9) / 45702
+BSO4_DRAM_BYTES_PER_ATOM = (44.30e6 + 1.019354e9) / 45702
 
 
 def _args():
@@ -70,6 +70,24 @@ def _dist():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     return rank, world
+
+
+def max_over_ranks(ms_step: float, world: int) -> float:
+    """The step time of the slowest replica (gloo all-reduce over the ranks; the process group
+    is initialised by the caller when world > 1)."""
+    if world <= 1:
+        return ms_step
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms_step], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rows_per_s(rows_per_replica: int, ms_step: float, world: int) -> float:
+    """Whole-job throughput of `world` replicas that each fit rows_per_replica rows in the
+    slowest replica's step time."""
+    return world * rows_per_replica / (ms_step * 1e-3)
 
 
 class Clocks:
@@ -576,17 +594,11 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("gloo")
     res = run_ours(a, rank, world)
-    ms_step = res["ms_step"]
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([ms_step], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
+    ms_step = max_over_ranks(res["ms_step"], world)
     if rank != 0:
         return
     M, A = res["M"], res["A"]
-    value = world * M / (ms_step * 1e-3)
+    value = aggregate_rows_per_s(M, ms_step, world)
     achieved = res["flops"] / (res["t_desc"] * 1e-3) / 1e12
     cpu = None if a.no_cpu else cpu_sample(res["ds"])
     line = {
