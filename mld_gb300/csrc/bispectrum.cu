@@ -678,16 +678,19 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
         }
         __syncthreads();
         // dB = (rank 0 + rank 1) + rank 2 of element e = col * K + k
-        auto dB_of = [&](int e) {
-          const int col = e / K, k = e - col * K;
-          const int s1 = srslot[k * (kRounds - 1)], s2 = srslot[k * (kRounds - 1) + 1];
-          T v = dBs[e];
-          if (s1 >= 0) v += dB1[(size_t)col * tb.nrank[1] + s1];
-          if (s2 >= 0) v += dB2[(size_t)col * tb.nrank[2] + s2];
-          return v;
-        };
+        // element (col, k): lanes take the components k, warps the columns, so each lane looks
+        // up its k's rank slots once and a warp's stores are contiguous
+        const int nr1 = tb.nrank[1], nr2 = tb.nrank[2];
         if (eval) {
-          for (int e = tid; e < ncols * K; e += nth) dBs[e] = dB_of(e);  // in place: own element
+          for (int k = lane; k < K; k += 32) {
+            const int s1 = srslot[k * (kRounds - 1)], s2 = srslot[k * (kRounds - 1) + 1];
+            for (int col = warp; col < ncols; col += kNW) {
+              T v = dBs[col * K + k];
+              if (s1 >= 0) v += dB1[col * nr1 + s1];
+              if (s2 >= 0) v += dB2[col * nr2 + s2];
+              dBs[col * K + k] = v;  // in place: own element
+            }
+          }
           __syncthreads();
           // forces and stress with the effective weights: the centre's for the forces, the
           // neighbour's for the stress (the neighbour's B in the quadratic stress rows,
@@ -724,9 +727,14 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
         } else {
           // w_ch * dB of every pair of the chunk; one channel's columns per pass
           T* out = args.dBout + (size_t)(p0 + base) * 3 * nchK + ch * K;
-          for (int e = tid; e < nb_here * 3 * K; e += nth) {
-            const int na = e / K, k = e - na * K;  // na = n*3 + a
-            out[(size_t)na * nchK + k] = dB_of(e) * nwt[ch * kNB + na / 3];
+          for (int k = lane; k < K; k += 32) {
+            const int s1 = srslot[k * (kRounds - 1)], s2 = srslot[k * (kRounds - 1) + 1];
+            for (int col = warp; col < ncols; col += kNW) {  // col = n*3 + a
+              T v = dBs[col * K + k];
+              if (s1 >= 0) v += dB1[col * nr1 + s1];
+              if (s2 >= 0) v += dB2[col * nr2 + s2];
+              out[(size_t)col * nchK + k] = v * nwt[ch * kNB + col / 3];
+            }
           }
         }
         __syncthreads();
