@@ -9,13 +9,14 @@
 // Outputs: B per atom and w_ch * dB per pair (the design rows are gathered from them by
 // rows.cu), or, for evaluation with fitted weights, per-pair force and stress contributions.
 // Only half of every layer is computed (X(-p,-q) = (-1)^((p-q)/2) conj X(p,q) for U, c, Z, V);
-// full-layer sums fold into weighted sums over the half.  The recursions run on groups of 8 or
-// 16 lanes per neighbour in phase 1 (8 where the groups' partial sums fit in shared memory without
-// costing a CTA per SM) and 16 in phase 3; phase 2 follows a host-balanced schedule of rounds of
-// 32 equal-shape terms per warp, each distinct Z computation evaluated once.
+// full-layer sums fold into weighted sums over the half.  The recursions run on lane groups:
+// in phase 1 of 16, 8, 6 or 4 lanes per neighbour (the widest that covers the atom's neighbours
+// in the fewest passes), each group writing its neighbour's U to a store that is summed in
+// group order; in phase 3 of 16 lanes; phase 2 follows a host-balanced schedule of rounds of 32
+// equal-shape terms per warp, each distinct Z computation evaluated once.
 //
-// Every floating-point sum has a fixed order: lane groups accumulate privately and are reduced
-// in group order, Z terms land in a term buffer from which the Y slots and B are summed, and the
+// Every floating-point sum has a fixed order: c is summed over the groups' U in group order,
+// pass after pass, Z terms land in a term buffer from which the Y slots and B are summed, and the
 // dB contraction writes each layer row into the buffer of its rank (a triple's distinct layers
 // in ascending order), where every triple has at most one row, so dB = (rank 0 + rank 1) +
 // rank 2.  Results are therefore bitwise reproducible and do not depend on which CTA takes which
@@ -298,7 +299,7 @@ struct KernelArgs {
   // Y (the contracted Z blocks, nch * NYP complex per atom) in global memory, one slice per CTA,
   // when it does not fit in shared memory next to the rest (FP64 with several channels)
   void* yglobal;
-  int g1;  // lanes per neighbour in phase 1 (8 or 16)
+  int g1;  // narrowest lane groups per neighbour in phase 1 (4, 6, 8 or 16) the U store allows
   // outputs: B (A x nch*K) and w_ch * dB (P x 3 x nch*K); or evaluation (ev.pair != nullptr)
   T* Bout;
   T* dBout;
@@ -309,15 +310,15 @@ constexpr int kNW = 8;                  // warps per CTA (== kZWarps)
 constexpr int kG = 16;                  // lanes per neighbour in the U/dU recursion (phase 3)
 constexpr int kNG = kNW * 32 / kG;      // lane groups per CTA in phase 3
 constexpr int kNB = kNG;                // neighbours per phase-3 chunk (one per group)
-// lanes per neighbour in the U recursion of phase 1: 8 (32 neighbours in flight) where the
-// groups' partial sums fit in shared memory next to the rest, else 16 (KernelArgs::g1)
+// lanes per neighbour in the U recursion of phase 1: 16, 8, 6 or 4 per atom (16 to 64
+// neighbours per pass), no narrower than the U store in shared memory allows (KernelArgs::g1)
 static_assert(kNW == kZWarps, "phase-2 schedule is built for the CTA's warps");
 
 // Shared-memory carve-up, in order (every region 16-byte aligned):
 //   rec[HU]  hoff[kMaxJ+2]  rowk[NROWS]  tiles[NTILE]  rank_slot[2K]  cfull[nch*NU]
 //   Y[nch*NYP] (shared Y)
-//   V region (phase 1: group partials + recursion buffers; phase 2: term buffer; phase 3: vecall
-//   of a chunk)
+//   V region (phase 1: U store of the lane groups, their f_c w_ch, c on half layers; phase 2:
+//   term buffer; phase 3: vecall of a chunk)
 //   W region (phase 2: CG coefficients; phase 3: recursion buffers, then the chunk's dB by rank:
 //   rank 0 [cols][K], rank 1 [cols][nrank1], rank 2 [cols][nrank2])
 //   Bk[nch*K]  nwt[nch*NB]  nuu[NB*4]  nidx[NB]  pacc[NB*9] (FP64)  next atom
@@ -327,12 +328,16 @@ struct SmemPlan {
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 
+// lane groups per CTA in phase 1 for g1 lanes per neighbour (whole groups per warp)
+__host__ __device__ constexpr int phase1_groups(int g1) { return kNW * (32 / g1); }
+
 __host__ __device__ inline SmemPlan smem_plan(const DevTables& tb, int nch, int eb, bool y_in_smem, int g1 = 16) {
-  const int ng1 = kNW * 32 / g1;
+  const int ng1 = phase1_groups(g1);
   const size_t LH = tb.hoff[tb.J + 1] - tb.hoff[tb.J];
   const size_t cxb = 2 * (size_t)eb;
   const size_t recb = eb == 8 ? sizeof(RecEntry64) : sizeof(RecEntry32);
-  const size_t v1 = (size_t)ng1 * nch * tb.HU + (size_t)ng1 * 2 * LH;  // phase 1
+  // phase 1: U of every group's neighbour (all half layers), the groups' f_c w_ch, c so far
+  const size_t v1 = (size_t)ng1 * tb.HU + ((size_t)ng1 * nch + 1) / 2 + (size_t)nch * tb.HU;
   const size_t v2 = (size_t)tb.NZT;                                      // phase 2
   const size_t v3 = (size_t)kNB * 3 * tb.HU;                             // phase 3
   const size_t vblock = v1 > v2 ? (v1 > v3 ? v1 : v3) : (v2 > v3 ? v2 : v3);
@@ -356,7 +361,7 @@ __host__ __device__ inline SmemPlan smem_plan(const DevTables& tb, int nch, int 
   s.nuu = o;   o = al16(o + (size_t)eb * kNB * 4);
   s.nidx = o;  o = al16(o + sizeof(int) * kNB);
   s.pacc = o;  o = al16(o + sizeof(double) * kNB * 9);
-  s.next = o;  o = al16(o + sizeof(int) * 4);
+  s.next = o;  o = al16(o + sizeof(int) * (4 + 3 * kMaxJ + 4 + kRounds));
   s.total = o;
   return s;
 }
@@ -387,24 +392,25 @@ __device__ __forceinline__ void pair_u(const KernelArgs<T>& args, size_t q, T* x
   x[2] = (T)u3[2];
 }
 
-// Phase 1 of one atom: lane groups of G1 lanes take the neighbours in turn and add
-// f_c w_ch U of each to their private partial in V (group g at V + g*nch*HU, recursion buffers
-// behind the partials of all groups).
-template <typename T, int G1>
-__device__ __forceinline__ void phase1_c(const KernelArgs<T>& args, const typename RecEntry<T>::type* srec,
-                                         const int* shoff, cx<T>* V, int nn, int p0, int ti, T rcut, T inv_r0, int J,
-                                         int HU, int LH, int nch, int warp, int lane, int tid) {
-  constexpr int NG1 = kNW * 32 / G1;
-  const int grp1 = tid / G1, sl1 = tid % G1;
-  cx<T>* cpart = V + (size_t)grp1 * nch * HU;
-  cx<T>* ub = V + (size_t)NG1 * nch * HU + (size_t)grp1 * 2 * LH;
-  for (int e = sl1; e < nch * HU; e += G1) cpart[e] = {T(0), T(0)};
-  __syncwarp();
-  for (int nb0 = warp * (32 / G1); nb0 < nn; nb0 += NG1) {
-    const int n = nb0 + (lane / G1);
-    const bool active = n < nn;
+// Phase 1 of one atom: c on half layers.  Lane groups of G lanes take one neighbour each
+// (whole groups per warp; neighbour = pass start + group index) and write its U, all half
+// layers, into the group's slot of the store Ust[group][HU], and f_c w_ch into fcw; after each
+// pass chalf += sum over the groups in group order of fcw * U (the diagonal's +1 after the
+// last pass).
+template <typename T, int G>
+__device__ __forceinline__ void phase1_c(const KernelArgs<T>& args, const typename RecEntry<T>::type* __restrict__ srec,
+                                         const int* __restrict__ shoff, cx<T>* Ust, T* fcw, cx<T>* chalf,
+                                         const int8_t* __restrict__ half_diag, int nn, int p0, int ti, T rcut, T inv_r0,
+                                         int J, int HU, int nch, int warp, int lane, int tid) {
+  constexpr int NGW = 32 / G, NG = kNW * NGW;
+  const int gw = lane / G, sl = lane - (lane / G) * G;
+  const int grp = warp * NGW + gw;
+  cx<T>* ug = Ust + (size_t)(gw < NGW ? grp : 0) * HU;
+  const int npass = (nn + NG - 1) / NG;
+  for (int pass = 0; pass < npass; ++pass) {
+    const int n = pass * NG + grp;
+    const bool active = gw < NGW && n < nn;
     NbrGeom<T> g;
-    T wch[kMaxCh] = {T(0), T(0), T(0)};
     if (active) {
       const int nb = args.nbr_idx[p0 + n];
       const int tn = args.types[nb];
@@ -412,11 +418,54 @@ __device__ __forceinline__ void phase1_c(const KernelArgs<T>& args, const typena
       T x[3];
       pair_u<T>(args, (size_t)(p0 + n), x);
       nbr_geometry<T>(x[0], x[1], x[2], rcut, inv_r0, rin, args.rin_w, &g);
+      if (sl == 0) {
+        ug[0] = {T(1), T(0)};
 #pragma unroll
-      for (int ch = 0; ch < kMaxCh; ++ch)
-        if (ch < nch) wch[ch] = args.chw[ch * args.p.ntypes + tn];
+        for (int ch = 0; ch < kMaxCh; ++ch)
+          if (ch < nch) fcw[grp * nch + ch] = g.fc * args.chw[ch * args.p.ntypes + tn];
+      }
     }
-    group_recursion<T, G1, false>(g, srec, J, shoff, ub, LH, nullptr, cpart, wch, nch, HU, sl1, active);
+    __syncwarp();
+    for (int j = 1; j <= J; ++j) {
+      const int h0 = shoff[j], ne = shoff[j + 1] - h0;
+      const cx<T>* prev = ug + shoff[j - 1];
+      if (active) {
+        for (int e = sl; e < ne; e += G) {
+          const auto r = srec[h0 + e];
+          const T tz = (T)r.tz, tx = (T)r.tx;
+          const bool qn = r.qneg != 0;
+          const cx<T> Z = qn ? g.zp : g.zm;
+          const cx<T> X = qn ? g.xm : g.xp;
+          const cx<T> A = {tz * Z.x, tz * Z.y};
+          const cx<T> Bc = {tx * X.y, -tx * X.x};  // -i*tx*X
+          cx<T> u = {T(0), T(0)};
+          if (r.sz >= 0) u = cmul(A, fetch(prev, r.sz));
+          if (r.sx >= 0) u = cfma(Bc, fetch(prev, r.sx), u);
+          ug[h0 + e] = u;
+        }
+      }
+      __syncwarp();
+    }
+    __syncthreads();  // the pass's U store complete
+    const int ngact = min(NG, nn - pass * NG);
+    const bool last = pass == npass - 1;
+    for (int e = tid; e < nch * HU; e += kNW * 32) {
+      const int ch = e / HU, h = e - ch * HU;
+      cx<T> acc = pass == 0 ? cx<T>{T(0), T(0)} : chalf[e];
+      for (int q = 0; q < ngact; ++q) {
+        const T w = fcw[q * nch + ch];
+        const cx<T> u = Ust[(size_t)q * HU + h];
+        acc.x = fma(w, u.x, acc.x);
+        acc.y = fma(w, u.y, acc.y);
+      }
+      if (last && half_diag[h]) acc.x += T(1);
+      chalf[e] = acc;
+    }
+    __syncthreads();  // chalf of this pass complete; the store may be overwritten
+  }
+  if (npass == 0) {  // no neighbours: c is the identity
+    for (int e = tid; e < nch * HU; e += kNW * 32) chalf[e] = {half_diag[e % HU] ? T(1) : T(0), T(0)};
+    __syncthreads();
   }
 }
 
@@ -436,7 +485,6 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
   constexpr int nth = kNW * 32;
   const int LH = tb.hoff[J + 1] - tb.hoff[J];  // largest half layer
   const SmemPlan sp = smem_plan(tb, nch, (int)sizeof(T), kYShared, args.g1);
-  const int ng1 = kNW * 32 / args.g1;
 
   Rec* srec = reinterpret_cast<Rec*>(smem_raw + sp.rec);
   int* shoff = reinterpret_cast<int*>(smem_raw + sp.hoff);
@@ -447,6 +495,10 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
   cx<T>* Y = kYShared ? reinterpret_cast<cx<T>*>(smem_raw + sp.Y)
                       : reinterpret_cast<cx<T>*>(args.yglobal) + (size_t)blockIdx.x * nch * NYP;
   cx<T>* V = reinterpret_cast<cx<T>*>(smem_raw + sp.V);
+  // phase 1 in V: the U store of the groups (as many as args.g1 gives), their f_c w_ch, c
+  cx<T>* p1u = V;
+  T* p1w = reinterpret_cast<T*>(V + (size_t)phase1_groups(args.g1) * HU);
+  cx<T>* p1c = V + (size_t)phase1_groups(args.g1) * HU + ((size_t)phase1_groups(args.g1) * nch + 1) / 2;
   unsigned char* W = smem_raw + sp.W;
   T* scg = reinterpret_cast<T*>(W);  // phase 2 only (restaged per atom)
   T* Bk = reinterpret_cast<T*>(smem_raw + sp.Bk);
@@ -459,6 +511,13 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
   // tables, once per CTA; Y zeroed once (its padding rows are never written)
   for (int e = tid; e < HU; e += nth) srec[e] = args.rec[e];
   for (int e = tid; e < kMaxJ + 2; e += nth) shoff[e] = tb.hoff[e];
+  int* sMp = snext + 4;
+  int* syoff = sMp + (kMaxJ + 1);
+  int* srko = syoff + (kMaxJ + 1);
+  int* snr = srko + (kMaxJ + 2);
+  for (int e = tid; e < kMaxJ + 1; e += nth) { sMp[e] = tb.Mp[e]; syoff[e] = tb.yoff[e]; }
+  for (int e = tid; e < kMaxJ + 2; e += nth) srko[e] = tb.rowk_off[e];
+  for (int e = tid; e < kRounds; e += nth) snr[e] = tb.nrank[e];
   for (int e = tid; e < tb.NROWS; e += nth) srowk[e] = tb.rowk[e];
   for (int e = tid; e < tb.NTILE; e += nth) stile[e] = tb.tiles[e];
   for (int e = tid; e < (kRounds - 1) * K; e += nth) srslot[e] = tb.rank_slot[e];
@@ -483,26 +542,27 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
     // ---------------- phase 1: c^j on half layers, one lane group per neighbour ------------
     // (the CG coefficients of phase 2 are loaded into W meanwhile; W held the previous atom's dB)
     for (int e = tid; e < tb.NCG; e += nth) scg[e] = args.cg[e];
-    if (args.g1 == 8)
-      phase1_c<T, 8>(args, srec, shoff, V, nn, p0, ti, rcut, inv_r0, J, HU, LH, nch, warp, lane, tid);
-    else
-      phase1_c<T, 16>(args, srec, shoff, V, nn, p0, ti, rcut, inv_r0, J, HU, LH, nch, warp, lane, tid);
-    __syncthreads();
-    // group partials summed in group order; the diagonal's +1; expansion to full layers
-    for (int e = tid; e < nch * HU; e += nth) {
-      cx<T> v = {T(0), T(0)};
-      for (int w = 0; w < ng1; ++w) {
-        const cx<T> q = V[(size_t)w * nch * HU + e];
-        v.x += q.x;
-        v.y += q.y;
+    {
+      // lanes per neighbour: the widest group that needs no more passes than the narrowest
+      // allowed one (args.g1)
+      const int npmin = (nn + phase1_groups(args.g1) - 1) / phase1_groups(args.g1);
+      int g1 = args.g1;
+      for (int cand : {16, 8, 6})
+        if (cand > g1 && (nn + phase1_groups(cand) - 1) / phase1_groups(cand) <= npmin) {
+          g1 = cand;
+          break;
+        }
+      switch (g1) {
+        case 16: phase1_c<T, 16>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
+        case 8: phase1_c<T, 8>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
+        case 6: phase1_c<T, 6>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
+        default: phase1_c<T, 4>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
       }
-      if (tb.half_diag[e % HU]) v.x += T(1);
-      V[e] = v;
     }
-    __syncthreads();
+    // expansion to full layers
     for (int e = tid; e < nch * NU; e += nth) {
       const int ch = e / NU, f = e - ch * NU;
-      cfull[e] = fetch(V + ch * HU, tb.expand[f]);
+      cfull[e] = fetch(p1c + ch * HU, tb.expand[f]);
     }
     __syncthreads();
 
@@ -635,8 +695,8 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
           const int tile = stile[tix];
           const int ct = it - tix * ncolt;
           const int j = tile >> 8, rt = tile & 255;
-          const int Mp = tb.Mp[j], H = shoff[j + 1] - shoff[j];
-          const cx<T>* Yp = Yc + tb.yoff[j] + rt * kRowTile;
+          const int Mp = sMp[j], H = shoff[j + 1] - shoff[j];
+          const cx<T>* Yp = Yc + syoff[j] + rt * kRowTile;
           // columns ct, ct + ncolt, ...: lanes of a warp read consecutive columns of V, whose
           // odd stride HU spreads them over distinct shared-memory banks
           const cx<T>* Vp[kCT];
@@ -664,11 +724,11 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
           }
 #pragma unroll
           for (int r = 0; r < kRowTile; ++r) {
-            const int code = srowk[tb.rowk_off[j] + rt * kRowTile + r];
+            const int code = srowk[srko[j] + rt * kRowTile + r];
             if (code < 0) continue;
             const int rank = code >> kRankShift, idx = code & ((1 << kRankShift) - 1);
             T* base = rank == 0 ? dBs : (rank == 1 ? dB1 : dB2);
-            const int ld = tb.nrank[rank];
+            const int ld = snr[rank];
 #pragma unroll
             for (int c = 0; c < kCT; ++c) {
               const int col = ct + c * ncolt;
@@ -796,12 +856,20 @@ cudaError_t launch_bso4(const DevTables& tb, const DevBatch& b, const BsoParams&
   if (ev) a.ev = *ev;
   if (a.ev.pair && dBout) return cudaErrorInvalidValue;
   const bool y_in_smem = smem_plan(tb, p.nch, sizeof(T), true).total <= (size_t)max_optin_smem();
-  // 8-lane phase-1 groups where their partials fit without costing a resident CTA per SM
+  // the narrowest phase-1 groups (most neighbours per pass) whose U store fits without costing
+  // a resident CTA per SM; each atom then takes the widest groups that need no more passes
   const size_t s16 = smem_plan(tb, p.nch, sizeof(T), y_in_smem, 16).total;
-  const size_t s8 = smem_plan(tb, p.nch, sizeof(T), y_in_smem, 8).total;
   const size_t per_sm = 228 * 1024;
-  a.g1 = (s8 <= (size_t)max_optin_smem() && per_sm / (s8 + 1024) >= per_sm / (s16 + 1024)) ? 8 : 16;
-  const size_t smem = a.g1 == 8 ? s8 : s16;
+  a.g1 = 16;
+  size_t smem = s16;
+  for (int g1 : {4, 6, 8}) {
+    const size_t sg = smem_plan(tb, p.nch, sizeof(T), y_in_smem, g1).total;
+    if (sg <= (size_t)max_optin_smem() && per_sm / (sg + 1024) >= per_sm / (s16 + 1024)) {
+      a.g1 = g1;
+      smem = sg;
+      break;
+    }
+  }
   if (smem > (size_t)max_optin_smem()) return cudaErrorInvalidConfiguration;
   a.yglobal = nullptr;
   auto kern = sh.col_tile == 2 ? (y_in_smem ? k_bso4<T, true, 2> : k_bso4<T, false, 2>)
