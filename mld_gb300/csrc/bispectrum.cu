@@ -165,28 +165,21 @@ __device__ __forceinline__ void nbr_geometry(T x0, T x1, T x2, T rcut, T inv_r0,
   for (int a = 0; a < 3; ++a) g->dfr[a] = dfc * drr[a];
 }
 
-// Layer recursion of one neighbour by a group of G lanes (sl = lane within the group) on half
-// layers; rec and hoff live in shared memory.  WITH_DU: U and dU, vecall written to
-// V[a*HU + h] (dU of layer j-1 stays raw in V until layer j is formed, then is converted).
-// Otherwise U only, f_c*w_ch*U added to the group's private partial cpart[ch*HU + h].  Every
-// group of the warp calls this with the same J so that the warp-wide __syncwarp calls line up;
-// inactive groups pass active = false.
-template <typename T, int G, bool WITH_DU>
+// U/dU layer recursion of one neighbour by a group of G lanes (sl = lane within the group) on
+// half layers (phase 3); rec and hoff live in shared memory.  vecall is written to V[a*HU + h]:
+// dU of layer j-1 stays raw in V until layer j is formed, then is converted.  Every group of the
+// warp calls this with the same J so that the warp-wide __syncwarp calls line up; inactive
+// groups pass active = false.
+template <typename T, int G>
 __device__ __forceinline__ void group_recursion(const NbrGeom<T>& g, const typename RecEntry<T>::type* __restrict__ rec,
                                                 int J, const int* __restrict__ hoff, cx<T>* ubuf, int LH, cx<T>* V,
-                                                cx<T>* cpart, const T* wch, int nch, int HU, int sl, bool active) {
+                                                int HU, int sl, bool active) {
   cx<T>* prev = ubuf;
   cx<T>* cur = ubuf + LH;
   if (active && sl == 0) {
     prev[0] = {T(1), T(0)};
-    if constexpr (WITH_DU) {
 #pragma unroll
-      for (int a = 0; a < 3; ++a) V[a * HU] = {T(0), T(0)};
-    } else {
-#pragma unroll
-      for (int ch = 0; ch < kMaxCh; ++ch)
-        if (ch < nch) cpart[ch * HU].x += g.fc * wch[ch];
-    }
+    for (int a = 0; a < 3; ++a) V[a * HU] = {T(0), T(0)};
   }
   __syncwarp();
   for (int j = 1; j <= J; ++j) {
@@ -204,75 +197,59 @@ __device__ __forceinline__ void group_recursion(const NbrGeom<T>& g, const typen
         const cx<T> A = {tz * Z.x, tz * Z.y};
         const cx<T> Bc = {tx * X.y, -tx * X.x};  // -i*tx*X
         cx<T> u = {T(0), T(0)};
-        if constexpr (WITH_DU) {
-          cx<T> du[3] = {{T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}};
-          if (sz >= 0) {
-            const cx<T> Uz = fetch(prev, sz);
-            u = cmul(A, Uz);
+        cx<T> du[3] = {{T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}};
+        if (sz >= 0) {
+          const cx<T> Uz = fetch(prev, sz);
+          u = cmul(A, Uz);
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-              const cx<T> dZ = qn ? g.dzp[a] : g.dzm[a];
-              du[a] = cfma(A, fetch(V + a * HU + pbase, sz), cmul(cx<T>{tz * dZ.x, tz * dZ.y}, Uz));
-            }
-          }
-          if (sx >= 0) {
-            const cx<T> Ux = fetch(prev, sx);
-            u = cfma(Bc, Ux, u);
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-              const cx<T> dX = qn ? g.dxm[a] : g.dxp[a];
-              du[a] = cfma(Bc, fetch(V + a * HU + pbase, sx), cfma(cx<T>{tx * dX.y, -tx * dX.x}, Ux, du[a]));
-            }
-          }
-#pragma unroll
-          for (int a = 0; a < 3; ++a) V[a * HU + idx] = du[a];
-        } else {
-          if (sz >= 0) u = cmul(A, fetch(prev, sz));
-          if (sx >= 0) u = cfma(Bc, fetch(prev, sx), u);
-#pragma unroll
-          for (int ch = 0; ch < kMaxCh; ++ch) {
-            if (ch >= nch) break;
-            const T f = g.fc * wch[ch];
-            cx<T> v = cpart[ch * HU + idx];
-            cpart[ch * HU + idx] = {fma(f, u.x, v.x), fma(f, u.y, v.y)};
+          for (int a = 0; a < 3; ++a) {
+            const cx<T> dZ = qn ? g.dzp[a] : g.dzm[a];
+            du[a] = cfma(A, fetch(V + a * HU + pbase, sz), cmul(cx<T>{tz * dZ.x, tz * dZ.y}, Uz));
           }
         }
+        if (sx >= 0) {
+          const cx<T> Ux = fetch(prev, sx);
+          u = cfma(Bc, Ux, u);
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            const cx<T> dX = qn ? g.dxm[a] : g.dxp[a];
+            du[a] = cfma(Bc, fetch(V + a * HU + pbase, sx), cfma(cx<T>{tx * dX.y, -tx * dX.x}, Ux, du[a]));
+          }
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) V[a * HU + idx] = du[a];
         cur[e] = u;
       }
     }
     __syncwarp();
-    if constexpr (WITH_DU) {
-      if (active) {
-        const int np = h0 - pbase;
-        for (int e = sl; e < np; e += G) {
-          const cx<T> U = prev[e];
-#pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            const cx<T> d = V[a * HU + pbase + e];
-            V[a * HU + pbase + e] = {fma(U.x, g.dfr[a], g.fc * d.x), fma(-U.y, g.dfr[a], -g.fc * d.y)};
-          }
-        }
-      }
-      __syncwarp();
-    }
-    cx<T>* t = prev;
-    prev = cur;
-    cur = t;
-  }
-  if constexpr (WITH_DU) {
     if (active) {
-      const int np = hoff[J + 1] - hoff[J];
+      const int np = h0 - pbase;
       for (int e = sl; e < np; e += G) {
         const cx<T> U = prev[e];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-          const cx<T> d = V[a * HU + hoff[J] + e];
-          V[a * HU + hoff[J] + e] = {fma(U.x, g.dfr[a], g.fc * d.x), fma(-U.y, g.dfr[a], -g.fc * d.y)};
+          const cx<T> d = V[a * HU + pbase + e];
+          V[a * HU + pbase + e] = {fma(U.x, g.dfr[a], g.fc * d.x), fma(-U.y, g.dfr[a], -g.fc * d.y)};
         }
       }
     }
     __syncwarp();
+    cx<T>* t = prev;
+    prev = cur;
+    cur = t;
   }
+  if (active) {
+    const int np = hoff[J + 1] - hoff[J];
+    for (int e = sl; e < np; e += G) {
+      const cx<T> U = prev[e];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const cx<T> d = V[a * HU + hoff[J] + e];
+        V[a * HU + hoff[J] + e] = {fma(U.x, g.dfr[a], g.fc * d.x), fma(-U.y, g.dfr[a], -g.fc * d.y)};
+      }
+    }
+  }
+  __syncwarp();
 }
 
 template <typename T>
@@ -677,8 +654,8 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
           }
         }
         if (eval && sl < 9) pacc[min(n, kNB - 1) * 9 + sl] = 0.0;
-        group_recursion<T, kG, true>(g, srec, J, shoff, ubuf3 + (size_t)grp * 2 * LH, LH,
-                                     V + (size_t)min(n, kNB - 1) * 3 * HU, nullptr, nullptr, nch, HU, sl, active);
+        group_recursion<T, kG>(g, srec, J, shoff, ubuf3 + (size_t)grp * 2 * LH, LH,
+                               V + (size_t)min(n, kNB - 1) * 3 * HU, HU, sl, active);
       }
       __syncthreads();  // V of the chunk complete; the recursion buffers become dBs
       const int ncols = 3 * nb_here;
