@@ -320,7 +320,7 @@ __host__ __device__ inline SmemPlan smem_plan(const DevTables& tb, int nch, int 
   const size_t vblock = v1 > v2 ? (v1 > v3 ? v1 : v3) : (v2 > v3 ? v2 : v3);
   const size_t wrec = (size_t)kNG * 2 * LH * cxb;
   const size_t wdb = (size_t)3 * kNB * (tb.nrank[0] + tb.nrank[1] + tb.nrank[2]) * eb;
-  const size_t wcg = (size_t)eb * tb.NCG;
+  const size_t wcg = al16((size_t)eb * tb.NCG) + (size_t)eb * 4 * tb.K;
   const size_t wblock = wrec > wdb ? (wrec > wcg ? wrec : wcg) : (wdb > wcg ? wdb : wcg);
   SmemPlan s;
   size_t o = 0;
@@ -588,16 +588,26 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
         }
         Yc[se.ypos] = {(T)se.wgt * v.x, (T)se.wgt * v.y};
       }
-      for (int k = tid; k < K; k += nth) {
+      // B_k in four fixed quarters of its items (threads from the top, which have fewer Y slots),
+      // then ((q0 + q1) + q2) + q3
+      T* bpart = reinterpret_cast<T*>(W + al16((size_t)tb.NCG * sizeof(T)));  // [4][K]
+      for (int t2 = nth - 1 - tid; t2 < 4 * K; t2 += nth) {
+        const int k = t2 >> 2, sub = t2 & 3;
+        const int i0 = tb.bk_off[k], i1 = tb.bk_off[k + 1];
+        const int per = (i1 - i0 + 3) >> 2;
+        const int a0 = i0 + sub * per, a1 = min(i1, a0 + per);
         T b = T(0);
-        for (int i = tb.bk_off[k]; i < tb.bk_off[k + 1]; ++i) {
+        for (int i = a0; i < a1; ++i) {
           const BkItem it = tb.bk_items[i];
           const cx<T> cv = cc[it.ufull];
           const cx<T> z = tbuf[it.term];
           b = fma((T)it.wgt, cv.x * z.x + cv.y * z.y, b);  // w * Re(conj(c) ZA)
         }
-        Bk[ch * K + k] = (nn == 0) ? T(0) : b;
+        bpart[sub * K + k] = b;
       }
+      __syncthreads();
+      for (int k = tid; k < K; k += nth)
+        Bk[ch * K + k] = (nn == 0) ? T(0) : ((bpart[k] + bpart[K + k]) + bpart[2 * K + k]) + bpart[3 * K + k];
       __syncthreads();
     }
     if (args.Bout)
