@@ -67,17 +67,19 @@ __global__ void k_reverse_pairs(int A, const int* __restrict__ nbr_off, const in
 }
 
 constexpr int kQT = 4;    // 4x4 output tiles of the triangle
-constexpr int kQC = 16;   // contributors staged per pass
+constexpr int kQC = 16;   // contributors staged per pass when they do not all fit
 
 // One CTA per atom: its 3 quadratic force rows (dedup layout, written at column offset qoff)
-// and its stress partials H[a][s][k].
+// and its stress partials H[a][s][k].  The contributors (the atom itself, then each neighbour)
+// are staged qc at a time: all at once when 1 + nn <= qc, so that every triangle block reads
+// them without restaging.
 template <typename T>
 __global__ void __launch_bounds__(256) k_quad_force(
     int A, int KK, const int* __restrict__ atom_struct, const int* __restrict__ atom_start,
     const int* __restrict__ nbr_off, const int* __restrict__ nbr_idx, const double* __restrict__ nbr_u,
     const int* __restrict__ rev, const int* __restrict__ small, double sign_big, const T* __restrict__ B,
     const T* __restrict__ dB, const long long* __restrict__ rowF, T* __restrict__ X, int ldx, int qoff,
-    T* __restrict__ H, int maxnn) {
+    T* __restrict__ H, int maxnn, int qc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int a = blockIdx.x;
   if (a >= A) return;
@@ -85,9 +87,9 @@ __global__ void __launch_bounds__(256) k_quad_force(
   const int a0 = atom_start[s];
   const int p0 = nbr_off[a], nn = nbr_off[a + 1] - p0;
   const int KP = (KK + kQT - 1) / kQT * kQT;
-  T* G = reinterpret_cast<T*>(smem_raw);        // kQC * 3 * KP
-  T* Bc = G + kQC * 3 * KP;                      // kQC * KP
-  T* fac = Bc + kQC * KP;                        // maxnn * 3: lever-arm factors of the reverse pairs
+  T* G = reinterpret_cast<T*>(smem_raw);        // qc * 3 * KP
+  T* Bc = G + (size_t)qc * 3 * KP;               // qc * KP
+  T* fac = Bc + (size_t)qc * KP;                 // maxnn * 3: lever-arm factors of the reverse pairs
   int* qrev = reinterpret_cast<int*>(fac + 3 * (size_t)maxnn);  // maxnn
   const int tid = threadIdx.x, nth = blockDim.x;
 
@@ -125,6 +127,37 @@ __global__ void __launch_bounds__(256) k_quad_force(
   const int nblk = KP / kQT;
   const int ntri = nblk * (nblk + 1) / 2;
   const int ncontrib = 1 + nn;
+  // contributors c0 .. c0 + cn - 1 into G (gradient rows, items (c, alpha, k)) and Bc: the atom
+  // itself (c = 0: its pairs' derivatives summed in pair order) or neighbour c - 1 (minus the
+  // derivative of its descriptor with respect to this atom)
+  auto stage = [&](int c0, int cn) {
+    for (int e = tid; e < cn * 3 * KP; e += nth) {
+      const int c = e / (3 * KP), r = e - c * 3 * KP, al = r / KP, k = r - al * KP;
+      const int cc = c0 + c;
+      T g = T(0);
+      if (k < KK) {
+        if (cc == 0) {
+          for (int n = 0; n < nn; ++n) g += dB[((size_t)(p0 + n) * 3 + al) * KK + k];
+        } else {
+          const int q = rev[p0 + cc - 1];
+          if (q >= 0) g = -dB[((size_t)q * 3 + al) * KK + k];
+        }
+      }
+      G[(c * 3 + al) * KP + k] = g;
+    }
+    for (int e = tid; e < cn * KP; e += nth) {
+      const int c = e / KP, k = e - c * KP;
+      const int cc = c0 + c;
+      const int src = cc == 0 ? a : nbr_idx[p0 + cc - 1];
+      Bc[c * KP + k] = k < KK ? B[(size_t)src * KK + k] : T(0);
+    }
+  };
+  const bool once = ncontrib <= qc;
+  if (once) {
+    __syncthreads();
+    stage(0, ncontrib);
+    __syncthreads();
+  }
   for (int tb = tid; tb < ((ntri + nth - 1) / nth) * nth; tb += nth) {
     // decode triangle block (bi <= bj)
     int bi = 0, t = tb;
@@ -141,34 +174,13 @@ __global__ void __launch_bounds__(256) k_quad_force(
       for (int x = 0; x < kQT; ++x)
 #pragma unroll
         for (int y = 0; y < kQT; ++y) acc[al][x][y] = T(0);
-    for (int c0 = 0; c0 < ncontrib; c0 += kQC) {
-      const int cn = min(kQC, ncontrib - c0);
-      __syncthreads();
-      for (int e = tid; e < cn * KP; e += nth) {
-        const int c = e / KP, k = e - c * KP;
-        const int cc = c0 + c;
-        T g[3] = {T(0), T(0), T(0)}, bv = T(0);
-        if (k < KK) {
-          if (cc == 0) {  // self: g = sum_n dB(a, n)
-            for (int n = 0; n < nn; ++n)
-#pragma unroll
-              for (int al = 0; al < 3; ++al) g[al] += dB[((size_t)(p0 + n) * 3 + al) * KK + k];
-            bv = B[(size_t)a * KK + k];
-          } else {        // neighbour b: g = -dB(b -> a)
-            const int n = cc - 1;
-            const int q = rev[p0 + n];
-            const int b = nbr_idx[p0 + n];
-            if (q >= 0)
-#pragma unroll
-              for (int al = 0; al < 3; ++al) g[al] = -dB[((size_t)q * 3 + al) * KK + k];
-            bv = B[(size_t)b * KK + k];
-          }
-        }
-#pragma unroll
-        for (int al = 0; al < 3; ++al) G[(c * 3 + al) * KP + k] = g[al];
-        Bc[c * KP + k] = bv;
+    for (int c0 = 0; c0 < ncontrib; c0 += qc) {
+      const int cn = min(qc, ncontrib - c0);
+      if (!once) {
+        __syncthreads();
+        stage(c0, cn);
+        __syncthreads();
       }
-      __syncthreads();
       if (valid) {
         for (int c = 0; c < cn; ++c) {
           T bi4[kQT], bj4[kQT];
@@ -306,11 +318,16 @@ cudaError_t launch_quad_rows(const DevBatch& b, const DevRows& rows, const BsoPa
   if (b.A == 0) return cudaSuccess;
   const int KP = (KK + kQT - 1) / kQT * kQT;
   const int mnn = std::max(1, b.maxnn);
-  size_t sm1 = sizeof(T) * ((size_t)kQC * 4 * KP + 3 * (size_t)mnn) + sizeof(int) * (size_t)mnn + 16;
+  // every contributor staged once when they fit in 96 KB (two CTAs per SM), else kQC at a time
+  auto smem_for = [&](int qc) {
+    return sizeof(T) * ((size_t)qc * 4 * KP + 3 * (size_t)mnn) + sizeof(int) * (size_t)mnn + 16;
+  };
+  const int qc = smem_for(1 + mnn) <= 96 * 1024 ? 1 + mnn : kQC;
+  const size_t sm1 = smem_for(qc);
   cudaError_t e = cudaFuncSetAttribute(k_quad_force<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
   if (e != cudaSuccess) return e;
   k_quad_force<T><<<b.A, 256, sm1, st>>>(b.A, KK, b.atom_struct, b.atom_start, b.nbr_off, b.nbr_idx, b.nbr_u, rev,
-                                         b.small, p.sign_big, B, dB, rows.rowF, X, rows.ldx, qoff, H, mnn);
+                                         b.small, p.sign_big, B, dB, rows.rowF, X, rows.ldx, qoff, H, mnn, qc);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   size_t sm2 = sizeof(T) * (size_t)2 * 32 * KP;
