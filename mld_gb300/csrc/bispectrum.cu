@@ -13,7 +13,7 @@
 // in phase 1 of 16, 8, 6 or 4 lanes per neighbour (the widest that covers the atom's neighbours
 // in the fewest passes), each group writing its neighbour's U to a store that is summed in
 // group order; in phase 3 of 16 lanes; phase 2 follows a host-balanced schedule of rounds of 32
-// equal-shape terms per warp, each distinct Z computation evaluated once.
+// terms of one inner extent per warp, each distinct Z computation evaluated once.
 //
 // Every floating-point sum has a fixed order: c is summed over the groups' U in group order,
 // pass after pass, Z terms land in a term buffer from which the Y slots and B are summed, and the
@@ -93,10 +93,12 @@ struct RecEntry<double> {
   using type = RecEntry64;
 };
 
+// The q < 0 variants are the conjugates: zm = conj(zp), xm = conj(xp), and their derivatives
+// likewise, so only the q >= 0 set is kept.
 template <typename T>
 struct NbrGeom {
-  cx<T> zp, zm, xp, xm;
-  cx<T> dzp[3], dzm[3], dxp[3], dxm[3];
+  cx<T> zp, xp;
+  cx<T> dzp[3], dxp[3];
   T fc, dfr[3];  // fc and dfc * u_a / r
 };
 
@@ -114,9 +116,7 @@ __device__ __forceinline__ void nbr_geometry(T x0, T x1, T x2, T rcut, T inv_r0,
   T sin_i = T(1) / s, tan_i = c / s;
   T l0 = rr * sin_i, l0i = T(1) / l0, z0 = rr * tan_i;
   g->zp = {z0 * l0i, x2 * l0i};
-  g->zm = {z0 * l0i, -x2 * l0i};
   g->xp = {x0 * l0i, x1 * l0i};
-  g->xm = {x0 * l0i, -x1 * l0i};
   T rinv = T(1) / rr;
   T drr[3] = {x0 * rinv, x1 * rinv, x2 * rinv};
   T dz = tan_i - th0 * sin_i * sin_i;
@@ -125,16 +125,11 @@ __device__ __forceinline__ void nbr_geometry(T x0, T x1, T x2, T rcut, T inv_r0,
   for (int a = 0; a < 3; ++a) {
     T base = dz * l0i * drr[a];
     g->dzp[a] = {z0 * dil0 * drr[a] + base, x2 * dil0 * drr[a]};
-    g->dzm[a] = {z0 * dil0 * drr[a] + base, -x2 * dil0 * drr[a]};
     g->dxp[a] = {x0 * dil0 * drr[a], x1 * dil0 * drr[a]};
-    g->dxm[a] = {x0 * dil0 * drr[a], -x1 * dil0 * drr[a]};
   }
   g->dzp[2].y += l0i;
-  g->dzm[2].y -= l0i;
   g->dxp[0].x += l0i;
   g->dxp[1].y += l0i;
-  g->dxm[0].x += l0i;
-  g->dxm[1].y -= l0i;
   // cutoff (neighbours.F90:598-645, types 2 and 3)
   T fo = 0, dfo = 0;
   if (rr <= rcut) {
@@ -191,11 +186,9 @@ __device__ __forceinline__ void group_recursion(const NbrGeom<T>& g, const typen
         const auto r = rec[idx];
         const T tz = (T)r.tz, tx = (T)r.tx;
         const int sz = r.sz, sx = r.sx;
-        const bool qn = r.qneg != 0;
-        const cx<T> Z = qn ? g.zp : g.zm;
-        const cx<T> X = qn ? g.xm : g.xp;
-        const cx<T> A = {tz * Z.x, tz * Z.y};
-        const cx<T> Bc = {tx * X.y, -tx * X.x};  // -i*tx*X
+        const T sq = r.qneg != 0 ? T(1) : T(-1);  // Z = zp or conj(zp), X = conj(xp) or xp
+        const cx<T> A = {tz * g.zp.x, tz * (sq * g.zp.y)};
+        const cx<T> Bc = {-tx * (sq * g.xp.y), -tx * g.xp.x};  // -i*tx*X
         cx<T> u = {T(0), T(0)};
         cx<T> du[3] = {{T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}};
         if (sz >= 0) {
@@ -203,8 +196,7 @@ __device__ __forceinline__ void group_recursion(const NbrGeom<T>& g, const typen
           u = cmul(A, Uz);
 #pragma unroll
           for (int a = 0; a < 3; ++a) {
-            const cx<T> dZ = qn ? g.dzp[a] : g.dzm[a];
-            du[a] = cfma(A, fetch(V + a * HU + pbase, sz), cmul(cx<T>{tz * dZ.x, tz * dZ.y}, Uz));
+            du[a] = cfma(A, fetch(V + a * HU + pbase, sz), cmul(cx<T>{tz * g.dzp[a].x, tz * (sq * g.dzp[a].y)}, Uz));
           }
         }
         if (sx >= 0) {
@@ -212,8 +204,7 @@ __device__ __forceinline__ void group_recursion(const NbrGeom<T>& g, const typen
           u = cfma(Bc, Ux, u);
 #pragma unroll
           for (int a = 0; a < 3; ++a) {
-            const cx<T> dX = qn ? g.dxm[a] : g.dxp[a];
-            du[a] = cfma(Bc, fetch(V + a * HU + pbase, sx), cfma(cx<T>{tx * dX.y, -tx * dX.x}, Ux, du[a]));
+            du[a] = cfma(Bc, fetch(V + a * HU + pbase, sx), cfma(cx<T>{-tx * (sq * g.dxp[a].y), -tx * g.dxp[a].x}, Ux, du[a]));
           }
         }
 #pragma unroll
@@ -410,11 +401,9 @@ __device__ __forceinline__ void phase1_c(const KernelArgs<T>& args, const typena
         for (int e = sl; e < ne; e += G) {
           const auto r = srec[h0 + e];
           const T tz = (T)r.tz, tx = (T)r.tx;
-          const bool qn = r.qneg != 0;
-          const cx<T> Z = qn ? g.zp : g.zm;
-          const cx<T> X = qn ? g.xm : g.xp;
-          const cx<T> A = {tz * Z.x, tz * Z.y};
-          const cx<T> Bc = {tx * X.y, -tx * X.x};  // -i*tx*X
+          const T sq = r.qneg != 0 ? T(1) : T(-1);  // Z = zp or conj(zp), X = conj(xp) or xp
+          const cx<T> A = {tz * g.zp.x, tz * (sq * g.zp.y)};
+          const cx<T> Bc = {-tx * (sq * g.xp.y), -tx * g.xp.x};  // -i*tx*X
           cx<T> u = {T(0), T(0)};
           if (r.sz >= 0) u = cmul(A, fetch(prev, r.sz));
           if (r.sx >= 0) u = cfma(Bc, fetch(prev, r.sx), u);
@@ -505,11 +494,16 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
   const bool need_d = eval || args.dBout != nullptr;
   const int grp = tid / kG, sl = tid % kG;
 
+  // thread 0 takes the next queue position while the current atom runs; it publishes it at the
+  // top of the loop, after at least one barrier that follows every thread's read of the last one
+  int nxt = 0;
+  if (tid == 0) nxt = atomicAdd(args.counter, 1);
   for (;;) {
-    if (tid == 0) snext[0] = atomicAdd(args.counter, 1);
+    if (tid == 0) snext[0] = nxt;
     __syncthreads();  // also orders the table staging and the previous atom's last reads
     const int qi = snext[0];
     if (qi >= A) break;
+    if (tid == 0) nxt = atomicAdd(args.counter, 1);
     const int atom = args.order ? args.order[qi] : qi;
     const int s = args.atom_struct[atom];
     const int ti = args.types[atom];
@@ -517,8 +511,16 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
     const int nn = args.nbr_off[atom + 1] - p0;
 
     // ---------------- phase 1: c^j on half layers, one lane group per neighbour ------------
-    // (the CG coefficients of phase 2 are loaded into W meanwhile; W held the previous atom's dB)
-    for (int e = tid; e < tb.NCG; e += nth) scg[e] = args.cg[e];
+    // (the CG coefficients of phase 2 are copied into W meanwhile by 16-byte asynchronous
+    // copies, the device table being padded to whole chunks; W held the previous atom's dB)
+    {
+      const int n16 = (tb.NCG * (int)sizeof(T) + 15) >> 4;
+      const char* src = reinterpret_cast<const char*>(args.cg);
+      const unsigned dst = (unsigned)__cvta_generic_to_shared(scg);
+      for (int e = tid; e < n16; e += nth)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst + 16u * e), "l"(src + 16 * (size_t)e) : "memory");
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+    }
     {
       // lanes per neighbour: the widest group that needs no more passes than the narrowest
       // allowed one (args.g1)
@@ -541,11 +543,13 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
       const int ch = e / NU, f = e - ch * NU;
       cfull[e] = fetch(p1c + ch * HU, tb.expand[f]);
     }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
 
     // ---------------- phase 2: Z terms -> term buffer -> Y slots and B ----------------------
-    // lane l of a round computes one Z term; the 32 terms of a round share their loop extents,
-    // so the warp runs without divergence.  Entries are prefetched two rounds ahead.
+    // lane l of a round computes one Z term; the 32 terms of a round share their inner extent nb
+    // and have outer extents na in descending order, so the warp diverges only at the end of
+    // the a loop.  Entries are prefetched two rounds ahead.
     cx<T>* tbuf = V;
     for (int ch = 0; ch < nch; ++ch) {
       const cx<T>* cc = cfull + ch * NU;
@@ -577,8 +581,13 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
       }
       __syncthreads();
       cx<T>* Yc = Y + (size_t)ch * NYP;
+      // slot entries (16 bytes) prefetched one iteration ahead
+      uint4 nse = make_uint4(0u, 0u, 0u, 0u);
+      if (tid < tb.NS) nse = __ldg(reinterpret_cast<const uint4*>(tb.slots) + tid);
       for (int e = tid; e < tb.NS; e += nth) {
-        const SlotEntry se = tb.slots[e];
+        SlotEntry se;
+        *reinterpret_cast<uint4*>(&se) = nse;
+        if (e + nth < tb.NS) nse = __ldg(reinterpret_cast<const uint4*>(tb.slots) + e + nth);
         cx<T> v = {T(0), T(0)};
         for (int t = 0; t < se.nterm; ++t) {
           const T sc = (T)se.snum[t] / (T)se.sden[t];

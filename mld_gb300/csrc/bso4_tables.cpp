@@ -328,13 +328,15 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
   }
   t->bk_off[t->K] = (int)t->bk_items.size();
 
-  // phase-2 schedule: every distinct Z computation is one work entry.  Entries of equal loop shape (na, nb)
-  // form rounds of 32, one per lane, padded with entries that write nothing, so that the lanes
-  // of a warp run identical loops; rounds go to the kZWarps warps longest-first (LPT) by their
-  // na * nb cost.  A term stores its Z value at its own index of the term buffer; the slots and
-  // B are summed from there in a fixed order.
+  // phase-2 schedule: every distinct Z computation is one work entry.  Entries of equal inner
+  // extent nb (the kernel unrolls the b loop for it) form rounds of 32, one per lane: sorted by
+  // descending na, so that a round's lanes run a-loops of nearly equal length (the round costs
+  // its first lane's na * nb), the last round of each nb padded with entries of na = 0 that write
+  // nothing.  Rounds go to the kZWarps warps longest-first (LPT) by that cost.  A term stores
+  // its Z value at its own index of the term buffer; the slots and B are summed from there in a
+  // fixed order.
   {
-    std::map<std::pair<int, int>, std::vector<ZItem>> byshape;
+    std::map<int, std::vector<ZItem>> bynb;
     for (size_t u = 0; u < zrep.size(); ++u) {
       const ZTerm& z = t->zterms[zrep[u]];
       ZItem it{};
@@ -347,17 +349,19 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
       it.s1 = z.s1;
       it.s2 = z.s2;
       it.term = (uint16_t)u;
-      byshape[{z.na, z.nb}].push_back(it);
+      bynb[z.nb].push_back(it);
     }
     struct Round { long long cost; std::vector<ZItem> lanes; };
     std::vector<Round> rounds;
-    for (auto& kv : byshape) {
-      const std::vector<ZItem>& v = kv.second;
+    for (auto& kv : bynb) {
+      std::vector<ZItem>& v = kv.second;
+      std::stable_sort(v.begin(), v.end(), [](const ZItem& x, const ZItem& y) { return x.na > y.na; });
       for (size_t i = 0; i < v.size(); i += 32) {
-        Round r{(long long)kv.first.first * kv.first.second, {}};
+        Round r{(long long)v[i].na * kv.first, {}};
         for (size_t l = i; l < std::min(v.size(), i + 32); ++l) r.lanes.push_back(v[l]);
         while (r.lanes.size() < 32) {
-          ZItem pad = v[i];
+          ZItem pad = v[i];  // valid offsets (the kernel loads its nb CG coefficients)
+          pad.na = 0;
           pad.term = kNoTerm;
           r.lanes.push_back(pad);
         }

@@ -90,7 +90,7 @@ constexpr int kRankShift = 12;  // row destination code: (rank << kRankShift) | 
 
 // Host-built constant tables of the SO(4) bispectrum for a given j_max.
 struct Bso4Tables {
-  std::vector<ZItem> zitems;    // phase-2 rounds of 32 equal-shape terms, grouped per warp (LPT)
+  std::vector<ZItem> zitems;    // phase-2 rounds of 32 terms of one nb (na descending), grouped per warp (LPT)
   std::vector<int> zitem_off;   // kZWarps + 1 round offsets (a round is 32 consecutive zitems)
   int J = 0, NU = 0, HU = 0, K = 0, NYP = 0;
   int off[kMaxJ + 2] = {0};     // full-layer offsets
@@ -185,7 +185,12 @@ cudaError_t fill_dev_tables(const Bso4Tables& t, DevTables* d, Put put) {
     d->yoff[j] = t.yoff[j];
   }
   for (int r = 0; r < kRounds; ++r) d->nrank[r] = t.nrank[r];
+  // the CG table padded to whole 16-byte chunks (the descriptor kernel stages it with 16-byte
+  // asynchronous copies)
+  std::vector<double> cg64(t.cg);
+  cg64.resize((cg64.size() + 1) / 2 * 2, 0.0);
   std::vector<float> cg32(t.cg.begin(), t.cg.end());
+  cg32.resize((cg32.size() + 3) / 4 * 4, 0.0f);
   std::vector<RecEntry32> r32;
   std::vector<RecEntry64> r64;
   pack_recursion(t, &r32, &r64);
@@ -193,7 +198,7 @@ cudaError_t fill_dev_tables(const Bso4Tables& t, DevTables* d, Put put) {
   if (e == cudaSuccess) e = put(t.rowk, &d->rowk);
   if (e == cudaSuccess) e = put(t.rank_slot, &d->rank_slot);
   if (e == cudaSuccess) e = put(t.tiles, &d->tiles);
-  if (e == cudaSuccess) e = put(t.cg, &d->cg64);
+  if (e == cudaSuccess) e = put(cg64, &d->cg64);
   if (e == cudaSuccess) e = put(cg32, &d->cg32);
   if (e == cudaSuccess) e = put(t.expand, &d->expand);
   if (e == cudaSuccess) e = put(t.half_diag, &d->half_diag);
