@@ -686,7 +686,12 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
         // triple's only row, so no two items write the same element
         T* dB1 = dBs + (size_t)3 * kNB * K;
         T* dB2 = dB1 + (size_t)3 * kNB * tb.nrank[1];
-        for (int it = tid; it < tb.NTILE * ncolt; it += nth) {
+        const int nitem = tb.NTILE * ncolt;
+        for (int k = 0; k * nth < nitem; ++k) {
+          // rounds alternate direction, so the threads with the heaviest items of one round take
+          // the lightest of the next (items are ordered heaviest layers first)
+          const int it = (k & 1) ? (k + 1) * nth - 1 - tid : k * nth + tid;
+          if (it >= nitem) continue;
           const int tix = it / ncolt;
           const int tile = stile[tix];
           const int ct = it - tix * ncolt;
