@@ -12,8 +12,9 @@
 // full-layer sums fold into weighted sums over the half.  The recursions run on lane groups:
 // in phase 1 of 16, 8, 6 or 4 lanes per neighbour (the widest that covers the atom's neighbours
 // in the fewest passes), each group writing its neighbour's U to a store that is summed in
-// group order; in phase 3 of 16 lanes; phase 2 follows a host-balanced schedule of rounds of 32
-// terms of one inner extent per warp, each distinct Z computation evaluated once.
+// group order; in phase 3 of 16 lanes (a warp for a last chunk of at most 8 neighbours);
+// phase 2 follows a host-balanced schedule of rounds of 32 terms of one inner extent per warp,
+// each distinct Z computation evaluated once.
 //
 // Every floating-point sum has a fixed order: c is summed over the groups' U in group order,
 // pass after pass, Z terms land in a term buffer from which the Y slots and B are summed, and the
@@ -275,7 +276,8 @@ struct KernelArgs {
 };
 
 constexpr int kNW = 8;                  // warps per CTA (== kZWarps)
-constexpr int kG = 16;                  // lanes per neighbour in the U/dU recursion (phase 3)
+constexpr int kG = 16;                  // lanes per neighbour in the U/dU recursion (phase 3; a last
+                                        // chunk of at most kNW neighbours takes a warp each)
 constexpr int kNG = kNW * 32 / kG;      // lane groups per CTA in phase 3
 constexpr int kNB = kNG;                // neighbours per phase-3 chunk (one per group)
 // lanes per neighbour in the U recursion of phase 1: 16, 8, 6 or 4 per atom (16 to 64
@@ -418,6 +420,7 @@ __device__ __forceinline__ void phase1_c(const KernelArgs<T>& args, const typena
     for (int e = tid; e < nch * HU; e += kNW * 32) {
       const int ch = e / HU, h = e - ch * HU;
       cx<T> acc = pass == 0 ? cx<T>{T(0), T(0)} : chalf[e];
+#pragma unroll 4
       for (int q = 0; q < ngact; ++q) {
         const T w = fcw[q * nch + ch];
         const cx<T> u = Ust[(size_t)q * HU + h];
@@ -492,7 +495,6 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
   const T rcut = (T)args.p.rcut, inv_r0 = (T)args.p.inv_r0;
   const bool eval = args.ev.pair != nullptr;
   const bool need_d = eval || args.dBout != nullptr;
-  const int grp = tid / kG, sl = tid % kG;
 
   // thread 0 takes the next queue position while the current atom runs; it publishes it at the
   // top of the loop, after at least one barrier that follows every thread's read of the last one
@@ -631,13 +633,15 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
     }
     if (!need_d || nn == 0) continue;
 
-    // ---------------- phase 3: dB per neighbour chunk ----------------------------------------
-    const int nchunk = (nn + kNB - 1) / kNB;
-    const int csz = (nn + nchunk - 1) / nchunk;  // balanced chunk size <= kNB
+    // ---------------- phase 3: dB per neighbour chunk (kNB neighbours, the last one the rest) -
     cx<T>* ubuf3 = reinterpret_cast<cx<T>*>(W);
     T* dBs = reinterpret_cast<T*>(W);  // 3*kNB*K [col][k], after the recursion of the chunk
-    for (int base = 0; base < nn; base += csz) {
-      const int nb_here = min(csz, nn - base);
+    for (int base = 0; base < nn; base += kNB) {
+      const int nb_here = min(kNB, nn - base);
+      // lanes per neighbour in the recursion: a whole warp when the chunk (the last one) has no
+      // more neighbours than warps, else kG
+      const bool wide = nb_here <= kNW;
+      const int grp = wide ? warp : tid / kG, sl = wide ? lane : tid % kG;
       {
         const int n = grp;  // one neighbour per group
         const bool active = n < nb_here;
@@ -673,8 +677,12 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
           }
         }
         if (eval && sl < 9) pacc[min(n, kNB - 1) * 9 + sl] = 0.0;
-        group_recursion<T, kG>(g, srec, J, shoff, ubuf3 + (size_t)grp * 2 * LH, LH,
-                               V + (size_t)min(n, kNB - 1) * 3 * HU, HU, sl, active);
+        if (wide)
+          group_recursion<T, 32>(g, srec, J, shoff, ubuf3 + (size_t)grp * 2 * LH, LH,
+                                 V + (size_t)min(n, kNB - 1) * 3 * HU, HU, sl, active);
+        else
+          group_recursion<T, kG>(g, srec, J, shoff, ubuf3 + (size_t)grp * 2 * LH, LH,
+                                 V + (size_t)min(n, kNB - 1) * 3 * HU, HU, sl, active);
       }
       __syncthreads();  // V of the chunk complete; the recursion buffers become dBs
       const int ncols = 3 * nb_here;
