@@ -161,6 +161,41 @@ __device__ __forceinline__ void nbr_geometry(T x0, T x1, T x2, T rcut, T inv_r0,
   for (int a = 0; a < 3; ++a) g->dfr[a] = dfc * drr[a];
 }
 
+// Geometry record of a neighbour in shared memory, written in phase 1 and read back in phase 3:
+// zp, xp, dzp[3], dxp[3] as (x, y) pairs, then fc and dfr[3] (kGeo values, a multiple of 4 so
+// that records stay 16-byte aligned).
+constexpr int kGeo = 20;
+
+template <typename T>
+__device__ __forceinline__ void put_geo(const NbrGeom<T>& g, T* r) {
+  r[0] = g.zp.x;
+  r[1] = g.zp.y;
+  r[2] = g.xp.x;
+  r[3] = g.xp.y;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    r[4 + 2 * a] = g.dzp[a].x;
+    r[5 + 2 * a] = g.dzp[a].y;
+    r[10 + 2 * a] = g.dxp[a].x;
+    r[11 + 2 * a] = g.dxp[a].y;
+    r[17 + a] = g.dfr[a];
+  }
+  r[16] = g.fc;
+}
+
+template <typename T>
+__device__ __forceinline__ void get_geo(const T* r, NbrGeom<T>* g) {
+  g->zp = {r[0], r[1]};
+  g->xp = {r[2], r[3]};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    g->dzp[a] = {r[4 + 2 * a], r[5 + 2 * a]};
+    g->dxp[a] = {r[10 + 2 * a], r[11 + 2 * a]};
+    g->dfr[a] = r[17 + a];
+  }
+  g->fc = r[16];
+}
+
 // U/dU layer recursion of one neighbour by a group of G lanes (sl = lane within the group) on
 // half layers (phase 3); rec and hoff live in shared memory.  vecall is written to V[a*HU + h]:
 // dU of layer j-1 stays raw in V until layer j is formed, then is converted.  Every group of the
@@ -269,6 +304,7 @@ struct KernelArgs {
   // when it does not fit in shared memory next to the rest (FP64 with several channels)
   void* yglobal;
   int g1;  // narrowest lane groups per neighbour in phase 1 (4, 6, 8 or 16) the U store allows
+  int geo_cap;  // neighbours whose phase-1 geometry records are kept for phase 3 (the rest recompute)
   // outputs: B (A x nch*K) and w_ch * dB (P x 3 x nch*K); or evaluation (ev.pair != nullptr)
   T* Bout;
   T* dBout;
@@ -292,8 +328,9 @@ static_assert(kNW == kZWarps, "phase-2 schedule is built for the CTA's warps");
 //   W region (phase 2: CG coefficients; phase 3: recursion buffers, then the chunk's dB by rank:
 //   rank 0 [cols][K], rank 1 [cols][nrank1], rank 2 [cols][nrank2])
 //   Bk[nch*K]  nwt[nch*NB]  nuu[NB*4]  nidx[NB]  pacc[NB*9] (FP64)  next atom
+//   geo[geo_cap*kGeo] (geometry records of the atom's first geo_cap neighbours)
 struct SmemPlan {
-  size_t rec, hoff, rowk, tiles, rslot, cfull, Y, V, W, Bk, nwt, nuu, nidx, pacc, next, total;
+  size_t rec, hoff, rowk, tiles, rslot, cfull, Y, V, W, Bk, nwt, nuu, nidx, pacc, next, geo, total;
 };
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -301,13 +338,14 @@ __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15
 // lane groups per CTA in phase 1 for g1 lanes per neighbour (whole groups per warp)
 __host__ __device__ constexpr int phase1_groups(int g1) { return kNW * (32 / g1); }
 
-__host__ __device__ inline SmemPlan smem_plan(const DevTables& tb, int nch, int eb, bool y_in_smem, int g1 = 16) {
+__host__ __device__ inline SmemPlan smem_plan(const DevTables& tb, int nch, int eb, bool y_in_smem, int g1 = 16,
+                                              int geo_cap = 0) {
   const int ng1 = phase1_groups(g1);
   const size_t LH = tb.hoff[tb.J + 1] - tb.hoff[tb.J];
   const size_t cxb = 2 * (size_t)eb;
   const size_t recb = eb == 8 ? sizeof(RecEntry64) : sizeof(RecEntry32);
   // phase 1: U of every group's neighbour (all half layers), the groups' f_c w_ch, c so far
-  const size_t v1 = (size_t)ng1 * tb.HU + ((size_t)ng1 * nch + 1) / 2 + (size_t)nch * tb.HU;
+  const size_t v1 = (size_t)ng1 * (tb.HU + 15) + ((size_t)ng1 * nch + 1) / 2 + (size_t)nch * tb.HU;
   const size_t v2 = (size_t)tb.NZT;                                      // phase 2
   const size_t v3 = (size_t)kNB * 3 * tb.HU;                             // phase 3
   const size_t vblock = v1 > v2 ? (v1 > v3 ? v1 : v3) : (v2 > v3 ? v2 : v3);
@@ -332,6 +370,7 @@ __host__ __device__ inline SmemPlan smem_plan(const DevTables& tb, int nch, int 
   s.nidx = o;  o = al16(o + sizeof(int) * kNB);
   s.pacc = o;  o = al16(o + sizeof(double) * kNB * 9);
   s.next = o;  o = al16(o + sizeof(int) * (4 + 3 * kMaxJ + 4 + kRounds));
+  s.geo = o;   o = al16(o + (size_t)eb * kGeo * geo_cap);
   s.total = o;
   return s;
 }
@@ -370,12 +409,14 @@ __device__ __forceinline__ void pair_u(const KernelArgs<T>& args, size_t q, T* x
 template <typename T, int G>
 __device__ __forceinline__ void phase1_c(const KernelArgs<T>& args, const typename RecEntry<T>::type* __restrict__ srec,
                                          const int* __restrict__ shoff, cx<T>* Ust, T* fcw, cx<T>* chalf,
-                                         const int8_t* __restrict__ half_diag, int nn, int p0, int ti, T rcut, T inv_r0,
-                                         int J, int HU, int nch, int warp, int lane, int tid) {
+                                         const int8_t* __restrict__ half_diag, T* sgeo, int nn, int p0, int ti, T rcut,
+                                         T inv_r0, int J, int HU, int nch, int warp, int lane, int tid) {
   constexpr int NGW = 32 / G, NG = kNW * NGW;
   const int gw = lane / G, sl = lane - (lane / G) * G;
   const int grp = warp * NGW + gw;
-  cx<T>* ug = Ust + (size_t)(gw < NGW ? grp : 0) * HU;
+  // group stride HS = G (mod 16): the 2G words of the groups of a warp fall on distinct banks
+  const int HS = HU + ((G - HU % 16) + 16) % 16;
+  cx<T>* ug = Ust + (size_t)(gw < NGW ? grp : 0) * HS;
   const int npass = (nn + NG - 1) / NG;
   for (int pass = 0; pass < npass; ++pass) {
     const int n = pass * NG + grp;
@@ -393,6 +434,7 @@ __device__ __forceinline__ void phase1_c(const KernelArgs<T>& args, const typena
 #pragma unroll
         for (int ch = 0; ch < kMaxCh; ++ch)
           if (ch < nch) fcw[grp * nch + ch] = g.fc * args.chw[ch * args.p.ntypes + tn];
+        if (n < args.geo_cap) put_geo(g, sgeo + (size_t)n * kGeo);
       }
     }
     __syncwarp();
@@ -423,7 +465,7 @@ __device__ __forceinline__ void phase1_c(const KernelArgs<T>& args, const typena
 #pragma unroll 4
       for (int q = 0; q < ngact; ++q) {
         const T w = fcw[q * nch + ch];
-        const cx<T> u = Ust[(size_t)q * HU + h];
+        const cx<T> u = Ust[(size_t)q * HS + h];
         acc.x = fma(w, u.x, acc.x);
         acc.y = fma(w, u.y, acc.y);
       }
@@ -453,7 +495,7 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int nth = kNW * 32;
   const int LH = tb.hoff[J + 1] - tb.hoff[J];  // largest half layer
-  const SmemPlan sp = smem_plan(tb, nch, (int)sizeof(T), kYShared, args.g1);
+  const SmemPlan sp = smem_plan(tb, nch, (int)sizeof(T), kYShared, args.g1, args.geo_cap);
 
   Rec* srec = reinterpret_cast<Rec*>(smem_raw + sp.rec);
   int* shoff = reinterpret_cast<int*>(smem_raw + sp.hoff);
@@ -466,8 +508,8 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
   cx<T>* V = reinterpret_cast<cx<T>*>(smem_raw + sp.V);
   // phase 1 in V: the U store of the groups (as many as args.g1 gives), their f_c w_ch, c
   cx<T>* p1u = V;
-  T* p1w = reinterpret_cast<T*>(V + (size_t)phase1_groups(args.g1) * HU);
-  cx<T>* p1c = V + (size_t)phase1_groups(args.g1) * HU + ((size_t)phase1_groups(args.g1) * nch + 1) / 2;
+  T* p1w = reinterpret_cast<T*>(V + (size_t)phase1_groups(args.g1) * (HU + 15));
+  cx<T>* p1c = V + (size_t)phase1_groups(args.g1) * (HU + 15) + ((size_t)phase1_groups(args.g1) * nch + 1) / 2;
   unsigned char* W = smem_raw + sp.W;
   T* scg = reinterpret_cast<T*>(W);  // phase 2 only (restaged per atom)
   T* Bk = reinterpret_cast<T*>(smem_raw + sp.Bk);
@@ -476,6 +518,7 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
   int* nidx = reinterpret_cast<int*>(smem_raw + sp.nidx);
   double* pacc = reinterpret_cast<double*>(smem_raw + sp.pacc);
   int* snext = reinterpret_cast<int*>(smem_raw + sp.next);
+  T* sgeo = reinterpret_cast<T*>(smem_raw + sp.geo);
 
   // tables, once per CTA; Y zeroed once (its padding rows are never written)
   for (int e = tid; e < HU; e += nth) srec[e] = args.rec[e];
@@ -534,10 +577,10 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
           break;
         }
       switch (g1) {
-        case 16: phase1_c<T, 16>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
-        case 8: phase1_c<T, 8>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
-        case 6: phase1_c<T, 6>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
-        default: phase1_c<T, 4>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
+        case 16: phase1_c<T, 16>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, sgeo, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
+        case 8: phase1_c<T, 8>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, sgeo, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
+        case 6: phase1_c<T, 6>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, sgeo, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
+        default: phase1_c<T, 4>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, sgeo, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
       }
     }
     // expansion to full layers
@@ -608,11 +651,21 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
         const int per = (i1 - i0 + 3) >> 2;
         const int a0 = i0 + sub * per, a1 = min(i1, a0 + per);
         T b = T(0);
-        for (int i = a0; i < a1; ++i) {
-          const BkItem it = tb.bk_items[i];
-          const cx<T> cv = cc[it.ufull];
-          const cx<T> z = tbuf[it.term];
-          b = fma((T)it.wgt, cv.x * z.x + cv.y * z.y, b);  // w * Re(conj(c) ZA)
+        for (int i0 = a0; i0 < a1; i0 += 4) {  // items loaded four at a time
+          uint2 q[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            q[u] = i0 + u < a1 ? __ldg(reinterpret_cast<const uint2*>(tb.bk_items) + i0 + u) : make_uint2(0u, 0u);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            if (i0 + u < a1) {
+              BkItem it;
+              *reinterpret_cast<uint2*>(&it) = q[u];
+              const cx<T> cv = cc[it.ufull];
+              const cx<T> z = tbuf[it.term];
+              b = fma((T)it.wgt, cv.x * z.x + cv.y * z.y, b);  // w * Re(conj(c) ZA)
+            }
+          }
         }
         bpart[sub * K + k] = b;
       }
@@ -650,10 +703,14 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
           const size_t q = (size_t)(p0 + base + n);
           const int nbi = args.nbr_idx[q];
           const int tn = args.types[nbi];
-          const T rin = args.p.has_rin ? args.rin[ti * args.p.ntypes + tn] : T(0);
-          T x[3];
-          pair_u<T>(args, q, x);
-          nbr_geometry<T>(x[0], x[1], x[2], rcut, inv_r0, rin, args.rin_w, &g);
+          if (base + n < args.geo_cap) {  // phase 1 kept the record
+            get_geo(sgeo + (size_t)(base + n) * kGeo, &g);
+          } else {
+            const T rin = args.p.has_rin ? args.rin[ti * args.p.ntypes + tn] : T(0);
+            T x[3];
+            pair_u<T>(args, q, x);
+            nbr_geometry<T>(x[0], x[1], x[2], rcut, inv_r0, rin, args.rin_w, &g);
+          }
           if (sl == 0) {
             for (int ch = 0; ch < nch; ++ch) nwt[ch * kNB + n] = args.chw[ch * args.p.ntypes + tn];
             nidx[n] = nbi;
@@ -880,6 +937,18 @@ cudaError_t launch_bso4(const DevTables& tb, const DevBatch& b, const BsoParams&
     }
   }
   if (smem > (size_t)max_optin_smem()) return cudaErrorInvalidConfiguration;
+  // geometry records for the first geo_cap neighbours of an atom (at most 128), as many as keep
+  // the resident CTAs per SM as they are.  The count depends on the configuration only, not on
+  // the batch, so that an atom's results do not depend on the batch it is evaluated in.
+  a.geo_cap = 0;
+  for (int cap = 128; cap > 0; cap -= 8) {
+    const size_t sc = smem_plan(tb, p.nch, sizeof(T), y_in_smem, a.g1, cap).total;
+    if (sc <= (size_t)max_optin_smem() && per_sm / (sc + 1024) >= per_sm / (smem + 1024)) {
+      a.geo_cap = cap;
+      smem = sc;
+      break;
+    }
+  }
   a.yglobal = nullptr;
   auto kern = sh.col_tile == 2 ? (y_in_smem ? k_bso4<T, true, 2> : k_bso4<T, false, 2>)
                                : (y_in_smem ? k_bso4<T, true, 4> : k_bso4<T, false, 4>);
