@@ -330,7 +330,7 @@ static_assert(kNW == kZWarps, "phase-2 schedule is built for the CTA's warps");
 //   Bk[nch*K]  nwt[nch*NB]  nuu[NB*4]  nidx[NB]  pacc[NB*9] (FP64)  next atom
 //   geo[geo_cap*kGeo] (geometry records of the atom's first geo_cap neighbours)
 struct SmemPlan {
-  size_t rec, hoff, rowk, tiles, rslot, cfull, Y, V, W, Bk, nwt, nuu, nidx, pacc, next, geo, total;
+  size_t rec, hoff, rowk, tiles, rslot, cfull, Y, V, W, Bk, nwt, nuu, nidx, pacc, next, sc, geo, total;
 };
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -370,6 +370,7 @@ __host__ __device__ inline SmemPlan smem_plan(const DevTables& tb, int nch, int 
   s.nidx = o;  o = al16(o + sizeof(int) * kNB);
   s.pacc = o;  o = al16(o + sizeof(double) * kNB * 9);
   s.next = o;  o = al16(o + sizeof(int) * (4 + 3 * kMaxJ + 4 + kRounds));
+  s.sc = o;    o = al16(o + (size_t)eb * 256);
   s.geo = o;   o = al16(o + (size_t)eb * kGeo * geo_cap);
   s.total = o;
   return s;
@@ -519,6 +520,7 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
   double* pacc = reinterpret_cast<double*>(smem_raw + sp.pacc);
   int* snext = reinterpret_cast<int*>(smem_raw + sp.next);
   T* sgeo = reinterpret_cast<T*>(smem_raw + sp.geo);
+  T* ssc = reinterpret_cast<T*>(smem_raw + sp.sc);  // ssc[16 n + d] = n / d, the Y-slot scales
 
   // tables, once per CTA; Y zeroed once (its padding rows are never written)
   for (int e = tid; e < HU; e += nth) srec[e] = args.rec[e];
@@ -534,6 +536,7 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
   for (int e = tid; e < tb.NTILE; e += nth) stile[e] = tb.tiles[e];
   for (int e = tid; e < (kRounds - 1) * K; e += nth) srslot[e] = tb.rank_slot[e];
   for (int e = tid; e < nch * NYP; e += nth) Y[e] = {T(0), T(0)};
+  for (int e = tid; e < 256; e += nth) ssc[e] = (e & 15) ? (T)(e >> 4) / (T)(e & 15) : T(0);
 
   const T rcut = (T)args.p.rcut, inv_r0 = (T)args.p.inv_r0;
   const bool eval = args.ev.pair != nullptr;
@@ -635,7 +638,7 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
         if (e + nth < tb.NS) nse = __ldg(reinterpret_cast<const uint4*>(tb.slots) + e + nth);
         cx<T> v = {T(0), T(0)};
         for (int t = 0; t < se.nterm; ++t) {
-          const T sc = (T)se.snum[t] / (T)se.sden[t];
+          const T sc = ssc[se.snum[t] * 16 + se.sden[t]];
           const cx<T> z = tbuf[se.term[t]];
           v.x = fma(sc, z.x, v.x);
           v.y = fma(sc, z.y, v.y);

@@ -63,6 +63,9 @@ struct SlotEntry {
   uint8_t snum[3], sden[3];
 };
 static_assert(sizeof(SlotEntry) == 16, "slot entries are 16 bytes");
+// snum and sden are doubled angular momenta + 1 <= kMaxJ + 1; the descriptor kernel looks
+// snum / sden up in a 16 x 16 table
+static_assert(kMaxJ + 1 < 16, "slot scales index a 16 x 16 table");
 
 // One ZA half entry of a triple: B_k = sum over its entries of wgt * Re(conj(c[ufull]) Z[term]).
 struct BkItem {
