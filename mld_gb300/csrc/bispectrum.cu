@@ -328,9 +328,10 @@ static_assert(kNW == kZWarps, "phase-2 schedule is built for the CTA's warps");
 //   W region (phase 2: CG coefficients; phase 3: recursion buffers, then the chunk's dB by rank:
 //   rank 0 [cols][K], rank 1 [cols][nrank1], rank 2 [cols][nrank2])
 //   Bk[nch*K]  nwt[nch*NB]  nuu[NB*4]  nidx[NB]  pacc[NB*9] (FP64)  next atom
+//   sc[256] (Y-slot scales)  expand[NU]  half_diag[HU]  bk_off[K+1] (tables staged once per CTA)
 //   geo[geo_cap*kGeo] (geometry records of the atom's first geo_cap neighbours)
 struct SmemPlan {
-  size_t rec, hoff, rowk, tiles, rslot, cfull, Y, V, W, Bk, nwt, nuu, nidx, pacc, next, sc, geo, total;
+  size_t rec, hoff, rowk, tiles, rslot, cfull, Y, V, W, Bk, nwt, nuu, nidx, pacc, next, sc, exp, hd, bko, geo, total;
 };
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -371,6 +372,9 @@ __host__ __device__ inline SmemPlan smem_plan(const DevTables& tb, int nch, int 
   s.pacc = o;  o = al16(o + sizeof(double) * kNB * 9);
   s.next = o;  o = al16(o + sizeof(int) * (4 + 3 * kMaxJ + 4 + kRounds));
   s.sc = o;    o = al16(o + (size_t)eb * 256);
+  s.exp = o;   o = al16(o + sizeof(int16_t) * tb.NU);
+  s.hd = o;    o = al16(o + tb.HU);
+  s.bko = o;   o = al16(o + sizeof(int) * (tb.K + 1));
   s.geo = o;   o = al16(o + (size_t)eb * kGeo * geo_cap);
   s.total = o;
   return s;
@@ -537,6 +541,13 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
   for (int e = tid; e < (kRounds - 1) * K; e += nth) srslot[e] = tb.rank_slot[e];
   for (int e = tid; e < nch * NYP; e += nth) Y[e] = {T(0), T(0)};
   for (int e = tid; e < 256; e += nth) ssc[e] = (e & 15) ? (T)(e >> 4) / (T)(e & 15) : T(0);
+  int16_t* sexp = reinterpret_cast<int16_t*>(smem_raw + sp.exp);
+  int8_t* shd = reinterpret_cast<int8_t*>(smem_raw + sp.hd);
+  int* sbko = reinterpret_cast<int*>(smem_raw + sp.bko);
+  for (int e = tid; e < NU; e += nth) sexp[e] = tb.expand[e];
+  for (int e = tid; e < HU; e += nth) shd[e] = tb.half_diag[e];
+  for (int e = tid; e <= K; e += nth) sbko[e] = tb.bk_off[e];
+  const int zr0 = tb.zitem_off[warp], zr1 = tb.zitem_off[warp + 1];  // this warp's Z rounds
 
   const T rcut = (T)args.p.rcut, inv_r0 = (T)args.p.inv_r0;
   const bool eval = args.ev.pair != nullptr;
@@ -580,16 +591,16 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
           break;
         }
       switch (g1) {
-        case 16: phase1_c<T, 16>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, sgeo, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
-        case 8: phase1_c<T, 8>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, sgeo, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
-        case 6: phase1_c<T, 6>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, sgeo, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
-        default: phase1_c<T, 4>(args, srec, shoff, p1u, p1w, p1c, tb.half_diag, sgeo, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
+        case 16: phase1_c<T, 16>(args, srec, shoff, p1u, p1w, p1c, shd, sgeo, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
+        case 8: phase1_c<T, 8>(args, srec, shoff, p1u, p1w, p1c, shd, sgeo, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
+        case 6: phase1_c<T, 6>(args, srec, shoff, p1u, p1w, p1c, shd, sgeo, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
+        default: phase1_c<T, 4>(args, srec, shoff, p1u, p1w, p1c, shd, sgeo, nn, p0, ti, rcut, inv_r0, J, HU, nch, warp, lane, tid); break;
       }
     }
     // expansion to full layers
     for (int e = tid; e < nch * NU; e += nth) {
       const int ch = e / NU, f = e - ch * NU;
-      cfull[e] = fetch(p1c + ch * HU, tb.expand[f]);
+      cfull[e] = fetch(p1c + ch * HU, sexp[f]);
     }
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
@@ -602,7 +613,7 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
     for (int ch = 0; ch < nch; ++ch) {
       const cx<T>* cc = cfull + ch * NU;
       {
-        const int r0 = tb.zitem_off[warp], r1 = tb.zitem_off[warp + 1];
+        const int r0 = zr0, r1 = zr1;
         ZItem n1{}, n2{};
         if (r0 < r1) n1 = load_zitem<T>(tb.zitems + (size_t)r0 * 32 + lane);
         if (r0 + 1 < r1) n2 = load_zitem<T>(tb.zitems + (size_t)(r0 + 1) * 32 + lane);
@@ -650,7 +661,7 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
       T* bpart = reinterpret_cast<T*>(W + al16((size_t)tb.NCG * sizeof(T)));  // [4][K]
       for (int t2 = nth - 1 - tid; t2 < 4 * K; t2 += nth) {
         const int k = t2 >> 2, sub = t2 & 3;
-        const int i0 = tb.bk_off[k], i1 = tb.bk_off[k + 1];
+        const int i0 = sbko[k], i1 = sbko[k + 1];
         const int per = (i1 - i0 + 3) >> 2;
         const int a0 = i0 + sub * per, a1 = min(i1, a0 + per);
         T b = T(0);
