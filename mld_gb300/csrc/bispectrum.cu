@@ -220,11 +220,11 @@ __device__ __forceinline__ void group_recursion(const NbrGeom<T>& g, const typen
       for (int e = sl; e < ne; e += G) {
         const int idx = h0 + e;
         const auto r = rec[idx];
-        const T tz = (T)r.tz, tx = (T)r.tx;
+        const T tzq = (T)r.tz, txq = (T)r.tx;  // tz, tx signed by q: Z = zp or conj(zp), X = conj(xp) or xp
+        const T tz = fabs(tzq), tx = fabs(txq);
         const int sz = r.sz, sx = r.sx;
-        const T sq = r.qneg != 0 ? T(1) : T(-1);  // Z = zp or conj(zp), X = conj(xp) or xp
-        const cx<T> A = {tz * g.zp.x, tz * (sq * g.zp.y)};
-        const cx<T> Bc = {-tx * (sq * g.xp.y), -tx * g.xp.x};  // -i*tx*X
+        const cx<T> A = {tz * g.zp.x, tzq * g.zp.y};
+        const cx<T> Bc = {-txq * g.xp.y, -tx * g.xp.x};  // -i*tx*X
         cx<T> u = {T(0), T(0)};
         cx<T> du[3] = {{T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}};
         if (sz >= 0) {
@@ -232,7 +232,7 @@ __device__ __forceinline__ void group_recursion(const NbrGeom<T>& g, const typen
           u = cmul(A, Uz);
 #pragma unroll
           for (int a = 0; a < 3; ++a) {
-            du[a] = cfma(A, fetch(V + a * HU + pbase, sz), cmul(cx<T>{tz * g.dzp[a].x, tz * (sq * g.dzp[a].y)}, Uz));
+            du[a] = cfma(A, fetch(V + a * HU + pbase, sz), cmul(cx<T>{tz * g.dzp[a].x, tzq * g.dzp[a].y}, Uz));
           }
         }
         if (sx >= 0) {
@@ -240,7 +240,7 @@ __device__ __forceinline__ void group_recursion(const NbrGeom<T>& g, const typen
           u = cfma(Bc, Ux, u);
 #pragma unroll
           for (int a = 0; a < 3; ++a) {
-            du[a] = cfma(Bc, fetch(V + a * HU + pbase, sx), cfma(cx<T>{-tx * (sq * g.dxp[a].y), -tx * g.dxp[a].x}, Ux, du[a]));
+            du[a] = cfma(Bc, fetch(V + a * HU + pbase, sx), cfma(cx<T>{-txq * g.dxp[a].y, -tx * g.dxp[a].x}, Ux, du[a]));
           }
         }
 #pragma unroll
@@ -449,10 +449,10 @@ __device__ __forceinline__ void phase1_c(const KernelArgs<T>& args, const typena
       if (active) {
         for (int e = sl; e < ne; e += G) {
           const auto r = srec[h0 + e];
-          const T tz = (T)r.tz, tx = (T)r.tx;
-          const T sq = r.qneg != 0 ? T(1) : T(-1);  // Z = zp or conj(zp), X = conj(xp) or xp
-          const cx<T> A = {tz * g.zp.x, tz * (sq * g.zp.y)};
-          const cx<T> Bc = {-tx * (sq * g.xp.y), -tx * g.xp.x};  // -i*tx*X
+          const T tzq = (T)r.tz, txq = (T)r.tx;  // tz, tx signed by q: Z = zp or conj(zp), X = conj(xp) or xp
+          const T tz = fabs(tzq), tx = fabs(txq);
+          const cx<T> A = {tz * g.zp.x, tzq * g.zp.y};
+          const cx<T> Bc = {-txq * g.xp.y, -tx * g.xp.x};  // -i*tx*X
           cx<T> u = {T(0), T(0)};
           if (r.sz >= 0) u = cmul(A, fetch(prev, r.sz));
           if (r.sx >= 0) u = cfma(Bc, fetch(prev, r.sx), u);

@@ -74,7 +74,9 @@ struct BkItem {
 };
 static_assert(sizeof(BkItem) == 8, "B items are 8 bytes");
 
-// Packed per-entry recursion record of the half layers (one 16-byte load per entry).
+// Packed per-entry recursion record of the half layers (one 16-byte load per entry).  tz and tx
+// (>= 0 in the tables) are stored with the sign that selects the entry's Z / conj(Z) and X
+// (+ for qneg != 0), so the kernel takes their magnitudes with fabs.
 struct RecEntry32 {
   float tz, tx;
   int16_t sz, sx;
@@ -159,8 +161,10 @@ inline void pack_recursion(const Bso4Tables& t, std::vector<RecEntry32>* r32, st
   r32->resize(t.HU);
   r64->resize(t.HU);
   for (int h = 0; h < t.HU; ++h) {
-    (*r32)[h] = RecEntry32{(float)t.rec_tz[h], (float)t.rec_tx[h], t.rec_sz[h], t.rec_sx[h], (int32_t)t.rec_qneg[h]};
-    (*r64)[h] = RecEntry64{t.rec_tz[h], t.rec_tx[h], t.rec_sz[h], t.rec_sx[h], (int32_t)t.rec_qneg[h], 0};
+    // tz, tx >= 0 carry the sign of the entry's q (+ for q >= 0), which selects Z / conj(Z) and X
+    const double sq = t.rec_qneg[h] ? 1.0 : -1.0;
+    (*r32)[h] = RecEntry32{(float)(sq * t.rec_tz[h]), (float)(sq * t.rec_tx[h]), t.rec_sz[h], t.rec_sx[h], (int32_t)t.rec_qneg[h]};
+    (*r64)[h] = RecEntry64{sq * t.rec_tz[h], sq * t.rec_tx[h], t.rec_sz[h], t.rec_sx[h], (int32_t)t.rec_qneg[h], 0};
   }
 }
 
