@@ -226,7 +226,7 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
 
   // layer-blocked Y: rows of layer j are the triples using layer j (any of l, l1, l2).  A
   // triple's distinct layers in ascending order have ranks 0, 1, 2; within a layer the rows are
-  // grouped by rank (each group padded to whole row tiles).  The dB contraction writes a row's
+  // grouped by rank, the layer padded to whole row tiles.  The dB contraction writes a row's
   // result into the buffer of its rank, where every triple has at most one row, so all tiles run
   // in one pass without atomics, and dB = (rank 0 + rank 1) + rank 2 in a fixed order.
   std::vector<std::vector<int>> rows(J + 1);  // row position -> triple (-1 padding)
@@ -254,10 +254,11 @@ bool build_bso4_tables(double j_max, Bso4Tables* t, std::string* err) {
           rowrank[j].push_back(r);
           if (r > 0) t->rank_slot[(size_t)k * (kRounds - 1) + r - 1] = (int16_t)t->nrank[r]++;
         }
-        while (rows[j].size() % kRowTile) {
-          rows[j].push_back(-1);
-          rowrank[j].push_back(0);
-        }
+      }
+    for (int j = 0; j <= J; ++j)
+      while (rows[j].size() % kRowTile) {
+        rows[j].push_back(-1);
+        rowrank[j].push_back(0);
       }
     t->nrank[0] = t->K;
   }
