@@ -648,11 +648,14 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
         *reinterpret_cast<uint4*>(&se) = nse;
         if (e + nth < tb.NS) nse = __ldg(reinterpret_cast<const uint4*>(tb.slots) + e + nth);
         cx<T> v = {T(0), T(0)};
-        for (int t = 0; t < se.nterm; ++t) {
-          const T sc = ssc[se.snum[t] * 16 + se.sden[t]];
-          const cx<T> z = tbuf[se.term[t]];
-          v.x = fma(sc, z.x, v.x);
-          v.y = fma(sc, z.y, v.y);
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {  // nterm <= 3
+          if (t < se.nterm) {
+            const T sc = ssc[se.snum[t] * 16 + se.sden[t]];
+            const cx<T> z = tbuf[se.term[t]];
+            v.x = fma(sc, z.x, v.x);
+            v.y = fma(sc, z.y, v.y);
+          }
         }
         Yc[se.ypos] = {(T)se.wgt * v.x, (T)se.wgt * v.y};
       }
