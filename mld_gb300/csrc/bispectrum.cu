@@ -59,15 +59,17 @@ __device__ __forceinline__ cx<T> fetch(const cx<T>* base, int code) {
 // One Z term: sum_a c1_a sum_b c2_b c[i1 + a s1 + b] c[i2 - a s2 - b] with NB = nb known at compile
 // time, so that the b loop unrolls and the term's NB coefficients c2 stay in registers.
 template <int NB, typename T>
-__device__ __forceinline__ cx<T> zterm(const cx<T>* __restrict__ cc, const T* __restrict__ cgs, const ZItem& zi) {
+__device__ __forceinline__ cx<T> zterm(const cx<T>* __restrict__ cc, const T* __restrict__ cgs, uint4 zi) {
+  // the item's 16 bytes: x = i1 | i2 << 16, y = cg1 | cg2 << 16, z = na | nb << 8 | s1 << 16 | s2 << 24
+  const int cg1 = zi.y & 0xFFFF, cg2 = zi.y >> 16, na = zi.z & 0xFF, s1 = (zi.z >> 16) & 0xFF, s2 = zi.z >> 24;
   T c2[NB];
 #pragma unroll
-  for (int b = 0; b < NB; ++b) c2[b] = cgs[zi.cg2 + b];
+  for (int b = 0; b < NB; ++b) c2[b] = cgs[cg2 + b];
   cx<T> zs = {T(0), T(0)};
-  int i1a = zi.i1, i2a = zi.i2;
+  int i1a = zi.x & 0xFFFF, i2a = zi.x >> 16;
 #pragma unroll (NB <= 2 ? 4 : (NB <= 5 ? 2 : 1))
-  for (int a = 0; a < zi.na; ++a) {
-    const T c1 = cgs[zi.cg1 + a];
+  for (int a = 0; a < na; ++a) {
+    const T c1 = cgs[cg1 + a];
     cx<T> part = {T(0), T(0)};
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
@@ -77,8 +79,8 @@ __device__ __forceinline__ cx<T> zterm(const cx<T>* __restrict__ cc, const T* __
     }
     zs.x = fma(c1, part.x, zs.x);
     zs.y = fma(c1, part.y, zs.y);
-    i1a += zi.s1;
-    i2a -= zi.s2;
+    i1a += s1;
+    i2a -= s2;
   }
   return zs;
 }
@@ -380,14 +382,6 @@ __host__ __device__ inline SmemPlan smem_plan(const DevTables& tb, int nch, int 
   return s;
 }
 
-template <typename T>
-__device__ __forceinline__ ZItem load_zitem(const ZItem* p) {
-  const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
-  ZItem z;
-  *reinterpret_cast<uint4*>(&z) = v;
-  return z;
-}
-
 // Displacement of pair q in T: the FP32 copy for T = float when present, else nbr_u.
 template <typename T>
 __device__ __forceinline__ void pair_u(const KernelArgs<T>& args, size_t q, T* x) {
@@ -614,15 +608,16 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
       const cx<T>* cc = cfull + ch * NU;
       {
         const int r0 = zr0, r1 = zr1;
-        ZItem n1{}, n2{};
-        if (r0 < r1) n1 = load_zitem<T>(tb.zitems + (size_t)r0 * 32 + lane);
-        if (r0 + 1 < r1) n2 = load_zitem<T>(tb.zitems + (size_t)(r0 + 1) * 32 + lane);
+        const uint4* zit = reinterpret_cast<const uint4*>(tb.zitems);
+        uint4 n1 = make_uint4(0u, 0u, 0u, 0u), n2 = n1;
+        if (r0 < r1) n1 = __ldg(zit + (size_t)r0 * 32 + lane);
+        if (r0 + 1 < r1) n2 = __ldg(zit + (size_t)(r0 + 1) * 32 + lane);
         for (int r = r0; r < r1; ++r) {
-          const ZItem zi = n1;
+          const uint4 zi = n1;
           n1 = n2;
-          if (r + 2 < r1) n2 = load_zitem<T>(tb.zitems + (size_t)(r + 2) * 32 + lane);
+          if (r + 2 < r1) n2 = __ldg(zit + (size_t)(r + 2) * 32 + lane);
           cx<T> zs;
-          switch (zi.nb) {  // uniform over the round
+          switch ((zi.z >> 8) & 0xFF) {  // nb, uniform over the round
             case 1: zs = zterm<1, T>(cc, scg, zi); break;
             case 2: zs = zterm<2, T>(cc, scg, zi); break;
             case 3: zs = zterm<3, T>(cc, scg, zi); break;
@@ -635,7 +630,7 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
             case 10: zs = zterm<10, T>(cc, scg, zi); break;
             default: zs = zterm<11, T>(cc, scg, zi); break;
           }
-          if (zi.term != kNoTerm) tbuf[zi.term] = zs;
+          if ((zi.w & 0xFFFF) != kNoTerm) tbuf[zi.w & 0xFFFF] = zs;
         }
       }
       __syncthreads();
@@ -644,20 +639,26 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
       uint4 nse = make_uint4(0u, 0u, 0u, 0u);
       if (tid < tb.NS) nse = __ldg(reinterpret_cast<const uint4*>(tb.slots) + tid);
       for (int e = tid; e < tb.NS; e += nth) {
-        SlotEntry se;
-        *reinterpret_cast<uint4*>(&se) = nse;
+        // the slot's 16 bytes: x = term0 | term1 << 16, y = term2 | ypos << 16,
+        // z = nterm | wgt << 8 | snum0 << 16 | snum1 << 24, w = snum2 | sden0 << 8 | sden1 << 16 | sden2 << 24
+        const uint4 se = nse;
         if (e + nth < tb.NS) nse = __ldg(reinterpret_cast<const uint4*>(tb.slots) + e + nth);
+        const int nterm = se.z & 0xFF;
+        const int terms[3] = {(int)(se.x & 0xFFFF), (int)(se.x >> 16), (int)(se.y & 0xFFFF)};
+        const int snum[3] = {(int)((se.z >> 16) & 0xFF), (int)(se.z >> 24), (int)(se.w & 0xFF)};
+        const int sden[3] = {(int)((se.w >> 8) & 0xFF), (int)((se.w >> 16) & 0xFF), (int)(se.w >> 24)};
         cx<T> v = {T(0), T(0)};
 #pragma unroll
         for (int t = 0; t < 3; ++t) {  // nterm <= 3
-          if (t < se.nterm) {
-            const T sc = ssc[se.snum[t] * 16 + se.sden[t]];
-            const cx<T> z = tbuf[se.term[t]];
+          if (t < nterm) {
+            const T sc = ssc[snum[t] * 16 + sden[t]];
+            const cx<T> z = tbuf[terms[t]];
             v.x = fma(sc, z.x, v.x);
             v.y = fma(sc, z.y, v.y);
           }
         }
-        Yc[se.ypos] = {(T)se.wgt * v.x, (T)se.wgt * v.y};
+        const T wgt = (T)((se.z >> 8) & 0xFF);
+        Yc[se.y >> 16] = {wgt * v.x, wgt * v.y};
       }
       // B_k in four fixed quarters of its items (threads from the top, which have fewer Y slots),
       // then ((q0 + q1) + q2) + q3
@@ -676,11 +677,10 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             if (i0 + u < a1) {
-              BkItem it;
-              *reinterpret_cast<uint2*>(&it) = q[u];
-              const cx<T> cv = cc[it.ufull];
-              const cx<T> z = tbuf[it.term];
-              b = fma((T)it.wgt, cv.x * z.x + cv.y * z.y, b);  // w * Re(conj(c) ZA)
+              // x = term | ufull << 16, y = wgt | pad << 8
+              const cx<T> cv = cc[q[u].x >> 16];
+              const cx<T> z = tbuf[q[u].x & 0xFFFF];
+              b = fma((T)(q[u].y & 0xFF), cv.x * z.x + cv.y * z.y, b);  // w * Re(conj(c) ZA)
             }
           }
         }

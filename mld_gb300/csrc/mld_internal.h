@@ -2,6 +2,8 @@
 // Nothing here is part of the public C ABI (include/mld_gpu.h).
 #pragma once
 #include <cuda_runtime.h>
+
+#include <cstddef>
 #include <stdint.h>
 #include <string>
 #include <vector>
@@ -53,6 +55,11 @@ struct alignas(16) ZItem {
   uint16_t pad;
 };
 static_assert(sizeof(ZItem) == 16, "phase-2 entries are 16 bytes");
+// the descriptor kernel decodes entries from their four 32-bit words at these byte offsets
+static_assert(offsetof(ZItem, i2) == 2 && offsetof(ZItem, cg1) == 4 && offsetof(ZItem, cg2) == 6 &&
+                  offsetof(ZItem, na) == 8 && offsetof(ZItem, nb) == 9 && offsetof(ZItem, s1) == 10 &&
+                  offsetof(ZItem, s2) == 11 && offsetof(ZItem, term) == 12,
+              "ZItem layout");
 constexpr uint16_t kNoTerm = 0xFFFF;
 
 // One folded Y slot for the kernel (16 bytes): Y[ypos] = wgt * sum_t (snum_t / sden_t) Z[term_t].
@@ -63,6 +70,9 @@ struct SlotEntry {
   uint8_t snum[3], sden[3];
 };
 static_assert(sizeof(SlotEntry) == 16, "slot entries are 16 bytes");
+static_assert(offsetof(SlotEntry, ypos) == 6 && offsetof(SlotEntry, nterm) == 8 && offsetof(SlotEntry, wgt) == 9 &&
+                  offsetof(SlotEntry, snum) == 10 && offsetof(SlotEntry, sden) == 13,
+              "SlotEntry layout (decoded from its words by the descriptor kernel)");
 // snum and sden are doubled angular momenta + 1 <= kMaxJ + 1; the descriptor kernel looks
 // snum / sden up in a 16 x 16 table
 static_assert(kMaxJ + 1 < 16, "slot scales index a 16 x 16 table");
@@ -73,6 +83,7 @@ struct BkItem {
   uint8_t wgt, pad[3];
 };
 static_assert(sizeof(BkItem) == 8, "B items are 8 bytes");
+static_assert(offsetof(BkItem, ufull) == 2 && offsetof(BkItem, wgt) == 4, "BkItem layout (decoded by the descriptor kernel)");
 
 // Packed per-entry recursion record of the half layers (one 16-byte load per entry).  tz and tx
 // (>= 0 in the tables) are stored with the sign that selects the entry's Z / conj(Z) and X
