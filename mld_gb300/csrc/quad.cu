@@ -72,9 +72,9 @@ constexpr int kQC = 16;   // contributors staged per pass when they do not all f
 // One CTA per atom: its 3 quadratic force rows (dedup layout, written at column offset qoff)
 // and its stress partials H[a][s][k].  The contributors (the atom itself, then each neighbour)
 // are staged qc at a time: all at once when 1 + nn <= qc, so that every triangle block reads
-// them without restaging.
+// them without restaging.  FP32: three resident CTAs per SM (registers capped at 80).
 template <typename T>
-__global__ void __launch_bounds__(256) k_quad_force(
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_quad_force(
     int A, int KK, const int* __restrict__ atom_struct, const int* __restrict__ atom_start,
     const int* __restrict__ nbr_off, const int* __restrict__ nbr_idx, const double* __restrict__ nbr_u,
     const int* __restrict__ rev, const int* __restrict__ small, double sign_big, const T* __restrict__ B,
