@@ -23,8 +23,10 @@
 // rank 2.  Results are therefore bitwise reproducible and do not depend on which CTA takes which
 // atom.
 //
-// CTAs are persistent: they stage the recursion records in shared memory once, then pull atoms
-// from a queue ordered by descending neighbour count (longest first).
+// CTAs are persistent: they stage the recursion records and the small tables in shared memory
+// once, then pull atoms from a queue (ordered by descending neighbour count, or in index order,
+// whichever the launch-shape autotuner found faster).  Each atom's phase-1 geometry records are
+// kept for phase 3.
 // T = double (plain FP64 method) or float (mixed method: FP32 descriptors).
 #include <cuda_runtime.h>
 
