@@ -165,10 +165,13 @@ __device__ __forceinline__ void nbr_geometry(T x0, T x1, T x2, T rcut, T inv_r0,
   for (int a = 0; a < 3; ++a) g->dfr[a] = dfc * drr[a];
 }
 
-// Geometry record of a neighbour in shared memory, written in phase 1 and read back in phase 3:
-// zp, xp, dzp[3], dxp[3] as (x, y) pairs, then fc and dfr[3] (kGeo values, a multiple of 4 so
-// that records stay 16-byte aligned).
-constexpr int kGeo = 20;
+// Record of a neighbour in shared memory, written in phase 1 and read back in phase 3: zp, xp,
+// dzp[3], dxp[3] as (x, y) pairs, then fc and dfr[3]; at kGeoIdx the neighbour's index and type
+// (two ints), at kGeoU its displacement and 1/r (kGeo values, a multiple of 4 so that records
+// stay 16-byte aligned).
+constexpr int kGeo = 28;
+constexpr int kGeoIdx = 20;
+constexpr int kGeoU = 22;
 
 template <typename T>
 __device__ __forceinline__ void put_geo(const NbrGeom<T>& g, T* r) {
@@ -384,15 +387,16 @@ __host__ __device__ inline SmemPlan smem_plan(const DevTables& tb, int nch, int 
   return s;
 }
 
-// Displacement of pair q in T: the FP32 copy for T = float when present, else nbr_u.
+// Displacement of pair q and 1/r in T (the values phase 3 uses for the stress lever arm).
 template <typename T>
-__device__ __forceinline__ void pair_u(const KernelArgs<T>& args, size_t q, T* x) {
+__device__ __forceinline__ void pair_u_rinv(const KernelArgs<T>& args, size_t q, T* x, T* rinv) {
   if constexpr (sizeof(T) == 4) {
     if (args.u32) {
       const float4 v = args.u32[q];
       x[0] = v.x;
       x[1] = v.y;
       x[2] = v.z;
+      *rinv = v.w;
       return;
     }
   }
@@ -400,6 +404,7 @@ __device__ __forceinline__ void pair_u(const KernelArgs<T>& args, size_t q, T* x
   x[0] = (T)u3[0];
   x[1] = (T)u3[1];
   x[2] = (T)u3[2];
+  *rinv = (T)(1.0 / sqrt(u3[0] * u3[0] + u3[1] * u3[1] + u3[2] * u3[2]));
 }
 
 // Phase 1 of one atom: c on half layers.  Lane groups of G lanes take one neighbour each
@@ -427,15 +432,24 @@ __device__ __forceinline__ void phase1_c(const KernelArgs<T>& args, const typena
       const int nb = args.nbr_idx[p0 + n];
       const int tn = args.types[nb];
       const T rin = args.p.has_rin ? args.rin[ti * args.p.ntypes + tn] : T(0);
-      T x[3];
-      pair_u<T>(args, (size_t)(p0 + n), x);
+      T x[3], rinv;
+      pair_u_rinv<T>(args, (size_t)(p0 + n), x, &rinv);
       nbr_geometry<T>(x[0], x[1], x[2], rcut, inv_r0, rin, args.rin_w, &g);
       if (sl == 0) {
         ug[0] = {T(1), T(0)};
 #pragma unroll
         for (int ch = 0; ch < kMaxCh; ++ch)
           if (ch < nch) fcw[grp * nch + ch] = g.fc * args.chw[ch * args.p.ntypes + tn];
-        if (n < args.geo_cap) put_geo(g, sgeo + (size_t)n * kGeo);
+        if (n < args.geo_cap) {
+          T* r = sgeo + (size_t)n * kGeo;
+          put_geo(g, r);
+          reinterpret_cast<int*>(r + kGeoIdx)[0] = nb;
+          reinterpret_cast<int*>(r + kGeoIdx)[1] = tn;
+          r[kGeoU + 0] = x[0];
+          r[kGeoU + 1] = x[1];
+          r[kGeoU + 2] = x[2];
+          r[kGeoU + 3] = rinv;
+        }
       }
     }
     __syncwarp();
@@ -720,36 +734,35 @@ __global__ void __launch_bounds__(kNW * 32, sizeof(T) == 4 ? 2 : 1) k_bso4(Kerne
         NbrGeom<T> g;
         if (active) {
           const size_t q = (size_t)(p0 + base + n);
-          const int nbi = args.nbr_idx[q];
-          const int tn = args.types[nbi];
-          if (base + n < args.geo_cap) {  // phase 1 kept the record
-            get_geo(sgeo + (size_t)(base + n) * kGeo, &g);
+          // neighbour index, type, displacement and 1/r: from phase 1's record (no global loads
+          // in front of the recursion), else from the lists
+          int nbi, tn;
+          T x[3], rinv;
+          if (base + n < args.geo_cap) {
+            const T* r = sgeo + (size_t)(base + n) * kGeo;
+            get_geo(r, &g);
+            nbi = reinterpret_cast<const int*>(r + kGeoIdx)[0];
+            tn = reinterpret_cast<const int*>(r + kGeoIdx)[1];
+            x[0] = r[kGeoU + 0];
+            x[1] = r[kGeoU + 1];
+            x[2] = r[kGeoU + 2];
+            rinv = r[kGeoU + 3];
           } else {
+            nbi = args.nbr_idx[q];
+            tn = args.types[nbi];
             const T rin = args.p.has_rin ? args.rin[ti * args.p.ntypes + tn] : T(0);
-            T x[3];
-            pair_u<T>(args, q, x);
+            pair_u_rinv<T>(args, q, x, &rinv);
             nbr_geometry<T>(x[0], x[1], x[2], rcut, inv_r0, rin, args.rin_w, &g);
           }
           if (sl == 0) {
             for (int ch = 0; ch < nch; ++ch) nwt[ch * kNB + n] = args.chw[ch * args.p.ntypes + tn];
             nidx[n] = nbi;
             // stress lever arm: x_n - x_i (small box) or sign_big*(x_i - x_n) (large box)
-            if (sizeof(T) == 4 && args.u32) {
-              const float4 v = args.u32[q];
-              const T sgn = args.small[s] ? T(1) : (T)(-args.p.sign_big);
-              nuu[n * 4 + 0] = sgn * v.x;
-              nuu[n * 4 + 1] = sgn * v.y;
-              nuu[n * 4 + 2] = sgn * v.z;
-              nuu[n * 4 + 3] = v.w;
-            } else {
-              const double* u3 = args.nbr_u + 3 * q;
-              const double r = sqrt(u3[0] * u3[0] + u3[1] * u3[1] + u3[2] * u3[2]);
-              const double sgn = args.small[s] ? 1.0 : -args.p.sign_big;
-              nuu[n * 4 + 0] = (T)(sgn * u3[0]);
-              nuu[n * 4 + 1] = (T)(sgn * u3[1]);
-              nuu[n * 4 + 2] = (T)(sgn * u3[2]);
-              nuu[n * 4 + 3] = (T)(1.0 / r);
-            }
+            const T sgn = args.small[s] ? T(1) : (T)(-args.p.sign_big);
+            nuu[n * 4 + 0] = sgn * x[0];
+            nuu[n * 4 + 1] = sgn * x[1];
+            nuu[n * 4 + 2] = sgn * x[2];
+            nuu[n * 4 + 3] = rinv;
           }
         }
         if (eval && sl < 9) pacc[min(n, kNB - 1) * 9 + sl] = 0.0;
