@@ -915,8 +915,16 @@ static int max_optin_smem() {
   return v;
 }
 
-size_t bso4_y_scratch_bytes(const DevTables& tb, int nch, int eb, int max_ctas) {
-  if (smem_plan(tb, nch, eb, true).total <= (size_t)max_optin_smem()) return 0;
+// Y in shared memory unless it does not fit or costs a resident CTA per SM (several channels)
+static bool y_shared(const DevTables& tb, int nch, int eb) {
+  const size_t ss = smem_plan(tb, nch, eb, true).total, sg = smem_plan(tb, nch, eb, false).total;
+  const size_t per_sm = 228 * 1024;
+  return ss <= (size_t)max_optin_smem() && per_sm / (ss + 1024) >= per_sm / (sg + 1024);
+}
+
+size_t bso4_y_scratch_bytes(const DevTables& tb, int nch, int eb, int max_ctas, bool only_if_required) {
+  const bool fits = smem_plan(tb, nch, eb, true).total <= (size_t)max_optin_smem();
+  if (fits && (only_if_required || y_shared(tb, nch, eb))) return 0;
   return (size_t)max_ctas * nch * tb.NYP * 2 * eb;
 }
 
@@ -953,11 +961,21 @@ cudaError_t launch_bso4(const DevTables& tb, const DevBatch& b, const BsoParams&
   a.dBout = dBout;
   if (ev) a.ev = *ev;
   if (a.ev.pair && dBout) return cudaErrorInvalidValue;
-  const bool y_in_smem = smem_plan(tb, p.nch, sizeof(T), true).total <= (size_t)max_optin_smem();
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const size_t per_sm = 228 * 1024;
+  // Y in shared memory when it fits, unless it costs a resident CTA per SM and the scratch holds
+  // a global slice for every CTA of the shape without it (several channels in FP32)
+  bool y_in_smem = smem_plan(tb, p.nch, sizeof(T), true).total <= (size_t)max_optin_smem();
+  if (y_in_smem && yscratch && !y_shared(tb, p.nch, (int)sizeof(T))) {
+    const size_t sg = smem_plan(tb, p.nch, sizeof(T), false).total;
+    const long long ctas = std::min<long long>((long long)b.A, (long long)nsm * (long long)(per_sm / (sg + 1024)));
+    if ((long long)(yscratch_bytes / ((size_t)p.nch * tb.NYP * 2 * sizeof(T))) >= ctas) y_in_smem = false;
+  }
   // the narrowest phase-1 groups (most neighbours per pass) whose U store fits without costing
   // a resident CTA per SM; each atom then takes the widest groups that need no more passes
   const size_t s16 = smem_plan(tb, p.nch, sizeof(T), y_in_smem, 16).total;
-  const size_t per_sm = 228 * 1024;
   a.g1 = 16;
   size_t smem = s16;
   for (int g1 : {4, 6, 8}) {
@@ -991,9 +1009,6 @@ cudaError_t launch_bso4(const DevTables& tb, const DevBatch& b, const BsoParams&
   if (e != cudaSuccess) return e;
   if (occ < 1) return cudaErrorInvalidConfiguration;
   if (sh.ctas_per_sm > 0) occ = std::min(occ, sh.ctas_per_sm);
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   long long grid = std::min<long long>((long long)b.A, (long long)nsm * occ);
   if (!y_in_smem) {
     // one Y slice per persistent CTA

@@ -305,7 +305,10 @@ cudaError_t launch_sort_lists(const DevBatch& b, cudaStream_t st);
 
 // Y scratch the descriptor kernel needs in global memory for up to max_ctas CTAs (0 when Y fits
 // in shared memory); pass it to launch_bso4, which then runs at most that many persistent CTAs.
-size_t bso4_y_scratch_bytes(const DevTables& tb, int nch, int eb, int max_ctas);
+// Bytes of the descriptor kernel's global Y slices for max_ctas persistent CTAs: needed when Y
+// does not fit in shared memory, and preferred (unless only_if_required) when it would cost a
+// resident CTA per SM; 0 otherwise.
+size_t bso4_y_scratch_bytes(const DevTables& tb, int nch, int eb, int max_ctas, bool only_if_required = false);
 // Evaluation with fitted weights instead of design rows: per-pair force and stress
 // contributions of dE/dB_a (beta_a = w_lin for the linear model; w_lin + (W + W^T) B_a for the
 // quadratic one), gathered into E/F/S by launch_eval_gather.

@@ -233,9 +233,9 @@ extern "C" int mld_gpu_descriptors_noalloc(const mld_gpu_config* cfg, int nat, c
   int* dmax = reinterpret_cast<int*>(take(sizeof(int) * 2));
   int* qcount = reinterpret_cast<int*>(take(sizeof(int)));  // descriptor kernel's queue counter
   float* bstage = mixed ? reinterpret_cast<float*>(take(sizeof(float) * (size_t)nat * KK)) : nullptr;
-  // global Y slices of the descriptor kernel when they do not fit in shared memory (FP64 with
-  // several channels); at most 64 persistent CTAs
-  const size_t ysb = bso4_y_scratch_bytes(dt, nch, mixed ? 4 : 8, 64);
+  // global Y slices of the descriptor kernel only when they do not fit in shared memory (FP64
+  // with several channels); at most 64 persistent CTAs
+  const size_t ysb = bso4_y_scratch_bytes(dt, nch, mixed ? 4 : 8, 64, true);
   void* yscr = ysb ? take(ysb) : nullptr;
   const size_t fixed = (size_t)(p - S->base);
   if (fixed > kScratchBytes) {
