@@ -308,7 +308,8 @@ struct KernelArgs {
   int* counter;
   BsoParams p;
   // Y (the contracted Z blocks, nch * NYP complex per atom) in global memory, one slice per CTA,
-  // when it does not fit in shared memory next to the rest (FP64 with several channels)
+  // when it does not fit in shared memory next to the rest (FP64 with several channels) or would
+  // cost a resident CTA per SM (FP32 with several channels)
   void* yglobal;
   int g1;  // narrowest lane groups per neighbour in phase 1 (4, 6, 8 or 16) the U store allows
   int geo_cap;  // neighbours whose phase-1 geometry records are kept for phase 3 (the rest recompute)
@@ -495,8 +496,8 @@ __device__ __forceinline__ void phase1_c(const KernelArgs<T>& args, const typena
   }
 }
 
-// kYShared: Y lives in shared memory (the common case); otherwise in the per-CTA global slice
-// args.yglobal (FP64 with several channels), a separate instantiation so that the shared-memory
+// kYShared: Y lives in shared memory (one channel); otherwise in the per-CTA global slice
+// args.yglobal (several channels), a separate instantiation so that the shared-memory
 // variant keeps shared-memory addressing.
 // kCT: columns (neighbour, component) per register tile of the dB contraction (autotuned).
 template <typename T, bool kYShared, int kCT>
