@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(kRowThreads) k_lin_force_rows(
   T* fac = reinterpret_cast<T*>(smem_raw + sizeof(int) * ((nn + 3) & ~3));  // nn * 3
   const int tid = threadIdx.x;
   const double sg = small[s] ? 1.0 : -sign_big;
-  for (int n = tid; n < nn; n += kRowThreads) {
+  for (int n = tid; n < nn; n += blockDim.x) {
     qrev[n] = rev[p0 + n];
     const double* u = nbr_u + 3 * (size_t)(p0 + n);
     const double f = sg / sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(kRowThreads) k_lin_force_rows(
   // each summed over the neighbours in order from one read of the atom's own derivatives
   const bool want_f = rf >= 0, want_s = rs >= 0 && Sp;
   if (!want_f && !want_s) return;
-  for (int c = tid; c < 3 * KK; c += kRowThreads) {
+  for (int c = tid; c < 3 * KK; c += blockDim.x) {
     const int a = c / KK, k = c - a * KK;
     T sum = T(0), acc[3] = {T(0), T(0), T(0)};
 #pragma unroll 4
@@ -218,8 +218,10 @@ cudaError_t launch_lin_rows(const DevBatch& b, const DevRows& rows, const BsoPar
     e = cudaFuncSetAttribute(k_lin_force_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
-  k_lin_force_rows<T><<<b.A, kRowThreads, sm, st>>>(b.A, KK, b.atom_struct, b.atom_start, b.nbr_off, b.nbr_u, rev,
-                                                    b.small, p.sign_big, dB, rows.rowF, rows.rowS, X, rows.ldx, Sp);
+  // one thread per (component, column) of the atom's force rows, in whole warps (192 for K = 55)
+  const int nthr = std::min(kRowThreads, (3 * KK + 31) / 32 * 32);
+  k_lin_force_rows<T><<<b.A, nthr, sm, st>>>(b.A, KK, b.atom_struct, b.atom_start, b.nbr_off, b.nbr_u, rev, b.small,
+                                             p.sign_big, dB, rows.rowF, rows.rowS, X, rows.ldx, Sp);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_lin_struct_rows<T><<<dim3(b.S, 7), kRowThreads, 0, st>>>(KK, b.atom_start, B, Sp, b.volume, p.sign_stress,
